@@ -1,0 +1,457 @@
+// extern "C" boundary of libhssgpu.so (declared in include/hssgpu.h).
+//
+// Every entry point converts exceptions into status codes; the message of the
+// last failure on the calling thread is kept for hss_last_error().
+#include <cstring>
+#include <string>
+
+#include "dense.cuh"
+#include "hss1d.h"
+#include "hss2d.h"
+
+namespace hss {
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace hss
+
+using namespace hss;
+
+#define HSS_TRY try {
+#define HSS_CATCH                                                      \
+  }                                                                    \
+  catch (const hss::Error& e) {                                        \
+    hss::set_last_error(e.what());                                     \
+    return e.code;                                                     \
+  }                                                                    \
+  catch (const std::bad_alloc&) {                                      \
+    hss::set_last_error("host allocation failed");                    \
+    return HSS_ERR_NOMEM;                                              \
+  }                                                                    \
+  catch (const std::exception& e) {                                    \
+    hss::set_last_error(e.what());                                     \
+    return HSS_ERR_ARG;                                                \
+  }                                                                    \
+  return HSS_OK;
+
+static cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+static void require_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    throw Error(HSS_ERR_CUDA, "no CUDA device available");
+  }
+}
+
+template <typename R>
+static void batched_inverse(R* d_A, int n, int batch, int* d_info, cudaStream_t s) {
+  HSS_REQUIRE(d_A && d_info && n > 0 && batch > 0, HSS_ERR_ARG, "bad arguments");
+  DevBuf<int> ipiv((size_t)batch * n);
+  DevBuf<R> W((size_t)batch * GJ_NB * n), Wf((size_t)batch * n * n);
+  HSS_CUDA(cudaMemsetAsync(d_info, 0, batch * sizeof(int), s));
+  std::vector<InvP<R>> P(batch);
+  for (int b = 0; b < batch; ++b)
+    P[b] = InvP<R>{d_A + (size_t)b * n * n, n, n, ipiv.p + (size_t)b * n, W.p + (size_t)b * GJ_NB * n,
+                   Wf.p + (size_t)b * n * n, d_info + b};
+  DevBuf<InvP<R>> dP(batch);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(InvP<R>), cudaMemcpyHostToDevice, s));
+  invert_batched<R>(dP.p, batch, n, s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+extern "C" {
+
+const char* hss_last_error(void) { return hss::g_last_error.c_str(); }
+
+int hss_version(void) { return 100; }
+
+int hss_device_count(int* count) {
+  HSS_TRY
+  HSS_REQUIRE(count != nullptr, HSS_ERR_ARG, "count is NULL");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) { cudaGetLastError(); n = 0; }
+  *count = n;
+  HSS_CATCH
+}
+
+// ---------------------------------------------------------------- HSS1D --
+int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf, double acc,
+                   const hss_kernel_params* kp, uint64_t seed) {
+  HSS_TRY
+  HSS_REQUIRE(out && X && kp, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *out = nullptr;
+  auto* h = new hss1d_matrix{nullptr};
+  try {
+    h->impl = new HSS1D();
+    h->impl->compress(X, N, ldx, leaf, acc, *kp, seed);
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *out = h;
+  HSS_CATCH
+}
+
+int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* parent, int32_t* c1, int32_t* c2,
+               int32_t* off, int32_t* cnt, int32_t* nskel, int32_t* kskel) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS1D* h = H->impl;
+  if (nboxes) *nboxes = h->nboxes;
+  for (int b = 0; b < h->nboxes; ++b) {
+    if (level) level[b] = h->level[b];
+    if (parent) parent[b] = h->parent[b];
+    if (c1) c1[b] = h->c1[b];
+    if (c2) c2[b] = h->c2[b];
+    if (off) off[b] = h->off[b];
+    if (cnt) cnt[b] = h->cnt[b];
+    if (nskel) nskel[b] = h->nskel[b];
+    if (kskel) kskel[b] = h->kskel[b];
+  }
+  HSS_CATCH
+}
+
+int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_t* I_skdn, int32_t* J_up,
+                     int32_t* J_dn, double* T_up, double* T_dn) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS1D* h = H->impl;
+  HSS_REQUIRE(box >= 1 && box < h->nboxes, HSS_ERR_ARG, "box out of range (the root has no skeleton)");
+  const int n = h->nskel[box], k = h->kskel[box];
+  if (I_skup) std::memcpy(I_skup, h->I_SKUP[box].data(), k * sizeof(int32_t));
+  if (I_skdn) std::memcpy(I_skdn, h->I_SKDN[box].data(), k * sizeof(int32_t));
+  if (J_up) std::memcpy(J_up, h->J_UP[box].data(), n * sizeof(int32_t));
+  if (J_dn) std::memcpy(J_dn, h->J_DN[box].data(), n * sizeof(int32_t));
+  const size_t tc = (size_t)k * (n - k);
+  if (tc > 0) {
+    if (T_up) HSS_CUDA(cudaMemcpy(T_up, h->T_UP.p + h->oT[box], tc * sizeof(double), cudaMemcpyDeviceToHost));
+    if (T_dn) HSS_CUDA(cudaMemcpy(T_dn, h->T_DN.p + h->oT[box], tc * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  HSS_CATCH
+}
+
+int hss1d_invert(hss1d_matrix* H) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->invert();
+  HSS_CATCH
+}
+
+static void host_roundtrip1(HSS1D* h, const double* X, double* Y, int nrhs, bool inv) {
+  HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
+  const size_t cnt = (size_t)h->N * nrhs;
+  DevBuf<double> dX(cnt), dY(cnt);
+  HSS_CUDA(cudaMemcpyAsync(dX.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (inv) h->applyinv_device(dX.p, dY.p, nrhs);
+  else h->apply_device(dX.p, dY.p, nrhs);
+  HSS_CUDA(cudaMemcpyAsync(Y, dY.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+int hss1d_apply(hss1d_matrix* H, const double* qq, double* uu, int32_t nrhs) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  host_roundtrip1(H->impl, qq, uu, nrhs, false);
+  HSS_CATCH
+}
+
+int hss1d_applyinv(hss1d_matrix* H, const double* ff, double* xx, int32_t nrhs) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  HSS_REQUIRE(H->impl->inverted, HSS_ERR_STATE, "hss1d_applyinv before hss1d_invert");
+  host_roundtrip1(H->impl, ff, xx, nrhs, true);
+  HSS_CATCH
+}
+
+int hss1d_applyinv_device(hss1d_matrix* H, const double* d_ff, double* d_xx, int32_t nrhs, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && d_ff && d_xx && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
+  HSS1D* h = H->impl;
+  cudaStream_t s = as_stream(stream);
+  cudaEvent_t ev;
+  HSS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (s) { HSS_CUDA(cudaEventRecord(ev, s)); HSS_CUDA(cudaStreamWaitEvent(h->stream, ev, 0)); }
+  h->applyinv_device(d_ff, d_xx, nrhs);
+  HSS_CUDA(cudaEventRecord(ev, h->stream));
+  if (s) HSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  else HSS_CUDA(cudaStreamSynchronize(h->stream));
+  cudaEventDestroy(ev);
+  HSS_CATCH
+}
+
+int hss1d_destroy(hss1d_matrix* H) {
+  HSS_TRY
+  if (H) {
+    delete H->impl;
+    delete H;
+  }
+  HSS_CATCH
+}
+
+// ---------------------------------------------------------------- HSS2D --
+int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p) {
+  HSS_TRY
+  HSS_REQUIRE(out != nullptr && p != nullptr, HSS_ERR_ARG, "NULL argument");
+  HSS_REQUIRE(p->interform == HSS_INTER_DENSE, HSS_ERR_ARG, "only INTERform 'dense' is supported");
+  HSS_REQUIRE(p->transinv == 0, HSS_ERR_ARG, "only the NTI (transinv = 0) path is supported");
+  HSS_REQUIRE(p->precision == HSS_PREC_FP64 || p->precision == HSS_PREC_MIXED, HSS_ERR_ARG, "bad precision");
+  require_device();
+  *out = nullptr;
+  auto* h = new hss2d_matrix{nullptr};
+  try {
+    h->impl = new HSS2D(*p);
+    h->impl->build_tree();
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *out = h;
+  HSS_CATCH
+}
+
+int hss2d_compress(hss2d_matrix* H) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->compress();
+  HSS_CATCH
+}
+
+int hss2d_invert(hss2d_matrix* H) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->invert();
+  HSS_CATCH
+}
+
+static void host_roundtrip(HSS2D* h, const double* X, double* Y, int nrhs, int which, double tol, int maxit,
+                           double* relres, int* iters) {
+  HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
+  const size_t cnt = (size_t)h->geo.N * nrhs;
+  DevBuf<double> dX(cnt), dY(cnt);
+  HSS_CUDA(cudaMemcpyAsync(dX.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (which == 0) h->apply_device(dX.p, dY.p, nrhs, h->stream);
+  else if (which == 1) h->applyinv_device(dX.p, dY.p, nrhs, h->stream);
+  else h->solve_device(dX.p, dY.p, nrhs, tol, maxit, relres, iters, h->stream);
+  HSS_CUDA(cudaMemcpyAsync(Y, dY.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+int hss2d_apply(hss2d_matrix* H, const double* X, double* Y, int32_t nrhs) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  host_roundtrip(H->impl, X, Y, nrhs, 0, 0.0, 1, nullptr, nullptr);
+  HSS_CATCH
+}
+
+int hss2d_apply_device(hss2d_matrix* H, const double* d_X, double* d_Y, int32_t nrhs, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && d_X && d_Y, HSS_ERR_ARG, "NULL argument");
+  H->impl->apply_device(d_X, d_Y, nrhs, as_stream(stream));
+  HSS_CATCH
+}
+
+int hss2d_applyinv(hss2d_matrix* H, const double* X, double* Y, int32_t nrhs) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  host_roundtrip(H->impl, X, Y, nrhs, 1, 0.0, 1, nullptr, nullptr);
+  HSS_CATCH
+}
+
+int hss2d_applyinv_device(hss2d_matrix* H, const double* d_X, double* d_Y, int32_t nrhs, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && d_X && d_Y, HSS_ERR_ARG, "NULL argument");
+  H->impl->applyinv_device(d_X, d_Y, nrhs, as_stream(stream));
+  HSS_CATCH
+}
+
+int hss2d_solve(hss2d_matrix* H, const double* f, double* x, int32_t nrhs, double tol, int32_t maxit,
+                double* relres, int32_t* iters) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  int it = 0;
+  host_roundtrip(H->impl, f, x, nrhs, 2, tol, maxit, relres, &it);
+  if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol, int32_t maxit,
+                       double* relres, int32_t* iters, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && d_f && d_x, HSS_ERR_ARG, "NULL argument");
+  int it = 0;
+  H->impl->solve_device(d_f, d_x, nrhs, tol, maxit, relres, &it, as_stream(stream));
+  if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  if (depth) *depth = H->impl->geo.depth;
+  if (nboxes) *nboxes = H->impl->geo.nboxes;
+  if (N) *N = H->impl->geo.N;
+  HSS_CATCH
+}
+
+int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* nproxy) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const auto& g = H->impl->geo;
+  for (int lev = 0; lev <= g.depth; ++lev) {
+    const auto& L = g.levels[lev];
+    for (int i = 0; i < L.nb; ++i) {
+      const int b = (1 << lev) - 1 + i;
+      if (n) n[b] = L.n;
+      if (k) k[b] = L.k;
+      if (nproxy) nproxy[b] = L.p;
+    }
+  }
+  HSS_CATCH
+}
+
+int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t* J, double* T_up, double* T_dn) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  HSS2D* h = H->impl;
+  HSS_REQUIRE(box >= 0 && box < h->geo.nboxes, HSS_ERR_ARG, "box out of range");
+  int lev = 0;
+  while (((1 << (lev + 1)) - 1) <= box) ++lev;
+  const auto& g = h->geo.levels[lev];
+  const int i = box - ((1 << lev) - 1);
+  if (I_src) std::memcpy(I_src, g.Isrc.data() + (size_t)i * g.n, g.n * sizeof(int32_t));
+  if (J) std::memcpy(J, g.J.data() + (size_t)i * g.n, g.n * sizeof(int32_t));
+  const size_t tcnt = (size_t)g.k * (g.n - g.k);
+  if (lev > 0 && tcnt > 0) {
+    auto& d = h->L[lev];
+    if (T_up) HSS_CUDA(cudaMemcpy(T_up, d.Tup.p + i * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
+    if (T_dn) HSS_CUDA(cudaMemcpy(T_dn, d.Tdn.p + i * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  HSS_CATCH
+}
+
+int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double* E) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  HSS2D* h = H->impl;
+  HSS_REQUIRE(h->inverted, HSS_ERR_STATE, "export_inverse before invert");
+  HSS_REQUIRE(box >= 0 && box < h->geo.nboxes, HSS_ERR_ARG, "box out of range");
+  int lev = 0;
+  while (((1 << (lev + 1)) - 1) <= box) ++lev;
+  const auto& g = h->geo.levels[lev];
+  const int i = box - ((1 << lev) - 1);
+  auto& d = h->L[lev];
+  auto fetch = [&](int which, size_t cnt, double* dst) {
+    if (!dst) return;
+    if (h->prm.precision == HSS_PREC_MIXED) {
+      std::vector<float> t(cnt);
+      HSS_CUDA(cudaMemcpy(t.data(), d.ff[which].p + i * cnt, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < cnt; ++q) dst[q] = t[q];
+    } else {
+      HSS_CUDA(cudaMemcpy(dst, d.fd[which].p + i * cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  };
+  fetch(0, (size_t)g.n * g.n, FI);
+  if (lev > 0) fetch(1, (size_t)g.k * g.k, E);
+  HSS_CATCH
+}
+
+int hss2d_solve_bytes(const hss2d_matrix* H, int64_t* bytes) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && bytes, HSS_ERR_ARG, "NULL argument");
+  *bytes = H->impl->solve_bytes();
+  HSS_CATCH
+}
+
+int hss2d_solve_launches(const hss2d_matrix* H, int32_t nrhs, int32_t* launches) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && launches, HSS_ERR_ARG, "NULL argument");
+  *launches = H->impl->solve_launches(nrhs);
+  HSS_CATCH
+}
+
+int hss2d_destroy(hss2d_matrix* H) {
+  HSS_TRY
+  if (H) {
+    delete H->impl;
+    delete H;
+  }
+  HSS_CATCH
+}
+
+// ---------------------------------------------------------------- primitives --
+int hss_batched_inverse_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info, void* stream) {
+  HSS_TRY
+  batched_inverse<double>(d_A, n, batch, d_info, as_stream(stream));
+  HSS_CATCH
+}
+
+int hss_batched_inverse_device_f32(float* d_A, int32_t n, int32_t batch, int32_t* d_info, void* stream) {
+  HSS_TRY
+  batched_inverse<float>(d_A, n, batch, d_info, as_stream(stream));
+  HSS_CATCH
+}
+
+int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(d_A && m > 0 && n > kf && kf > 0 && kf <= m && batch > 0, HSS_ERR_ARG, "bad arguments");
+  cudaStream_t s = as_stream(stream);
+  DevBuf<double> V((size_t)batch * m * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * kf);
+  std::vector<QrP<double>> P(batch);
+  for (int b = 0; b < batch; ++b)
+    P[b] = QrP<double>{d_A + (size_t)b * m * n, m, n, kf, m, V.p + (size_t)b * m * QR_NB,
+                       Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * kf};
+  DevBuf<QrP<double>> dP(batch);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, s));
+  lstsq_batched<double>(dP.p, batch, m, n, kf, s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+  HSS_CATCH
+}
+
+int hss_batched_id_device(const double* d_A, int32_t m, int32_t n, int32_t batch, double acc, uint64_t seed,
+                          int32_t force_k, int32_t* d_rank, int32_t* d_perm, double* d_T, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(d_A && d_rank && d_perm && d_T && m > 0 && n > 0 && n <= 4096 && batch > 0, HSS_ERR_ARG,
+              "bad arguments");
+  HSS_REQUIRE(force_k < 0 || force_k <= std::min(m, n), HSS_ERR_RANK, "fixed rank exceeds min(m, n)");
+  cudaStream_t s = as_stream(stream);
+  DevBuf<double> W((size_t)batch * m * n), SW((size_t)batch * n * n), SV((size_t)batch * n * n);
+  DevBuf<double> x((size_t)batch * 2 * n), y((size_t)batch * (m + n));
+  std::vector<IdP> P(batch);
+  for (int b = 0; b < batch; ++b)
+    P[b] = IdP{d_A + (size_t)b * m * n, W.p + (size_t)b * m * n, m, n, d_perm + (size_t)b * n, d_rank + b,
+               d_T + (size_t)b * n * n, -1, SW.p + (size_t)b * n * n, SV.p + (size_t)b * n * n,
+               x.p + (size_t)b * 2 * n, y.p + (size_t)b * (m + n), b, 0};
+  DevBuf<IdP> dP(batch);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(IdP), cudaMemcpyHostToDevice, s));
+  id_adaptive_batched(dP.p, batch, acc, seed, s);
+  if (force_k >= 0) {
+    for (auto& q : P) q.force_k = force_k;
+    HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(IdP), cudaMemcpyHostToDevice, s));
+    id_fixed_batched(dP.p, batch, s);
+  }
+  HSS_CUDA(cudaStreamSynchronize(s));
+  HSS_CATCH
+}
+
+int hss_batched_gemm_device(const double* d_A, const double* d_B, double* d_C, int32_t M, int32_t N, int32_t K,
+                            int32_t batch, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(d_A && d_B && d_C && M > 0 && N > 0 && K > 0 && batch > 0, HSS_ERR_ARG, "bad arguments");
+  cudaStream_t s = as_stream(stream);
+  std::vector<GemmP<double>> P(batch);
+  for (int b = 0; b < batch; ++b)
+    P[b] = GemmP<double>{d_A + (size_t)b * M * K, d_B + (size_t)b * K * N, d_C + (size_t)b * M * N, M, N, K, M, K, M};
+  DevBuf<GemmP<double>> dP(batch);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(GemmP<double>), cudaMemcpyHostToDevice, s));
+  if (N <= 8) gemm_skinny<double>(dP.p, batch, M, 1.0, 0.0, s);
+  else gemm_batched<double>(dP.p, batch, M, N, false, false, 1.0, 0.0, s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+  HSS_CATCH
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+// Shared definitions for the HSS GB300 library: status codes, error plumbing,
+// the kernel-parameter block and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/hssgpu.h"
+
+namespace hss {
+
+// Exception carrying an hss status code; every extern "C" entry point catches
+// it and returns the code, so no C++ exception crosses the C boundary.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define HSS_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e__ = (call);                                                 \
+    if (e__ != cudaSuccess)                                                   \
+      throw ::hss::Error(HSS_ERR_CUDA, std::string(#call) + ": " +            \
+                                           cudaGetErrorString(e__));          \
+  } while (0)
+
+#define HSS_REQUIRE(cond, code, msg)                                          \
+  do {                                                                        \
+    if (!(cond)) throw ::hss::Error((code), (msg));                           \
+  } while (0)
+
+inline void check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    throw Error(HSS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Device copy of hss_kernel_params with derived constants.
+struct KernelDev {
+  int flag;
+  double h2half;  // h*h*0.5
+  double b_alpha, b_x0, b_y0, b_isig;
+  double c_alpha, c_x0, c_y0, c_isig;
+};
+
+inline KernelDev make_kernel_dev(const hss_kernel_params& p) {
+  KernelDev k;
+  k.flag = p.flag;
+  k.h2half = p.h * p.h * 0.5;
+  k.b_alpha = p.b_alpha; k.b_x0 = p.b_x0; k.b_y0 = p.b_y0; k.b_isig = p.b_isig;
+  k.c_alpha = p.c_alpha; k.c_x0 = p.c_x0; k.c_y0 = p.c_y0; k.c_isig = p.c_isig;
+  return k;
+}
+
+// Structure-of-arrays point table on the device (real points, then proxies).
+struct PointsDev {
+  const double* x;
+  const double* y;
+  const double* nx;
+  const double* ny;
+  const double* w;
+  const double* kap;
+};
+
+// RAII device buffer.
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t cnt) { alloc(cnt); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t cnt) {
+    release();
+    n = cnt;
+    if (cnt) {
+      cudaError_t e = cudaMalloc(&p, cnt * sizeof(T));
+      if (e != cudaSuccess) {
+        p = nullptr; n = 0;
+        throw Error(HSS_ERR_NOMEM, "cudaMalloc of " + std::to_string(cnt * sizeof(T)) + " bytes failed");
+      }
+    }
+  }
+  // grow-only: keeps the current allocation (and every pointer into it) when large enough
+  void ensure(size_t cnt) {
+    if (n < cnt) alloc(cnt);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) {
+    if (h.size() > n) alloc(h.size());
+    if (!h.empty())
+      HSS_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void zero(cudaStream_t s) {
+    if (n) HSS_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+};
+
+template <typename T>
+inline void download(std::vector<T>& h, const T* d, size_t cnt, cudaStream_t s) {
+  h.resize(cnt);
+  if (cnt) HSS_CUDA(cudaMemcpyAsync(h.data(), d, cnt * sizeof(T), cudaMemcpyDeviceToHost, s));
+}
+
+}  // namespace hss

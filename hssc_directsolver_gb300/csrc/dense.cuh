@@ -1,0 +1,87 @@
+// Batched dense linear algebra for the HSS levels (declarations).
+//
+// Every routine works on a batch of independent column-major problems whose
+// descriptors live in device memory, so one launch covers every box of a tree
+// level (and every problem of a batch).  Sizes may differ per problem; a
+// problem whose size is already finished simply idles in that launch.
+#pragma once
+
+#include "common.cuh"
+
+namespace hss {
+
+// C_b = alpha * op(A_b) * op(B_b) + beta * C_b
+template <typename R>
+struct GemmP {
+  const R* A;
+  const R* B;
+  R* C;
+  int M, N, K;
+  int lda, ldb, ldc;
+};
+
+template <typename R>
+void gemm_batched(const GemmP<R>* dP, int batch, int maxM, int maxN, bool tA, bool tB,
+                  R alpha, R beta, cudaStream_t s);
+
+// Same product for skinny outputs (N <= 8 columns, the right-hand sides of a
+// solve): one warp per 32 rows, K split over the warps of a block; the result
+// is deterministic (fixed summation order).
+template <typename R>
+void gemm_skinny(const GemmP<R>* dP, int batch, int maxM, R alpha, R beta, cudaStream_t s);
+
+// In-place inversion by blocked Gauss-Jordan with partial (row) pivoting.
+template <typename R>
+struct InvP {
+  R* A;
+  int n, lda;
+  int* ipiv;  // n entries
+  R* W;       // GJ_NB x n workspace
+  R* Wfull;   // n x n workspace (final column permutation)
+  int* info;  // 0 ok, j+1 if pivot j was exactly zero, -1 non-finite
+};
+constexpr int GJ_NB = 32;
+
+template <typename R>
+void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s);
+
+// Least squares X = A(:, 0:kf) \ A(:, kf:n) for tall full-rank problems, by
+// blocked Householder QR of the first kf columns applied to the remaining
+// ones, then a blocked back substitution.  The result overwrites
+// A(0:kf, kf:n).  diag receives |R_ii| (kf entries) for rank diagnostics.
+template <typename R>
+struct QrP {
+  R* A;
+  int m, n, kf, lda;
+  R* V;     // m x QR_NB workspace (explicit reflectors)
+  R* Tf;    // QR_NB x QR_NB workspace (compact-WY factor)
+  R* diag;  // kf entries
+};
+constexpr int QR_NB = 32;
+
+template <typename R>
+void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s);
+
+// Interpolative decomposition of one m x n block per problem (the pivoted-QR
+// rank detection of the reference ID, with its randomized posterior check).
+struct IdP {
+  const double* A;  // original block, column-major m x n, ld = m
+  double* W;        // m x n workspace: overwritten by the pivoted QR (R on top)
+  int m, n;
+  int* perm;        // n: column permutation (0-based)
+  int* rank;        // output rank k
+  double* T;        // output k x (n-k) interpolation matrix (ld = n)
+  int force_k;      // >= 0: fixed-rank mode on an already factored W
+  double* svdW;     // n x n workspace (fixed-rank mode)
+  double* svdV;     // n x n workspace (fixed-rank mode)
+  double* x;        // 2*n workspace (random vectors)
+  double* y;        // m+n workspace
+  int problem;      // id for the random stream
+  int status;       // padding / spare
+};
+
+void id_adaptive_batched(const IdP* dP, int batch, double acc, unsigned long long seed,
+                         cudaStream_t s);
+void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s);
+
+}  // namespace hss

@@ -1,0 +1,778 @@
+// HSS1D solver for curves (non-symmetric form), FP64.
+//
+//  compress : HSS1D/HSS1D_compress_nsym.m ('green' trick).  The host walks
+//             the tree level by level (deepest first); for every box of a
+//             level the GPU generates A_out = K[X_in_inside u X_proxy, X_out]
+//             and A_in^T = K[X_in, X_out_inside u X_proxy]^T (:151-156) and runs
+//             the pivoted-QR ID with its randomized check (Common/ID.m:40-65),
+//             then the fixed-rank re-ID of the side whose rank is raised to
+//             k = max(k_out, k_in) (:189-196, ID.m:106-113).  Skeleton index
+//             sets go back to the host, which assembles the next level.
+//  invert   : HSS1D/HSS1D_invert_nsym.m:44-91, level-batched.
+//  apply    : HSS1D/HSS1D_apply_nsym.m:38-130.
+//  applyinv : HSS1D/HSS1D_applyinv_nsym.m:43-86.
+#include "hss1d.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace hss {
+
+static constexpr double RADIUS_REL = 1.75;  // HSS1D_compress_nsym.m:51
+static constexpr int NPROXY = 50;           // HSS1D_compress_nsym.m:52
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_move(const MoveP* __restrict__ P) {
+  const MoveP p = P[blockIdx.x];
+  const long long tot = (long long)p.nrows * p.ncols;
+  for (long long e = threadIdx.x; e < tot; e += 256) {
+    const int i = (int)(e % p.nrows), c = (int)(e / p.nrows);
+    if (p.mode == 0) {
+      const int si = p.idx ? p.idx[i] : i;
+      p.dst[i + (size_t)c * p.ldd] = p.src[si + (size_t)c * p.lds];
+    } else if (p.mode == 1) {
+      const int sc = p.idx ? p.idx[c] : c;
+      p.dst[i + (size_t)c * p.ldd] = p.src[i + (size_t)sc * p.lds];
+    } else if (p.mode == 2) {
+      const int di = p.idx ? p.idx[i] : i;
+      double* d = p.dst + di + (size_t)c * p.ldd;
+      const double v = p.src[i + (size_t)c * p.lds];
+      *d = p.accumulate ? *d + v : v;
+    } else {  // 3: transpose copy dst(c, i) = src(i, c)
+      p.dst[c + (size_t)i * p.ldd] = p.src[i + (size_t)c * p.lds];
+    }
+  }
+}
+
+void move_batched(const MoveP* dP, int batch, cudaStream_t s) {
+  if (batch <= 0) return;
+  HSS_REQUIRE(batch <= 2147483647, HSS_ERR_ARG, "move batch too large");
+  k_move<<<batch, 256, 0, s>>>(dP);
+  check_launch("k_move");
+}
+
+struct F1P {  // F = [E1 S1; S2 E2] (two children) or F = M (leaf)
+  double* F;
+  int n, k1;
+  const double *E1, *S1, *S2, *E2, *M;
+};
+
+__global__ void __launch_bounds__(256) k_assemble1(const F1P* __restrict__ P) {
+  const F1P p = P[blockIdx.x];
+  const int n = p.n, k1 = p.k1, k2 = n - k1;
+  for (long long e = threadIdx.x; e < (long long)n * n; e += 256) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    double v;
+    if (p.M) v = p.M[e];
+    else if (i < k1 && j < k1) v = p.E1[i + (size_t)j * k1];
+    else if (i < k1) v = p.S1[i + (size_t)(j - k1) * k1];
+    else if (j < k1) v = p.S2[(i - k1) + (size_t)j * k2];
+    else v = p.E2[(i - k1) + (size_t)(j - k1) * k2];
+    p.F[e] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+static T* upload_vec(DevBuf<T>& buf, const std::vector<T>& h, cudaStream_t s) {
+  buf.alloc(std::max<size_t>(h.size(), 1));
+  if (!h.empty()) HSS_CUDA(cudaMemcpyAsync(buf.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return buf.p;
+}
+
+static void run_moves(const std::vector<MoveP>& mv, cudaStream_t s) {
+  if (mv.empty()) return;
+  DevBuf<MoveP> d;
+  upload_vec(d, mv, s);
+  move_batched(d.p, (int)mv.size(), s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+static void run_gemms(const std::vector<GemmP<double>>& P, bool tA, bool tB, double alpha, double beta,
+                      cudaStream_t s, bool skinny = false) {
+  if (P.empty()) return;
+  int maxM = 0, maxN = 0;
+  for (auto& p : P) { maxM = std::max(maxM, p.M); maxN = std::max(maxN, p.N); }
+  DevBuf<GemmP<double>> d;
+  upload_vec(d, P, s);
+  for (size_t off = 0; off < P.size(); off += 65535) {
+    const int cnt = (int)std::min<size_t>(65535, P.size() - off);
+    if (skinny) gemm_skinny<double>(d.p + off, cnt, maxM, alpha, beta, s);
+    else gemm_batched<double>(d.p + off, cnt, maxM, maxN, tA, tB, alpha, beta, s);
+  }
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t s) {
+  if (mats.empty()) return;
+  const int nb = (int)mats.size();
+  int maxn = 0;
+  long long tot = 0;
+  for (auto& m : mats) { maxn = std::max(maxn, m.second); tot += (long long)m.second * m.second; }
+  long long totn = 0;
+  for (auto& m : mats) totn += m.second;
+  DevBuf<int> ipiv(totn), info(nb);
+  DevBuf<double> W((size_t)GJ_NB * totn), Wf(tot);
+  info.zero(s);
+  std::vector<InvP<double>> P(nb);
+  long long on = 0, o2 = 0;
+  for (int i = 0; i < nb; ++i) {
+    const int n = mats[i].second;
+    P[i] = InvP<double>{mats[i].first, n, n, ipiv.p + on, W.p + (size_t)GJ_NB * on, Wf.p + o2, info.p + i};
+    on += n;
+    o2 += (long long)n * n;
+  }
+  DevBuf<InvP<double>> dP;
+  upload_vec(dP, P, s);
+  invert_batched<double>(dP.p, nb, maxn, s);
+  std::vector<int> hi;
+  download(hi, info.p, nb, s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+  for (int v : hi) {
+    HSS_REQUIRE(v >= 0, HSS_ERR_NONFINITE, "non-finite pivot in block inversion");
+    HSS_REQUIRE(v == 0, HSS_ERR_SINGULAR, "singular diagonal block in inversion");
+  }
+}
+
+// LOCAL_get_circum_circle (HSS1D_compress_nsym.m:339-356) on X rows idx
+static void circum_circle(const std::vector<double>& X, const std::vector<int>& idx, double& xc, double& yc,
+                          double& R) {
+  const int nloc = (int)idx.size();
+  auto px = [&](int i) { return X[6 * (size_t)idx[i]]; };
+  auto py = [&](int i) { return X[6 * (size_t)idx[i] + 1]; };
+  xc = 0.5 * (px(0) + px(nloc - 1));
+  yc = 0.5 * (py(0) + py(nloc - 1));
+  double mx = -1.0;
+  for (int i = 0; i < nloc; ++i) {
+    const double dx = px(i) - xc, dy = py(i) - yc;
+    mx = std::max(mx, dx * dx + dy * dy);
+  }
+  R = std::sqrt(mx);
+  const double ex = px(0) - px(nloc - 1), ey = py(0) - py(nloc - 1);
+  const double e = ex * ex + ey * ey;
+  if ((1.2 * R * R) > e) {
+    double sx = 0.0, sy = 0.0;
+    for (int i = 0; i < nloc; ++i) { sx += px(i); sy += py(i); }
+    const double inv = 1.0 / (double)nloc;
+    xc = sx * inv;
+    yc = sy * inv;
+    mx = -1.0;
+    for (int i = 0; i < nloc; ++i) {
+      const double dx = px(i) - xc, dy = py(i) - yc;
+      mx = std::max(mx, dx * dx + dy * dy);
+    }
+    R = std::sqrt(mx);
+  }
+}
+
+HSS1D::HSS1D() { HSS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); }
+HSS1D::~HSS1D() {
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, double acc_,
+                     const hss_kernel_params& kp_, unsigned long long seed_) {
+  HSS_REQUIRE(Xh && N_ >= 2 && ldx >= N_ && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
+  HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
+  HSS_REQUIRE(N_ < (1LL << 30), HSS_ERR_ARG, "N too large");
+  N = N_; leaf = leaf_; acc = acc_; kp = kp_; seed = seed_;
+  kdev = make_kernel_dev(kp);
+  X.resize(6 * (size_t)N);
+  for (long long i = 0; i < N; ++i)
+    for (int c = 0; c < 6; ++c) X[6 * i + c] = Xh[i + c * ldx];
+  // ---- tree (LOCAL_get_tree, :277-334)
+  level = {0}; parent = {-1}; c1 = {-1}; c2 = {-1}; off = {0}; cnt = {(int)N};
+  {
+    int last = -1, created = 1, ilev = 0;
+    while (created > 0) {
+      const int first = last + 1;
+      last = last + created;
+      created = 0;
+      for (int b = first; b <= last; ++b) {
+        const int nbx = cnt[b];
+        if (nbx > leaf) {
+          const int half = (nbx + 1) / 2;
+          const int s1 = last + created + 1;
+          c1[b] = s1;
+          c2[b] = s1 + 1;
+          for (int t = 0; t < 2; ++t) {
+            level.push_back(ilev + 1);
+            parent.push_back(b);
+            c1.push_back(-1);
+            c2.push_back(-1);
+            off.push_back(t == 0 ? off[b] : off[b] + half);
+            cnt.push_back(t == 0 ? half : nbx - half);
+          }
+          created += 2;
+        }
+      }
+      ++ilev;
+    }
+  }
+  nboxes = (int)level.size();
+  HSS_REQUIRE(nboxes >= 3, HSS_ERR_ARG, "N must exceed the leaf size (at least one split)");
+  maxlev = *std::max_element(level.begin(), level.end());
+  // ---- neighbour lists (:376-412)
+  std::vector<std::vector<int>> nei(nboxes);
+  nei[0] = {0};
+  for (int b = 1; b < nboxes; ++b) {
+    std::vector<int> r(cnt[b]);
+    std::iota(r.begin(), r.end(), off[b]);
+    double xc, yc, R;
+    circum_circle(X, r, xc, yc, R);
+    std::vector<int> pot;
+    for (int j : nei[parent[b]]) {
+      if (c1[j] >= 0) pot.push_back(c1[j]);
+      if (c2[j] >= 0) pot.push_back(c2[j]);
+    }
+    const double rr = RADIUS_REL * RADIUS_REL * R * R;
+    for (int j : pot) {
+      double mn = INFINITY;
+      for (int i = off[j]; i < off[j] + cnt[j]; ++i) {
+        const double dx = X[6 * (size_t)i] - xc, dy = X[6 * (size_t)i + 1] - yc;
+        mn = std::min(mn, dx * dx + dy * dy);
+      }
+      if (mn < rr) nei[b].push_back(j);
+    }
+  }
+  for (int b = 1; b < nboxes; ++b) {
+    auto& l = nei[b];
+    l.erase(std::remove(l.begin(), l.end(), b), l.end());
+    std::sort(l.begin(), l.end());
+  }
+  // ---- point table: N points + NPROXY proxies per box
+  const size_t npts = (size_t)N + (size_t)NPROXY * nboxes;
+  std::vector<double> hx(npts, 0.0), hy(npts, 0.0), hnx(npts, 0.0), hny(npts, 0.0), hw(npts, 0.0),
+      hk(npts, 0.0);
+  for (long long i = 0; i < N; ++i) {
+    hx[i] = X[6 * i]; hy[i] = X[6 * i + 1]; hnx[i] = X[6 * i + 2]; hny[i] = X[6 * i + 3];
+    hw[i] = X[6 * i + 4]; hk[i] = X[6 * i + 5];
+  }
+  nskel.assign(nboxes, 0);
+  kskel.assign(nboxes, 0);
+  I_SKUP.assign(nboxes, {});
+  I_SKDN.assign(nboxes, {});
+  J_UP.assign(nboxes, {});
+  J_DN.assign(nboxes, {});
+  std::vector<DevBuf<double>> Tkeep;  // per level: T of each ID problem (n x n, ld n)
+  std::vector<std::vector<long long>> Toff(nboxes);
+  std::vector<int> Tlev(nboxes, -1);
+  // proxy geometry needs the skeletons of the level below: compute per level
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<int> boxes;
+    for (int b = 1; b < nboxes; ++b)
+      if (level[b] == L) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    const int nbL = (int)boxes.size();
+    std::vector<std::vector<int>> outs(nbL), inns(nbL), rows_out(nbL), rows_in(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q];
+      auto& out = outs[q];
+      auto& inn = inns[q];
+      if (is_leaf(b)) {
+        out.resize(cnt[b]);
+        std::iota(out.begin(), out.end(), off[b]);
+        inn = out;
+      } else {
+        HSS_REQUIRE(c1[b] >= 0 && c2[b] >= 0, HSS_ERR_ARG, "one-child boxes are not produced by the halving tree");
+        out = I_SKUP[c1[b]];
+        out.insert(out.end(), I_SKUP[c2[b]].begin(), I_SKUP[c2[b]].end());
+        inn = I_SKDN[c1[b]];
+        inn.insert(inn.end(), I_SKDN[c2[b]].begin(), I_SKDN[c2[b]].end());
+      }
+      std::vector<int> both = out;
+      both.insert(both.end(), inn.begin(), inn.end());
+      std::sort(both.begin(), both.end());
+      double xc, yc, R;
+      circum_circle(X, both, xc, yc, R);
+      const double Rp = RADIUS_REL * R;
+      // LOCAL_construct_circle: tt = linspace(0, 2 pi (1 - 1/n), n)
+      const double stop = 2.0 * M_PI * (1.0 - 1.0 / NPROXY);
+      const double step = stop / (double)(NPROXY - 1);
+      const size_t pb = (size_t)N + (size_t)NPROXY * b;
+      for (int t = 0; t < NPROXY; ++t) {
+        const double tt = (t == NPROXY - 1) ? stop : (double)t * step;
+        const double c = std::cos(tt), s = std::sin(tt);
+        hx[pb + t] = xc + Rp * c;
+        hy[pb + t] = yc + Rp * s;
+        hnx[pb + t] = c;
+        hny[pb + t] = s;
+        hw[pb + t] = 2.0 * M_PI * Rp / NPROXY;
+        hk[pb + t] = 1.0 / Rp;
+      }
+      std::vector<int> out_maybe, in_maybe;
+      for (int j : nei[b]) {
+        if (is_leaf(j)) {
+          for (int i = off[j]; i < off[j] + cnt[j]; ++i) { out_maybe.push_back(i); in_maybe.push_back(i); }
+        } else if (c1[j] >= 0 && c2[j] >= 0) {
+          for (int s : {c1[j], c2[j]}) {
+            out_maybe.insert(out_maybe.end(), I_SKUP[s].begin(), I_SKUP[s].end());
+          }
+          for (int s : {c1[j], c2[j]}) {
+            in_maybe.insert(in_maybe.end(), I_SKDN[s].begin(), I_SKDN[s].end());
+          }
+        } else {
+          const int s = std::max(c1[j], c2[j]);
+          out_maybe.insert(out_maybe.end(), I_SKUP[s].begin(), I_SKUP[s].end());
+          in_maybe.insert(in_maybe.end(), I_SKDN[s].begin(), I_SKDN[s].end());
+        }
+      }
+      const double rr = Rp * Rp;
+      std::vector<int> out_inside, in_inside;
+      for (int i : out_maybe) {
+        const double dx = X[6 * (size_t)i] - xc, dy = X[6 * (size_t)i + 1] - yc;
+        if (dx * dx + dy * dy < rr) out_inside.push_back(i);
+      }
+      for (int i : in_maybe) {
+        const double dx = X[6 * (size_t)i] - xc, dy = X[6 * (size_t)i + 1] - yc;
+        if (dx * dx + dy * dy < rr) in_inside.push_back(i);
+      }
+      rows_out[q] = in_inside;
+      rows_in[q] = out_inside;
+      for (int t = 0; t < NPROXY; ++t) {
+        rows_out[q].push_back((int)(pb + t));
+        rows_in[q].push_back((int)(pb + t));
+      }
+      HSS_REQUIRE(out.size() <= 4096, HSS_ERR_RANK, "skeleton set exceeds 4096 points");
+    }
+    pts.upload(hx, hy, hnx, hny, hw, hk, kp, stream);
+    // index arrays and block storage
+    std::vector<int> idx;
+    std::vector<long long> o_ro(nbL), o_ri(nbL), o_out(nbL), o_in(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      o_ro[q] = idx.size(); idx.insert(idx.end(), rows_out[q].begin(), rows_out[q].end());
+      o_ri[q] = idx.size(); idx.insert(idx.end(), rows_in[q].begin(), rows_in[q].end());
+      o_out[q] = idx.size(); idx.insert(idx.end(), outs[q].begin(), outs[q].end());
+      o_in[q] = idx.size(); idx.insert(idx.end(), inns[q].begin(), inns[q].end());
+    }
+    DevBuf<int> didx;
+    upload_vec(didx, idx, stream);
+    const int nprob = 2 * nbL;
+    std::vector<long long> oA(nprob), oT2(nprob), oX(nprob), oY(nprob), oP(nprob);
+    long long tA = 0, tT = 0, tX = 0, tY = 0, tP = 0;
+    std::vector<int> pm(nprob), pn(nprob);
+    for (int q = 0; q < nbL; ++q) {
+      for (int s = 0; s < 2; ++s) {
+        const int pr = 2 * q + s;
+        const int m = (int)(s == 0 ? rows_out[q].size() : rows_in[q].size());
+        const int n = (int)outs[q].size();
+        pm[pr] = m; pn[pr] = n;
+        oA[pr] = tA; tA += (long long)m * n;
+        oT2[pr] = tT; tT += (long long)n * n;
+        oX[pr] = tX; tX += 2LL * n;
+        oY[pr] = tY; tY += (long long)m + n;
+        oP[pr] = tP; tP += n;
+      }
+    }
+    DevBuf<double> A(tA), W(tA), SW(tT), SV(tT), xw(tX), yw(tY);
+    Tkeep.emplace_back(tT);
+    DevBuf<double>& Tb = Tkeep.back();
+    DevBuf<int> perm(tP), rank(nprob);
+    std::vector<KgenP<double>> kg(nprob);
+    std::vector<IdP> ip(nprob);
+    for (int q = 0; q < nbL; ++q) {
+      const int n = (int)outs[q].size();
+      kg[2 * q] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[2 * q], n, A.p + oA[2 * q], pm[2 * q], 0};
+      kg[2 * q + 1] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], n, pm[2 * q + 1], A.p + oA[2 * q + 1],
+                                    pm[2 * q + 1], 1};
+    }
+    for (int pr = 0; pr < nprob; ++pr) {
+      const int b = boxes[pr / 2];
+      ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], pm[pr], pn[pr], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * b + (pr & 1), 0};
+    }
+    long long maxe = 0;
+    for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
+    DevBuf<KgenP<double>> dkg;
+    upload_vec(dkg, kg, stream);
+    kgen_batched<double>(dkg.p, nprob, maxe, view(pts), kdev, stream);
+    DevBuf<IdP> dip;
+    upload_vec(dip, ip, stream);
+    id_adaptive_batched(dip.p, nprob, acc, seed, stream);
+    std::vector<int> hr;
+    download(hr, rank.p, nprob, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    bool any = false;
+    std::vector<int> kbox(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      const int ko = hr[2 * q], ki = hr[2 * q + 1];
+      const int k = std::max(ko, ki);
+      kbox[q] = k;
+      if (k != ko) { ip[2 * q].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q], pn[2 * q]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+      else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q + 1], pn[2 * q + 1]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+    }
+    if (any) {
+      HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob * sizeof(IdP), cudaMemcpyHostToDevice, stream));
+      id_fixed_batched(dip.p, nprob, stream);
+    }
+    std::vector<int> hp;
+    download(hp, perm.p, tP, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q];
+      const int n = (int)outs[q].size(), k = kbox[q];
+      nskel[b] = n;
+      kskel[b] = k;
+      J_UP[b].assign(hp.begin() + oP[2 * q], hp.begin() + oP[2 * q] + n);
+      J_DN[b].assign(hp.begin() + oP[2 * q + 1], hp.begin() + oP[2 * q + 1] + n);
+      I_SKUP[b].resize(k);
+      I_SKDN[b].resize(k);
+      for (int t = 0; t < k; ++t) {
+        I_SKUP[b][t] = outs[q][J_UP[b][t]];
+        I_SKDN[b][t] = inns[q][J_DN[b][t]];
+      }
+      Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
+      Tlev[b] = (int)Tkeep.size() - 1;
+    }
+  }
+  // ---- compact T_UP / T_DN / T_DN^T and J arenas
+  oT.assign(nboxes, 0);
+  oJ.assign(nboxes, 0);
+  long long tt = 0, tj = 0;
+  for (int b = 1; b < nboxes; ++b) {
+    oT[b] = tt; tt += (long long)kskel[b] * (nskel[b] - kskel[b]);
+    oJ[b] = tj; tj += nskel[b];
+  }
+  T_UP.alloc(std::max(tt, 1LL)); T_DN.alloc(std::max(tt, 1LL)); TDNT.alloc(std::max(tt, 1LL));
+  std::vector<MoveP> mv;
+  std::vector<int> hJU(std::max(tj, 1LL)), hJD(std::max(tj, 1LL));
+  for (int b = 1; b < nboxes; ++b) {
+    const int n = nskel[b], k = kskel[b];
+    std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
+    std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJ[b]);
+    if (n - k <= 0 || k == 0) continue;
+    const double* Tl = Tkeep[Tlev[b]].p;
+    mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, 3, 0});
+  }
+  run_moves(mv, stream);
+  upload_vec(JUPd, hJU, stream);
+  upload_vec(JDNd, hJD, stream);
+  Tkeep.clear();
+  // ---- M_SELF (leaves) and M_SIB (:220-271)
+  oSelf.assign(nboxes, -1);
+  oSib.assign(nboxes, -1);
+  long long ts = 0, tb = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (b > 0 && is_leaf(b)) { oSelf[b] = ts; ts += (long long)cnt[b] * cnt[b]; }
+    if (!is_leaf(b)) {
+      const int s1 = c1[b], s2 = c2[b];
+      oSib[s1] = tb; tb += (long long)kskel[s1] * kskel[s2];
+      oSib[s2] = tb; tb += (long long)kskel[s2] * kskel[s1];
+    }
+  }
+  M_SELF.alloc(std::max(ts, 1LL));
+  M_SIB.alloc(std::max(tb, 1LL));
+  std::vector<int> idx;
+  std::vector<KgenP<double>> kg;
+  std::vector<long long> io;
+  auto push = [&](const std::vector<int>& v) { io.push_back(idx.size()); idx.insert(idx.end(), v.begin(), v.end()); };
+  for (int b = 0; b < nboxes; ++b) {
+    if (b > 0 && is_leaf(b)) {
+      std::vector<int> r(cnt[b]);
+      std::iota(r.begin(), r.end(), off[b]);
+      push(r);
+    }
+    if (!is_leaf(b)) {
+      push(I_SKDN[c1[b]]); push(I_SKUP[c2[b]]);
+      push(I_SKDN[c2[b]]); push(I_SKUP[c1[b]]);
+    }
+  }
+  DevBuf<int> didx;
+  upload_vec(didx, idx, stream);
+  size_t q = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (b > 0 && is_leaf(b)) {
+      const int* r = didx.p + io[q++];
+      kg.push_back(KgenP<double>{r, r, cnt[b], cnt[b], M_SELF.p + oSelf[b], cnt[b], 0});
+    }
+    if (!is_leaf(b)) {
+      const int s1 = c1[b], s2 = c2[b];
+      const int* a = didx.p + io[q++];
+      const int* bb = didx.p + io[q++];
+      kg.push_back(KgenP<double>{a, bb, kskel[s1], kskel[s2], M_SIB.p + oSib[s1], kskel[s1], 0});
+      const int* c = didx.p + io[q++];
+      const int* d = didx.p + io[q++];
+      kg.push_back(KgenP<double>{c, d, kskel[s2], kskel[s1], M_SIB.p + oSib[s2], kskel[s2], 0});
+    }
+  }
+  long long maxe = 0;
+  for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
+  DevBuf<KgenP<double>> dkg;
+  upload_vec(dkg, kg, stream);
+  for (size_t o = 0; o < kg.size(); o += 65535) {
+    const int c = (int)std::min<size_t>(65535, kg.size() - o);
+    kgen_batched<double>(dkg.p + o, c, maxe, view(pts), kdev, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  inverted = false;
+}
+
+// ---------------------------------------------------------------------------
+void HSS1D::invert() {
+  oL.assign(nboxes, 0); oR.assign(nboxes, 0); oD.assign(nboxes, 0); oE.assign(nboxes, 0);
+  long long tl = 0, td = 0, te = 0;
+  for (int b = 1; b < nboxes; ++b) {
+    const long long n = nskel[b], k = kskel[b];
+    oL[b] = tl; oR[b] = tl; tl += n * k;
+    oD[b] = td; td += n * n;
+    oE[b] = te; te += k * k;
+  }
+  Linv.alloc(std::max(tl, 1LL)); Rinv.alloc(std::max(tl, 1LL)); Dinv.alloc(std::max(td, 1LL));
+  Einv.alloc(std::max(te, 1LL));
+  DevBuf<double> Fw(std::max(td, 1LL)), W1(std::max(td, 1LL)), W2(std::max(td, 1LL)), W3(std::max(tl, 1LL));
+  for (int Lv = maxlev; Lv >= 1; --Lv) {
+    std::vector<int> boxes;
+    for (int b = 1; b < nboxes; ++b)
+      if (level[b] == Lv) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    std::vector<F1P> fa;
+    std::vector<std::pair<double*, int>> mats;
+    for (int b : boxes) {
+      const int n = nskel[b];
+      if (is_leaf(b)) {
+        fa.push_back(F1P{Fw.p + oD[b], n, 0, nullptr, nullptr, nullptr, nullptr, M_SELF.p + oSelf[b]});
+      } else {
+        const int s1 = c1[b], s2 = c2[b];
+        fa.push_back(F1P{Fw.p + oD[b], n, kskel[s1], Einv.p + oE[s1], M_SIB.p + oSib[s1], M_SIB.p + oSib[s2],
+                         Einv.p + oE[s2], nullptr});
+      }
+      mats.push_back({Fw.p + oD[b], n});
+    }
+    {
+      DevBuf<F1P> d;
+      upload_vec(d, fa, stream);
+      k_assemble1<<<(int)fa.size(), 256, 0, stream>>>(d.p);
+      check_launch("k_assemble1");
+      HSS_CUDA(cudaStreamSynchronize(stream));
+    }
+    invert_many(mats, stream);
+    std::vector<MoveP> mv;
+    for (int b : boxes) {
+      const int n = nskel[b];
+      mv.push_back(MoveP{Fw.p + oD[b], W1.p + oD[b], JUPd.p + oJ[b], n, n, n, n, 0, 0});   // Finv[J_UP, :]
+      mv.push_back(MoveP{Fw.p + oD[b], W2.p + oD[b], JDNd.p + oJ[b], n, n, n, n, 1, 0});   // Finv[:, J_DN]
+    }
+    run_moves(mv, stream);
+    std::vector<GemmP<double>> P1, P2;
+    for (int b : boxes) {
+      const int n = nskel[b], k = kskel[b], nr = n - k;
+      if (nr <= 0 || k == 0) continue;
+      // RF = W1[0:k,:] + T_UP W1[k:n,:]   ;  FL = W2[:,0:k] + W2[:,k:n] T_DN^T
+      P1.push_back(GemmP<double>{T_UP.p + oT[b], W1.p + oD[b] + k, W1.p + oD[b], k, n, nr, k, n, n});
+      P2.push_back(GemmP<double>{W2.p + oD[b] + (size_t)k * n, T_DN.p + oT[b], W2.p + oD[b], n, k, nr, n, k, n});
+    }
+    run_gemms(P1, false, false, 1.0, 1.0, stream);
+    run_gemms(P2, false, true, 1.0, 1.0, stream);
+    mv.clear();
+    for (int b : boxes) {
+      const int n = nskel[b], k = kskel[b];
+      mv.push_back(MoveP{W1.p + oD[b], W3.p + oL[b], JDNd.p + oJ[b], k, n, n, k, 1, 0});  // RF[:, J_DN]
+    }
+    run_moves(mv, stream);
+    P1.clear();
+    for (int b : boxes) {
+      const int n = nskel[b], k = kskel[b], nr = n - k;
+      if (nr <= 0 || k == 0) continue;
+      P1.push_back(GemmP<double>{W3.p + oL[b] + (size_t)k * k, T_DN.p + oT[b], W3.p + oL[b], k, k, nr, k, k, k});
+    }
+    run_gemms(P1, false, true, 1.0, 1.0, stream);
+    mv.clear();
+    mats.clear();
+    for (int b : boxes) {
+      const int k = kskel[b];
+      mv.push_back(MoveP{W3.p + oL[b], Einv.p + oE[b], nullptr, k, k, k, k, 0, 0});
+      mats.push_back({Einv.p + oE[b], k});
+    }
+    run_moves(mv, stream);
+    invert_many(mats, stream);
+    // Linv = FL E ; Rinv = E RF ; Dinv = Finv - Linv RF
+    std::vector<GemmP<double>> PL, PR, PD;
+    mv.clear();
+    for (int b : boxes) {
+      const int n = nskel[b], k = kskel[b];
+      PL.push_back(GemmP<double>{W2.p + oD[b], Einv.p + oE[b], Linv.p + oL[b], n, k, k, n, k, n});
+      PR.push_back(GemmP<double>{Einv.p + oE[b], W1.p + oD[b], Rinv.p + oR[b], k, n, k, k, n, k});
+      mv.push_back(MoveP{Fw.p + oD[b], Dinv.p + oD[b], nullptr, n, n, n, n, 0, 0});
+    }
+    run_gemms(PL, false, false, 1.0, 0.0, stream);
+    run_gemms(PR, false, false, 1.0, 0.0, stream);
+    run_moves(mv, stream);
+    for (int b : boxes) {
+      const int n = nskel[b], k = kskel[b];
+      PD.push_back(GemmP<double>{Linv.p + oL[b], W1.p + oD[b], Dinv.p + oD[b], n, n, k, n, n, n});
+    }
+    run_gemms(PD, false, false, -1.0, 1.0, stream);
+  }
+  // top: FT = [E2 M_SIB2; M_SIB3 E3] (reference boxes 2, 3 = ids 1, 2)
+  const int ka = kskel[1], kb = kskel[2];
+  ktop = ka + kb;
+  FTinv.alloc((size_t)ktop * ktop);
+  std::vector<F1P> fa = {F1P{FTinv.p, ktop, ka, Einv.p + oE[1], M_SIB.p + oSib[1], M_SIB.p + oSib[2],
+                             Einv.p + oE[2], nullptr}};
+  DevBuf<F1P> d;
+  upload_vec(d, fa, stream);
+  k_assemble1<<<1, 256, 0, stream>>>(d.p);
+  check_launch("k_assemble1 top");
+  std::vector<std::pair<double*, int>> mats = {{FTinv.p, ktop}};
+  invert_many(mats, stream);
+  inverted = true;
+}
+
+// ---------------------------------------------------------------------------
+// per-level stacked vectors: rows of level L are its boxes in id order
+struct Stack1 {
+  std::vector<long long> base;  // per level: element offset of the level block
+  std::vector<int> ld;          // per level: total rows
+  std::vector<long long> row;   // per box: row offset within its level
+};
+
+static Stack1 make_stack(const HSS1D& H, int width) {
+  Stack1 s;
+  s.base.assign(H.maxlev + 2, 0);
+  s.ld.assign(H.maxlev + 2, 0);
+  s.row.assign(H.nboxes, 0);
+  for (int b = 1; b < H.nboxes; ++b) {
+    s.row[b] = s.ld[H.level[b]];
+    s.ld[H.level[b]] += H.kskel[b];
+  }
+  long long acc = 0;
+  for (int L = 0; L <= H.maxlev + 1; ++L) { s.base[L] = acc; acc += (long long)s.ld[L] * width; }
+  s.base.push_back(acc);
+  return s;
+}
+
+void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_applyinv before hss1d_invert");
+  const Stack1 S = make_stack(*this, 8);
+  v1.alloc(std::max(S.base.back(), 1LL));
+  v2.alloc(std::max(S.base.back(), 1LL));
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    const double* ff = dX + (size_t)c0 * N;
+    double* xx = dY + (size_t)c0 * N;
+    auto vin = [&](int b, const double*& p, int& ld) {
+      if (is_leaf(b)) { p = ff + off[b]; ld = (int)N; }
+      else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
+    };
+    for (int L = maxlev; L >= 1; --L) {
+      std::vector<GemmP<double>> P;
+      for (int b = 1; b < nboxes; ++b) {
+        if (level[b] != L) continue;
+        const double* in;
+        int ldi;
+        vin(b, in, ldi);
+        P.push_back(GemmP<double>{Rinv.p + oR[b], in, v1.p + S.base[L] + S.row[b], kskel[b], r, nskel[b], kskel[b],
+                                  ldi, S.ld[L]});
+      }
+      run_gemms(P, false, false, 1.0, 0.0, stream, true);
+    }
+    {
+      std::vector<GemmP<double>> P = {GemmP<double>{FTinv.p, v1.p + S.base[1], v2.p + S.base[1], ktop, r, ktop, ktop,
+                                                    S.ld[1], S.ld[1]}};
+      run_gemms(P, false, false, 1.0, 0.0, stream, true);
+    }
+    for (int L = 1; L <= maxlev; ++L) {
+      std::vector<GemmP<double>> P1, P2;
+      for (int b = 1; b < nboxes; ++b) {
+        if (level[b] != L) continue;
+        double* out;
+        int ldo;
+        if (is_leaf(b)) { out = xx + off[b]; ldo = (int)N; }
+        else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
+        const double* in;
+        int ldi;
+        vin(b, in, ldi);
+        P1.push_back(GemmP<double>{Linv.p + oL[b], v2.p + S.base[L] + S.row[b], out, nskel[b], r, kskel[b], nskel[b],
+                                   S.ld[L], ldo});
+        P2.push_back(GemmP<double>{Dinv.p + oD[b], in, out, nskel[b], r, nskel[b], nskel[b], ldi, ldo});
+      }
+      run_gemms(P1, false, false, 1.0, 0.0, stream, true);
+      run_gemms(P2, false, false, 1.0, 1.0, stream, true);
+    }
+  }
+}
+
+void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
+  const Stack1 S = make_stack(*this, 8);
+  v1.alloc(std::max(S.base.back(), 1LL));
+  v2.alloc(std::max(S.base.back(), 1LL));
+  std::vector<long long> oS(nboxes, 0);
+  long long ts = 0;
+  for (int b = 1; b < nboxes; ++b) { oS[b] = ts; ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8; }
+  v3.alloc(std::max(ts, 1LL));
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    const double* qq = dX + (size_t)c0 * N;
+    double* uu = dY + (size_t)c0 * N;
+    auto vin = [&](int b, const double*& p, int& ld) {
+      if (is_leaf(b)) { p = qq + off[b]; ld = (int)N; }
+      else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
+    };
+    // upward: phi_up = q(J(1:k)) + T_UP q(J(k+1:n))
+    for (int L = maxlev; L >= 1; --L) {
+      std::vector<MoveP> mv;
+      std::vector<GemmP<double>> P;
+      for (int b = 1; b < nboxes; ++b) {
+        if (level[b] != L) continue;
+        const int n = nskel[b], k = kskel[b], nr = n - k;
+        const double* in;
+        int ldi;
+        vin(b, in, ldi);
+        mv.push_back(MoveP{in, v1.p + S.base[L] + S.row[b], JUPd.p + oJ[b], k, r, ldi, S.ld[L], 0, 0});
+        if (nr > 0) {
+          mv.push_back(MoveP{in, v3.p + oS[b], JUPd.p + oJ[b] + k, nr, r, ldi, nr, 0, 0});
+          P.push_back(GemmP<double>{T_UP.p + oT[b], v3.p + oS[b], v1.p + S.base[L] + S.row[b], k, r, nr, k, nr,
+                                    S.ld[L]});
+        }
+      }
+      run_moves(mv, stream);
+      run_gemms(P, false, false, 1.0, 1.0, stream, true);
+    }
+    // top sibling interactions
+    {
+      std::vector<GemmP<double>> P = {
+          GemmP<double>{M_SIB.p + oSib[1], v1.p + S.base[1] + S.row[2], v2.p + S.base[1] + S.row[1], kskel[1], r,
+                        kskel[2], kskel[1], S.ld[1], S.ld[1]},
+          GemmP<double>{M_SIB.p + oSib[2], v1.p + S.base[1] + S.row[1], v2.p + S.base[1] + S.row[2], kskel[2], r,
+                        kskel[1], kskel[2], S.ld[1], S.ld[1]}};
+      run_gemms(P, false, false, 1.0, 0.0, stream, true);
+    }
+    // downward: u_long = L phi_dn (+ sibling terms or self term)
+    for (int L = 1; L <= maxlev; ++L) {
+      std::vector<GemmP<double>> PT, PS;
+      std::vector<MoveP> mv;
+      for (int b = 1; b < nboxes; ++b) {
+        if (level[b] != L) continue;
+        const int n = nskel[b], k = kskel[b], nr = n - k;
+        const double* dn = v2.p + S.base[L] + S.row[b];
+        double* out;
+        int ldo;
+        if (is_leaf(b)) { out = uu + off[b]; ldo = (int)N; }
+        else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
+        if (nr > 0)
+          PT.push_back(GemmP<double>{TDNT.p + oT[b], dn, v3.p + oS[b], nr, r, k, nr, S.ld[L], nr});
+        mv.push_back(MoveP{dn, out, JDNd.p + oJ[b], k, r, S.ld[L], ldo, 2, 0});
+        if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJ[b] + k, nr, r, nr, ldo, 2, 0});
+        if (is_leaf(b)) {
+          PS.push_back(GemmP<double>{M_SELF.p + oSelf[b], qq + off[b], out, n, r, n, n, (int)N, ldo});
+        } else {
+          const int s1 = c1[b], s2 = c2[b];
+          const double* up1 = v1.p + S.base[L + 1] + S.row[s1];
+          const double* up2 = v1.p + S.base[L + 1] + S.row[s2];
+          PS.push_back(GemmP<double>{M_SIB.p + oSib[s1], up2, out, kskel[s1], r, kskel[s2], kskel[s1], S.ld[L + 1],
+                                     ldo});
+          PS.push_back(GemmP<double>{M_SIB.p + oSib[s2], up1, out + kskel[s1], kskel[s2], r, kskel[s1], kskel[s2],
+                                     S.ld[L + 1], ldo});
+        }
+      }
+      run_gemms(PT, false, false, 1.0, 0.0, stream, true);
+      run_moves(mv, stream);
+      run_gemms(PS, false, false, 1.0, 1.0, stream, true);
+    }
+  }
+}
+
+}  // namespace hss

@@ -1,0 +1,842 @@
+// HSS2D dense-block ("HSS-D") solver on the GPU.
+//
+//  build_tree : host geometry (hss2d_tree.cpp) + level-batched least squares
+//               T = K(Xp,X_sk) \ K(Xp,X_rs)   (interpolation_operator.m:57-77)
+//  compress   : Bself, B12, B21 kernel blocks (HSS2D_compress_nsym.m:81-107)
+//  invert     : per level, FI = inv([E1 B12; B21 E2]) and E = inv(R FI L)
+//               (HSS2D_invert_nsym.m:70-155, build_Finv_nsym.m:92-100,
+//               build_E_nsym.m:43-51), stored in the precomputed form
+//                 U = E R FI (k x n),  G = FI L (n x k),  GE = G E (n x k)
+//               so the inverse apply of HSS2D_applyinv_nsym.m:74-243 becomes
+//                 up:   phi_up = U q
+//                 down: phi    = FI q - G phi_up + GE phi_dn
+//               (algebraically identical: R FI q = tmp, E tmp = phi_up,
+//               lam = q - L phi_up, eta = L E phi_dn, phi = FI (eta + lam)).
+//  apply      : forward telescoping product (HSS2D_apply_nsym.m:74-218), FP64.
+//  solve      : inverse apply + iterative refinement against the FP64 forward
+//               operator (Iterative_Refinement.m:20-35).
+#include "hss2d.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace hss {
+
+// ---------------------------------------------------------------------------
+// small batched kernels
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_assemble_F(int nb, int n, int kc, int leaf, const double* __restrict__ Bself,
+                             const double* __restrict__ B12, const double* __restrict__ B21,
+                             const R* __restrict__ Ech, R* __restrict__ F) {
+  const long long per = (long long)n * n;
+  const long long tot = per * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / per);
+    const long long r = e - (long long)b * per;
+    const int i = (int)(r % n), j = (int)(r / n);
+    R v;
+    if (leaf) {
+      v = (R)Bself[e];
+    } else {
+      const int bi = i >= kc, bj = j >= kc;
+      const int ii = i - bi * kc, jj = j - bj * kc;
+      const long long o = ii + (long long)jj * kc;
+      const long long kk = (long long)kc * kc;
+      if (!bi && !bj) v = Ech[(2LL * b) * kk + o];
+      else if (!bi && bj) v = (R)B12[(long long)b * kk + o];
+      else if (bi && !bj) v = (R)B21[(long long)b * kk + o];
+      else v = Ech[(2LL * b + 1) * kk + o];
+    }
+    F[e] = v;
+  }
+}
+
+// dst_b[i + c*ldd] = src_b[J_b[i] + c*lds]  (row gather), rows i < n, cols c < ncol
+template <typename R>
+__global__ void k_gather_rows(int nb, int n, int ncol, const int* __restrict__ J, const R* __restrict__ src,
+                              long long sstride, int lds, R* __restrict__ dst, long long dstride, int ldd) {
+  const long long per = (long long)n * ncol, tot = per * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / per);
+    const long long r = e - (long long)b * per;
+    const int i = (int)(r % n), c = (int)(r / n);
+    dst[b * dstride + i + (long long)c * ldd] = src[b * sstride + J[(long long)b * n + i] + (long long)c * lds];
+  }
+}
+
+// dst_b[i + c*ldd] = src_b[i + J_b[c]*lds]  (column gather), rows i < nrow, cols c < n
+template <typename R>
+__global__ void k_gather_cols(int nb, int nrow, int n, const int* __restrict__ J, const R* __restrict__ src,
+                              long long sstride, int lds, R* __restrict__ dst, long long dstride, int ldd) {
+  const long long per = (long long)nrow * n, tot = per * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / per);
+    const long long r = e - (long long)b * per;
+    const int i = (int)(r % nrow), c = (int)(r / nrow);
+    dst[b * dstride + i + (long long)c * ldd] = src[b * sstride + i + (long long)J[(long long)b * n + c] * lds];
+  }
+}
+
+// strided batched copy with conversion: dst_b(0:m,0:n) = src_b(0:m,0:n)
+template <typename S, typename D>
+__global__ void k_copy2d(int nb, int m, int n, const S* __restrict__ src, long long sstride, int lds,
+                         D* __restrict__ dst, long long dstride, int ldd) {
+  const long long per = (long long)m * n, tot = per * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / per);
+    const long long r = e - (long long)b * per;
+    const int i = (int)(r % m), j = (int)(r / m);
+    dst[b * dstride + i + (long long)j * ldd] = (D)src[b * sstride + i + (long long)j * lds];
+  }
+}
+
+// transpose copy: dst_b(j, i) = src_b(i, j), src m x n
+__global__ void k_transpose(int nb, int m, int n, const double* __restrict__ src, long long sstride, int lds,
+                            double* __restrict__ dst, long long dstride, int ldd) {
+  const long long per = (long long)m * n, tot = per * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / per);
+    const long long r = e - (long long)b * per;
+    const int j = (int)(r % n), i = (int)(r / n);
+    dst[b * dstride + j + (long long)i * ldd] = src[b * sstride + i + (long long)j * lds];
+  }
+}
+
+// Row map of box i, local row q (J order) into the level's input / output:
+//   leaf  : global point IsrcJ[i*n+q]            (vector ld = N)
+//   parent: children stack row 2i*kc + J[i*n+q]   (vector ld = 2*nb*kc)
+__device__ __forceinline__ long long rowmap(int leaf, const int* J, const int* IsrcJ, int i, int n, int kc,
+                                            int q) {
+  const long long o = (long long)i * n + q;
+  return leaf ? (long long)IsrcJ[o] : (long long)(2 * i) * kc + J[o];
+}
+
+// forward apply gather: q in J order -> [phi_up (k rows) | rs (n-k rows)]
+__global__ void k_fwd_gather(int nb, int n, int k, int kc, int leaf, int r, const int* __restrict__ J,
+                             const int* __restrict__ IsrcJ, const double* __restrict__ src, long long lds,
+                             double* __restrict__ up, long long ldu, double* __restrict__ rs, long long ldr) {
+  const long long tot = (long long)nb * n * r;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e / ((long long)nb * n));
+    const long long t = e - (long long)c * nb * n;
+    const int i = (int)(t / n), q = (int)(t % n);
+    const double v = src[rowmap(leaf, J, IsrcJ, i, n, kc, q) + c * lds];
+    if (q < k) up[(long long)i * k + q + c * ldu] = v;
+    else rs[(long long)i * (n - k) + (q - k) + c * ldr] = v;
+  }
+}
+
+// forward apply scatter-add: phi[J[q]] += q < k ? dn[q] : tmp[q-k]
+__global__ void k_fwd_scatter(int nb, int n, int k, int kc, int leaf, int r, const int* __restrict__ J,
+                              const int* __restrict__ IsrcJ, double* __restrict__ dst, long long ldd,
+                              const double* __restrict__ dn, long long ldn, const double* __restrict__ tmp,
+                              long long ldt) {
+  const long long tot = (long long)nb * n * r;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e / ((long long)nb * n));
+    const long long t = e - (long long)c * nb * n;
+    const int i = (int)(t / n), q = (int)(t % n);
+    const double v = (q < k) ? dn[(long long)i * k + q + c * ldn] : tmp[(long long)i * (n - k) + (q - k) + c * ldt];
+    dst[rowmap(leaf, J, IsrcJ, i, n, kc, q) + c * ldd] += v;
+  }
+}
+
+template <typename S, typename D>
+__global__ void k_convert(long long cnt, const S* __restrict__ a, D* __restrict__ b) {
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < cnt; e += (long long)gridDim.x * 256) b[e] = (D)a[e];
+}
+
+// res = f - y (column-major N x r), and per-column squared norms of res and f
+__global__ void k_residual(long long N, int r, const double* __restrict__ f, long long ldf,
+                           const double* __restrict__ y, long long ldy, double* __restrict__ res,
+                           long long ldr, double* __restrict__ part /* gridDim.x x r x 2 */) {
+  __shared__ double sr[8], sf[8];
+  for (int c = 0; c < r; ++c) {
+    double a = 0.0, b = 0.0;
+    for (long long i = blockIdx.x * 256LL + threadIdx.x; i < N; i += (long long)gridDim.x * 256) {
+      const double fv = f[i + c * ldf];
+      const double rv = fv - y[i + c * ldy];
+      res[i + c * ldr] = rv;
+      a += rv * rv;
+      b += fv * fv;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = a; sf[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int w = 0; w < 8; ++w) { ta += sr[w]; tb += sf[w]; }
+      part[((long long)blockIdx.x * r + c) * 2] = ta;
+      part[((long long)blockIdx.x * r + c) * 2 + 1] = tb;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_axpy(long long N, int r, const double* __restrict__ dx, long long ldd, double* __restrict__ x,
+                       long long ldx) {
+  const long long tot = N * r;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const long long i = e % N, c = e / N;
+    x[i + c * ldx] += dx[i + c * ldd];
+  }
+}
+
+static int grid_for(long long tot) { return std::max(1, std::min(ceil_div(tot, 256), 4096)); }
+
+// ---------------------------------------------------------------------------
+// descriptor helpers
+// ---------------------------------------------------------------------------
+template <typename R>
+static void run_gemm(std::vector<GemmP<R>>& P, bool tA, bool tB, R alpha, R beta, cudaStream_t s,
+                     DevBuf<GemmP<R>>& scratch) {
+  if (P.empty()) return;
+  int maxM = 0, maxN = 0;
+  for (auto& p : P) { maxM = std::max(maxM, p.M); maxN = std::max(maxN, p.N); }
+  scratch.alloc(P.size());
+  HSS_CUDA(cudaMemcpyAsync(scratch.p, P.data(), P.size() * sizeof(GemmP<R>), cudaMemcpyHostToDevice, s));
+  gemm_batched<R>(scratch.p, (int)P.size(), maxM, maxN, tA, tB, alpha, beta, s);
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename R>
+void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s) {
+  Step st;
+  st.batch = (int)P.size();
+  st.maxM = 0;
+  for (auto& p : P) st.maxM = std::max(st.maxM, p.M);
+  st.alpha = alpha;
+  st.beta = beta;
+  st.d.alloc(P.size());
+  HSS_CUDA(cudaMemcpyAsync(st.d.p, P.data(), P.size() * sizeof(GemmP<R>), cudaMemcpyHostToDevice, s));
+  steps.push_back(std::move(st));
+}
+
+template <typename R>
+void SolvePlan<R>::run(cudaStream_t s) const {
+  for (auto& st : steps) gemm_skinny<R>(st.d.p, st.batch, st.maxM, st.alpha, st.beta, s);
+}
+
+template struct SolvePlan<double>;
+template struct SolvePlan<float>;
+
+// ---------------------------------------------------------------------------
+// build_tree
+// ---------------------------------------------------------------------------
+void HSS2D::build_tree() {
+  build_tree_geometry(prm, geo);
+  kdev = make_kernel_dev(prm.kp);
+  const long long N = geo.N;
+  const size_t npts = (size_t)N + geo.proxy_x.size();
+  std::vector<double> hx(npts), hy(npts), zero(npts, 0.0);
+  for (long long i = 0; i < N; ++i) { hx[i] = geo.X[2 * i]; hy[i] = geo.X[2 * i + 1]; }
+  for (size_t i = 0; i < geo.proxy_x.size(); ++i) { hx[N + i] = geo.proxy_x[i]; hy[N + i] = geo.proxy_y[i]; }
+  pts.upload(hx, hy, zero, zero, zero, zero, prm.kp, stream);
+  L.clear();
+  L.resize(geo.depth + 1);
+  for (int lev = 0; lev <= geo.depth; ++lev) {
+    auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    d.J.upload(g.J, stream);
+    d.Isrc.upload(g.Isrc, stream);
+    d.IsrcJ.upload(g.IsrcJ, stream);
+    d.proxy.upload(g.proxy, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  for (int lev = geo.depth; lev >= 1; --lev) compute_T(lev);
+  tree_built = true;
+}
+
+void HSS2D::compute_T(int lev) {
+  auto& g = geo.levels[lev];
+  auto& d = L[lev];
+  const int nb = g.nb, n = g.n, k = g.k, p = g.p, nr = n - k;
+  d.Tup.alloc((size_t)nb * k * std::max(nr, 1));
+  d.Tdn.alloc((size_t)nb * k * std::max(nr, 1));
+  d.TdnT.alloc((size_t)nb * k * std::max(nr, 1));
+  if (nr == 0 || k == 0) return;
+  HSS_REQUIRE(p >= k, HSS_ERR_ARG, "proxy set smaller than skeleton: least squares is underdetermined");
+  const int batch = 2 * nb;
+  DevBuf<double> A((size_t)batch * p * n);
+  // kernel blocks: problem 2i = [K(Xp, X_sk) | K(Xp, X_rs)], 2i+1 = K(X_src[J], Xp)^T
+  std::vector<KgenP<double>> kg(batch);
+  for (int i = 0; i < nb; ++i) {
+    kg[2 * i] = KgenP<double>{d.proxy.p + (size_t)i * p, d.IsrcJ.p + (size_t)i * n, p, n,
+                              A.p + (size_t)(2 * i) * p * n, p, 0};
+    kg[2 * i + 1] = KgenP<double>{d.IsrcJ.p + (size_t)i * n, d.proxy.p + (size_t)i * p, n, p,
+                                  A.p + (size_t)(2 * i + 1) * p * n, p, 1};
+  }
+  DevBuf<KgenP<double>> dkg(batch);
+  HSS_CUDA(cudaMemcpyAsync(dkg.p, kg.data(), batch * sizeof(KgenP<double>), cudaMemcpyHostToDevice, stream));
+  kgen_batched<double>(dkg.p, batch, (long long)p * n, view(pts), kdev, stream);
+  DevBuf<double> V((size_t)batch * p * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * k);
+  std::vector<QrP<double>> qp(batch);
+  for (int b = 0; b < batch; ++b)
+    qp[b] = QrP<double>{A.p + (size_t)b * p * n, p, n, k, p, V.p + (size_t)b * p * QR_NB,
+                        Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k};
+  DevBuf<QrP<double>> dqp(batch);
+  HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
+  lstsq_batched<double>(dqp.p, batch, p, n, k, stream);
+  // T_up from even problems, T_dn from odd ones: A(0:k, k:n), ld p
+  k_copy2d<double, double><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(
+      nb, k, nr, A.p + (size_t)k * p, 2LL * p * n, p, d.Tup.p, (long long)k * nr, k);
+  k_copy2d<double, double><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(
+      nb, k, nr, A.p + (size_t)p * n + (size_t)k * p, 2LL * p * n, p, d.Tdn.p, (long long)k * nr, k);
+  k_transpose<<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(nb, k, nr, d.Tdn.p, (long long)k * nr, k,
+                                                                     d.TdnT.p, (long long)k * nr, nr);
+  check_launch("compute_T copies");
+  // rank diagnostics: smallest/largest |R_ii| over the level
+  std::vector<double> hd;
+  download(hd, diag.p, (size_t)batch * k, stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  double mn = INFINITY, mx = 0.0;
+  bool finite = true;
+  for (double v : hd) { finite = finite && std::isfinite(v); mn = std::min(mn, v); mx = std::max(mx, v); }
+  HSS_REQUIRE(finite, HSS_ERR_NONFINITE, "non-finite value in interpolation least squares");
+  d.rdiag_min = mn;
+  d.rdiag_max = mx;
+}
+
+// ---------------------------------------------------------------------------
+// compress
+// ---------------------------------------------------------------------------
+void HSS2D::compress() {
+  HSS_REQUIRE(tree_built, HSS_ERR_STATE, "hss2d_compress before hss2d_build_tree");
+  const int depth = geo.depth;
+  std::vector<KgenP<double>> kg;
+  {
+    auto& g = geo.levels[depth];
+    auto& d = L[depth];
+    d.Bself.alloc((size_t)g.nb * g.n * g.n);
+    for (int i = 0; i < g.nb; ++i)
+      kg.push_back(KgenP<double>{d.Isrc.p + (size_t)i * g.n, d.Isrc.p + (size_t)i * g.n, g.n, g.n,
+                                 d.Bself.p + (size_t)i * g.n * g.n, g.n, 0});
+  }
+  for (int lev = 0; lev < depth; ++lev) {
+    auto& gc = geo.levels[lev + 1];
+    auto& dc = L[lev + 1];
+    auto& d = L[lev];
+    const int nb = geo.levels[lev].nb, kc = gc.k, nc = gc.n;
+    d.B12.alloc((size_t)nb * kc * kc);
+    d.B21.alloc((size_t)nb * kc * kc);
+    for (int i = 0; i < nb; ++i) {
+      const int* s1 = dc.IsrcJ.p + (size_t)(2 * i) * nc;
+      const int* s2 = dc.IsrcJ.p + (size_t)(2 * i + 1) * nc;
+      kg.push_back(KgenP<double>{s1, s2, kc, kc, d.B12.p + (size_t)i * kc * kc, kc, 0});
+      kg.push_back(KgenP<double>{s2, s1, kc, kc, d.B21.p + (size_t)i * kc * kc, kc, 0});
+    }
+  }
+  long long maxe = 0;
+  for (auto& q : kg) maxe = std::max(maxe, (long long)q.m * q.n);
+  for (size_t off = 0; off < kg.size(); off += 65535) {
+    const int cnt = (int)std::min<size_t>(65535, kg.size() - off);
+    DevBuf<KgenP<double>> dkg(cnt);
+    HSS_CUDA(cudaMemcpyAsync(dkg.p, kg.data() + off, cnt * sizeof(KgenP<double>), cudaMemcpyHostToDevice, stream));
+    kgen_batched<double>(dkg.p, cnt, maxe, view(pts), kdev, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+  compressed = true;
+  fwd_plans.clear();
+}
+
+// ---------------------------------------------------------------------------
+// invert
+// ---------------------------------------------------------------------------
+template <typename R>
+static R* fac(Level2Dev& d, int which);
+
+template <typename R>
+void HSS2D::invert_impl() {
+  const int depth = geo.depth;
+  DevBuf<GemmP<R>> gscratch;
+  for (int lev = depth; lev >= 0; --lev) {
+    auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    const int nb = g.nb, n = g.n, k = g.k, nr = n - k;
+    const bool leaf = (lev == depth);
+    const int kc = leaf ? 0 : geo.levels[lev + 1].k;
+    auto& FIb = d.fac<R>(0);
+    FIb.alloc((size_t)nb * n * n);
+    R* FI = FIb.p;
+    const R* Ech = leaf ? nullptr : L[lev + 1].fac<R>(1).p;
+    k_assemble_F<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(
+        nb, n, kc, leaf ? 1 : 0, leaf ? d.Bself.p : nullptr, leaf ? nullptr : d.B12.p,
+        leaf ? nullptr : d.B21.p, Ech, FI);
+    check_launch("k_assemble_F");
+    invert_level<R>(FI, n, nb);
+    if (lev == 0) break;
+    // interpolation operators in the factor precision
+    DevBuf<R> Tup, Tdn;
+    const R* pTup;
+    const R* pTdn;
+    if (std::is_same<R, double>::value) {
+      pTup = reinterpret_cast<const R*>(d.Tup.p);
+      pTdn = reinterpret_cast<const R*>(d.Tdn.p);
+    } else {
+      Tup.alloc((size_t)nb * k * std::max(nr, 1));
+      Tdn.alloc((size_t)nb * k * std::max(nr, 1));
+      if (nr > 0) {
+        k_convert<double, R><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>((long long)nb * k * nr, d.Tup.p, Tup.p);
+        k_convert<double, R><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>((long long)nb * k * nr, d.Tdn.p, Tdn.p);
+      }
+      pTup = Tup.p;
+      pTdn = Tdn.p;
+    }
+    DevBuf<R> W1((size_t)nb * n * n), W2((size_t)nb * k * n);
+    // (1) FIJ = FI[J, :]
+    k_gather_rows<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(nb, n, n, d.J.p, FI, (long long)n * n, n,
+                                                                          W1.p, (long long)n * n, n);
+    // (2) RFI = FIJ[0:k,:] + Tup * FIJ[k:n,:]   (in place, rows 0..k-1 of W1)
+    std::vector<GemmP<R>> P;
+    if (nr > 0) {
+      P.clear();
+      for (int i = 0; i < nb; ++i)
+        P.push_back(GemmP<R>{pTup + (size_t)i * k * nr, W1.p + (size_t)i * n * n + k, W1.p + (size_t)i * n * n, k, n,
+                             nr, k, n, n});
+      run_gemm<R>(P, false, false, R(1), R(1), stream, gscratch);
+    }
+    // (3) W2 = RFI[:, J]   (k x n, ld k)
+    k_gather_cols<R><<<grid_for((long long)nb * k * n), 256, 0, stream>>>(nb, k, n, d.J.p, W1.p, (long long)n * n, n,
+                                                                          W2.p, (long long)k * n, k);
+    // (4) EI = W2[:,0:k] + W2[:,k:n] * Tdn^T
+    if (nr > 0) {
+      P.clear();
+      for (int i = 0; i < nb; ++i)
+        P.push_back(GemmP<R>{W2.p + (size_t)i * k * n + (size_t)k * k, pTdn + (size_t)i * k * nr,
+                             W2.p + (size_t)i * k * n, k, k, nr, k, k, k});
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch);
+    }
+    // (5) E = inv(EI)
+    auto& Eb = d.fac<R>(1);
+    Eb.alloc((size_t)nb * k * k);
+    k_copy2d<R, R><<<grid_for((long long)nb * k * k), 256, 0, stream>>>(nb, k, k, W2.p, (long long)k * n, k, Eb.p,
+                                                                       (long long)k * k, k);
+    invert_level<R>(Eb.p, k, nb);
+    // (6) U = E * RFI
+    auto& Ub = d.fac<R>(2);
+    Ub.alloc((size_t)nb * k * n);
+    P.clear();
+    for (int i = 0; i < nb; ++i)
+      P.push_back(GemmP<R>{Eb.p + (size_t)i * k * k, W1.p + (size_t)i * n * n, Ub.p + (size_t)i * k * n, k, n, k, k,
+                           n, k});
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch);
+    // (7) FIc = FI[:, J]
+    k_gather_cols<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(nb, n, n, d.J.p, FI, (long long)n * n, n,
+                                                                          W1.p, (long long)n * n, n);
+    // (8) G = FIc[:,0:k] + FIc[:,k:n] * Tdn^T   (in place, columns 0..k-1)
+    if (nr > 0) {
+      P.clear();
+      for (int i = 0; i < nb; ++i)
+        P.push_back(GemmP<R>{W1.p + (size_t)i * n * n + (size_t)k * n, pTdn + (size_t)i * k * nr,
+                             W1.p + (size_t)i * n * n, n, k, nr, n, k, n});
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch);
+    }
+    auto& Gb = d.fac<R>(3);
+    Gb.alloc((size_t)nb * n * k);
+    k_copy2d<R, R><<<grid_for((long long)nb * n * k), 256, 0, stream>>>(nb, n, k, W1.p, (long long)n * n, n, Gb.p,
+                                                                       (long long)n * k, n);
+    // (10) GE = G * E
+    auto& GEb = d.fac<R>(4);
+    GEb.alloc((size_t)nb * n * k);
+    P.clear();
+    for (int i = 0; i < nb; ++i)
+      P.push_back(GemmP<R>{Gb.p + (size_t)i * n * k, Eb.p + (size_t)i * k * k, GEb.p + (size_t)i * n * k, n, k, k, n,
+                           k, n});
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch);
+    check_launch("invert level");
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+}
+
+template <typename R>
+void HSS2D::invert_level(R* A, int n, int nb) {
+  DevBuf<int> ipiv((size_t)nb * n), info(nb);
+  DevBuf<R> W((size_t)nb * GJ_NB * n), Wf((size_t)nb * n * n);
+  info.zero(stream);
+  std::vector<InvP<R>> P(nb);
+  for (int i = 0; i < nb; ++i)
+    P[i] = InvP<R>{A + (size_t)i * n * n, n, n, ipiv.p + (size_t)i * n, W.p + (size_t)i * GJ_NB * n,
+                   Wf.p + (size_t)i * n * n, info.p + i};
+  DevBuf<InvP<R>> dP(nb);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), nb * sizeof(InvP<R>), cudaMemcpyHostToDevice, stream));
+  invert_batched<R>(dP.p, nb, n, stream);
+  std::vector<int> hi;
+  download(hi, info.p, nb, stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  for (int v : hi) {
+    HSS_REQUIRE(v >= 0, HSS_ERR_NONFINITE, "non-finite pivot in block inversion");
+    HSS_REQUIRE(v == 0, HSS_ERR_SINGULAR, "singular diagonal block in inversion");
+  }
+}
+
+void HSS2D::invert() {
+  HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_invert before hss2d_compress");
+  if (prm.precision == HSS_PREC_MIXED) invert_impl<float>();
+  else invert_impl<double>();
+  inverted = true;
+  inv_plans_d.clear();
+  inv_plans_f.clear();
+}
+
+// ---------------------------------------------------------------------------
+// inverse apply
+// ---------------------------------------------------------------------------
+template <typename R>
+SolvePlan<R>& HSS2D::inv_plan(int r) {
+  auto& cache = plan_cache<R>();
+  auto it = cache.find(r);
+  if (it != cache.end()) return it->second;
+  SolvePlan<R>& pl = cache[r];
+  const int depth = geo.depth;
+  const long long N = geo.N;
+  auto& vin = stage_in<R>();
+  auto& vout = stage_out<R>();
+  const int NG = prm.Ng * prm.Ng;
+  for (int lev = 0; lev <= depth; ++lev) {
+    auto& d = L[lev];
+    const auto& g = geo.levels[lev];
+    d.vec<R>(0).ensure((size_t)g.nb * g.k * 8);
+    d.vec<R>(1).ensure((size_t)g.nb * g.k * 8);
+  }
+  auto qptr = [&](int lev, int i, const R*& ptr, int& ld) {
+    const auto& g = geo.levels[lev];
+    if (lev == depth) {
+      const int b = (1 << lev) - 1 + i;
+      ptr = vin.p + (size_t)NG * geo.leaf_panel[b];
+      ld = (int)N;
+    } else {
+      const auto& gc = geo.levels[lev + 1];
+      ptr = L[lev + 1].vec<R>(0).p + (size_t)(2 * i) * gc.k;
+      ld = gc.nb * gc.k;
+    }
+    (void)g;
+  };
+  // upward pass
+  for (int lev = depth; lev >= 1; --lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    std::vector<GemmP<R>> P;
+    for (int i = 0; i < g.nb; ++i) {
+      const R* q;
+      int ldq;
+      qptr(lev, i, q, ldq);
+      P.push_back(GemmP<R>{d.fac<R>(2).p + (size_t)i * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
+                           g.k, ldq, g.nb * g.k});
+    }
+    pl.add(P, R(1), R(0), stream);
+  }
+  // downward pass
+  for (int lev = 0; lev <= depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    std::vector<GemmP<R>> P1, P2, P3;
+    for (int i = 0; i < g.nb; ++i) {
+      R* out;
+      int ldo;
+      if (lev == depth) {
+        const int b = (1 << lev) - 1 + i;
+        out = vout.p + (size_t)NG * geo.leaf_panel[b];
+        ldo = (int)N;
+      } else {
+        const auto& gc = geo.levels[lev + 1];
+        out = L[lev + 1].vec<R>(1).p + (size_t)(2 * i) * gc.k;
+        ldo = gc.nb * gc.k;
+      }
+      const R* q;
+      int ldq;
+      qptr(lev, i, q, ldq);
+      P1.push_back(GemmP<R>{d.fac<R>(0).p + (size_t)i * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
+      if (lev > 0) {
+        P2.push_back(GemmP<R>{d.fac<R>(3).p + (size_t)i * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
+                              g.k, g.n, g.nb * g.k, ldo});
+        P3.push_back(GemmP<R>{d.fac<R>(4).p + (size_t)i * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
+                              g.k, g.n, g.nb * g.k, ldo});
+      }
+    }
+    pl.add(P1, R(1), R(0), stream);
+    if (lev > 0) {
+      pl.add(P2, R(-1), R(1), stream);
+      pl.add(P3, R(1), R(1), stream);
+    }
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  return pl;
+}
+
+template <typename R>
+void HSS2D::applyinv_stage(int r) {
+  // vin (N x r, ld N) -> vout
+  inv_plan<R>(r).run(stream);
+}
+
+void HSS2D::ensure_stage() {
+  const size_t cnt = (size_t)geo.N * 8;
+  Xd.ensure(cnt);
+  Yd.ensure(cnt);
+  if (prm.precision == HSS_PREC_MIXED) { Xf.ensure(cnt); Yf.ensure(cnt); }
+}
+
+void HSS2D::applyinv_device(const double* dX, double* dY, int nrhs, cudaStream_t user) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss2d_applyinv before hss2d_invert");
+  HSS_REQUIRE(nrhs >= 1, HSS_ERR_ARG, "nrhs must be >= 1");
+  ensure_stage();
+  sync_from(user);
+  const long long N = geo.N;
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    if (prm.precision == HSS_PREC_MIXED) {
+      k_convert<double, float><<<grid_for(N * r), 256, 0, stream>>>(N * r, dX + (size_t)c0 * N, Xf.p);
+      applyinv_stage<float>(r);
+      k_convert<float, double><<<grid_for(N * r), 256, 0, stream>>>(N * r, Yf.p, dY + (size_t)c0 * N);
+    } else {
+      HSS_CUDA(cudaMemcpyAsync(Xd.p, dX + (size_t)c0 * N, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+      applyinv_stage<double>(r);
+      HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * N, Yd.p, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    }
+    check_launch("applyinv");
+  }
+  sync_to(user);
+}
+
+// ---------------------------------------------------------------------------
+// forward apply (FP64)
+// ---------------------------------------------------------------------------
+void HSS2D::fwd_prepare(int r) {
+  if (fwd_plans.count(r)) return;
+  FwdPlan& fp = fwd_plans[r];
+  const int depth = geo.depth;
+  const long long N = geo.N;
+  const int NG = prm.Ng * prm.Ng;
+  for (int lev = 0; lev <= depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    d.upF.ensure((size_t)g.nb * g.k * 8);
+    d.dnF.ensure((size_t)g.nb * g.k * 8);
+    d.rsF.ensure((size_t)g.nb * std::max(g.n - g.k, 1) * 8);
+    d.tmF.ensure((size_t)g.nb * std::max(g.n - g.k, 1) * 8);
+  }
+  fp.up.resize(depth + 1);
+  fp.lam.resize(depth + 1);
+  fp.eta.resize(depth + 1);
+  for (int lev = depth; lev >= 1; --lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    const int nr = g.n - g.k;
+    if (nr > 0) {
+      std::vector<GemmP<double>> P;
+      for (int i = 0; i < g.nb; ++i)
+        P.push_back(GemmP<double>{d.Tup.p + (size_t)i * g.k * nr, d.rsF.p + (size_t)i * nr,
+                                  d.upF.p + (size_t)i * g.k, g.k, r, nr, g.k, g.nb * nr, g.nb * g.k});
+      fp.up[lev].add(P, 1.0, 1.0, stream);
+    }
+  }
+  for (int lev = 0; lev <= depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    std::vector<GemmP<double>> P;
+    for (int i = 0; i < g.nb; ++i) {
+      double* out;
+      int ldo;
+      if (lev == depth) {
+        const int b = (1 << lev) - 1 + i;
+        out = Yd.p + (size_t)NG * geo.leaf_panel[b];
+        ldo = (int)N;
+        P.push_back(GemmP<double>{d.Bself.p + (size_t)i * g.n * g.n, Xd.p + (size_t)NG * geo.leaf_panel[b], out, g.n,
+                                  r, g.n, g.n, (int)N, ldo});
+      } else {
+        const auto& gc = geo.levels[lev + 1];
+        auto& dc = L[lev + 1];
+        out = dc.dnF.p + (size_t)(2 * i) * gc.k;
+        ldo = gc.nb * gc.k;
+        const int kc = gc.k;
+        P.push_back(GemmP<double>{d.B12.p + (size_t)i * kc * kc, dc.upF.p + (size_t)(2 * i + 1) * kc, out, kc, r, kc,
+                                  kc, gc.nb * kc, ldo});
+        P.push_back(GemmP<double>{d.B21.p + (size_t)i * kc * kc, dc.upF.p + (size_t)(2 * i) * kc, out + kc, kc, r, kc,
+                                  kc, gc.nb * kc, ldo});
+      }
+    }
+    fp.lam[lev].add(P, 1.0, 0.0, stream);
+    const int nr = g.n - g.k;
+    if (lev > 0 && nr > 0) {
+      std::vector<GemmP<double>> Q;
+      for (int i = 0; i < g.nb; ++i)
+        Q.push_back(GemmP<double>{d.TdnT.p + (size_t)i * g.k * nr, d.dnF.p + (size_t)i * g.k,
+                                  d.tmF.p + (size_t)i * nr, nr, r, g.k, nr, g.nb * g.k, g.nb * nr});
+      fp.eta[lev].add(Q, 1.0, 0.0, stream);
+    }
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+void HSS2D::apply_stage(int r) {
+  // Xd (N x r) -> Yd
+  fwd_prepare(r);
+  FwdPlan& fp = fwd_plans[r];
+  const int depth = geo.depth;
+  const long long N = geo.N;
+  for (int lev = depth; lev >= 1; --lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    const bool leaf = (lev == depth);
+    const int kc = leaf ? 0 : geo.levels[lev + 1].k;
+    const double* src = leaf ? Xd.p : L[lev + 1].upF.p;
+    const long long lds = leaf ? N : (long long)geo.levels[lev + 1].nb * kc;
+    const int nr = g.n - g.k;
+    k_fwd_gather<<<grid_for((long long)g.nb * g.n * r), 256, 0, stream>>>(
+        g.nb, g.n, g.k, kc, leaf ? 1 : 0, r, d.J.p, d.IsrcJ.p, src, lds, d.upF.p, (long long)g.nb * g.k, d.rsF.p,
+        (long long)g.nb * std::max(nr, 1));
+    fp.up[lev].run(stream);
+  }
+  for (int lev = 0; lev <= depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    fp.lam[lev].run(stream);
+    if (lev == 0) continue;
+    const bool leaf = (lev == depth);
+    const int kc = leaf ? 0 : geo.levels[lev + 1].k;
+    double* dst = leaf ? Yd.p : L[lev + 1].dnF.p;
+    const long long ldd = leaf ? N : (long long)geo.levels[lev + 1].nb * kc;
+    const int nr = g.n - g.k;
+    fp.eta[lev].run(stream);
+    k_fwd_scatter<<<grid_for((long long)g.nb * g.n * r), 256, 0, stream>>>(
+        g.nb, g.n, g.k, kc, leaf ? 1 : 0, r, d.J.p, d.IsrcJ.p, dst, ldd, d.dnF.p, (long long)g.nb * g.k, d.tmF.p,
+        (long long)g.nb * std::max(nr, 1));
+  }
+  check_launch("apply");
+}
+
+void HSS2D::apply_device(const double* dX, double* dY, int nrhs, cudaStream_t user) {
+  HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_apply before hss2d_compress");
+  HSS_REQUIRE(nrhs >= 1, HSS_ERR_ARG, "nrhs must be >= 1");
+  ensure_stage();
+  sync_from(user);
+  const long long N = geo.N;
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    HSS_CUDA(cudaMemcpyAsync(Xd.p, dX + (size_t)c0 * N, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    apply_stage(r);
+    HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * N, Yd.p, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  }
+  sync_to(user);
+}
+
+// ---------------------------------------------------------------------------
+// solve with iterative refinement
+// ---------------------------------------------------------------------------
+void HSS2D::solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres,
+                         int* iters, cudaStream_t user) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss2d_solve before hss2d_invert");
+  HSS_REQUIRE(nrhs >= 1 && maxit >= 1, HSS_ERR_ARG, "nrhs and maxit must be >= 1");
+  ensure_stage();
+  sync_from(user);
+  const long long N = geo.N;
+  Rd.ensure((size_t)N * 8);
+  Dd.ensure((size_t)N * 8);
+  const int gx = 256;
+  DevBuf<double> part((size_t)gx * 8 * 2);
+  double worst_all = 0.0;
+  int used_all = 0;
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    const double* f = df + (size_t)c0 * N;
+    double* x = dx + (size_t)c0 * N;
+    // x = A^-1 f
+    solve_once(f, x, r);
+    int used = 1;
+    double worst = 0.0;
+    while (true) {
+      // res = f - A x
+      HSS_CUDA(cudaMemcpyAsync(Xd.p, x, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+      apply_stage(r);
+      k_residual<<<gx, 256, 0, stream>>>(N, r, f, N, Yd.p, N, Rd.p, N, part.p);
+      std::vector<double> hp;
+      download(hp, part.p, (size_t)gx * r * 2, stream);
+      HSS_CUDA(cudaStreamSynchronize(stream));
+      worst = 0.0;
+      for (int c = 0; c < r; ++c) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < gx; ++q) { a += hp[((size_t)q * r + c) * 2]; b += hp[((size_t)q * r + c) * 2 + 1]; }
+        const double rel = (b > 0.0) ? std::sqrt(a / b) : std::sqrt(a);
+        HSS_REQUIRE(std::isfinite(rel), HSS_ERR_NONFINITE, "non-finite residual in refinement");
+        worst = std::max(worst, rel);
+      }
+      if (worst <= tol || used >= maxit) break;
+      solve_once(Rd.p, Dd.p, r);
+      k_axpy<<<grid_for(N * r), 256, 0, stream>>>(N, r, Dd.p, N, x, N);
+      ++used;
+    }
+    worst_all = std::max(worst_all, worst);
+    used_all = std::max(used_all, used);
+  }
+  if (relres) *relres = worst_all;
+  if (iters) *iters = used_all;
+  sync_to(user);
+}
+
+void HSS2D::solve_once(const double* f, double* x, int r) {
+  const long long N = geo.N;
+  if (prm.precision == HSS_PREC_MIXED) {
+    k_convert<double, float><<<grid_for(N * r), 256, 0, stream>>>(N * r, f, Xf.p);
+    applyinv_stage<float>(r);
+    k_convert<float, double><<<grid_for(N * r), 256, 0, stream>>>(N * r, Yf.p, x);
+  } else {
+    HSS_CUDA(cudaMemcpyAsync(Xd.p, f, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    applyinv_stage<double>(r);
+    HSS_CUDA(cudaMemcpyAsync(x, Yd.p, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  }
+  check_launch("solve_once");
+}
+
+// ---------------------------------------------------------------------------
+// stream ordering with a caller stream
+// ---------------------------------------------------------------------------
+void HSS2D::sync_from(cudaStream_t user) {
+  if (user == nullptr || user == stream) return;
+  HSS_CUDA(cudaEventRecord(ev, user));
+  HSS_CUDA(cudaStreamWaitEvent(stream, ev, 0));
+}
+
+void HSS2D::sync_to(cudaStream_t user) {
+  if (user == nullptr) {
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    return;
+  }
+  if (user == stream) return;
+  HSS_CUDA(cudaEventRecord(ev, stream));
+  HSS_CUDA(cudaStreamWaitEvent(user, ev, 0));
+}
+
+HSS2D::HSS2D(const hss2d_params& p) : prm(p) {
+  HSS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  HSS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+}
+
+HSS2D::~HSS2D() {
+  L.clear();
+  if (ev) cudaEventDestroy(ev);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+long long HSS2D::solve_bytes() const {
+  const size_t es = (prm.precision == HSS_PREC_MIXED) ? sizeof(float) : sizeof(double);
+  long long b = 0;
+  for (int lev = 0; lev <= geo.depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    long long per = (long long)g.n * g.n;
+    if (lev > 0) per += 3LL * g.n * g.k;
+    b += per * g.nb;
+  }
+  return b * (long long)es;
+}
+
+int HSS2D::solve_launches(int nrhs) const {
+  // per chunk of 8: 2 staging copies + depth up steps + 1 + 3*depth down steps
+  const int chunks = (nrhs + 7) / 8;
+  return chunks * (2 + geo.depth + 1 + 3 * geo.depth);
+}
+
+}  // namespace hss

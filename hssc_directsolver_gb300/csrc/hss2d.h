@@ -1,0 +1,128 @@
+// HSS2D solver state (device side).  See hss2d.cu.
+#pragma once
+
+#include <map>
+#include <type_traits>
+#include <vector>
+
+#include "dense.cuh"
+#include "hss2d_tree.h"
+#include "kgen.cuh"
+
+namespace hss {
+
+// A fixed sequence of batched skinny products (one inverse or forward apply
+// pass for a given number of right-hand sides); descriptors stay on the device.
+template <typename R>
+struct SolvePlan {
+  struct Step {
+    DevBuf<GemmP<R>> d;
+    int batch = 0, maxM = 0;
+    R alpha = R(1), beta = R(0);
+  };
+  std::vector<Step> steps;
+  void add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s);
+  void run(cudaStream_t s) const;
+  int launches() const { return (int)steps.size(); }
+};
+
+struct Level2Dev {
+  DevBuf<int> J, Isrc, IsrcJ, proxy;
+  // forward operator, FP64
+  DevBuf<double> Tup, Tdn, TdnT;  // k x (n-k) (ld k), k x (n-k), (n-k) x k
+  DevBuf<double> Bself;           // leaves: n x n
+  DevBuf<double> B12, B21;        // parents: kc x kc
+  // inverse factors: 0 FI (n x n), 1 E (k x k), 2 U (k x n), 3 G (n x k), 4 GE (n x k)
+  DevBuf<double> fd[5];
+  DevBuf<float> ff[5];
+  // inverse-apply vectors: 0 phi_up, 1 phi_dn (nb*k x 8)
+  DevBuf<double> vd[2];
+  DevBuf<float> vf[2];
+  // forward-apply vectors (FP64)
+  DevBuf<double> upF, dnF, rsF, tmF;
+  double rdiag_min = 0, rdiag_max = 0;
+
+  template <typename R>
+  DevBuf<R>& fac(int i) {
+    if constexpr (std::is_same<R, double>::value) return fd[i];
+    else return ff[i];
+  }
+  template <typename R>
+  DevBuf<R>& vec(int i) {
+    if constexpr (std::is_same<R, double>::value) return vd[i];
+    else return vf[i];
+  }
+};
+
+struct FwdPlan {
+  std::vector<SolvePlan<double>> up, lam, eta;
+};
+
+struct HSS2D {
+  hss2d_params prm;
+  Tree2D geo;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev = nullptr;
+  PointTable pts;
+  KernelDev kdev{};
+  std::vector<Level2Dev> L;
+  bool tree_built = false, compressed = false, inverted = false;
+  // staging (N x 8): FP64 in/out, FP32 in/out, residual, correction
+  DevBuf<double> Xd, Yd, Rd, Dd;
+  DevBuf<float> Xf, Yf;
+  std::map<int, SolvePlan<double>> inv_plans_d;
+  std::map<int, SolvePlan<float>> inv_plans_f;
+  std::map<int, FwdPlan> fwd_plans;
+
+  explicit HSS2D(const hss2d_params& p);
+  ~HSS2D();
+
+  void build_tree();
+  void compute_T(int lev);
+  void compress();
+  void invert();
+  void applyinv_device(const double* dX, double* dY, int nrhs, cudaStream_t user);
+  void apply_device(const double* dX, double* dY, int nrhs, cudaStream_t user);
+  void solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres, int* iters,
+                    cudaStream_t user);
+  long long solve_bytes() const;
+  int solve_launches(int nrhs) const;
+
+  template <typename R>
+  void invert_impl();
+  template <typename R>
+  void invert_level(R* A, int n, int nb);
+  template <typename R>
+  SolvePlan<R>& inv_plan(int r);
+  template <typename R>
+  void applyinv_stage(int r);
+  void apply_stage(int r);
+  void fwd_prepare(int r);
+  void solve_once(const double* f, double* x, int r);
+  void ensure_stage();
+  void sync_from(cudaStream_t user);
+  void sync_to(cudaStream_t user);
+
+  template <typename R>
+  std::map<int, SolvePlan<R>>& plan_cache() {
+    if constexpr (std::is_same<R, double>::value) return inv_plans_d;
+    else return inv_plans_f;
+  }
+  template <typename R>
+  DevBuf<R>& stage_in() {
+    if constexpr (std::is_same<R, double>::value) return Xd;
+    else return Xf;
+  }
+  template <typename R>
+  DevBuf<R>& stage_out() {
+    if constexpr (std::is_same<R, double>::value) return Yd;
+    else return Yf;
+  }
+};
+
+}  // namespace hss
+
+// opaque C handle
+struct hss2d_matrix {
+  hss::HSS2D* impl;
+};

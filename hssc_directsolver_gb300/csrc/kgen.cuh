@@ -1,0 +1,47 @@
+// Kernel-matrix generation (Common/Kernel_Eval.m) into batched blocks.
+#pragma once
+
+#include "common.cuh"
+
+namespace hss {
+
+// Block b: out[i + j*ld] = K(target ti[i], source si[j])   (trans = 0)
+//          out[j + i*ld] = K(target ti[i], source si[j])   (trans = 1)
+// Indices address the device point table.
+template <typename R>
+struct KgenP {
+  const int* ti;
+  const int* si;
+  int m, n;
+  R* out;
+  int ld;
+  int trans;
+};
+
+// Point table: coordinates plus the per-point modulation values b(p), c(p)
+// and the double-layer source data.
+struct PointTable {
+  DevBuf<double> x, y, nx, ny, w, kap, bval, cval;
+  int count = 0;
+  void upload(const std::vector<double>& hx, const std::vector<double>& hy,
+              const std::vector<double>& hnx, const std::vector<double>& hny,
+              const std::vector<double>& hw, const std::vector<double>& hkap,
+              const hss_kernel_params& kp, cudaStream_t s);
+};
+
+struct PointView {
+  const double *x, *y, *nx, *ny, *w, *kap, *bval, *cval;
+};
+
+inline PointView view(const PointTable& t) {
+  return PointView{t.x.p, t.y.p, t.nx.p, t.ny.p, t.w.p, t.kap.p, t.bval.p, t.cval.p};
+}
+
+// modulation f(p) = 1 + alpha*exp(-isig*|p-p0|^2) evaluated on the host
+double modulation(double alpha, double x0, double y0, double isig, double px, double py);
+
+template <typename R>
+void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const PointView& pts,
+                  const KernelDev& k, cudaStream_t s);
+
+}  // namespace hss

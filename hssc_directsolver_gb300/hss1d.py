@@ -1,0 +1,112 @@
+"""HSS1D host interface mirroring the reference's MATLAB entry points.
+
+    K_HSS          = HSS1D_compress_nsym('green', X, TREE, acc, knl_params)
+    [HSSinv,FTinv] = HSS1D_invert_nsym(K_HSS, acc)
+    uu             = HSS1D_apply_nsym(K_HSS, qq)
+    xx             = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff)
+
+(HSS1D/HSS1D_compress_nsym.m:1, HSS1D_invert_nsym.m:1, HSS1D_apply_nsym.m:1,
+HSS1D_applyinv_nsym.m:1).  All work runs in libhssgpu.so on the GPU; the
+returned K_HSS object owns the device factors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .kernels import Kernel
+
+
+class HSS1DMatrix:
+    """K_HSS: tree, skeletons, interpolation matrices and self/sibling blocks on the GPU."""
+
+    def __init__(self, handle: C.c_void_p, N: int):
+        self._h = handle
+        self.N = N
+        self.inverted = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                L.lib().hss1d_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # --- box_constants.m rows -------------------------------------------------
+    def info(self):
+        lib = L.lib()
+        nb = C.c_int32(0)
+        L.check(lib.hss1d_info(self._h, C.byref(nb), *([None] * 8)))
+        n = nb.value
+        arrs = {k: np.zeros(n, dtype=np.int32) for k in
+                ("level", "parent", "c1", "c2", "off", "cnt", "nskel", "kskel")}
+        p = lambda a: a.ctypes.data_as(L._I32P)
+        L.check(lib.hss1d_info(self._h, C.byref(nb), p(arrs["level"]), p(arrs["parent"]), p(arrs["c1"]),
+                               p(arrs["c2"]), p(arrs["off"]), p(arrs["cnt"]), p(arrs["nskel"]),
+                               p(arrs["kskel"])))
+        arrs["nboxes"] = n
+        return arrs
+
+    def export_box(self, box: int):
+        inf = self.info()
+        n, k = int(inf["nskel"][box]), int(inf["kskel"][box])
+        out = dict(I_SKUP=np.zeros(k, np.int32), I_SKDN=np.zeros(k, np.int32),
+                   J_UP=np.zeros(n, np.int32), J_DN=np.zeros(n, np.int32),
+                   T_UP=np.zeros((k, n - k), order="F"), T_DN=np.zeros((k, n - k), order="F"))
+        ip = lambda a: a.ctypes.data_as(L._I32P)
+        dp = lambda a: a.ctypes.data_as(L._DP)
+        L.check(L.lib().hss1d_export_box(self._h, box, ip(out["I_SKUP"]), ip(out["I_SKDN"]), ip(out["J_UP"]),
+                                         ip(out["J_DN"]), dp(out["T_UP"]), dp(out["T_DN"])))
+        return out
+
+
+def _as_f64(a):
+    a = np.asarray(a, dtype=np.float64)
+    return np.asfortranarray(a)
+
+
+def HSS1D_compress_nsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel, seed: int = 0) -> HSS1DMatrix:
+    if type_ != "green":
+        raise ValueError("only the 'green' construction is implemented on the GPU")
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim != 2 or X.shape[1] not in (2, 6):
+        raise ValueError("X must be N x 2 or N x 6 ([x y nx ny w kappa])")
+    if X.shape[1] == 2:
+        X6 = np.zeros((X.shape[0], 6))
+        X6[:, :2] = X
+        X = X6
+    Xf = np.asfortranarray(X)
+    h = C.c_void_p()
+    kp = knl_params.to_c()
+    L.check(L.lib().hss1d_compress(C.byref(h), L.ptr(Xf), Xf.shape[0], Xf.shape[0], int(TREE), float(acc),
+                                   C.byref(kp), int(seed)))
+    return HSS1DMatrix(h, Xf.shape[0])
+
+
+def HSS1D_invert_nsym(K_HSS: HSS1DMatrix, acc: float = 0.0):
+    """Returns (HSSinv, FTinv); both are views of the factors kept inside K_HSS."""
+    L.check(L.lib().hss1d_invert(K_HSS._h))
+    K_HSS.inverted = True
+    return K_HSS, K_HSS
+
+
+def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
+    q = _as_f64(qq)
+    vec = q.ndim == 1
+    q2 = q.reshape(K_HSS.N, -1, order="F")
+    out = np.zeros_like(q2, order="F")
+    L.check(L.lib().hss1d_apply(K_HSS._h, L.ptr(q2), L.ptr(out), q2.shape[1]))
+    return out[:, 0] if vec else out
+
+
+def HSS1D_applyinv_nsym(K_HSS: HSS1DMatrix, HSSinv, FTinv, ff) -> np.ndarray:
+    f = _as_f64(ff)
+    vec = f.ndim == 1
+    f2 = f.reshape(K_HSS.N, -1, order="F")
+    out = np.zeros_like(f2, order="F")
+    L.check(L.lib().hss1d_applyinv(K_HSS._h, L.ptr(f2), L.ptr(out), f2.shape[1]))
+    return out[:, 0] if vec else out

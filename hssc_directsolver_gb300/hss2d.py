@@ -1,0 +1,188 @@
+"""HSS2D host interface mirroring the reference's MATLAB entry points.
+
+    params    = HSS_tree_parameters(pot, kh, sym, Ng, np, acc, lay, n_cut, TI)
+    INFO_TREE = HSS2D_build_tree_nsym(params)
+    A_HSS     = HSS2D_compress_nsym(INFO_TREE, params)
+    A_HSS     = HSS2D_invert_nsym(INFO_TREE, params)          (params.Fopts = 'dense')
+    Y         = HSS2D_apply_nsym(INFO_TREE, A_HSS, X, params)
+    Y         = HSS2D_applyinv_nsym(INFO_TREE, A_HSS, X, params)
+    X, hist   = Iterative_Refinement(...)                      (hss2d_solve)
+
+(Common/HSS_tree_parameters.m:1, HSS2D/HSS2D_build_tree_nsym.m:1,
+HSS2D_compress_nsym.m:1, HSS2D_invert_nsym.m:1, HSS2D_apply_nsym.m:1,
+HSS2D_applyinv_nsym.m:1, Common/Iterative_Refinement.m:1).  Every stage runs
+in libhssgpu.so on the GPU; INFO_TREE owns the device state.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .kernels import Kernel, Modulation, reference_modulations
+
+
+@dataclass
+class HSS2DParams:
+    """The params struct of Common/HSS_tree_parameters.m:115-139 (dense path fields)."""
+
+    Ng: int
+    npan: int
+    acc: float = 1e-10
+    layers: int = 2
+    kernel: Kernel = field(default_factory=Kernel)
+    INTERform: str = "dense"
+    transinv: int = 0
+    sym: int = 0
+    precision: str = "fp64"   # "fp64" or "mixed"
+    n_cut: int = 400
+    Fopts: str = "dense"
+
+    @property
+    def h(self) -> float:
+        return 2.0 / (self.Ng * self.npan)
+
+    @property
+    def depth(self) -> int:
+        return int(round(2 * (math.log(self.npan) / math.log(2) - 1) + 3)) - 1
+
+    @property
+    def N(self) -> int:
+        return self.npan * self.npan * self.Ng * self.Ng
+
+    def to_c(self) -> L.hss2d_params:
+        if self.INTERform != "dense":
+            raise ValueError("INTERform 'dense' is the implemented interpolation storage")
+        if self.Fopts != "dense":
+            raise ValueError("Fopts 'dense' (HSS-D) is the implemented inverse storage")
+        prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED}[self.precision]
+        k = self.kernel
+        k.h = self.h
+        return L.hss2d_params(self.Ng, self.npan, self.layers, L.HSS_INTER_DENSE, self.transinv, self.sym, prec, 0,
+                              float(self.acc), k.to_c())
+
+
+def HSS_tree_parameters(pot: str, kh: float, sym: int, Ng: int, npan: int, acc: float, lay: int, n_cut: int,
+                        TI: int, proxy: int = 0) -> HSS2DParams:
+    """Common/HSS_tree_parameters.m:108-139 for the Laplace kernel (kh = 0)."""
+    if kh != 0:
+        raise ValueError("the oscillatory kernels are not part of the GPU path")
+    b, c = reference_modulations(sym, proxy, TI)
+    return HSS2DParams(Ng=Ng, npan=npan, acc=acc, layers=lay, kernel=Kernel(pot, 2.0 / (Ng * npan), b, c),
+                       transinv=TI, sym=sym, n_cut=n_cut)
+
+
+class InfoTree:
+    """INFO_TREE (and the A_HSS factors once compressed / inverted) on the GPU."""
+
+    def __init__(self, params: HSS2DParams):
+        self.params = params
+        self._h = C.c_void_p()
+        self._cp = params.to_c()
+        L.check(L.lib().hss2d_build_tree(C.byref(self._h), C.byref(self._cp)))
+        d, nb, n = C.c_int32(), C.c_int32(), C.c_int64()
+        L.check(L.lib().hss2d_info(self._h, C.byref(d), C.byref(nb), C.byref(n)))
+        self.depth, self.nboxes, self.N = d.value, nb.value, n.value
+        self.compressed = False
+        self.inverted = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                L.lib().hss2d_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def box_sizes(self):
+        n = np.zeros(self.nboxes, np.int32)
+        k = np.zeros(self.nboxes, np.int32)
+        p = np.zeros(self.nboxes, np.int32)
+        ip = lambda a: a.ctypes.data_as(L._I32P)
+        L.check(L.lib().hss2d_box_sizes(self._h, ip(n), ip(k), ip(p)))
+        return n, k, p
+
+    def export_box(self, box: int):
+        n, k, _ = self.box_sizes()
+        nb, kb = int(n[box]), int(k[box])
+        out = dict(I_src=np.zeros(nb, np.int32), J=np.zeros(nb, np.int32),
+                   T_up=np.zeros((kb, nb - kb), order="F"), T_dn=np.zeros((kb, nb - kb), order="F"))
+        ip = lambda a: a.ctypes.data_as(L._I32P)
+        dp = lambda a: a.ctypes.data_as(L._DP)
+        L.check(L.lib().hss2d_export_box(self._h, box, ip(out["I_src"]), ip(out["J"]), dp(out["T_up"]),
+                                         dp(out["T_dn"])))
+        return out
+
+    def export_inverse(self, box: int):
+        n, k, _ = self.box_sizes()
+        nb, kb = int(n[box]), int(k[box])
+        FI = np.zeros((nb, nb), order="F")
+        E = np.zeros((kb, kb), order="F")
+        L.check(L.lib().hss2d_export_inverse(self._h, box, FI.ctypes.data_as(L._DP), E.ctypes.data_as(L._DP)))
+        return FI, E
+
+    def solve_bytes(self) -> int:
+        b = C.c_int64()
+        L.check(L.lib().hss2d_solve_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def solve_launches(self, nrhs: int) -> int:
+        n = C.c_int32()
+        L.check(L.lib().hss2d_solve_launches(self._h, nrhs, C.byref(n)))
+        return n.value
+
+
+def HSS2D_build_tree_nsym(params: HSS2DParams) -> InfoTree:
+    return InfoTree(params)
+
+
+def HSS2D_compress_nsym(INFO_TREE: InfoTree, params: HSS2DParams | None = None) -> InfoTree:
+    L.check(L.lib().hss2d_compress(INFO_TREE._h))
+    INFO_TREE.compressed = True
+    return INFO_TREE
+
+
+def HSS2D_invert_nsym(INFO_TREE: InfoTree, params: HSS2DParams | None = None) -> InfoTree:
+    if not INFO_TREE.compressed:
+        HSS2D_compress_nsym(INFO_TREE, params)
+    L.check(L.lib().hss2d_invert(INFO_TREE._h))
+    INFO_TREE.inverted = True
+    return INFO_TREE
+
+
+def _vec(INFO_TREE, X):
+    X = np.asfortranarray(np.asarray(X, dtype=np.float64))
+    vec = X.ndim == 1
+    X2 = X.reshape(INFO_TREE.N, -1, order="F")
+    return X2, vec
+
+
+def HSS2D_apply_nsym(INFO_TREE: InfoTree, A_HSS, X, params=None) -> np.ndarray:
+    X2, vec = _vec(INFO_TREE, X)
+    Y = np.zeros_like(X2, order="F")
+    L.check(L.lib().hss2d_apply(INFO_TREE._h, L.ptr(X2), L.ptr(Y), X2.shape[1]))
+    return Y[:, 0] if vec else Y
+
+
+def HSS2D_applyinv_nsym(INFO_TREE: InfoTree, A_HSS, X, params=None) -> np.ndarray:
+    X2, vec = _vec(INFO_TREE, X)
+    Y = np.zeros_like(X2, order="F")
+    L.check(L.lib().hss2d_applyinv(INFO_TREE._h, L.ptr(X2), L.ptr(Y), X2.shape[1]))
+    return Y[:, 0] if vec else Y
+
+
+def HSS2D_solve(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 5):
+    """x = A^-1 f with iterative refinement (Common/Iterative_Refinement.m:20-35).
+
+    Returns (x, relres, solves used)."""
+    F2, vec = _vec(INFO_TREE, F)
+    Xs = np.zeros_like(F2, order="F")
+    rr = C.c_double()
+    it = C.c_int32()
+    L.check(L.lib().hss2d_solve(INFO_TREE._h, L.ptr(F2), L.ptr(Xs), F2.shape[1], tol, maxit, C.byref(rr),
+                                C.byref(it)))
+    return (Xs[:, 0] if vec else Xs), rr.value, it.value

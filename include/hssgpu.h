@@ -1,0 +1,173 @@
+/*
+ * hssgpu.h -- C ABI of the GB300 HSS direct-solver library (libhssgpu.so).
+ *
+ * Drop-in boundary for the MATLAB-level entry points of
+ * EduardoCorona84/HSSC_DirectSolver.  Each function below names the reference
+ * function it replaces (file:line of the reference project).  Conventions:
+ *
+ *  - Every entry point returns an int status (HSS_OK = 0); the reference
+ *    raises MATLAB errors instead.  hss_last_error() gives a message.
+ *  - Dense arrays are column-major (MATLAB layout).  Index arrays exported by
+ *    this library are 0-based; the MEX shim adds 1.
+ *  - Handles own their device memory and one CUDA stream; a handle is not
+ *    thread-safe, distinct handles are.
+ *  - Host-pointer calls copy inputs to the device and results back; the
+ *    *_device variants take device pointers and a cudaStream_t (as void*).
+ *  - Plain types only: no C++ or torch types cross this boundary.
+ */
+#ifndef HSSGPU_H
+#define HSSGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define HSS_OK 0
+#define HSS_ERR_ARG 1       /* invalid argument / size */
+#define HSS_ERR_CUDA 2      /* CUDA runtime failure or no device */
+#define HSS_ERR_SINGULAR 3  /* exact zero pivot in a block inversion */
+#define HSS_ERR_NONFINITE 4 /* NaN/Inf met in inputs or factors */
+#define HSS_ERR_RANK 5      /* rank / buffer capacity exceeded */
+#define HSS_ERR_STATE 6     /* call out of order (e.g. applyinv before invert) */
+#define HSS_ERR_NOMEM 7     /* device allocation failed */
+
+/* ---- kernels (Common/Kernel_Eval.m) ------------------------------------ */
+#define HSS_SL_L_2D 0 /* Kernel_Eval.m:60-61, (den==0) + h^2/2 b(x) log(den) c(y) */
+#define HSS_DL_L_2D 1 /* custom-kernel slot Kernel_Eval.m:75-79: Laplace double layer */
+
+/* precision modes */
+#define HSS_PREC_FP64 0  /* plain FP64 everywhere */
+#define HSS_PREC_MIXED 1 /* FP32 inverse factors, FP64 forward operator + refinement */
+
+/* HSS2D interpolation-operator storage (params.INTERform) */
+#define HSS_INTER_DENSE 0
+
+/* b(x) = 1 + b_alpha*exp(-b_isig*|x-(b_x0,b_y0)|^2), c(y) likewise; alpha = 0
+ * switches a modulation off (LOCAL_get_bc, Kernel_Eval.m:98-159). */
+typedef struct hss_kernel_params {
+  int32_t flag;
+  int32_t pad_;
+  double h;
+  double b_alpha, b_x0, b_y0, b_isig;
+  double c_alpha, c_x0, c_y0, c_isig;
+} hss_kernel_params;
+
+const char* hss_last_error(void);
+int hss_version(void);
+/* number of CUDA devices visible (0 on a machine without GPU) */
+int hss_device_count(int* count);
+
+/* ---- HSS1D (curves) ---------------------------------------------------- */
+typedef struct hss1d_matrix hss1d_matrix;
+
+/* K_HSS = HSS1D_compress_nsym('green', X, TREE, acc, knl_params)
+ *   HSS1D/HSS1D_compress_nsym.m:1 (tree :277-334, skeletons :84-216,
+ *   self/sibling blocks :220-271).
+ * X: N x 6 column-major [x y nx ny w kappa] (ldx >= N); leaf = nbox_max.
+ * seed: key of the counter RNG drawing the rank-check vectors (ID.m:68-86). */
+int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
+                   double acc, const hss_kernel_params* kp, uint64_t seed);
+/* tree and skeleton sizes: arrays of nboxes entries (any may be NULL) */
+int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* parent,
+               int32_t* c1, int32_t* c2, int32_t* off, int32_t* cnt, int32_t* nskel,
+               int32_t* kskel);
+/* K_HSS{I_SKUP,I_SKDN,J_UP,J_DN,T_UP,T_DN} of one box (box_constants.m:33-52);
+ * T_* are k x (n-k) column-major; any pointer may be NULL. */
+int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_t* I_skdn,
+                     int32_t* J_up, int32_t* J_dn, double* T_up, double* T_dn);
+/* [HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D/HSS1D_invert_nsym.m:44-91 */
+int hss1d_invert(hss1d_matrix* H);
+/* uu = HSS1D_apply_nsym(K_HSS, qq), HSS1D/HSS1D_apply_nsym.m:38-100 */
+int hss1d_apply(hss1d_matrix* H, const double* qq, double* uu, int32_t nrhs);
+/* xx = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff), HSS1D/HSS1D_applyinv_nsym.m:43-86 */
+int hss1d_applyinv(hss1d_matrix* H, const double* ff, double* xx, int32_t nrhs);
+int hss1d_applyinv_device(hss1d_matrix* H, const double* d_ff, double* d_xx, int32_t nrhs,
+                          void* stream);
+int hss1d_destroy(hss1d_matrix* H);
+
+/* ---- HSS2D (planar volumes) -------------------------------------------- */
+typedef struct hss2d_matrix hss2d_matrix;
+
+/* the params fields of Common/HSS_tree_parameters.m:108-139 the dense path uses */
+typedef struct hss2d_params {
+  int32_t Ng;        /* points per panel side */
+  int32_t npan;      /* panels per domain side (power of two) */
+  int32_t layers;    /* boundary layers of the preset skeletons */
+  int32_t interform; /* HSS_INTER_DENSE */
+  int32_t transinv;  /* 0: NTI (per-box operators) */
+  int32_t sym;       /* 0: nsym */
+  int32_t precision; /* HSS_PREC_FP64 or HSS_PREC_MIXED */
+  int32_t pad_;
+  double acc;
+  hss_kernel_params kp;
+} hss2d_params;
+
+/* INFO_TREE = HSS2D_build_tree_nsym(params), HSS2D/HSS2D_build_tree_nsym.m:80-610
+ * ('uniform' tree, 'bdry' preset skeletons, 'bdry' proxies, dense T). */
+int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p);
+/* A_HSS = HSS2D_compress_nsym(INFO_TREE, params) dense blocks, HSS2D/HSS2D_compress_nsym.m:67-125 */
+int hss2d_compress(hss2d_matrix* H);
+/* A_HSS = HSS2D_invert_nsym(INFO_TREE, params), Fopts = 'dense',
+ * HSS2D/HSS2D_invert_nsym.m:70-155 with HSS2D_build_Finv_nsym.m:92-100 and
+ * HSS2D_build_E_nsym.m:43-51 */
+int hss2d_invert(hss2d_matrix* H);
+/* Y = HSS2D_apply_nsym(INFO_TREE, A_HSS, X, params), HSS2D/HSS2D_apply_nsym.m:74-218 */
+int hss2d_apply(hss2d_matrix* H, const double* X, double* Y, int32_t nrhs);
+int hss2d_apply_device(hss2d_matrix* H, const double* d_X, double* d_Y, int32_t nrhs, void* stream);
+/* Y = HSS2D_applyinv_nsym(INFO_TREE, A_HSS, X, params), HSS2D/HSS2D_applyinv_nsym.m:74-243 */
+int hss2d_applyinv(hss2d_matrix* H, const double* X, double* Y, int32_t nrhs);
+int hss2d_applyinv_device(hss2d_matrix* H, const double* d_X, double* d_Y, int32_t nrhs,
+                          void* stream);
+/* solve with iterative refinement (Common/Iterative_Refinement.m:20-35): x = A^-1 f,
+ * then x += A^-1 (f - A x) until max_col ||f - A x||/||f|| <= tol or maxit solves.
+ * A is the FP64 forward HSS operator, as the reference test uses it
+ * (HSS2D/Test/Test_HSS2D_InverseCompression.m:281-298).  relres (may be NULL)
+ * receives the final max column relative residual, iters the solves used. */
+int hss2d_solve(hss2d_matrix* H, const double* f, double* x, int32_t nrhs, double tol,
+                int32_t maxit, double* relres, int32_t* iters);
+int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
+                       int32_t maxit, double* relres, int32_t* iters, void* stream);
+/* tree sizes: depth, box count, N */
+int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N);
+/* per-box sizes: n (|I_src|), k (|I_sk|), proxy count; arrays of nboxes (NULL ok) */
+int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* nproxy);
+/* INFO_TREE.BOX(b).{I_src, J, T_up, T_dn} (T_* k x (n-k) column-major); NULL ok */
+int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t* J,
+                     double* T_up, double* T_dn);
+/* A_HSS(b).FI (n x n) and .E (k x k), FP64 copies; NULL ok */
+int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double* E);
+/* bytes of factor storage read by one inverse apply (roofline accounting) */
+int hss2d_solve_bytes(const hss2d_matrix* H, int64_t* bytes);
+/* launches issued by one applyinv of nrhs columns (counted by the host) */
+int hss2d_solve_launches(const hss2d_matrix* H, int32_t nrhs, int32_t* launches);
+int hss2d_destroy(hss2d_matrix* H);
+
+/* ---- batched dense primitives (exposed for parity tests and benches) ---- */
+/* In-place inversion of `batch` n x n column-major matrices stored back to back
+ * (device pointer), blocked Gauss-Jordan with partial pivoting; info[b] = 0 ok. */
+int hss_batched_inverse_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info,
+                               void* stream);
+int hss_batched_inverse_device_f32(float* d_A, int32_t n, int32_t batch, int32_t* d_info,
+                                   void* stream);
+/* Least squares X_b = A_b(:,0:kf) \ A_b(:,kf:n) for `batch` m x n blocks back to
+ * back (device); X overwrites A_b(0:kf, kf:n). */
+int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch,
+                             void* stream);
+/* Interpolative decomposition of `batch` m x n blocks (device, back to back):
+ * rank[b], perm[b*n..], T[b*n*n..] (k x (n-k), ld n).  force_k < 0: adaptive
+ * (ID.m:40-65), else fixed rank (ID.m:106-113). */
+int hss_batched_id_device(const double* d_A, int32_t m, int32_t n, int32_t batch, double acc,
+                          uint64_t seed, int32_t force_k, int32_t* d_rank, int32_t* d_perm,
+                          double* d_T, void* stream);
+/* C = A*B for `batch` column-major blocks back to back (device), FP64. */
+int hss_batched_gemm_device(const double* d_A, const double* d_B, double* d_C, int32_t M,
+                            int32_t N, int32_t K, int32_t batch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HSSGPU_H */

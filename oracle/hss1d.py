@@ -1,0 +1,493 @@
+"""HSS1D compress / invert / apply / applyinv / transforminv (oracle restatement).
+
+Follows, function by function:
+  HSS1D/HSS1D_compress_nsym.m   (compress, 'green' and 'brute'; tree :277-334,
+                                  circle :339-371, neighbour list :376-412)
+  HSS1D/HSS1D_invert_nsym.m     (:44-91)
+  HSS1D/HSS1D_apply_nsym.m      (:38-130)
+  HSS1D/HSS1D_applyinv_nsym.m   (:43-86)
+  HSS1D/HSS1D_transforminv_nsym.m (:38-161)
+
+The cell array ``K_HSS{row, ibox}`` of Common/box_constants.m:33-52 becomes an
+``HSS1DMatrix`` whose per-box lists are indexed by the 0-based box id (box 0 is
+the reference's box 1, the root).  Index arrays are 0-based here.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from .kernels import KernelParams, kernel_eval, DL_L_2D, SL_L_2D
+from . import idecomp
+
+RADIUS_REL = 1.75   # HSS1D_compress_nsym.m:51
+NPROXY = 50         # HSS1D_compress_nsym.m:52
+
+
+@dataclass
+class HSS1DTree:
+    level: np.ndarray
+    parent: np.ndarray
+    c1: np.ndarray
+    c2: np.ndarray
+    off: np.ndarray   # 0-based first point (END1 - 1)
+    cnt: np.ndarray   # number of points (END2)
+
+    @property
+    def nboxes(self):
+        return len(self.level)
+
+    def is_leaf(self, b):
+        return self.c1[b] < 0 and self.c2[b] < 0
+
+
+def get_tree(ntot: int, nbox_max: int) -> HSS1DTree:
+    """LOCAL_get_tree, HSS1D_compress_nsym.m:277-334 (BFS halving, son1 = ceil(n/2))."""
+    level = [0]
+    parent = [-1]
+    c1 = [-1]
+    c2 = [-1]
+    off = [0]
+    cnt = [ntot]
+    ibox_last = -1
+    ncreated = 1
+    ilevel = 0
+    while ncreated > 0:
+        ibox_first = ibox_last + 1
+        ibox_last = ibox_last + ncreated
+        ncreated = 0
+        for ibox in range(ibox_first, ibox_last + 1):
+            nbox = cnt[ibox]
+            if nbox > nbox_max:
+                nhalf = (nbox + 1) // 2
+                s1 = ibox_last + ncreated + 1
+                s2 = s1 + 1
+                c1[ibox] = s1
+                c2[ibox] = s2
+                for s, o, c in ((s1, off[ibox], nhalf), (s2, off[ibox] + nhalf, nbox - nhalf)):
+                    assert len(level) == s
+                    level.append(ilevel + 1)
+                    parent.append(ibox)
+                    c1.append(-1)
+                    c2.append(-1)
+                    off.append(o)
+                    cnt.append(c)
+                ncreated += 2
+        ilevel += 1
+    a = lambda v: np.asarray(v, dtype=np.int64)
+    return HSS1DTree(a(level), a(parent), a(c1), a(c2), a(off), a(cnt))
+
+
+def circum_circle(X: np.ndarray):
+    """LOCAL_get_circum_circle, HSS1D_compress_nsym.m:339-356."""
+    nloc = X.shape[0]
+    xxc = 0.5 * (X[0, :2] + X[-1, :2])
+    d = (X[:, 0] - xxc[0]) ** 2 + (X[:, 1] - xxc[1]) ** 2
+    R = math.sqrt(np.max(d))
+    e = (X[0, 0] - X[-1, 0]) ** 2 + (X[0, 1] - X[-1, 1]) ** 2
+    if (1.2 * R * R) > e:
+        sx = sy = 0.0
+        for a, b in zip(X[:, 0].tolist(), X[:, 1].tolist()):   # sequential sums
+            sx += a
+            sy += b
+        xxc = np.array([sx, sy]) * (1.0 / nloc)
+        d = (X[:, 0] - xxc[0]) ** 2 + (X[:, 1] - xxc[1]) ** 2
+        R = math.sqrt(np.max(d))
+    return xxc, R
+
+
+def proxy_circle(xxc, R, n):
+    """LOCAL_construct_circle (HSS1D_compress_nsym.m:361-371) as (n,6) points.
+
+    The normal (cos t, sin t) and weight 2 pi R / n are what the double-layer
+    kernel uses for proxy sources; curvature 1/R.
+    """
+    tt = np.linspace(0.0, 2.0 * math.pi * (1.0 - 1.0 / n), n)
+    P = np.zeros((n, 6))
+    c = np.array([math.cos(t) for t in tt.tolist()])   # libm, as the host C++ does
+    s = np.array([math.sin(t) for t in tt.tolist()])
+    P[:, 0] = xxc[0] + R * c
+    P[:, 1] = xxc[1] + R * s
+    P[:, 2] = c
+    P[:, 3] = s
+    P[:, 4] = 2.0 * math.pi * R / n
+    P[:, 5] = 1.0 / R
+    return P
+
+
+def neighbor_list(X: np.ndarray, tree: HSS1DTree, radius_rel=RADIUS_REL):
+    """LOCAL_construct_potential_neighborlist, HSS1D_compress_nsym.m:376-412."""
+    nb = tree.nboxes
+    nei = [[] for _ in range(nb)]
+    nei[0] = [0]
+    for ibox in range(1, nb):
+        o, c = tree.off[ibox], tree.cnt[ibox]
+        xxc, R = circum_circle(X[o:o + c])
+        pot = []
+        for jbox in nei[tree.parent[ibox]]:
+            if tree.c1[jbox] >= 0:
+                pot.append(int(tree.c1[jbox]))
+            if tree.c2[jbox] >= 0:
+                pot.append(int(tree.c2[jbox]))
+        rr = radius_rel * radius_rel * R * R
+        for jbox in pot:
+            oj, cj = tree.off[jbox], tree.cnt[jbox]
+            d = (X[oj:oj + cj, 0] - xxc[0]) ** 2 + (X[oj:oj + cj, 1] - xxc[1]) ** 2
+            if np.min(d) < rr:
+                nei[ibox].append(jbox)
+    for ibox in range(1, nb):
+        lst = list(nei[ibox])
+        if ibox in lst:
+            lst.remove(ibox)
+        nei[ibox] = sorted(lst)
+    return nei
+
+
+@dataclass
+class HSS1DMatrix:
+    tree: HSS1DTree
+    nskel: list = field(default_factory=list)
+    kskel: list = field(default_factory=list)
+    I_SKUP: list = field(default_factory=list)
+    I_SKDN: list = field(default_factory=list)
+    T_UP: list = field(default_factory=list)
+    J_UP: list = field(default_factory=list)
+    T_DN: list = field(default_factory=list)
+    J_DN: list = field(default_factory=list)
+    M_SELF: list = field(default_factory=list)
+    M_SIB: list = field(default_factory=list)
+    # diagnostics: per-box ID problem shapes (m_out, m_in, n, k)
+    census: list = field(default_factory=list)
+
+
+def _leaf_range(tree, b):
+    return np.arange(tree.off[b], tree.off[b] + tree.cnt[b])
+
+
+def _box_skel_sets(H, b):
+    """indskel_out / indskel_in of HSS1D_compress_nsym.m:87-100."""
+    t = H.tree
+    if t.is_leaf(b):
+        ind = _leaf_range(t, b)
+        return ind, ind
+    if t.c1[b] >= 0 and t.c2[b] >= 0:
+        s1, s2 = t.c1[b], t.c2[b]
+        return (np.concatenate([H.I_SKUP[s1], H.I_SKUP[s2]]),
+                np.concatenate([H.I_SKDN[s1], H.I_SKDN[s2]]))
+    s = max(t.c1[b], t.c2[b])
+    return H.I_SKUP[s], H.I_SKDN[s]
+
+
+def compress_green_blocks(H, X, ibox, nei, kp: KernelParams, ntot):
+    """A_out and A_in of HSS1D_compress_nsym.m:106-156 (the 'green' trick)."""
+    t = H.tree
+    out, inn = _box_skel_sets(H, ibox)
+    both = np.sort(np.concatenate([out, inn]), kind="stable")
+    xxc, R = circum_circle(X[both])
+    nproxy = NPROXY
+    Cp = proxy_circle(xxc, RADIUS_REL * R, nproxy)
+    out_maybe, in_maybe = [], []
+    for j in nei[ibox]:
+        if t.is_leaf(j):
+            r = _leaf_range(t, j)
+            out_maybe.append(r)
+            in_maybe.append(r)
+        elif t.c1[j] >= 0 and t.c2[j] >= 0:
+            out_maybe += [H.I_SKUP[t.c1[j]], H.I_SKUP[t.c2[j]]]
+            in_maybe += [H.I_SKDN[t.c1[j]], H.I_SKDN[t.c2[j]]]
+        else:
+            s = max(t.c1[j], t.c2[j])
+            out_maybe.append(H.I_SKUP[s])
+            in_maybe.append(H.I_SKDN[s])
+    cat = lambda L: np.concatenate(L) if L else np.zeros(0, dtype=np.int64)
+    out_maybe = cat(out_maybe)
+    in_maybe = cat(in_maybe)
+    rr = (RADIUS_REL * R) ** 2
+    d = (X[out_maybe, 0] - xxc[0]) ** 2 + (X[out_maybe, 1] - xxc[1]) ** 2
+    out_inside = out_maybe[d < rr]
+    d = (X[in_maybe, 0] - xxc[0]) ** 2 + (X[in_maybe, 1] - xxc[1]) ** 2
+    in_inside = in_maybe[d < rr]
+    A_out = np.vstack([kernel_eval(X[in_inside], X[out], kp), kernel_eval(Cp, X[out], kp)])
+    A_in = np.hstack([kernel_eval(X[inn], X[out_inside], kp), kernel_eval(X[inn], Cp, kp)])
+    return out, inn, A_out, A_in
+
+
+def compress_nsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: int = 0,
+                  tree: HSS1DTree | None = None) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compress_nsym('green', X, TREE, acc, knl_params).
+
+    ID problem numbering for the shared RNG: box b's outgoing ID is problem
+    2*b, its incoming ID 2*b+1.
+    """
+    X = np.asarray(X, dtype=np.float64)
+    ntot = X.shape[0]
+    t = tree if tree is not None else get_tree(ntot, leaf)
+    nb = t.nboxes
+    H = HSS1DMatrix(t)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census"):
+        setattr(H, name, [None] * nb)
+    nei = neighbor_list(X, t)
+    for ibox in range(nb - 1, 0, -1):
+        out, inn, A_out, A_in = compress_green_blocks(H, X, ibox, nei, kp, ntot)
+        Tout, Jout, kout, Rout = idecomp.id_adaptive(A_out, acc, seed, 2 * ibox)
+        Tin, Jin, kin, Rin = idecomp.id_adaptive(A_in.T, acc, seed, 2 * ibox + 1)
+        k = max(kout, kin)
+        if k != kout:
+            Tout = idecomp.id_fixed_from_qr(Rout, Jout, k)
+        elif k != kin:
+            Tin = idecomp.id_fixed_from_qr(Rin, Jin, k)
+        H.I_SKUP[ibox] = out[Jout[:k]]
+        H.T_UP[ibox] = Tout
+        H.J_UP[ibox] = Jout
+        H.I_SKDN[ibox] = inn[Jin[:k]]
+        H.T_DN[ibox] = Tin
+        H.J_DN[ibox] = Jin
+        H.nskel[ibox] = len(out)
+        H.kskel[ibox] = k
+        H.census[ibox] = (A_out.shape[0], A_in.shape[1], len(out), k, kout, kin)
+    for ibox in range(nb - 1, -1, -1):
+        if t.is_leaf(ibox):
+            ind = _leaf_range(t, ibox)
+            H.M_SELF[ibox] = kernel_eval(X[ind], X[ind], kp)
+        elif t.c1[ibox] >= 0 and t.c2[ibox] >= 0:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            H.M_SIB[s1] = kernel_eval(X[H.I_SKDN[s1]], X[H.I_SKUP[s2]], kp)
+            H.M_SIB[s2] = kernel_eval(X[H.I_SKDN[s2]], X[H.I_SKUP[s1]], kp)
+    return H
+
+
+def _RL(H, b):
+    """R (k x n) and L (n x k) of HSS1D_invert_nsym.m:63-72."""
+    n, k = H.nskel[b], H.kskel[b]
+    R = np.zeros((k, n))
+    R[:, H.J_UP[b][:k]] = np.eye(k)
+    R[:, H.J_UP[b][k:]] = H.T_UP[b]
+    L = np.zeros((n, k))
+    L[H.J_DN[b][:k], :] = np.eye(k)
+    L[H.J_DN[b][k:], :] = H.T_DN[b].T
+    return R, L
+
+
+def invert_nsym(H: HSS1DMatrix):
+    """[HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D_invert_nsym.m:44-91.
+
+    Returns dict with lists Linv, Rinv, Dinv (index = box) and FTinv.
+    """
+    t = H.tree
+    nb = t.nboxes
+    E = [None] * nb
+    Linv = [None] * nb
+    Rinv = [None] * nb
+    Dinv = [None] * nb
+    for b in range(nb - 1, 0, -1):
+        F = _diag_block(H, E, b)
+        R, L = _RL(H, b)
+        Finv = np.linalg.inv(F)
+        Eb = np.linalg.inv(R @ Finv @ L)
+        E[b] = Eb
+        Linv[b] = Finv @ L @ Eb
+        Rinv[b] = Eb @ R @ Finv
+        Dinv[b] = Finv - Linv[b] @ (R @ Finv)
+    FT = np.block([[E[1], H.M_SIB[1]], [H.M_SIB[2], E[2]]])
+    return {"Linv": Linv, "Rinv": Rinv, "Dinv": Dinv, "FTinv": np.linalg.inv(FT), "E": E}
+
+
+def _diag_block(H, E, b):
+    t = H.tree
+    if t.is_leaf(b):
+        return H.M_SELF[b]
+    if t.c1[b] >= 0 and t.c2[b] >= 0:
+        s1, s2 = t.c1[b], t.c2[b]
+        return np.block([[E[s1], H.M_SIB[s1]], [H.M_SIB[s2], E[s2]]])
+    return E[max(t.c1[b], t.c2[b])]
+
+
+def _skel_proj(T, J, q):
+    """LOCAL_skel_proj, HSS1D_apply_nsym.m:108-115."""
+    if T.shape[1] == 0:
+        return q[J]
+    k = T.shape[0]
+    return q[J[:k]] + T @ q[J[k:]]
+
+
+def _skel_eval(T, J, u):
+    """LOCAL_skel_eval, HSS1D_apply_nsym.m:121-130."""
+    out = np.zeros((len(J), u.shape[1]))
+    if T.shape[1] == 0:
+        out[J] = u
+    else:
+        k = T.shape[0]
+        out[J[:k]] = u
+        out[J[k:]] = T.T @ u
+    return out
+
+
+def apply_nsym(H: HSS1DMatrix, qq: np.ndarray) -> np.ndarray:
+    """uu = HSS1D_apply_nsym(K_HSS, qq), HSS1D_apply_nsym.m:38-100."""
+    t = H.tree
+    nb = t.nboxes
+    qq = np.asarray(qq, dtype=np.float64)
+    vec = qq.ndim == 1
+    if vec:
+        qq = qq[:, None]
+    up = [None] * nb
+    dn = [None] * nb
+    for b in range(nb - 1, 0, -1):
+        if t.is_leaf(b):
+            up[b] = _skel_proj(H.T_UP[b], H.J_UP[b], qq[_leaf_range(t, b)])
+    for b in range(nb - 1, 0, -1):
+        if not t.is_leaf(b):
+            parts = [up[s] for s in (t.c1[b], t.c2[b]) if s >= 0]
+            up[b] = _skel_proj(H.T_UP[b], H.J_UP[b], np.vstack(parts))
+    dn[1] = H.M_SIB[1] @ up[2]
+    dn[2] = H.M_SIB[2] @ up[1]
+    for b in range(1, nb):
+        if not t.is_leaf(b):
+            s1, s2 = t.c1[b], t.c2[b]
+            if s1 >= 0 and s2 >= 0:
+                n1 = len(H.I_SKDN[s1])
+                u = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b])
+                dn[s1] = u[:n1] + H.M_SIB[s1] @ up[s2]
+                dn[s2] = u[n1:] + H.M_SIB[s2] @ up[s1]
+            else:
+                dn[max(s1, s2)] = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b])
+    uu = np.zeros_like(qq)
+    for b in range(nb - 1, 0, -1):
+        if t.is_leaf(b):
+            ind = _leaf_range(t, b)
+            uu[ind] = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b]) + H.M_SELF[b] @ qq[ind]
+    return uu[:, 0] if vec else uu
+
+
+def applyinv_nsym(H: HSS1DMatrix, inv: dict, ff: np.ndarray) -> np.ndarray:
+    """xx = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff), HSS1D_applyinv_nsym.m:43-86."""
+    t = H.tree
+    nb = t.nboxes
+    ff = np.asarray(ff, dtype=np.float64)
+    vec = ff.ndim == 1
+    if vec:
+        ff = ff[:, None]
+    f1 = [None] * nb
+    f2 = [None] * nb
+    for b in range(nb - 1, 0, -1):
+        if t.is_leaf(b):
+            f1[b] = inv["Rinv"][b] @ ff[_leaf_range(t, b)]
+        else:
+            parts = [f1[s] for s in (t.c1[b], t.c2[b]) if s >= 0]
+            f1[b] = inv["Rinv"][b] @ np.vstack(parts)
+    x_top = inv["FTinv"] @ np.vstack([f1[1], f1[2]])
+    k2 = inv["Linv"][1].shape[1]
+    f2[1] = x_top[:k2]
+    f2[2] = x_top[k2:]
+    xx = np.zeros_like(ff)
+    for b in range(1, nb):
+        if t.is_leaf(b):
+            ind = _leaf_range(t, b)
+            xx[ind] = inv["Linv"][b] @ f2[b] + inv["Dinv"][b] @ ff[ind]
+        else:
+            s1, s2 = t.c1[b], t.c2[b]
+            if s1 >= 0 and s2 >= 0:
+                k1 = H.kskel[s1]
+                xl = inv["Linv"][b] @ f2[b] + inv["Dinv"][b] @ np.vstack([f1[s1], f1[s2]])
+                f2[s1] = xl[:k1]
+                f2[s2] = xl[k1:]
+            else:
+                s = max(s1, s2)
+                f2[s] = inv["Linv"][b] @ f2[b] + inv["Dinv"][b] @ f1[s]
+    return xx[:, 0] if vec else xx
+
+
+def transforminv_nsym(H: HSS1DMatrix, inv: dict) -> HSS1DMatrix:
+    """Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv), :38-161."""
+    t = H.tree
+    nb = t.nboxes
+    Lv = [None if x is None else x.copy() for x in inv["Linv"]]
+    Rv = [None if x is None else x.copy() for x in inv["Rinv"]]
+    Dv = [None if x is None else x.copy() for x in inv["Dinv"]]
+    FT = inv["FTinv"].copy()
+    k1, k2 = H.kskel[1], H.kskel[2]
+    i1 = slice(0, k1)
+    i2 = slice(k1, k1 + k2)
+    Dv[1] = Dv[1] + Lv[1] @ FT[i1, i1] @ Rv[1]
+    Dv[2] = Dv[2] + Lv[2] @ FT[i2, i2] @ Rv[2]
+    FT[i1, i1] = 0.0
+    FT[i2, i2] = 0.0
+    for b in range(1, nb):
+        s1, s2 = t.c1[b], t.c2[b]
+        if s1 >= 0 and s2 >= 0:
+            ka, kb = H.kskel[s1], H.kskel[s2]
+            ia = slice(0, ka)
+            ib = slice(ka, ka + kb)
+            Dv[s1] = Dv[s1] + Lv[s1] @ Dv[b][ia, ia] @ Rv[s1]
+            Dv[s2] = Dv[s2] + Lv[s2] @ Dv[b][ib, ib] @ Rv[s2]
+            Dv[b][ia, ia] = 0.0
+            Dv[b][ib, ib] = 0.0
+        elif s1 >= 0 or s2 >= 0:
+            s = max(s1, s2)
+            Dv[s] = Dv[s] + Lv[s] @ Dv[b] @ Rv[s]
+            Dv[b] = np.zeros((H.kskel[s], H.kskel[s]))
+    for b in range(nb - 1, 0, -1):
+        n, k = H.nskel[b], H.kskel[b]
+        JC, JR = H.J_UP[b], H.J_DN[b]
+        L, R = Lv[b], Rv[b]
+        P = L[JC[:k], :]
+        Q = R[:, JR[:k]]
+        Lnew = np.zeros((n, k))
+        Lnew[JC[:k]] = np.eye(k)
+        Lnew[JC[k:]] = np.linalg.solve(P.T, L[JC[k:], :].T).T
+        Rnew = np.zeros((k, n))
+        Rnew[:, JR[:k]] = np.eye(k)
+        Rnew[:, JR[k:]] = np.linalg.solve(Q, R[:, JR[k:]])
+        Lv[b] = Lnew
+        Rv[b] = Rnew
+        f = t.parent[b]
+        if b == t.c2[f] and t.c1[f] >= 0:
+            ind = slice(H.kskel[t.c1[f]], H.kskel[t.c1[f]] + k)
+        else:
+            ind = slice(0, k)
+        if t.level[b] > 1:
+            Lv[f][ind, :] = P @ Lv[f][ind, :]
+            Rv[f][:, ind] = Rv[f][:, ind] @ Q
+            Dv[f][ind, :] = P @ Dv[f][ind, :]
+            Dv[f][:, ind] = Dv[f][:, ind] @ Q
+        else:
+            FT[ind, :] = P @ FT[ind, :]
+            FT[:, ind] = FT[:, ind] @ Q
+    K = HSS1DMatrix(t)
+    K.nskel = list(H.nskel)
+    K.kskel = list(H.kskel)
+    K.I_SKUP = list(H.I_SKUP)
+    K.I_SKDN = list(H.I_SKDN)
+    K.T_UP = [None] * nb
+    K.J_UP = [None] * nb
+    K.T_DN = [None] * nb
+    K.J_DN = [None] * nb
+    K.M_SELF = [None] * nb
+    K.M_SIB = [None] * nb
+    for b in range(1, nb):
+        n, k = H.nskel[b], H.kskel[b]
+        JC, JR = H.J_UP[b], H.J_DN[b]
+        K.T_UP[b] = Rv[b][:, JR[k:]]
+        K.J_UP[b] = JR
+        K.T_DN[b] = Lv[b][JC[k:], :].T
+        K.J_DN[b] = JC
+    ka = H.kskel[1]
+    kb = H.kskel[2]
+    K.M_SIB[1] = FT[0:ka, ka:ka + kb]
+    K.M_SIB[2] = FT[ka:ka + kb, 0:ka]
+    for b in range(1, nb):
+        s1, s2 = t.c1[b], t.c2[b]
+        if s1 >= 0 and s2 >= 0:
+            ka, kb = H.kskel[s1], H.kskel[s2]
+            K.M_SIB[s1] = Dv[b][0:ka, ka:ka + kb]
+            K.M_SIB[s2] = Dv[b][ka:ka + kb, 0:ka]
+        elif t.is_leaf(b):
+            K.M_SELF[b] = Dv[b]
+    return K
+
+
+def dense_from_points(X, kp):
+    return kernel_eval(X, X, kp)

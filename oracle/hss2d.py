@@ -1,0 +1,472 @@
+"""HSS2D (compressed-block HSS, dense-block "HSS-D" path) oracle restatement.
+
+Follows:
+  Common/HSS_tree_parameters.m:108-162     (params, X_source)
+  HSS2D/HSS2D_build_tree_nsym.m            (uniform tree :145-277 with bisect_level
+                                            :1183-1240; Build_I_source_unif :1097-1124;
+                                            upward skeleton pass :342-559; 'bdry' preset
+                                            skeletons :732-792; orient :794-811; dense
+                                            interpolation operators :814-868; proxy
+                                            :870-961)
+  HSS2D/build_box_proxy.m:52-88
+  HSS2D/interpolation_operator.m:57-77     (dense T = K11 \\ K21)
+  HSS2D/HSS2D_compress_nsym.m:67-125       (dense Bself, B12, B21)
+  HSS2D/HSS2D_invert_nsym.m:70-155         (Fopts='dense')
+  HSS2D/HSS2D_build_Finv_nsym.m:92-100     (dense FI = inv([E1 K12; K21 E2]))
+  HSS2D/HSS2D_build_E_nsym.m:43-51         (dense, LR = 0: E = inv(R FI L))
+  HSS2D/HSS2D_apply_nsym.m:74-218
+  HSS2D/HSS2D_applyinv_nsym.m:74-243 with HSS2D_applyFinv_nsym.m:30-31
+
+Boxes are 0-based heap-numbered (box b has children 2b+1, 2b+2), which is the
+reference's 1-based numbering (children 2B, 2B+1) shifted by one.  Index arrays
+are 0-based.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from .kernels import KernelParams, kernel_eval, SL_L_2D
+from . import geometry
+from . import idecomp
+
+
+@dataclass
+class HSS2DParams:
+    """The fields of params (HSS_tree_parameters.m:115-139) the dense path reads."""
+
+    Ng: int
+    npan: int
+    acc: float = 1e-10
+    layers: int = 2
+    kp: KernelParams = field(default_factory=KernelParams)
+    INTERform: str = "dense"
+    transinv: int = 0
+    sym: int = 0
+
+    @property
+    def h(self):
+        return 2.0 / (self.Ng * self.npan)
+
+    @property
+    def depth(self):
+        nlevels = int(round(2 * (math.log(self.npan) / math.log(2) - 1) + 3))
+        return nlevels - 1
+
+    @property
+    def N(self):
+        return self.npan * self.npan * self.Ng * self.Ng
+
+    def X_source(self):
+        return geometry.grid_source(self.Ng, self.npan)
+
+
+def box_radii(lev):
+    """(colrad, rowrad) of a level (HSS2D_build_tree_nsym.m:343-347)."""
+    scl = lev // 2
+    rowrad = 2.0 ** (-scl)
+    colrad = rowrad / (2 ** (lev % 2))
+    return colrad, rowrad
+
+
+def box_centers(depth):
+    """cent of bisect_level (:1183-1240): level-even boxes split in x, odd in y."""
+    nb = 2 ** (depth + 1) - 1
+    cent = np.zeros((nb, 2))
+    for lev in range(depth):
+        scl = lev // 2
+        d = 0.5 * (0.5 ** scl)
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            c = cent[b]
+            if lev % 2 == 0:
+                cent[2 * b + 1] = (c[0] - d, c[1])
+                cent[2 * b + 2] = (c[0] + d, c[1])
+            else:
+                cent[2 * b + 1] = (c[0], c[1] + d)
+                cent[2 * b + 2] = (c[0], c[1] - d)
+    return cent
+
+
+def _colon(a, step, b):
+    """MATLAB a:step:b for values on an h-grid."""
+    n = int(math.floor((b - a) / step + 1e-9)) + 1
+    if n <= 0:
+        return np.zeros(0)
+    return a + step * np.arange(n)
+
+
+def build_box_proxy(cB, colrad, rowrad, layers, h):
+    """build_box_proxy.m:52-88; returns [X_proxy; X_extra] as the 'bdry' rule uses it."""
+    cx, cy = cB
+    width = (layers - 0.5) * h
+    xs1 = _colon(cx - colrad - width, h, cx - colrad - h / 2)
+    ys1 = _colon(cy - rowrad - width, h, cy + rowrad + width)
+    X1 = np.stack([np.tile(xs1, len(ys1)), np.repeat(ys1, len(xs1))], axis=1)
+    xs2 = _colon(cx - colrad + h / 2, h, cx + colrad - h / 2)
+    ys2 = _colon(cy + rowrad + width, -h, cy + rowrad + h / 2)
+    X2 = np.stack([np.repeat(xs2, len(ys2)), np.tile(ys2, len(xs2))], axis=1)
+    xs3 = _colon(cx + colrad + h / 2, h, cx + colrad + width)
+    ys3 = _colon(cy + rowrad + width, -h, cy - rowrad - width)
+    X3 = np.stack([np.tile(xs3, len(ys3)), np.repeat(ys3, len(xs3))], axis=1)
+    xs4 = _colon(cx + colrad - h / 2, -h, cx - colrad + h / 2)
+    ys4 = _colon(cy - rowrad - h / 2, -h, cy - rowrad - width)
+    X4 = np.stack([np.repeat(xs4, len(ys4)), np.tile(ys4, len(xs4))], axis=1)
+    r1 = layers * layers - 0.5
+    r2 = layers * layers + 0.5
+    W = rowrad + width
+    V = colrad + width
+    I1 = ((np.abs(X1[:, 0] - cx) > (V - h / 2)) & ((X1[:, 1] - cy > (W - r1 * h)) | (X1[:, 1] - cy < -(W - r2 * h)))) \
+        | (np.abs(X1[:, 1] - cy) > (W - h / 2))
+    I2 = (np.abs(X2[:, 1] - cy) > (W - h / 2)) & ((X2[:, 0] - cx > (V - r1 * h)) | (X2[:, 0] - cx < -(V - r2 * h)))
+    I3 = ((np.abs(X3[:, 0] - cx) > (V - h / 2)) & ((X3[:, 1] - cy > (W - r2 * h)) | (X3[:, 1] - cy < -(W - r1 * h)))) \
+        | (np.abs(X3[:, 1] - cy) > (W - h / 2))
+    I4 = (np.abs(X4[:, 1] - cy) > (W - h / 2)) & ((X4[:, 0] - cx > (V - r2 * h)) | (X4[:, 0] - cx < -(V - r1 * h)))
+    return np.vstack([X1[~I1], X2[~I2], X3[~I3], X4[~I4], X1[I1], X2[I2], X3[I3], X4[I4]])
+
+
+def orient_residual(X_rs, nrm, tan):
+    """LOCAL_orient_residual, HSS2D_build_tree_nsym.m:805-811 (stable sorts)."""
+    J1 = np.argsort(X_rs[:, nrm], kind="stable")
+    J2 = np.argsort(-X_rs[J1, tan], kind="stable")
+    return J1[J2]
+
+
+def orient_skeleton(X_sk, cB, th0):
+    """LOCAL_orient_skeleton, HSS2D_build_tree_nsym.m:794-802."""
+    dx = X_sk[:, 0] - cB[0]
+    dy = X_sk[:, 1] - cB[1]
+    # libm atan2/hypot (cart2pol), the same calls the host C++ tree builder makes
+    th = np.array([math.atan2(a, b) for a, b in zip(dy.tolist(), dx.tolist())])
+    rho = np.array([math.hypot(a, b) for a, b in zip(dx.tolist(), dy.tolist())])
+    th = np.where(th < th0, th + 2.0 * math.pi, th)
+    J1 = np.argsort(rho, kind="stable")
+    J2 = np.argsort(th[J1], kind="stable")
+    return J1[J2]
+
+
+def preset_skeleton(X_src, cB, lev, colrad, rowrad, layers, h):
+    """LOCAL_Preset_Skeleton_Info 'bdry' branch, :732-792. Returns (J, k)."""
+    width = layers * h
+    bdry = (np.abs(X_src[:, 0] - cB[0]) > (colrad - width)) | (np.abs(X_src[:, 1] - cB[1]) > (rowrad - width))
+    if lev % 2 == 0:
+        nrm, tan, th0 = 0, 1, math.pi / 2
+    else:
+        nrm, tan, th0 = 1, 0, 0.0
+    idx = np.arange(X_src.shape[0])
+    I_rs = idx[~bdry]
+    I_rs = I_rs[orient_residual(X_src[~bdry], nrm, tan)]
+    I_sk = idx[bdry]
+    I_sk = I_sk[orient_skeleton(X_src[bdry], cB, th0)]
+    return np.concatenate([I_sk, I_rs]), len(I_sk)
+
+
+@dataclass
+class HSS2DTree:
+    depth: int
+    cent: np.ndarray
+    I_src: list
+    I_sk: list
+    J: list
+    k: list
+    T_up: list
+    T_dn: list
+    proxy: list
+    leaf_of_panel: np.ndarray
+
+    @property
+    def nboxes(self):
+        return len(self.I_src)
+
+    def children(self, b):
+        return 2 * b + 1, 2 * b + 2
+
+    def is_leaf(self, b):
+        return 2 * b + 1 >= self.nboxes
+
+
+def lay_prox(prm: HSS2DParams, lev):
+    """HSS2D_build_tree_nsym.m:360-368."""
+    if lev > 0:
+        if prm.kp.flag == SL_L_2D:
+            return prm.layers + 1
+        colrad, rowrad = box_radii(lev)
+        return 2 * int(round(min(colrad, rowrad) / prm.h))
+    return prm.layers
+
+
+def leaf_sources(prm: HSS2DParams, cent):
+    """Build_I_source_unif (:1097-1124): the panel whose first point a leaf holds."""
+    depth = prm.depth
+    J = prm.Ng * prm.Ng
+    X = prm.X_source()
+    first = X[0::J]
+    colrad, rowrad = box_radii(depth)
+    l0 = 2 ** depth - 1
+    leaf_of_panel = np.empty(first.shape[0], dtype=np.int64)
+    lc = cent[l0:]
+    for i, p in enumerate(first):
+        hit = np.nonzero((np.abs(p[0] - lc[:, 0]) < colrad) & (np.abs(p[1] - lc[:, 1]) < rowrad))[0]
+        assert hit.size == 1
+        leaf_of_panel[i] = l0 + hit[0]
+    return leaf_of_panel
+
+
+def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
+    """INFO_TREE = HSS2D_build_tree_nsym(params), 'uniform'/'bdry'/'bdry', NTI."""
+    assert prm.transinv == 0
+    depth = prm.depth
+    h = prm.h
+    X = prm.X_source()
+    cent = box_centers(depth)
+    nb = 2 ** (depth + 1) - 1
+    lop = leaf_sources(prm, cent)
+    J = prm.Ng * prm.Ng
+    I_src = [None] * nb
+    for i, b in enumerate(lop):
+        I_src[b] = np.arange(J * i, J * (i + 1))
+    I_sk = [None] * nb
+    Js = [None] * nb
+    ks = [0] * nb
+    T_up = [None] * nb
+    T_dn = [None] * nb
+    proxy = [None] * nb
+    for lev in range(depth, -1, -1):
+        colrad, rowrad = box_radii(lev)
+        lp = lay_prox(prm, lev)
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            if 2 * b + 1 < nb:
+                I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
+            X_src = X[I_src[b]]
+            Jb, kb = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
+            Js[b] = Jb
+            ks[b] = kb
+            I_sk[b] = I_src[b][Jb[:kb]]
+            Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
+            proxy[b] = Xp
+            if with_T and lev > 0:
+                T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_src[Jb[:kb]], X_src[Jb[kb:]])
+    return HSS2DTree(depth, cent, I_src, I_sk, Js, ks, T_up, T_dn, proxy, lop)
+
+
+def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):
+    """interpolation_operator.m:57-77 with lr = 0: T_up (box_2_proxy), T_dn (proxy_2_box)."""
+    k = X_sk.shape[0]
+    if k == 0 or X_rs.shape[0] == 0:
+        z = np.zeros((k, X_rs.shape[0]))
+        return z, z
+    kp = prm.kp
+    K11 = kernel_eval(Xp, X_sk, kp)
+    K21 = kernel_eval(Xp, X_rs, kp)
+    Tu = idecomp.lstsq_qr(K11, K21)
+    K11d = kernel_eval(X_sk, Xp, kp).T
+    K21d = kernel_eval(X_rs, Xp, kp).T
+    Td = idecomp.lstsq_qr(K11d, K21d)
+    return Tu, Td
+
+
+@dataclass
+class HSS2DBlocks:
+    Bself: dict
+    B12: dict
+    B21: dict
+
+
+def compress_nsym(tree: HSS2DTree, prm: HSS2DParams) -> HSS2DBlocks:
+    """A_HSS = HSS2D_compress_nsym(INFO_TREE, params), dense branch (:81-107)."""
+    X = prm.X_source()
+    kp = prm.kp
+    Bs, B12, B21 = {}, {}, {}
+    for b in range(tree.nboxes):
+        if tree.is_leaf(b):
+            Xi = X[tree.I_src[b]]
+            Bs[b] = kernel_eval(Xi, Xi, kp)
+        else:
+            c1, c2 = tree.children(b)
+            X1 = X[tree.I_sk[c1]]
+            X2 = X[tree.I_sk[c2]]
+            B12[b] = kernel_eval(X1, X2, kp)
+            B21[b] = kernel_eval(X2, X1, kp)
+    return HSS2DBlocks(Bs, B12, B21)
+
+
+def _R_L(tree, b):
+    k = tree.k[b]
+    Jb = tree.J[b]
+    n = len(Jb)
+    R = np.zeros((k, n))
+    R[:, Jb] = np.hstack([np.eye(k), tree.T_up[b]])
+    L = np.zeros((n, k))
+    L[Jb, :] = np.hstack([np.eye(k), tree.T_dn[b]]).T
+    return R, L
+
+
+def invert_nsym(tree: HSS2DTree, prm: HSS2DParams, blocks: HSS2DBlocks | None = None):
+    """A_HSS = HSS2D_invert_nsym(INFO_TREE, params) with Fopts = 'dense'.
+
+    Returns dict with FI (per box) and E (per non-root box).
+    """
+    X = prm.X_source()
+    kp = prm.kp
+    nb = tree.nboxes
+    FI = [None] * nb
+    E = [None] * nb
+    for lev in range(tree.depth, -1, -1):
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            if tree.is_leaf(b):
+                Xi = X[tree.I_src[b]]
+                A = blocks.Bself[b] if blocks is not None else kernel_eval(Xi, Xi, kp)
+                FI[b] = np.linalg.inv(A)
+            else:
+                c1, c2 = tree.children(b)
+                if blocks is not None:
+                    K12, K21 = blocks.B12[b], blocks.B21[b]
+                else:
+                    X1, X2 = X[tree.I_sk[c1]], X[tree.I_sk[c2]]
+                    K12, K21 = kernel_eval(X1, X2, kp), kernel_eval(X2, X1, kp)
+                F = np.block([[E[c1], K12], [K21, E[c2]]])
+                FI[b] = np.linalg.inv(F)
+            if lev > 0:
+                R, L = _R_L(tree, b)
+                E[b] = np.linalg.inv(R @ (FI[b] @ L))
+    return {"FI": FI, "E": E}
+
+
+def apply_nsym(tree: HSS2DTree, blocks: HSS2DBlocks, Xv: np.ndarray) -> np.ndarray:
+    """Y = HSS2D_apply_nsym(INFO_TREE, A_HSS, X, params), :74-218 (LR = 0)."""
+    Xv = np.asarray(Xv, dtype=np.float64)
+    vec = Xv.ndim == 1
+    if vec:
+        Xv = Xv[:, None]
+    nb = tree.nboxes
+    up = [None] * nb
+    dn = [None] * nb
+    for lev in range(tree.depth, 0, -1):
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            if tree.is_leaf(b):
+                q = Xv[tree.I_src[b]]
+            else:
+                c1, c2 = tree.children(b)
+                q = np.vstack([up[c1], up[c2]])
+            k = tree.k[b]
+            Jb = tree.J[b]
+            if k < len(Jb):
+                up[b] = q[Jb[:k]] + tree.T_up[b] @ q[Jb[k:]]
+            else:
+                up[b] = q[Jb]
+    Y = np.zeros_like(Xv)
+    for lev in range(0, tree.depth + 1):
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            if tree.is_leaf(b):
+                lam = blocks.Bself[b] @ Xv[tree.I_src[b]]
+            else:
+                c1, c2 = tree.children(b)
+                lam = np.vstack([blocks.B12[b] @ up[c2], blocks.B21[b] @ up[c1]])
+            eta = np.zeros_like(lam)
+            if lev > 0:
+                k = tree.k[b]
+                Jb = tree.J[b]
+                tmp = dn[b]
+                if k < len(Jb):
+                    eta[Jb] = np.vstack([tmp, tree.T_dn[b].T @ tmp])
+                else:
+                    eta[Jb] = tmp
+            phi = eta + lam
+            if tree.is_leaf(b):
+                Y[tree.I_src[b]] = phi
+            else:
+                c1, c2 = tree.children(b)
+                k1 = tree.k[c1]
+                dn[c1] = phi[:k1]
+                dn[c2] = phi[k1:]
+    return Y[:, 0] if vec else Y
+
+
+def applyinv_nsym(tree: HSS2DTree, inv: dict, Xv: np.ndarray) -> np.ndarray:
+    """Y = HSS2D_applyinv_nsym(INFO_TREE, A_HSS, X, params), :74-243 (dense, LR = 0)."""
+    Xv = np.asarray(Xv, dtype=np.float64)
+    vec = Xv.ndim == 1
+    if vec:
+        Xv = Xv[:, None]
+    nb = tree.nboxes
+    FI, E = inv["FI"], inv["E"]
+    up = [None] * nb
+    dn = [None] * nb
+    for lev in range(tree.depth, 0, -1):
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            if tree.is_leaf(b):
+                q = Xv[tree.I_src[b]]
+            else:
+                c1, c2 = tree.children(b)
+                q = np.vstack([up[c1], up[c2]])
+            psi = FI[b] @ q
+            k = tree.k[b]
+            Jb = tree.J[b]
+            if k < len(Jb):
+                tmp = psi[Jb[:k]] + tree.T_up[b] @ psi[Jb[k:]]
+            else:
+                tmp = psi[Jb]
+            up[b] = E[b] @ tmp
+    Y = np.zeros_like(Xv)
+    for lev in range(0, tree.depth + 1):
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            k = tree.k[b]
+            Jb = tree.J[b]
+            n = len(Jb)
+            if lev == 0:
+                lam = np.vstack([up[1], up[2]])
+                eta = np.zeros_like(lam)
+            else:
+                tmp = np.zeros((n, Xv.shape[1]))
+                if k < n:
+                    tmp[Jb] = np.vstack([up[b], tree.T_dn[b].T @ up[b]])
+                else:
+                    tmp[Jb] = up[b]
+                if tree.is_leaf(b):
+                    q = Xv[tree.I_src[b]]
+                else:
+                    c1, c2 = tree.children(b)
+                    q = np.vstack([up[c1], up[c2]])
+                lam = q - tmp
+                t2 = E[b] @ dn[b]
+                eta = np.zeros_like(lam)
+                if k < n:
+                    eta[Jb] = np.vstack([t2, tree.T_dn[b].T @ t2])
+                else:
+                    eta[Jb] = t2
+            phi = FI[b] @ (eta + lam)
+            if tree.is_leaf(b):
+                Y[tree.I_src[b]] = phi
+            else:
+                c1, c2 = tree.children(b)
+                k1 = tree.k[c1]
+                dn[c1] = phi[:k1]
+                dn[c2] = phi[k1:]
+    return Y[:, 0] if vec else Y
+
+
+def kernel_matvec(prm: HSS2DParams, Xv: np.ndarray, block: int = 4096) -> np.ndarray:
+    """A @ Xv for the dense kernel matrix A = K[X_source, X_source], blockwise."""
+    X = prm.X_source()
+    Xv = np.asarray(Xv, dtype=np.float64)
+    out = np.zeros_like(Xv)
+    for i in range(0, X.shape[0], block):
+        out[i:i + block] = kernel_eval(X[i:i + block], X, prm.kp) @ Xv
+    return out
+
+
+def iterative_refinement(apply_A, apply_inv, B, acc, maxit=10):
+    """Common/Iterative_Refinement.m:20-35 (absolute-norm stop, as the reference)."""
+    Xs = apply_inv(B)
+    res = B - apply_A(Xs)
+    err = np.linalg.norm(res)
+    it = 1
+    hist = [err]
+    while err > acc and it < maxit:
+        Xs = Xs + apply_inv(res)
+        res = B - apply_A(Xs)
+        err = np.linalg.norm(res)
+        it += 1
+        hist.append(err)
+    return Xs, hist
