@@ -1,0 +1,66 @@
+"""The C ABI: the library builds, loads and exports every symbol include/hssgpu.h declares
+(CPU only: no compute call is made without a GPU)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+HEADER = os.path.join(ROOT, "include", "hssgpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(hss\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from hssc_directsolver_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return _lib.lib()
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for need in ("hss1d_compress", "hss1d_invert", "hss1d_apply", "hss1d_applyinv", "hss2d_build_tree",
+                 "hss2d_compress", "hss2d_invert", "hss2d_apply", "hss2d_applyinv", "hss2d_solve"):
+        assert need in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header():
+    from hssc_directsolver_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_status_paths_without_gpu(lib):
+    from hssc_directsolver_gb300 import _lib
+    n = C.c_int32(-1)
+    assert lib.hss_device_count(C.byref(n)) == _lib.HSS_OK
+    assert n.value >= 0
+    assert lib.hss_version() >= 100
+    # NULL arguments are rejected before any device work
+    assert lib.hss2d_compress(None) == _lib.HSS_ERR_ARG
+    assert lib.hss1d_invert(None) == _lib.HSS_ERR_ARG
+    assert b"NULL" in lib.hss_last_error()
+    if n.value == 0:
+        h = C.c_void_p()
+        p = _lib.hss2d_params(8, 4, 2, 0, 0, 0, 0, 0, 1e-10, _lib.hss_kernel_params())
+        assert lib.hss2d_build_tree(C.byref(h), C.byref(p)) == _lib.HSS_ERR_CUDA
+
+
+def test_product_fails_loudly_without_library(monkeypatch, tmp_path):
+    from hssc_directsolver_gb300 import _lib
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError):
+        _lib.lib()

@@ -1,0 +1,97 @@
+"""HSS1D on the GPU against the oracle and the golden fixture (GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import geometry, hss1d as O1, hss2d as O2, kernels as OK
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def star(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    g = np.load(os.path.join(GOLD, "hss1d_star4096.npz"))
+    X = geometry.star_curve(int(g["N"]))
+    H = G1.HSS1D_compress_nsym("green", X, int(g["leaf"]), float(g["acc"]), GK.Kernel("DL_L_2D"))
+    Ho = O1.compress_nsym(X, int(g["leaf"]), float(g["acc"]), OK.KernelParams(flag=OK.DL_L_2D))
+    return G1, g, X, H, Ho
+
+
+def test_ranks_and_skeletons_exact(star):
+    G1, g, X, H, Ho = star
+    inf = H.info()
+    assert np.array_equal(inf["kskel"], g["kskel"])
+    nb = inf["nboxes"]
+    up = np.concatenate([H.export_box(b)["I_SKUP"] for b in range(1, nb)])
+    dn = np.concatenate([H.export_box(b)["I_SKDN"] for b in range(1, nb)])
+    assert np.array_equal(up, g["I_SKUP"]) and np.array_equal(dn, g["I_SKDN"])
+    for b in (1, 2, nb - 1):
+        e = H.export_box(b)
+        k = Ho.kskel[b]
+        assert np.array_equal(e["J_UP"][:k], Ho.J_UP[b][:k])
+        if e["T_UP"].size:
+            # residual columns past the rank may be ordered differently (their norms tie at
+            # rounding level); compare the interpolation coefficients column by residual point
+            pos = {c: i for i, c in enumerate(e["J_UP"][k:])}
+            Tg = np.stack([e["T_UP"][:, pos[c]] for c in Ho.J_UP[b][k:]], axis=1)
+            assert np.abs(Tg - Ho.T_UP[b]).max() <= 1e-6 * max(1, np.abs(Ho.T_UP[b]).max())
+
+
+def test_apply_matches_oracle(star):
+    G1, g, X, H, Ho = star
+    q = np.random.default_rng(5).standard_normal((X.shape[0], 3))
+    u = G1.HSS1D_apply_nsym(H, q)
+    uo = O1.apply_nsym(Ho, q)
+    assert np.linalg.norm(u - uo) <= 1e-12 * np.linalg.norm(uo)
+
+
+def test_applyinv_matches_oracle_1e12(star):
+    G1, g, X, H, Ho = star
+    G1.HSS1D_invert_nsym(H)
+    x = G1.HSS1D_applyinv_nsym(H, None, None, g["f"])
+    assert np.linalg.norm(x - g["x"]) <= 1e-12 * np.linalg.norm(g["x"])
+    A = OK.kernel_eval(X, X, OK.KernelParams(flag=OK.DL_L_2D))
+    assert np.linalg.norm(A @ x - g["f"]) / np.linalg.norm(g["f"]) < 1e-10
+    F = np.random.default_rng(6).standard_normal((X.shape[0], 11))   # more than one 8-column chunk
+    Y = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    Yo = O1.applyinv_nsym(Ho, O1.invert_nsym(Ho), F)
+    assert np.linalg.norm(Y - Yo) <= 1e-12 * np.linalg.norm(Yo)
+
+
+def test_reference_test_geometry(gpu):
+    """Run_HSS1D_tests.m parameters: Laplace SL on the 2-layer skeleton of box 2 (Ng=7, np=16)."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    Ng, npan = 7, 16
+    h = 2.0 / (Ng * npan)
+    b, c = OK.reference_modulations(sym=0, proxy=1, transinv=0)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=h, b=b, c=c)
+    prm = O2.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    X = prm.X_source()[O2.build_tree_nsym(prm, with_T=False).I_sk[1]]
+    gk = GK.Kernel("SL_L_2D", h, GK.Modulation(b.alpha, b.x0, b.y0, b.isig), GK.Modulation(c.alpha, c.x0, c.y0, c.isig))
+    H = G1.HSS1D_compress_nsym("green", X, 56, 1e-10, gk)
+    Ho = O1.compress_nsym(X, 56, 1e-10, kp)
+    inf = H.info()
+    assert np.array_equal(inf["kskel"][1:], np.array(Ho.kskel[1:]))
+    G1.HSS1D_invert_nsym(H)
+    q = np.random.default_rng(0).standard_normal((X.shape[0], 10))
+    A = OK.kernel_eval(X, X, kp)
+    y = G1.HSS1D_applyinv_nsym(H, None, None, q)
+    yd = np.linalg.solve(A, q)
+    assert np.linalg.norm(y - yd) / np.linalg.norm(yd) < 1e-8       # INSTALL.txt criterion
+    yo = O1.applyinv_nsym(Ho, O1.invert_nsym(Ho), q)
+    assert np.linalg.norm(y - yo) <= 1e-12 * np.linalg.norm(yo)
+
+
+def test_errors_are_status_codes(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, _lib as L
+    X = geometry.star_curve(256)
+    with pytest.raises(L.HSSError) as e:
+        G1.HSS1D_compress_nsym("green", X, 64, 2.0, GK.Kernel("DL_L_2D"))
+    assert e.value.code == L.HSS_ERR_ARG
+    H = G1.HSS1D_compress_nsym("green", X, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    with pytest.raises(L.HSSError) as e:
+        G1.HSS1D_applyinv_nsym(H, None, None, np.ones(256))
+    assert e.value.code == L.HSS_ERR_STATE

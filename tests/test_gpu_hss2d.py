@@ -1,0 +1,124 @@
+"""HSS2D on the GPU against the oracle, the golden fixture and full-size properties (GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import hss2d as O2, kernels as OK
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def params(npan, precision="fp64", Ng=8):
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    h = 2.0 / (Ng * npan)
+    return G2.HSS2DParams(Ng=Ng, npan=npan, kernel=GK.Kernel("SL_L_2D", h, GK.Modulation(),
+                                                               GK.Modulation(0.5, 0, 0, 20.0)),
+                          precision=precision)
+
+
+def oracle(npan, Ng=8):
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / (Ng * npan), c=OK.Modulation(0.5, 0, 0, 20.0))
+    prm = O2.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    tree = O2.build_tree_nsym(prm)
+    blk = O2.compress_nsym(tree, prm)
+    return prm, tree, blk, O2.invert_nsym(tree, prm, blk)
+
+
+@pytest.fixture(scope="module", params=[4, 8])
+def case(request, gpu):
+    from hssc_directsolver_gb300 import hss2d as G2
+    npan = request.param
+    t = G2.HSS2D_build_tree_nsym(params(npan))
+    G2.HSS2D_compress_nsym(t)
+    G2.HSS2D_invert_nsym(t)
+    return G2, t, oracle(npan)
+
+
+def test_tree_exact(case):
+    G2, t, (prm, ot, blk, inv) = case
+    n, k, p = t.box_sizes()
+    for b in range(t.nboxes):
+        e = t.export_box(b)
+        assert np.array_equal(e["J"], ot.J[b]) and np.array_equal(e["I_src"], ot.I_src[b])
+        assert k[b] == ot.k[b] and p[b] == ot.proxy[b].shape[0]
+        if b > 0 and ot.T_up[b].size:
+            s = max(1.0, np.abs(ot.T_up[b]).max())
+            assert np.abs(e["T_up"] - ot.T_up[b]).max() <= 1e-7 * s
+            assert np.abs(e["T_dn"] - ot.T_dn[b]).max() <= 1e-7 * s
+
+
+def test_inverse_factors(case):
+    G2, t, (prm, ot, blk, inv) = case
+    for b in (0, 1, t.nboxes - 1):
+        FI, E = t.export_inverse(b)
+        assert np.abs(FI - inv["FI"][b]).max() <= 1e-7 * np.abs(inv["FI"][b]).max()
+        if b > 0:
+            assert np.abs(E - inv["E"][b]).max() <= 1e-7 * np.abs(inv["E"][b]).max()
+
+
+def test_apply_and_applyinv_match_oracle(case):
+    G2, t, (prm, ot, blk, inv) = case
+    q = np.random.default_rng(7).standard_normal((prm.N, 5))
+    u = G2.HSS2D_apply_nsym(t, None, q)
+    assert np.linalg.norm(u - O2.apply_nsym(ot, blk, q)) <= 1e-13 * np.linalg.norm(u)
+    x = G2.HSS2D_applyinv_nsym(t, None, q)
+    xo = O2.applyinv_nsym(ot, inv, q)
+    assert np.linalg.norm(x - xo) <= 1e-12 * np.linalg.norm(xo)
+    X = prm.X_source()
+    A = OK.kernel_eval(X, X, prm.kp)
+    assert np.linalg.norm(q - A @ x) / np.linalg.norm(q) < 1e-9
+
+
+def test_golden_fixture(gpu):
+    from hssc_directsolver_gb300 import hss2d as G2
+    g = np.load(os.path.join(GOLD, "hss2d_npan4.npz"))
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(params(4)))
+    x = G2.HSS2D_applyinv_nsym(t, None, g["f"])
+    assert np.linalg.norm(x - g["x"]) <= 1e-12 * np.linalg.norm(g["x"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_refinement(gpu, precision):
+    from hssc_directsolver_gb300 import hss2d as G2
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(params(8, precision)))
+    prm, ot, blk, inv = oracle(8)
+    f = np.random.default_rng(8).standard_normal((prm.N, 4))
+    x, rr, it = G2.HSS2D_solve(t, f, 1e-12, 8)
+    assert rr <= 1e-12
+    r = f - O2.apply_nsym(ot, blk, x)
+    assert np.linalg.norm(r, axis=0).max() / np.linalg.norm(f, axis=0).min() < 1e-11
+
+
+def test_full_size_properties(gpu):
+    """The 256x256 workload (N = 65536): forward(inverse(f)) = f to 1e-10, linearity."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(params(32)))
+    assert t.N == 65536 and t.depth == 10
+    r = np.random.default_rng(0)
+    f = r.standard_normal((t.N, 4))
+    x = G2.HSS2D_applyinv_nsym(t, None, f)
+    back = G2.HSS2D_apply_nsym(t, None, x)
+    assert np.linalg.norm(back - f, axis=0).max() / np.linalg.norm(f, axis=0).min() < 1e-10
+    x2 = G2.HSS2D_applyinv_nsym(t, None, 2.0 * f[:, :2] - 3.0 * f[:, 2:])
+    assert np.linalg.norm(x2 - (2.0 * x[:, :2] - 3.0 * x[:, 2:])) <= 1e-11 * np.linalg.norm(x2)
+    xs, rr, it = G2.HSS2D_solve(t, f, 1e-10, 3)
+    assert rr <= 1e-10 and it == 1
+
+
+def test_status_codes(gpu):
+    from hssc_directsolver_gb300 import hss2d as G2, _lib as L
+    with pytest.raises(L.HSSError) as e:
+        G2.HSS2D_build_tree_nsym(params(6))       # npan must be a power of two
+    assert e.value.code == L.HSS_ERR_ARG
+    t = G2.HSS2D_build_tree_nsym(params(4))
+    with pytest.raises(L.HSSError) as e:
+        G2.HSS2D_applyinv_nsym(t, None, np.ones(t.N))
+    assert e.value.code == L.HSS_ERR_STATE
+    G2.HSS2D_invert_nsym(t)
+    f = np.ones(t.N)
+    f[3] = np.nan
+    with pytest.raises(L.HSSError) as e:
+        G2.HSS2D_solve(t, f, 1e-10, 2)
+    assert e.value.code == L.HSS_ERR_NONFINITE
