@@ -249,6 +249,13 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         inv_ms = e0.elapsed_time(e1) / args.steps
+        # forward FP64 apply (the refinement residual operator)
+        e0.record(stream)
+        for _ in range(args.steps):
+            L.check(L.lib().hss2d_apply_device(tree._h, L.ptr(dY), L.ptr(dX), dF.shape[0], sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / args.steps
         # end to end through the C ABI with host buffers (H2D of f, D2H of x each step)
         Fh = np.asfortranarray(F)
         Xh = np.zeros_like(Fh)
@@ -266,6 +273,7 @@ def main():
         e2e_s = max_over_ranks((time.perf_counter() - te0) / args.steps)
         results[prec] = dict(compress_invert_s=ci, tree_s=t1 - t0, compress_s=t2 - t1, invert_s=t3 - t2,
                              solve_ms=ms, relres=rr.value, solves_used=it.value, applyinv_ms=inv_ms,
+                             apply_ms=fwd_ms,
                              solve_bytes=tree.solve_bytes(), launches=tree.solve_launches(dF.shape[0]),
                              e2e_s=e2e_s, e2e_relres=rr2.value, clocks=clk.summary())
         del tree
@@ -299,6 +307,8 @@ def main():
         "solves_per_s": {p: 1e3 / results[p]["solve_ms"] for p in results},
         "relres": {p: results[p]["relres"] for p in results},
         "solves_used": {p: results[p]["solves_used"] for p in results},
+        "applyinv_ms": {p: results[p]["applyinv_ms"] for p in results},
+        "apply_fp64_ms": {p: results[p]["apply_ms"] for p in results},
         "e2e": {"value": 1.0 / r["e2e_s"] * world, "unit": "solves/s",
                 "h2d_bytes_per_step": int(N * nrhs * 8), "d2h_bytes_per_step": int(N * nrhs * 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

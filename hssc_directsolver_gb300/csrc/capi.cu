@@ -47,13 +47,13 @@ static void require_device() {
 template <typename R>
 static void batched_inverse(R* d_A, int n, int batch, int* d_info, cudaStream_t s) {
   HSS_REQUIRE(d_A && d_info && n > 0 && batch > 0, HSS_ERR_ARG, "bad arguments");
-  DevBuf<int> ipiv((size_t)batch * n);
-  DevBuf<R> W((size_t)batch * GJ_NB * n), Wf((size_t)batch * n * n);
+  DevBuf<int> ipiv((size_t)batch * n), aux((size_t)batch * GJ_AUX);
+  DevBuf<R> W((size_t)batch * 2 * GJ_NB * n), Wf((size_t)batch * n * n);
   HSS_CUDA(cudaMemsetAsync(d_info, 0, batch * sizeof(int), s));
   std::vector<InvP<R>> P(batch);
   for (int b = 0; b < batch; ++b)
-    P[b] = InvP<R>{d_A + (size_t)b * n * n, n, n, ipiv.p + (size_t)b * n, W.p + (size_t)b * GJ_NB * n,
-                   Wf.p + (size_t)b * n * n, d_info + b};
+    P[b] = InvP<R>{d_A + (size_t)b * n * n, n, n, ipiv.p + (size_t)b * n, W.p + (size_t)b * 2 * GJ_NB * n,
+                   Wf.p + (size_t)b * n * n, d_info + b, aux.p + (size_t)b * GJ_AUX};
   DevBuf<InvP<R>> dP(batch);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(InvP<R>), cudaMemcpyHostToDevice, s));
   invert_batched<R>(dP.p, batch, n, s);
@@ -400,14 +400,21 @@ int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int3
   HSS_TRY
   HSS_REQUIRE(d_A && m > 0 && n > kf && kf > 0 && kf <= m && batch > 0, HSS_ERR_ARG, "bad arguments");
   cudaStream_t s = as_stream(stream);
+  const int nr = n - kf;
   DevBuf<double> V((size_t)batch * m * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * kf);
+  DevBuf<double> X((size_t)batch * kf * nr);
   std::vector<QrP<double>> P(batch);
   for (int b = 0; b < batch; ++b)
     P[b] = QrP<double>{d_A + (size_t)b * m * n, m, n, kf, m, V.p + (size_t)b * m * QR_NB,
-                       Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * kf};
+                       Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * kf, X.p + (size_t)b * kf * nr, kf};
   DevBuf<QrP<double>> dP(batch);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, s));
   lstsq_batched<double>(dP.p, batch, m, n, kf, s);
+  // the solution goes to A(0:kf, kf:n) (leading dimension m)
+  for (int b = 0; b < batch; ++b)
+    HSS_CUDA(cudaMemcpy2DAsync(d_A + (size_t)b * m * n + (size_t)kf * m, (size_t)m * sizeof(double),
+                               X.p + (size_t)b * kf * nr, (size_t)kf * sizeof(double), (size_t)kf * sizeof(double),
+                               nr, cudaMemcpyDeviceToDevice, s));
   HSS_CUDA(cudaStreamSynchronize(s));
   HSS_CATCH
 }

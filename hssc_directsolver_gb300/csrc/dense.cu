@@ -3,6 +3,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cooperative_groups.h>
 
 namespace hss {
 
@@ -208,71 +209,189 @@ void gemm_skinny(const GemmP<R>* dP, int batch, int maxM, R alpha, R beta, cudaS
 
 // ---------------------------------------------------------------------------
 // Blocked Gauss-Jordan inversion with partial pivoting.
+//
+// Per block of GJ_NB columns:
+//  1. k_gj_panel_cl: one thread-block cluster per matrix factors the panel
+//     (all n rows x GJ_NB columns) held in the distributed shared memory of the
+//     cluster (rows split across the CTAs).  Pivot search, pivot-row exchange
+//     and elimination run on the panel columns only; the interchanges are
+//     recorded in ipiv.
+//  2. k_gj_gather: the row interchanges of the block are composed into a row
+//     map; the rows it touches (panel rows and the rows they displaced) are
+//     copied, for every non-panel column, into W.
+//  3. k_gj_update: every non-panel column is permuted and updated with the
+//     panel: A(:,c) = base(:,c) + P * W(pivot rows, c), base being 0 on the
+//     panel rows, the displaced row content on the displaced rows and A(:,c)
+//     elsewhere.
+// The cluster barriers are reached the same number of times by every CTA of
+// a cluster (all of them take the same pivot decisions), so they cannot hang.
 // ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
 template <typename R>
-__global__ void __launch_bounds__(256) k_gj_panel(const InvP<R>* __restrict__ P, int j0) {
-  const InvP<R> p = P[blockIdx.x];
+__device__ void block_argmax_any(R& val, int& idx, R* shv, int* shi) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R ov = __shfl_xor_sync(0xffffffffu, val, o);
+    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > val || (ov == val && oi < idx)) { val = ov; idx = oi; }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) { shv[w] = val; shi[w] = idx; }
+  __syncthreads();
+  val = shv[0];
+  idx = shi[0];
+  for (int i = 1; i < nw; ++i)
+    if (shv[i] > val || (shv[i] == val && shi[i] < idx)) { val = shv[i]; idx = shi[i]; }
+  __syncthreads();
+}
+
+constexpr int GJ_THREADS = 512;
+
+template <typename R>
+__global__ void __launch_bounds__(GJ_THREADS) k_gj_panel_cl(const InvP<R>* __restrict__ P, int j0, int rows_per) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int crank = (int)cl.block_rank();
+  const InvP<R> p = P[blockIdx.x / C];
   const int n = p.n;
-  if (j0 >= n) return;
-  if (*p.info != 0) return;
-  const int tid = threadIdx.x;
+  if (j0 >= n) return;        // same for the whole cluster
+  if (*p.info != 0) return;   // read before any CTA of this launch can write it
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  R* pan = reinterpret_cast<R*>(s_raw);  // rows_per x GJ_NB, ld rows_per
+  __shared__ R s_slot_v;
+  __shared__ int s_slot_i;
+  __shared__ R rowJ[GJ_NB], rowP[GJ_NB], s_row[GJ_NB];
+  __shared__ R shv[32];
+  __shared__ int shi[32];
+  __shared__ R s_gv;
+  __shared__ int s_gi;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int r0 = crank * rows_per, r1 = min(n, r0 + rows_per);
   const int jend = min(j0 + GJ_NB, n), nbk = jend - j0;
   R* A = p.A;
   const size_t lda = p.lda;
-  __shared__ R s_row[GJ_NB];
-  __shared__ R shv[8];
-  __shared__ int shi[8];
+  for (int e = tid; e < rows_per * nbk; e += nt) {
+    const int i = e % rows_per, c = e / rows_per;
+    pan[i + c * rows_per] = (r0 + i < r1) ? A[(r0 + i) + (size_t)(j0 + c) * lda] : R(0);
+  }
+  __syncthreads();
+  bool failed = false;
   for (int j = j0; j < jend; ++j) {
+    const int jj = j - j0;
     R best = R(-1);
     int bi = INT_MAX;
-    for (int i = j + tid; i < n; i += 256) {
-      const R v = fabs(A[i + j * lda]);
+    for (int i = max(j, r0) + tid; i < r1; i += nt) {
+      const R v = fabs(pan[(i - r0) + jj * rows_per]);
       if (v > best) { best = v; bi = i; }
     }
-    block_argmax256(best, bi, shv, shi);
+    block_argmax_any(best, bi, shv, shi);
+    if (tid == 0) { s_slot_v = best; s_slot_i = bi; }
+    cl.sync();
+    if (tid == 0) {
+      R gv = R(-1);
+      int gi = INT_MAX;
+      for (int q = 0; q < C; ++q) {
+        const R v = *cl.map_shared_rank(&s_slot_v, q);
+        const int i = *cl.map_shared_rank(&s_slot_i, q);
+        if (v > gv || (v == gv && i < gi)) { gv = v; gi = i; }
+      }
+      s_gv = gv;
+      s_gi = gi;
+    }
+    __syncthreads();
+    best = s_gv;
+    bi = s_gi;
     if (bi == INT_MAX || !(best > R(0)) || !isfinite(best)) {
-      if (tid == 0) *p.info = (best == R(0)) ? (j + 1) : -1;
-      return;
+      if (crank == 0 && tid == 0) *p.info = (best == R(0)) ? (j + 1) : -1;
+      failed = true;
+      break;
     }
-    if (tid == 0) p.ipiv[j] = bi;
-    if (bi != j) {
-      for (int c = tid; c < n; c += 256) {
-        const R t = A[j + c * lda];
-        A[j + c * lda] = A[bi + c * lda];
-        A[bi + c * lda] = t;
-      }
-    }
-    __syncthreads();
-    const R piv = A[j + j * lda];
-    const R rp = R(1) / piv;
+    const int oj = j / rows_per, ob = bi / rows_per;
     if (tid < nbk) {
-      const int c = j0 + tid;
-      s_row[tid] = (c == j) ? rp : A[j + c * lda] * rp;
+      rowJ[tid] = *cl.map_shared_rank(&pan[(j - oj * rows_per) + tid * rows_per], oj);
+      rowP[tid] = *cl.map_shared_rank(&pan[(bi - ob * rows_per) + tid * rows_per], ob);
     }
+    cl.sync();  // every CTA holds rows j and bi before any CTA rewrites them
+    const R rp = R(1) / rowP[jj];
+    if (tid < nbk) s_row[tid] = (tid == jj) ? rp : rowP[tid] * rp;
+    if (crank == 0 && tid == 0) p.ipiv[j] = bi;
     __syncthreads();
-    for (int i = tid; i < n; i += 256) {
-      if (i == j) continue;
-      const R aij = A[i + j * lda];
-      for (int cc = 0; cc < nbk; ++cc) {
-        const int c = j0 + cc;
-        if (c == j) continue;
-        A[i + c * lda] -= aij * s_row[cc];
+    for (int i = r0 + tid; i < r1; i += nt) {
+      R* row = pan + (i - r0);
+      if (i == j) {
+        for (int c = 0; c < nbk; ++c) row[c * rows_per] = s_row[c];
+        continue;
       }
-      A[i + j * lda] = -aij * rp;
+      const bool moved = (i == bi);
+      const R aij = moved ? rowJ[jj] : row[jj * rows_per];
+      for (int c = 0; c < nbk; ++c) {
+        if (c == jj) continue;
+        const R cur = moved ? rowJ[c] : row[c * rows_per];
+        row[c * rows_per] = cur - aij * s_row[c];
+      }
+      row[jj * rows_per] = -aij * rp;
     }
-    __syncthreads();
-    if (tid < nbk) A[j + (j0 + tid) * lda] = s_row[tid];
     __syncthreads();
   }
-  // Save the pivot rows of every column for the delayed update.
-  for (int e = tid; e < nbk * n; e += 256) {
-    const int r = e % nbk, c = e / nbk;
-    p.W[r + (size_t)c * GJ_NB] = A[j0 + r + c * lda];
+  if (!failed) {
+    for (int e = tid; e < rows_per * nbk; e += nt) {
+      const int i = e % rows_per, c = e / rows_per;
+      if (r0 + i < r1) A[(r0 + i) + (size_t)(j0 + c) * lda] = pan[i + c * rows_per];
+    }
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+// Compose the block's interchanges into a row map and copy the touched rows
+// of every non-panel column into W: rows 0..nbk-1 = new panel rows, rows
+// GJ_NB.. = new content of the displaced rows.  aux = [np, prow[GJ_NB], ...].
+template <typename R>
+__global__ void __launch_bounds__(256) k_gj_gather(const InvP<R>* __restrict__ P, int j0) {
+  const InvP<R> p = P[blockIdx.y];
+  const int n = p.n;
+  if (j0 >= n) return;
+  if (*p.info != 0) return;
+  const int jend = min(j0 + GJ_NB, n), nbk = jend - j0;
+  __shared__ int pos[2 * GJ_NB], src[2 * GJ_NB];
+  __shared__ int s_cnt, s_np;
+  __shared__ int rsrc[GJ_NB], prow[GJ_NB], psrc[GJ_NB];
+  if (threadIdx.x == 0) {
+    int cnt = 0;
+    auto find = [&](int r) {
+      for (int q = 0; q < cnt; ++q)
+        if (pos[q] == r) return q;
+      pos[cnt] = r;
+      src[cnt] = r;
+      return cnt++;
+    };
+    for (int j = j0; j < jend; ++j) {
+      const int a = find(j), b = find(p.ipiv[j]);
+      const int t = src[a]; src[a] = src[b]; src[b] = t;
+    }
+    int np = 0;
+    for (int r = 0; r < nbk; ++r) rsrc[r] = src[find(j0 + r)];
+    for (int q = 0; q < cnt; ++q)
+      if ((pos[q] < j0 || pos[q] >= jend) && src[q] != pos[q]) { prow[np] = pos[q]; psrc[np] = src[q]; ++np; }
+    s_cnt = cnt;
+    s_np = np;
+    if (blockIdx.x == 0) {
+      p.aux[0] = np;
+      for (int q = 0; q < np; ++q) p.aux[1 + q] = prow[q];
+    }
+  }
+  __syncthreads();
+  const int np = s_np;
+  const R* A = p.A;
+  const size_t lda = p.lda;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    if (c >= j0 && c < jend) continue;
+    for (int r = 0; r < nbk; ++r) p.W[r + (size_t)c * 2 * GJ_NB] = A[rsrc[r] + c * lda];
+    for (int q = 0; q < np; ++q) p.W[GJ_NB + q + (size_t)c * 2 * GJ_NB] = A[psrc[q] + c * lda];
   }
 }
 
-// A[:, c] = mask(A[:, c]) + A[:, panel] * W[:, c] for every c outside the panel,
-// mask zeroing the panel rows.
 template <typename R>
 __global__ void __launch_bounds__(256) k_gj_update(const InvP<R>* __restrict__ P, int j0) {
   const InvP<R> p = P[blockIdx.z];
@@ -282,12 +401,20 @@ __global__ void __launch_bounds__(256) k_gj_update(const InvP<R>* __restrict__ P
   const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
   if (m0 >= n || n0 >= n) return;
   const int jend = min(j0 + GJ_NB, n), nbk = jend - j0;
-  if (n0 >= j0 && n0 + 64 <= jend) return;
   __shared__ R Ps[GJ_NB][64 + 1];
   __shared__ R Ws[GJ_NB][64 + 1];
+  __shared__ int rowq[64];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   R* A = p.A;
   const size_t lda = p.lda;
+  const int np = p.aux[0];
+  if (tid < 64) {
+    const int gi = m0 + tid;
+    int q = -1;
+    for (int t = 0; t < np; ++t)
+      if (p.aux[1 + t] == gi) q = t;
+    rowq[tid] = q;
+  }
   for (int e = tid; e < 64 * GJ_NB; e += 256) {
     const int i = e & 63, r = e >> 6;
     const int gi = m0 + i;
@@ -296,7 +423,7 @@ __global__ void __launch_bounds__(256) k_gj_update(const InvP<R>* __restrict__ P
   for (int e = tid; e < 64 * GJ_NB; e += 256) {
     const int r = e % GJ_NB, j = e / GJ_NB;
     const int gj = n0 + j;
-    Ws[r][j] = (gj < n && r < nbk) ? p.W[r + (size_t)gj * GJ_NB] : R(0);
+    Ws[r][j] = (gj < n && r < nbk) ? p.W[r + (size_t)gj * 2 * GJ_NB] : R(0);
   }
   __syncthreads();
   R acc[4][4];
@@ -321,11 +448,14 @@ __global__ void __launch_bounds__(256) k_gj_update(const InvP<R>* __restrict__ P
     if (gj >= n || (gj >= j0 && gj < jend)) continue;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int gi = m0 + tx + 16 * i;
+      const int li = tx + 16 * i, gi = m0 + li;
       if (gi >= n) continue;
       R* c = A + gi + (size_t)gj * lda;
-      const bool prow = (gi >= j0 && gi < jend);
-      *c = prow ? acc[i][j] : (*c + acc[i][j]);
+      R base;
+      if (gi >= j0 && gi < jend) base = R(0);
+      else if (rowq[li] >= 0) base = p.W[GJ_NB + rowq[li] + (size_t)gj * 2 * GJ_NB];
+      else base = *c;
+      *c = base + acc[i][j];
     }
   }
 }
@@ -346,7 +476,7 @@ __global__ void k_gj_perm(const InvP<R>* __restrict__ P) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_gj_gather(const InvP<R>* __restrict__ P) {
+__global__ void __launch_bounds__(256) k_gj_colgather(const InvP<R>* __restrict__ P) {
   const InvP<R> p = P[blockIdx.y];
   if (*p.info != 0) return;
   const int n = p.n;
@@ -371,12 +501,49 @@ __global__ void __launch_bounds__(256) k_gj_copyback(const InvP<R>* __restrict__
 }
 
 template <typename R>
+static int gj_cluster(int n, int batch, int& rows_per) {
+  int C = 1;
+  if (batch < 152 && n > 256) {
+    while (C < 8 && (n + C - 1) / C > 256) C *= 2;
+  }
+  rows_per = (n + C - 1) / C;
+  while ((size_t)rows_per * GJ_NB * sizeof(R) > 200 * 1024 && C < 8) {
+    C *= 2;
+    rows_per = (n + C - 1) / C;
+  }
+  return C;
+}
+
+template <typename R>
 void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s) {
   if (batch <= 0 || maxn <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "invert batch too large");
+  int rows_per = 0;
+  const int C = gj_cluster<R>(maxn, batch, rows_per);
+  const size_t smem = (size_t)rows_per * GJ_NB * sizeof(R);
+  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "block too large for the cluster panel (n > 6400)");
+  static bool attr_set = false;
+  if (!attr_set) {
+    HSS_CUDA(cudaFuncSetAttribute(k_gj_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(batch * C, 1, 1);
+  cfg.blockDim = dim3(GJ_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int gcols = std::max(1, std::min(ceil_div(maxn, 256), 64));
   for (int j0 = 0; j0 < maxn; j0 += GJ_NB) {
-    k_gj_panel<R><<<batch, 256, 0, s>>>(dP, j0);
-    check_launch("k_gj_panel");
+    HSS_CUDA(cudaLaunchKernelEx(&cfg, k_gj_panel_cl<R>, dP, j0, rows_per));
+    k_gj_gather<R><<<dim3(gcols, batch), 256, 0, s>>>(dP, j0);
+    check_launch("k_gj_gather");
     dim3 g(ceil_div(maxn, 64), ceil_div(maxn, 64), batch);
     k_gj_update<R><<<g, 256, 0, s>>>(dP, j0);
     check_launch("k_gj_update");
@@ -384,8 +551,8 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s) {
   k_gj_perm<R><<<batch, 32, 0, s>>>(dP);
   check_launch("k_gj_perm");
   const int gx = std::max(1, std::min(ceil_div((long long)maxn * maxn, 256), 1024));
-  k_gj_gather<R><<<dim3(gx, batch), 256, 0, s>>>(dP);
-  check_launch("k_gj_gather");
+  k_gj_colgather<R><<<dim3(gx, batch), 256, 0, s>>>(dP);
+  check_launch("k_gj_colgather");
   k_gj_copyback<R><<<dim3(gx, batch), 256, 0, s>>>(dP);
   check_launch("k_gj_copyback");
 }
@@ -394,88 +561,168 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // Blocked Householder least squares.
 // ---------------------------------------------------------------------------
-// Unblocked Householder on the panel A[j0:m, j0:jend] (one block per problem);
-// writes the explicit reflectors to V (rows j0..m-1, ld m) and the compact-WY
-// factor Tf (ld QR_NB).
+// Householder factorization of the panel A[j0:m, j0:jend], one thread-block
+// cluster per problem with the panel rows split over the CTAs' shared memory
+// (two cluster barriers per column: the norm and the reflector dot products
+// are summed over the cluster in a fixed order).  Writes R into A, the explicit
+// reflectors into V (rows j0..m-1, ld m) and the compact-WY factor Tf.
+constexpr int QR_THREADS = 512;
+
 template <typename R>
-__global__ void __launch_bounds__(256) k_qr_panel(const QrP<R>* __restrict__ P, int j0) {
-  const QrP<R> p = P[blockIdx.x];
-  if (j0 >= p.kf) return;
-  const int m = p.m, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+__global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __restrict__ P, int j0, int cap_rows) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int crank = (int)cl.block_rank();
+  const QrP<R> p = P[blockIdx.x / C];
+  if (j0 >= p.kf) return;  // same for the whole cluster
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  R* pan = reinterpret_cast<R*>(s_raw);  // rows_per x QR_NB, ld rows_per
+  __shared__ R slot1[2];
+  __shared__ R slot2[QR_NB];
+  __shared__ R s_dot[QR_NB];
+  __shared__ R s_tau[QR_NB];
+  __shared__ R sh[32];
+  __shared__ R s_gram[QR_NB][QR_NB + 1];
+  const int m = p.m, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
   const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
+  const int mm = m - j0;
+  const int rows_per = (mm + C - 1) / C;
+  const int r0 = j0 + crank * rows_per, r1 = min(m, r0 + rows_per);
   R* A = p.A;
   const size_t lda = p.lda;
-  R* V = p.V;
-  __shared__ R s_tau[QR_NB];
-  __shared__ R sh[8];
-  __shared__ R s_z[QR_NB][QR_NB];
-  // zero V panel
-  for (long long e = tid; e < (long long)(m - j0) * QR_NB; e += 256) {
-    const int i = (int)(e % (m - j0)), c = (int)(e / (m - j0));
-    V[i + (size_t)c * m] = R(0);
+  (void)cap_rows;
+  for (int e = tid; e < rows_per * QR_NB; e += nt) {
+    const int i = e % rows_per, c = e / rows_per;
+    pan[i + c * rows_per] = (c < nbk && r0 + i < r1) ? A[(r0 + i) + (size_t)(j0 + c) * lda] : R(0);
   }
   __syncthreads();
   for (int j = j0; j < jend; ++j) {
     const int jj = j - j0;
+    // squared norm of the column below the diagonal, summed over the cluster
     R part = R(0);
-    for (int i = j + 1 + tid; i < m; i += 256) {
-      const R v = A[i + j * lda];
+    for (int i = max(j + 1, r0) + tid; i < r1; i += nt) {
+      const R v = pan[(i - r0) + jj * rows_per];
       part += v * v;
     }
-    const R xn2 = block_sum256(part, sh);
-    const R alpha = A[j + j * lda];
+    part = warp_sum(part);
+    __syncthreads();
+    if (lane == 0) sh[w] = part;
+    __syncthreads();
+    if (tid == 0) {
+      R t = R(0);
+      for (int q = 0; q < nw; ++q) t += sh[q];
+      slot1[0] = t;
+      // the owner of row j publishes alpha before anyone may rewrite it
+      if (j >= r0 && j < r1) slot1[1] = pan[(j - r0) + jj * rows_per];
+    }
+    cl.sync();
+    const int oj = (j - j0) / rows_per;
+    R xn2 = R(0);
+    for (int q = 0; q < C; ++q) xn2 += *cl.map_shared_rank(&slot1[0], q);
+    const R alpha = *cl.map_shared_rank(&slot1[1], oj);
     R tau, beta, scal;
-    if (xn2 == R(0)) {
-      tau = R(0); beta = alpha; scal = R(0);
-    } else {
+    if (xn2 == R(0)) { tau = R(0); beta = alpha; scal = R(0); }
+    else {
       beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
       tau = (beta - alpha) / beta;
       scal = R(1) / (alpha - beta);
     }
-    for (int i = j + tid; i < m; i += 256) {
+    if (tid == 0) s_tau[jj] = tau;
+    // reflector into the panel column (v_j = 1 on the diagonal row)
+    for (int i = r0 + tid; i < r1; i += nt) {
+      R* x = pan + (i - r0) + jj * rows_per;
+      if (i > j) *x = *x * scal;
+      else if (i == j) *x = R(1);
+    }
+    __syncthreads();
+    // partial dot products v . a_c for the remaining panel columns
+    for (int c = jj + 1 + w; c < nbk; c += nw) {
+      R d = R(0);
+      for (int i = max(j, r0) + lane; i < r1; i += 32) d += pan[(i - r0) + jj * rows_per] * pan[(i - r0) + c * rows_per];
+      d = warp_sum(d);
+      if (lane == 0) slot2[c] = d;
+    }
+    cl.sync();
+    if (tid < nbk && tid > jj) {
+      R t = R(0);
+      for (int q = 0; q < C; ++q) t += *cl.map_shared_rank(&slot2[tid], q);
+      s_dot[tid] = t * tau;
+    }
+    __syncthreads();
+    for (int e = tid; e < rows_per * nbk; e += nt) {
+      const int i = e % rows_per, c = e / rows_per;
+      const int gi = r0 + i;
+      if (c <= jj || gi >= r1 || gi < j) continue;
+      pan[i + c * rows_per] -= s_dot[c] * pan[i + jj * rows_per];
+    }
+    if (crank == oj && tid == 0) p.diag[j] = fabs(beta);
+    // beta goes to the R diagonal when the panel is written back
+    if (tid == 0) s_dot[jj] = beta;
+    __syncthreads();
+  }
+  // partial Gram matrix V^T V of the own rows
+  for (int e = tid; e < nbk * nbk; e += nt) {
+    const int a = e % nbk, b = e / nbk;
+    R d = R(0);
+    if (a < b)
+      for (int i = r0; i < r1; ++i) {
+        const int gi = i;
+        const R va = (gi >= j0 + a) ? pan[(i - r0) + a * rows_per] : R(0);
+        const R vb = (gi >= j0 + b) ? pan[(i - r0) + b * rows_per] : R(0);
+        d += va * vb;
+      }
+    s_gram[a][b] = d;
+  }
+  // V (explicit, zero above the diagonal) and the panel back to A (R on and above the diagonal)
+  for (int e = tid; e < rows_per * QR_NB; e += nt) {
+    const int i = e % rows_per, c = e / rows_per;
+    const int gi = r0 + i;
+    if (gi >= r1) continue;
+    R v = R(0);
+    if (c < nbk) {
+      const int gj = j0 + c;
+      if (gi > gj) v = pan[i + c * rows_per];
+      else if (gi == gj) v = R(1);
+    }
+    p.V[(gi - j0) + (size_t)c * m] = v;
+  }
+  cl.sync();
+  if (crank == 0) {
+    // rows j0..jend-1 of the panel (R block) are owned by the first CTAs: gather R's
+    // upper triangle and the strict-lower reflector part is not needed in A
+    for (int e = tid; e < nbk * nbk; e += nt) {
+      const int a = e % nbk, b = e / nbk;  // row j0+a, column j0+b
+      if (a > b) continue;
+      const int gi = j0 + a;
+      const int o = (gi - j0) / rows_per;
       R v;
-      if (i == j) v = R(1);
-      else v = A[i + j * lda] * scal;
-      V[(i - j0) + (size_t)jj * m] = v;
+      if (a == b) v = s_dot[b];  // beta of column b (same in every CTA)
+      else v = *cl.map_shared_rank(&pan[(gi - j0 - o * rows_per) + b * rows_per], o);
+      A[gi + (size_t)(j0 + b) * lda] = v;
     }
     if (tid == 0) {
-      s_tau[jj] = tau;
-      p.diag[j] = fabs(beta);
-    }
-    __syncthreads();
-    if (tid == 0) A[j + j * lda] = beta;
-    // apply H_j to the remaining panel columns, one warp per column
-    for (int c = j + 1 + w; c < jend; c += 8) {
-      R d = R(0);
-      for (int i = j + lane; i < m; i += 32) d += V[(i - j0) + (size_t)jj * m] * A[i + c * lda];
-      d = warp_sum(d) * tau;
-      for (int i = j + lane; i < m; i += 32) A[i + c * lda] -= d * V[(i - j0) + (size_t)jj * m];
-    }
-    __syncthreads();
-  }
-  // Gram matrix Z = V^T V (lower part needed), then the T recurrence.
-  for (int pr = w; pr < nbk * nbk; pr += 8) {
-    const int a = pr % nbk, b = pr / nbk;
-    if (a >= b) continue;
-    R d = R(0);
-    for (int i = j0 + b + lane; i < m; i += 32) d += V[(i - j0) + (size_t)a * m] * V[(i - j0) + (size_t)b * m];
-    d = warp_sum(d);
-    if (lane == 0) s_z[a][b] = d;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    R* Tf = p.Tf;
-    for (int b = 0; b < QR_NB; ++b)
-      for (int a = 0; a < QR_NB; ++a) Tf[a + b * QR_NB] = R(0);
-    for (int b = 0; b < nbk; ++b) {
-      Tf[b + b * QR_NB] = s_tau[b];
-      for (int a = 0; a < b; ++a) {
-        R t = R(0);
-        for (int c = a; c < b; ++c) t += Tf[a + c * QR_NB] * s_z[c][b];
-        Tf[a + b * QR_NB] = -s_tau[b] * t;
+      R* Tf = p.Tf;
+      // cluster totals of the Gram entries, stored in place (each entry reads all
+      // ranks, its own included, before it is overwritten)
+      for (int b = 0; b < nbk; ++b)
+        for (int a = 0; a < b; ++a) {
+          R t = R(0);
+          for (int q = 0; q < C; ++q) t += cl.map_shared_rank(&s_gram[0][0], q)[a * (QR_NB + 1) + b];
+          s_gram[a][b] = t;
+        }
+      for (int b = 0; b < QR_NB; ++b)
+        for (int a = 0; a < QR_NB; ++a) Tf[a + b * QR_NB] = R(0);
+      for (int b = 0; b < nbk; ++b) {
+        Tf[b + b * QR_NB] = s_tau[b];
+        for (int a = 0; a < b; ++a) {
+          R t = R(0);
+          for (int c = a; c < b; ++c) t += Tf[a + c * QR_NB] * s_gram[c][b];
+          Tf[a + b * QR_NB] = -s_tau[b] * t;
+        }
       }
     }
   }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // Apply (I - V Tf V^T)^T = I - V Tf^T V^T to A[j0:m, jend:n] in 32-column tiles.
@@ -551,17 +798,22 @@ __global__ void __launch_bounds__(256) k_qr_update(const QrP<R>* __restrict__ P,
   }
 }
 
-// One back-substitution block step: solve R[b0:b1,b0:b1] X = C[b0:b1, tile]
-// and update C[0:b0, tile] -= R[0:b0, b0:b1] X, where C = A[0:kf, kf:n].
+// One back-substitution block step: solve R[b0:b1,b0:b1] X[b0:b1, tile] =
+// C[b0:b1, tile] (C = A[0:kf, kf:n], already updated by the blocks below) and
+// update C[rows of this CTA's chunk of 0:b0, tile] -= R[.., b0:b1] X.  Every
+// CTA of a column tile solves the small block redundantly; blockIdx.y == 0
+// stores it into X, so no CTA reads rows another one writes.
 template <typename R>
 __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P, int blk) {
-  const QrP<R> p = P[blockIdx.y];
+  const QrP<R> p = P[blockIdx.z];
   const int kf = p.kf, ncol = p.n - p.kf;
   const int b0 = blk * 32;
   if (b0 >= kf) return;
   const int b1 = min(b0 + 32, kf), nb = b1 - b0;
   const int c0 = blockIdx.x * 32;
   if (c0 >= ncol) return;
+  const int rc0 = blockIdx.y * 256;
+  if (blockIdx.y > 0 && rc0 >= b0) return;
   const int nc = min(32, ncol - c0);
   R* A = p.A;
   const size_t lda = p.lda;
@@ -575,7 +827,6 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
     Xs[i][j] = (i < nb && j < nc) ? C[(b0 + i) + (size_t)(c0 + j) * lda] : R(0);
   }
   __syncthreads();
-  // each warp solves 4 columns; lane = row
   for (int q = 0; q < 4; ++q) {
     const int cc = w + 8 * q;
     R x = Xs[lane][cc];
@@ -588,20 +839,22 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
     Xs[lane][cc] = x;
   }
   __syncthreads();
-  for (int e = tid; e < 32 * 32; e += 256) {
-    const int i = e & 31, j = e >> 5;
-    if (i < nb && j < nc) C[(b0 + i) + (size_t)(c0 + j) * lda] = Xs[i][j];
+  if (blockIdx.y == 0) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, j = e >> 5;
+      if (i < nb && j < nc) p.X[(b0 + i) + (size_t)(c0 + j) * p.ldx] = Xs[i][j];
+    }
   }
-  // update rows above
-  for (int i = tid; i < b0; i += 256) {
+  const int rend = min(b0, rc0 + 256);
+  for (int i = rc0 + tid; i < rend; i += 256) {
     R rr[32];
 #pragma unroll
     for (int t = 0; t < 32; ++t) rr[t] = (t < nb) ? A[i + (size_t)(b0 + t) * lda] : R(0);
     for (int j = 0; j < nc; ++j) {
-      R s = R(0);
+      R sacc = R(0);
 #pragma unroll
-      for (int t = 0; t < 32; ++t) s += rr[t] * Xs[t][j];
-      C[i + (size_t)(c0 + j) * lda] -= s;
+      for (int t = 0; t < 32; ++t) sacc += rr[t] * Xs[t][j];
+      C[i + (size_t)(c0 + j) * lda] -= sacc;
     }
   }
 }
@@ -610,9 +863,32 @@ template <typename R>
 void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s) {
   if (batch <= 0 || maxkf <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "lstsq batch too large");
+  int C = 1;
+  if (batch < 152 && maxm > 256)
+    while (C < 8 && (maxm + C - 1) / C > 256) C *= 2;
+  while ((size_t)((maxm + C - 1) / C) * QR_NB * sizeof(R) > 200 * 1024 && C < 8) C *= 2;
+  const int cap = (maxm + C - 1) / C;
+  const size_t smem = (size_t)cap * QR_NB * sizeof(R);
+  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "least-squares panel too tall for the cluster (m > 6400)");
+  static bool attr_set = false;
+  if (!attr_set) {
+    HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(batch * C, 1, 1);
+  cfg.blockDim = dim3(QR_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   for (int j0 = 0; j0 < maxkf; j0 += QR_NB) {
-    k_qr_panel<R><<<batch, 256, 0, s>>>(dP, j0);
-    check_launch("k_qr_panel");
+    HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl<R>, dP, j0, cap));
     const int jend = std::min(j0 + QR_NB, maxkf);
     const int ncols = maxn - jend;
     if (ncols > 0) {
@@ -620,10 +896,11 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
       check_launch("k_qr_update");
     }
   }
-  const int nrhs = maxn - 0;  // upper bound of n - kf over the batch
   const int nblk = ceil_div(maxkf, 32);
   for (int blk = nblk - 1; blk >= 0; --blk) {
-    k_trsm_step<R><<<dim3(ceil_div(nrhs, 32), batch), 256, 0, s>>>(dP, blk);
+    const int rows_above = blk * 32;
+    dim3 g(ceil_div(maxn, 32), std::max(1, ceil_div(rows_above, 256)), batch);
+    k_trsm_step<R><<<g, 256, 0, s>>>(dP, blk);
     check_launch("k_trsm_step");
   }
 }

@@ -36,19 +36,21 @@ struct InvP {
   R* A;
   int n, lda;
   int* ipiv;  // n entries
-  R* W;       // GJ_NB x n workspace
+  R* W;       // 2*GJ_NB x n workspace (pivot rows, then displaced rows)
   R* Wfull;   // n x n workspace (final column permutation)
   int* info;  // 0 ok, j+1 if pivot j was exactly zero, -1 non-finite
+  int* aux;   // GJ_AUX ints: row-permutation bookkeeping of the current panel
 };
 constexpr int GJ_NB = 32;
+constexpr int GJ_AUX = 4 * GJ_NB + 4;
 
 template <typename R>
 void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s);
 
 // Least squares X = A(:, 0:kf) \ A(:, kf:n) for tall full-rank problems, by
 // blocked Householder QR of the first kf columns applied to the remaining
-// ones, then a blocked back substitution.  The result overwrites
-// A(0:kf, kf:n).  diag receives |R_ii| (kf entries) for rank diagnostics.
+// ones, then a blocked back substitution into X (A is overwritten).  diag
+// receives |R_ii| (kf entries) for rank diagnostics.
 template <typename R>
 struct QrP {
   R* A;
@@ -56,6 +58,8 @@ struct QrP {
   R* V;     // m x QR_NB workspace (explicit reflectors)
   R* Tf;    // QR_NB x QR_NB workspace (compact-WY factor)
   R* diag;  // kf entries
+  R* X;     // output: kf x (n - kf) solution, leading dimension ldx
+  int ldx;
 };
 constexpr int QR_NB = 32;
 

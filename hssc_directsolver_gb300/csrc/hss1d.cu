@@ -112,14 +112,15 @@ static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t
   for (auto& m : mats) { maxn = std::max(maxn, m.second); tot += (long long)m.second * m.second; }
   long long totn = 0;
   for (auto& m : mats) totn += m.second;
-  DevBuf<int> ipiv(totn), info(nb);
-  DevBuf<double> W((size_t)GJ_NB * totn), Wf(tot);
+  DevBuf<int> ipiv(totn), info(nb), aux((size_t)nb * GJ_AUX);
+  DevBuf<double> W((size_t)2 * GJ_NB * totn), Wf(tot);
   info.zero(s);
   std::vector<InvP<double>> P(nb);
   long long on = 0, o2 = 0;
   for (int i = 0; i < nb; ++i) {
     const int n = mats[i].second;
-    P[i] = InvP<double>{mats[i].first, n, n, ipiv.p + on, W.p + (size_t)GJ_NB * on, Wf.p + o2, info.p + i};
+    P[i] = InvP<double>{mats[i].first, n, n, ipiv.p + on, W.p + (size_t)2 * GJ_NB * on, Wf.p + o2, info.p + i,
+                        aux.p + (size_t)i * GJ_AUX};
     on += n;
     o2 += (long long)n * n;
   }

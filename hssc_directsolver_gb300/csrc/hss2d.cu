@@ -275,17 +275,15 @@ void HSS2D::compute_T(int lev) {
   kgen_batched<double>(dkg.p, batch, (long long)p * n, view(pts), kdev, stream);
   DevBuf<double> V((size_t)batch * p * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * k);
   std::vector<QrP<double>> qp(batch);
-  for (int b = 0; b < batch; ++b)
+  for (int b = 0; b < batch; ++b) {
+    double* X = ((b & 1) ? d.Tdn.p : d.Tup.p) + (size_t)(b / 2) * k * nr;
     qp[b] = QrP<double>{A.p + (size_t)b * p * n, p, n, k, p, V.p + (size_t)b * p * QR_NB,
-                        Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k};
+                        Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k, X, k};
+  }
   DevBuf<QrP<double>> dqp(batch);
   HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
   lstsq_batched<double>(dqp.p, batch, p, n, k, stream);
-  // T_up from even problems, T_dn from odd ones: A(0:k, k:n), ld p
-  k_copy2d<double, double><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(
-      nb, k, nr, A.p + (size_t)k * p, 2LL * p * n, p, d.Tup.p, (long long)k * nr, k);
-  k_copy2d<double, double><<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(
-      nb, k, nr, A.p + (size_t)p * n + (size_t)k * p, 2LL * p * n, p, d.Tdn.p, (long long)k * nr, k);
+  // T_up came from the even problems, T_dn from the odd ones
   k_transpose<<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(nb, k, nr, d.Tdn.p, (long long)k * nr, k,
                                                                      d.TdnT.p, (long long)k * nr, nr);
   check_launch("compute_T copies");
@@ -454,13 +452,13 @@ void HSS2D::invert_impl() {
 
 template <typename R>
 void HSS2D::invert_level(R* A, int n, int nb) {
-  DevBuf<int> ipiv((size_t)nb * n), info(nb);
-  DevBuf<R> W((size_t)nb * GJ_NB * n), Wf((size_t)nb * n * n);
+  DevBuf<int> ipiv((size_t)nb * n), info(nb), aux((size_t)nb * GJ_AUX);
+  DevBuf<R> W((size_t)nb * 2 * GJ_NB * n), Wf((size_t)nb * n * n);
   info.zero(stream);
   std::vector<InvP<R>> P(nb);
   for (int i = 0; i < nb; ++i)
-    P[i] = InvP<R>{A + (size_t)i * n * n, n, n, ipiv.p + (size_t)i * n, W.p + (size_t)i * GJ_NB * n,
-                   Wf.p + (size_t)i * n * n, info.p + i};
+    P[i] = InvP<R>{A + (size_t)i * n * n, n, n, ipiv.p + (size_t)i * n, W.p + (size_t)i * 2 * GJ_NB * n,
+                   Wf.p + (size_t)i * n * n, info.p + i, aux.p + (size_t)i * GJ_AUX};
   DevBuf<InvP<R>> dP(nb);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), nb * sizeof(InvP<R>), cudaMemcpyHostToDevice, stream));
   invert_batched<R>(dP.p, nb, n, stream);
