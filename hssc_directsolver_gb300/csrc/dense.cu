@@ -139,72 +139,141 @@ void gemm_batched(const GemmP<R>* dP, int batch, int maxM, int maxN, bool tA, bo
 
 // ---------------------------------------------------------------------------
 // Skinny GEMM: C (M x N, N <= 8) = alpha*A(M x K)*B(K x N) + beta*C.
-// One block = 32 rows; the 8 warps take interleaved K indices; fixed-order
-// cross-warp reduction.
+//
+// The right-hand-side products of a solve.  A CTA owns 32*V rows (V = 16-byte
+// vector width: 4 floats or 2 doubles per lane); its 8 warps take interleaved
+// k of the CTA's K range; B is staged in shared memory in chunks of SK_KC rows
+// so every k costs one 16-byte load of A and a broadcast shared-memory read of
+// B.  Under-filled launches split K over ksplit CTAs whose partial sums go to a
+// workspace and are added in a fixed order by k_skinny_reduce, so results are
+// bitwise reproducible.
 // ---------------------------------------------------------------------------
-constexpr int SKINNY_NR = 8;
+template <typename R> struct Vec16;
+template <> struct Vec16<float> { using T = float4; static constexpr int V = 4; };
+template <> struct Vec16<double> { using T = double2; static constexpr int V = 2; };
+
+constexpr int SK_KC = 128;
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_gemm_skinny(const GemmP<R>* __restrict__ P, R alpha, R beta) {
-  const GemmP<R> p = P[blockIdx.y];
-  const int row0 = blockIdx.x * 32;
+__device__ __forceinline__ void unpack16(const typename Vec16<R>::T& t, R* a);
+template <>
+__device__ __forceinline__ void unpack16<float>(const float4& t, float* a) { a[0] = t.x; a[1] = t.y; a[2] = t.z; a[3] = t.w; }
+template <>
+__device__ __forceinline__ void unpack16<double>(const double2& t, double* a) { a[0] = t.x; a[1] = t.y; }
+
+template <typename R, int NR>
+__global__ void __launch_bounds__(256) k_skinny(const GemmP<R>* __restrict__ P, R alpha, R beta, int ksplit,
+                                                R* __restrict__ part, int mmax) {
+  using VT = typename Vec16<R>::T;
+  constexpr int V = Vec16<R>::V;
+  constexpr int ROWS = 32 * V;
+  const GemmP<R> p = P[blockIdx.z];
+  const int row0 = blockIdx.x * ROWS;
   if (row0 >= p.M) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int row = row0 + lane;
-  const bool live = row < p.M;
   const int N = p.N;
-  R acc[SKINNY_NR];
+  const int kper = (((p.K + ksplit - 1) / ksplit) + 7) & ~7;
+  const int kb = blockIdx.y * kper, ke = min(p.K, kb + kper);
+  __shared__ __align__(16) R Bs[SK_KC][NR];
+  __shared__ R red[8][NR][ROWS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int r = row0 + lane * V;
+  const bool vec_ok = ((p.lda % V) == 0) && ((reinterpret_cast<uintptr_t>(p.A) & 15) == 0);
+  R acc[V][NR];
 #pragma unroll
-  for (int c = 0; c < SKINNY_NR; ++c) acc[c] = R(0);
-  const R* __restrict__ A = p.A + (live ? row : 0);
-  const R* __restrict__ B = p.B;
-  int k = w;
-  for (; k + 24 < p.K; k += 32) {
-    R a0 = live ? __ldg(A + (size_t)k * p.lda) : R(0);
-    R a1 = live ? __ldg(A + (size_t)(k + 8) * p.lda) : R(0);
-    R a2 = live ? __ldg(A + (size_t)(k + 16) * p.lda) : R(0);
-    R a3 = live ? __ldg(A + (size_t)(k + 24) * p.lda) : R(0);
+  for (int v = 0; v < V; ++v)
 #pragma unroll
-    for (int c = 0; c < SKINNY_NR; ++c) {
-      if (c < N) {
-        const R* bc = B + (size_t)c * p.ldb;
-        acc[c] += a0 * __ldg(bc + k);
-        acc[c] += a1 * __ldg(bc + k + 8);
-        acc[c] += a2 * __ldg(bc + k + 16);
-        acc[c] += a3 * __ldg(bc + k + 24);
+    for (int c = 0; c < NR; ++c) acc[v][c] = R(0);
+  for (int kc = kb; kc < ke; kc += SK_KC) {
+    const int kn = min(SK_KC, ke - kc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < SK_KC * NR; e += 256) {
+      const int kk = e % SK_KC, c = e / SK_KC;
+      Bs[kk][c] = (kk < kn && c < N) ? p.B[(size_t)(kc + kk) + (size_t)c * p.ldb] : R(0);
+    }
+    __syncthreads();
+    for (int kk = w; kk < kn; kk += 8) {
+      const R* col = p.A + (size_t)(kc + kk) * p.lda;
+      R a[V];
+      if (vec_ok && r + V <= p.M) {
+        unpack16<R>(__ldg(reinterpret_cast<const VT*>(col + r)), a);
+      } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) a[v] = (r + v < p.M) ? __ldg(col + r + v) : R(0);
       }
+      R b[NR];
+#pragma unroll
+      for (int c = 0; c < NR; ++c) b[c] = Bs[kk][c];
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) acc[v][c] += a[v] * b[c];
     }
   }
-  for (; k < p.K; k += 8) {
-    R a0 = live ? __ldg(A + (size_t)k * p.lda) : R(0);
 #pragma unroll
-    for (int c = 0; c < SKINNY_NR; ++c)
-      if (c < N) acc[c] += a0 * __ldg(B + (size_t)c * p.ldb + k);
-  }
-  __shared__ R red[8][SKINNY_NR][32];
+  for (int v = 0; v < V; ++v)
 #pragma unroll
-  for (int c = 0; c < SKINNY_NR; ++c) red[w][c][lane] = acc[c];
+    for (int c = 0; c < NR; ++c) red[w][c][lane * V + v] = acc[v][c];
   __syncthreads();
-  if (w == 0 && live) {
+  for (int e = threadIdx.x; e < ROWS * N; e += 256) {
+    const int rr = e % ROWS, c = e / ROWS;
+    const int row = row0 + rr;
+    if (row >= p.M) continue;
+    R t = red[0][c][rr];
 #pragma unroll
-    for (int c = 0; c < SKINNY_NR; ++c) {
-      if (c >= N) break;
-      R t = red[0][c][lane];
-#pragma unroll
-      for (int q = 1; q < 8; ++q) t += red[q][c][lane];
+    for (int q = 1; q < 8; ++q) t += red[q][c][rr];
+    if (ksplit == 1) {
       R* cp = p.C + row + (size_t)c * p.ldc;
       *cp = (beta == R(0)) ? alpha * t : alpha * t + beta * (*cp);
+    } else {
+      part[(((size_t)blockIdx.z * ksplit + blockIdx.y) * mmax + row) * 8 + c] = t;
     }
   }
 }
 
 template <typename R>
-void gemm_skinny(const GemmP<R>* dP, int batch, int maxM, R alpha, R beta, cudaStream_t s) {
+__global__ void __launch_bounds__(256) k_skinny_reduce(const GemmP<R>* __restrict__ P, R alpha, R beta, int ksplit,
+                                                       const R* __restrict__ part, int mmax) {
+  const GemmP<R> p = P[blockIdx.y];
+  for (int e = blockIdx.x * 256 + threadIdx.x; e < p.M * p.N; e += gridDim.x * 256) {
+    const int row = e % p.M, c = e / p.M;
+    R t = R(0);
+    for (int y = 0; y < ksplit; ++y) t += part[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
+    R* cp = p.C + row + (size_t)c * p.ldc;
+    *cp = (beta == R(0)) ? alpha * t : alpha * t + beta * (*cp);
+  }
+}
+
+template <typename R>
+int skinny_ksplit(int batch, int maxM, int maxK) {
+  constexpr int ROWS = 32 * Vec16<R>::V;
+  const long long ctas = (long long)ceil_div(maxM, ROWS) * batch;
+  if (ctas >= 304 || maxK < 256) return 1;
+  int ks = (int)std::min<long long>(16, (304 + ctas - 1) / ctas);
+  ks = std::max(1, std::min(ks, maxK / 128));
+  return ks;
+}
+
+template <typename R>
+void gemm_skinny_split(const GemmP<R>* dP, int batch, int maxM, int maxN, R alpha, R beta, int ksplit, R* part,
+                       cudaStream_t s) {
   if (batch <= 0 || maxM <= 0) return;
-  HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "skinny gemm batch too large");
-  dim3 grid(ceil_div(maxM, 32), batch);
-  k_gemm_skinny<R><<<grid, 256, 0, s>>>(dP, alpha, beta);
-  check_launch("k_gemm_skinny");
+  HSS_REQUIRE(batch <= 65535 && maxN <= 8, HSS_ERR_ARG, "skinny gemm: batch <= 65535 and N <= 8");
+  HSS_REQUIRE(ksplit == 1 || part != nullptr, HSS_ERR_ARG, "skinny gemm: split-K needs a workspace");
+  constexpr int ROWS = 32 * Vec16<R>::V;
+  dim3 grid(ceil_div(maxM, ROWS), ksplit, batch);
+  if (maxN <= 4) k_skinny<R, 4><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  else k_skinny<R, 8><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  check_launch("k_skinny");
+  if (ksplit > 1) {
+    const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 64));
+    k_skinny_reduce<R><<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+    check_launch("k_skinny_reduce");
+  }
+}
+
+template <typename R>
+void gemm_skinny(const GemmP<R>* dP, int batch, int maxM, R alpha, R beta, cudaStream_t s) {
+  gemm_skinny_split<R>(dP, batch, maxM, 8, alpha, beta, 1, nullptr, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1222,6 +1291,8 @@ void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {
 #define HSS_INST(R)                                                                          \
   template void gemm_batched<R>(const GemmP<R>*, int, int, int, bool, bool, R, R, cudaStream_t); \
   template void gemm_skinny<R>(const GemmP<R>*, int, int, R, R, cudaStream_t);               \
+  template void gemm_skinny_split<R>(const GemmP<R>*, int, int, int, R, R, int, R*, cudaStream_t); \
+  template int skinny_ksplit<R>(int, int, int);                                              \
   template void invert_batched<R>(const InvP<R>*, int, int, cudaStream_t);                   \
   template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t);
 HSS_INST(double)

@@ -29,6 +29,13 @@ void gemm_batched(const GemmP<R>* dP, int batch, int maxM, int maxN, bool tA, bo
 // is deterministic (fixed summation order).
 template <typename R>
 void gemm_skinny(const GemmP<R>* dP, int batch, int maxM, R alpha, R beta, cudaStream_t s);
+// split-K variant: ksplit CTAs per row tile write partial sums to `part`
+// (batch * ksplit * maxM * 8 entries), added in a fixed order by a second pass
+template <typename R>
+void gemm_skinny_split(const GemmP<R>* dP, int batch, int maxM, int maxN, R alpha, R beta, int ksplit, R* part,
+                       cudaStream_t s);
+template <typename R>
+int skinny_ksplit(int batch, int maxM, int maxK);
 
 // In-place inversion by blocked Gauss-Jordan with partial (row) pivoting.
 template <typename R>

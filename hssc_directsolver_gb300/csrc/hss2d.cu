@@ -208,9 +208,12 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
   Step st;
   st.batch = (int)P.size();
   st.maxM = 0;
-  for (auto& p : P) st.maxM = std::max(st.maxM, p.M);
+  int maxK = 0;
+  for (auto& p : P) { st.maxM = std::max(st.maxM, p.M); st.maxN = std::max(st.maxN, p.N); maxK = std::max(maxK, p.K); }
   st.alpha = alpha;
   st.beta = beta;
+  st.ksplit = skinny_ksplit<R>(st.batch, st.maxM, maxK);
+  if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
   st.d.alloc(P.size());
   HSS_CUDA(cudaMemcpyAsync(st.d.p, P.data(), P.size() * sizeof(GemmP<R>), cudaMemcpyHostToDevice, s));
   steps.push_back(std::move(st));
@@ -218,7 +221,8 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
 
 template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
-  for (auto& st : steps) gemm_skinny<R>(st.d.p, st.batch, st.maxM, st.alpha, st.beta, s);
+  for (auto& st : steps)
+    gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
 }
 
 template struct SolvePlan<double>;
@@ -338,6 +342,7 @@ void HSS2D::compress() {
     HSS_CUDA(cudaStreamSynchronize(stream));
   }
   compressed = true;
+  g_fwd.clear();
   fwd_plans.clear();
 }
 
@@ -476,6 +481,8 @@ void HSS2D::invert() {
   if (prm.precision == HSS_PREC_MIXED) invert_impl<float>();
   else invert_impl<double>();
   inverted = true;
+  g_inv_d.clear();
+  g_inv_f.clear();
   inv_plans_d.clear();
   inv_plans_f.clear();
 }
@@ -565,10 +572,39 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
   return pl;
 }
 
+// Capture body() on the stream into a graph once per key, then replay it.
+template <typename F>
+static void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&& body) {
+  if (!enabled) {
+    body();
+    return;
+  }
+  auto it = gc.g.find(key);
+  if (it == gc.g.end()) {
+    cudaGraph_t graph = nullptr;
+    HSS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    HSS_CUDA(cudaStreamEndCapture(s, &graph));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    HSS_REQUIRE(e == cudaSuccess, HSS_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    it = gc.g.emplace(key, ex).first;
+  }
+  HSS_CUDA(cudaGraphLaunch(it->second, s));
+}
+
 template <typename R>
 void HSS2D::applyinv_stage(int r) {
-  // vin (N x r, ld N) -> vout
-  inv_plan<R>(r).run(stream);
+  // vin (N x r, ld N) -> vout; the plan is built (and synchronised) before capture
+  SolvePlan<R>& pl = inv_plan<R>(r);
+  run_graph(inv_graphs<R>(), r, stream, use_graphs, [&] { pl.run(stream); });
 }
 
 void HSS2D::ensure_stage() {
@@ -673,6 +709,10 @@ void HSS2D::fwd_prepare(int r) {
 void HSS2D::apply_stage(int r) {
   // Xd (N x r) -> Yd
   fwd_prepare(r);
+  run_graph(g_fwd, r, stream, use_graphs, [&] { apply_stage_body(r); });
+}
+
+void HSS2D::apply_stage_body(int r) {
   FwdPlan& fp = fwd_plans[r];
   const int depth = geo.depth;
   const long long N = geo.N;
@@ -814,6 +854,9 @@ HSS2D::HSS2D(const hss2d_params& p) : prm(p) {
 }
 
 HSS2D::~HSS2D() {
+  g_inv_d.clear();
+  g_inv_f.clear();
+  g_fwd.clear();
   L.clear();
   if (ev) cudaEventDestroy(ev);
   if (stream) cudaStreamDestroy(stream);

@@ -17,13 +17,18 @@ template <typename R>
 struct SolvePlan {
   struct Step {
     DevBuf<GemmP<R>> d;
-    int batch = 0, maxM = 0;
+    DevBuf<R> part;  // split-K partial sums
+    int batch = 0, maxM = 0, maxN = 0, ksplit = 1;
     R alpha = R(1), beta = R(0);
   };
   std::vector<Step> steps;
   void add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s);
   void run(cudaStream_t s) const;
-  int launches() const { return (int)steps.size(); }
+  int launches() const {
+    int n = 0;
+    for (auto& st : steps) n += (st.ksplit > 1) ? 2 : 1;
+    return n;
+  }
 };
 
 struct Level2Dev {
@@ -58,6 +63,20 @@ struct FwdPlan {
   std::vector<SolvePlan<double>> up, lam, eta;
 };
 
+// Instantiated CUDA graphs of fixed launch sequences, keyed by the number of
+// right-hand sides.
+struct GraphCache {
+  std::map<int, cudaGraphExec_t> g;
+  GraphCache() = default;
+  GraphCache(const GraphCache&) = delete;
+  GraphCache& operator=(const GraphCache&) = delete;
+  ~GraphCache() { clear(); }
+  void clear() {
+    for (auto& kv : g) cudaGraphExecDestroy(kv.second);
+    g.clear();
+  }
+};
+
 struct HSS2D {
   hss2d_params prm;
   Tree2D geo;
@@ -73,6 +92,8 @@ struct HSS2D {
   std::map<int, SolvePlan<double>> inv_plans_d;
   std::map<int, SolvePlan<float>> inv_plans_f;
   std::map<int, FwdPlan> fwd_plans;
+  GraphCache g_inv_d, g_inv_f, g_fwd;
+  bool use_graphs = true;
 
   explicit HSS2D(const hss2d_params& p);
   ~HSS2D();
@@ -97,12 +118,18 @@ struct HSS2D {
   template <typename R>
   void applyinv_stage(int r);
   void apply_stage(int r);
+  void apply_stage_body(int r);
   void fwd_prepare(int r);
   void solve_once(const double* f, double* x, int r);
   void ensure_stage();
   void sync_from(cudaStream_t user);
   void sync_to(cudaStream_t user);
 
+  template <typename R>
+  GraphCache& inv_graphs() {
+    if constexpr (std::is_same<R, double>::value) return g_inv_d;
+    else return g_inv_f;
+  }
   template <typename R>
   std::map<int, SolvePlan<R>>& plan_cache() {
     if constexpr (std::is_same<R, double>::value) return inv_plans_d;
