@@ -197,7 +197,9 @@ int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p) {
   HSS_TRY
   HSS_REQUIRE(out != nullptr && p != nullptr, HSS_ERR_ARG, "NULL argument");
   HSS_REQUIRE(p->interform == HSS_INTER_DENSE, HSS_ERR_ARG, "only INTERform 'dense' is supported");
-  HSS_REQUIRE(p->transinv == 0, HSS_ERR_ARG, "only the NTI (transinv = 0) path is supported");
+  HSS_REQUIRE(p->transinv == 0 || p->transinv == 1, HSS_ERR_ARG, "transinv must be 0 or 1");
+  HSS_REQUIRE(p->transinv == 0 || (p->kp.b_alpha == 0.0 && p->kp.c_alpha == 0.0), HSS_ERR_ARG,
+              "translation-invariant mode needs an unmodulated kernel (b = c = 1)");
   HSS_REQUIRE(p->precision == HSS_PREC_FP64 || p->precision == HSS_PREC_MIXED, HSS_ERR_ARG, "bad precision");
   require_device();
   *out = nullptr;
@@ -328,8 +330,9 @@ int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t
   const size_t tcnt = (size_t)g.k * (g.n - g.k);
   if (lev > 0 && tcnt > 0) {
     auto& d = h->L[lev];
-    if (T_up) HSS_CUDA(cudaMemcpy(T_up, d.Tup.p + i * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
-    if (T_dn) HSS_CUDA(cudaMemcpy(T_dn, d.Tdn.p + i * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t fi = h->fo(i);
+    if (T_up) HSS_CUDA(cudaMemcpy(T_up, d.Tup.p + fi * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
+    if (T_dn) HSS_CUDA(cudaMemcpy(T_dn, d.Tdn.p + fi * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
   }
   HSS_CATCH
 }
@@ -345,14 +348,15 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
   const auto& g = h->geo.levels[lev];
   const int i = box - ((1 << lev) - 1);
   auto& d = h->L[lev];
+  const size_t fi = h->fo(i);
   auto fetch = [&](int which, size_t cnt, double* dst) {
     if (!dst) return;
     if (h->prm.precision == HSS_PREC_MIXED) {
       std::vector<float> t(cnt);
-      HSS_CUDA(cudaMemcpy(t.data(), d.ff[which].p + i * cnt, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+      HSS_CUDA(cudaMemcpy(t.data(), d.ff[which].p + fi * cnt, cnt * sizeof(float), cudaMemcpyDeviceToHost));
       for (size_t q = 0; q < cnt; ++q) dst[q] = t[q];
     } else {
-      HSS_CUDA(cudaMemcpy(dst, d.fd[which].p + i * cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+      HSS_CUDA(cudaMemcpy(dst, d.fd[which].p + fi * cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost));
     }
   };
   fetch(0, (size_t)g.n * g.n, FI);

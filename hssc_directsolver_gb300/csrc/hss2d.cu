@@ -26,7 +26,7 @@ namespace hss {
 // small batched kernels
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void k_assemble_F(int nb, int n, int kc, int leaf, const double* __restrict__ Bself,
+__global__ void k_assemble_F(int nb, int n, int kc, int leaf, int ti, const double* __restrict__ Bself,
                              const double* __restrict__ B12, const double* __restrict__ B21,
                              const R* __restrict__ Ech, R* __restrict__ F) {
   const long long per = (long long)n * n;
@@ -43,10 +43,11 @@ __global__ void k_assemble_F(int nb, int n, int kc, int leaf, const double* __re
       const int ii = i - bi * kc, jj = j - bj * kc;
       const long long o = ii + (long long)jj * kc;
       const long long kk = (long long)kc * kc;
-      if (!bi && !bj) v = Ech[(2LL * b) * kk + o];
+      const long long e1 = ti ? 0 : 2LL * b, e2 = ti ? 0 : 2LL * b + 1;
+      if (!bi && !bj) v = Ech[e1 * kk + o];
       else if (!bi && bj) v = (R)B12[(long long)b * kk + o];
       else if (bi && !bj) v = (R)B21[(long long)b * kk + o];
-      else v = Ech[(2LL * b + 1) * kk + o];
+      else v = Ech[e2 * kk + o];
     }
     F[e] = v;
   }
@@ -258,7 +259,7 @@ void HSS2D::build_tree() {
 void HSS2D::compute_T(int lev) {
   auto& g = geo.levels[lev];
   auto& d = L[lev];
-  const int nb = g.nb, n = g.n, k = g.k, p = g.p, nr = n - k;
+  const int nb = nf(g), n = g.n, k = g.k, p = g.p, nr = n - k;
   d.Tup.alloc((size_t)nb * k * std::max(nr, 1));
   d.Tdn.alloc((size_t)nb * k * std::max(nr, 1));
   d.TdnT.alloc((size_t)nb * k * std::max(nr, 1));
@@ -313,23 +314,23 @@ void HSS2D::compress() {
   {
     auto& g = geo.levels[depth];
     auto& d = L[depth];
-    d.Bself.alloc((size_t)g.nb * g.n * g.n);
-    for (int i = 0; i < g.nb; ++i)
+    d.Bself.alloc((size_t)nf(g) * g.n * g.n);
+    for (int i = 0; i < nf(g); ++i)
       kg.push_back(KgenP<double>{d.Isrc.p + (size_t)i * g.n, d.Isrc.p + (size_t)i * g.n, g.n, g.n,
-                                 d.Bself.p + (size_t)i * g.n * g.n, g.n, 0});
+                                 d.Bself.p + fo(i) * g.n * g.n, g.n, 0});
   }
   for (int lev = 0; lev < depth; ++lev) {
     auto& gc = geo.levels[lev + 1];
     auto& dc = L[lev + 1];
     auto& d = L[lev];
-    const int nb = geo.levels[lev].nb, kc = gc.k, nc = gc.n;
+    const int nb = nf(geo.levels[lev]), kc = gc.k, nc = gc.n;
     d.B12.alloc((size_t)nb * kc * kc);
     d.B21.alloc((size_t)nb * kc * kc);
-    for (int i = 0; i < nb; ++i) {
+    for (int i = 0; i < nb; ++i) {  // nb = factor boxes (1 in translation-invariant mode)
       const int* s1 = dc.IsrcJ.p + (size_t)(2 * i) * nc;
       const int* s2 = dc.IsrcJ.p + (size_t)(2 * i + 1) * nc;
-      kg.push_back(KgenP<double>{s1, s2, kc, kc, d.B12.p + (size_t)i * kc * kc, kc, 0});
-      kg.push_back(KgenP<double>{s2, s1, kc, kc, d.B21.p + (size_t)i * kc * kc, kc, 0});
+      kg.push_back(KgenP<double>{s1, s2, kc, kc, d.B12.p + fo(i) * kc * kc, kc, 0});
+      kg.push_back(KgenP<double>{s2, s1, kc, kc, d.B21.p + fo(i) * kc * kc, kc, 0});
     }
   }
   long long maxe = 0;
@@ -359,7 +360,7 @@ void HSS2D::invert_impl() {
   for (int lev = depth; lev >= 0; --lev) {
     auto& g = geo.levels[lev];
     auto& d = L[lev];
-    const int nb = g.nb, n = g.n, k = g.k, nr = n - k;
+    const int nb = nf(g), n = g.n, k = g.k, nr = n - k;
     const bool leaf = (lev == depth);
     const int kc = leaf ? 0 : geo.levels[lev + 1].k;
     auto& FIb = d.fac<R>(0);
@@ -367,7 +368,7 @@ void HSS2D::invert_impl() {
     R* FI = FIb.p;
     const R* Ech = leaf ? nullptr : L[lev + 1].fac<R>(1).p;
     k_assemble_F<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(
-        nb, n, kc, leaf ? 1 : 0, leaf ? d.Bself.p : nullptr, leaf ? nullptr : d.B12.p,
+        nb, n, kc, leaf ? 1 : 0, prm.transinv ? 1 : 0, leaf ? d.Bself.p : nullptr, leaf ? nullptr : d.B12.p,
         leaf ? nullptr : d.B21.p, Ech, FI);
     check_launch("k_assemble_F");
     invert_level<R>(FI, n, nb);
@@ -529,7 +530,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
-      P.push_back(GemmP<R>{d.fac<R>(2).p + (size_t)i * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
+      P.push_back(GemmP<R>{d.fac<R>(2).p + fo(i) * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
                            g.k, ldq, g.nb * g.k});
     }
     pl.add(P, R(1), R(0), stream);
@@ -554,11 +555,11 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
-      P1.push_back(GemmP<R>{d.fac<R>(0).p + (size_t)i * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
+      P1.push_back(GemmP<R>{d.fac<R>(0).p + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
       if (lev > 0) {
-        P2.push_back(GemmP<R>{d.fac<R>(3).p + (size_t)i * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
+        P2.push_back(GemmP<R>{d.fac<R>(3).p + fo(i) * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
                               g.k, g.n, g.nb * g.k, ldo});
-        P3.push_back(GemmP<R>{d.fac<R>(4).p + (size_t)i * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
+        P3.push_back(GemmP<R>{d.fac<R>(4).p + fo(i) * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
                               g.k, g.n, g.nb * g.k, ldo});
       }
     }
@@ -663,7 +664,7 @@ void HSS2D::fwd_prepare(int r) {
     if (nr > 0) {
       std::vector<GemmP<double>> P;
       for (int i = 0; i < g.nb; ++i)
-        P.push_back(GemmP<double>{d.Tup.p + (size_t)i * g.k * nr, d.rsF.p + (size_t)i * nr,
+        P.push_back(GemmP<double>{d.Tup.p + fo(i) * g.k * nr, d.rsF.p + (size_t)i * nr,
                                   d.upF.p + (size_t)i * g.k, g.k, r, nr, g.k, g.nb * nr, g.nb * g.k});
       fp.up[lev].add(P, 1.0, 1.0, stream);
     }
@@ -679,7 +680,7 @@ void HSS2D::fwd_prepare(int r) {
         const int b = (1 << lev) - 1 + i;
         out = Yd.p + (size_t)NG * geo.leaf_panel[b];
         ldo = (int)N;
-        P.push_back(GemmP<double>{d.Bself.p + (size_t)i * g.n * g.n, Xd.p + (size_t)NG * geo.leaf_panel[b], out, g.n,
+        P.push_back(GemmP<double>{d.Bself.p + fo(i) * g.n * g.n, Xd.p + (size_t)NG * geo.leaf_panel[b], out, g.n,
                                   r, g.n, g.n, (int)N, ldo});
       } else {
         const auto& gc = geo.levels[lev + 1];
@@ -687,9 +688,9 @@ void HSS2D::fwd_prepare(int r) {
         out = dc.dnF.p + (size_t)(2 * i) * gc.k;
         ldo = gc.nb * gc.k;
         const int kc = gc.k;
-        P.push_back(GemmP<double>{d.B12.p + (size_t)i * kc * kc, dc.upF.p + (size_t)(2 * i + 1) * kc, out, kc, r, kc,
+        P.push_back(GemmP<double>{d.B12.p + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i + 1) * kc, out, kc, r, kc,
                                   kc, gc.nb * kc, ldo});
-        P.push_back(GemmP<double>{d.B21.p + (size_t)i * kc * kc, dc.upF.p + (size_t)(2 * i) * kc, out + kc, kc, r, kc,
+        P.push_back(GemmP<double>{d.B21.p + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i) * kc, out + kc, kc, r, kc,
                                   kc, gc.nb * kc, ldo});
       }
     }
@@ -698,7 +699,7 @@ void HSS2D::fwd_prepare(int r) {
     if (lev > 0 && nr > 0) {
       std::vector<GemmP<double>> Q;
       for (int i = 0; i < g.nb; ++i)
-        Q.push_back(GemmP<double>{d.TdnT.p + (size_t)i * g.k * nr, d.dnF.p + (size_t)i * g.k,
+        Q.push_back(GemmP<double>{d.TdnT.p + fo(i) * g.k * nr, d.dnF.p + (size_t)i * g.k,
                                   d.tmF.p + (size_t)i * nr, nr, r, g.k, nr, g.nb * g.k, g.nb * nr});
       fp.eta[lev].add(Q, 1.0, 0.0, stream);
     }

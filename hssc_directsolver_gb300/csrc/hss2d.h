@@ -107,6 +107,10 @@ struct HSS2D {
   void solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres, int* iters,
                     cudaStream_t user);
   long long solve_bytes() const;
+  // Translation-invariant mode keeps one factor set per level: nf() boxes
+  // carry factors, box i of a level uses factor box fo(i).
+  int nf(const Level2Geom& g) const { return prm.transinv ? 1 : g.nb; }
+  size_t fo(int i) const { return prm.transinv ? 0 : (size_t)i; }
   int solve_launches(int nrhs) const;
 
   template <typename R>

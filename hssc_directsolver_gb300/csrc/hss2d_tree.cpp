@@ -223,8 +223,15 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
       }
       std::vector<int> Jb;
       int kb = 0;
-      preset_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad,
-                      prm.layers, hh, Jb, kb);
+      if (prm.transinv && i > 0) {
+        // translation-invariant mode: every box of the level uses box 0's J and k
+        // (INFO_TREE.LEV(l) of HSS2D_build_tree_nsym.m:438-449, 499-540)
+        Jb.assign(L.J.begin(), L.J.begin() + L.n);
+        kb = L.k;
+      } else {
+        preset_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad,
+                        prm.layers, hh, Jb, kb);
+      }
       const int n = (int)I_src[b].size();
       if (i == 0) { L.n = n; L.k = kb; }
       HSS_REQUIRE(n == L.n && kb == L.k, HSS_ERR_ARG, "non-uniform level sizes");

@@ -70,6 +70,7 @@ def HSS_tree_parameters(pot: str, kh: float, sym: int, Ng: int, npan: int, acc: 
     """Common/HSS_tree_parameters.m:108-139 for the Laplace kernel (kh = 0)."""
     if kh != 0:
         raise ValueError("the oscillatory kernels are not part of the GPU path")
+    # transinv = 1 keeps one factor set per tree level (INFO_TREE.LEV); the kernel has b = c = 1
     b, c = reference_modulations(sym, proxy, TI)
     return HSS2DParams(Ng=Ng, npan=npan, acc=acc, layers=lay, kernel=Kernel(pot, 2.0 / (Ng * npan), b, c),
                        transinv=TI, sym=sym, n_cut=n_cut)

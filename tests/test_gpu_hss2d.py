@@ -122,3 +122,29 @@ def test_status_codes(gpu):
     with pytest.raises(L.HSSError) as e:
         G2.HSS2D_solve(t, f, 1e-10, 2)
     assert e.value.code == L.HSS_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("npan", [4, 8])
+def test_translation_invariant_mode(gpu, npan):
+    """transinv = 1 (one factor set per level, INFO_TREE.LEV) on the unmodulated kernel agrees with
+    the per-box (NTI) oracle, whose boxes of a level are all translates of each other."""
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    Ng = 8
+    h = 2.0 / (Ng * npan)
+    gp = G2.HSS2DParams(Ng=Ng, npan=npan, kernel=GK.Kernel("SL_L_2D", h), transinv=1)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(gp))
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=h)
+    prm = O2.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    ot = O2.build_tree_nsym(prm)
+    blk = O2.compress_nsym(ot, prm)
+    inv = O2.invert_nsym(ot, prm, blk)
+    f = np.random.default_rng(9).standard_normal((prm.N, 3))
+    x = G2.HSS2D_applyinv_nsym(t, None, f)
+    xo = O2.applyinv_nsym(ot, inv, f)
+    assert np.linalg.norm(x - xo) <= 1e-11 * np.linalg.norm(xo)
+    u = G2.HSS2D_apply_nsym(t, None, f)
+    assert np.linalg.norm(u - O2.apply_nsym(ot, blk, f)) <= 1e-12 * np.linalg.norm(u)
+    with pytest.raises(Exception):
+        G2.HSS2D_build_tree_nsym(G2.HSS2DParams(Ng=Ng, npan=npan, transinv=1,
+                                                kernel=GK.Kernel("SL_L_2D", h, GK.Modulation(),
+                                                                 GK.Modulation(0.5, 0, 0, 20.0))))
