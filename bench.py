@@ -161,6 +161,51 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+def bench_batched(args, L, dev):
+    """The batched-curves workload: 512 double-layer curves r = 1 + sum_k a_k cos(k t + phi_k)
+    (a_k ~ U(0, 0.3/k), k <= 8), N log-uniform in [1024, 16384], leaf 64, tol 1e-10, 8 RHS per
+    curve, all curves compressed / inverted / solved as one forest (FP64)."""
+    import torch
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(args.curves, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    t1 = time.perf_counter()
+    G1.HSS1D_invert_nsym(H)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    Nt = sum(sizes)
+    F = np.random.default_rng(0).standard_normal((8, Nt))
+    dF = torch.from_numpy(F).to(dev)
+    dX = torch.zeros_like(dF)
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    rr = C.c_double()
+    it = C.c_int32()
+
+    def solve():
+        L.check(L.lib().hss1d_solve_device(H._h, L.ptr(dF), L.ptr(dX), 8, 1e-10, 4, C.byref(rr), C.byref(it), sp))
+
+    for _ in range(2):
+        solve()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    steps = max(3, args.steps // 4)
+    e0.record(stream)
+    for _ in range(steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": f"{args.curves} Laplace double-layer curves, N log-uniform [1024,16384] "
+                        f"(total {Nt}), leaf 64, tol 1e-10, 8 RHS each, one forest",
+            "compress_s": t1 - t0, "invert_s": t2 - t1, "compress_invert_s": t2 - t0,
+            "solve_ms": ms, "solves_per_s": 1e3 / ms, "relres": rr.value, "solves_used": it.value,
+            "dtype": "f64"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,6 +214,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--npan", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-curve batched HSS1D section")
+    ap.add_argument("--curves", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -279,6 +326,10 @@ def main():
         del tree
         torch.cuda.empty_cache()
 
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched(args, L, dev)
+
     ok = [p for p in ("mixed", "fp64") if results[p]["relres"] <= 1e-10]
     best = min(ok, key=lambda p: results[p]["solve_ms"]) if ok else "fp64"
     r = results[best]
@@ -317,6 +368,8 @@ def main():
         "gpu_launches": int(args.steps * launches_per_solve),
         "clocks": r["clocks"],
     }
+    if batched is not None:
+        line["batched_hss1d"] = batched
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cores = os.cpu_count() or 1

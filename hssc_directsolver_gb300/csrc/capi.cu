@@ -77,22 +77,56 @@ int hss_device_count(int* count) {
 }
 
 // ---------------------------------------------------------------- HSS1D --
-int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf, double acc,
-                   const hss_kernel_params* kp, uint64_t seed) {
-  HSS_TRY
-  HSS_REQUIRE(out && X && kp, HSS_ERR_ARG, "NULL argument");
+static void hss1d_make(hss1d_matrix** out, int nprob, const long long* N, const double* const* X,
+                       const long long* ldx, int leaf, double acc, const hss_kernel_params* kp,
+                       const unsigned long long* seeds) {
+  HSS_REQUIRE(out && X && kp && N && ldx, HSS_ERR_ARG, "NULL argument");
   require_device();
   *out = nullptr;
   auto* h = new hss1d_matrix{nullptr};
   try {
     h->impl = new HSS1D();
-    h->impl->compress(X, N, ldx, leaf, acc, *kp, seed);
+    h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds);
   } catch (...) {
     delete h->impl;
     delete h;
     throw;
   }
   *out = h;
+}
+
+int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf, double acc,
+                   const hss_kernel_params* kp, uint64_t seed) {
+  HSS_TRY
+  const long long n = N, l = ldx;
+  const unsigned long long sd = seed;
+  hss1d_make(out, 1, &n, &X, &l, leaf, acc, kp, &sd);
+  HSS_CATCH
+}
+
+int hss1d_compress_batch(hss1d_matrix** out, int32_t nprob, const int64_t* N, const double* const* X,
+                         const int64_t* ldx, int32_t leaf, double acc, const hss_kernel_params* kp,
+                         const uint64_t* seeds) {
+  HSS_TRY
+  HSS_REQUIRE(nprob >= 1 && N && ldx, HSS_ERR_ARG, "bad batch arguments");
+  std::vector<long long> n(N, N + nprob), l(ldx, ldx + nprob);
+  std::vector<unsigned long long> sd(nprob, 0ULL);
+  if (seeds)
+    for (int p = 0; p < nprob; ++p) sd[p] = seeds[p];
+  hss1d_make(out, nprob, n.data(), X, l.data(), leaf, acc, kp, sd.data());
+  HSS_CATCH
+}
+
+int hss1d_forest_info(const hss1d_matrix* H, int32_t* nprob, int64_t* Ntot, int32_t* root, int64_t* pbase) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS1D* h = H->impl;
+  if (nprob) *nprob = h->nprob;
+  if (Ntot) *Ntot = h->Ntot;
+  for (int p = 0; p < h->nprob; ++p) {
+    if (root) root[p] = h->proot[p];
+    if (pbase) pbase[p] = h->pbase[p];
+  }
   HSS_CATCH
 }
 
@@ -120,7 +154,8 @@ int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
   const HSS1D* h = H->impl;
-  HSS_REQUIRE(box >= 1 && box < h->nboxes, HSS_ERR_ARG, "box out of range (the root has no skeleton)");
+  HSS_REQUIRE(box >= 0 && box < h->nboxes && h->parent[box] >= 0, HSS_ERR_ARG,
+              "box out of range (a root has no skeleton)");
   const int n = h->nskel[box], k = h->kskel[box];
   if (I_skup) std::memcpy(I_skup, h->I_SKUP[box].data(), k * sizeof(int32_t));
   if (I_skdn) std::memcpy(I_skdn, h->I_SKDN[box].data(), k * sizeof(int32_t));
@@ -143,7 +178,7 @@ int hss1d_invert(hss1d_matrix* H) {
 
 static void host_roundtrip1(HSS1D* h, const double* X, double* Y, int nrhs, bool inv) {
   HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
-  const size_t cnt = (size_t)h->N * nrhs;
+  const size_t cnt = (size_t)h->Ntot * nrhs;
   DevBuf<double> dX(cnt), dY(cnt);
   HSS_CUDA(cudaMemcpyAsync(dX.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   if (inv) h->applyinv_device(dX.p, dY.p, nrhs);
@@ -180,6 +215,40 @@ int hss1d_applyinv_device(hss1d_matrix* H, const double* d_ff, double* d_xx, int
   if (s) HSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
   else HSS_CUDA(cudaStreamSynchronize(h->stream));
   cudaEventDestroy(ev);
+  HSS_CATCH
+}
+
+int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, double tol, int32_t maxit,
+                double* relres, int32_t* iters) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && f && x && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
+  HSS1D* h = H->impl;
+  const size_t cnt = (size_t)h->Ntot * nrhs;
+  DevBuf<double> dF(cnt), dX(cnt);
+  HSS_CUDA(cudaMemcpyAsync(dF.p, f, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int it = 0;
+  h->solve_device(dF.p, dX.p, nrhs, tol, maxit, relres, &it);
+  HSS_CUDA(cudaMemcpyAsync(x, dX.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaStreamSynchronize(h->stream));
+  if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol, int32_t maxit,
+                       double* relres, int32_t* iters, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && d_f && d_x && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
+  HSS1D* h = H->impl;
+  cudaStream_t s = as_stream(stream);
+  cudaEvent_t ev;
+  HSS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (s) { HSS_CUDA(cudaEventRecord(ev, s)); HSS_CUDA(cudaStreamWaitEvent(h->stream, ev, 0)); }
+  int it = 0;
+  h->solve_device(d_f, d_x, nrhs, tol, maxit, relres, &it);
+  HSS_CUDA(cudaEventRecord(ev, h->stream));
+  if (s) HSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  cudaEventDestroy(ev);
+  if (iters) *iters = it;
   HSS_CATCH
 }
 
@@ -436,10 +505,10 @@ int hss_batched_id_device(const double* d_A, int32_t m, int32_t n, int32_t batch
   for (int b = 0; b < batch; ++b)
     P[b] = IdP{d_A + (size_t)b * m * n, W.p + (size_t)b * m * n, m, n, d_perm + (size_t)b * n, d_rank + b,
                d_T + (size_t)b * n * n, -1, SW.p + (size_t)b * n * n, SV.p + (size_t)b * n * n,
-               x.p + (size_t)b * 2 * n, y.p + (size_t)b * (m + n), b, 0};
+               x.p + (size_t)b * 2 * n, y.p + (size_t)b * (m + n), b, 0, (unsigned long long)seed};
   DevBuf<IdP> dP(batch);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(IdP), cudaMemcpyHostToDevice, s));
-  id_adaptive_batched(dP.p, batch, acc, seed, s);
+  id_adaptive_batched(dP.p, batch, acc, s);
   if (force_k >= 0) {
     for (auto& q : P) q.force_k = force_k;
     HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(IdP), cudaMemcpyHostToDevice, s));

@@ -1070,9 +1070,9 @@ __device__ double id_rand_error(const IdP& p, int k, const double* T, const doub
   return sqrt(sqrt(z2));
 }
 
-__global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, double acc,
-                                                     unsigned long long seed) {
+__global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, double acc) {
   const IdP p = P[blockIdx.x];
+  const unsigned long long seed = p.seed;
   const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int l = min(m, n);
   double* W = p.W;
@@ -1190,10 +1190,10 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
   if (tid == 0) *p.rank = k;
 }
 
-void id_adaptive_batched(const IdP* dP, int batch, double acc, unsigned long long seed, cudaStream_t s) {
+void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s) {
   if (batch <= 0) return;
   // dynamic shared memory: norms (n doubles); the host guarantees n <= 4096
-  k_id_adaptive<<<batch, 256, 4096 * sizeof(double), s>>>(dP, acc, seed);
+  k_id_adaptive<<<batch, 256, 4096 * sizeof(double), s>>>(dP, acc);
   check_launch("k_id_adaptive");
 }
 

@@ -87,12 +87,12 @@ struct IdP {
   double* svdV;     // n x n workspace (fixed-rank mode)
   double* x;        // 2*n workspace (random vectors)
   double* y;        // m+n workspace
-  int problem;      // id for the random stream
-  int status;       // padding / spare
+  int problem;      // id for the random stream (2*box + side, box local to its tree)
+  int status;       // spare
+  unsigned long long seed;  // key of the random stream (one per independent problem)
 };
 
-void id_adaptive_batched(const IdP* dP, int batch, double acc, unsigned long long seed,
-                         cudaStream_t s);
+void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s);
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s);
 
 }  // namespace hss

@@ -126,7 +126,12 @@ static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t
   }
   DevBuf<InvP<double>> dP;
   upload_vec(dP, P, s);
-  invert_batched<double>(dP.p, nb, maxn, s);
+  for (int o = 0; o < nb; o += 65535) {
+    int mx = 0;
+    const int cnt = std::min(65535, nb - o);
+    for (int i = o; i < o + cnt; ++i) mx = std::max(mx, mats[i].second);
+    invert_batched<double>(dP.p + o, cnt, mx, s);
+  }
   std::vector<int> hi;
   download(hi, info.p, nb, s);
   HSS_CUDA(cudaStreamSynchronize(s));
@@ -172,20 +177,36 @@ HSS1D::~HSS1D() {
   if (stream) cudaStreamDestroy(stream);
 }
 
-void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, double acc_,
-                     const hss_kernel_params& kp_, unsigned long long seed_) {
-  HSS_REQUIRE(Xh && N_ >= 2 && ldx >= N_ && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
+void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, const long long* ldx, int leaf_,
+                     double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds) {
+  HSS_REQUIRE(np_ >= 1 && Np && Xp && ldx && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
   HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
-  HSS_REQUIRE(N_ < (1LL << 30), HSS_ERR_ARG, "N too large");
-  N = N_; leaf = leaf_; acc = acc_; kp = kp_; seed = seed_;
+  nprob = np_; leaf = leaf_; acc = acc_; kp = kp_;
   kdev = make_kernel_dev(kp);
-  X.resize(6 * (size_t)N);
-  for (long long i = 0; i < N; ++i)
-    for (int c = 0; c < 6; ++c) X[6 * i + c] = Xh[i + c * ldx];
-  // ---- tree (LOCAL_get_tree, :277-334)
-  level = {0}; parent = {-1}; c1 = {-1}; c2 = {-1}; off = {0}; cnt = {(int)N};
-  {
-    int last = -1, created = 1, ilev = 0;
+  pN.assign(Np, Np + nprob);
+  pbase.assign(nprob, 0);
+  pseed.assign(nprob, 0);
+  Ntot = 0;
+  for (int p = 0; p < nprob; ++p) {
+    HSS_REQUIRE(Xp[p] && pN[p] >= 2 && ldx[p] >= pN[p], HSS_ERR_ARG, "bad problem size");
+    pbase[p] = Ntot;
+    Ntot += pN[p];
+    pseed[p] = seeds ? seeds[p] : 0ULL;
+  }
+  HSS_REQUIRE(Ntot < (1LL << 30), HSS_ERR_ARG, "total points too large");
+  X.resize(6 * (size_t)Ntot);
+  for (int p = 0; p < nprob; ++p)
+    for (long long i = 0; i < pN[p]; ++i)
+      for (int c = 0; c < 6; ++c) X[6 * (pbase[p] + i) + c] = Xp[p][i + c * ldx[p]];
+  // ---- trees (LOCAL_get_tree, :277-334), one per problem, global box ids
+  prob.clear(); level.clear(); parent.clear(); c1.clear(); c2.clear(); off.clear(); cnt.clear();
+  proot.assign(nprob, 0);
+  for (int p = 0; p < nprob; ++p) {
+    const int g0 = (int)level.size();
+    proot[p] = g0;
+    prob.push_back(p); level.push_back(0); parent.push_back(-1); c1.push_back(-1); c2.push_back(-1);
+    off.push_back((int)pbase[p]); cnt.push_back((int)pN[p]);
+    int last = g0 - 1, created = 1, ilev = 0;
     while (created > 0) {
       const int first = last + 1;
       last = last + created;
@@ -198,6 +219,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
           c1[b] = s1;
           c2[b] = s1 + 1;
           for (int t = 0; t < 2; ++t) {
+            prob.push_back(p);
             level.push_back(ilev + 1);
             parent.push_back(b);
             c1.push_back(-1);
@@ -210,14 +232,14 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
       }
       ++ilev;
     }
+    HSS_REQUIRE((int)level.size() - g0 >= 3, HSS_ERR_ARG, "each problem must exceed the leaf size (one split)");
   }
   nboxes = (int)level.size();
-  HSS_REQUIRE(nboxes >= 3, HSS_ERR_ARG, "N must exceed the leaf size (at least one split)");
   maxlev = *std::max_element(level.begin(), level.end());
-  // ---- neighbour lists (:376-412)
+  // ---- neighbour lists (:376-412), boxes in increasing global id (parents first)
   std::vector<std::vector<int>> nei(nboxes);
-  nei[0] = {0};
-  for (int b = 1; b < nboxes; ++b) {
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) { nei[b] = {b}; continue; }
     std::vector<int> r(cnt[b]);
     std::iota(r.begin(), r.end(), off[b]);
     double xc, yc, R;
@@ -237,16 +259,18 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
       if (mn < rr) nei[b].push_back(j);
     }
   }
-  for (int b = 1; b < nboxes; ++b) {
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
     auto& l = nei[b];
     l.erase(std::remove(l.begin(), l.end(), b), l.end());
     std::sort(l.begin(), l.end());
   }
-  // ---- point table: N points + NPROXY proxies per box
-  const size_t npts = (size_t)N + (size_t)NPROXY * nboxes;
+  // ---- point table: Ntot points + NPROXY proxies per box
+  const size_t npts = (size_t)Ntot + (size_t)NPROXY * nboxes;
+  HSS_REQUIRE(npts < (1ULL << 31), HSS_ERR_ARG, "point table exceeds 2^31 entries");
   std::vector<double> hx(npts, 0.0), hy(npts, 0.0), hnx(npts, 0.0), hny(npts, 0.0), hw(npts, 0.0),
       hk(npts, 0.0);
-  for (long long i = 0; i < N; ++i) {
+  for (long long i = 0; i < Ntot; ++i) {
     hx[i] = X[6 * i]; hy[i] = X[6 * i + 1]; hnx[i] = X[6 * i + 2]; hny[i] = X[6 * i + 3];
     hw[i] = X[6 * i + 4]; hk[i] = X[6 * i + 5];
   }
@@ -256,13 +280,13 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
   I_SKDN.assign(nboxes, {});
   J_UP.assign(nboxes, {});
   J_DN.assign(nboxes, {});
+  census.assign(4 * (size_t)nboxes, 0);
   std::vector<DevBuf<double>> Tkeep;  // per level: T of each ID problem (n x n, ld n)
   std::vector<std::vector<long long>> Toff(nboxes);
   std::vector<int> Tlev(nboxes, -1);
-  // proxy geometry needs the skeletons of the level below: compute per level
   for (int L = maxlev; L >= 1; --L) {
     std::vector<int> boxes;
-    for (int b = 1; b < nboxes; ++b)
+    for (int b = 0; b < nboxes; ++b)
       if (level[b] == L) boxes.push_back(b);
     if (boxes.empty()) continue;
     const int nbL = (int)boxes.size();
@@ -291,7 +315,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
       // LOCAL_construct_circle: tt = linspace(0, 2 pi (1 - 1/n), n)
       const double stop = 2.0 * M_PI * (1.0 - 1.0 / NPROXY);
       const double step = stop / (double)(NPROXY - 1);
-      const size_t pb = (size_t)N + (size_t)NPROXY * b;
+      const size_t pb = (size_t)Ntot + (size_t)NPROXY * b;
       for (int t = 0; t < NPROXY; ++t) {
         const double tt = (t == NPROXY - 1) ? stop : (double)t * step;
         const double c = std::cos(tt), s = std::sin(tt);
@@ -302,7 +326,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
         hw[pb + t] = 2.0 * M_PI * Rp / NPROXY;
         hk[pb + t] = 1.0 / Rp;
       }
-      std::vector<int> out_maybe, in_maybe;
+    std::vector<int> out_maybe, in_maybe;
       for (int j : nei[b]) {
         if (is_leaf(j)) {
           for (int i = off[j]; i < off[j] + cnt[j]; ++i) { out_maybe.push_back(i); in_maybe.push_back(i); }
@@ -349,10 +373,10 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
     }
     DevBuf<int> didx;
     upload_vec(didx, idx, stream);
-    const int nprob = 2 * nbL;
-    std::vector<long long> oA(nprob), oT2(nprob), oX(nprob), oY(nprob), oP(nprob);
+    const int nprob2 = 2 * nbL;
+    std::vector<long long> oA(nprob2), oT2(nprob2), oX(nprob2), oY(nprob2), oP(nprob2);
     long long tA = 0, tT = 0, tX = 0, tY = 0, tP = 0;
-    std::vector<int> pm(nprob), pn(nprob);
+    std::vector<int> pm(nprob2), pn(nprob2);
     for (int q = 0; q < nbL; ++q) {
       for (int s = 0; s < 2; ++s) {
         const int pr = 2 * q + s;
@@ -369,30 +393,33 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
     DevBuf<double> A(tA), W(tA), SW(tT), SV(tT), xw(tX), yw(tY);
     Tkeep.emplace_back(tT);
     DevBuf<double>& Tb = Tkeep.back();
-    DevBuf<int> perm(tP), rank(nprob);
-    std::vector<KgenP<double>> kg(nprob);
-    std::vector<IdP> ip(nprob);
+    DevBuf<int> perm(tP), rank(nprob2);
+    std::vector<KgenP<double>> kg(nprob2);
+    std::vector<IdP> ip(nprob2);
     for (int q = 0; q < nbL; ++q) {
       const int n = (int)outs[q].size();
       kg[2 * q] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[2 * q], n, A.p + oA[2 * q], pm[2 * q], 0};
       kg[2 * q + 1] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], n, pm[2 * q + 1], A.p + oA[2 * q + 1],
                                     pm[2 * q + 1], 1};
     }
-    for (int pr = 0; pr < nprob; ++pr) {
+    for (int pr = 0; pr < nprob2; ++pr) {
       const int b = boxes[pr / 2];
+      const int lb = b - proot[prob[b]];  // box id local to its tree: the random stream of the oracle
       ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], pm[pr], pn[pr], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
-                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * b + (pr & 1), 0};
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * lb + (pr & 1), 0,
+                   pseed[prob[b]]};
     }
     long long maxe = 0;
     for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
     DevBuf<KgenP<double>> dkg;
     upload_vec(dkg, kg, stream);
-    kgen_batched<double>(dkg.p, nprob, maxe, view(pts), kdev, stream);
+    for (int o = 0; o < nprob2; o += 65535)
+      kgen_batched<double>(dkg.p + o, std::min(65535, nprob2 - o), maxe, view(pts), kdev, stream);
     DevBuf<IdP> dip;
     upload_vec(dip, ip, stream);
-    id_adaptive_batched(dip.p, nprob, acc, seed, stream);
+    id_adaptive_batched(dip.p, nprob2, acc, stream);
     std::vector<int> hr;
-    download(hr, rank.p, nprob, stream);
+    download(hr, rank.p, nprob2, stream);
     HSS_CUDA(cudaStreamSynchronize(stream));
     bool any = false;
     std::vector<int> kbox(nbL);
@@ -404,8 +431,8 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
       else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q + 1], pn[2 * q + 1]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
     }
     if (any) {
-      HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob * sizeof(IdP), cudaMemcpyHostToDevice, stream));
-      id_fixed_batched(dip.p, nprob, stream);
+      HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob2 * sizeof(IdP), cudaMemcpyHostToDevice, stream));
+      id_fixed_batched(dip.p, nprob2, stream);
     }
     std::vector<int> hp;
     download(hp, perm.p, tP, stream);
@@ -425,20 +452,23 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
       }
       Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
       Tlev[b] = (int)Tkeep.size() - 1;
+      census[4 * b] = pm[2 * q]; census[4 * b + 1] = pm[2 * q + 1]; census[4 * b + 2] = n; census[4 * b + 3] = k;
     }
   }
   // ---- compact T_UP / T_DN / T_DN^T and J arenas
   oT.assign(nboxes, 0);
   oJ.assign(nboxes, 0);
   long long tt = 0, tj = 0;
-  for (int b = 1; b < nboxes; ++b) {
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
     oT[b] = tt; tt += (long long)kskel[b] * (nskel[b] - kskel[b]);
     oJ[b] = tj; tj += nskel[b];
   }
   T_UP.alloc(std::max(tt, 1LL)); T_DN.alloc(std::max(tt, 1LL)); TDNT.alloc(std::max(tt, 1LL));
   std::vector<MoveP> mv;
   std::vector<int> hJU(std::max(tj, 1LL)), hJD(std::max(tj, 1LL));
-  for (int b = 1; b < nboxes; ++b) {
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
     const int n = nskel[b], k = kskel[b];
     std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
     std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJ[b]);
@@ -457,7 +487,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
   oSib.assign(nboxes, -1);
   long long ts = 0, tb = 0;
   for (int b = 0; b < nboxes; ++b) {
-    if (b > 0 && is_leaf(b)) { oSelf[b] = ts; ts += (long long)cnt[b] * cnt[b]; }
+    if (parent[b] >= 0 && is_leaf(b)) { oSelf[b] = ts; ts += (long long)cnt[b] * cnt[b]; }
     if (!is_leaf(b)) {
       const int s1 = c1[b], s2 = c2[b];
       oSib[s1] = tb; tb += (long long)kskel[s1] * kskel[s2];
@@ -471,7 +501,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
   std::vector<long long> io;
   auto push = [&](const std::vector<int>& v) { io.push_back(idx.size()); idx.insert(idx.end(), v.begin(), v.end()); };
   for (int b = 0; b < nboxes; ++b) {
-    if (b > 0 && is_leaf(b)) {
+    if (parent[b] >= 0 && is_leaf(b)) {
       std::vector<int> r(cnt[b]);
       std::iota(r.begin(), r.end(), off[b]);
       push(r);
@@ -485,7 +515,7 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
   upload_vec(didx, idx, stream);
   size_t q = 0;
   for (int b = 0; b < nboxes; ++b) {
-    if (b > 0 && is_leaf(b)) {
+    if (parent[b] >= 0 && is_leaf(b)) {
       const int* r = didx.p + io[q++];
       kg.push_back(KgenP<double>{r, r, cnt[b], cnt[b], M_SELF.p + oSelf[b], cnt[b], 0});
     }
@@ -515,7 +545,8 @@ void HSS1D::compress(const double* Xh, long long N_, long long ldx, int leaf_, d
 void HSS1D::invert() {
   oL.assign(nboxes, 0); oR.assign(nboxes, 0); oD.assign(nboxes, 0); oE.assign(nboxes, 0);
   long long tl = 0, td = 0, te = 0;
-  for (int b = 1; b < nboxes; ++b) {
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
     const long long n = nskel[b], k = kskel[b];
     oL[b] = tl; oR[b] = tl; tl += n * k;
     oD[b] = td; td += n * n;
@@ -526,7 +557,7 @@ void HSS1D::invert() {
   DevBuf<double> Fw(std::max(td, 1LL)), W1(std::max(td, 1LL)), W2(std::max(td, 1LL)), W3(std::max(tl, 1LL));
   for (int Lv = maxlev; Lv >= 1; --Lv) {
     std::vector<int> boxes;
-    for (int b = 1; b < nboxes; ++b)
+    for (int b = 0; b < nboxes; ++b)
       if (level[b] == Lv) boxes.push_back(b);
     if (boxes.empty()) continue;
     std::vector<F1P> fa;
@@ -607,17 +638,30 @@ void HSS1D::invert() {
     }
     run_gemms(PD, false, false, -1.0, 1.0, stream);
   }
-  // top: FT = [E2 M_SIB2; M_SIB3 E3] (reference boxes 2, 3 = ids 1, 2)
-  const int ka = kskel[1], kb = kskel[2];
-  ktop = ka + kb;
-  FTinv.alloc((size_t)ktop * ktop);
-  std::vector<F1P> fa = {F1P{FTinv.p, ktop, ka, Einv.p + oE[1], M_SIB.p + oSib[1], M_SIB.p + oSib[2],
-                             Einv.p + oE[2], nullptr}};
+  // top of every tree: FT = [E2 M_SIB2; M_SIB3 E3] (the root's children, reference boxes 2 and 3)
+  ktop.assign(nprob, 0);
+  oFT.assign(nprob, 0);
+  long long tft = 0;
+  for (int p = 0; p < nprob; ++p) {
+    const int r = proot[p];
+    ktop[p] = kskel[c1[r]] + kskel[c2[r]];
+    oFT[p] = tft;
+    tft += (long long)ktop[p] * ktop[p];
+  }
+  FTinv.alloc(std::max(tft, 1LL));
+  std::vector<F1P> fa;
+  std::vector<std::pair<double*, int>> mats;
+  for (int p = 0; p < nprob; ++p) {
+    const int r = proot[p], a = c1[r], b = c2[r];
+    fa.push_back(F1P{FTinv.p + oFT[p], ktop[p], kskel[a], Einv.p + oE[a], M_SIB.p + oSib[a], M_SIB.p + oSib[b],
+                     Einv.p + oE[b], nullptr});
+    mats.push_back({FTinv.p + oFT[p], ktop[p]});
+  }
   DevBuf<F1P> d;
   upload_vec(d, fa, stream);
-  k_assemble1<<<1, 256, 0, stream>>>(d.p);
+  k_assemble1<<<(int)fa.size(), 256, 0, stream>>>(d.p);
   check_launch("k_assemble1 top");
-  std::vector<std::pair<double*, int>> mats = {{FTinv.p, ktop}};
+  HSS_CUDA(cudaStreamSynchronize(stream));
   invert_many(mats, stream);
   inverted = true;
 }
@@ -635,7 +679,8 @@ static Stack1 make_stack(const HSS1D& H, int width) {
   s.base.assign(H.maxlev + 2, 0);
   s.ld.assign(H.maxlev + 2, 0);
   s.row.assign(H.nboxes, 0);
-  for (int b = 1; b < H.nboxes; ++b) {
+  for (int b = 0; b < H.nboxes; ++b) {
+    if (H.parent[b] < 0) continue;
     s.row[b] = s.ld[H.level[b]];
     s.ld[H.level[b]] += H.kskel[b];
   }
@@ -652,15 +697,15 @@ void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
   v2.alloc(std::max(S.base.back(), 1LL));
   for (int c0 = 0; c0 < nrhs; c0 += 8) {
     const int r = std::min(8, nrhs - c0);
-    const double* ff = dX + (size_t)c0 * N;
-    double* xx = dY + (size_t)c0 * N;
+    const double* ff = dX + (size_t)c0 * Ntot;
+    double* xx = dY + (size_t)c0 * Ntot;
     auto vin = [&](int b, const double*& p, int& ld) {
-      if (is_leaf(b)) { p = ff + off[b]; ld = (int)N; }
+      if (is_leaf(b)) { p = ff + off[b]; ld = (int)Ntot; }
       else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
     };
     for (int L = maxlev; L >= 1; --L) {
       std::vector<GemmP<double>> P;
-      for (int b = 1; b < nboxes; ++b) {
+      for (int b = 0; b < nboxes; ++b) {
         if (level[b] != L) continue;
         const double* in;
         int ldi;
@@ -671,17 +716,21 @@ void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
       run_gemms(P, false, false, 1.0, 0.0, stream, true);
     }
     {
-      std::vector<GemmP<double>> P = {GemmP<double>{FTinv.p, v1.p + S.base[1], v2.p + S.base[1], ktop, r, ktop, ktop,
-                                                    S.ld[1], S.ld[1]}};
+      std::vector<GemmP<double>> P;
+      for (int p = 0; p < nprob; ++p) {
+        const int a = c1[proot[p]];
+        P.push_back(GemmP<double>{FTinv.p + oFT[p], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[a],
+                                  ktop[p], r, ktop[p], ktop[p], S.ld[1], S.ld[1]});
+      }
       run_gemms(P, false, false, 1.0, 0.0, stream, true);
     }
     for (int L = 1; L <= maxlev; ++L) {
       std::vector<GemmP<double>> P1, P2;
-      for (int b = 1; b < nboxes; ++b) {
+      for (int b = 0; b < nboxes; ++b) {
         if (level[b] != L) continue;
         double* out;
         int ldo;
-        if (is_leaf(b)) { out = xx + off[b]; ldo = (int)N; }
+        if (is_leaf(b)) { out = xx + off[b]; ldo = (int)Ntot; }
         else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
         const double* in;
         int ldi;
@@ -702,21 +751,25 @@ void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
   v2.alloc(std::max(S.base.back(), 1LL));
   std::vector<long long> oS(nboxes, 0);
   long long ts = 0;
-  for (int b = 1; b < nboxes; ++b) { oS[b] = ts; ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8; }
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    oS[b] = ts;
+    ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8;
+  }
   v3.alloc(std::max(ts, 1LL));
   for (int c0 = 0; c0 < nrhs; c0 += 8) {
     const int r = std::min(8, nrhs - c0);
-    const double* qq = dX + (size_t)c0 * N;
-    double* uu = dY + (size_t)c0 * N;
+    const double* qq = dX + (size_t)c0 * Ntot;
+    double* uu = dY + (size_t)c0 * Ntot;
     auto vin = [&](int b, const double*& p, int& ld) {
-      if (is_leaf(b)) { p = qq + off[b]; ld = (int)N; }
+      if (is_leaf(b)) { p = qq + off[b]; ld = (int)Ntot; }
       else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
     };
     // upward: phi_up = q(J(1:k)) + T_UP q(J(k+1:n))
     for (int L = maxlev; L >= 1; --L) {
       std::vector<MoveP> mv;
       std::vector<GemmP<double>> P;
-      for (int b = 1; b < nboxes; ++b) {
+      for (int b = 0; b < nboxes; ++b) {
         if (level[b] != L) continue;
         const int n = nskel[b], k = kskel[b], nr = n - k;
         const double* in;
@@ -732,33 +785,36 @@ void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
       run_moves(mv, stream);
       run_gemms(P, false, false, 1.0, 1.0, stream, true);
     }
-    // top sibling interactions
+    // top sibling interactions of every tree
     {
-      std::vector<GemmP<double>> P = {
-          GemmP<double>{M_SIB.p + oSib[1], v1.p + S.base[1] + S.row[2], v2.p + S.base[1] + S.row[1], kskel[1], r,
-                        kskel[2], kskel[1], S.ld[1], S.ld[1]},
-          GemmP<double>{M_SIB.p + oSib[2], v1.p + S.base[1] + S.row[1], v2.p + S.base[1] + S.row[2], kskel[2], r,
-                        kskel[1], kskel[2], S.ld[1], S.ld[1]}};
+      std::vector<GemmP<double>> P;
+      for (int p = 0; p < nprob; ++p) {
+        const int a = c1[proot[p]], b = c2[proot[p]];
+        P.push_back(GemmP<double>{M_SIB.p + oSib[a], v1.p + S.base[1] + S.row[b], v2.p + S.base[1] + S.row[a],
+                                  kskel[a], r, kskel[b], kskel[a], S.ld[1], S.ld[1]});
+        P.push_back(GemmP<double>{M_SIB.p + oSib[b], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[b],
+                                  kskel[b], r, kskel[a], kskel[b], S.ld[1], S.ld[1]});
+      }
       run_gemms(P, false, false, 1.0, 0.0, stream, true);
     }
     // downward: u_long = L phi_dn (+ sibling terms or self term)
     for (int L = 1; L <= maxlev; ++L) {
       std::vector<GemmP<double>> PT, PS;
       std::vector<MoveP> mv;
-      for (int b = 1; b < nboxes; ++b) {
+      for (int b = 0; b < nboxes; ++b) {
         if (level[b] != L) continue;
         const int n = nskel[b], k = kskel[b], nr = n - k;
         const double* dn = v2.p + S.base[L] + S.row[b];
         double* out;
         int ldo;
-        if (is_leaf(b)) { out = uu + off[b]; ldo = (int)N; }
+        if (is_leaf(b)) { out = uu + off[b]; ldo = (int)Ntot; }
         else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
         if (nr > 0)
           PT.push_back(GemmP<double>{TDNT.p + oT[b], dn, v3.p + oS[b], nr, r, k, nr, S.ld[L], nr});
         mv.push_back(MoveP{dn, out, JDNd.p + oJ[b], k, r, S.ld[L], ldo, 2, 0});
         if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJ[b] + k, nr, r, nr, ldo, 2, 0});
         if (is_leaf(b)) {
-          PS.push_back(GemmP<double>{M_SELF.p + oSelf[b], qq + off[b], out, n, r, n, n, (int)N, ldo});
+          PS.push_back(GemmP<double>{M_SELF.p + oSelf[b], qq + off[b], out, n, r, n, n, (int)Ntot, ldo});
         } else {
           const int s1 = c1[b], s2 = c2[b];
           const double* up1 = v1.p + S.base[L + 1] + S.row[s1];
@@ -774,6 +830,77 @@ void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
       run_gemms(PS, false, false, 1.0, 1.0, stream, true);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Refinement (Common/Iterative_Refinement.m:20-35) against the FP64 forward operator.
+__global__ void k_res1(long long N, int r, const double* __restrict__ f, const double* __restrict__ y,
+                       double* __restrict__ res, double* __restrict__ part) {
+  __shared__ double sa[8], sb[8];
+  for (int c = 0; c < r; ++c) {
+    double a = 0.0, b = 0.0;
+    for (long long i = blockIdx.x * 256LL + threadIdx.x; i < N; i += (long long)gridDim.x * 256) {
+      const double fv = f[i + c * N];
+      const double rv = fv - y[i + c * N];
+      res[i + c * N] = rv;
+      a += rv * rv;
+      b += fv * fv;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int w = 0; w < 8; ++w) { ta += sa[w]; tb += sb[w]; }
+      part[((long long)blockIdx.x * r + c) * 2] = ta;
+      part[((long long)blockIdx.x * r + c) * 2 + 1] = tb;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_axpy1(long long n, const double* __restrict__ d, double* __restrict__ x) {
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) x[e] += d[e];
+}
+
+void HSS1D::solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres,
+                         int* iters) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_solve before hss1d_invert");
+  HSS_REQUIRE(nrhs >= 1 && maxit >= 1, HSS_ERR_ARG, "nrhs and maxit must be >= 1");
+  const long long cnt = Ntot * nrhs;
+  DevBuf<double> y(cnt), res(cnt), dd(cnt);
+  const int gx = 256;
+  DevBuf<double> part((size_t)gx * nrhs * 2);
+  applyinv_device(df, dx, nrhs);
+  int used = 1;
+  double worst = 0.0;
+  while (true) {
+    apply_device(dx, y.p, nrhs);
+    k_res1<<<gx, 256, 0, stream>>>(Ntot, nrhs, df, y.p, res.p, part.p);
+    check_launch("k_res1");
+    std::vector<double> hp;
+    download(hp, part.p, (size_t)gx * nrhs * 2, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    worst = 0.0;
+    for (int c = 0; c < nrhs; ++c) {
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < gx; ++q) { a += hp[((size_t)q * nrhs + c) * 2]; b += hp[((size_t)q * nrhs + c) * 2 + 1]; }
+      const double rel = (b > 0.0) ? std::sqrt(a / b) : std::sqrt(a);
+      HSS_REQUIRE(std::isfinite(rel), HSS_ERR_NONFINITE, "non-finite residual in refinement");
+      worst = std::max(worst, rel);
+    }
+    if (worst <= tol || used >= maxit) break;
+    applyinv_device(res.p, dd.p, nrhs);
+    k_axpy1<<<std::max(1, std::min(ceil_div(cnt, 256), 4096)), 256, 0, stream>>>(cnt, dd.p, dx);
+    check_launch("k_axpy1");
+    ++used;
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  if (relres) *relres = worst;
+  if (iters) *iters = used;
 }
 
 }  // namespace hss

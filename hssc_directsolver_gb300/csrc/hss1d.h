@@ -1,4 +1,8 @@
 // HSS1D solver state.  See hss1d.cu.
+//
+// A handle holds a forest: one or many independent curves ("problems") whose
+// trees share one global box numbering, one point table and one set of device
+// arenas, so every level of every problem is processed by the same launches.
 #pragma once
 
 #include <vector>
@@ -10,7 +14,8 @@ namespace hss {
 
 // Generic small block move: mode 0 row gather dst(i,c) = src(idx[i], c);
 // mode 1 column gather dst(i,c) = src(i, idx[c]); mode 2 row scatter
-// dst(idx[i], c) (+)= src(i, c).  idx == nullptr means identity.
+// dst(idx[i], c) (+)= src(i, c); mode 3 transpose dst(c,i) = src(i,c).
+// idx == nullptr means identity.
 struct MoveP {
   const double* src;
   double* dst;
@@ -20,16 +25,18 @@ struct MoveP {
 void move_batched(const MoveP* dP, int batch, cudaStream_t s);
 
 struct HSS1D {
-  // tree (box_constants.m rows LEVEL..END2)
-  long long N = 0;
-  int nboxes = 0, leaf = 0, maxlev = 0;
+  // forest: global box ids; box_constants.m rows LEVEL..END2 per box
+  long long Ntot = 0;
+  int nprob = 0, nboxes = 0, leaf = 0, maxlev = 0;
   double acc = 0;
-  unsigned long long seed = 0;
-  std::vector<int> level, parent, c1, c2, off, cnt;
-  // skeletons (host copies, 0-based)
+  std::vector<long long> pN, pbase;   // points per problem, first global point
+  std::vector<int> proot;              // root box of each problem
+  std::vector<unsigned long long> pseed;
+  std::vector<int> prob, level, parent, c1, c2, off, cnt;  // off = global point index
+  // skeletons (host copies, global point indices)
   std::vector<int> nskel, kskel;
   std::vector<std::vector<int>> I_SKUP, I_SKDN, J_UP, J_DN;
-  std::vector<double> X;  // N x 6 row-major
+  std::vector<double> X;  // Ntot x 6 row-major
   hss_kernel_params kp{};
   KernelDev kdev{};
   PointTable pts;
@@ -41,20 +48,23 @@ struct HSS1D {
   std::vector<long long> oJ;
   // inverse factors
   DevBuf<double> Linv, Rinv, Dinv, Einv, FTinv;
-  std::vector<long long> oL, oR, oD, oE;
-  int ktop = 0;
+  std::vector<long long> oL, oR, oD, oE, oFT;
+  std::vector<int> ktop;
   bool inverted = false;
-  // solve workspaces: per-box vectors (k x 8) for up/down passes
-  DevBuf<double> v1, v2, v3, qs, ys;
-  std::vector<long long> oV;  // per-level stacked offsets (rows), by box
+  // solve workspaces
+  DevBuf<double> v1, v2, v3;
+  // ID problem shapes of the last compress: (m_out, m_in, n, k) per non-root box
+  std::vector<int> census;
 
   HSS1D();
   ~HSS1D();
-  void compress(const double* Xh, long long N, long long ldx, int leaf, double acc, const hss_kernel_params& kp,
-                unsigned long long seed);
+  // problem p: X_p is an N_p x 6 column-major block [x y nx ny w kappa] (ld ldx_p)
+  void compress(int nprob, const long long* N, const double* const* Xp, const long long* ldx, int leaf, double acc,
+                const hss_kernel_params& kp, const unsigned long long* seeds);
   void invert();
   void applyinv_device(const double* dX, double* dY, int nrhs);
   void apply_device(const double* dX, double* dY, int nrhs);
+  void solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres, int* iters);
   bool is_leaf(int b) const { return c1[b] < 0 && c2[b] < 0; }
 };
 

@@ -87,6 +87,41 @@ def HSS1D_compress_nsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel
     return HSS1DMatrix(h, Xf.shape[0])
 
 
+def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None) -> HSS1DMatrix:
+    """Many independent curves compressed together (every level of every tree in the
+    same launches).  Vectors of the returned matrix are the problems' vectors stacked."""
+    mats = []
+    for X in Xs:
+        X = np.asarray(X, dtype=np.float64)
+        if X.shape[1] == 2:
+            X6 = np.zeros((X.shape[0], 6))
+            X6[:, :2] = X
+            X = X6
+        mats.append(np.asfortranarray(X))
+    P = len(mats)
+    N = (C.c_int64 * P)(*[m.shape[0] for m in mats])
+    ptrs = (C.c_void_p * P)(*[m.ctypes.data for m in mats])
+    seeds = list(range(P)) if seeds is None else list(seeds)
+    sd = (C.c_uint64 * P)(*seeds)
+    h = C.c_void_p()
+    kp = knl_params.to_c()
+    L.check(L.lib().hss1d_compress_batch(C.byref(h), P, N, ptrs, N, int(TREE), float(acc), C.byref(kp), sd))
+    M = HSS1DMatrix(h, int(sum(m.shape[0] for m in mats)))
+    M.sizes = [m.shape[0] for m in mats]
+    return M
+
+
+def forest_info(K_HSS: HSS1DMatrix):
+    P = C.c_int32()
+    Nt = C.c_int64()
+    L.check(L.lib().hss1d_forest_info(K_HSS._h, C.byref(P), C.byref(Nt), None, None))
+    roots = np.zeros(P.value, np.int32)
+    base = np.zeros(P.value, np.int64)
+    L.check(L.lib().hss1d_forest_info(K_HSS._h, None, None, roots.ctypes.data_as(L._I32P),
+                                      base.ctypes.data_as(L._I64P)))
+    return roots, base
+
+
 def HSS1D_invert_nsym(K_HSS: HSS1DMatrix, acc: float = 0.0):
     """Returns (HSSinv, FTinv); both are views of the factors kept inside K_HSS."""
     L.check(L.lib().hss1d_invert(K_HSS._h))
@@ -110,3 +145,17 @@ def HSS1D_applyinv_nsym(K_HSS: HSS1DMatrix, HSSinv, FTinv, ff) -> np.ndarray:
     out = np.zeros_like(f2, order="F")
     L.check(L.lib().hss1d_applyinv(K_HSS._h, L.ptr(f2), L.ptr(out), f2.shape[1]))
     return out[:, 0] if vec else out
+
+
+def HSS1D_solve(K_HSS: HSS1DMatrix, ff, tol: float = 1e-10, maxit: int = 5):
+    """x = A^-1 f refined against the FP64 HSS1D forward operator
+    (Common/Iterative_Refinement.m:20-35).  Returns (x, relres, inverse applies used)."""
+    f = _as_f64(ff)
+    vec = f.ndim == 1
+    f2 = f.reshape(K_HSS.N, -1, order="F")
+    out = np.zeros_like(f2, order="F")
+    rr = C.c_double()
+    it = C.c_int32()
+    L.check(L.lib().hss1d_solve(K_HSS._h, L.ptr(f2), L.ptr(out), f2.shape[1], tol, maxit, C.byref(rr),
+                                C.byref(it)))
+    return (out[:, 0] if vec else out), rr.value, it.value

@@ -70,7 +70,18 @@ typedef struct hss1d_matrix hss1d_matrix;
  * seed: key of the counter RNG drawing the rank-check vectors (ID.m:68-86). */
 int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
                    double acc, const hss_kernel_params* kp, uint64_t seed);
-/* tree and skeleton sizes: arrays of nboxes entries (any may be NULL) */
+/* Batched HSS1D: nprob independent curves of uneven N compressed as one forest, every level of
+ * every tree in the same launches.  X[p] is N[p] x 6 column-major (ld ldx[p]); seeds[p] keys
+ * the rank-check stream of problem p (NULL: all 0).  No reference counterpart for the batching
+ * itself: each tree is HSS1D_compress_nsym (HSS1D/HSS1D_compress_nsym.m:1).  Vectors passed to
+ * the apply calls are the problems' vectors stacked (sum of N rows). */
+int hss1d_compress_batch(hss1d_matrix** out, int32_t nprob, const int64_t* N, const double* const* X,
+                         const int64_t* ldx, int32_t leaf, double acc, const hss_kernel_params* kp,
+                         const uint64_t* seeds);
+/* problems of a forest: count, total points, root box and first stacked row of each (NULL ok) */
+int hss1d_forest_info(const hss1d_matrix* H, int32_t* nprob, int64_t* Ntot, int32_t* root, int64_t* pbase);
+/* tree and skeleton sizes over the forest's global box ids: arrays of nboxes entries (NULL ok);
+ * off is the global (stacked) first point of a box */
 int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* parent,
                int32_t* c1, int32_t* c2, int32_t* off, int32_t* cnt, int32_t* nskel,
                int32_t* kskel);
@@ -86,6 +97,13 @@ int hss1d_apply(hss1d_matrix* H, const double* qq, double* uu, int32_t nrhs);
 int hss1d_applyinv(hss1d_matrix* H, const double* ff, double* xx, int32_t nrhs);
 int hss1d_applyinv_device(hss1d_matrix* H, const double* d_ff, double* d_xx, int32_t nrhs,
                           void* stream);
+/* inverse apply with iterative refinement against the FP64 HSS1D forward operator
+ * (Common/Iterative_Refinement.m:20-35); relres = final max column ||f - A x|| / ||f|| over the
+ * (stacked) vectors, iters = inverse applies used (either may be NULL) */
+int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, double tol, int32_t maxit,
+                double* relres, int32_t* iters);
+int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
+                       int32_t maxit, double* relres, int32_t* iters, void* stream);
 int hss1d_destroy(hss1d_matrix* H);
 
 /* ---- HSS2D (planar volumes) -------------------------------------------- */

@@ -95,3 +95,40 @@ def test_errors_are_status_codes(gpu):
     with pytest.raises(L.HSSError) as e:
         G1.HSS1D_applyinv_nsym(H, None, None, np.ones(256))
     assert e.value.code == L.HSS_ERR_STATE
+
+
+def test_batched_forest_matches_per_problem_oracle(gpu):
+    """Many curves of uneven N in one forest: every tree equals the oracle run on its own
+    (ranks exact, inverse apply <= 1e-12), with per-problem rank-check seeds."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(5, nmin=600, nmax=3000, seed=3)
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"), seeds=[11 * p for p in range(5)])
+    roots, base = G1.forest_info(H)
+    assert list(np.diff(base)) == sizes[:-1]
+    inf = H.info()
+    G1.HSS1D_invert_nsym(H)
+    F = np.random.default_rng(4).standard_normal((sum(sizes), 2))
+    X = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    U = G1.HSS1D_apply_nsym(H, F)
+    for p, Xp in enumerate(Xs):
+        Ho = O1.compress_nsym(Xp, 64, 1e-10, OK.KernelParams(flag=OK.DL_L_2D), seed=11 * p)
+        nb = Ho.tree.nboxes
+        kg = inf["kskel"][roots[p] + 1:roots[p] + nb]
+        assert np.array_equal(kg, np.array(Ho.kskel[1:]))
+        sl = slice(base[p], base[p] + sizes[p])
+        xo = O1.applyinv_nsym(Ho, O1.invert_nsym(Ho), F[sl])
+        assert np.linalg.norm(X[sl] - xo) <= 1e-12 * np.linalg.norm(xo)
+        uo = O1.apply_nsym(Ho, F[sl])
+        assert np.linalg.norm(U[sl] - uo) <= 1e-12 * np.linalg.norm(uo)
+
+
+def test_refined_solve_reaches_tolerance(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(6, nmin=800, nmax=2500, seed=7)
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    G1.HSS1D_invert_nsym(H)
+    F = np.random.default_rng(1).standard_normal((sum(sizes), 3))
+    x, rr, it = G1.HSS1D_solve(H, F, 1e-13, 4)
+    assert rr <= 1e-13 and 1 <= it <= 4
+    r = F - G1.HSS1D_apply_nsym(H, x)
+    assert np.linalg.norm(r, axis=0).max() / np.linalg.norm(F, axis=0).min() < 1e-12
