@@ -10,6 +10,7 @@
 #include "hss2d.h"
 
 namespace hss {
+void batched_inverse_noalloc(double* d_A, int n, int batch, int* d_info, cudaStream_t s);
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace hss
@@ -460,6 +461,12 @@ int hss2d_destroy(hss2d_matrix* H) {
 int hss_batched_inverse_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info, void* stream) {
   HSS_TRY
   batched_inverse<double>(d_A, n, batch, d_info, as_stream(stream));
+  HSS_CATCH
+}
+
+int hss_batched_inverse_noalloc_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info, void* stream) {
+  HSS_TRY
+  batched_inverse_noalloc(d_A, n, batch, d_info, as_stream(stream));
   HSS_CATCH
 }
 

@@ -170,6 +170,18 @@ int hss_batched_inverse_device(double* d_A, int32_t n, int32_t batch, int32_t* d
                                void* stream);
 int hss_batched_inverse_device_f32(float* d_A, int32_t n, int32_t batch, int32_t* d_info,
                                    void* stream);
+/* Same inversion without any device allocation, for callers that cannot call
+ * cudaMalloc/cudaFree while running (device memory owned by their own pool
+ * allocator, or latency-bound loops where allocation would synchronise the
+ * device).  No counterpart in the reference (MATLAB allocates freely).  All
+ * scratch comes from one fixed 16 MiB array in device global memory (held by
+ * every GPU that loads the library): batch <= 256 and
+ * batch*(n*n + 64*n)*8 + batch*(n + 132)*4 bytes plus descriptors must fit, else
+ * HSS_ERR_ARG.  The first call on a device resolves the array's address there.
+ * Calls share the array: overlapping calls on the GPU race and must be ordered
+ * by the caller.  d_info is cleared by each call. */
+int hss_batched_inverse_noalloc_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info,
+                                       void* stream);
 /* Least squares X_b = A_b(:,0:kf) \ A_b(:,kf:n) for `batch` m x n blocks back to
  * back (device); X overwrites A_b(0:kf, kf:n). */
 int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch,
