@@ -75,6 +75,19 @@ SIGNATURES = {
     "hss1d_solve": (C.c_int, [_P, _P, _P, C.c_int32, C.c_double, C.c_int32, _DP, _I32P]),
     "hss1d_solve_device": (C.c_int, [_P, _P, _P, C.c_int32, C.c_double, C.c_int32, _DP, _I32P, _P]),
     "hss1d_destroy": (C.c_int, [_P]),
+    "hss_mlp_create": (C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32, C.c_uint64]),
+    "hss_mlp_nparams": (C.c_int, [_P, _I32P]),
+    "hss_mlp_get_params": (C.c_int, [_P, _P]),
+    "hss_mlp_set_params": (C.c_int, [_P, _P]),
+    "hss_mlp_grad": (C.c_int, [_P, _P, _P, C.c_int32, _P, C.POINTER(C.c_float)]),
+    "hss_mlp_train": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_float)]),
+    "hss_mlp_predict": (C.c_int, [_P, _P, C.c_int32, _P]),
+    "hss_mlp_destroy": (C.c_int, [_P]),
+    "hss1d_features": (C.c_int, [_P, _P, _P]),
+    "hss1d_id_stats": (C.c_int, [_P, _I64P, _I64P, _I32P]),
+    "hss1d_phase_times": (C.c_int, [_P, _DP]),
+    "hss1d_compress_batch_learned": (C.c_int, [C.POINTER(_P), C.c_int32, _I64P, C.POINTER(C.c_void_p), _I64P,
+                                               C.c_int32, C.c_double, _P, _P, _P]),
     "hss2d_build_tree": (C.c_int, [C.POINTER(_P), C.POINTER(hss2d_params)]),
     "hss2d_compress": (C.c_int, [_P]),
     "hss2d_invert": (C.c_int, [_P]),

@@ -8,6 +8,7 @@
 #include "dense.cuh"
 #include "hss1d.h"
 #include "hss2d.h"
+#include "mlp.h"
 
 namespace hss {
 void batched_inverse_noalloc(double* d_A, int n, int batch, int* d_info, cudaStream_t s);
@@ -80,14 +81,14 @@ int hss_device_count(int* count) {
 // ---------------------------------------------------------------- HSS1D --
 static void hss1d_make(hss1d_matrix** out, int nprob, const long long* N, const double* const* X,
                        const long long* ldx, int leaf, double acc, const hss_kernel_params* kp,
-                       const unsigned long long* seeds) {
+                       const unsigned long long* seeds, MLP* mlp = nullptr) {
   HSS_REQUIRE(out && X && kp && N && ldx, HSS_ERR_ARG, "NULL argument");
   require_device();
   *out = nullptr;
   auto* h = new hss1d_matrix{nullptr};
   try {
     h->impl = new HSS1D();
-    h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds);
+    h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds, mlp);
   } catch (...) {
     delete h->impl;
     delete h;
@@ -115,6 +116,147 @@ int hss1d_compress_batch(hss1d_matrix** out, int32_t nprob, const int64_t* N, co
   if (seeds)
     for (int p = 0; p < nprob; ++p) sd[p] = seeds[p];
   hss1d_make(out, nprob, n.data(), X, l.data(), leaf, acc, kp, sd.data());
+  HSS_CATCH
+}
+
+int hss1d_compress_batch_learned(hss1d_matrix** out, int32_t nprob, const int64_t* N, const double* const* X,
+                                 const int64_t* ldx, int32_t leaf, double acc, const hss_kernel_params* kp,
+                                 const uint64_t* seeds, hss_mlp* M) {
+  HSS_TRY
+  HSS_REQUIRE(nprob >= 1 && N && ldx && M && M->impl, HSS_ERR_ARG, "bad batch arguments");
+  std::vector<long long> n(N, N + nprob), l(ldx, ldx + nprob);
+  std::vector<unsigned long long> sd(nprob, 0ULL);
+  if (seeds)
+    for (int p = 0; p < nprob; ++p) sd[p] = seeds[p];
+  hss1d_make(out, nprob, n.data(), X, l.data(), leaf, acc, kp, sd.data(), M->impl);
+  HSS_CATCH
+}
+
+int hss1d_features(const hss1d_matrix* H, float* feat, float* rank_frac) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS1D* h = H->impl;
+  if (feat) std::copy(h->feat.begin(), h->feat.end(), feat);
+  if (rank_frac)
+    for (int b = 0; b < h->nboxes; ++b) {
+      const int n = h->census[4 * b + 2];
+      rank_frac[b] = (n > 0) ? (float)h->census[4 * b + 3] / (float)n : 0.f;
+    }
+  HSS_CATCH
+}
+
+int hss1d_phase_times(const hss1d_matrix* H, double* seconds) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && seconds, HSS_ERR_ARG, "NULL argument");
+  std::copy(H->impl->phase_s, H->impl->phase_s + HSS1D::NPHASE, seconds);
+  HSS_CATCH
+}
+
+int hss1d_id_stats(const hss1d_matrix* H, int64_t* qr_steps, int64_t* qr_steps_full, int32_t* reruns) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  if (qr_steps) *qr_steps = H->impl->qr_steps;
+  if (qr_steps_full) *qr_steps_full = H->impl->qr_steps_full;
+  if (reruns) *reruns = H->impl->reruns;
+  HSS_CATCH
+}
+
+// --------------------------------------------------------------- MLP --
+int hss_mlp_create(hss_mlp** out, int32_t nin, int32_t hidden, uint64_t seed) {
+  HSS_TRY
+  HSS_REQUIRE(out, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *out = nullptr;
+  auto* m = new hss_mlp{nullptr};
+  try {
+    m->impl = new MLP(nin, hidden, seed);
+  } catch (...) {
+    delete m;
+    throw;
+  }
+  *out = m;
+  HSS_CATCH
+}
+
+int hss_mlp_nparams(const hss_mlp* M, int32_t* np) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && np, HSS_ERR_ARG, "NULL argument");
+  *np = mlp_nparams(M->impl->nin, M->impl->H);
+  HSS_CATCH
+}
+
+int hss_mlp_get_params(const hss_mlp* M, float* params) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && params, HSS_ERR_ARG, "NULL argument");
+  MLP* m = M->impl;
+  const int np = mlp_nparams(m->nin, m->H);
+  HSS_CUDA(cudaMemcpyAsync(params, m->p.p, np * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+  HSS_CUDA(cudaStreamSynchronize(m->stream));
+  HSS_CATCH
+}
+
+int hss_mlp_set_params(hss_mlp* M, const float* params) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && params, HSS_ERR_ARG, "NULL argument");
+  MLP* m = M->impl;
+  const int np = mlp_nparams(m->nin, m->H);
+  HSS_CUDA(cudaMemcpyAsync(m->p.p, params, np * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  m->m.zero(m->stream);
+  m->v.zero(m->stream);
+  m->step = 0;
+  HSS_CUDA(cudaStreamSynchronize(m->stream));
+  HSS_CATCH
+}
+
+int hss_mlp_grad(hss_mlp* M, const float* X, const float* t, int32_t B, float* grad, float* loss) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && X && t && B >= 1, HSS_ERR_ARG, "bad arguments");
+  MLP* m = M->impl;
+  const int np = mlp_nparams(m->nin, m->H);
+  DevBuf<float> dX, dt;
+  dX.upload(std::vector<float>(X, X + (size_t)B * m->nin), m->stream);
+  dt.upload(std::vector<float>(t, t + B), m->stream);
+  const float l = m->grad(dX.p, dt.p, B, 1.f / (float)B, m->stream, true);
+  if (grad) {
+    HSS_CUDA(cudaMemcpyAsync(grad, m->g.p, np * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    HSS_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  if (loss) *loss = l;
+  HSS_CATCH
+}
+
+int hss_mlp_train(hss_mlp* M, const float* X, const float* t, int32_t B, int32_t epochs, int32_t batch, float lr,
+                  float* loss) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && X && t && B >= 1, HSS_ERR_ARG, "bad arguments");
+  MLP* m = M->impl;
+  DevBuf<float> dX, dt;
+  dX.upload(std::vector<float>(X, X + (size_t)B * m->nin), m->stream);
+  dt.upload(std::vector<float>(t, t + B), m->stream);
+  const float l = m->train(dX.p, dt.p, B, epochs, batch, lr);
+  if (loss) *loss = l;
+  HSS_CATCH
+}
+
+int hss_mlp_predict(hss_mlp* M, const float* X, int32_t B, float* y) {
+  HSS_TRY
+  HSS_REQUIRE(M && M->impl && X && y && B >= 0, HSS_ERR_ARG, "bad arguments");
+  if (B == 0) return HSS_OK;
+  MLP* m = M->impl;
+  DevBuf<float> dX, dy(B);
+  dX.upload(std::vector<float>(X, X + (size_t)B * m->nin), m->stream);
+  m->forward(dX.p, dy.p, B, m->stream);
+  HSS_CUDA(cudaMemcpyAsync(y, dy.p, B * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+  HSS_CUDA(cudaStreamSynchronize(m->stream));
+  HSS_CATCH
+}
+
+int hss_mlp_destroy(hss_mlp* M) {
+  HSS_TRY
+  if (M) {
+    delete M->impl;
+    delete M;
+  }
   HSS_CATCH
 }
 
@@ -512,7 +654,7 @@ int hss_batched_id_device(const double* d_A, int32_t m, int32_t n, int32_t batch
   for (int b = 0; b < batch; ++b)
     P[b] = IdP{d_A + (size_t)b * m * n, W.p + (size_t)b * m * n, m, n, d_perm + (size_t)b * n, d_rank + b,
                d_T + (size_t)b * n * n, -1, SW.p + (size_t)b * n * n, SV.p + (size_t)b * n * n,
-               x.p + (size_t)b * 2 * n, y.p + (size_t)b * (m + n), b, 0, (unsigned long long)seed};
+               x.p + (size_t)b * 2 * n, y.p + (size_t)b * (m + n), b, -1, (unsigned long long)seed, nullptr};
   DevBuf<IdP> dP(batch);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(IdP), cudaMemcpyHostToDevice, s));
   id_adaptive_batched(dP.p, batch, acc, s);

@@ -1091,7 +1091,21 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     if (lane == 0) norms[c] = d;
   }
   __syncthreads();
+  // Learned-rank mode: at step steps_hint, stop if |R_jj| is already below the
+  // rank threshold with room for two relaxations of the randomized check; if not,
+  // look again after another half as many steps.  Pivoted QR with exact column
+  // norms has non-increasing |R_jj|, so the rank count, the first k pivots and T
+  // equal those of the full factorization.
+  int s_hint = (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
+  int jdone = l;
   for (int j = 0; j < l; ++j) {
+    if (j == s_hint && j > 0) {
+      if (fabs(W[(size_t)(j - 1) * (m + 1)]) <= fabs(W[0]) * acc * 0.5625) {
+        jdone = j;
+        break;
+      }
+      s_hint = min(l, j + max(4, j / 2));
+    }
     double best = -1.0;
     int bi = INT_MAX;
     for (int c = j + tid; c < n; c += 256) {
@@ -1141,11 +1155,11 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     }
     __syncthreads();
   }
-  // rank detection (Common/ID.m:51-52)
+  // rank detection (Common/ID.m:51-52) over the computed diagonal
   double Rmx = (l > 0) ? fabs(W[0]) * acc : 0.0;
   auto count_rank = [&](double thr) {
     int cnt = 0;
-    for (int i = tid; i < l; i += 256) cnt += (fabs(W[i + (size_t)i * m]) > thr) ? 1 : 0;
+    for (int i = tid; i < jdone; i += 256) cnt += (fabs(W[i + (size_t)i * m]) > thr) ? 1 : 0;
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     __syncthreads();
     if (lane == 0) shi[w] = cnt;
@@ -1166,10 +1180,12 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     const int r = n - k;
     const unsigned long long st0 = ((unsigned long long)p.problem << 8) | (unsigned)(draw & 0xFF);
     const unsigned long long st1 = ((unsigned long long)p.problem << 8) | (unsigned)((draw + 1) & 0xFF);
-    // two unit random vectors: x[0:r] for the error, x[n:n+r] for the norm
+    // two unit random vectors: x[0:r] for the error, x[n:n+r] for the norm; entry i is
+    // drawn at the residual column's own index, independent of the residual order
     double pa = 0.0, pb = 0.0;
     for (int i = tid; i < r; i += 256) {
-      const double a = rng_uniform(seed, st0, i), b = rng_uniform(seed, st1, i);
+      const int c = p.perm[k + i];
+      const double a = rng_uniform(seed, st0, c), b = rng_uniform(seed, st1, c);
       x[i] = a; x[n + i] = b;
       pa += a * a; pb += b * b;
     }
@@ -1182,12 +1198,24 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     const double nr = id_rand_norm(p, k, x + n, y, sh);
     if (!(e > nr * acc)) break;
     Rmx = 0.75 * Rmx;
+    if (jdone < l && !(fabs(W[(size_t)(jdone - 1) * (m + 1)]) <= Rmx)) {
+      // the relaxed threshold reaches past the truncated factorization: rerun in full
+      if (tid == 0 && p.stat) p.stat[0] = 2;
+      if (tid == 0) *p.rank = k;
+      return;
+    }
     k = count_rank(Rmx);
     id_trisolve(W, m, n, k, p.T);
     __syncthreads();
     if (draw > 250) break;
   }
-  if (tid == 0) *p.rank = k;
+  if (tid == 0) {
+    *p.rank = k;
+    if (p.stat) {
+      p.stat[0] = (jdone < l) ? 1 : 0;
+      p.stat[1] = jdone;
+    }
+  }
 }
 
 void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s) {

@@ -88,8 +88,9 @@ struct IdP {
   double* x;        // 2*n workspace (random vectors)
   double* y;        // m+n workspace
   int problem;      // id for the random stream (2*box + side, box local to its tree)
-  int status;       // spare
+  int steps_hint;   // > 0: stop the pivoted QR after this many steps if the rank is resolved
   unsigned long long seed;  // key of the random stream (one per independent problem)
+  int* stat;        // out (may be null): [0] 0 full / 1 truncated / 2 needs a full rerun, [1] QR steps done
 };
 
 void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s);

@@ -13,6 +13,8 @@
 //  applyinv : HSS1D/HSS1D_applyinv_nsym.m:43-86.
 #include "hss1d.h"
 
+#include <chrono>
+
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -178,9 +180,17 @@ HSS1D::~HSS1D() {
 }
 
 void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, const long long* ldx, int leaf_,
-                     double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds) {
+                     double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds, MLP* mlp) {
   HSS_REQUIRE(np_ >= 1 && Np && Xp && ldx && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
   HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
+  using clk = std::chrono::steady_clock;
+  std::fill(phase_s, phase_s + NPHASE, 0.0);
+  auto tick = clk::now();
+  auto lap = [&](int ph) {
+    const auto t = clk::now();
+    phase_s[ph] += std::chrono::duration<double>(t - tick).count();
+    tick = t;
+  };
   nprob = np_; leaf = leaf_; acc = acc_; kp = kp_;
   kdev = make_kernel_dev(kp);
   pN.assign(Np, Np + nprob);
@@ -265,8 +275,14 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     l.erase(std::remove(l.begin(), l.end(), b), l.end());
     std::sort(l.begin(), l.end());
   }
-  // ---- point table: Ntot points + NPROXY proxies per box
-  const size_t npts = (size_t)Ntot + (size_t)NPROXY * nboxes;
+  // ---- point table: Ntot points + NPROXY proxies per non-root box; a box's proxy slot
+  // follows the order levels are compressed in, so each level uploads one contiguous range
+  std::vector<int> pslot(nboxes, -1);
+  int nslot = 0;
+  for (int L = maxlev; L >= 1; --L)
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == L) pslot[b] = nslot++;
+  const size_t npts = (size_t)Ntot + (size_t)NPROXY * nslot;
   HSS_REQUIRE(npts < (1ULL << 31), HSS_ERR_ARG, "point table exceeds 2^31 entries");
   std::vector<double> hx(npts, 0.0), hy(npts, 0.0), hnx(npts, 0.0), hny(npts, 0.0), hw(npts, 0.0),
       hk(npts, 0.0);
@@ -274,6 +290,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     hx[i] = X[6 * i]; hy[i] = X[6 * i + 1]; hnx[i] = X[6 * i + 2]; hny[i] = X[6 * i + 3];
     hw[i] = X[6 * i + 4]; hk[i] = X[6 * i + 5];
   }
+  pts.reserve(npts);
+  pts.upload_range(0, (size_t)Ntot, hx.data(), hy.data(), hnx.data(), hny.data(), hw.data(), hk.data(), kp, stream);
   nskel.assign(nboxes, 0);
   kskel.assign(nboxes, 0);
   I_SKUP.assign(nboxes, {});
@@ -281,9 +299,14 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
   J_UP.assign(nboxes, {});
   J_DN.assign(nboxes, {});
   census.assign(4 * (size_t)nboxes, 0);
+  feat.assign((size_t)NFEAT * nboxes, 0.f);
+  qr_steps = qr_steps_full = 0;
+  reruns = 0;
+  HSS_REQUIRE(!mlp || mlp->nin == NFEAT, HSS_ERR_ARG, "rank predictor must take 8 features");
   std::vector<DevBuf<double>> Tkeep;  // per level: T of each ID problem (n x n, ld n)
   std::vector<std::vector<long long>> Toff(nboxes);
   std::vector<int> Tlev(nboxes, -1);
+  lap(0);
   for (int L = maxlev; L >= 1; --L) {
     std::vector<int> boxes;
     for (int b = 0; b < nboxes; ++b)
@@ -315,7 +338,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       // LOCAL_construct_circle: tt = linspace(0, 2 pi (1 - 1/n), n)
       const double stop = 2.0 * M_PI * (1.0 - 1.0 / NPROXY);
       const double step = stop / (double)(NPROXY - 1);
-      const size_t pb = (size_t)Ntot + (size_t)NPROXY * b;
+      const size_t pb = (size_t)Ntot + (size_t)NPROXY * pslot[b];
       for (int t = 0; t < NPROXY; ++t) {
         const double tt = (t == NPROXY - 1) ? stop : (double)t * step;
         const double c = std::cos(tt), s = std::sin(tt);
@@ -355,13 +378,34 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       }
       rows_out[q] = in_inside;
       rows_in[q] = out_inside;
+      {  // rank-predictor features of the box (all known before its ID)
+        double arc = 0.0, kmax = 0.0;
+        for (int i = off[b]; i < off[b] + cnt[b]; ++i) {
+          arc += X[6 * (size_t)i + 4];
+          kmax = std::max(kmax, std::fabs(X[6 * (size_t)i + 5]));
+        }
+        float* f = &feat[(size_t)NFEAT * b];
+        f[0] = (float)std::log2((double)out.size());
+        f[1] = (float)(-std::log10(acc) / 10.0);
+        f[2] = (float)std::log2(1.0 + (double)in_inside.size());
+        f[3] = (float)std::log2(1.0 + (double)out_inside.size());
+        f[4] = (float)((arc > 0.0) ? R / arc : 0.0);
+        f[5] = (float)(kmax * R);
+        f[6] = (float)L / 16.f;
+        f[7] = (float)kp.flag;
+      }
       for (int t = 0; t < NPROXY; ++t) {
         rows_out[q].push_back((int)(pb + t));
         rows_in[q].push_back((int)(pb + t));
       }
       HSS_REQUIRE(out.size() <= 4096, HSS_ERR_RANK, "skeleton set exceeds 4096 points");
     }
-    pts.upload(hx, hy, hnx, hny, hw, hk, kp, stream);
+    lap(1);
+    {
+      const size_t p0 = (size_t)Ntot + (size_t)NPROXY * pslot[boxes[0]];
+      pts.upload_range(p0, (size_t)NPROXY * nbL, hx.data() + p0, hy.data() + p0, hnx.data() + p0, hny.data() + p0,
+                       hw.data() + p0, hk.data() + p0, kp, stream);
+    }
     // index arrays and block storage
     std::vector<int> idx;
     std::vector<long long> o_ro(nbL), o_ri(nbL), o_out(nbL), o_in(nbL);
@@ -406,8 +450,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       const int b = boxes[pr / 2];
       const int lb = b - proot[prob[b]];  // box id local to its tree: the random stream of the oracle
       ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], pm[pr], pn[pr], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
-                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * lb + (pr & 1), 0,
-                   pseed[prob[b]]};
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * lb + (pr & 1), -1,
+                   pseed[prob[b]], nullptr};
     }
     long long maxe = 0;
     for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
@@ -415,12 +459,57 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     upload_vec(dkg, kg, stream);
     for (int o = 0; o < nprob2; o += 65535)
       kgen_batched<double>(dkg.p + o, std::min(65535, nprob2 - o), maxe, view(pts), kdev, stream);
+    lap(2);
+    DevBuf<int> stat((size_t)2 * nprob2);
+    stat.zero(stream);
+    for (int pr = 0; pr < nprob2; ++pr) ip[pr].stat = stat.p + 2 * pr;
+    if (mlp) {
+      // predicted rank fraction -> QR step budget of both IDs of the box
+      std::vector<float> fx((size_t)NFEAT * nbL);
+      for (int q = 0; q < nbL; ++q)
+        std::copy(&feat[(size_t)NFEAT * boxes[q]], &feat[(size_t)NFEAT * boxes[q]] + NFEAT, &fx[(size_t)NFEAT * q]);
+      DevBuf<float> dfx, dy(nbL);
+      upload_vec(dfx, fx, stream);
+      mlp->forward(dfx.p, dy.p, nbL, stream);
+      std::vector<float> yh;
+      download(yh, dy.p, nbL, stream);
+      HSS_CUDA(cudaStreamSynchronize(stream));
+      for (int q = 0; q < nbL; ++q) {
+        const int n = (int)outs[q].size();
+        const int kh = (int)std::ceil((double)yh[q] * n);
+        const int hint = kh + std::max(4, (int)std::ceil(0.15 * kh));
+        ip[2 * q].steps_hint = hint;
+        ip[2 * q + 1].steps_hint = hint;
+      }
+    }
     DevBuf<IdP> dip;
     upload_vec(dip, ip, stream);
     id_adaptive_batched(dip.p, nprob2, acc, stream);
-    std::vector<int> hr;
+    std::vector<int> hr, hs;
     download(hr, rank.p, nprob2, stream);
+    download(hs, stat.p, (size_t)2 * nprob2, stream);
     HSS_CUDA(cudaStreamSynchronize(stream));
+    {
+      // boxes whose truncated factorization could not settle the rank are redone in full
+      std::vector<IdP> redo;
+      std::vector<int> redo_ix;
+      for (int pr = 0; pr < nprob2; ++pr)
+        if (hs[2 * pr] == 2) { IdP r = ip[pr]; r.steps_hint = -1; redo.push_back(r); redo_ix.push_back(pr); }
+      if (!redo.empty()) {
+        DevBuf<IdP> dr;
+        upload_vec(dr, redo, stream);
+        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream);
+        download(hr, rank.p, nprob2, stream);
+        download(hs, stat.p, (size_t)2 * nprob2, stream);
+        HSS_CUDA(cudaStreamSynchronize(stream));
+        reruns += (int)redo.size();
+        for (int pr : redo_ix) ip[pr].steps_hint = -1;
+      }
+    }
+    for (int pr = 0; pr < nprob2; ++pr) {
+      qr_steps += hs[2 * pr + 1];
+      qr_steps_full += std::min(pm[pr], pn[pr]);
+    }
     bool any = false;
     std::vector<int> kbox(nbL);
     for (int q = 0; q < nbL; ++q) {
@@ -431,12 +520,29 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q + 1], pn[2 * q + 1]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
     }
     if (any) {
+      // a fixed-rank re-ID needs R(0:k, :) of the full factorization up to k
+      std::vector<IdP> redo;
+      for (int pr = 0; pr < nprob2; ++pr)
+        if (ip[pr].force_k >= 0 && hs[2 * pr + 1] < ip[pr].force_k) {
+          IdP r = ip[pr];
+          r.force_k = -1;
+          r.steps_hint = -1;
+          redo.push_back(r);
+        }
+      if (!redo.empty()) {
+        DevBuf<IdP> dr;
+        upload_vec(dr, redo, stream);
+        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream);
+        HSS_CUDA(cudaStreamSynchronize(stream));
+        reruns += (int)redo.size();
+      }
       HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob2 * sizeof(IdP), cudaMemcpyHostToDevice, stream));
       id_fixed_batched(dip.p, nprob2, stream);
     }
     std::vector<int> hp;
     download(hp, perm.p, tP, stream);
     HSS_CUDA(cudaStreamSynchronize(stream));
+    lap(3);
     for (int q = 0; q < nbL; ++q) {
       const int b = boxes[q];
       const int n = (int)outs[q].size(), k = kbox[q];
@@ -454,6 +560,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       Tlev[b] = (int)Tkeep.size() - 1;
       census[4 * b] = pm[2 * q]; census[4 * b + 1] = pm[2 * q + 1]; census[4 * b + 2] = n; census[4 * b + 3] = k;
     }
+    lap(4);
   }
   // ---- compact T_UP / T_DN / T_DN^T and J arenas
   oT.assign(nboxes, 0);
@@ -538,6 +645,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     kgen_batched<double>(dkg.p + o, c, maxe, view(pts), kdev, stream);
   }
   HSS_CUDA(cudaStreamSynchronize(stream));
+  lap(5);
   inverted = false;
 }
 

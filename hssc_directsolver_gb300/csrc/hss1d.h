@@ -9,6 +9,7 @@
 
 #include "dense.cuh"
 #include "kgen.cuh"
+#include "mlp.h"
 
 namespace hss {
 
@@ -55,12 +56,23 @@ struct HSS1D {
   DevBuf<double> v1, v2, v3;
   // ID problem shapes of the last compress: (m_out, m_in, n, k) per non-root box
   std::vector<int> census;
+  // rank-predictor features per box (NFEAT floats, known before the box's ID)
+  static constexpr int NFEAT = 8;
+  std::vector<float> feat;
+  // learned-rank statistics: QR steps done, QR steps a full factorization takes, full reruns
+  long long qr_steps = 0, qr_steps_full = 0;
+  int reruns = 0;
+  // host wall seconds of the last compress: setup (trees, neighbours, points), level
+  // geometry, level uploads + launches, level GPU work up to the sync, level bookkeeping,
+  // final blocks
+  static constexpr int NPHASE = 6;
+  double phase_s[NPHASE] = {};
 
   HSS1D();
   ~HSS1D();
   // problem p: X_p is an N_p x 6 column-major block [x y nx ny w kappa] (ld ldx_p)
   void compress(int nprob, const long long* N, const double* const* Xp, const long long* ldx, int leaf, double acc,
-                const hss_kernel_params& kp, const unsigned long long* seeds);
+                const hss_kernel_params& kp, const unsigned long long* seeds, MLP* mlp = nullptr);
   void invert();
   void applyinv_device(const double* dX, double* dY, int nrhs);
   void apply_device(const double* dX, double* dY, int nrhs);

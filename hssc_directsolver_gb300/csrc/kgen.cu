@@ -33,6 +33,29 @@ void PointTable::upload(const std::vector<double>& hx, const std::vector<double>
   HSS_CUDA(cudaStreamSynchronize(s));
 }
 
+void PointTable::reserve(size_t n) {
+  x.alloc(n); y.alloc(n); nx.alloc(n); ny.alloc(n); w.alloc(n); kap.alloc(n); bval.alloc(n); cval.alloc(n);
+  count = (int)n;
+}
+
+void PointTable::upload_range(size_t first, size_t n, const double* hx, const double* hy, const double* hnx,
+                              const double* hny, const double* hw, const double* hkap, const hss_kernel_params& kp,
+                              cudaStream_t s) {
+  HSS_REQUIRE(first + n <= (size_t)count, HSS_ERR_ARG, "point range outside the table");
+  if (n == 0) return;
+  std::vector<double> b(n), c(n);
+  for (size_t i = 0; i < n; ++i) {
+    b[i] = modulation(kp.b_alpha, kp.b_x0, kp.b_y0, kp.b_isig, hx[i], hy[i]);
+    c[i] = modulation(kp.c_alpha, kp.c_x0, kp.c_y0, kp.c_isig, hx[i], hy[i]);
+  }
+  const size_t bytes = n * sizeof(double);
+  const double* src[8] = {hx, hy, hnx, hny, hw, hkap, b.data(), c.data()};
+  double* dst[8] = {x.p, y.p, nx.p, ny.p, w.p, kap.p, bval.p, cval.p};
+  for (int a = 0; a < 8; ++a)
+    HSS_CUDA(cudaMemcpyAsync(dst[a] + first, src[a], bytes, cudaMemcpyHostToDevice, s));
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
 __device__ __forceinline__ double kernel_entry(const KernelDev& k, const PointView& P, int t, int s) {
   const double dx = __dadd_rn(P.x[t], -P.x[s]);
   const double dy = __dadd_rn(P.y[t], -P.y[s]);

@@ -27,6 +27,11 @@ struct PointTable {
               const std::vector<double>& hnx, const std::vector<double>& hny,
               const std::vector<double>& hw, const std::vector<double>& hkap,
               const hss_kernel_params& kp, cudaStream_t s);
+  // allocate n entries (contents undefined), then fill entries [first, first+n) piecewise
+  void reserve(size_t n);
+  void upload_range(size_t first, size_t n, const double* hx, const double* hy, const double* hnx,
+                    const double* hny, const double* hw, const double* hkap, const hss_kernel_params& kp,
+                    cudaStream_t s);
 };
 
 struct PointView {

@@ -63,6 +63,28 @@ class HSS1DMatrix:
                                          ip(out["J_DN"]), dp(out["T_UP"]), dp(out["T_DN"])))
         return out
 
+    # --- learned ranks ----------------------------------------------------------
+    def features(self):
+        """(nboxes x 8 rank features, k/n of each box's plain ID) of the last compress."""
+        n = self.info()["nboxes"]
+        F = np.zeros((n, 8), np.float32)
+        y = np.zeros(n, np.float32)
+        L.check(L.lib().hss1d_features(self._h, L.ptr(F), L.ptr(y)))
+        return F, y
+
+    def phase_times(self):
+        """Host wall seconds of the last compress: setup, level geometry, level uploads,
+        level GPU work, level bookkeeping, final blocks."""
+        t = np.zeros(6)
+        L.check(L.lib().hss1d_phase_times(self._h, t.ctypes.data_as(L._DP)))
+        return t
+
+    def id_stats(self):
+        """(QR steps done, QR steps of full factorizations, boxes redone in full)."""
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int32()
+        L.check(L.lib().hss1d_id_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
 
 def _as_f64(a):
     a = np.asarray(a, dtype=np.float64)
@@ -87,9 +109,12 @@ def HSS1D_compress_nsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel
     return HSS1DMatrix(h, Xf.shape[0])
 
 
-def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None) -> HSS1DMatrix:
+def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None,
+                         predictor=None) -> HSS1DMatrix:
     """Many independent curves compressed together (every level of every tree in the
-    same launches).  Vectors of the returned matrix are the problems' vectors stacked."""
+    same launches).  Vectors of the returned matrix are the problems' vectors stacked.
+    With a ``RankPredictor`` the IDs stop their pivoted QR early at the predicted rank;
+    the result equals the plain compress."""
     mats = []
     for X in Xs:
         X = np.asarray(X, dtype=np.float64)
@@ -105,7 +130,11 @@ def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=No
     sd = (C.c_uint64 * P)(*seeds)
     h = C.c_void_p()
     kp = knl_params.to_c()
-    L.check(L.lib().hss1d_compress_batch(C.byref(h), P, N, ptrs, N, int(TREE), float(acc), C.byref(kp), sd))
+    if predictor is None:
+        L.check(L.lib().hss1d_compress_batch(C.byref(h), P, N, ptrs, N, int(TREE), float(acc), C.byref(kp), sd))
+    else:
+        L.check(L.lib().hss1d_compress_batch_learned(C.byref(h), P, N, ptrs, N, int(TREE), float(acc),
+                                                     C.byref(kp), sd, predictor._h))
     M = HSS1DMatrix(h, int(sum(m.shape[0] for m in mats)))
     M.sizes = [m.shape[0] for m in mats]
     return M

@@ -106,6 +106,45 @@ int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t 
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
 int hss1d_destroy(hss1d_matrix* H);
 
+/* ---- learned ranks (HSS1D) ---------------------------------------------- */
+/* A small MLP (nin -> 32 -> 32 -> 1, ReLU, sigmoid) predicting the ID rank fraction k/n of a
+ * box from features known before its ID.  It replaces the reference's hand-fitted rank table
+ * (HSS2D/predict_rank.m:5-23): the learned compress below uses the prediction only to stop
+ * the pivoted QR early, so ranks, skeletons and T equal those of the plain compress; a box
+ * whose rank check reaches past the truncated factorization is redone in full.
+ * Parameters: one float32 vector [W1 (32 x nin row-major), b1, W2 (32 x 32), b2, W3, b3]. */
+typedef struct hss_mlp hss_mlp;
+int hss_mlp_create(hss_mlp** out, int32_t nin, int32_t hidden, uint64_t seed);
+int hss_mlp_nparams(const hss_mlp* M, int32_t* nparams);
+int hss_mlp_get_params(const hss_mlp* M, float* params);
+int hss_mlp_set_params(hss_mlp* M, const float* params);
+/* gradient of 0.5*mean((y - t)^2) over B samples (X: B x nin row-major, host buffers);
+ * grad: nparams floats (NULL ok); loss may be NULL */
+int hss_mlp_grad(hss_mlp* M, const float* X, const float* t, int32_t B, float* grad, float* loss);
+/* Adam (lr, 0.9, 0.999, 1e-8) over `epochs` passes of minibatches of `batch` samples in order;
+ * loss = final full-batch loss (NULL ok) */
+int hss_mlp_train(hss_mlp* M, const float* X, const float* t, int32_t B, int32_t epochs,
+                  int32_t batch, float lr, float* loss);
+int hss_mlp_predict(hss_mlp* M, const float* X, int32_t B, float* y);
+int hss_mlp_destroy(hss_mlp* M);
+/* per-box rank features of the last compress (nboxes x 8 row-major floats; roots are 0):
+ * log2 n, -log10(acc)/10, log2(1+near in-skeletons), log2(1+near out-skeletons),
+ * radius / arc length, max|curvature| * radius, level / 16, kernel flag.
+ * rank_frac[b] = k/n of the box's plain ID (NULL ok). */
+int hss1d_features(const hss1d_matrix* H, float* feat, float* rank_frac);
+/* QR steps done by the last compress, steps a full factorization takes, boxes redone in full */
+int hss1d_id_stats(const hss1d_matrix* H, int64_t* qr_steps, int64_t* qr_steps_full,
+                   int32_t* reruns);
+/* host wall seconds of the last compress by phase (6 entries): setup (trees, neighbour lists,
+ * point upload), per-level geometry, per-level uploads and launches, per-level GPU work up to
+ * its sync, per-level bookkeeping, final blocks (the reference's tic/toc reports) */
+int hss1d_phase_times(const hss1d_matrix* H, double* seconds);
+/* hss1d_compress_batch with a rank predictor (M: 8 inputs) bounding each ID's QR steps */
+int hss1d_compress_batch_learned(hss1d_matrix** out, int32_t nprob, const int64_t* N,
+                                 const double* const* X, const int64_t* ldx, int32_t leaf,
+                                 double acc, const hss_kernel_params* kp, const uint64_t* seeds,
+                                 hss_mlp* M);
+
 /* ---- HSS2D (planar volumes) -------------------------------------------- */
 typedef struct hss2d_matrix hss2d_matrix;
 

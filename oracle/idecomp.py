@@ -55,8 +55,12 @@ def pivoted_qr(A: np.ndarray, pivot: bool = True):
     return R, perm
 
 
-def _rand_unit(seed, problem, draw, r):
-    x = rng.uniform(seed, rng.id_stream(problem, draw), r)
+def _rand_unit(seed, problem, draw, cols):
+    """Unit random vector over the residual columns ``cols``: entry i is drawn at
+    counter ``cols[i]`` (the column's own index), so the vector does not depend on
+    the order in which the factorization left the residual columns."""
+    n = int(np.max(cols)) + 1 if len(cols) else 0
+    x = rng.uniform(seed, rng.id_stream(problem, draw), n)[np.asarray(cols, dtype=np.int64)]
     return x / np.linalg.norm(x)
 
 
@@ -94,9 +98,8 @@ def id_adaptive(A: np.ndarray, acc: float, seed: int = 0, problem: int = 0):
     l = min(m, n)
     draw = 0
     while k < l:
-        r = n - k
-        xe = _rand_unit(seed, problem, draw, r)
-        xn = _rand_unit(seed, problem, draw + 1, r)
+        xe = _rand_unit(seed, problem, draw, I[k:])
+        xn = _rand_unit(seed, problem, draw + 1, I[k:])
         draw += 2
         if not (rand_error(A, T, I, k, xe) > rand_norm(A, I, k, xn) * acc):
             break
