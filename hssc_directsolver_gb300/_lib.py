@@ -63,12 +63,15 @@ SIGNATURES = {
     "hss_device_count": (C.c_int, [_I32P]),
     "hss1d_compress": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                  C.POINTER(hss_kernel_params), C.c_uint64]),
+    "hss1d_compress_fsym": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
+                                      C.POINTER(hss_kernel_params), C.c_uint64]),
     "hss1d_compress_batch": (C.c_int, [C.POINTER(_P), C.c_int32, _I64P, C.POINTER(C.c_void_p), _I64P, C.c_int32,
                                        C.c_double, C.POINTER(hss_kernel_params), C.POINTER(C.c_uint64)]),
     "hss1d_forest_info": (C.c_int, [_P, _I32P, _I64P, _I32P, _I64P]),
     "hss1d_info": (C.c_int, [_P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P]),
     "hss1d_export_box": (C.c_int, [_P, C.c_int32, _I32P, _I32P, _I32P, _I32P, _DP, _DP]),
     "hss1d_invert": (C.c_int, [_P]),
+    "hss1d_transforminv": (C.c_int, [_P, C.POINTER(_P)]),
     "hss1d_apply": (C.c_int, [_P, _P, _P, C.c_int32]),
     "hss1d_applyinv": (C.c_int, [_P, _P, _P, C.c_int32]),
     "hss1d_applyinv_device": (C.c_int, [_P, _P, _P, C.c_int32, _P]),

@@ -81,14 +81,14 @@ int hss_device_count(int* count) {
 // ---------------------------------------------------------------- HSS1D --
 static void hss1d_make(hss1d_matrix** out, int nprob, const long long* N, const double* const* X,
                        const long long* ldx, int leaf, double acc, const hss_kernel_params* kp,
-                       const unsigned long long* seeds, MLP* mlp = nullptr) {
+                       const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false) {
   HSS_REQUIRE(out && X && kp && N && ldx, HSS_ERR_ARG, "NULL argument");
   require_device();
   *out = nullptr;
   auto* h = new hss1d_matrix{nullptr};
   try {
     h->impl = new HSS1D();
-    h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds, mlp);
+    h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds, mlp, sym);
   } catch (...) {
     delete h->impl;
     delete h;
@@ -103,6 +103,15 @@ int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, 
   const long long n = N, l = ldx;
   const unsigned long long sd = seed;
   hss1d_make(out, 1, &n, &X, &l, leaf, acc, kp, &sd);
+  HSS_CATCH
+}
+
+int hss1d_compress_fsym(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf, double acc,
+                        const hss_kernel_params* kp, uint64_t seed) {
+  HSS_TRY
+  const long long n = N, l = ldx;
+  const unsigned long long sd = seed;
+  hss1d_make(out, 1, &n, &X, &l, leaf, acc, kp, &sd, nullptr, true);
   HSS_CATCH
 }
 
@@ -392,6 +401,23 @@ int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t 
   if (s) HSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
   cudaEventDestroy(ev);
   if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss1d_transforminv(hss1d_matrix* H, hss1d_matrix** out) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && out, HSS_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* k = new hss1d_matrix{nullptr};
+  try {
+    k->impl = new HSS1D();
+    H->impl->transforminv(*k->impl);
+  } catch (...) {
+    delete k->impl;
+    delete k;
+    throw;
+  }
+  *out = k;
   HSS_CATCH
 }
 

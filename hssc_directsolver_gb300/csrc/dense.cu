@@ -988,8 +988,44 @@ __device__ __forceinline__ double rng_uniform(unsigned long long seed, unsigned 
 }
 
 // T(0:k, 0:n-k) = R(0:k,0:k) \ R(0:k, k:n); T has leading dimension n.
+// Back substitution R(0:r0+1, 0:r0+1) x = b for one column held by a warp in
+// registers (tv[q] = row lane + 32 q, rows < 128).  Same operations in the same
+// order as the shared-column form below, so both give the same bits.
+__device__ __forceinline__ void warp_backsolve128(const double* W, int m, int r0, double (&tv)[4]) {
+  const int lane = threadIdx.x & 31;
+  for (int r = r0; r >= 0; --r) {
+    const int s = r >> 5;
+    const double v = (s == 0) ? tv[0] : (s == 1) ? tv[1] : (s == 2) ? tv[2] : tv[3];
+    const double xr = __shfl_sync(0xffffffffu, v, r & 31) / W[r + (size_t)r * m];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = lane + 32 * q;
+      if (i < r) tv[q] -= W[i + (size_t)r * m] * xr;
+      else if (i == r) tv[q] = xr;
+    }
+  }
+}
+
 __device__ void id_trisolve(const double* W, int m, int n, int k, double* T) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (k <= 128) {
+    for (int c = k + w; c < n; c += 8) {
+      double tv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = lane + 32 * q;
+        tv[q] = (i < k) ? W[i + (size_t)c * m] : 0.0;
+      }
+      warp_backsolve128(W, m, k - 1, tv);
+      double* t = T + (size_t)(c - k) * n;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = lane + 32 * q;
+        if (i < k) t[i] = tv[q];
+      }
+    }
+    return;
+  }
   for (int c = k + w; c < n; c += 8) {
     double* t = T + (size_t)(c - k) * n;
     for (int i = lane; i < k; i += 32) t[i] = W[i + (size_t)c * m];
@@ -1225,21 +1261,49 @@ void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s) {
   check_launch("k_id_adaptive");
 }
 
-// Fixed-rank ID reusing the pivoted QR in W: one-sided Jacobi SVD of
-// R11 = W(0:k,0:k), then T = V_q diag(1/s_q) U_q^T R12 with s > 1e-12
-// (skel_col_fixed, Common/ID.m:106-113).
+// Fixed-rank ID reusing the pivoted QR in W: T = V_q diag(1/s_q) U_q^T R12 over
+// the singular triplets of R11 = W(0:k,0:k) with s > 1e-12 (skel_col_fixed,
+// Common/ID.m:106-113).  When every singular value is provably above the cut --
+// 1/||R11^-1||_F <= s_min -- the pseudo-inverse is the inverse and T = R11 \ R12
+// by back substitution; otherwise a one-sided Jacobi SVD applies the cut.
 __global__ void __launch_bounds__(256) k_id_fixed(const IdP* __restrict__ P) {
   const IdP p = P[blockIdx.x];
   const int k = p.force_k;
   if (k < 0) return;
   const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const double* Wq = p.W;
-  double* U = p.svdW;  // k x k, ld k
+  __shared__ double sh[8];
+  if (k >= 1 && k <= 128) {
+    double part = 0.0;
+    for (int c = w; c < k; c += 8) {  // column c of R11^-1 (zero below row c)
+      double tv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tv[q] = (lane + 32 * q == c) ? 1.0 : 0.0;
+      warp_backsolve128(Wq, m, c, tv);
+      double ss = 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) ss += tv[q] * tv[q];
+      ss = warp_sum(ss);
+      if (lane == 0) part += ss;
+    }
+    const double fro2 = block_sum256(part, sh);
+    if (1.0 / sqrt(fro2) > 2e-12) {  // factor-2 margin over rounding in the computed inverse
+      id_trisolve(Wq, m, n, k, p.T);
+      if (tid == 0) *p.rank = k;
+      return;
+    }
+  }
+  // One-sided Jacobi on X = R11^T (R11 comes from a column-pivoted QR, which
+  // makes the columns of its transpose nearly orthogonal: few sweeps, as in
+  // Drmac & Veselic, "New fast and accurate Jacobi SVD algorithm", SIMAX 2008).
+  // X V = M with orthogonal columns M_q = s_q u_q, so R11 = V S U^T and
+  // pinv(R11) = sum_q M_q V_q^T / s_q^2.
+  double* U = p.svdW;  // k x k, ld k: X, rotated into M
   double* V = p.svdV;  // k x k, ld k
   __shared__ int s_rot;
   for (int e = tid; e < k * k; e += 256) {
     const int i = e % k, j = e / k;
-    U[e] = (i <= j) ? Wq[i + (size_t)j * m] : 0.0;
+    U[e] = (j <= i) ? Wq[j + (size_t)i * m] : 0.0;
     V[e] = (i == j) ? 1.0 : 0.0;
   }
   __syncthreads();
@@ -1290,7 +1354,7 @@ __global__ void __launch_bounds__(256) k_id_fixed(const IdP* __restrict__ P) {
     if (lane == 0) s2[c] = d;
   }
   __syncthreads();
-  // T(:, c) = sum_{i: s_i > 1e-12} v_i (w_i . R12(:,c)) / s_i^2
+  // T(:, c) = sum_{q: s_q > 1e-12} M_q (V_q . R12(:,c)) / s_q^2
   for (int c = k + w; c < n; c += 8) {
     double* t = p.T + (size_t)(c - k) * n;
     for (int i = lane; i < k; i += 32) t[i] = 0.0;
@@ -1298,9 +1362,9 @@ __global__ void __launch_bounds__(256) k_id_fixed(const IdP* __restrict__ P) {
     for (int q = 0; q < k; ++q) {
       if (!(sqrt(s2[q]) > 1e-12)) continue;
       double d = 0.0;
-      for (int i = lane; i < k; i += 32) d += U[i + (size_t)q * k] * Wq[i + (size_t)c * m];
+      for (int i = lane; i < k; i += 32) d += V[i + (size_t)q * k] * Wq[i + (size_t)c * m];
       d = warp_sum(d) / s2[q];
-      for (int i = lane; i < k; i += 32) t[i] += V[i + (size_t)q * k] * d;
+      for (int i = lane; i < k; i += 32) t[i] += U[i + (size_t)q * k] * d;
       __syncwarp();
     }
   }

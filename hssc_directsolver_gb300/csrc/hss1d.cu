@@ -180,7 +180,8 @@ HSS1D::~HSS1D() {
 }
 
 void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, const long long* ldx, int leaf_,
-                     double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds, MLP* mlp) {
+                     double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds, MLP* mlp,
+                     bool sym_) {
   HSS_REQUIRE(np_ >= 1 && Np && Xp && ldx && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
   HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
   using clk = std::chrono::steady_clock;
@@ -191,7 +192,10 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     phase_s[ph] += std::chrono::duration<double>(t - tick).count();
     tick = t;
   };
-  nprob = np_; leaf = leaf_; acc = acc_; kp = kp_;
+  nprob = np_; leaf = leaf_; acc = acc_; kp = kp_; sym = sym_;
+  // ID problems per box: outgoing and incoming (nsym), or the outgoing one only (fsym,
+  // HSS1D_compress_fsym.m:186-198, whose incoming skeletons equal the outgoing ones)
+  const int ps = sym ? 1 : 2;
   kdev = make_kernel_dev(kp);
   pN.assign(Np, Np + nprob);
   pbase.assign(nprob, 0);
@@ -417,13 +421,13 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     }
     DevBuf<int> didx;
     upload_vec(didx, idx, stream);
-    const int nprob2 = 2 * nbL;
+    const int nprob2 = ps * nbL;
     std::vector<long long> oA(nprob2), oT2(nprob2), oX(nprob2), oY(nprob2), oP(nprob2);
     long long tA = 0, tT = 0, tX = 0, tY = 0, tP = 0;
     std::vector<int> pm(nprob2), pn(nprob2);
     for (int q = 0; q < nbL; ++q) {
-      for (int s = 0; s < 2; ++s) {
-        const int pr = 2 * q + s;
+      for (int s = 0; s < ps; ++s) {
+        const int pr = ps * q + s;
         const int m = (int)(s == 0 ? rows_out[q].size() : rows_in[q].size());
         const int n = (int)outs[q].size();
         pm[pr] = m; pn[pr] = n;
@@ -441,16 +445,16 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     std::vector<KgenP<double>> kg(nprob2);
     std::vector<IdP> ip(nprob2);
     for (int q = 0; q < nbL; ++q) {
-      const int n = (int)outs[q].size();
-      kg[2 * q] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[2 * q], n, A.p + oA[2 * q], pm[2 * q], 0};
-      kg[2 * q + 1] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], n, pm[2 * q + 1], A.p + oA[2 * q + 1],
-                                    pm[2 * q + 1], 1};
+      const int n = (int)outs[q].size(), po = ps * q;
+      kg[po] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[po], n, A.p + oA[po], pm[po], 0};
+      if (!sym)
+        kg[po + 1] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], n, pm[po + 1], A.p + oA[po + 1], pm[po + 1], 1};
     }
     for (int pr = 0; pr < nprob2; ++pr) {
-      const int b = boxes[pr / 2];
+      const int b = boxes[pr / ps], s = pr % ps;
       const int lb = b - proot[prob[b]];  // box id local to its tree: the random stream of the oracle
       ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], pm[pr], pn[pr], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
-                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * lb + (pr & 1), -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * lb + s, -1,
                    pseed[prob[b]], nullptr};
     }
     long long maxe = 0;
@@ -478,8 +482,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
         const int n = (int)outs[q].size();
         const int kh = (int)std::ceil((double)yh[q] * n);
         const int hint = kh + std::max(4, (int)std::ceil(0.15 * kh));
-        ip[2 * q].steps_hint = hint;
-        ip[2 * q + 1].steps_hint = hint;
+        for (int s = 0; s < ps; ++s) ip[ps * q + s].steps_hint = hint;
       }
     }
     DevBuf<IdP> dip;
@@ -513,11 +516,12 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     bool any = false;
     std::vector<int> kbox(nbL);
     for (int q = 0; q < nbL; ++q) {
-      const int ko = hr[2 * q], ki = hr[2 * q + 1];
+      const int ko = hr[ps * q], ki = hr[ps * q + ps - 1];
       const int k = std::max(ko, ki);
       kbox[q] = k;
-      if (k != ko) { ip[2 * q].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q], pn[2 * q]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
-      else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[2 * q + 1], pn[2 * q + 1]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+      const int po = ps * q, pi = ps * q + ps - 1;
+      if (k != ko) { ip[po].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[po], pn[po]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+      else if (k != ki) { ip[pi].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[pi], pn[pi]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
     }
     if (any) {
       // a fixed-rank re-ID needs R(0:k, :) of the full factorization up to k
@@ -545,20 +549,20 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     lap(3);
     for (int q = 0; q < nbL; ++q) {
       const int b = boxes[q];
-      const int n = (int)outs[q].size(), k = kbox[q];
+      const int n = (int)outs[q].size(), k = kbox[q], po = ps * q, pi = ps * q + ps - 1;
       nskel[b] = n;
       kskel[b] = k;
-      J_UP[b].assign(hp.begin() + oP[2 * q], hp.begin() + oP[2 * q] + n);
-      J_DN[b].assign(hp.begin() + oP[2 * q + 1], hp.begin() + oP[2 * q + 1] + n);
+      J_UP[b].assign(hp.begin() + oP[po], hp.begin() + oP[po] + n);
+      J_DN[b].assign(hp.begin() + oP[pi], hp.begin() + oP[pi] + n);
       I_SKUP[b].resize(k);
       I_SKDN[b].resize(k);
       for (int t = 0; t < k; ++t) {
         I_SKUP[b][t] = outs[q][J_UP[b][t]];
         I_SKDN[b][t] = inns[q][J_DN[b][t]];
       }
-      Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
+      Toff[b] = {oT2[po], oT2[pi]};
       Tlev[b] = (int)Tkeep.size() - 1;
-      census[4 * b] = pm[2 * q]; census[4 * b + 1] = pm[2 * q + 1]; census[4 * b + 2] = n; census[4 * b + 3] = k;
+      census[4 * b] = pm[po]; census[4 * b + 1] = pm[pi]; census[4 * b + 2] = n; census[4 * b + 3] = k;
     }
     lap(4);
   }
@@ -615,7 +619,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     }
     if (!is_leaf(b)) {
       push(I_SKDN[c1[b]]); push(I_SKUP[c2[b]]);
-      push(I_SKDN[c2[b]]); push(I_SKUP[c1[b]]);
+      if (!sym) { push(I_SKDN[c2[b]]); push(I_SKUP[c1[b]]); }
     }
   }
   DevBuf<int> didx;
@@ -631,9 +635,11 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       const int* a = didx.p + io[q++];
       const int* bb = didx.p + io[q++];
       kg.push_back(KgenP<double>{a, bb, kskel[s1], kskel[s2], M_SIB.p + oSib[s1], kskel[s1], 0});
-      const int* c = didx.p + io[q++];
-      const int* d = didx.p + io[q++];
-      kg.push_back(KgenP<double>{c, d, kskel[s2], kskel[s1], M_SIB.p + oSib[s2], kskel[s2], 0});
+      if (!sym) {
+        const int* c = didx.p + io[q++];
+        const int* d = didx.p + io[q++];
+        kg.push_back(KgenP<double>{c, d, kskel[s2], kskel[s1], M_SIB.p + oSib[s2], kskel[s2], 0});
+      }
     }
   }
   long long maxe = 0;
@@ -644,9 +650,194 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     const int c = (int)std::min<size_t>(65535, kg.size() - o);
     kgen_batched<double>(dkg.p + o, c, maxe, view(pts), kdev, stream);
   }
+  if (sym) {  // M_SIB{c2} = M_SIB{c1}.' (HSS1D_compress_fsym.m:245)
+    std::vector<MoveP> mv;
+    for (int b = 0; b < nboxes; ++b)
+      if (!is_leaf(b) && kskel[c1[b]] > 0 && kskel[c2[b]] > 0)
+        mv.push_back(MoveP{M_SIB.p + oSib[c1[b]], M_SIB.p + oSib[c2[b]], nullptr, kskel[c1[b]], kskel[c2[b]],
+                           kskel[c1[b]], kskel[c2[b]], 3, 0});
+    run_moves(mv, stream);
+  }
   HSS_CUDA(cudaStreamSynchronize(stream));
   lap(5);
   inverted = false;
+}
+
+// ---------------------------------------------------------------------------
+// Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv), HSS1D/HSS1D_transforminv_nsym.m:38-161.
+// Rewrites the inverse factors as an HSS1D matrix in the compressed format, so that the
+// forward apply of K applies the inverse.  Three tree sweeps, each level batched over every
+// box of every problem: (1) top-down, the diagonal blocks of each parent's Dinv (FTinv at
+// the top) move into its sons' Dinv as L * block * R (:38-77); (2) bottom-up, each box's
+// Linv/Rinv become [I; T] form through P = Linv(J_UP(1:k),:) and Q = Rinv(:,J_DN(1:k)), whose
+// factors move into the parent's rows and columns (:83-125); (3) the parents' off-diagonal
+// blocks become sibling matrices and the leaves' Dinv the self blocks (:128-161).
+void HSS1D::transforminv(HSS1D& K) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "transforminv needs the inverse factors (call invert first)");
+  K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;
+  K.pN = pN; K.pbase = pbase; K.proot = proot; K.pseed = pseed;
+  K.prob = prob; K.level = level; K.parent = parent; K.c1 = c1; K.c2 = c2; K.off = off; K.cnt = cnt;
+  K.nskel = nskel; K.kskel = kskel; K.I_SKUP = I_SKUP; K.I_SKDN = I_SKDN;
+  K.J_UP = J_DN;  // Kinv's up projection comes from Rinv, whose skeleton order is J_DN (:151-154)
+  K.J_DN = J_UP;
+  K.X = X; K.kp = kp; K.kdev = kdev; K.census = census;
+  K.oT = oT; K.oSelf = oSelf; K.oSib = oSib; K.oJ = oJ;
+  K.inverted = false;
+  const cudaStream_t st = stream;
+  auto d2d = [&](DevBuf<double>& dst, const DevBuf<double>& src) {
+    dst.alloc(std::max<size_t>(src.n, 1));
+    if (src.n) HSS_CUDA(cudaMemcpyAsync(dst.p, src.p, src.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  };
+  K.JUPd.alloc(std::max<size_t>(JDNd.n, 1));
+  K.JDNd.alloc(std::max<size_t>(JUPd.n, 1));
+  if (JDNd.n) HSS_CUDA(cudaMemcpyAsync(K.JUPd.p, JDNd.p, JDNd.n * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  if (JUPd.n) HSS_CUDA(cudaMemcpyAsync(K.JDNd.p, JUPd.p, JUPd.n * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  K.T_UP.alloc(std::max<size_t>(T_UP.n, 1));
+  K.T_DN.alloc(std::max<size_t>(T_DN.n, 1));
+  K.TDNT.alloc(std::max<size_t>(TDNT.n, 1));
+  K.M_SELF.alloc(std::max<size_t>(M_SELF.n, 1));
+  K.M_SIB.alloc(std::max<size_t>(M_SIB.n, 1));
+  DevBuf<double> Lw, Rw, Dw, FTw;
+  d2d(Lw, Linv);
+  d2d(Rw, Rinv);
+  d2d(Dw, Dinv);
+  d2d(FTw, FTinv);
+  int maxk = 1;
+  for (int b = 0; b < nboxes; ++b) maxk = std::max(maxk, kskel[b]);
+  DevBuf<double> zero((size_t)maxk * maxk), Wt(std::max<size_t>(Linv.n, 1));
+  zero.zero(st);
+  // the block of box s's parent that belongs to s: (matrix, leading dim, offset of s)
+  auto parent_block = [&](int s, double*& B, int& ld, int& o) {
+    const int f = parent[s];
+    if (parent[f] < 0) { B = FTw.p + oFT[prob[f]]; ld = ktop[prob[f]]; }
+    else { B = Dw.p + oD[f]; ld = nskel[f]; }
+    o = (s == c2[f] && c1[f] >= 0) ? kskel[c1[f]] : 0;
+  };
+  // (1) top-down: D_s += L_s * D_f(ind_s, ind_s) * R_s, then clear that block
+  for (int Lv = 1; Lv <= maxlev; ++Lv) {
+    std::vector<GemmP<double>> G1, G2;
+    std::vector<MoveP> Z;
+    for (int s = 0; s < nboxes; ++s) {
+      if (level[s] != Lv) continue;
+      const int n = nskel[s], k = kskel[s];
+      if (k == 0) continue;
+      double* B;
+      int ld, o;
+      parent_block(s, B, ld, o);
+      double* blk = B + o + (size_t)o * ld;
+      G1.push_back(GemmP<double>{Lw.p + oL[s], blk, Wt.p + oL[s], n, k, k, n, ld, n});
+      G2.push_back(GemmP<double>{Wt.p + oL[s], Rw.p + oR[s], Dw.p + oD[s], n, n, k, n, k, n});
+      Z.push_back(MoveP{zero.p, blk, nullptr, k, k, k, ld, 0, 0});
+    }
+    run_gemms(G1, false, false, 1.0, 0.0, st);
+    run_gemms(G2, false, false, 1.0, 1.0, st);
+    run_moves(Z, st);
+  }
+  // (2) bottom-up: [I T] forms and the parents' row / column factors
+  for (int Lv = maxlev; Lv >= 1; --Lv) {
+    std::vector<int> boxes;
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == Lv && kskel[b] > 0) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    std::vector<long long> oq(boxes.size()), orr(boxes.size()), ocol(boxes.size());
+    long long tq = 0, tr = 0, tc = 0;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      const int b = boxes[i], k = kskel[b], f = parent[b];
+      const int nf = (parent[f] < 0) ? ktop[prob[f]] : nskel[f];
+      oq[i] = tq; tq += (long long)k * k;
+      orr[i] = tr; tr += (long long)k * (2 * nf);   // P * Lw_f(ind,:) and P * D_f(ind,:)
+      ocol[i] = tc; tc += (long long)(2 * nf) * k;  // Rw_f(:,ind) * Q and D_f(:,ind) * Q
+    }
+    DevBuf<double> Pm(tq), Qm(tq), Pi(tq), Qi(tq), Lr(std::max<size_t>(Linv.n, 1)), Rr(std::max<size_t>(Linv.n, 1)),
+        Tr(std::max(tr, 1LL)), Tc(std::max(tc, 1LL));
+    std::vector<MoveP> mv;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      const int b = boxes[i], n = nskel[b], k = kskel[b], nr = n - k;
+      mv.push_back(MoveP{Lw.p + oL[b], Pm.p + oq[i], JUPd.p + oJ[b], k, k, n, k, 0, 0});  // P = L(JC(1:k),:)
+      mv.push_back(MoveP{Rw.p + oR[b], Qm.p + oq[i], JDNd.p + oJ[b], k, k, k, k, 1, 0});  // Q = R(:,JR(1:k))
+      if (nr > 0) {
+        mv.push_back(MoveP{Lw.p + oL[b], Lr.p + oL[b], JUPd.p + oJ[b] + k, nr, k, n, nr, 0, 0});  // L(JC(k+1:n),:)
+        mv.push_back(MoveP{Rw.p + oR[b], Rr.p + oL[b], JDNd.p + oJ[b] + k, k, nr, k, k, 1, 0});  // R(:,JR(k+1:n))
+      }
+    }
+    run_moves(mv, st);
+    mv.clear();
+    for (size_t i = 0; i < boxes.size(); ++i) {  // copies to invert, after the gathers above
+      const int k = kskel[boxes[i]];
+      mv.push_back(MoveP{Pm.p + oq[i], Pi.p + oq[i], nullptr, k, k, k, k, 0, 0});
+      mv.push_back(MoveP{Qm.p + oq[i], Qi.p + oq[i], nullptr, k, k, k, k, 0, 0});
+    }
+    run_moves(mv, st);
+    std::vector<std::pair<double*, int>> mats;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      const int k = kskel[boxes[i]];
+      mats.push_back({Pi.p + oq[i], k});
+      mats.push_back({Qi.p + oq[i], k});
+    }
+    invert_many(mats, st);
+    // Kinv T_DN^T = L(JC(k+1:n),:) / P ; Kinv T_UP = Q \ R(:,JR(k+1:n))
+    std::vector<GemmP<double>> GL, GR;
+    mv.clear();
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      const int b = boxes[i], n = nskel[b], k = kskel[b], nr = n - k;
+      if (nr <= 0) continue;
+      GL.push_back(GemmP<double>{Lr.p + oL[b], Pi.p + oq[i], K.TDNT.p + oT[b], nr, k, k, nr, k, nr});
+      GR.push_back(GemmP<double>{Qi.p + oq[i], Rr.p + oL[b], K.T_UP.p + oT[b], k, nr, k, k, k, k});
+      mv.push_back(MoveP{K.TDNT.p + oT[b], K.T_DN.p + oT[b], nullptr, nr, k, nr, k, 3, 0});
+    }
+    run_gemms(GL, false, false, 1.0, 0.0, st);
+    run_gemms(GR, false, false, 1.0, 0.0, st);
+    run_moves(mv, st);
+    // parents: rows ind *= P (Linv_f and D_f), then columns ind *= Q (Rinv_f and D_f); the
+    // sons of one parent own disjoint rows and columns, so the level is one batch each
+    std::vector<GemmP<double>> GP, GQ;
+    std::vector<MoveP> backP, backQ;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      const int b = boxes[i], k = kskel[b], f = parent[b];
+      double* B;
+      int ld, o;
+      parent_block(b, B, ld, o);
+      const int nf = ld;
+      double* tr0 = Tr.p + orr[i];
+      double* tc0 = Tc.p + ocol[i];
+      if (parent[f] >= 0) {
+        const int kf = kskel[f];
+        GP.push_back(GemmP<double>{Pm.p + oq[i], Lw.p + oL[f] + o, tr0, k, kf, k, k, nf, k});
+        backP.push_back(MoveP{tr0, Lw.p + oL[f] + o, nullptr, k, kf, k, nf, 0, 0});
+        GQ.push_back(GemmP<double>{Rw.p + oR[f] + (size_t)o * kf, Qm.p + oq[i], tc0, kf, k, k, kf, k, kf});
+        backQ.push_back(MoveP{tc0, Rw.p + oR[f] + (size_t)o * kf, nullptr, kf, k, kf, kf, 0, 0});
+        tr0 += (size_t)k * nf;
+        tc0 += (size_t)nf * k;
+      }
+      GP.push_back(GemmP<double>{Pm.p + oq[i], B + o, tr0, k, nf, k, k, ld, k});
+      backP.push_back(MoveP{tr0, B + o, nullptr, k, nf, k, ld, 0, 0});
+      GQ.push_back(GemmP<double>{B + (size_t)o * ld, Qm.p + oq[i], tc0, nf, k, k, ld, k, nf});
+      backQ.push_back(MoveP{tc0, B + (size_t)o * ld, nullptr, nf, k, nf, ld, 0, 0});
+    }
+    run_gemms(GP, false, false, 1.0, 0.0, st);
+    run_moves(backP, st);
+    run_gemms(GQ, false, false, 1.0, 0.0, st);
+    run_moves(backQ, st);
+  }
+  // (3) sibling blocks from each parent's off-diagonal blocks; self blocks from leaf Dinv
+  std::vector<MoveP> mv;
+  for (int f = 0; f < nboxes; ++f) {
+    if (c1[f] < 0 || c2[f] < 0) continue;
+    const int a = c1[f], b = c2[f], ka = kskel[a], kb = kskel[b];
+    const double* B;
+    int ld;
+    if (parent[f] < 0) { B = FTw.p + oFT[prob[f]]; ld = ktop[prob[f]]; }
+    else { B = Dw.p + oD[f]; ld = nskel[f]; }
+    if (ka > 0 && kb > 0) {
+      mv.push_back(MoveP{B + (size_t)ka * ld, K.M_SIB.p + oSib[a], nullptr, ka, kb, ld, ka, 0, 0});
+      mv.push_back(MoveP{B + ka, K.M_SIB.p + oSib[b], nullptr, kb, ka, ld, kb, 0, 0});
+    }
+  }
+  for (int b = 0; b < nboxes; ++b)
+    if (parent[b] >= 0 && is_leaf(b))
+      mv.push_back(MoveP{Dw.p + oD[b], K.M_SELF.p + oSelf[b], nullptr, nskel[b], nskel[b], nskel[b], cnt[b], 0, 0});
+  run_moves(mv, st);
+  HSS_CUDA(cudaStreamSynchronize(st));
 }
 
 // ---------------------------------------------------------------------------

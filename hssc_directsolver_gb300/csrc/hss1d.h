@@ -30,6 +30,7 @@ struct HSS1D {
   long long Ntot = 0;
   int nprob = 0, nboxes = 0, leaf = 0, maxlev = 0;
   double acc = 0;
+  bool sym = false;  // fsym compression: one ID per box, incoming skeletons = outgoing
   std::vector<long long> pN, pbase;   // points per problem, first global point
   std::vector<int> proot;              // root box of each problem
   std::vector<unsigned long long> pseed;
@@ -72,8 +73,10 @@ struct HSS1D {
   ~HSS1D();
   // problem p: X_p is an N_p x 6 column-major block [x y nx ny w kappa] (ld ldx_p)
   void compress(int nprob, const long long* N, const double* const* Xp, const long long* ldx, int leaf, double acc,
-                const hss_kernel_params& kp, const unsigned long long* seeds, MLP* mlp = nullptr);
+                const hss_kernel_params& kp, const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false);
   void invert();
+  // K = the inverse in compressed format (HSS1D_transforminv_nsym)
+  void transforminv(HSS1D& K);
   void applyinv_device(const double* dX, double* dY, int nrhs);
   void apply_device(const double* dX, double* dY, int nrhs);
   void solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres, int* iters);

@@ -109,6 +109,26 @@ def HSS1D_compress_nsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel
     return HSS1DMatrix(h, Xf.shape[0])
 
 
+def HSS1D_compress_fsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel, seed: int = 0) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compress_fsym('green', X, TREE, acc, knl_params): one ID per box, for
+    kernels the caller treats as symmetric (HSS1D/HSS1D_compress_fsym.m:98-248)."""
+    if type_ != "green":
+        raise ValueError("only the 'green' construction is implemented on the GPU")
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim != 2 or X.shape[1] not in (2, 6):
+        raise ValueError("X must be N x 2 or N x 6 ([x y nx ny w kappa])")
+    if X.shape[1] == 2:
+        X6 = np.zeros((X.shape[0], 6))
+        X6[:, :2] = X
+        X = X6
+    Xf = np.asfortranarray(X)
+    h = C.c_void_p()
+    kp = knl_params.to_c()
+    L.check(L.lib().hss1d_compress_fsym(C.byref(h), L.ptr(Xf), Xf.shape[0], Xf.shape[0], int(TREE), float(acc),
+                                        C.byref(kp), int(seed)))
+    return HSS1DMatrix(h, Xf.shape[0])
+
+
 def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None,
                          predictor=None) -> HSS1DMatrix:
     """Many independent curves compressed together (every level of every tree in the
@@ -158,6 +178,18 @@ def HSS1D_invert_nsym(K_HSS: HSS1DMatrix, acc: float = 0.0):
     return K_HSS, K_HSS
 
 
+def HSS1D_transforminv_nsym(K_HSS: HSS1DMatrix, HSSinv=None, FTinv=None) -> HSS1DMatrix:
+    """Kinv_HSS: the inverse rewritten in K_HSS's compressed format
+    (HSS1D/HSS1D_transforminv_nsym.m:38-161); ``HSS1D_apply_nsym(Kinv_HSS, f)`` applies
+    the inverse.  HSSinv/FTinv are the factors inside K_HSS (from HSS1D_invert_nsym)."""
+    h = C.c_void_p()
+    L.check(L.lib().hss1d_transforminv(K_HSS._h, C.byref(h)))
+    K = HSS1DMatrix(h, K_HSS.N)
+    if hasattr(K_HSS, "sizes"):
+        K.sizes = K_HSS.sizes
+    return K
+
+
 def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
     q = _as_f64(qq)
     vec = q.ndim == 1
@@ -188,3 +220,10 @@ def HSS1D_solve(K_HSS: HSS1DMatrix, ff, tol: float = 1e-10, maxit: int = 5):
     L.check(L.lib().hss1d_solve(K_HSS._h, L.ptr(f2), L.ptr(out), f2.shape[1], tol, maxit, C.byref(rr),
                                 C.byref(it)))
     return (out[:, 0] if vec else out), rr.value, it.value
+
+
+# fsym handles carry T_DN = T_UP; the nsym algorithms are the fsym ones on them
+# (HSS1D_invert_fsym.m:47-90 with E at :79, HSS1D_apply_fsym.m:1-118, HSS1D_applyinv_fsym.m:38-86)
+HSS1D_invert_fsym = HSS1D_invert_nsym
+HSS1D_apply_fsym = HSS1D_apply_nsym
+HSS1D_applyinv_fsym = HSS1D_applyinv_nsym

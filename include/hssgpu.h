@@ -70,6 +70,12 @@ typedef struct hss1d_matrix hss1d_matrix;
  * seed: key of the counter RNG drawing the rank-check vectors (ID.m:68-86). */
 int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
                    double acc, const hss_kernel_params* kp, uint64_t seed);
+/* K_HSS = HSS1D_compress_fsym('green', X, TREE, acc, knl_params), HSS1D/HSS1D_compress_fsym.m:98-248:
+ * one ID per box (incoming skeletons = outgoing, T_DN = T_UP) and M_SIB{c2} = M_SIB{c1}.'.
+ * hss1d_invert / hss1d_apply / hss1d_applyinv then act as HSS1D_invert_fsym (with its E fix at
+ * :79), HSS1D_apply_fsym and HSS1D_applyinv_fsym. */
+int hss1d_compress_fsym(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
+                        double acc, const hss_kernel_params* kp, uint64_t seed);
 /* Batched HSS1D: nprob independent curves of uneven N compressed as one forest, every level of
  * every tree in the same launches.  X[p] is N[p] x 6 column-major (ld ldx[p]); seeds[p] keys
  * the rank-check stream of problem p (NULL: all 0).  No reference counterpart for the batching
@@ -91,6 +97,11 @@ int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_
                      int32_t* J_up, int32_t* J_dn, double* T_up, double* T_dn);
 /* [HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D/HSS1D_invert_nsym.m:44-91 */
 int hss1d_invert(hss1d_matrix* H);
+/* Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv),
+ * HSS1D/HSS1D_transforminv_nsym.m:38-161: a new handle holding the inverse in compressed
+ * format (same tree and skeleton sets, J_UP/J_DN swapped), so hss1d_apply on *out applies
+ * the inverse.  H must be inverted. */
+int hss1d_transforminv(hss1d_matrix* H, hss1d_matrix** out);
 /* uu = HSS1D_apply_nsym(K_HSS, qq), HSS1D/HSS1D_apply_nsym.m:38-100 */
 int hss1d_apply(hss1d_matrix* H, const double* qq, double* uu, int32_t nrhs);
 /* xx = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff), HSS1D/HSS1D_applyinv_nsym.m:43-86 */

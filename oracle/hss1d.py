@@ -259,6 +259,42 @@ def compress_nsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: 
     return H
 
 
+def compress_fsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: int = 0,
+                  tree: HSS1DTree | None = None) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compress_fsym('green', X, TREE, acc, knl_params),
+    HSS1D/HSS1D_compress_fsym.m:98-248: one ID per box on A_out = K([X_inside; X_proxy],
+    X_skel) (:114-164, :186-198; problem 2*b of the shared RNG), incoming skeletons equal
+    to the outgoing ones, and M_SIB{c2} = M_SIB{c1}.' (:245).  The nsym invert and apply
+    functions run on the result unchanged (their L is the transpose of R here)."""
+    X = np.asarray(X, dtype=np.float64)
+    ntot = X.shape[0]
+    t = tree if tree is not None else get_tree(ntot, leaf)
+    nb = t.nboxes
+    H = HSS1DMatrix(t)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census"):
+        setattr(H, name, [None] * nb)
+    nei = neighbor_list(X, t)
+    for ibox in range(nb - 1, 0, -1):
+        out, _, A_out, _ = compress_green_blocks(H, X, ibox, nei, kp, ntot)
+        T, J, k, _ = idecomp.id_adaptive(A_out, acc, seed, 2 * ibox)
+        H.I_SKUP[ibox] = H.I_SKDN[ibox] = out[J[:k]]
+        H.T_UP[ibox] = H.T_DN[ibox] = T
+        H.J_UP[ibox] = H.J_DN[ibox] = J
+        H.nskel[ibox] = len(out)
+        H.kskel[ibox] = k
+        H.census[ibox] = (A_out.shape[0], A_out.shape[0], len(out), k, k, k)
+    for ibox in range(nb - 1, -1, -1):
+        if t.is_leaf(ibox):
+            ind = _leaf_range(t, ibox)
+            H.M_SELF[ibox] = kernel_eval(X[ind], X[ind], kp)
+        elif t.c1[ibox] >= 0 and t.c2[ibox] >= 0:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            H.M_SIB[s1] = kernel_eval(X[H.I_SKUP[s1]], X[H.I_SKUP[s2]], kp)
+            H.M_SIB[s2] = H.M_SIB[s1].T.copy()
+    return H
+
+
 def _RL(H, b):
     """R (k x n) and L (n x k) of HSS1D_invert_nsym.m:63-72."""
     n, k = H.nskel[b], H.kskel[b]

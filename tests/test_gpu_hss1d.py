@@ -132,3 +132,68 @@ def test_refined_solve_reaches_tolerance(gpu):
     assert rr <= 1e-13 and 1 <= it <= 4
     r = F - G1.HSS1D_apply_nsym(H, x)
     assert np.linalg.norm(r, axis=0).max() / np.linalg.norm(F, axis=0).min() < 1e-12
+
+
+def test_transforminv_matches_oracle(star):
+    """Kinv_HSS = HSS1D_transforminv_nsym: its forward apply equals the oracle's transformed
+    inverse and the inverse apply; its J/T rows match the oracle's."""
+    G1, g, X, H, Ho = star
+    G1.HSS1D_invert_nsym(H)
+    Ki = G1.HSS1D_transforminv_nsym(H, None, None)
+    inv = O1.invert_nsym(Ho)
+    Ko = O1.transforminv_nsym(Ho, inv)
+    F = np.random.default_rng(9).standard_normal((X.shape[0], 3))
+    y = G1.HSS1D_apply_nsym(Ki, F)
+    yo = O1.apply_nsym(Ko, F)
+    assert np.linalg.norm(y - yo) <= 1e-10 * np.linalg.norm(yo)
+    x = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    assert np.linalg.norm(y - x) <= 1e-10 * np.linalg.norm(x)
+    for b in (1, 2, H.info()["nboxes"] - 1):
+        e = Ki.export_box(b)
+        k = Ho.kskel[b]
+        assert np.array_equal(e["J_UP"][:k], Ho.J_DN[b][:k]) and np.array_equal(e["J_DN"][:k], Ho.J_UP[b][:k])
+        if e["T_UP"].size:
+            pos = {c: i for i, c in enumerate(e["J_UP"][k:])}
+            Tg = np.stack([e["T_UP"][:, pos[c]] for c in Ko.J_UP[b][k:]], axis=1)
+            # P and Q inverses amplify rounding (cond ~1e6 here): entries agree to ~1e-6
+            assert np.abs(Tg - Ko.T_UP[b]).max() <= 1e-5 * max(1.0, np.abs(Ko.T_UP[b]).max())
+
+
+def test_transforminv_forest(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(4, nmin=700, nmax=2500, seed=12)
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    G1.HSS1D_invert_nsym(H)
+    Ki = G1.HSS1D_transforminv_nsym(H)
+    F = np.random.default_rng(2).standard_normal((sum(sizes), 2))
+    x = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    assert np.linalg.norm(G1.HSS1D_apply_nsym(Ki, F) - x) <= 1e-10 * np.linalg.norm(x)
+
+
+def test_fsym_matches_oracle(gpu):
+    """HSS1D_compress_fsym on the symmetric reference geometry: ranks and skeletons equal
+    the oracle's, inverse apply within 1e-12 of it and 1e-8 of the dense solve."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    Ng, npan = 7, 16
+    h = 2.0 / (Ng * npan)
+    b, c = OK.reference_modulations(sym=1, proxy=0, transinv=0)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=h, b=b, c=c)
+    prm = O2.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    X = prm.X_source()[O2.build_tree_nsym(prm, with_T=False).I_sk[1]]
+    gk = GK.Kernel("SL_L_2D", h, GK.Modulation(b.alpha, b.x0, b.y0, b.isig), GK.Modulation(c.alpha, c.x0, c.y0, c.isig))
+    H = G1.HSS1D_compress_fsym("green", X, 56, 1e-10, gk)
+    Ho = O1.compress_fsym(X, 56, 1e-10, kp)
+    inf = H.info()
+    assert np.array_equal(inf["kskel"][1:], np.array(Ho.kskel[1:]))
+    for bx in range(1, inf["nboxes"]):
+        e = H.export_box(bx)
+        assert np.array_equal(e["I_SKUP"], Ho.I_SKUP[bx]) and np.array_equal(e["I_SKDN"], Ho.I_SKUP[bx])
+    G1.HSS1D_invert_fsym(H)
+    q = np.random.default_rng(0).standard_normal((X.shape[0], 5))
+    y = G1.HSS1D_applyinv_fsym(H, None, None, q)
+    yo = O1.applyinv_nsym(Ho, O1.invert_nsym(Ho), q)
+    assert np.linalg.norm(y - yo) <= 1e-12 * np.linalg.norm(yo)
+    A = OK.kernel_eval(X, X, kp)
+    assert np.linalg.norm(y - np.linalg.solve(A, q)) < 1e-8 * np.linalg.norm(yo)
+    u = G1.HSS1D_apply_fsym(H, q)
+    assert np.linalg.norm(u - O1.apply_nsym(Ho, q)) <= 1e-12 * np.linalg.norm(u)

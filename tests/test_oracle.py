@@ -152,3 +152,35 @@ def test_iterative_refinement_reference_semantics():
     A = np.eye(5) * 2.0
     x, hist = hss2d.iterative_refinement(lambda v: A @ v, lambda v: v * 0.45, np.ones(5), 1e-12, 50)
     assert hist[-1] <= 1e-12 and len(hist) < 50
+
+
+def _reference_hss1d_case_sym():
+    """Run_HSS1D_tests.m geometry with the symmetric modulation pair (sym=1): b = c."""
+    Ng, npan = 7, 16
+    h = 2.0 / (Ng * npan)
+    b, c = kernels.reference_modulations(sym=1, proxy=0, transinv=0)
+    kp = kernels.KernelParams(flag=kernels.SL_L_2D, h=h, b=b, c=c)
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    X = prm.X_source()[hss2d.build_tree_nsym(prm, with_T=False).I_sk[1]]
+    return X, kp
+
+
+def test_fsym_compress_symmetric_kernel():
+    """HSS1D_compress_fsym on a symmetric kernel: one ID per box, T_DN = T_UP,
+    M_SIB{c2} = M_SIB{c1}.', and the INSTALL.txt error criterion for apply and solve."""
+    X, kp = _reference_hss1d_case_sym()
+    A = kernels.kernel_eval(X, X, kp)
+    assert np.abs(A - A.T).max() <= 1e-15 * np.abs(A).max()
+    H = hss1d.compress_fsym(X, 56, 1e-10, kp)
+    for b in range(1, H.tree.nboxes):
+        assert H.T_DN[b] is H.T_UP[b] and np.array_equal(H.I_SKDN[b], H.I_SKUP[b])
+    t = H.tree
+    s1, s2 = t.c1[0], t.c2[0]
+    assert np.array_equal(H.M_SIB[s2], H.M_SIB[s1].T)
+    q = np.random.default_rng(1).standard_normal((X.shape[0], 4))
+    assert np.linalg.norm(hss1d.apply_nsym(H, q) - A @ q) < 1e-8 * np.linalg.norm(A @ q)
+    y = hss1d.applyinv_nsym(H, hss1d.invert_nsym(H), q)
+    yd = np.linalg.solve(A, q)
+    assert np.linalg.norm(y - yd) < 1e-8 * np.linalg.norm(yd)
+    Hn = hss1d.compress_nsym(X, 56, 1e-10, kp)
+    assert sum(H.kskel[1:]) <= sum(Hn.kskel[1:])
