@@ -31,6 +31,7 @@ HSS_DL_L_2D = 1
 HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_INTER_DENSE = 0
+HSS_INTER_LOWRANK = 1
 
 
 class hss_kernel_params(C.Structure):
@@ -42,7 +43,8 @@ class hss_kernel_params(C.Structure):
 class hss2d_params(C.Structure):
     _fields_ = [("Ng", C.c_int32), ("npan", C.c_int32), ("layers", C.c_int32), ("interform", C.c_int32),
                 ("transinv", C.c_int32), ("sym", C.c_int32), ("precision", C.c_int32), ("pad_", C.c_int32),
-                ("acc", C.c_double), ("kp", hss_kernel_params)]
+                ("acc", C.c_double), ("kp", hss_kernel_params), ("k_cut", C.c_int32), ("pad2_", C.c_int32),
+                ("seed", C.c_uint64)]
 
 
 class HSSError(RuntimeError):
@@ -104,6 +106,7 @@ SIGNATURES = {
     "hss2d_box_sizes": (C.c_int, [_P, _I32P, _I32P, _I32P]),
     "hss2d_export_box": (C.c_int, [_P, C.c_int32, _I32P, _I32P, _DP, _DP]),
     "hss2d_export_inverse": (C.c_int, [_P, C.c_int32, _DP, _DP]),
+    "hss2d_interp_ranks": (C.c_int, [_P, _I32P, _I32P]),
     "hss2d_solve_bytes": (C.c_int, [_P, _I64P]),
     "hss2d_solve_launches": (C.c_int, [_P, C.c_int32, _I32P]),
     "hss2d_destroy": (C.c_int, [_P]),

@@ -434,7 +434,9 @@ int hss1d_destroy(hss1d_matrix* H) {
 int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p) {
   HSS_TRY
   HSS_REQUIRE(out != nullptr && p != nullptr, HSS_ERR_ARG, "NULL argument");
-  HSS_REQUIRE(p->interform == HSS_INTER_DENSE, HSS_ERR_ARG, "only INTERform 'dense' is supported");
+  HSS_REQUIRE(p->interform == HSS_INTER_DENSE || p->interform == HSS_INTER_LOWRANK, HSS_ERR_ARG,
+              "INTERform must be 'dense' or 'lowrank'");
+  HSS_REQUIRE(p->k_cut >= 0, HSS_ERR_ARG, "k_cut must be >= 0");
   HSS_REQUIRE(p->transinv == 0 || p->transinv == 1, HSS_ERR_ARG, "transinv must be 0 or 1");
   HSS_REQUIRE(p->transinv == 0 || (p->kp.b_alpha == 0.0 && p->kp.c_alpha == 0.0), HSS_ERR_ARG,
               "translation-invariant mode needs an unmodulated kernel (b = c = 1)");
@@ -599,6 +601,23 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
   };
   fetch(0, (size_t)g.n * g.n, FI);
   if (lev > 0) fetch(1, (size_t)g.k * g.k, E);
+  HSS_CATCH
+}
+
+int hss2d_interp_ranks(const hss2d_matrix* H, int32_t* q_up, int32_t* q_dn) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS2D* h = H->impl;
+  HSS_REQUIRE(h->tree_built, HSS_ERR_STATE, "tree not built");
+  for (int lev = 0; lev <= h->geo.depth; ++lev) {
+    const int nb = h->geo.levels[lev].nb, b0 = (1 << lev) - 1;
+    const bool lr = lev < (int)h->qrank_up.size() && !h->qrank_up[lev].empty();
+    for (int i = 0; i < nb; ++i) {
+      const size_t f = h->fo(i);
+      if (q_up) q_up[b0 + i] = lr ? h->qrank_up[lev][f] : -1;
+      if (q_dn) q_dn[b0 + i] = lr ? h->qrank_dn[lev][f] : -1;
+    }
+  }
   HSS_CATCH
 }
 

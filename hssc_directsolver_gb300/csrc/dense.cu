@@ -1191,6 +1191,13 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     }
     __syncthreads();
   }
+  if (p.steps_hint == ID_QR_ONLY) {  // pivoted QR for a fixed-rank ID of the caller
+    if (tid == 0) {
+      *p.rank = l;
+      if (p.stat) { p.stat[0] = 0; p.stat[1] = l; }
+    }
+    return;
+  }
   // rank detection (Common/ID.m:51-52) over the computed diagonal
   double Rmx = (l > 0) ? fabs(W[0]) * acc : 0.0;
   auto count_rank = [&](double thr) {
@@ -1369,6 +1376,127 @@ __global__ void __launch_bounds__(256) k_id_fixed(const IdP* __restrict__ P) {
     }
   }
   if (tid == 0) *p.rank = k;
+}
+
+// Pivoted Householder QR with the explicit thin Q (QR_findrank's [Q,R,~] = qr(Y,0),
+// Common/QR_findrank.m:50-70): the pivot rule, reflectors and norms of k_id_adaptive,
+// then Q = H_0 ... H_{l-1} [I; 0] accumulated backwards (LAPACK dorg2r order).
+__global__ void __launch_bounds__(256) k_pqr_q(const PqrP* __restrict__ P) {
+  const PqrP p = P[blockIdx.x];
+  const int m = p.m, n = p.l, ld = p.ldw, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int l = min(m, n);
+  double* W = p.W;
+  extern __shared__ double s_dyn[];
+  double* norms = s_dyn;  // n
+  __shared__ double sh[8];
+  __shared__ double shv[8];
+  __shared__ int shi[8];
+  for (int c = w; c < n; c += 8) {
+    double d = 0.0;
+    for (int i = lane; i < m; i += 32) { const double v = W[i + (size_t)c * ld]; d += v * v; }
+    d = warp_sum(d);
+    if (lane == 0) norms[c] = d;
+  }
+  __syncthreads();
+  for (int j = 0; j < l; ++j) {
+    double best = -1.0;
+    int bi = INT_MAX;
+    for (int c = j + tid; c < n; c += 256) {
+      const double v = norms[c];
+      if (v > best) { best = v; bi = c; }
+    }
+    block_argmax256(best, bi, shv, shi);
+    if (bi == INT_MAX) bi = j;
+    if (bi != j) {
+      for (int i = tid; i < m; i += 256) {
+        const double t = W[i + (size_t)j * ld];
+        W[i + (size_t)j * ld] = W[i + (size_t)bi * ld];
+        W[i + (size_t)bi * ld] = t;
+      }
+      if (tid == 0) { const double u = norms[j]; norms[j] = norms[bi]; norms[bi] = u; }
+    }
+    __syncthreads();
+    double part = 0.0;
+    for (int i = j + 1 + tid; i < m; i += 256) { const double v = W[i + (size_t)j * ld]; part += v * v; }
+    const double xn2 = block_sum256(part, sh);
+    const double alpha = W[j + (size_t)j * ld];
+    double tau = 0.0, beta = alpha, scal = 0.0;
+    if (xn2 != 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      tau = (beta - alpha) / beta;
+      scal = 1.0 / (alpha - beta);
+    }
+    for (int i = j + 1 + tid; i < m; i += 256) W[i + (size_t)j * ld] *= scal;
+    __syncthreads();
+    if (tid == 0) {
+      W[j + (size_t)j * ld] = beta;
+      p.tau[j] = tau;
+      p.D[j] = fabs(beta);
+    }
+    for (int c = j + 1 + w; c < n; c += 8) {
+      double d = W[j + (size_t)c * ld] * (lane == 0 ? 1.0 : 0.0);
+      for (int i = j + 1 + lane; i < m; i += 32) d += W[i + (size_t)j * ld] * W[i + (size_t)c * ld];
+      d = warp_sum(d) * tau;
+      if (lane == 0) W[j + (size_t)c * ld] -= d;
+      double nn = 0.0;
+      for (int i = j + 1 + lane; i < m; i += 32) {
+        const double v = W[i + (size_t)c * ld] - d * W[i + (size_t)j * ld];
+        W[i + (size_t)c * ld] = v;
+        nn += v * v;
+      }
+      nn = warp_sum(nn);
+      if (lane == 0) norms[c] = nn;
+    }
+    __syncthreads();
+  }
+  // Q = [I; 0], then H_j from j = l-1 down to 0 on columns c >= j (the others are e_c)
+  for (long long e = tid; e < (long long)m * l; e += 256) {
+    const int i = (int)(e % m), c = (int)(e / m);
+    p.Q[i + (size_t)c * p.ldq] = (i == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int j = l - 1; j >= 0; --j) {
+    const double tau = p.tau[j];
+    if (tau != 0.0) {
+      for (int c = j + w; c < l; c += 8) {
+        double* q = p.Q + (size_t)c * p.ldq;
+        double d = (lane == 0) ? q[j] : 0.0;
+        for (int i = j + 1 + lane; i < m; i += 32) d += W[i + (size_t)j * ld] * q[i];
+        d = warp_sum(d) * tau;
+        if (lane == 0) q[j] -= d;
+        for (int i = j + 1 + lane; i < m; i += 32) q[i] -= d * W[i + (size_t)j * ld];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+void pqr_q_batched(const PqrP* dP, int batch, cudaStream_t s) {
+  if (batch <= 0) return;
+  // dynamic shared memory: column norms (l doubles); the host guarantees l <= 4096
+  k_pqr_q<<<batch, 256, 4096 * sizeof(double), s>>>(dP);
+  check_launch("k_pqr_q");
+}
+
+__global__ void k_gauss(const GaussP* __restrict__ P, long long maxEntries) {
+  const GaussP g = P[blockIdx.y];
+  const long long cnt = (long long)g.m * g.l;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt && e < maxEntries;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.m), j = (int)(e / g.m);
+    const unsigned long long c0 = 12ULL * (unsigned long long)e;
+    double v = rng_uniform(g.seed, g.stream, c0);
+    for (int t = 1; t < 12; ++t) v = __dadd_rn(v, rng_uniform(g.seed, g.stream, c0 + t));
+    g.G[i + (size_t)j * g.ldg] = __dadd_rn(v, -6.0);
+  }
+}
+
+void gauss_batched(const GaussP* dP, int batch, long long maxEntries, cudaStream_t s) {
+  if (batch <= 0 || maxEntries <= 0) return;
+  HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "gauss batch too large");
+  const int gx = std::min(ceil_div(maxEntries, 256), 1024);
+  k_gauss<<<dim3(gx, batch), 256, 0, s>>>(dP, maxEntries);
+  check_launch("k_gauss");
 }
 
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {

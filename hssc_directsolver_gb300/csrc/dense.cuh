@@ -88,12 +88,37 @@ struct IdP {
   double* x;        // 2*n workspace (random vectors)
   double* y;        // m+n workspace
   int problem;      // id for the random stream (2*box + side, box local to its tree)
-  int steps_hint;   // > 0: stop the pivoted QR after this many steps if the rank is resolved
+  int steps_hint;   // > 0: stop the pivoted QR after this many steps if the rank is resolved;
+                    // ID_QR_ONLY: the full pivoted QR only (rank = min(m, n), T untouched)
   unsigned long long seed;  // key of the random stream (one per independent problem)
   int* stat;        // out (may be null): [0] 0 full / 1 truncated / 2 needs a full rerun, [1] QR steps done
 };
 
+constexpr int ID_QR_ONLY = -2;
+
 void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s);
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s);
+
+// Householder QR with column pivoting of W (m x l, ld ldw; overwritten) and the
+// explicit thin Q (m x min(m,l), ld ldq); D = |diag R|.  Same pivots and
+// reflectors as the ID's pivoted QR.  One block per problem; l <= 4096.
+struct PqrP {
+  double* W;
+  int m, l, ldw;
+  double* tau;  // min(m,l) workspace
+  double* Q;
+  int ldq;
+  double* D;    // min(m,l)
+};
+void pqr_q_batched(const PqrP* dP, int batch, cudaStream_t s);
+
+// Gaussian test matrix G (m x l, ld ldg): entry (i, j) is the Irwin-Hall sum of the
+// 12 uniforms u(seed, stream, 12*(i + m*j) + t), t = 0..11, added in order, minus 6.
+struct GaussP {
+  double* G;
+  int m, l, ldg;
+  unsigned long long seed, stream;
+};
+void gauss_batched(const GaussP* dP, int batch, long long maxEntries, cudaStream_t s);
 
 }  // namespace hss

@@ -252,6 +252,9 @@ void HSS2D::build_tree() {
     d.proxy.upload(g.proxy, stream);
   }
   HSS_CUDA(cudaStreamSynchronize(stream));
+  qlev.assign(geo.depth + 1, 0);
+  qrank_up.assign(geo.depth + 1, {});
+  qrank_dn.assign(geo.depth + 1, {});
   for (int lev = geo.depth; lev >= 1; --lev) compute_T(lev);
   tree_built = true;
 }
@@ -279,15 +282,22 @@ void HSS2D::compute_T(int lev) {
   HSS_CUDA(cudaMemcpyAsync(dkg.p, kg.data(), batch * sizeof(KgenP<double>), cudaMemcpyHostToDevice, stream));
   kgen_batched<double>(dkg.p, batch, (long long)p * n, view(pts), kdev, stream);
   DevBuf<double> V((size_t)batch * p * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * k);
-  std::vector<QrP<double>> qp(batch);
-  for (int b = 0; b < batch; ++b) {
-    double* X = ((b & 1) ? d.Tdn.p : d.Tup.p) + (size_t)(b / 2) * k * nr;
-    qp[b] = QrP<double>{A.p + (size_t)b * p * n, p, n, k, p, V.p + (size_t)b * p * QR_NB,
-                        Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k, X, k};
+  if (uses_lowrank(lev)) {
+    diag.zero(stream);
+    lowrank_T(lev, A.p, V, Tf, diag);
+  } else {
+    std::vector<QrP<double>> qp(batch);
+    for (int b = 0; b < batch; ++b) {
+      double* X = ((b & 1) ? d.Tdn.p : d.Tup.p) + (size_t)(b / 2) * k * nr;
+      qp[b] = QrP<double>{A.p + (size_t)b * p * n, p, n, k, p, V.p + (size_t)b * p * QR_NB,
+                          Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k, X, k};
+    }
+    DevBuf<QrP<double>> dqp(batch);
+    HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
+    lstsq_batched<double>(dqp.p, batch, p, n, k, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    qlev[lev] = nr;  // a dense T.U is k x nr
   }
-  DevBuf<QrP<double>> dqp(batch);
-  HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
-  lstsq_batched<double>(dqp.p, batch, p, n, k, stream);
   // T_up came from the even problems, T_dn from the odd ones
   k_transpose<<<grid_for((long long)nb * k * nr), 256, 0, stream>>>(nb, k, nr, d.Tdn.p, (long long)k * nr, k,
                                                                      d.TdnT.p, (long long)k * nr, nr);

@@ -98,8 +98,17 @@ struct HSS2D {
   explicit HSS2D(const hss2d_params& p);
   ~HSS2D();
 
+  // low-rank interpolation ('lowrank' INTERform): widest T.U per level (q(lev+1) of the
+  // reference), the randomized ranks of T_up / T_dn per factor box of a level (empty on
+  // dense levels)
+  std::vector<int> qlev;
+  std::vector<std::vector<int>> qrank_up, qrank_dn;
+
   void build_tree();
   void compute_T(int lev);
+  bool uses_lowrank(int lev) const;
+  void sample_guess(int lev, int m, int n, bool up, int& k0, int& C) const;
+  void lowrank_T(int lev, const double* A, DevBuf<double>& Vw, DevBuf<double>& Tf, DevBuf<double>& diag);
   void compress();
   void invert();
   void applyinv_device(const double* dX, double* dY, int nrhs, cudaStream_t user);

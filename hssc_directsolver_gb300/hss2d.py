@@ -40,6 +40,8 @@ class HSS2DParams:
     precision: str = "fp64"   # "fp64" or "mixed"
     n_cut: int = 400
     Fopts: str = "dense"
+    k_cut: int = 2500         # low-rank T only where k < k_cut
+    seed: int = 0             # key of the randomized ID's Gaussian samples
 
     @property
     def h(self) -> float:
@@ -54,15 +56,16 @@ class HSS2DParams:
         return self.npan * self.npan * self.Ng * self.Ng
 
     def to_c(self) -> L.hss2d_params:
-        if self.INTERform != "dense":
-            raise ValueError("INTERform 'dense' is the implemented interpolation storage")
+        forms = {"dense": L.HSS_INTER_DENSE, "lowrank": L.HSS_INTER_LOWRANK}
+        if self.INTERform not in forms:
+            raise ValueError("INTERform must be 'dense' or 'lowrank'")
         if self.Fopts != "dense":
             raise ValueError("Fopts 'dense' (HSS-D) is the implemented inverse storage")
         prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED}[self.precision]
         k = self.kernel
         k.h = self.h
-        return L.hss2d_params(self.Ng, self.npan, self.layers, L.HSS_INTER_DENSE, self.transinv, self.sym, prec, 0,
-                              float(self.acc), k.to_c())
+        return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,
+                              0, float(self.acc), k.to_c(), int(self.k_cut), 0, int(self.seed))
 
 
 def HSS_tree_parameters(pot: str, kh: float, sym: int, Ng: int, npan: int, acc: float, lay: int, n_cut: int,
@@ -72,8 +75,9 @@ def HSS_tree_parameters(pot: str, kh: float, sym: int, Ng: int, npan: int, acc: 
         raise ValueError("the oscillatory kernels are not part of the GPU path")
     # transinv = 1 keeps one factor set per tree level (INFO_TREE.LEV); the kernel has b = c = 1
     b, c = reference_modulations(sym, proxy, TI)
+    # INTERform 'lowrank' and k_cut 2500 are the reference's defaults (HSS_tree_parameters.m:131-134)
     return HSS2DParams(Ng=Ng, npan=npan, acc=acc, layers=lay, kernel=Kernel(pot, 2.0 / (Ng * npan), b, c),
-                       transinv=TI, sym=sym, n_cut=n_cut)
+                       transinv=TI, sym=sym, n_cut=n_cut, INTERform="lowrank", k_cut=2500)
 
 
 class InfoTree:
@@ -106,6 +110,13 @@ class InfoTree:
         ip = lambda a: a.ctypes.data_as(L._I32P)
         L.check(L.lib().hss2d_box_sizes(self._h, ip(n), ip(k), ip(p)))
         return n, k, p
+
+    def interp_ranks(self):
+        """(q_up, q_dn): rank of each box's low-rank T_up / T_dn, -1 where T is dense."""
+        qu = np.zeros(self.nboxes, np.int32)
+        qd = np.zeros(self.nboxes, np.int32)
+        L.check(L.lib().hss2d_interp_ranks(self._h, qu.ctypes.data_as(L._I32P), qd.ctypes.data_as(L._I32P)))
+        return qu, qd
 
     def export_box(self, box: int):
         n, k, _ = self.box_sizes()

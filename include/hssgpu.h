@@ -44,6 +44,7 @@ extern "C" {
 
 /* HSS2D interpolation-operator storage (params.INTERform) */
 #define HSS_INTER_DENSE 0
+#define HSS_INTER_LOWRANK 1
 
 /* b(x) = 1 + b_alpha*exp(-b_isig*|x-(b_x0,b_y0)|^2), c(y) likewise; alpha = 0
  * switches a modulation off (LOCAL_get_bc, Kernel_Eval.m:98-159). */
@@ -164,13 +165,16 @@ typedef struct hss2d_params {
   int32_t Ng;        /* points per panel side */
   int32_t npan;      /* panels per domain side (power of two) */
   int32_t layers;    /* boundary layers of the preset skeletons */
-  int32_t interform; /* HSS_INTER_DENSE */
+  int32_t interform; /* HSS_INTER_DENSE or HSS_INTER_LOWRANK (the reference default) */
   int32_t transinv;  /* 0: NTI (per-box operators) */
   int32_t sym;       /* 0: nsym */
   int32_t precision; /* HSS_PREC_FP64 or HSS_PREC_MIXED */
   int32_t pad_;
   double acc;
   hss_kernel_params kp;
+  int32_t k_cut;     /* low-rank T only where k < k_cut (0: 2500) */
+  int32_t pad2_;
+  uint64_t seed;     /* key of the randomized ID's Gaussian samples */
 } hss2d_params;
 
 /* INFO_TREE = HSS2D_build_tree_nsym(params), HSS2D/HSS2D_build_tree_nsym.m:80-610
@@ -207,6 +211,9 @@ int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t
                      double* T_up, double* T_dn);
 /* A_HSS(b).FI (n x n) and .E (k x k), FP64 copies; NULL ok */
 int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double* E);
+/* ranks of the low-rank interpolation operators T_up = T.U T.V^T and T_dn per box
+ * (nboxes entries each; -1 where T is dense: the root, the two finest levels, k >= k_cut) */
+int hss2d_interp_ranks(const hss2d_matrix* H, int32_t* q_up, int32_t* q_dn);
 /* bytes of factor storage read by one inverse apply (roofline accounting) */
 int hss2d_solve_bytes(const hss2d_matrix* H, int64_t* bytes);
 /* launches issued by one applyinv of nrhs columns (counted by the host) */

@@ -45,6 +45,8 @@ class HSS2DParams:
     INTERform: str = "dense"
     transinv: int = 0
     sym: int = 0
+    k_cut: int = 2500
+    seed: int = 0
 
     @property
     def h(self):
@@ -232,9 +234,12 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
     T_up = [None] * nb
     T_dn = [None] * nb
     proxy = [None] * nb
+    lowrank = {}
+    q = [0] * (depth + 1)          # q(lev+1) of the reference: widest T.U of each level
     for lev in range(depth, -1, -1):
         colrad, rowrad = box_radii(lev)
         lp = lay_prox(prm, lev)
+        qlev = 0
         for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
             if 2 * b + 1 < nb:
                 I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
@@ -246,8 +251,69 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
             proxy[b] = Xp
             if with_T and lev > 0:
-                T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_src[Jb[:kb]], X_src[Jb[kb:]])
-    return HSS2DTree(depth, cent, I_src, I_sk, Js, ks, T_up, T_dn, proxy, lop)
+                X_sk, X_rs = X_src[Jb[:kb]], X_src[Jb[kb:]]
+                if uses_lowrank(prm, lev, depth, kb, X_rs.shape[0]):
+                    lr = interpolation_lowrank(prm, Xp, X_sk, X_rs, q, lev, b)
+                    lowrank[b] = lr
+                    T_up[b] = lr["Uu"] @ lr["Vu"].T
+                    T_dn[b] = lr["Ud"] @ lr["Vd"].T
+                    qlev = max(qlev, lr["Uu"].shape[1], lr["Ud"].shape[1])
+                else:
+                    T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_sk, X_rs)
+                    qlev = max(qlev, T_up[b].shape[1])
+        if lev > 0:
+            q[lev] = qlev
+    tree = HSS2DTree(depth, cent, I_src, I_sk, Js, ks, T_up, T_dn, proxy, lop)
+    tree.lowrank = lowrank
+    tree.q = q
+    return tree
+
+
+def uses_lowrank(prm: HSS2DParams, lev: int, depth: int, k: int, nr: int) -> bool:
+    """LOCAL_Interpolation_Operators (HSS2D_build_tree_nsym.m:842-846): the low-rank T of
+    INTERform 'lowrank' on levels above the leaves' parents with k < k_cut (the k >= k_cut
+    branch, interpolation_operator_HSS, is the compressed-block path and is not built)."""
+    return prm.INTERform == "lowrank" and lev < depth - 1 and k < prm.k_cut and k > 0 and nr > 0
+
+
+def sample_guess(q, lev, m, n, up: bool):
+    """First sample count k0 and block size C of the randomized ID
+    (interpolation_operator.m:98-116 for box_2_proxy, :143-152 for proxy_2_box).
+
+    The boxes of a level are processed together, so the same-level guess
+    ``q(lev+1) + 1`` of the reference's box-by-box loop (:99-101) is never available:
+    every box takes the finer-level guess.  ``q[l]`` = widest T.U on level l (0 if none).
+    """
+    mn = min(m, n)
+    if sum(1 for v in q if v > 0) < 5:
+        return min(math.ceil(9 * math.log2(mn) - 20), mn), 5
+    a, b = q[lev + 2], q[lev + 4]
+    if up:
+        return min(max(math.ceil(2 * a - b + 2), a), mn), math.ceil(abs(a - b) / 2) + 1
+    return min(math.ceil(2 * a - b + 2), mn), math.ceil(a - b / 2) + 1
+
+
+def interpolation_lowrank(prm: HSS2DParams, Xp, X_sk, X_rs, q, lev, box):
+    """interpolation_operator.m:79-131 (lr = 1): K21 ~ U V^T by LRID_rand, T.U = K11 \\ U,
+    T.V = V, for box_2_proxy (randomized problem 2*box) and proxy_2_box (2*box+1)."""
+    from . import randid
+    kp = prm.kp
+    out = {}
+    for up, tag in ((True, "u"), (False, "d")):
+        if up:
+            K11 = kernel_eval(Xp, X_sk, kp)
+            A = kernel_eval(Xp, X_rs, kp)          # p x nr; matvec K21*x
+        else:
+            K11 = kernel_eval(X_sk, Xp, kp).T
+            A = kernel_eval(X_rs, Xp, kp).T        # p x nr; matvec K21.'*x
+        m, n = A.shape
+        k0, C = sample_guess(q, lev, m, n, up)
+        U, V = randid.lrid_rand(A, k0, C, prm.acc, prm.seed, 2 * box + (0 if up else 1))
+        out["U" + tag] = idecomp.lstsq_qr(K11, U)
+        out["V" + tag] = V
+        out["k0" + tag] = k0
+        out["C" + tag] = C
+    return out
 
 
 def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):

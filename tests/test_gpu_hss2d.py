@@ -148,3 +148,51 @@ def test_translation_invariant_mode(gpu, npan):
         G2.HSS2D_build_tree_nsym(G2.HSS2DParams(Ng=Ng, npan=npan, transinv=1,
                                                 kernel=GK.Kernel("SL_L_2D", h, GK.Modulation(),
                                                                  GK.Modulation(0.5, 0, 0, 20.0))))
+
+
+# ---- INTERform 'lowrank' (the reference default): randomized ID of K21, T = T.U T.V^T ----
+
+@pytest.fixture(scope="module")
+def lowrank8(gpu):
+    from hssc_directsolver_gb300 import hss2d as G2
+    prm = params(8)
+    prm.INTERform = "lowrank"
+    t = G2.HSS2D_build_tree_nsym(prm)
+    G2.HSS2D_compress_nsym(t)
+    G2.HSS2D_invert_nsym(t)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / 64, c=OK.Modulation(0.5, 0, 0, 20.0))
+    oprm = O2.HSS2DParams(Ng=8, npan=8, kp=kp, INTERform="lowrank")
+    ot = O2.build_tree_nsym(oprm)
+    return G2, t, oprm, ot
+
+
+def test_lowrank_ranks_and_T_match_oracle(lowrank8):
+    """Randomized ranks of every low-rank T equal the oracle's (same Gaussian samples from
+    the counter RNG); T = T.U T.V^T agrees to the least-squares conditioning."""
+    G2, t, oprm, ot = lowrank8
+    qu, qd = t.interp_ranks()
+    assert len(ot.lowrank) > 0
+    for b in range(t.nboxes):
+        if b in ot.lowrank:
+            lr = ot.lowrank[b]
+            assert qu[b] == lr["Uu"].shape[1] and qd[b] == lr["Ud"].shape[1]
+        else:
+            assert qu[b] == -1 and qd[b] == -1
+    for b in ot.lowrank:
+        e = t.export_box(b)
+        s = max(1.0, np.abs(ot.T_up[b]).max())
+        assert np.abs(e["T_up"] - ot.T_up[b]).max() <= 1e-6 * s
+        assert np.abs(e["T_dn"] - ot.T_dn[b]).max() <= 1e-6 * s
+
+
+def test_lowrank_solve_accuracy(lowrank8):
+    """The low-rank compressed inverse solves to the dense path's accuracy: relative
+    residual against the kernel matrix ~acc before refinement, <= 1e-10 after."""
+    G2, t, oprm, ot = lowrank8
+    f = np.random.default_rng(0).standard_normal((oprm.N, 2))
+    x = G2.HSS2D_applyinv_nsym(t, t, f)
+    r = O2.kernel_matvec(oprm, x) - f
+    assert np.linalg.norm(r) / np.linalg.norm(f) < 1e-8
+    xs, relres, its = G2.HSS2D_solve(t, f, 1e-10, 5)
+    r = O2.kernel_matvec(oprm, xs) - f
+    assert np.linalg.norm(r) / np.linalg.norm(f) < 5e-10
