@@ -148,6 +148,21 @@ class InfoTree:
         return n.value
 
 
+def levHSS(INFO_TREE: InfoTree, n_cut: int, trinv: int = 0) -> int:
+    """lev_HSS = levHSS(INFO_TREE, n_cut, trinv), HSS2D/levHSS.m:33-65: the first tree
+    level whose smallest skeleton is <= n_cut (forced even), -1 when the top boxes are
+    already below it.  It selects where the compressed-block (HSS-C) inverse would start."""
+    _, k, _ = INFO_TREE.box_sizes()
+    n_min = max(int(k[0]), int(k[1]), int(k[2]))
+    lev = 0
+    while n_min > n_cut and lev < INFO_TREE.depth - 1:
+        lev += 1
+        n_min = int(k[2 ** lev - 1:2 ** (lev + 1) - 1].min())
+    if lev > 0:
+        return lev - 1 if lev % 2 == 1 else lev
+    return -1
+
+
 def HSS2D_build_tree_nsym(params: HSS2DParams) -> InfoTree:
     return InfoTree(params)
 

@@ -536,3 +536,19 @@ def iterative_refinement(apply_A, apply_inv, B, acc, maxit=10):
         it += 1
         hist.append(err)
     return Xs, hist
+
+
+def lev_hss(tree: HSS2DTree, n_cut: int, trinv: int = 0) -> int:
+    """lHSS = levHSS(TREE, n_cut, trinv), HSS2D/levHSS.m:33-65: the first level whose
+    smallest skeleton is <= n_cut (searched from the top; forced even), -1 if the top
+    boxes are already small enough.  With the uniform tree every box of a level has the
+    same k, which is also the translation-invariant LEV(l).k."""
+    k = tree.k
+    n_min = max(k[0], k[1], k[2])
+    lev = 0
+    while n_min > n_cut and lev < tree.depth - 1:
+        lev += 1
+        n_min = min(k[b] for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1))
+    if lev > 0:
+        return lev - 1 if lev % 2 == 1 else lev
+    return -1

@@ -196,3 +196,9 @@ def test_lowrank_solve_accuracy(lowrank8):
     xs, relres, its = G2.HSS2D_solve(t, f, 1e-10, 5)
     r = O2.kernel_matvec(oprm, xs) - f
     assert np.linalg.norm(r) / np.linalg.norm(f) < 5e-10
+
+
+def test_levhss_matches_oracle(case):
+    G2, t, (prm, ot, blk, inv) = case
+    for n_cut in (10, 40, 100, 400, 10 ** 6):
+        assert G2.levHSS(t, n_cut) == O2.lev_hss(ot, n_cut)

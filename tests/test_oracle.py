@@ -184,3 +184,16 @@ def test_fsym_compress_symmetric_kernel():
     assert np.linalg.norm(y - yd) < 1e-8 * np.linalg.norm(yd)
     Hn = hss1d.compress_nsym(X, 56, 1e-10, kp)
     assert sum(H.kskel[1:]) <= sum(Hn.kskel[1:])
+
+
+def test_levhss_rule():
+    """levHSS.m:33-65 on the uniform tree: the first level with min k <= n_cut, forced even."""
+    kp = kernels.KernelParams(flag=kernels.SL_L_2D, h=2.0 / 64)
+    prm = hss2d.HSS2DParams(Ng=8, npan=8, kp=kp)
+    tree = hss2d.build_tree_nsym(prm, with_T=False)
+    ks = [tree.k[2 ** l - 1] for l in range(tree.depth + 1)]
+    assert hss2d.lev_hss(tree, 10 ** 6) == -1
+    for n_cut in (10, 50, 100, 200, 300):
+        lev = next((l for l in range(1, tree.depth) if ks[l] <= n_cut), tree.depth - 1)
+        want = -1 if max(ks[0], ks[1]) <= n_cut else (lev - 1 if lev % 2 else lev)
+        assert hss2d.lev_hss(tree, n_cut) == want
