@@ -243,6 +243,225 @@ __global__ void __launch_bounds__(256) k_skinny_reduce(const GemmP<R>* __restric
   }
 }
 
+// ---- double-float skinny product ----------------------------------------
+// (sh, sl) += (ah + al) * (bh + bl) to ~2^-48 relative: p + e = ah*bh exactly
+// (FMA error term), t = ah*bl + al*bh + e, TwoSum (Knuth) of sh and p, then a
+// Fast2Sum renormalisation keeps |sl| <= ulp(sh)/2.  al*bl (2^-48) is dropped.
+// Intrinsics keep the compiler from contracting or reassociating any step.
+__device__ __forceinline__ void df_madd(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = __fmaf_rn(ah, bh, -p);
+  const float t = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+  const float s = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(s, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  const float lo = __fadd_rn(sl, __fadd_rn(err, t));
+  const float hi = __fadd_rn(s, lo);
+  sl = __fsub_rn(lo, __fsub_rn(hi, s));
+  sh = hi;
+}
+
+// x = hi + lo to 2^-47 relative using integer operations only (GB300 runs
+// double<->float conversions on its narrow FP64 pipe): hi keeps the sign, the
+// exponent and the top 23 stored mantissa bits, lo the remaining 29 bits,
+// renormalised and truncated to 24.  Entries below 2^-102 lose lo (float
+// underflow); outside the float exponent range the FP64 conversion is used.
+__device__ __forceinline__ void split_d2f(double x, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7FF);
+  const int ef = e - 896;
+  if (ef <= 0 || ef >= 255) {
+    hi = __double2float_rn(x);
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((unsigned int)ef << 23) | (unsigned int)((u >> 29) & 0x7FFFFFu));
+  const unsigned int ml = (unsigned int)(u & 0x1FFFFFFFu);
+  const int lz = __clz(ml);
+  const int efl = e - 917 - lz;
+  if (ml == 0u || efl <= 0) {
+    lo = 0.f;
+    return;
+  }
+  const int sh = lz - 8;
+  const unsigned int mm = (sh >= 0) ? (ml << sh) : (ml >> (-sh));
+  lo = __uint_as_float(sign | ((unsigned int)efl << 23) | (mm & 0x7FFFFFu));
+}
+
+// (ah, al) += (bh, bl): TwoSum of the high parts, the low parts and the error
+// added, Fast2Sum renormalisation.  FP32 pipes only.
+__device__ __forceinline__ void df_add(float& ah, float& al, float bh, float bl) {
+  const float s = __fadd_rn(ah, bh);
+  const float bb = __fsub_rn(s, ah);
+  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+  const float lo = __fadd_rn(__fadd_rn(al, bl), err);
+  const float hi = __fadd_rn(s, lo);
+  al = __fsub_rn(lo, __fsub_rn(hi, s));
+  ah = hi;
+}
+
+// (ah, al) *= (bh, bl) to ~2^-47 (exact high product plus cross terms).
+__device__ __forceinline__ void df_mul(float& ah, float& al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = __fmaf_rn(ah, bh, -p);
+  const float t = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+  const float hi = __fadd_rn(p, t);
+  al = __fsub_rn(t, __fsub_rn(hi, p));
+  ah = hi;
+}
+
+// double nearest-below-rounding of hi + lo (|lo| <= ulp(hi)/2), integer operations
+// only: hi's 24-bit significand widened to 53 bits, lo's aligned and added or
+// subtracted, one renormalisation step.  Zero, tiny, huge and non-finite hi take
+// the FP64 conversion path.
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  const unsigned int hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
+  if (eh == 0 || eh == 255 || el == 255) return (double)hi + (double)lo;
+  long long M = (long long)((1ULL << 52) | ((unsigned long long)(hb & 0x7FFFFFu) << 29));
+  int e = eh + 896;  // double biased exponent of hi
+  if (el != 0) {
+    const long long L = (long long)((1u << 23) | (lb & 0x7FFFFFu));
+    const int g = eh - el;  // >= 24 after renormalisation
+    long long Ls = 0;
+    if (g <= 29) Ls = L << (29 - g);
+    else if (g < 29 + 24) Ls = L >> (g - 29);
+    M = ((hb ^ lb) & 0x80000000u) ? M - Ls : M + Ls;
+    if (M >= (1LL << 53)) { M >>= 1; ++e; }
+    else if (M < (1LL << 52)) { M <<= 1; --e; }
+  }
+  const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) | ((unsigned long long)e << 52) |
+                                  ((unsigned long long)M & ((1ULL << 52) - 1));
+  return __longlong_as_double((long long)bits);
+}
+
+// out = alpha * t + beta * C for a double-float t, stored as FP64.
+__device__ __forceinline__ double df_epilogue(float th, float tl, float ah, float al, double beta, double c) {
+  df_mul(th, tl, ah, al);
+  if (beta != 0.0) {
+    float ch, cl, bh, bl;
+    split_d2f(c, ch, cl);
+    split_d2f(beta, bh, bl);
+    df_mul(ch, cl, bh, bl);
+    df_add(th, tl, ch, cl);
+  }
+  return df_to_double(th, tl);
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
+                                                   int ksplit, double* __restrict__ part, int mmax) {
+  constexpr int V = 2;  // one 16-byte load = two (hi, lo) pairs
+  constexpr int ROWS = 32 * V;
+  const GemmP<double> p = P[blockIdx.z];
+  const int row0 = blockIdx.x * ROWS;
+  if (row0 >= p.M) return;
+  const float2* A = reinterpret_cast<const float2*>(p.A);
+  const int N = p.N;
+  const int kper = (((p.K + ksplit - 1) / ksplit) + 7) & ~7;
+  const int kb = blockIdx.y * kper, ke = min(p.K, kb + kper);
+  __shared__ float Bh[SK_KC][NR], Bl[SK_KC][NR];
+  __shared__ float2 red[8][NR][ROWS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int r = row0 + lane * V;
+  const bool vec_ok = ((p.lda % V) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  float sh[V][NR], sl[V][NR];
+#pragma unroll
+  for (int v = 0; v < V; ++v)
+#pragma unroll
+    for (int c = 0; c < NR; ++c) { sh[v][c] = 0.f; sl[v][c] = 0.f; }
+  for (int kc = kb; kc < ke; kc += SK_KC) {
+    const int kn = min(SK_KC, ke - kc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < SK_KC * NR; e += 256) {
+      const int kk = e % SK_KC, c = e / SK_KC;
+      const double x = (kk < kn && c < N) ? p.B[(size_t)(kc + kk) + (size_t)c * p.ldb] : 0.0;
+      float xh, xl;
+      split_d2f(x, xh, xl);
+      Bh[kk][c] = xh;
+      Bl[kk][c] = xl;
+    }
+    __syncthreads();
+    // software-pipelined: the next column's 16 bytes are in flight during this column's math
+    auto load = [&](int kk) -> float4 {
+      const float2* col = A + (size_t)(kc + kk) * p.lda;
+      if (vec_ok && r + V <= p.M) return __ldg(reinterpret_cast<const float4*>(col + r));
+      const float2 q0 = (r < p.M) ? __ldg(col + r) : make_float2(0.f, 0.f);
+      const float2 q1 = (r + 1 < p.M) ? __ldg(col + r + 1) : make_float2(0.f, 0.f);
+      return make_float4(q0.x, q0.y, q1.x, q1.y);
+    };
+    float4 cur = (w < kn) ? load(w) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int kk = w; kk < kn; kk += 8) {
+      const float4 nxt = (kk + 8 < kn) ? load(kk + 8) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float ah[V] = {cur.x, cur.z}, al[V] = {cur.y, cur.w};
+#pragma unroll
+      for (int c = 0; c < NR; ++c) {
+        const float bh = Bh[kk][c], bl = Bl[kk][c];
+#pragma unroll
+        for (int v = 0; v < V; ++v) df_madd(sh[v][c], sl[v][c], ah[v], al[v], bh, bl);
+      }
+      cur = nxt;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v)
+#pragma unroll
+    for (int c = 0; c < NR; ++c) red[w][c][lane * V + v] = make_float2(sh[v][c], sl[v][c]);
+  __syncthreads();
+  float alh, all;
+  split_d2f(alpha, alh, all);
+  for (int e = threadIdx.x; e < ROWS * N; e += 256) {
+    const int rr = e % ROWS, c = e / ROWS;
+    const int row = row0 + rr;
+    if (row >= p.M) continue;
+    float th = red[0][c][rr].x, tl = red[0][c][rr].y;
+#pragma unroll
+    for (int q = 1; q < 8; ++q) df_add(th, tl, red[q][c][rr].x, red[q][c][rr].y);
+    if (ksplit == 1) {
+      double* cp = p.C + row + (size_t)c * p.ldc;
+      *cp = df_epilogue(th, tl, alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
+    } else {
+      reinterpret_cast<float2*>(part)[(((size_t)blockIdx.z * ksplit + blockIdx.y) * mmax + row) * 8 + c] =
+          make_float2(th, tl);
+    }
+  }
+}
+
+// split-K partials of k_skinny_df (float pairs) summed in double-float arithmetic
+__global__ void __launch_bounds__(256) k_skinny_reduce_df(const GemmP<double>* __restrict__ P, double alpha,
+                                                          double beta, int ksplit, const double* __restrict__ part,
+                                                          int mmax) {
+  const GemmP<double> p = P[blockIdx.y];
+  const float2* pp = reinterpret_cast<const float2*>(part);
+  float alh, all;
+  split_d2f(alpha, alh, all);
+  for (int e = blockIdx.x * 256 + threadIdx.x; e < p.M * p.N; e += gridDim.x * 256) {
+    const int row = e % p.M, c = e / p.M;
+    float th = 0.f, tl = 0.f;
+    for (int y = 0; y < ksplit; ++y) {
+      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
+      df_add(th, tl, q.x, q.y);
+    }
+    double* cp = p.C + row + (size_t)c * p.ldc;
+    *cp = df_epilogue(th, tl, alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
+  }
+}
+
+__global__ void k_split_df(const double* __restrict__ src, float2* __restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double x = src[i];
+    const float h = __double2float_rn(x);
+    dst[i] = make_float2(h, __double2float_rn(__dsub_rn(x, (double)h)));
+  }
+}
+
+void split_df(const double* src, double* dst, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_split_df<<<std::min(ceil_div(n, 256), 4096), 256, 0, s>>>(src, reinterpret_cast<float2*>(dst), n);
+  check_launch("k_split_df");
+}
+
 template <typename R>
 int skinny_ksplit(int batch, int maxM, int maxK) {
   constexpr int ROWS = 32 * Vec16<R>::V;
@@ -268,6 +487,22 @@ void gemm_skinny_split(const GemmP<R>* dP, int batch, int maxM, int maxN, R alph
     const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 64));
     k_skinny_reduce<R><<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
     check_launch("k_skinny_reduce");
+  }
+}
+
+void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
+                          int ksplit, double* part, cudaStream_t s) {
+  if (batch <= 0 || maxM <= 0) return;
+  HSS_REQUIRE(batch <= 65535 && maxN <= 8, HSS_ERR_ARG, "skinny gemm: batch <= 65535 and N <= 8");
+  HSS_REQUIRE(ksplit == 1 || part != nullptr, HSS_ERR_ARG, "skinny gemm: split-K needs a workspace");
+  dim3 grid(ceil_div(maxM, 64), ksplit, batch);
+  if (maxN <= 4) k_skinny_df<4><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  else k_skinny_df<8><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  check_launch("k_skinny_df");
+  if (ksplit > 1) {
+    const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 64));
+    k_skinny_reduce_df<<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+    check_launch("k_skinny_reduce_df");
   }
 }
 

@@ -20,6 +20,17 @@ struct GemmP {
   int lda, ldb, ldc;
 };
 
+// Double-float ("FP64 x FP32 pairs") skinny product: A holds every FP64 element
+// as a float pair (hi, lo) with hi + lo equal to it to 2^-48 (same 8 bytes per
+// element), B and C are FP64.  Each multiply-add runs on the FP32 pipes: an exact
+// product (FMA error term) plus the cross terms, added into a (hi, lo) float
+// accumulator with TwoSum and a Fast2Sum renormalisation.  GB300 issues FP32 at
+// 64x its FP64 rate, so this outruns native FP64 for matrix-vector products.
+void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
+                          int ksplit, double* part, cudaStream_t s);
+// dst[i] = (hi, lo) float pair of src[i], stored in the 8 bytes of dst[i]
+void split_df(const double* src, double* dst, long long n, cudaStream_t s);
+
 template <typename R>
 void gemm_batched(const GemmP<R>* dP, int batch, int maxM, int maxN, bool tA, bool tB,
                   R alpha, R beta, cudaStream_t s);

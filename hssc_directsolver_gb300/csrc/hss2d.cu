@@ -222,8 +222,15 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
 
 template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
-  for (auto& st : steps)
+  for (auto& st : steps) {
+    if constexpr (std::is_same<R, double>::value) {
+      if (df) {
+        gemm_skinny_split_df(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+        continue;
+      }
+    }
     gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+  }
 }
 
 template struct SolvePlan<double>;
@@ -352,6 +359,7 @@ void HSS2D::compress() {
     kgen_batched<double>(dkg.p, cnt, maxe, view(pts), kdev, stream);
     HSS_CUDA(cudaStreamSynchronize(stream));
   }
+  if (dfm()) make_df_forward();
   compressed = true;
   g_fwd.clear();
   fwd_plans.clear();
@@ -487,10 +495,35 @@ void HSS2D::invert_level(R* A, int n, int nb) {
   }
 }
 
+static void split_copy(const DevBuf<double>& src, DevBuf<double>& dst, cudaStream_t s) {
+  dst.alloc(std::max<size_t>(src.n, 1));
+  split_df(src.p, dst.p, (long long)src.n, s);
+}
+
+// Float-pair copies of the forward operator's blocks (T, Bself, B12, B21).
+void HSS2D::make_df_forward() {
+  for (auto& d : L) {
+    split_copy(d.Tup, d.Tup_df, stream);
+    split_copy(d.TdnT, d.TdnT_df, stream);
+    split_copy(d.Bself, d.Bself_df, stream);
+    split_copy(d.B12, d.B12_df, stream);
+    split_copy(d.B21, d.B21_df, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+// Float-pair copies of the FP64 inverse factors (FI, E, U, G, GE).
+void HSS2D::make_df_inverse() {
+  for (auto& d : L)
+    for (int i = 0; i < 5; ++i) split_copy(d.fd[i], d.fdf[i], stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
 void HSS2D::invert() {
   HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_invert before hss2d_compress");
   if (prm.precision == HSS_PREC_MIXED) invert_impl<float>();
   else invert_impl<double>();
+  if (dfm()) make_df_inverse();
   inverted = true;
   g_inv_d.clear();
   g_inv_f.clear();
@@ -509,6 +542,15 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
   SolvePlan<R>& pl = cache[r];
   const int depth = geo.depth;
   const long long N = geo.N;
+  bool use_df = false;
+  if constexpr (std::is_same<R, double>::value) use_df = dfm();
+  pl.df = use_df;
+  auto F = [&](Level2Dev& d, int i) -> const R* {
+    if constexpr (std::is_same<R, double>::value) {
+      if (use_df) return d.fdf[i].p;
+    }
+    return d.fac<R>(i).p;
+  };
   auto& vin = stage_in<R>();
   auto& vout = stage_out<R>();
   const int NG = prm.Ng * prm.Ng;
@@ -540,7 +582,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
-      P.push_back(GemmP<R>{d.fac<R>(2).p + fo(i) * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
+      P.push_back(GemmP<R>{F(d, 2) + fo(i) * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
                            g.k, ldq, g.nb * g.k});
     }
     pl.add(P, R(1), R(0), stream);
@@ -565,11 +607,11 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
-      P1.push_back(GemmP<R>{d.fac<R>(0).p + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
+      P1.push_back(GemmP<R>{F(d, 0) + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
       if (lev > 0) {
-        P2.push_back(GemmP<R>{d.fac<R>(3).p + fo(i) * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
+        P2.push_back(GemmP<R>{F(d, 3) + fo(i) * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
                               g.k, g.n, g.nb * g.k, ldo});
-        P3.push_back(GemmP<R>{d.fac<R>(4).p + fo(i) * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
+        P3.push_back(GemmP<R>{F(d, 4) + fo(i) * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
                               g.k, g.n, g.nb * g.k, ldo});
       }
     }
@@ -667,6 +709,9 @@ void HSS2D::fwd_prepare(int r) {
   fp.up.resize(depth + 1);
   fp.lam.resize(depth + 1);
   fp.eta.resize(depth + 1);
+  const bool df = dfm();
+  for (int lev = 0; lev <= depth; ++lev) fp.up[lev].df = fp.lam[lev].df = fp.eta[lev].df = df;
+  auto pick = [&](DevBuf<double>& a, DevBuf<double>& b) -> const double* { return df ? b.p : a.p; };
   for (int lev = depth; lev >= 1; --lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
@@ -674,7 +719,7 @@ void HSS2D::fwd_prepare(int r) {
     if (nr > 0) {
       std::vector<GemmP<double>> P;
       for (int i = 0; i < g.nb; ++i)
-        P.push_back(GemmP<double>{d.Tup.p + fo(i) * g.k * nr, d.rsF.p + (size_t)i * nr,
+        P.push_back(GemmP<double>{pick(d.Tup, d.Tup_df) + fo(i) * g.k * nr, d.rsF.p + (size_t)i * nr,
                                   d.upF.p + (size_t)i * g.k, g.k, r, nr, g.k, g.nb * nr, g.nb * g.k});
       fp.up[lev].add(P, 1.0, 1.0, stream);
     }
@@ -690,7 +735,7 @@ void HSS2D::fwd_prepare(int r) {
         const int b = (1 << lev) - 1 + i;
         out = Yd.p + (size_t)NG * geo.leaf_panel[b];
         ldo = (int)N;
-        P.push_back(GemmP<double>{d.Bself.p + fo(i) * g.n * g.n, Xd.p + (size_t)NG * geo.leaf_panel[b], out, g.n,
+        P.push_back(GemmP<double>{pick(d.Bself, d.Bself_df) + fo(i) * g.n * g.n, Xd.p + (size_t)NG * geo.leaf_panel[b], out, g.n,
                                   r, g.n, g.n, (int)N, ldo});
       } else {
         const auto& gc = geo.levels[lev + 1];
@@ -698,9 +743,9 @@ void HSS2D::fwd_prepare(int r) {
         out = dc.dnF.p + (size_t)(2 * i) * gc.k;
         ldo = gc.nb * gc.k;
         const int kc = gc.k;
-        P.push_back(GemmP<double>{d.B12.p + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i + 1) * kc, out, kc, r, kc,
+        P.push_back(GemmP<double>{pick(d.B12, d.B12_df) + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i + 1) * kc, out, kc, r, kc,
                                   kc, gc.nb * kc, ldo});
-        P.push_back(GemmP<double>{d.B21.p + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i) * kc, out + kc, kc, r, kc,
+        P.push_back(GemmP<double>{pick(d.B21, d.B21_df) + fo(i) * kc * kc, dc.upF.p + (size_t)(2 * i) * kc, out + kc, kc, r, kc,
                                   kc, gc.nb * kc, ldo});
       }
     }
@@ -709,7 +754,7 @@ void HSS2D::fwd_prepare(int r) {
     if (lev > 0 && nr > 0) {
       std::vector<GemmP<double>> Q;
       for (int i = 0; i < g.nb; ++i)
-        Q.push_back(GemmP<double>{d.TdnT.p + fo(i) * g.k * nr, d.dnF.p + (size_t)i * g.k,
+        Q.push_back(GemmP<double>{pick(d.TdnT, d.TdnT_df) + fo(i) * g.k * nr, d.dnF.p + (size_t)i * g.k,
                                   d.tmF.p + (size_t)i * nr, nr, r, g.k, nr, g.nb * g.k, g.nb * nr});
       fp.eta[lev].add(Q, 1.0, 0.0, stream);
     }

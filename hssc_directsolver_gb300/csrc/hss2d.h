@@ -22,6 +22,7 @@ struct SolvePlan {
     R alpha = R(1), beta = R(0);
   };
   std::vector<Step> steps;
+  bool df = false;  // FP64 operands stored as float pairs, products on the FP32 pipes
   void add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s);
   void run(cudaStream_t s) const;
   int launches() const {
@@ -40,6 +41,9 @@ struct Level2Dev {
   // inverse factors: 0 FI (n x n), 1 E (k x k), 2 U (k x n), 3 G (n x k), 4 GE (n x k)
   DevBuf<double> fd[5];
   DevBuf<float> ff[5];
+  // HSS_PREC_DFLOAT: the same FP64 factors and forward blocks as float pairs (8 bytes each)
+  DevBuf<double> fdf[5];
+  DevBuf<double> Tup_df, TdnT_df, Bself_df, B12_df, B21_df;
   // inverse-apply vectors: 0 phi_up, 1 phi_dn (nb*k x 8)
   DevBuf<double> vd[2];
   DevBuf<float> vf[2];
@@ -94,6 +98,9 @@ struct HSS2D {
   std::map<int, FwdPlan> fwd_plans;
   GraphCache g_inv_d, g_inv_f, g_fwd;
   bool use_graphs = true;
+  bool dfm() const { return prm.precision == HSS_PREC_DFLOAT; }
+  void make_df_forward();
+  void make_df_inverse();
 
   explicit HSS2D(const hss2d_params& p);
   ~HSS2D();

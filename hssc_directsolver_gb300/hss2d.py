@@ -37,7 +37,7 @@ class HSS2DParams:
     INTERform: str = "dense"
     transinv: int = 0
     sym: int = 0
-    precision: str = "fp64"   # "fp64" or "mixed"
+    precision: str = "fp64"   # "fp64", "mixed" or "dfloat" (FP64 factors, paired-FP32 solve products)
     n_cut: int = 400
     Fopts: str = "dense"
     k_cut: int = 2500         # low-rank T only where k < k_cut
@@ -61,7 +61,7 @@ class HSS2DParams:
             raise ValueError("INTERform must be 'dense' or 'lowrank'")
         if self.Fopts != "dense":
             raise ValueError("Fopts 'dense' (HSS-D) is the implemented inverse storage")
-        prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED}[self.precision]
+        prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED, "dfloat": L.HSS_PREC_DFLOAT}[self.precision]
         k = self.kernel
         k.h = self.h
         return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,

@@ -41,6 +41,8 @@ extern "C" {
 /* precision modes */
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
 #define HSS_PREC_MIXED 1 /* FP32 inverse factors, FP64 forward operator + refinement */
+#define HSS_PREC_DFLOAT 2 /* FP64 factors; solve products in paired FP32 arithmetic (~2^-48),
+                             FP64 refinement against the forward operator */
 
 /* HSS2D interpolation-operator storage (params.INTERform) */
 #define HSS_INTER_DENSE 0
@@ -168,7 +170,7 @@ typedef struct hss2d_params {
   int32_t interform; /* HSS_INTER_DENSE or HSS_INTER_LOWRANK (the reference default) */
   int32_t transinv;  /* 0: NTI (per-box operators) */
   int32_t sym;       /* 0: nsym */
-  int32_t precision; /* HSS_PREC_FP64 or HSS_PREC_MIXED */
+  int32_t precision; /* HSS_PREC_FP64, HSS_PREC_MIXED or HSS_PREC_DFLOAT */
   int32_t pad_;
   double acc;
   hss_kernel_params kp;
