@@ -349,10 +349,61 @@ __device__ __forceinline__ double df_epilogue(float th, float tl, float ah, floa
   return df_to_double(th, tl);
 }
 
+// Paired-FP32 SIMD (sm_100+ f32x2): two lanes of FP32 per instruction, used for
+// the two rows a thread owns.  Values are 64-bit registers {row0, row1}.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_pack(float a, float b) {
+  f32x2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+  return d;
+}
+__device__ __forceinline__ void x2_unpack(f32x2 d, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(d));
+}
+
+// df_madd on two rows at once.  bh2 = (bh, bh), bhn2 = -bh2, bln2 = -(bl, bl).
+// en = ah*(-bh) + p = -(exact error of p); tn = -(ah*bl + al*bh + e).  The high
+// sum takes the TwoSum of p; every low-order term (its rounding error and tn)
+// goes into sl, renormalised only at the end: the loop-carried chain is one add
+// for sh and one for sl, so the eight accumulators of a thread overlap.  sl then
+// carries ~2^-24 |sl| per step, ~K 2^-48 of the sum over K steps.
+__device__ __forceinline__ void df_madd_x2(f32x2& sh, f32x2& sl, f32x2 ah, f32x2 al, f32x2 bh2, f32x2 bhn2,
+                                           f32x2 bln2) {
+  const f32x2 p = x2_mul(ah, bh2);
+  const f32x2 en = x2_fma(ah, bhn2, p);
+  const f32x2 tn = x2_fma(ah, bln2, x2_fma(al, bhn2, en));
+  const f32x2 s = x2_add(sh, p);
+  const f32x2 bb = x2_sub(s, sh);
+  const f32x2 err = x2_add(x2_sub(sh, x2_sub(s, bb)), x2_sub(p, bb));
+  sl = x2_add(sl, x2_sub(err, tn));
+  sh = s;
+}
+
 template <int NR>
-__global__ void __launch_bounds__(256) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
+__global__ void __launch_bounds__(256, (NR > 4) ? 3 : 5) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
                                                    int ksplit, double* __restrict__ part, int mmax) {
   constexpr int V = 2;  // one 16-byte load = two (hi, lo) pairs
+  constexpr int KC = (NR > 4) ? SK_KC / 2 : SK_KC;  // static shared memory under 48 KB
   constexpr int ROWS = 32 * V;
   const GemmP<double> p = P[blockIdx.z];
   const int row0 = blockIdx.x * ROWS;
@@ -361,26 +412,25 @@ __global__ void __launch_bounds__(256) k_skinny_df(const GemmP<double>* __restri
   const int N = p.N;
   const int kper = (((p.K + ksplit - 1) / ksplit) + 7) & ~7;
   const int kb = blockIdx.y * kper, ke = min(p.K, kb + kper);
-  __shared__ float Bh[SK_KC][NR], Bl[SK_KC][NR];
+  __shared__ f32x2 Bh2[KC][NR], Bhn2[KC][NR], Bln2[KC][NR];
   __shared__ float2 red[8][NR][ROWS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int r = row0 + lane * V;
   const bool vec_ok = ((p.lda % V) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
-  float sh[V][NR], sl[V][NR];
+  f32x2 sh[NR], sl[NR];  // {row r, row r+1} accumulators
 #pragma unroll
-  for (int v = 0; v < V; ++v)
-#pragma unroll
-    for (int c = 0; c < NR; ++c) { sh[v][c] = 0.f; sl[v][c] = 0.f; }
-  for (int kc = kb; kc < ke; kc += SK_KC) {
-    const int kn = min(SK_KC, ke - kc);
+  for (int c = 0; c < NR; ++c) { sh[c] = 0ULL; sl[c] = 0ULL; }
+  for (int kc = kb; kc < ke; kc += KC) {
+    const int kn = min(KC, ke - kc);
     __syncthreads();
-    for (int e = threadIdx.x; e < SK_KC * NR; e += 256) {
-      const int kk = e % SK_KC, c = e / SK_KC;
+    for (int e = threadIdx.x; e < KC * NR; e += 256) {
+      const int kk = e % KC, c = e / KC;
       const double x = (kk < kn && c < N) ? p.B[(size_t)(kc + kk) + (size_t)c * p.ldb] : 0.0;
       float xh, xl;
       split_d2f(x, xh, xl);
-      Bh[kk][c] = xh;
-      Bl[kk][c] = xl;
+      Bh2[kk][c] = x2_pack(xh, xh);
+      Bhn2[kk][c] = x2_pack(-xh, -xh);
+      Bln2[kk][c] = x2_pack(-xl, -xl);
     }
     __syncthreads();
     // software-pipelined: the next column's 16 bytes are in flight during this column's math
@@ -394,20 +444,22 @@ __global__ void __launch_bounds__(256) k_skinny_df(const GemmP<double>* __restri
     float4 cur = (w < kn) ? load(w) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int kk = w; kk < kn; kk += 8) {
       const float4 nxt = (kk + 8 < kn) ? load(kk + 8) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float ah[V] = {cur.x, cur.z}, al[V] = {cur.y, cur.w};
+      const f32x2 ah = x2_pack(cur.x, cur.z), al = x2_pack(cur.y, cur.w);
 #pragma unroll
-      for (int c = 0; c < NR; ++c) {
-        const float bh = Bh[kk][c], bl = Bl[kk][c];
-#pragma unroll
-        for (int v = 0; v < V; ++v) df_madd(sh[v][c], sl[v][c], ah[v], al[v], bh, bl);
-      }
+      for (int c = 0; c < NR; ++c) df_madd_x2(sh[c], sl[c], ah, al, Bh2[kk][c], Bhn2[kk][c], Bln2[kk][c]);
       cur = nxt;
     }
   }
 #pragma unroll
-  for (int v = 0; v < V; ++v)
-#pragma unroll
-    for (int c = 0; c < NR; ++c) red[w][c][lane * V + v] = make_float2(sh[v][c], sl[v][c]);
+  for (int c = 0; c < NR; ++c) {
+    const f32x2 hi = x2_add(sh[c], sl[c]);  // Fast2Sum renormalisation
+    const f32x2 lo = x2_sub(sl[c], x2_sub(hi, sh[c]));
+    float h0, h1, l0, l1;
+    x2_unpack(hi, h0, h1);
+    x2_unpack(lo, l0, l1);
+    red[w][c][lane * V] = make_float2(h0, l0);
+    red[w][c][lane * V + 1] = make_float2(h1, l1);
+  }
   __syncthreads();
   float alh, all;
   split_d2f(alpha, alh, all);
@@ -438,13 +490,25 @@ __global__ void __launch_bounds__(256) k_skinny_reduce_df(const GemmP<double>* _
   split_d2f(alpha, alh, all);
   for (int e = blockIdx.x * 256 + threadIdx.x; e < p.M * p.N; e += gridDim.x * 256) {
     const int row = e % p.M, c = e / p.M;
-    float th = 0.f, tl = 0.f;
-    for (int y = 0; y < ksplit; ++y) {
-      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
-      df_add(th, tl, q.x, q.y);
+    // four independent running sums (slices y = j mod 4), combined in a fixed order
+    float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
+    int y = 0;
+    for (; y + 4 <= ksplit; y += 4) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float2 q = pp[(((size_t)blockIdx.y * ksplit + y + j) * mmax + row) * 8 + c];
+        df_add(th[j], tl[j], q.x, q.y);
+      }
     }
+    for (; y < ksplit; ++y) {
+      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
+      df_add(th[y & 3], tl[y & 3], q.x, q.y);
+    }
+    df_add(th[0], tl[0], th[1], tl[1]);
+    df_add(th[2], tl[2], th[3], tl[3]);
+    df_add(th[0], tl[0], th[2], tl[2]);
     double* cp = p.C + row + (size_t)c * p.ldc;
-    *cp = df_epilogue(th, tl, alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
+    *cp = df_epilogue(th[0], tl[0], alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
   }
 }
 
@@ -490,6 +554,14 @@ void gemm_skinny_split(const GemmP<R>* dP, int batch, int maxM, int maxN, R alph
   }
 }
 
+int skinny_ksplit_df(int batch, int maxM, int maxK) {
+  const long long ctas = (long long)ceil_div(maxM, 64) * batch;
+  if (ctas >= 1216 || maxK < 128) return 1;
+  int ks = (int)std::min<long long>(32, (1216 + ctas - 1) / ctas);
+  ks = std::max(1, std::min(ks, maxK / 64));
+  return ks;
+}
+
 void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
                           int ksplit, double* part, cudaStream_t s) {
   if (batch <= 0 || maxM <= 0) return;
@@ -500,7 +572,7 @@ void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN
   else k_skinny_df<8><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
   check_launch("k_skinny_df");
   if (ksplit > 1) {
-    const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 64));
+    const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 256));
     k_skinny_reduce_df<<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
     check_launch("k_skinny_reduce_df");
   }

@@ -28,6 +28,9 @@ struct GemmP {
 // 64x its FP64 rate, so this outruns native FP64 for matrix-vector products.
 void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
                           int ksplit, double* part, cudaStream_t s);
+// K slices for gemm_skinny_split_df: enough CTAs for several waves on 152 SMs
+// (the double-float kernel does ~15x the arithmetic per byte of the FP64 one)
+int skinny_ksplit_df(int batch, int maxM, int maxK);
 // dst[i] = (hi, lo) float pair of src[i], stored in the 8 bytes of dst[i]
 void split_df(const double* src, double* dst, long long n, cudaStream_t s);
 

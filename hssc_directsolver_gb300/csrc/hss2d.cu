@@ -213,7 +213,7 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
   for (auto& p : P) { st.maxM = std::max(st.maxM, p.M); st.maxN = std::max(st.maxN, p.N); maxK = std::max(maxK, p.K); }
   st.alpha = alpha;
   st.beta = beta;
-  st.ksplit = skinny_ksplit<R>(st.batch, st.maxM, maxK);
+  st.ksplit = df ? skinny_ksplit_df(st.batch, st.maxM, maxK) : skinny_ksplit<R>(st.batch, st.maxM, maxK);
   if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
   st.d.alloc(P.size());
   HSS_CUDA(cudaMemcpyAsync(st.d.p, P.data(), P.size() * sizeof(GemmP<R>), cudaMemcpyHostToDevice, s));

@@ -225,3 +225,7 @@ def test_dfloat_solve_matches_fp64(gpu):
     x, rr, it = G2.HSS2D_solve(ts["dfloat"], f, 1e-10, 5)
     assert rr <= 1e-10
     assert np.linalg.norm(x - x64) <= 1e-10 * np.linalg.norm(x64)
+    f11 = np.random.default_rng(4).standard_normal((ts["fp64"].N, 11))   # 8 + 3 columns
+    a = G2.HSS2D_applyinv_nsym(ts["fp64"], ts["fp64"], f11)
+    b = G2.HSS2D_applyinv_nsym(ts["dfloat"], ts["dfloat"], f11)
+    assert np.linalg.norm(b - a) <= 1e-11 * np.linalg.norm(a)
