@@ -35,6 +35,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 METRIC = "compress+invert s and solves/s at 1e-10 residual: mixed/batched vs plain FP64"
+
+# DRAM bytes (read + write) of the skinny-product kernels of one inverse apply at this
+# workload, from the ncu capture summarised in profiles/skinny_hss2d_n65536.md
+TRAFFIC_PER_APPLYINV = {}
 WORKLOAD = "HSS2D 256x256 grid (Ng=8, 32x32 panels, N=65536), leaf 8x8, tol 1e-10, 4 RHS"
 
 
@@ -247,7 +251,7 @@ def main():
 
     F = rhs(workload_params("fp64", args.npan).N)
     results = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "dfloat"):
         prm = workload_params(prec, args.npan)
         barrier()
         t0 = time.perf_counter()
@@ -330,7 +334,7 @@ def main():
     if not args.no_batched:
         batched = bench_batched(args, L, dev)
 
-    ok = [p for p in ("mixed", "fp64") if results[p]["relres"] <= 1e-10]
+    ok = [p for p in ("dfloat", "mixed", "fp64") if results[p]["relres"] <= 1e-10]
     best = min(ok, key=lambda p: results[p]["solve_ms"]) if ok else "fp64"
     r = results[best]
     peaks = {}
@@ -345,11 +349,12 @@ def main():
     achieved = r["solve_bytes"] / (r["applyinv_ms"] * 1e-3) / 1e9
     N = workload_params("fp64", args.npan).N
     nrhs = F.shape[1]
-    launches_per_solve = r["launches"] + (r["solves_used"] - 1) * r["launches"]
+    launches_per_solve = r["launches"] * r["solves_used"]
     line = {
         "metric": METRIC, "value": 1e3 / r["solve_ms"] * world, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["solve_ms"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if best == "mixed" else "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"mixed": "f32+f64", "dfloat": "f64 (products as f32 pairs)"}.get(best, "f64"),
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nrhs": nrhs, "path": best, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (factors %.2f GB per solve)" % (r["solve_bytes"] / 1e9)},
@@ -363,8 +368,11 @@ def main():
         "e2e": {"value": 1.0 / r["e2e_s"] * world, "unit": "solves/s",
                 "h2d_bytes_per_step": int(N * nrhs * 8), "d2h_bytes_per_step": int(N * nrhs * 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "k_gemm_skinny chain of one inverse apply",
-                     "peak_source": peak_src},
+                     "traffic": TRAFFIC_PER_APPLYINV.get(best),
+                     "kernel": {"dfloat": "k_skinny_df", "mixed": "k_skinny<float>"}.get(best, "k_skinny<double>")
+                               + " chain of one inverse apply",
+                     "peak_source": peak_src,
+                     "algorithmic_bytes": r["solve_bytes"]},
         "gpu_launches": int(args.steps * launches_per_solve),
         "clocks": r["clocks"],
     }

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256) k_skinny(const GemmP<R>* __restrict__ P, 
       R* cp = p.C + row + (size_t)c * p.ldc;
       *cp = (beta == R(0)) ? alpha * t : alpha * t + beta * (*cp);
     } else {
-      part[(((size_t)blockIdx.z * ksplit + blockIdx.y) * mmax + row) * 8 + c] = t;
+      part[(((size_t)blockIdx.z * ksplit + blockIdx.y) * 8 + c) * mmax + row] = t;
     }
   }
 }
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) k_skinny_reduce(const GemmP<R>* __restric
   for (int e = blockIdx.x * 256 + threadIdx.x; e < p.M * p.N; e += gridDim.x * 256) {
     const int row = e % p.M, c = e / p.M;
     R t = R(0);
-    for (int y = 0; y < ksplit; ++y) t += part[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
+    for (int y = 0; y < ksplit; ++y) t += part[(((size_t)blockIdx.y * ksplit + y) * 8 + c) * mmax + row];
     R* cp = p.C + row + (size_t)c * p.ldc;
     *cp = (beta == R(0)) ? alpha * t : alpha * t + beta * (*cp);
   }
@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 5) k_skinny_df(const GemmP
       double* cp = p.C + row + (size_t)c * p.ldc;
       *cp = df_epilogue(th, tl, alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
     } else {
-      reinterpret_cast<float2*>(part)[(((size_t)blockIdx.z * ksplit + blockIdx.y) * mmax + row) * 8 + c] =
+      reinterpret_cast<float2*>(part)[(((size_t)blockIdx.z * ksplit + blockIdx.y) * 8 + c) * mmax + row] =
           make_float2(th, tl);
     }
   }
@@ -496,12 +496,12 @@ __global__ void __launch_bounds__(256) k_skinny_reduce_df(const GemmP<double>* _
     for (; y + 4 <= ksplit; y += 4) {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const float2 q = pp[(((size_t)blockIdx.y * ksplit + y + j) * mmax + row) * 8 + c];
+        const float2 q = pp[(((size_t)blockIdx.y * ksplit + y + j) * 8 + c) * mmax + row];
         df_add(th[j], tl[j], q.x, q.y);
       }
     }
     for (; y < ksplit; ++y) {
-      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * mmax + row) * 8 + c];
+      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * 8 + c) * mmax + row];
       df_add(th[y & 3], tl[y & 3], q.x, q.y);
     }
     df_add(th[0], tl[0], th[1], tl[1]);

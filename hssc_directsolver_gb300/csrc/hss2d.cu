@@ -930,10 +930,34 @@ long long HSS2D::solve_bytes() const {
   return b * (long long)es;
 }
 
+// Kernels of one solve with one residual check: inverse apply (skinny steps and
+// split-K reductions of the cached plan), forward apply (gather, products,
+// scatter per level) and the residual kernel; conversions in mixed precision.
 int HSS2D::solve_launches(int nrhs) const {
-  // per chunk of 8: 2 staging copies + depth up steps + 1 + 3*depth down steps
-  const int chunks = (nrhs + 7) / 8;
-  return chunks * (2 + geo.depth + 1 + 3 * geo.depth);
+  int total = 0;
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    int inv = 0;
+    if (prm.precision == HSS_PREC_MIXED) {
+      auto it = inv_plans_f.find(r);
+      inv = (it != inv_plans_f.end()) ? it->second.launches() : (geo.depth + 1 + 3 * geo.depth);
+      inv += 2;  // FP64 <-> FP32 conversions
+    } else {
+      auto it = inv_plans_d.find(r);
+      inv = (it != inv_plans_d.end()) ? it->second.launches() : (geo.depth + 1 + 3 * geo.depth);
+    }
+    int fwd = 2 * geo.depth;  // gather and scatter per level
+    auto f = fwd_plans.find(r);
+    if (f != fwd_plans.end()) {
+      for (auto& pl : f->second.up) fwd += pl.launches();
+      for (auto& pl : f->second.lam) fwd += pl.launches();
+      for (auto& pl : f->second.eta) fwd += pl.launches();
+    } else {
+      fwd += 3 * geo.depth + 1;
+    }
+    total += inv + fwd + 1;
+  }
+  return total;
 }
 
 }  // namespace hss

@@ -218,7 +218,8 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
 int hss2d_interp_ranks(const hss2d_matrix* H, int32_t* q_up, int32_t* q_dn);
 /* bytes of factor storage read by one inverse apply (roofline accounting) */
 int hss2d_solve_bytes(const hss2d_matrix* H, int64_t* bytes);
-/* launches issued by one applyinv of nrhs columns (counted by the host) */
+/* kernels launched by one solve of nrhs columns with one residual check: the inverse
+ * apply, the forward apply and the residual (counted by the host from the cached plans) */
 int hss2d_solve_launches(const hss2d_matrix* H, int32_t nrhs, int32_t* launches);
 int hss2d_destroy(hss2d_matrix* H);
 
