@@ -421,6 +421,13 @@ int hss1d_transforminv(hss1d_matrix* H, hss1d_matrix** out) {
   HSS_CATCH
 }
 
+int hss1d_set_precision(hss1d_matrix* H, int32_t precision) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->set_precision(precision);
+  HSS_CATCH
+}
+
 int hss1d_destroy(hss1d_matrix* H) {
   HSS_TRY
   if (H) {

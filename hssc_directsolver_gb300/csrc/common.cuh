@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <map>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -119,6 +120,48 @@ template <typename T>
 inline void download(std::vector<T>& h, const T* d, size_t cnt, cudaStream_t s) {
   h.resize(cnt);
   if (cnt) HSS_CUDA(cudaMemcpyAsync(h.data(), d, cnt * sizeof(T), cudaMemcpyDeviceToHost, s));
+}
+
+// Instantiated CUDA graphs of fixed launch sequences, keyed by the number of
+// right-hand sides.
+struct GraphCache {
+  std::map<int, cudaGraphExec_t> g;
+  GraphCache() = default;
+  GraphCache(const GraphCache&) = delete;
+  GraphCache& operator=(const GraphCache&) = delete;
+  ~GraphCache() { clear(); }
+  void clear() {
+    for (auto& kv : g) cudaGraphExecDestroy(kv.second);
+    g.clear();
+  }
+};
+
+// Capture body() on the stream into a graph once per key, then replay it.
+template <typename F>
+inline void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&& body) {
+  if (!enabled) {
+    body();
+    return;
+  }
+  auto it = gc.g.find(key);
+  if (it == gc.g.end()) {
+    cudaGraph_t graph = nullptr;
+    HSS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    HSS_CUDA(cudaStreamEndCapture(s, &graph));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    HSS_REQUIRE(e == cudaSuccess, HSS_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    it = gc.g.emplace(key, ex).first;
+  }
+  HSS_CUDA(cudaGraphLaunch(it->second, s));
 }
 
 }  // namespace hss

@@ -842,6 +842,7 @@ void HSS1D::transforminv(HSS1D& K) {
 
 // ---------------------------------------------------------------------------
 void HSS1D::invert() {
+  clear_plans();
   oL.assign(nboxes, 0); oR.assign(nboxes, 0); oD.assign(nboxes, 0); oE.assign(nboxes, 0);
   long long tl = 0, td = 0, te = 0;
   for (int b = 0; b < nboxes; ++b) {
@@ -963,6 +964,7 @@ void HSS1D::invert() {
   HSS_CUDA(cudaStreamSynchronize(stream));
   invert_many(mats, stream);
   inverted = true;
+  if (dfm()) make_df();
 }
 
 // ---------------------------------------------------------------------------
@@ -989,65 +991,176 @@ static Stack1 make_stack(const HSS1D& H, int width) {
   return s;
 }
 
-void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
-  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_applyinv before hss1d_invert");
-  const Stack1 S = make_stack(*this, 8);
-  v1.alloc(std::max(S.base.back(), 1LL));
-  v2.alloc(std::max(S.base.back(), 1LL));
-  for (int c0 = 0; c0 < nrhs; c0 += 8) {
-    const int r = std::min(8, nrhs - c0);
-    const double* ff = dX + (size_t)c0 * Ntot;
-    double* xx = dY + (size_t)c0 * Ntot;
-    auto vin = [&](int b, const double*& p, int& ld) {
-      if (is_leaf(b)) { p = ff + off[b]; ld = (int)Ntot; }
-      else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
-    };
-    for (int L = maxlev; L >= 1; --L) {
-      std::vector<GemmP<double>> P;
-      for (int b = 0; b < nboxes; ++b) {
-        if (level[b] != L) continue;
-        const double* in;
-        int ldi;
-        vin(b, in, ldi);
-        P.push_back(GemmP<double>{Rinv.p + oR[b], in, v1.p + S.base[L] + S.row[b], kskel[b], r, nskel[b], kskel[b],
-                                  ldi, S.ld[L]});
-      }
-      run_gemms(P, false, false, 1.0, 0.0, stream, true);
-    }
-    {
-      std::vector<GemmP<double>> P;
-      for (int p = 0; p < nprob; ++p) {
-        const int a = c1[proot[p]];
-        P.push_back(GemmP<double>{FTinv.p + oFT[p], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[a],
-                                  ktop[p], r, ktop[p], ktop[p], S.ld[1], S.ld[1]});
-      }
-      run_gemms(P, false, false, 1.0, 0.0, stream, true);
-    }
-    for (int L = 1; L <= maxlev; ++L) {
-      std::vector<GemmP<double>> P1, P2;
-      for (int b = 0; b < nboxes; ++b) {
-        if (level[b] != L) continue;
-        double* out;
-        int ldo;
-        if (is_leaf(b)) { out = xx + off[b]; ldo = (int)Ntot; }
-        else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
-        const double* in;
-        int ldi;
-        vin(b, in, ldi);
-        P1.push_back(GemmP<double>{Linv.p + oL[b], v2.p + S.base[L] + S.row[b], out, nskel[b], r, kskel[b], nskel[b],
-                                   S.ld[L], ldo});
-        P2.push_back(GemmP<double>{Dinv.p + oD[b], in, out, nskel[b], r, nskel[b], nskel[b], ldi, ldo});
-      }
-      run_gemms(P1, false, false, 1.0, 0.0, stream, true);
-      run_gemms(P2, false, false, 1.0, 1.0, stream, true);
+void Plan1::gemm(const std::vector<GemmP<double>>& P, double alpha, double beta, cudaStream_t s) {
+  if (P.empty()) return;
+  Step st;
+  st.batch = (int)P.size();
+  int maxK = 0;
+  for (auto& p : P) { st.maxM = std::max(st.maxM, p.M); st.maxN = std::max(st.maxN, p.N); maxK = std::max(maxK, p.K); }
+  st.alpha = alpha;
+  st.beta = beta;
+  st.ksplit = df ? skinny_ksplit_df(st.batch, st.maxM, maxK) : skinny_ksplit<double>(st.batch, st.maxM, maxK);
+  if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
+  st.g.upload(P, s);
+  steps.push_back(std::move(st));
+}
+
+void Plan1::moves(const std::vector<MoveP>& mv, cudaStream_t s) {
+  if (mv.empty()) return;
+  Step st;
+  st.move = true;
+  st.batch = (int)mv.size();
+  st.m.upload(mv, s);
+  steps.push_back(std::move(st));
+}
+
+void Plan1::run(cudaStream_t s) const {
+  for (auto& st : steps) {
+    for (int o = 0; o < st.batch; o += 65535) {
+      const int cnt = std::min(65535, st.batch - o);
+      double* part = st.part.p ? st.part.p + (size_t)o * st.ksplit * st.maxM * 8 : nullptr;
+      if (st.move) move_batched(st.m.p + o, cnt, s);
+      else if (df) gemm_skinny_split_df(st.g.p + o, cnt, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, part, s);
+      else gemm_skinny_split<double>(st.g.p + o, cnt, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, part, s);
     }
   }
 }
 
-void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
+int Plan1::launches() const {
+  int n = 0;
+  for (auto& st : steps) n += ((st.batch + 65534) / 65535) * ((!st.move && st.ksplit > 1) ? 2 : 1);
+  return n;
+}
+
+void HSS1D::ensure_work() {
   const Stack1 S = make_stack(*this, 8);
-  v1.alloc(std::max(S.base.back(), 1LL));
-  v2.alloc(std::max(S.base.back(), 1LL));
+  v1.ensure(std::max(S.base.back(), 1LL));
+  v2.ensure(std::max(S.base.back(), 1LL));
+  long long ts = 0;
+  for (int b = 0; b < nboxes; ++b)
+    if (parent[b] >= 0) ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8;
+  v3.ensure(std::max(ts, 1LL));
+  Xs.ensure((size_t)Ntot * 8);
+  Ys.ensure((size_t)Ntot * 8);
+}
+
+// inverse apply of r columns Xs -> Ys (HSS1D_applyinv_nsym.m:43-86): up Rinv, top FTinv,
+// down Linv (+ Dinv on the box input)
+Plan1& HSS1D::inv_plan(int r) {
+  auto it = inv_plans.find(r);
+  if (it != inv_plans.end()) return it->second;
+  ensure_work();
+  Plan1& pl = inv_plans[r];
+  pl.df = dfm();
+  const double* RI = dfm() ? Rinv_df.p : Rinv.p;
+  const double* LI = dfm() ? Linv_df.p : Linv.p;
+  const double* DI = dfm() ? Dinv_df.p : Dinv.p;
+  const double* FT = dfm() ? FTinv_df.p : FTinv.p;
+  const Stack1 S = make_stack(*this, 8);
+  const double* ff = Xs.p;
+  double* xx = Ys.p;
+  auto vin = [&](int b, const double*& p, int& ld) {
+    if (is_leaf(b)) { p = ff + off[b]; ld = (int)Ntot; }
+    else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
+  };
+  std::vector<std::vector<int>> bylev(maxlev + 1);
+  for (int b = 0; b < nboxes; ++b)
+    if (parent[b] >= 0) bylev[level[b]].push_back(b);
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<GemmP<double>> P;
+    for (int b : bylev[L]) {
+      const double* in;
+      int ldi;
+      vin(b, in, ldi);
+      P.push_back(GemmP<double>{RI + oR[b], in, v1.p + S.base[L] + S.row[b], kskel[b], r, nskel[b], kskel[b],
+                                ldi, S.ld[L]});
+    }
+    pl.gemm(P, 1.0, 0.0, stream);
+  }
+  {
+    std::vector<GemmP<double>> P;
+    for (int p = 0; p < nprob; ++p) {
+      const int a = c1[proot[p]];
+      P.push_back(GemmP<double>{FT + oFT[p], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[a],
+                                ktop[p], r, ktop[p], ktop[p], S.ld[1], S.ld[1]});
+    }
+    pl.gemm(P, 1.0, 0.0, stream);
+  }
+  for (int L = 1; L <= maxlev; ++L) {
+    std::vector<GemmP<double>> P1, P2;
+    for (int b : bylev[L]) {
+      double* out;
+      int ldo;
+      if (is_leaf(b)) { out = xx + off[b]; ldo = (int)Ntot; }
+      else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
+      const double* in;
+      int ldi;
+      vin(b, in, ldi);
+      P1.push_back(GemmP<double>{LI + oL[b], v2.p + S.base[L] + S.row[b], out, nskel[b], r, kskel[b], nskel[b],
+                                 S.ld[L], ldo});
+      P2.push_back(GemmP<double>{DI + oD[b], in, out, nskel[b], r, nskel[b], nskel[b], ldi, ldo});
+    }
+    pl.gemm(P1, 1.0, 0.0, stream);
+    pl.gemm(P2, 1.0, 1.0, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  return pl;
+}
+
+static void split_into(const DevBuf<double>& src, DevBuf<double>& dst, cudaStream_t s) {
+  dst.alloc(std::max<size_t>(src.n, 1));
+  split_df(src.p, dst.p, (long long)src.n, s);
+}
+
+// float-pair copies of the operators the solve products read
+void HSS1D::make_df() {
+  split_into(T_UP, T_UP_df, stream);
+  split_into(TDNT, TDNT_df, stream);
+  split_into(M_SELF, M_SELF_df, stream);
+  split_into(M_SIB, M_SIB_df, stream);
+  if (inverted) {
+    split_into(Linv, Linv_df, stream);
+    split_into(Rinv, Rinv_df, stream);
+    split_into(Dinv, Dinv_df, stream);
+    split_into(FTinv, FTinv_df, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+void HSS1D::set_precision(int prec) {
+  HSS_REQUIRE(prec == HSS_PREC_FP64 || prec == HSS_PREC_DFLOAT, HSS_ERR_ARG,
+              "HSS1D solves run in HSS_PREC_FP64 or HSS_PREC_DFLOAT");
+  precision = prec;
+  clear_plans();
+  if (dfm()) make_df();
+}
+
+void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
+  HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_applyinv before hss1d_invert");
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    Plan1& pl = inv_plan(r);
+    HSS_CUDA(cudaMemcpyAsync(Xs.p, dX + (size_t)c0 * Ntot, (size_t)Ntot * r * sizeof(double),
+                             cudaMemcpyDeviceToDevice, stream));
+    run_graph(g_inv, r, stream, use_graphs, [&] { pl.run(stream); });
+    HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * Ntot, Ys.p, (size_t)Ntot * r * sizeof(double),
+                             cudaMemcpyDeviceToDevice, stream));
+  }
+}
+
+// forward apply of r columns Xs -> Ys (HSS1D_apply_nsym.m:38-100): up projections
+// q(J(1:k)) + T_UP q(J(k+1:n)), top siblings, down evaluations with M_SIB / M_SELF
+Plan1& HSS1D::fwd_plan(int r) {
+  auto it = fwd_plans.find(r);
+  if (it != fwd_plans.end()) return it->second;
+  ensure_work();
+  Plan1& pl = fwd_plans[r];
+  pl.df = dfm();
+  const double* TU = dfm() ? T_UP_df.p : T_UP.p;
+  const double* TD = dfm() ? TDNT_df.p : TDNT.p;
+  const double* MS = dfm() ? M_SELF_df.p : M_SELF.p;
+  const double* MB = dfm() ? M_SIB_df.p : M_SIB.p;
+  const Stack1 S = make_stack(*this, 8);
   std::vector<long long> oS(nboxes, 0);
   long long ts = 0;
   for (int b = 0; b < nboxes; ++b) {
@@ -1055,79 +1168,86 @@ void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
     oS[b] = ts;
     ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8;
   }
-  v3.alloc(std::max(ts, 1LL));
+  const double* qq = Xs.p;
+  double* uu = Ys.p;
+  auto vin = [&](int b, const double*& p, int& ld) {
+    if (is_leaf(b)) { p = qq + off[b]; ld = (int)Ntot; }
+    else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
+  };
+  std::vector<std::vector<int>> bylev(maxlev + 1);
+  for (int b = 0; b < nboxes; ++b)
+    if (parent[b] >= 0) bylev[level[b]].push_back(b);
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<MoveP> mv;
+    std::vector<GemmP<double>> P;
+    for (int b : bylev[L]) {
+      const int n = nskel[b], k = kskel[b], nr = n - k;
+      const double* in;
+      int ldi;
+      vin(b, in, ldi);
+      mv.push_back(MoveP{in, v1.p + S.base[L] + S.row[b], JUPd.p + oJ[b], k, r, ldi, S.ld[L], 0, 0});
+      if (nr > 0) {
+        mv.push_back(MoveP{in, v3.p + oS[b], JUPd.p + oJ[b] + k, nr, r, ldi, nr, 0, 0});
+        P.push_back(GemmP<double>{TU + oT[b], v3.p + oS[b], v1.p + S.base[L] + S.row[b], k, r, nr, k, nr,
+                                  S.ld[L]});
+      }
+    }
+    pl.moves(mv, stream);
+    pl.gemm(P, 1.0, 1.0, stream);
+  }
+  {
+    std::vector<GemmP<double>> P;
+    for (int p = 0; p < nprob; ++p) {
+      const int a = c1[proot[p]], b = c2[proot[p]];
+      P.push_back(GemmP<double>{MB + oSib[a], v1.p + S.base[1] + S.row[b], v2.p + S.base[1] + S.row[a],
+                                kskel[a], r, kskel[b], kskel[a], S.ld[1], S.ld[1]});
+      P.push_back(GemmP<double>{MB + oSib[b], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[b],
+                                kskel[b], r, kskel[a], kskel[b], S.ld[1], S.ld[1]});
+    }
+    pl.gemm(P, 1.0, 0.0, stream);
+  }
+  for (int L = 1; L <= maxlev; ++L) {
+    std::vector<GemmP<double>> PT, PS;
+    std::vector<MoveP> mv;
+    for (int b : bylev[L]) {
+      const int n = nskel[b], k = kskel[b], nr = n - k;
+      const double* dn = v2.p + S.base[L] + S.row[b];
+      double* out;
+      int ldo;
+      if (is_leaf(b)) { out = uu + off[b]; ldo = (int)Ntot; }
+      else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
+      if (nr > 0) PT.push_back(GemmP<double>{TD + oT[b], dn, v3.p + oS[b], nr, r, k, nr, S.ld[L], nr});
+      mv.push_back(MoveP{dn, out, JDNd.p + oJ[b], k, r, S.ld[L], ldo, 2, 0});
+      if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJ[b] + k, nr, r, nr, ldo, 2, 0});
+      if (is_leaf(b)) {
+        PS.push_back(GemmP<double>{MS + oSelf[b], qq + off[b], out, n, r, n, n, (int)Ntot, ldo});
+      } else {
+        const int s1 = c1[b], s2 = c2[b];
+        const double* up1 = v1.p + S.base[L + 1] + S.row[s1];
+        const double* up2 = v1.p + S.base[L + 1] + S.row[s2];
+        PS.push_back(GemmP<double>{MB + oSib[s1], up2, out, kskel[s1], r, kskel[s2], kskel[s1], S.ld[L + 1],
+                                   ldo});
+        PS.push_back(GemmP<double>{MB + oSib[s2], up1, out + kskel[s1], kskel[s2], r, kskel[s1], kskel[s2],
+                                   S.ld[L + 1], ldo});
+      }
+    }
+    pl.gemm(PT, 1.0, 0.0, stream);
+    pl.moves(mv, stream);
+    pl.gemm(PS, 1.0, 1.0, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  return pl;
+}
+
+void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
   for (int c0 = 0; c0 < nrhs; c0 += 8) {
     const int r = std::min(8, nrhs - c0);
-    const double* qq = dX + (size_t)c0 * Ntot;
-    double* uu = dY + (size_t)c0 * Ntot;
-    auto vin = [&](int b, const double*& p, int& ld) {
-      if (is_leaf(b)) { p = qq + off[b]; ld = (int)Ntot; }
-      else { const int L = level[b] + 1; p = v1.p + S.base[L] + S.row[c1[b]]; ld = S.ld[L]; }
-    };
-    // upward: phi_up = q(J(1:k)) + T_UP q(J(k+1:n))
-    for (int L = maxlev; L >= 1; --L) {
-      std::vector<MoveP> mv;
-      std::vector<GemmP<double>> P;
-      for (int b = 0; b < nboxes; ++b) {
-        if (level[b] != L) continue;
-        const int n = nskel[b], k = kskel[b], nr = n - k;
-        const double* in;
-        int ldi;
-        vin(b, in, ldi);
-        mv.push_back(MoveP{in, v1.p + S.base[L] + S.row[b], JUPd.p + oJ[b], k, r, ldi, S.ld[L], 0, 0});
-        if (nr > 0) {
-          mv.push_back(MoveP{in, v3.p + oS[b], JUPd.p + oJ[b] + k, nr, r, ldi, nr, 0, 0});
-          P.push_back(GemmP<double>{T_UP.p + oT[b], v3.p + oS[b], v1.p + S.base[L] + S.row[b], k, r, nr, k, nr,
-                                    S.ld[L]});
-        }
-      }
-      run_moves(mv, stream);
-      run_gemms(P, false, false, 1.0, 1.0, stream, true);
-    }
-    // top sibling interactions of every tree
-    {
-      std::vector<GemmP<double>> P;
-      for (int p = 0; p < nprob; ++p) {
-        const int a = c1[proot[p]], b = c2[proot[p]];
-        P.push_back(GemmP<double>{M_SIB.p + oSib[a], v1.p + S.base[1] + S.row[b], v2.p + S.base[1] + S.row[a],
-                                  kskel[a], r, kskel[b], kskel[a], S.ld[1], S.ld[1]});
-        P.push_back(GemmP<double>{M_SIB.p + oSib[b], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[b],
-                                  kskel[b], r, kskel[a], kskel[b], S.ld[1], S.ld[1]});
-      }
-      run_gemms(P, false, false, 1.0, 0.0, stream, true);
-    }
-    // downward: u_long = L phi_dn (+ sibling terms or self term)
-    for (int L = 1; L <= maxlev; ++L) {
-      std::vector<GemmP<double>> PT, PS;
-      std::vector<MoveP> mv;
-      for (int b = 0; b < nboxes; ++b) {
-        if (level[b] != L) continue;
-        const int n = nskel[b], k = kskel[b], nr = n - k;
-        const double* dn = v2.p + S.base[L] + S.row[b];
-        double* out;
-        int ldo;
-        if (is_leaf(b)) { out = uu + off[b]; ldo = (int)Ntot; }
-        else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
-        if (nr > 0)
-          PT.push_back(GemmP<double>{TDNT.p + oT[b], dn, v3.p + oS[b], nr, r, k, nr, S.ld[L], nr});
-        mv.push_back(MoveP{dn, out, JDNd.p + oJ[b], k, r, S.ld[L], ldo, 2, 0});
-        if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJ[b] + k, nr, r, nr, ldo, 2, 0});
-        if (is_leaf(b)) {
-          PS.push_back(GemmP<double>{M_SELF.p + oSelf[b], qq + off[b], out, n, r, n, n, (int)Ntot, ldo});
-        } else {
-          const int s1 = c1[b], s2 = c2[b];
-          const double* up1 = v1.p + S.base[L + 1] + S.row[s1];
-          const double* up2 = v1.p + S.base[L + 1] + S.row[s2];
-          PS.push_back(GemmP<double>{M_SIB.p + oSib[s1], up2, out, kskel[s1], r, kskel[s2], kskel[s1], S.ld[L + 1],
-                                     ldo});
-          PS.push_back(GemmP<double>{M_SIB.p + oSib[s2], up1, out + kskel[s1], kskel[s2], r, kskel[s1], kskel[s2],
-                                     S.ld[L + 1], ldo});
-        }
-      }
-      run_gemms(PT, false, false, 1.0, 0.0, stream, true);
-      run_moves(mv, stream);
-      run_gemms(PS, false, false, 1.0, 1.0, stream, true);
-    }
+    Plan1& pl = fwd_plan(r);
+    HSS_CUDA(cudaMemcpyAsync(Xs.p, dX + (size_t)c0 * Ntot, (size_t)Ntot * r * sizeof(double),
+                             cudaMemcpyDeviceToDevice, stream));
+    run_graph(g_fwd, r, stream, use_graphs, [&] { pl.run(stream); });
+    HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * Ntot, Ys.p, (size_t)Ntot * r * sizeof(double),
+                             cudaMemcpyDeviceToDevice, stream));
   }
 }
 
@@ -1170,7 +1290,12 @@ void HSS1D::solve_device(const double* df, double* dx, int nrhs, double tol, int
   HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_solve before hss1d_invert");
   HSS_REQUIRE(nrhs >= 1 && maxit >= 1, HSS_ERR_ARG, "nrhs and maxit must be >= 1");
   const long long cnt = Ntot * nrhs;
-  DevBuf<double> y(cnt), res(cnt), dd(cnt);
+  ir_y.ensure(cnt);
+  ir_res.ensure(cnt);
+  ir_dd.ensure(cnt);
+  DevBuf<double>& y = ir_y;
+  DevBuf<double>& res = ir_res;
+  DevBuf<double>& dd = ir_dd;
   const int gx = 256;
   DevBuf<double> part((size_t)gx * nrhs * 2);
   applyinv_device(df, dx, nrhs);

@@ -5,6 +5,7 @@
 // arenas, so every level of every problem is processed by the same launches.
 #pragma once
 
+#include <map>
 #include <vector>
 
 #include "dense.cuh"
@@ -24,6 +25,26 @@ struct MoveP {
   int nrows, ncols, lds, ldd, mode, accumulate;
 };
 void move_batched(const MoveP* dP, int batch, cudaStream_t s);
+
+// A fixed sequence of batched skinny products and block moves (one inverse or
+// forward apply for a given number of right-hand sides); descriptors stay on the
+// device so the sequence can be replayed as a CUDA graph.
+struct Plan1 {
+  struct Step {
+    bool move = false;
+    DevBuf<GemmP<double>> g;
+    DevBuf<MoveP> m;
+    DevBuf<double> part;
+    int batch = 0, maxM = 0, maxN = 0, ksplit = 1;
+    double alpha = 1.0, beta = 0.0;
+  };
+  std::vector<Step> steps;
+  bool df = false;  // operands stored as float pairs, products on the FP32 pipes
+  void gemm(const std::vector<GemmP<double>>& P, double alpha, double beta, cudaStream_t s);
+  void moves(const std::vector<MoveP>& mv, cudaStream_t s);
+  void run(cudaStream_t s) const;
+  int launches() const;
+};
 
 struct HSS1D {
   // forest: global box ids; box_constants.m rows LEVEL..END2 per box
@@ -53,8 +74,26 @@ struct HSS1D {
   std::vector<long long> oL, oR, oD, oE, oFT;
   std::vector<int> ktop;
   bool inverted = false;
-  // solve workspaces
-  DevBuf<double> v1, v2, v3;
+  // solve workspaces, staging (Ntot x 8) and cached plans / graphs per RHS count
+  DevBuf<double> v1, v2, v3, Xs, Ys, ir_y, ir_res, ir_dd;
+  std::map<int, Plan1> inv_plans, fwd_plans;
+  GraphCache g_inv, g_fwd;
+  bool use_graphs = true;
+  // HSS_PREC_DFLOAT: solve products in double-float arithmetic on float-pair copies
+  int precision = HSS_PREC_FP64;
+  DevBuf<double> Linv_df, Rinv_df, Dinv_df, FTinv_df, T_UP_df, TDNT_df, M_SELF_df, M_SIB_df;
+  void set_precision(int prec);
+  void make_df();
+  bool dfm() const { return precision == HSS_PREC_DFLOAT; }
+  void clear_plans() {
+    g_inv.clear();
+    g_fwd.clear();
+    inv_plans.clear();
+    fwd_plans.clear();
+  }
+  Plan1& inv_plan(int r);
+  Plan1& fwd_plan(int r);
+  void ensure_work();
   // ID problem shapes of the last compress: (m_out, m_in, n, k) per non-root box
   std::vector<int> census;
   // rank-predictor features per box (NFEAT floats, known before the box's ID)

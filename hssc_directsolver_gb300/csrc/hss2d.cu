@@ -625,34 +625,6 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
   return pl;
 }
 
-// Capture body() on the stream into a graph once per key, then replay it.
-template <typename F>
-static void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&& body) {
-  if (!enabled) {
-    body();
-    return;
-  }
-  auto it = gc.g.find(key);
-  if (it == gc.g.end()) {
-    cudaGraph_t graph = nullptr;
-    HSS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    try {
-      body();
-    } catch (...) {
-      cudaStreamEndCapture(s, &graph);
-      if (graph) cudaGraphDestroy(graph);
-      throw;
-    }
-    HSS_CUDA(cudaStreamEndCapture(s, &graph));
-    cudaGraphExec_t ex = nullptr;
-    cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
-    cudaGraphDestroy(graph);
-    HSS_REQUIRE(e == cudaSuccess, HSS_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-    it = gc.g.emplace(key, ex).first;
-  }
-  HSS_CUDA(cudaGraphLaunch(it->second, s));
-}
-
 template <typename R>
 void HSS2D::applyinv_stage(int r) {
   // vin (N x r, ld N) -> vout; the plan is built (and synchronised) before capture

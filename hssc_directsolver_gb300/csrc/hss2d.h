@@ -67,20 +67,6 @@ struct FwdPlan {
   std::vector<SolvePlan<double>> up, lam, eta;
 };
 
-// Instantiated CUDA graphs of fixed launch sequences, keyed by the number of
-// right-hand sides.
-struct GraphCache {
-  std::map<int, cudaGraphExec_t> g;
-  GraphCache() = default;
-  GraphCache(const GraphCache&) = delete;
-  GraphCache& operator=(const GraphCache&) = delete;
-  ~GraphCache() { clear(); }
-  void clear() {
-    for (auto& kv : g) cudaGraphExecDestroy(kv.second);
-    g.clear();
-  }
-};
-
 struct HSS2D {
   hss2d_params prm;
   Tree2D geo;

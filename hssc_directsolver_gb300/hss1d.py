@@ -63,6 +63,11 @@ class HSS1DMatrix:
                                          ip(out["J_DN"]), dp(out["T_UP"]), dp(out["T_DN"])))
         return out
 
+    def set_precision(self, precision: str):
+        """'fp64' or 'dfloat': arithmetic of the apply / inverse-apply products."""
+        code = {"fp64": L.HSS_PREC_FP64, "dfloat": L.HSS_PREC_DFLOAT}[precision]
+        L.check(L.lib().hss1d_set_precision(self._h, code))
+
     # --- learned ranks ----------------------------------------------------------
     def features(self):
         """(nboxes x 8 rank features, k/n of each box's plain ID) of the last compress."""

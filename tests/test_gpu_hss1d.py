@@ -197,3 +197,22 @@ def test_fsym_matches_oracle(gpu):
     assert np.linalg.norm(y - np.linalg.solve(A, q)) < 1e-8 * np.linalg.norm(yo)
     u = G1.HSS1D_apply_fsym(H, q)
     assert np.linalg.norm(u - O1.apply_nsym(Ho, q)) <= 1e-12 * np.linalg.norm(u)
+
+
+def test_dfloat_forest_solve(gpu):
+    """Double-float solve products on a forest: inverse and forward applies agree with FP64
+    to ~1e-12, and the refined solve reaches 1e-12."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(5, nmin=800, nmax=3000, seed=17)
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    G1.HSS1D_invert_nsym(H)
+    F = np.random.default_rng(2).standard_normal((sum(sizes), 11))
+    x64 = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    u64 = G1.HSS1D_apply_nsym(H, F)
+    H.set_precision("dfloat")
+    xdf = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    udf = G1.HSS1D_apply_nsym(H, F)
+    assert np.linalg.norm(xdf - x64) <= 1e-12 * np.linalg.norm(x64)
+    assert np.linalg.norm(udf - u64) <= 1e-13 * np.linalg.norm(u64)
+    x, rr, it = G1.HSS1D_solve(H, F[:, :3], 1e-12, 4)
+    assert rr <= 1e-12
