@@ -612,6 +612,13 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
   HSS_CATCH
 }
 
+int hss2d_phase_times(const hss2d_matrix* H, double* seconds) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && seconds, HSS_ERR_ARG, "NULL argument");
+  std::copy(H->impl->phase_s, H->impl->phase_s + 5, seconds);
+  HSS_CATCH
+}
+
 int hss2d_interp_ranks(const hss2d_matrix* H, int32_t* q_up, int32_t* q_dn) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

@@ -18,6 +18,7 @@
 #include "hss2d.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 
 namespace hss {
@@ -240,7 +241,11 @@ template struct SolvePlan<float>;
 // build_tree
 // ---------------------------------------------------------------------------
 void HSS2D::build_tree() {
+  using clk = std::chrono::steady_clock;
+  auto t0 = clk::now();
   build_tree_geometry(prm, geo);
+  auto t1 = clk::now();
+  phase_s[0] = std::chrono::duration<double>(t1 - t0).count();
   kdev = make_kernel_dev(prm.kp);
   const long long N = geo.N;
   const size_t npts = (size_t)N + geo.proxy_x.size();
@@ -262,7 +267,11 @@ void HSS2D::build_tree() {
   qlev.assign(geo.depth + 1, 0);
   qrank_up.assign(geo.depth + 1, {});
   qrank_dn.assign(geo.depth + 1, {});
+  auto t2 = clk::now();
+  phase_s[1] = std::chrono::duration<double>(t2 - t1).count();
   for (int lev = geo.depth; lev >= 1; --lev) compute_T(lev);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  phase_s[2] = std::chrono::duration<double>(clk::now() - t2).count();
   tree_built = true;
 }
 
@@ -326,6 +335,7 @@ void HSS2D::compute_T(int lev) {
 // ---------------------------------------------------------------------------
 void HSS2D::compress() {
   HSS_REQUIRE(tree_built, HSS_ERR_STATE, "hss2d_compress before hss2d_build_tree");
+  const auto tc0 = std::chrono::steady_clock::now();
   const int depth = geo.depth;
   std::vector<KgenP<double>> kg;
   {
@@ -360,6 +370,8 @@ void HSS2D::compress() {
     HSS_CUDA(cudaStreamSynchronize(stream));
   }
   if (dfm()) make_df_forward();
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  phase_s[3] = std::chrono::duration<double>(std::chrono::steady_clock::now() - tc0).count();
   compressed = true;
   g_fwd.clear();
   fwd_plans.clear();
@@ -521,9 +533,12 @@ void HSS2D::make_df_inverse() {
 
 void HSS2D::invert() {
   HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_invert before hss2d_compress");
+  const auto ti0 = std::chrono::steady_clock::now();
   if (prm.precision == HSS_PREC_MIXED) invert_impl<float>();
   else invert_impl<double>();
   if (dfm()) make_df_inverse();
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  phase_s[4] = std::chrono::duration<double>(std::chrono::steady_clock::now() - ti0).count();
   inverted = true;
   g_inv_d.clear();
   g_inv_f.clear();

@@ -94,6 +94,9 @@ struct HSS2D {
   // low-rank interpolation ('lowrank' INTERform): widest T.U per level (q(lev+1) of the
   // reference), the randomized ranks of T_up / T_dn per factor box of a level (empty on
   // dense levels)
+  // host wall seconds: tree geometry, point/index uploads, interpolation operators (GPU),
+  // compress, invert
+  double phase_s[5] = {};
   std::vector<int> qlev;
   std::vector<std::vector<int>> qrank_up, qrank_dn;
 

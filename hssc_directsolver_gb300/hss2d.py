@@ -111,6 +111,12 @@ class InfoTree:
         L.check(L.lib().hss2d_box_sizes(self._h, ip(n), ip(k), ip(p)))
         return n, k, p
 
+    def phase_times(self):
+        """Host wall seconds: tree geometry, uploads, interpolation operators, compress, invert."""
+        t = np.zeros(5)
+        L.check(L.lib().hss2d_phase_times(self._h, t.ctypes.data_as(L._DP)))
+        return t
+
     def interp_ranks(self):
         """(q_up, q_dn): rank of each box's low-rank T_up / T_dn, -1 where T is dense."""
         qu = np.zeros(self.nboxes, np.int32)

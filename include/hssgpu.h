@@ -216,6 +216,9 @@ int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t
                      double* T_up, double* T_dn);
 /* A_HSS(b).FI (n x n) and .E (k x k), FP64 copies; NULL ok */
 int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double* E);
+/* host wall seconds of the last build/compress/invert by phase (5 entries): tree geometry,
+ * point and index uploads, interpolation operators, compress, invert */
+int hss2d_phase_times(const hss2d_matrix* H, double* seconds);
 /* ranks of the low-rank interpolation operators T_up = T.U T.V^T and T_dn per box
  * (nboxes entries each; -1 where T is dense: the root, the two finest levels, k >= k_cut) */
 int hss2d_interp_ranks(const hss2d_matrix* H, int32_t* q_up, int32_t* q_dn);
