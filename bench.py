@@ -38,7 +38,7 @@ METRIC = "compress+invert s and solves/s at 1e-10 residual: mixed/batched vs pla
 
 # DRAM bytes (read + write) of the skinny-product kernels of one inverse apply at this
 # workload, from the ncu capture summarised in profiles/skinny_hss2d_n65536.md
-TRAFFIC_PER_APPLYINV = {}
+TRAFFIC_PER_APPLYINV = {"dfloat": 2.0057e9, "dfloat_inv": 2.0057e9, "fp64": 1.9471e9}
 WORKLOAD = "HSS2D 256x256 grid (Ng=8, 32x32 panels, N=65536), leaf 8x8, tol 1e-10, 4 RHS"
 
 
@@ -226,8 +226,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-curve batched HSS1D section")
     ap.add_argument("--curves", type=int, default=512)
-    ap.add_argument("--paths", default="fp64,mixed,dfloat",
-                    help="solve paths to measure (comma list of fp64, mixed, dfloat)")
+    ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv",
+                    help="solve paths to measure (comma list of fp64, mixed, dfloat, dfloat_inv)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -363,7 +363,8 @@ def main():
         "metric": METRIC, "value": 1e3 / r["solve_ms"] * world, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["solve_ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"mixed": "f32+f64", "dfloat": "f64 (products as f32 pairs)"}.get(best, "f64"),
+        "dtype": {"mixed": "f32+f64", "dfloat": "f64 (products as f32 pairs)",
+                  "dfloat_inv": "f64 (products and inversion as f32 pairs)"}.get(best, "f64"),
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nrhs": nrhs, "path": best, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (factors %.2f GB per solve)" % (r["solve_bytes"] / 1e9)},
@@ -378,7 +379,8 @@ def main():
                 "h2d_bytes_per_step": int(N * nrhs * 8), "d2h_bytes_per_step": int(N * nrhs * 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_PER_APPLYINV.get(best),
-                     "kernel": {"dfloat": "k_skinny_df", "mixed": "k_skinny<float>"}.get(best, "k_skinny<double>")
+                     "kernel": {"dfloat": "k_skinny_df", "dfloat_inv": "k_skinny_df",
+                                "mixed": "k_skinny<float>"}.get(best, "k_skinny<double>")
                                + " chain of one inverse apply",
                      "peak_source": peak_src,
                      "algorithmic_bytes": r["solve_bytes"]},

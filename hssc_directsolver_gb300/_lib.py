@@ -31,6 +31,7 @@ HSS_DL_L_2D = 1
 HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_PREC_DFLOAT = 2
+HSS_PREC_DFLOAT_INV = 3
 HSS_INTER_DENSE = 0
 HSS_INTER_LOWRANK = 1
 

@@ -447,7 +447,8 @@ int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p) {
   HSS_REQUIRE(p->transinv == 0 || p->transinv == 1, HSS_ERR_ARG, "transinv must be 0 or 1");
   HSS_REQUIRE(p->transinv == 0 || (p->kp.b_alpha == 0.0 && p->kp.c_alpha == 0.0), HSS_ERR_ARG,
               "translation-invariant mode needs an unmodulated kernel (b = c = 1)");
-  HSS_REQUIRE(p->precision == HSS_PREC_FP64 || p->precision == HSS_PREC_MIXED || p->precision == HSS_PREC_DFLOAT,
+  HSS_REQUIRE(p->precision == HSS_PREC_FP64 || p->precision == HSS_PREC_MIXED || p->precision == HSS_PREC_DFLOAT ||
+                  p->precision == HSS_PREC_DFLOAT_INV,
               HSS_ERR_ARG, "bad precision");
   require_device();
   *out = nullptr;

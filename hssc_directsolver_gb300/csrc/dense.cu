@@ -3,6 +3,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
 #include <cooperative_groups.h>
 
 namespace hss {
@@ -526,6 +527,112 @@ void split_df(const double* src, double* dst, long long n, cudaStream_t s) {
   check_launch("k_split_df");
 }
 
+// ---- double-float tiled GEMM ----------------------------------------------
+// C = alpha op(A) op(B) + beta C for FP64 operands in memory, computed in
+// double-float arithmetic (~2^-47 per product).  64x64 tile, K step 16, 256
+// threads, 4x4 outputs per thread as two f32x2 row pairs.  Tiles are split
+// into (hi, lo) floats with integer operations while staging; the B tile is
+// also kept negated for the exact-product error terms.  The accumulators are
+// renormalised after every K step and combined to FP64 with integer operations.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_gemm_df(const GemmP<double>* __restrict__ P, double alpha, double beta) {
+  const GemmP<double> p = P[blockIdx.z];
+  const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+  if (m0 >= p.M || n0 >= p.N) return;
+  __shared__ float Ah[16][64 + 1], Al[16][64 + 1];
+  __shared__ float Bh[16][64 + 1], Bhn[16][64 + 1], Bln[16][64 + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  f32x2 sh[2][4], sl[2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { sh[i][j] = 0ULL; sl[i][j] = 0ULL; }
+  for (int k0 = 0; k0 < p.K; k0 += 16) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + 256 * r;
+      int i, kk;
+      if (!TA) { i = e & 63; kk = e >> 6; } else { kk = e & 15; i = e >> 4; }
+      const int gi = m0 + i, gk = k0 + kk;
+      double v = 0.0;
+      if (gi < p.M && gk < p.K) v = TA ? p.A[gk + (size_t)gi * p.lda] : p.A[gi + (size_t)gk * p.lda];
+      float h, l;
+      split_d2f(v, h, l);
+      Ah[kk][i] = h;
+      Al[kk][i] = l;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + 256 * r;
+      int j, kk;
+      if (!TB) { kk = e & 15; j = e >> 4; } else { j = e & 63; kk = e >> 6; }
+      const int gj = n0 + j, gk = k0 + kk;
+      double v = 0.0;
+      if (gj < p.N && gk < p.K) v = TB ? p.B[gj + (size_t)gk * p.ldb] : p.B[gk + (size_t)gj * p.ldb];
+      float h, l;
+      split_d2f(v, h, l);
+      Bh[kk][j] = h;
+      Bhn[kk][j] = -h;
+      Bln[kk][j] = -l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < 16; ++kk) {
+      const f32x2 ah0 = x2_pack(Ah[kk][tx], Ah[kk][tx + 16]), al0 = x2_pack(Al[kk][tx], Al[kk][tx + 16]);
+      const f32x2 ah1 = x2_pack(Ah[kk][tx + 32], Ah[kk][tx + 48]), al1 = x2_pack(Al[kk][tx + 32], Al[kk][tx + 48]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = ty + 16 * j;
+        const float bh = Bh[kk][c], bhn = Bhn[kk][c], bln = Bln[kk][c];
+        const f32x2 bh2 = x2_pack(bh, bh), bhn2 = x2_pack(bhn, bhn), bln2 = x2_pack(bln, bln);
+        df_madd_x2(sh[0][j], sl[0][j], ah0, al0, bh2, bhn2, bln2);
+        df_madd_x2(sh[1][j], sl[1][j], ah1, al1, bh2, bhn2, bln2);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const f32x2 hi = x2_add(sh[i][j], sl[i][j]);
+        sl[i][j] = x2_sub(sl[i][j], x2_sub(hi, sh[i][j]));
+        sh[i][j] = hi;
+      }
+    __syncthreads();
+  }
+  float alh, all;
+  split_d2f(alpha, alh, all);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    float h[2], l[2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      x2_unpack(sh[i][j], h[0], h[1]);
+      x2_unpack(sl[i][j], l[0], l[1]);
+      const int gj = n0 + ty + 16 * j;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int gi = m0 + tx + 16 * (2 * i + u);
+        if (gi >= p.M || gj >= p.N) continue;
+        double* c = p.C + gi + (size_t)gj * p.ldc;
+        *c = df_epilogue(h[u], l[u], alh, all, beta, (beta == 0.0) ? 0.0 : *c);
+      }
+    }
+  }
+}
+
+void gemm_batched_df(const GemmP<double>* dP, int batch, int maxM, int maxN, bool tA, bool tB, double alpha,
+                     double beta, cudaStream_t s) {
+  if (batch <= 0 || maxM <= 0 || maxN <= 0) return;
+  HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "gemm batch too large");
+  dim3 grid(ceil_div(maxM, 64), ceil_div(maxN, 64), batch);
+  HSS_REQUIRE(grid.y <= 65535, HSS_ERR_ARG, "gemm N too large");
+  if (!tA && !tB) k_gemm_df<false, false><<<grid, 256, 0, s>>>(dP, alpha, beta);
+  else if (!tA && tB) k_gemm_df<false, true><<<grid, 256, 0, s>>>(dP, alpha, beta);
+  else if (tA && !tB) k_gemm_df<true, false><<<grid, 256, 0, s>>>(dP, alpha, beta);
+  else k_gemm_df<true, true><<<grid, 256, 0, s>>>(dP, alpha, beta);
+  check_launch("k_gemm_df");
+}
+
 template <typename R>
 int skinny_ksplit(int batch, int maxM, int maxK) {
   constexpr int ROWS = 32 * Vec16<R>::V;
@@ -836,6 +943,94 @@ __global__ void __launch_bounds__(256) k_gj_update(const InvP<R>* __restrict__ P
   }
 }
 
+// k_gj_update in double-float arithmetic for FP64 matrices: the rank-32 panel
+// product on the FP32 pipes (f32x2 row pairs), then added to the gathered base.
+__global__ void __launch_bounds__(256) k_gj_update_df(const InvP<double>* __restrict__ P, int j0) {
+  const InvP<double> p = P[blockIdx.z];
+  const int n = p.n;
+  if (j0 >= n) return;
+  if (*p.info != 0) return;
+  const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+  if (m0 >= n || n0 >= n) return;
+  const int jend = min(j0 + GJ_NB, n), nbk = jend - j0;
+  __shared__ float Ph[GJ_NB][64 + 1], Pl[GJ_NB][64 + 1];
+  __shared__ float Wh[GJ_NB][64 + 1], Whn[GJ_NB][64 + 1], Wln[GJ_NB][64 + 1];
+  __shared__ int rowq[64];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  double* A = p.A;
+  const size_t lda = p.lda;
+  const int np = p.aux[0];
+  if (tid < 64) {
+    const int gi = m0 + tid;
+    int q = -1;
+    for (int t = 0; t < np; ++t)
+      if (p.aux[1 + t] == gi) q = t;
+    rowq[tid] = q;
+  }
+  for (int e = tid; e < 64 * GJ_NB; e += 256) {
+    const int i = e & 63, r = e >> 6;
+    const int gi = m0 + i;
+    float h, l;
+    split_d2f((gi < n && r < nbk) ? A[gi + (size_t)(j0 + r) * lda] : 0.0, h, l);
+    Ph[r][i] = h;
+    Pl[r][i] = l;
+  }
+  for (int e = tid; e < 64 * GJ_NB; e += 256) {
+    const int r = e % GJ_NB, j = e / GJ_NB;
+    const int gj = n0 + j;
+    float h, l;
+    split_d2f((gj < n && r < nbk) ? p.W[r + (size_t)gj * 2 * GJ_NB] : 0.0, h, l);
+    Wh[r][j] = h;
+    Whn[r][j] = -h;
+    Wln[r][j] = -l;
+  }
+  __syncthreads();
+  f32x2 sh[2][4], sl[2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { sh[i][j] = 0ULL; sl[i][j] = 0ULL; }
+  for (int r = 0; r < nbk; ++r) {
+    const f32x2 ah0 = x2_pack(Ph[r][tx], Ph[r][tx + 16]), al0 = x2_pack(Pl[r][tx], Pl[r][tx + 16]);
+    const f32x2 ah1 = x2_pack(Ph[r][tx + 32], Ph[r][tx + 48]), al1 = x2_pack(Pl[r][tx + 32], Pl[r][tx + 48]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = ty + 16 * j;
+      const f32x2 bh2 = x2_pack(Wh[r][c], Wh[r][c]), bhn2 = x2_pack(Whn[r][c], Whn[r][c]),
+                  bln2 = x2_pack(Wln[r][c], Wln[r][c]);
+      df_madd_x2(sh[0][j], sl[0][j], ah0, al0, bh2, bhn2, bln2);
+      df_madd_x2(sh[1][j], sl[1][j], ah1, al1, bh2, bhn2, bln2);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float h[2], l[2];
+      const f32x2 hi = x2_add(sh[i][j], sl[i][j]);
+      const f32x2 lo = x2_sub(sl[i][j], x2_sub(hi, sh[i][j]));
+      x2_unpack(hi, h[0], h[1]);
+      x2_unpack(lo, l[0], l[1]);
+      const int gj = n0 + ty + 16 * j;
+      if (gj >= n || (gj >= j0 && gj < jend)) continue;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int li = tx + 16 * (2 * i + u), gi = m0 + li;
+        if (gi >= n) continue;
+        double* c = A + gi + (size_t)gj * lda;
+        double base;
+        if (gi >= j0 && gi < jend) base = 0.0;
+        else if (rowq[li] >= 0) base = p.W[GJ_NB + rowq[li] + (size_t)gj * 2 * GJ_NB];
+        else base = *c;
+        float bh, bl;
+        split_d2f(base, bh, bl);
+        float th = h[u], tl = l[u];
+        df_add(th, tl, bh, bl);
+        *c = df_to_double(th, tl);
+      }
+    }
+}
+
 // Column permutation undoing the row interchanges (applied in reverse).
 template <typename R>
 __global__ void k_gj_perm(const InvP<R>* __restrict__ P) {
@@ -891,7 +1086,7 @@ static int gj_cluster(int n, int batch, int& rows_per) {
 }
 
 template <typename R>
-void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s) {
+void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool df) {
   if (batch <= 0 || maxn <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "invert batch too large");
   int rows_per = 0;
@@ -921,6 +1116,13 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s) {
     k_gj_gather<R><<<dim3(gcols, batch), 256, 0, s>>>(dP, j0);
     check_launch("k_gj_gather");
     dim3 g(ceil_div(maxn, 64), ceil_div(maxn, 64), batch);
+    if constexpr (std::is_same<R, double>::value) {
+      if (df) {
+        k_gj_update_df<<<g, 256, 0, s>>>(dP, j0);
+        check_launch("k_gj_update_df");
+        continue;
+      }
+    }
     k_gj_update<R><<<g, 256, 0, s>>>(dP, j0);
     check_launch("k_gj_update");
   }
@@ -1820,7 +2022,7 @@ void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {
   template void gemm_skinny<R>(const GemmP<R>*, int, int, R, R, cudaStream_t);               \
   template void gemm_skinny_split<R>(const GemmP<R>*, int, int, int, R, R, int, R*, cudaStream_t); \
   template int skinny_ksplit<R>(int, int, int);                                              \
-  template void invert_batched<R>(const InvP<R>*, int, int, cudaStream_t);                   \
+  template void invert_batched<R>(const InvP<R>*, int, int, cudaStream_t, bool);             \
   template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t);
 HSS_INST(double)
 HSS_INST(float)

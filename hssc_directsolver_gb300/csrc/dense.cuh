@@ -28,6 +28,9 @@ struct GemmP {
 // 64x its FP64 rate, so this outruns native FP64 for matrix-vector products.
 void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
                           int ksplit, double* part, cudaStream_t s);
+// gemm_batched in double-float arithmetic (FP64 in and out, ~2^-47 per product)
+void gemm_batched_df(const GemmP<double>* dP, int batch, int maxM, int maxN, bool tA, bool tB, double alpha,
+                     double beta, cudaStream_t s);
 // K slices for gemm_skinny_split_df: enough CTAs for several waves on 152 SMs
 // (the double-float kernel does ~15x the arithmetic per byte of the FP64 one)
 int skinny_ksplit_df(int batch, int maxM, int maxK);
@@ -66,7 +69,8 @@ constexpr int GJ_NB = 32;
 constexpr int GJ_AUX = 4 * GJ_NB + 4;
 
 template <typename R>
-void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s);
+// df (FP64 only): the rank-32 trailing updates in double-float arithmetic
+void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool df = false);
 
 // Least squares X = A(:, 0:kf) \ A(:, kf:n) for tall full-rank problems, by
 // blocked Householder QR of the first kf columns applied to the remaining

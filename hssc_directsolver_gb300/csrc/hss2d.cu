@@ -195,12 +195,19 @@ static int grid_for(long long tot) { return std::max(1, std::min(ceil_div(tot, 2
 // ---------------------------------------------------------------------------
 template <typename R>
 static void run_gemm(std::vector<GemmP<R>>& P, bool tA, bool tB, R alpha, R beta, cudaStream_t s,
-                     DevBuf<GemmP<R>>& scratch) {
+                     DevBuf<GemmP<R>>& scratch, bool df = false) {
   if (P.empty()) return;
   int maxM = 0, maxN = 0;
   for (auto& p : P) { maxM = std::max(maxM, p.M); maxN = std::max(maxN, p.N); }
   scratch.alloc(P.size());
   HSS_CUDA(cudaMemcpyAsync(scratch.p, P.data(), P.size() * sizeof(GemmP<R>), cudaMemcpyHostToDevice, s));
+  if constexpr (std::is_same<R, double>::value) {
+    if (df) {
+      gemm_batched_df(scratch.p, (int)P.size(), maxM, maxN, tA, tB, alpha, beta, s);
+      HSS_CUDA(cudaStreamSynchronize(s));
+      return;
+    }
+  }
   gemm_batched<R>(scratch.p, (int)P.size(), maxM, maxN, tA, tB, alpha, beta, s);
   HSS_CUDA(cudaStreamSynchronize(s));
 }
@@ -431,7 +438,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{pTup + (size_t)i * k * nr, W1.p + (size_t)i * n * n + k, W1.p + (size_t)i * n * n, k, n,
                              nr, k, n, n});
-      run_gemm<R>(P, false, false, R(1), R(1), stream, gscratch);
+      run_gemm<R>(P, false, false, R(1), R(1), stream, gscratch, dfinv());
     }
     // (3) W2 = RFI[:, J]   (k x n, ld k)
     k_gather_cols<R><<<grid_for((long long)nb * k * n), 256, 0, stream>>>(nb, k, n, d.J.p, W1.p, (long long)n * n, n,
@@ -442,7 +449,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{W2.p + (size_t)i * k * n + (size_t)k * k, pTdn + (size_t)i * k * nr,
                              W2.p + (size_t)i * k * n, k, k, nr, k, k, k});
-      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch);
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfinv());
     }
     // (5) E = inv(EI)
     auto& Eb = d.fac<R>(1);
@@ -457,7 +464,7 @@ void HSS2D::invert_impl() {
     for (int i = 0; i < nb; ++i)
       P.push_back(GemmP<R>{Eb.p + (size_t)i * k * k, W1.p + (size_t)i * n * n, Ub.p + (size_t)i * k * n, k, n, k, k,
                            n, k});
-    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch);
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfinv());
     // (7) FIc = FI[:, J]
     k_gather_cols<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(nb, n, n, d.J.p, FI, (long long)n * n, n,
                                                                           W1.p, (long long)n * n, n);
@@ -467,7 +474,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{W1.p + (size_t)i * n * n + (size_t)k * n, pTdn + (size_t)i * k * nr,
                              W1.p + (size_t)i * n * n, n, k, nr, n, k, n});
-      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch);
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfinv());
     }
     auto& Gb = d.fac<R>(3);
     Gb.alloc((size_t)nb * n * k);
@@ -480,7 +487,7 @@ void HSS2D::invert_impl() {
     for (int i = 0; i < nb; ++i)
       P.push_back(GemmP<R>{Gb.p + (size_t)i * n * k, Eb.p + (size_t)i * k * k, GEb.p + (size_t)i * n * k, n, k, k, n,
                            k, n});
-    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch);
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfinv());
     check_launch("invert level");
     HSS_CUDA(cudaStreamSynchronize(stream));
   }
@@ -497,7 +504,7 @@ void HSS2D::invert_level(R* A, int n, int nb) {
                    Wf.p + (size_t)i * n * n, info.p + i, aux.p + (size_t)i * GJ_AUX};
   DevBuf<InvP<R>> dP(nb);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), nb * sizeof(InvP<R>), cudaMemcpyHostToDevice, stream));
-  invert_batched<R>(dP.p, nb, n, stream);
+  invert_batched<R>(dP.p, nb, n, stream, dfinv());
   std::vector<int> hi;
   download(hi, info.p, nb, stream);
   HSS_CUDA(cudaStreamSynchronize(stream));

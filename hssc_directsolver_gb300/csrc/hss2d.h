@@ -84,7 +84,8 @@ struct HSS2D {
   std::map<int, FwdPlan> fwd_plans;
   GraphCache g_inv_d, g_inv_f, g_fwd;
   bool use_graphs = true;
-  bool dfm() const { return prm.precision == HSS_PREC_DFLOAT; }
+  bool dfm() const { return prm.precision == HSS_PREC_DFLOAT || prm.precision == HSS_PREC_DFLOAT_INV; }
+  bool dfinv() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
   void make_df_forward();
   void make_df_inverse();
 

@@ -37,7 +37,8 @@ class HSS2DParams:
     INTERform: str = "dense"
     transinv: int = 0
     sym: int = 0
-    precision: str = "fp64"   # "fp64", "mixed" or "dfloat" (FP64 factors, paired-FP32 solve products)
+    precision: str = "fp64"   # "fp64", "mixed", "dfloat" (FP64 factors, paired-FP32 solve products)
+                              # or "dfloat_inv" (also the inversion in paired FP32)
     n_cut: int = 400
     Fopts: str = "dense"
     k_cut: int = 2500         # low-rank T only where k < k_cut
@@ -61,7 +62,8 @@ class HSS2DParams:
             raise ValueError("INTERform must be 'dense' or 'lowrank'")
         if self.Fopts != "dense":
             raise ValueError("Fopts 'dense' (HSS-D) is the implemented inverse storage")
-        prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED, "dfloat": L.HSS_PREC_DFLOAT}[self.precision]
+        prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED, "dfloat": L.HSS_PREC_DFLOAT,
+                "dfloat_inv": L.HSS_PREC_DFLOAT_INV}[self.precision]
         k = self.kernel
         k.h = self.h
         return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,

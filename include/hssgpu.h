@@ -43,6 +43,8 @@ extern "C" {
 #define HSS_PREC_MIXED 1 /* FP32 inverse factors, FP64 forward operator + refinement */
 #define HSS_PREC_DFLOAT 2 /* FP64 factors; solve products in paired FP32 arithmetic (~2^-48),
                              FP64 refinement against the forward operator */
+#define HSS_PREC_DFLOAT_INV 3 /* HSS_PREC_DFLOAT plus the inversion's trailing updates and
+                                 products in paired FP32 (factors ~5 bits short of FP64) */
 
 /* HSS2D interpolation-operator storage (params.INTERform) */
 #define HSS_INTER_DENSE 0
@@ -173,7 +175,7 @@ typedef struct hss2d_params {
   int32_t interform; /* HSS_INTER_DENSE or HSS_INTER_LOWRANK (the reference default) */
   int32_t transinv;  /* 0: NTI (per-box operators) */
   int32_t sym;       /* 0: nsym */
-  int32_t precision; /* HSS_PREC_FP64, HSS_PREC_MIXED or HSS_PREC_DFLOAT */
+  int32_t precision; /* HSS_PREC_FP64, HSS_PREC_MIXED, HSS_PREC_DFLOAT or HSS_PREC_DFLOAT_INV */
   int32_t pad_;
   double acc;
   hss_kernel_params kp;

@@ -229,3 +229,23 @@ def test_dfloat_solve_matches_fp64(gpu):
     a = G2.HSS2D_applyinv_nsym(ts["fp64"], ts["fp64"], f11)
     b = G2.HSS2D_applyinv_nsym(ts["dfloat"], ts["dfloat"], f11)
     assert np.linalg.norm(b - a) <= 1e-11 * np.linalg.norm(a)
+
+
+def test_dfloat_inv_solves_to_tolerance(gpu):
+    """HSS_PREC_DFLOAT_INV: the inversion's updates and products in paired FP32 too. The
+    factors are a few bits short of FP64, so the refined solve is the contract: relres
+    <= 1e-10 and the solution within 1e-9 of the FP64 path."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    t64 = G2.HSS2D_build_tree_nsym(params(8, "fp64"))
+    G2.HSS2D_compress_nsym(t64)
+    G2.HSS2D_invert_nsym(t64)
+    t = G2.HSS2D_build_tree_nsym(params(8, "dfloat_inv"))
+    G2.HSS2D_compress_nsym(t)
+    G2.HSS2D_invert_nsym(t)
+    f = np.random.default_rng(8).standard_normal((t.N, 4))
+    x64 = G2.HSS2D_applyinv_nsym(t64, t64, f)
+    x = G2.HSS2D_applyinv_nsym(t, t, f)
+    assert np.linalg.norm(x - x64) <= 1e-9 * np.linalg.norm(x64)
+    xs, rr, it = G2.HSS2D_solve(t, f, 1e-10, 5)
+    assert rr <= 1e-10 and it <= 2
+    assert np.linalg.norm(xs - x64) <= 1e-9 * np.linalg.norm(x64)
