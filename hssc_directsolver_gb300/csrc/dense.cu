@@ -272,6 +272,11 @@ __device__ __forceinline__ void split_d2f(double x, float& hi, float& lo) {
   const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
   const int e = (int)((u >> 52) & 0x7FF);
   const int ef = e - 896;
+  if ((u << 1) == 0ULL) {  // +-0 (padding and structural zeros stay off the FP64 pipe)
+    hi = __uint_as_float(sign);
+    lo = 0.f;
+    return;
+  }
   if (ef <= 0 || ef >= 255) {
     hi = __double2float_rn(x);
     lo = 0.f;
@@ -319,6 +324,7 @@ __device__ __forceinline__ void df_mul(float& ah, float& al, float bh, float bl)
 __device__ __forceinline__ double df_to_double(float hi, float lo) {
   const unsigned int hb = __float_as_uint(hi), lb = __float_as_uint(lo);
   const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
+  if ((hb << 1) == 0u && (lb << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)hb << 32));
   if (eh == 0 || eh == 255 || el == 255) return (double)hi + (double)lo;
   long long M = (long long)((1ULL << 52) | ((unsigned long long)(hb & 0x7FFFFFu) << 29));
   int e = eh + 896;  // double biased exponent of hi
@@ -400,8 +406,10 @@ __device__ __forceinline__ void df_madd_x2(f32x2& sh, f32x2& sl, f32x2 ah, f32x2
   sh = s;
 }
 
+constexpr int SKD_STAGES = 4;  // cp.async columns in flight per thread (<= 4 right-hand sides)
+
 template <int NR>
-__global__ void __launch_bounds__(256, (NR > 4) ? 3 : 5) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
+__global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
                                                    int ksplit, double* __restrict__ part, int mmax) {
   constexpr int V = 2;  // one 16-byte load = two (hi, lo) pairs
   constexpr int KC = (NR > 4) ? SK_KC / 2 : SK_KC;  // static shared memory under 48 KB
@@ -415,6 +423,7 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 5) k_skinny_df(const GemmP
   const int kb = blockIdx.y * kper, ke = min(p.K, kb + kper);
   __shared__ f32x2 Bh2[KC][NR], Bhn2[KC][NR], Bln2[KC][NR];
   __shared__ float2 red[8][NR][ROWS];
+  __shared__ __align__(16) float4 ring[(NR <= 4) ? SKD_STAGES : 1][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int r = row0 + lane * V;
   const bool vec_ok = ((p.lda % V) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
@@ -434,6 +443,37 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 5) k_skinny_df(const GemmP
       Bln2[kk][c] = x2_pack(-xl, -xl);
     }
     __syncthreads();
+    if constexpr (NR <= 4) {
+      if (vec_ok) {
+        // cp.async ring: each thread keeps its next SKD_STAGES columns' 16 bytes in
+        // flight into its own shared-memory slots (it reads only what it copied, so
+        // the per-thread group wait is the only synchronisation needed)
+        const int niter = (w < kn) ? (kn - w + 7) / 8 : 0;
+        const int nv = (r + V <= p.M) ? 16 : (r < p.M ? 8 : 0);
+        auto issue = [&](int it) {
+          const int kk = w + 8 * it;
+          const bool live = it < niter;
+          const float2* src = live ? A + (size_t)(kc + kk) * p.lda + (nv ? r : 0) : A;
+          const unsigned dst = (unsigned)__cvta_generic_to_shared(&ring[it % SKD_STAGES][threadIdx.x]);
+          const int bytes = live ? nv : 0;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes));
+          asm volatile("cp.async.commit_group;\n" ::);
+        };
+#pragma unroll
+        for (int it = 0; it < SKD_STAGES; ++it) issue(it);
+        for (int it = 0; it < niter; ++it) {
+          asm volatile("cp.async.wait_group %0;\n" ::"n"(SKD_STAGES - 1));
+          const float4 cur = ring[it % SKD_STAGES][threadIdx.x];
+          const int kk = w + 8 * it;
+          const f32x2 ah = x2_pack(cur.x, cur.z), al = x2_pack(cur.y, cur.w);
+#pragma unroll
+          for (int c = 0; c < NR; ++c) df_madd_x2(sh[c], sl[c], ah, al, Bh2[kk][c], Bhn2[kk][c], Bln2[kk][c]);
+          issue(it + SKD_STAGES);
+        }
+        asm volatile("cp.async.wait_all;\n" ::);
+        continue;
+      }
+    }
     // software-pipelined: the next column's 16 bytes are in flight during this column's math
     auto load = [&](int kk) -> float4 {
       const float2* col = A + (size_t)(kc + kk) * p.lda;
