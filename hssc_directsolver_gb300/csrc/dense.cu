@@ -1201,6 +1201,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __rest
   __shared__ R s_tau[QR_NB];
   __shared__ R sh[32];
   __shared__ R s_gram[QR_NB][QR_NB + 1];
+  __shared__ R s_tf[QR_NB][QR_NB + 1];
   const int m = p.m, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
   const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
   const int mm = m - j0;
@@ -1318,27 +1319,29 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __rest
       else v = *cl.map_shared_rank(&pan[(gi - j0 - o * rows_per) + b * rows_per], o);
       A[gi + (size_t)(j0 + b) * lda] = v;
     }
-    if (tid == 0) {
-      R* Tf = p.Tf;
-      // cluster totals of the Gram entries, stored in place (each entry reads all
-      // ranks, its own included, before it is overwritten)
-      for (int b = 0; b < nbk; ++b)
-        for (int a = 0; a < b; ++a) {
-          R t = R(0);
-          for (int q = 0; q < C; ++q) t += cl.map_shared_rank(&s_gram[0][0], q)[a * (QR_NB + 1) + b];
-          s_gram[a][b] = t;
-        }
-      for (int b = 0; b < QR_NB; ++b)
-        for (int a = 0; a < QR_NB; ++a) Tf[a + b * QR_NB] = R(0);
-      for (int b = 0; b < nbk; ++b) {
-        Tf[b + b * QR_NB] = s_tau[b];
-        for (int a = 0; a < b; ++a) {
-          R t = R(0);
-          for (int c = a; c < b; ++c) t += Tf[a + c * QR_NB] * s_gram[c][b];
-          Tf[a + b * QR_NB] = -s_tau[b] * t;
-        }
-      }
+    // cluster totals of the Gram entries, stored in place: each entry is read (all
+    // ranks, its own included) and then overwritten by the one thread that owns it
+    for (int e = tid; e < nbk * nbk; e += nt) {
+      const int a = e % nbk, b = e / nbk;
+      if (a >= b) continue;
+      R t = R(0);
+      for (int q = 0; q < C; ++q) t += cl.map_shared_rank(&s_gram[0][0], q)[a * (QR_NB + 1) + b];
+      s_gram[a][b] = t;
     }
+    for (int e = tid; e < QR_NB * QR_NB; e += nt) s_tf[e % QR_NB][e / QR_NB] = R(0);
+    __syncthreads();
+    // compact-WY factor, one column at a time (the column's entries in parallel)
+    for (int b = 0; b < nbk; ++b) {
+      if (tid == 0) s_tf[b][b] = s_tau[b];
+      if (tid < b) {
+        const int a = tid;
+        R t = R(0);
+        for (int c = a; c < b; ++c) t += s_tf[a][c] * s_gram[c][b];
+        s_tf[a][b] = -s_tau[b] * t;
+      }
+      __syncthreads();
+    }
+    for (int e = tid; e < QR_NB * QR_NB; e += nt) p.Tf[e] = s_tf[e % QR_NB][e / QR_NB];
   }
   cl.sync();  // no CTA leaves while another may still read its shared memory
 }
