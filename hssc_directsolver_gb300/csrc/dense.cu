@@ -1419,6 +1419,129 @@ __global__ void __launch_bounds__(256) k_qr_update(const QrP<R>* __restrict__ P,
   }
 }
 
+// k_qr_update in double-float arithmetic for FP64 problems: W = V^T A,
+// W2 = Tf^T W and A -= V W2 for one 32-column tile, with every product on the
+// FP32 pipes (rows of V are the broadcast operand, column pairs of A / W2 the
+// f32x2 operand).  32-row chunks keep the static shared memory under 48 KB.
+__global__ void __launch_bounds__(256) k_qr_update_df(const QrP<double>* __restrict__ P, int j0) {
+  const QrP<double> p = P[blockIdx.y];
+  if (j0 >= p.kf) return;
+  const int m = p.m, n = p.n, tid = threadIdx.x;
+  const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
+  const int c0 = jend + blockIdx.x * 32;
+  if (c0 >= n) return;
+  const int nc = min(32, n - c0);
+  double* A = p.A;
+  const size_t lda = p.lda;
+  const double* V = p.V;
+  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
+  __shared__ float Xh[32][33], Xl[32][33];  // A chunk in phase 1, W2 in phase 3
+  __shared__ float Wh[32][33], Wl[32][33];
+  const int lo5 = tid & 31, hi3 = tid >> 5;
+  auto stage_v = [&](int r0) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, jj = e >> 5;
+      const int gi = r0 + i;
+      float h, l;
+      split_d2f((gi < m && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
+      Vh[i][jj] = h;
+      Vhn[i][jj] = -h;
+      Vln[i][jj] = -l;
+    }
+  };
+  // phase 1: thread owns W[jj = lo5][cc in {hi3, hi3+8} and {hi3+16, hi3+24}]
+  f32x2 sh[2] = {0ULL, 0ULL}, sl[2] = {0ULL, 0ULL};
+  for (int r0 = j0; r0 < m; r0 += 32) {
+    stage_v(r0);
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, cc = e >> 5;
+      const int gi = r0 + i;
+      float h, l;
+      split_d2f((gi < m && cc < nc) ? A[gi + (size_t)(c0 + cc) * lda] : 0.0, h, l);
+      Xh[i][cc] = h;
+      Xl[i][cc] = l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < 32; ++i) {
+      const float vh = Vh[i][lo5], vhn = Vhn[i][lo5], vln = Vln[i][lo5];
+      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int ca = hi3 + 16 * u, cb = ca + 8;
+        df_madd_x2(sh[u], sl[u], x2_pack(Xh[i][ca], Xh[i][cb]), x2_pack(Xl[i][ca], Xl[i][cb]), b2, bn2, bl2);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {  // renormalise once per chunk
+      const f32x2 h = x2_add(sh[u], sl[u]);
+      sl[u] = x2_sub(sl[u], x2_sub(h, sh[u]));
+      sh[u] = h;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    float h0, h1, l0, l1;
+    x2_unpack(sh[u], h0, h1);
+    x2_unpack(sl[u], l0, l1);
+    const int ca = hi3 + 16 * u, cb = ca + 8;
+    Wh[lo5][ca] = h0; Wl[lo5][ca] = l0;
+    Wh[lo5][cb] = h1; Wl[lo5][cb] = l1;
+  }
+  __syncthreads();
+  // phase 2: W2[jj][cc] = sum_{a <= jj} Tf[a, jj] W[a][cc]  (Tf upper triangular)
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int cc = hi3 + 8 * q;
+    float th = 0.f, tl = 0.f;
+    if (lo5 < nbk)
+      for (int a = 0; a <= lo5; ++a) {
+        float fh, fl;
+        split_d2f(p.Tf[a + lo5 * QR_NB], fh, fl);
+        df_madd(th, tl, Wh[a][cc], Wl[a][cc], fh, fl);
+      }
+    Xh[lo5][cc] = th;  // W2 (the A chunk is no longer needed)
+    Xl[lo5][cc] = tl;
+  }
+  __syncthreads();
+  // phase 3: A -= V W2; thread owns rows i = lo5 of the chunk, columns as in phase 1
+  for (int r0 = j0; r0 < m; r0 += 32) {
+    stage_v(r0);
+    __syncthreads();
+    f32x2 ah[2] = {0ULL, 0ULL}, al[2] = {0ULL, 0ULL};
+    for (int jj = 0; jj < nbk; ++jj) {
+      const float vh = Vh[lo5][jj], vhn = Vhn[lo5][jj], vln = Vln[lo5][jj];
+      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int ca = hi3 + 16 * u, cb = ca + 8;
+        df_madd_x2(ah[u], al[u], x2_pack(Xh[jj][ca], Xh[jj][cb]), x2_pack(Xl[jj][ca], Xl[jj][cb]), b2, bn2, bl2);
+      }
+    }
+    const int gi = r0 + lo5;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const f32x2 h = x2_add(ah[u], al[u]);
+      const f32x2 l = x2_sub(al[u], x2_sub(h, ah[u]));
+      float h2[2], l2[2];
+      x2_unpack(h, h2[0], h2[1]);
+      x2_unpack(l, l2[0], l2[1]);
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int cc = hi3 + 16 * u + 8 * v;
+        if (gi >= m || cc >= nc) continue;
+        double* c = A + gi + (size_t)(c0 + cc) * lda;
+        float xh, xl;
+        split_d2f(*c, xh, xl);
+        df_add(xh, xl, -h2[v], -l2[v]);
+        *c = df_to_double(xh, xl);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One back-substitution block step: solve R[b0:b1,b0:b1] X[b0:b1, tile] =
 // C[b0:b1, tile] (C = A[0:kf, kf:n], already updated by the blocks below) and
 // update C[rows of this CTA's chunk of 0:b0, tile] -= R[.., b0:b1] X.  Every
@@ -1481,7 +1604,7 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
 }
 
 template <typename R>
-void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s) {
+void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df) {
   if (batch <= 0 || maxkf <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "lstsq batch too large");
   int C = 1;
@@ -1513,6 +1636,13 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
     const int jend = std::min(j0 + QR_NB, maxkf);
     const int ncols = maxn - jend;
     if (ncols > 0) {
+      if constexpr (std::is_same<R, double>::value) {
+        if (df) {
+          k_qr_update_df<<<dim3(ceil_div(ncols, 32), batch), 256, 0, s>>>(dP, j0);
+          check_launch("k_qr_update_df");
+          continue;
+        }
+      }
       k_qr_update<R><<<dim3(ceil_div(ncols, 32), batch), 256, 0, s>>>(dP, j0);
       check_launch("k_qr_update");
     }
@@ -2066,7 +2196,7 @@ void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {
   template void gemm_skinny_split<R>(const GemmP<R>*, int, int, int, R, R, int, R*, cudaStream_t); \
   template int skinny_ksplit<R>(int, int, int);                                              \
   template void invert_batched<R>(const InvP<R>*, int, int, cudaStream_t, bool);             \
-  template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t);
+  template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t, bool);
 HSS_INST(double)
 HSS_INST(float)
 #undef HSS_INST

@@ -89,7 +89,8 @@ struct QrP {
 constexpr int QR_NB = 32;
 
 template <typename R>
-void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s);
+// df (FP64 only): the compact-WY trailing updates in double-float arithmetic
+void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df = false);
 
 // Interpolative decomposition of one m x n block per problem (the pivoted-QR
 // rank detection of the reference ID, with its randomized posterior check).

@@ -249,3 +249,9 @@ def test_dfloat_inv_solves_to_tolerance(gpu):
     xs, rr, it = G2.HSS2D_solve(t, f, 1e-10, 5)
     assert rr <= 1e-10 and it <= 2
     assert np.linalg.norm(xs - x64) <= 1e-9 * np.linalg.norm(x64)
+    # the interpolation operators come from a double-float least squares too: the
+    # solution still solves the kernel system to the compression tolerance
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / 64, c=OK.Modulation(0.5, 0, 0, 20.0))
+    oprm = O2.HSS2DParams(Ng=8, npan=8, kp=kp)
+    r = O2.kernel_matvec(oprm, xs) - f
+    assert np.linalg.norm(r) / np.linalg.norm(f) < 1e-9
