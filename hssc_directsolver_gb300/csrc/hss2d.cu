@@ -317,7 +317,7 @@ void HSS2D::compute_T(int lev) {
     }
     DevBuf<QrP<double>> dqp(batch);
     HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
-    lstsq_batched<double>(dqp.p, batch, p, n, k, stream, dfinv());
+    lstsq_batched<double>(dqp.p, batch, p, n, k, stream, dftree());
     HSS_CUDA(cudaStreamSynchronize(stream));
     qlev[lev] = nr;  // a dense T.U is k x nr
   }

@@ -84,8 +84,16 @@ struct HSS2D {
   std::map<int, FwdPlan> fwd_plans;
   GraphCache g_inv_d, g_inv_f, g_fwd;
   bool use_graphs = true;
-  bool dfm() const { return prm.precision == HSS_PREC_DFLOAT || prm.precision == HSS_PREC_DFLOAT_INV; }
+  // double-float solve products (the inverse apply when its factors are FP64, the
+  // forward apply of the refinement always in these modes)
+  bool dfm() const {
+    return prm.precision == HSS_PREC_DFLOAT || prm.precision == HSS_PREC_DFLOAT_INV ||
+           prm.precision == HSS_PREC_MIXED;
+  }
+  // double-float inversion updates and products
   bool dfinv() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
+  // double-float trailing updates in the interpolation least squares
+  bool dftree() const { return prm.precision == HSS_PREC_DFLOAT_INV || prm.precision == HSS_PREC_MIXED; }
   void make_df_forward();
   void make_df_inverse();
 

@@ -277,7 +277,7 @@ void HSS2D::lowrank_T(int lev, const double* A, DevBuf<double>& Vw, DevBuf<doubl
   if (!qp.empty()) {
     DevBuf<QrP<double>> dq;
     dq.upload(qp, st);
-    lstsq_batched<double>(dq.p, (int)qp.size(), p, k + qmax, k, st, dfinv());
+    lstsq_batched<double>(dq.p, (int)qp.size(), p, k + qmax, k, st, dftree());
     HSS_CUDA(cudaStreamSynchronize(st));
   }
   run_gemm_list(gt, false, true, 1.0, 0.0, st);
