@@ -280,7 +280,7 @@ def main():
         sp = C.c_void_p(stream.cuda_stream)
 
         def solve():
-            L.check(L.lib().hss2d_solve_device(tree._h, L.ptr(dF), L.ptr(dX), dF.shape[0], 1e-10, 4,
+            L.check(L.lib().hss2d_solve_device(tree._h, L.ptr(dF), L.ptr(dX), dF.shape[0], 1e-10, 10,
                                                C.byref(rr), C.byref(it), sp))
 
         for _ in range(args.warmup):
@@ -322,12 +322,12 @@ def main():
         rr2 = C.c_double()
         it2 = C.c_int32()
         for _ in range(2):
-            L.check(L.lib().hss2d_solve(tree._h, L.ptr(Fh), L.ptr(Xh), Fh.shape[1], 1e-10, 4, C.byref(rr2),
+            L.check(L.lib().hss2d_solve(tree._h, L.ptr(Fh), L.ptr(Xh), Fh.shape[1], 1e-10, 10, C.byref(rr2),
                                         C.byref(it2)))
         barrier()
         te0 = time.perf_counter()
         for _ in range(args.steps):
-            L.check(L.lib().hss2d_solve(tree._h, L.ptr(Fh), L.ptr(Xh), Fh.shape[1], 1e-10, 4, C.byref(rr2),
+            L.check(L.lib().hss2d_solve(tree._h, L.ptr(Fh), L.ptr(Xh), Fh.shape[1], 1e-10, 10, C.byref(rr2),
                                         C.byref(it2)))
         barrier()
         e2e_s = max_over_ranks((time.perf_counter() - te0) / args.steps)

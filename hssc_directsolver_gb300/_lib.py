@@ -111,6 +111,7 @@ SIGNATURES = {
     "hss2d_export_inverse": (C.c_int, [_P, C.c_int32, _DP, _DP]),
     "hss2d_interp_ranks": (C.c_int, [_P, _I32P, _I32P]),
     "hss2d_phase_times": (C.c_int, [_P, _DP]),
+    "hss2d_bicgstab": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_double, C.c_int32, _DP, _I32P]),
     "hss2d_solve_bytes": (C.c_int, [_P, _I64P]),
     "hss2d_solve_launches": (C.c_int, [_P, C.c_int32, _I32P]),
     "hss2d_destroy": (C.c_int, [_P]),

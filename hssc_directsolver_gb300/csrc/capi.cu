@@ -613,6 +613,23 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
   HSS_CATCH
 }
 
+int hss2d_bicgstab(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x, int32_t nrhs, double tol,
+                   int32_t maxit, double* relres, int32_t* iters) {
+  HSS_TRY
+  HSS_REQUIRE(A && A->impl && f && x, HSS_ERR_ARG, "NULL argument");
+  HSS_REQUIRE(nrhs >= 1, HSS_ERR_ARG, "nrhs must be >= 1");
+  HSS2D* h = A->impl;
+  const size_t cnt = (size_t)h->geo.N * nrhs;
+  DevBuf<double> df(cnt), dx(cnt);
+  HSS_CUDA(cudaMemcpyAsync(df.p, f, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int it = 0;
+  bicgstab_device(*h, M ? M->impl : nullptr, df.p, dx.p, nrhs, tol, maxit, relres, &it);
+  HSS_CUDA(cudaMemcpyAsync(x, dx.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaStreamSynchronize(h->stream));
+  if (iters) *iters = it;
+  HSS_CATCH
+}
+
 int hss2d_phase_times(const hss2d_matrix* H, double* seconds) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl && seconds, HSS_ERR_ARG, "NULL argument");

@@ -165,6 +165,10 @@ struct HSS2D {
   }
 };
 
+// x = A^-1 f by BiCGSTAB preconditioned with M^-1 (krylov.cu)
+void bicgstab_device(HSS2D& A, HSS2D* M, const double* f, double* x, int nrhs, double tol, int maxit,
+                     double* relres, int* iters);
+
 }  // namespace hss
 
 // opaque C handle

@@ -221,3 +221,17 @@ def HSS2D_solve(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 5):
     L.check(L.lib().hss2d_solve(INFO_TREE._h, L.ptr(F2), L.ptr(Xs), F2.shape[1], tol, maxit, C.byref(rr),
                                 C.byref(it)))
     return (Xs[:, 0] if vec else Xs), rr.value, it.value
+
+
+def HSS2D_bicgstab(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 200, PRECOND: InfoTree | None = None):
+    """[x, flag, relres, iter] = bicgstab(Mapp, F, tol, maxit, Iapp) of the reference's
+    iterative solution (HSS2D/Test/Test_HSS2D_InverseCompression.m:201-228): Mapp is the
+    forward apply of INFO_TREE's compressed operator, Iapp the inverse apply of PRECOND
+    (an inverted tree, e.g. the translation-invariant one).  Returns (x, relres, iters)."""
+    F2, vec = _vec(INFO_TREE, F)
+    Xs = np.zeros_like(F2, order="F")
+    rr = C.c_double()
+    it = C.c_int32()
+    L.check(L.lib().hss2d_bicgstab(INFO_TREE._h, PRECOND._h if PRECOND is not None else None, L.ptr(F2), L.ptr(Xs),
+                                   F2.shape[1], float(tol), int(maxit), C.byref(rr), C.byref(it)))
+    return (Xs[:, 0] if vec else Xs), rr.value, it.value

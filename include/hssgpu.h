@@ -212,6 +212,13 @@ int hss2d_solve(hss2d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
 int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
 /* tree sizes: depth, box count, N */
+/* [x,flag,relres,iter] = bicgstab(Mapp, f, tol, maxit, Iapp) of the reference's iterative
+ * solution (HSS2D/Test/Test_HSS2D_InverseCompression.m:201-228): Mapp = forward apply of
+ * the compressed operator A, Iapp = inverse apply of the inverted handle M (e.g. a
+ * translation-invariant tree of the constant-coefficient kernel); M may be NULL.
+ * f, x host N x nrhs column-major; relres = max column true residual; iters = iterations. */
+int hss2d_bicgstab(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x, int32_t nrhs,
+                   double tol, int32_t maxit, double* relres, int32_t* iters);
 int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N);
 /* per-box sizes: n (|I_src|), k (|I_sk|), proxy count; arrays of nboxes (NULL ok) */
 int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* nproxy);
