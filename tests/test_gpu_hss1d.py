@@ -216,3 +216,17 @@ def test_dfloat_forest_solve(gpu):
     assert np.linalg.norm(udf - u64) <= 1e-13 * np.linalg.norm(u64)
     x, rr, it = G1.HSS1D_solve(H, F[:, :3], 1e-12, 4)
     assert rr <= 1e-12
+
+
+def test_fsym_transforminv_and_precision_errors(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, _lib as L
+    X = geometry.star_curve(1500)
+    H = G1.HSS1D_compress_fsym("green", X, 64, 1e-10, GK.Kernel("SL_L_2D", 0.01))
+    G1.HSS1D_invert_fsym(H)
+    K = G1.HSS1D_transforminv_nsym(H)
+    f = np.random.default_rng(1).standard_normal((1500, 2))
+    x = G1.HSS1D_applyinv_fsym(H, None, None, f)
+    assert np.linalg.norm(G1.HSS1D_apply_nsym(K, f) - x) <= 1e-10 * np.linalg.norm(x)
+    with pytest.raises(L.HSSError) as e:
+        L.check(L.lib().hss1d_set_precision(H._h, L.HSS_PREC_MIXED))
+    assert e.value.code == L.HSS_ERR_ARG

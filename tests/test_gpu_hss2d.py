@@ -277,3 +277,41 @@ def test_bicgstab_with_translation_invariant_preconditioner(gpu):
     # with the operator's own inverse as preconditioner it is a one-step method
     x1, rr1, it1 = G2.HSS2D_bicgstab(A, f, 1e-10, 10, PRECOND=A)
     assert rr1 <= 1e-10 and it1 <= 2
+
+
+def test_translation_invariant_lowrank_dfloat(gpu):
+    """Mode combinations: translation-invariant tree (one factor set per level) with the
+    low-rank interpolation operators and double-float solves agrees with the same tree in
+    FP64 dense form to the compression tolerance."""
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    out = {}
+    for form, prec in (("dense", "fp64"), ("lowrank", "dfloat")):
+        prm = G2.HSS2DParams(Ng=8, npan=8, kernel=GK.Kernel("SL_L_2D", 2.0 / 64), transinv=1, INTERform=form,
+                             precision=prec)
+        t = G2.HSS2D_build_tree_nsym(prm)
+        G2.HSS2D_compress_nsym(t)
+        G2.HSS2D_invert_nsym(t)
+        f = np.random.default_rng(5).standard_normal((t.N, 2))
+        x, rr, it = G2.HSS2D_solve(t, f, 1e-10, 4)
+        assert rr <= 1e-10
+        out[form] = x
+        if form == "lowrank":
+            qu, qd = t.interp_ranks()
+            assert (qu > 0).any()
+    assert np.linalg.norm(out["lowrank"] - out["dense"]) <= 1e-8 * np.linalg.norm(out["dense"])
+
+
+def test_krylov_argument_errors(gpu):
+    from hssc_directsolver_gb300 import hss2d as G2, _lib as L
+    A = G2.HSS2D_build_tree_nsym(params(4))
+    G2.HSS2D_compress_nsym(A)
+    M = G2.HSS2D_build_tree_nsym(params(8))
+    G2.HSS2D_compress_nsym(M)
+    f = np.ones((A.N, 1))
+    with pytest.raises(L.HSSError) as e:
+        G2.HSS2D_bicgstab(A, f, 1e-10, 10, PRECOND=M)   # M not inverted
+    assert e.value.code == L.HSS_ERR_STATE
+    G2.HSS2D_invert_nsym(M)
+    with pytest.raises(L.HSSError) as e:
+        G2.HSS2D_bicgstab(A, f, 1e-10, 10, PRECOND=M)   # sizes differ
+    assert e.value.code == L.HSS_ERR_ARG
