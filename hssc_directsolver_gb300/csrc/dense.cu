@@ -1118,11 +1118,24 @@ static int gj_cluster(int n, int batch, int& rows_per) {
     while (C < 8 && (n + C - 1) / C > 256) C *= 2;
   }
   rows_per = (n + C - 1) / C;
-  while ((size_t)rows_per * GJ_NB * sizeof(R) > 200 * 1024 && C < 8) {
+  // blocks above 6400 rows take the non-portable 16-CTA cluster (n up to 12800)
+  while ((size_t)rows_per * GJ_NB * sizeof(R) > 200 * 1024 && C < 16) {
     C *= 2;
     rows_per = (n + C - 1) / C;
   }
   return C;
+}
+
+// A cluster launch of C CTAs must fit on the GPU at once: 16-CTA clusters need the
+// non-portable opt-in and one GPC with 16 SMs of free shared memory.  Returns an error
+// status instead of launching what cannot be co-scheduled.
+template <typename K>
+static void require_cluster_fits(K kernel, cudaLaunchConfig_t& cfg, int C) {
+  if (C <= 8) return;
+  int nclusters = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, kernel, &cfg);
+  HSS_REQUIRE(e == cudaSuccess && nclusters > 0, HSS_ERR_ARG,
+              "block too large: a 16-CTA cluster panel does not fit on this GPU");
 }
 
 template <typename R>
@@ -1132,10 +1145,11 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool
   int rows_per = 0;
   const int C = gj_cluster<R>(maxn, batch, rows_per);
   const size_t smem = (size_t)rows_per * GJ_NB * sizeof(R);
-  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "block too large for the cluster panel (n > 6400)");
+  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "block too large for the cluster panel (n > 12800)");
   static bool attr_set = false;
   if (!attr_set) {
     HSS_CUDA(cudaFuncSetAttribute(k_gj_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    HSS_CUDA(cudaFuncSetAttribute(k_gj_panel_cl<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     attr_set = true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -1150,6 +1164,7 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  require_cluster_fits(k_gj_panel_cl<R>, cfg, C);
   const int gcols = std::max(1, std::min(ceil_div(maxn, 256), 64));
   for (int j0 = 0; j0 < maxn; j0 += GJ_NB) {
     HSS_CUDA(cudaLaunchKernelEx(&cfg, k_gj_panel_cl<R>, dP, j0, rows_per));
@@ -1610,13 +1625,14 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   int C = 1;
   if (batch < 152 && maxm > 256)
     while (C < 8 && (maxm + C - 1) / C > 256) C *= 2;
-  while ((size_t)((maxm + C - 1) / C) * QR_NB * sizeof(R) > 200 * 1024 && C < 8) C *= 2;
+  while ((size_t)((maxm + C - 1) / C) * QR_NB * sizeof(R) > 200 * 1024 && C < 16) C *= 2;
   const int cap = (maxm + C - 1) / C;
   const size_t smem = (size_t)cap * QR_NB * sizeof(R);
-  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "least-squares panel too tall for the cluster (m > 6400)");
+  HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "least-squares panel too tall for the cluster (m > 12800)");
   static bool attr_set = false;
   if (!attr_set) {
     HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     attr_set = true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -1631,6 +1647,7 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  require_cluster_fits(k_qr_panel_cl<R>, cfg, C);
   for (int j0 = 0; j0 < maxkf; j0 += QR_NB) {
     HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl<R>, dP, j0, cap));
     const int jend = std::min(j0 + QR_NB, maxkf);
