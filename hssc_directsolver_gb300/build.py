@@ -53,7 +53,7 @@ def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", OUT + ".tmp", *objs, "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", OUT + ".tmp", *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -4,6 +4,9 @@
 
 #include <cuda_runtime.h>
 #include <map>
+#include <atomic>
+#include <exception>
+#include <thread>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -162,6 +165,39 @@ inline void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&&
     it = gc.g.emplace(key, ex).first;
   }
   HSS_CUDA(cudaGraphLaunch(it->second, s));
+}
+
+// Host-side parallel loop over [0, n): chunks handed out dynamically to up to
+// hardware_concurrency() threads; the first exception of any chunk is rethrown.
+template <typename F>
+inline void parallel_for(int n, F&& f, int min_per_thread = 64) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::max(1, std::min(hw, n / std::max(1, min_per_thread)));
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next(0);
+  std::exception_ptr err = nullptr;
+  std::atomic<bool> failed(false);
+  const int chunk = std::max(1, n / (nt * 8));
+  auto work = [&] {
+    try {
+      for (;;) {
+        const int i0 = next.fetch_add(chunk);
+        if (i0 >= n || failed.load()) break;
+        const int i1 = std::min(n, i0 + chunk);
+        for (int i = i0; i < i1; ++i) f(i);
+      }
+    } catch (...) {
+      if (!failed.exchange(true)) err = std::current_exception();
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+  if (err) std::rethrow_exception(err);
 }
 
 }  // namespace hss

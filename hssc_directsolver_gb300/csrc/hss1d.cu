@@ -252,8 +252,9 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
   maxlev = *std::max_element(level.begin(), level.end());
   // ---- neighbour lists (:376-412), boxes in increasing global id (parents first)
   std::vector<std::vector<int>> nei(nboxes);
-  for (int b = 0; b < nboxes; ++b) {
-    if (parent[b] < 0) { nei[b] = {b}; continue; }
+  // problems are independent (their boxes are a contiguous id range, parents first)
+  auto neighbours = [&](int b) {
+    if (parent[b] < 0) { nei[b] = {b}; return; }
     std::vector<int> r(cnt[b]);
     std::iota(r.begin(), r.end(), off[b]);
     double xc, yc, R;
@@ -272,13 +273,17 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       }
       if (mn < rr) nei[b].push_back(j);
     }
-  }
-  for (int b = 0; b < nboxes; ++b) {
-    if (parent[b] < 0) continue;
-    auto& l = nei[b];
-    l.erase(std::remove(l.begin(), l.end(), b), l.end());
-    std::sort(l.begin(), l.end());
-  }
+  };
+  parallel_for(nprob, [&](int p) {
+    const int b1 = (p + 1 < nprob) ? proot[p + 1] : nboxes;
+    for (int b = proot[p]; b < b1; ++b) neighbours(b);
+    for (int b = proot[p]; b < b1; ++b) {
+      if (parent[b] < 0) continue;
+      auto& l = nei[b];
+      l.erase(std::remove(l.begin(), l.end(), b), l.end());
+      std::sort(l.begin(), l.end());
+    }
+  }, 1);
   // ---- point table: Ntot points + NPROXY proxies per non-root box; a box's proxy slot
   // follows the order levels are compressed in, so each level uploads one contiguous range
   std::vector<int> pslot(nboxes, -1);
@@ -318,7 +323,9 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     if (boxes.empty()) continue;
     const int nbL = (int)boxes.size();
     std::vector<std::vector<int>> outs(nbL), inns(nbL), rows_out(nbL), rows_in(nbL);
-    for (int q = 0; q < nbL; ++q) {
+    // every box of the level reads its children's skeletons and writes only its own
+    // slots (sets, proxy ring, features): the boxes run in parallel on the host cores
+    parallel_for(nbL, [&](int q) {
       const int b = boxes[q];
       auto& out = outs[q];
       auto& inn = inns[q];
@@ -403,7 +410,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
         rows_in[q].push_back((int)(pb + t));
       }
       HSS_REQUIRE(out.size() <= 4096, HSS_ERR_RANK, "skeleton set exceeds 4096 points");
-    }
+    }, 16);
     lap(1);
     {
       const size_t p0 = (size_t)Ntot + (size_t)NPROXY * pslot[boxes[0]];
