@@ -92,7 +92,7 @@ static void run_moves(const std::vector<MoveP>& mv, cudaStream_t s) {
 }
 
 static void run_gemms(const std::vector<GemmP<double>>& P, bool tA, bool tB, double alpha, double beta,
-                      cudaStream_t s, bool skinny = false) {
+                      cudaStream_t s, bool skinny = false, bool df = false) {
   if (P.empty()) return;
   int maxM = 0, maxN = 0;
   for (auto& p : P) { maxM = std::max(maxM, p.M); maxN = std::max(maxN, p.N); }
@@ -101,12 +101,13 @@ static void run_gemms(const std::vector<GemmP<double>>& P, bool tA, bool tB, dou
   for (size_t off = 0; off < P.size(); off += 65535) {
     const int cnt = (int)std::min<size_t>(65535, P.size() - off);
     if (skinny) gemm_skinny<double>(d.p + off, cnt, maxM, alpha, beta, s);
+    else if (df) gemm_batched_df(d.p + off, cnt, maxM, maxN, tA, tB, alpha, beta, s);
     else gemm_batched<double>(d.p + off, cnt, maxM, maxN, tA, tB, alpha, beta, s);
   }
   HSS_CUDA(cudaStreamSynchronize(s));
 }
 
-static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t s) {
+static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t s, bool df = false) {
   if (mats.empty()) return;
   const int nb = (int)mats.size();
   int maxn = 0;
@@ -132,7 +133,7 @@ static void invert_many(std::vector<std::pair<double*, int>>& mats, cudaStream_t
     int mx = 0;
     const int cnt = std::min(65535, nb - o);
     for (int i = o; i < o + cnt; ++i) mx = std::max(mx, mats[i].second);
-    invert_batched<double>(dP.p + o, cnt, mx, s);
+    invert_batched<double>(dP.p + o, cnt, mx, s, df);
   }
   std::vector<int> hi;
   download(hi, info.p, nb, s);
@@ -887,7 +888,7 @@ void HSS1D::invert() {
       check_launch("k_assemble1");
       HSS_CUDA(cudaStreamSynchronize(stream));
     }
-    invert_many(mats, stream);
+    invert_many(mats, stream, dfinv());
     std::vector<MoveP> mv;
     for (int b : boxes) {
       const int n = nskel[b];
@@ -903,8 +904,8 @@ void HSS1D::invert() {
       P1.push_back(GemmP<double>{T_UP.p + oT[b], W1.p + oD[b] + k, W1.p + oD[b], k, n, nr, k, n, n});
       P2.push_back(GemmP<double>{W2.p + oD[b] + (size_t)k * n, T_DN.p + oT[b], W2.p + oD[b], n, k, nr, n, k, n});
     }
-    run_gemms(P1, false, false, 1.0, 1.0, stream);
-    run_gemms(P2, false, true, 1.0, 1.0, stream);
+    run_gemms(P1, false, false, 1.0, 1.0, stream, false, dfinv());
+    run_gemms(P2, false, true, 1.0, 1.0, stream, false, dfinv());
     mv.clear();
     for (int b : boxes) {
       const int n = nskel[b], k = kskel[b];
@@ -917,7 +918,7 @@ void HSS1D::invert() {
       if (nr <= 0 || k == 0) continue;
       P1.push_back(GemmP<double>{W3.p + oL[b] + (size_t)k * k, T_DN.p + oT[b], W3.p + oL[b], k, k, nr, k, k, k});
     }
-    run_gemms(P1, false, true, 1.0, 1.0, stream);
+    run_gemms(P1, false, true, 1.0, 1.0, stream, false, dfinv());
     mv.clear();
     mats.clear();
     for (int b : boxes) {
@@ -926,7 +927,7 @@ void HSS1D::invert() {
       mats.push_back({Einv.p + oE[b], k});
     }
     run_moves(mv, stream);
-    invert_many(mats, stream);
+    invert_many(mats, stream, dfinv());
     // Linv = FL E ; Rinv = E RF ; Dinv = Finv - Linv RF
     std::vector<GemmP<double>> PL, PR, PD;
     mv.clear();
@@ -936,14 +937,14 @@ void HSS1D::invert() {
       PR.push_back(GemmP<double>{Einv.p + oE[b], W1.p + oD[b], Rinv.p + oR[b], k, n, k, k, n, k});
       mv.push_back(MoveP{Fw.p + oD[b], Dinv.p + oD[b], nullptr, n, n, n, n, 0, 0});
     }
-    run_gemms(PL, false, false, 1.0, 0.0, stream);
-    run_gemms(PR, false, false, 1.0, 0.0, stream);
+    run_gemms(PL, false, false, 1.0, 0.0, stream, false, dfinv());
+    run_gemms(PR, false, false, 1.0, 0.0, stream, false, dfinv());
     run_moves(mv, stream);
     for (int b : boxes) {
       const int n = nskel[b], k = kskel[b];
       PD.push_back(GemmP<double>{Linv.p + oL[b], W1.p + oD[b], Dinv.p + oD[b], n, n, k, n, n, n});
     }
-    run_gemms(PD, false, false, -1.0, 1.0, stream);
+    run_gemms(PD, false, false, -1.0, 1.0, stream, false, dfinv());
   }
   // top of every tree: FT = [E2 M_SIB2; M_SIB3 E3] (the root's children, reference boxes 2 and 3)
   ktop.assign(nprob, 0);
@@ -969,7 +970,7 @@ void HSS1D::invert() {
   k_assemble1<<<(int)fa.size(), 256, 0, stream>>>(d.p);
   check_launch("k_assemble1 top");
   HSS_CUDA(cudaStreamSynchronize(stream));
-  invert_many(mats, stream);
+  invert_many(mats, stream, dfinv());
   inverted = true;
   if (dfm()) make_df();
 }
@@ -1135,8 +1136,8 @@ void HSS1D::make_df() {
 }
 
 void HSS1D::set_precision(int prec) {
-  HSS_REQUIRE(prec == HSS_PREC_FP64 || prec == HSS_PREC_DFLOAT, HSS_ERR_ARG,
-              "HSS1D solves run in HSS_PREC_FP64 or HSS_PREC_DFLOAT");
+  HSS_REQUIRE(prec == HSS_PREC_FP64 || prec == HSS_PREC_DFLOAT || prec == HSS_PREC_DFLOAT_INV, HSS_ERR_ARG,
+              "HSS1D runs in HSS_PREC_FP64, HSS_PREC_DFLOAT or HSS_PREC_DFLOAT_INV");
   precision = prec;
   clear_plans();
   if (dfm()) make_df();

@@ -84,7 +84,8 @@ struct HSS1D {
   DevBuf<double> Linv_df, Rinv_df, Dinv_df, FTinv_df, T_UP_df, TDNT_df, M_SELF_df, M_SIB_df;
   void set_precision(int prec);
   void make_df();
-  bool dfm() const { return precision == HSS_PREC_DFLOAT; }
+  bool dfm() const { return precision == HSS_PREC_DFLOAT || precision == HSS_PREC_DFLOAT_INV; }
+  bool dfinv() const { return precision == HSS_PREC_DFLOAT_INV; }
   void clear_plans() {
     g_inv.clear();
     g_fwd.clear();

@@ -64,8 +64,9 @@ class HSS1DMatrix:
         return out
 
     def set_precision(self, precision: str):
-        """'fp64' or 'dfloat': arithmetic of the apply / inverse-apply products."""
-        code = {"fp64": L.HSS_PREC_FP64, "dfloat": L.HSS_PREC_DFLOAT}[precision]
+        """'fp64', 'dfloat' (double-float apply / inverse-apply products) or 'dfloat_inv'
+        (also the next hss1d_invert's updates and products in double-float)."""
+        code = {"fp64": L.HSS_PREC_FP64, "dfloat": L.HSS_PREC_DFLOAT, "dfloat_inv": L.HSS_PREC_DFLOAT_INV}[precision]
         L.check(L.lib().hss1d_set_precision(self._h, code))
 
     # --- learned ranks ----------------------------------------------------------

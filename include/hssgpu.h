@@ -122,8 +122,9 @@ int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
                 double* relres, int32_t* iters);
 int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
-/* arithmetic of the solve products: HSS_PREC_FP64 (default) or HSS_PREC_DFLOAT (float-pair
- * copies of the FP64 operators, products on the FP32 pipes, ~2^-48 per product) */
+/* arithmetic of the solve products: HSS_PREC_FP64 (default), HSS_PREC_DFLOAT (float-pair
+ * copies of the FP64 operators, products on the FP32 pipes, ~2^-48 per product) or
+ * HSS_PREC_DFLOAT_INV (also the following hss1d_invert's updates and products) */
 int hss1d_set_precision(hss1d_matrix* H, int32_t precision);
 int hss1d_destroy(hss1d_matrix* H);
 

@@ -230,3 +230,20 @@ def test_fsym_transforminv_and_precision_errors(gpu):
     with pytest.raises(L.HSSError) as e:
         L.check(L.lib().hss1d_set_precision(H._h, L.HSS_PREC_MIXED))
     assert e.value.code == L.HSS_ERR_ARG
+
+
+def test_dfloat_inv_forest(gpu):
+    """HSS_PREC_DFLOAT_INV: the inversion's updates and products in double-float; the
+    refined solve reaches 1e-10 and matches the FP64 inverse apply to 1e-9."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(4, nmin=800, nmax=3000, seed=19)
+    H64 = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    G1.HSS1D_invert_nsym(H64)
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    H.set_precision("dfloat_inv")
+    G1.HSS1D_invert_nsym(H)
+    F = np.random.default_rng(6).standard_normal((sum(sizes), 3))
+    x64 = G1.HSS1D_applyinv_nsym(H64, None, None, F)
+    x, rr, it = G1.HSS1D_solve(H, F, 1e-10, 4)
+    assert rr <= 1e-10
+    assert np.linalg.norm(x - x64) <= 1e-9 * np.linalg.norm(x64)
