@@ -216,6 +216,60 @@ def bench_batched(args, L, dev):
             "solve_ms_by_path": {p: out[p][0] for p in out}, "dtype": "f64"}
 
 
+def bench_config5(args, L, dev):
+    """The learned-rank configuration at scale: 2048 double-layer curves (N log-uniform in
+    [2048, 32768], ~23 M points) compressed plainly and with the rank MLP trained on the
+    ranks of a 256-curve batched compress, plus the 1024 x 1024 HSS2D grid
+    (N = 1,048,576) in the double-float inversion mode.  Reports seconds and the QR steps
+    the network saved; the adaptive ID stays the judge of every rank."""
+    import torch
+    from hssc_directsolver_gb300 import hss1d as G1, hss2d as G2, kernels as GK, geometry as GG
+    from hssc_directsolver_gb300.rank_mlp import RankPredictor, training_set
+    kern = GK.Kernel("DL_L_2D")
+    Xt, _ = GG.batched_curves(256, nmin=1024, nmax=16384, seed=1)
+    Ht = G1.HSS1D_compress_batch(Xt, 64, 1e-10, kern)
+    Ft, yt = training_set(Ht)
+    del Ht
+    P = RankPredictor(seed=0)
+    t0 = time.perf_counter()
+    loss = P.train(Ft, yt, epochs=100, batch=512, lr=3e-3)
+    t_train = time.perf_counter() - t0
+    Xs, ss = GG.batched_curves(2048, nmin=2048, nmax=32768, seed=5)
+    out = {"curves": {"workload": f"2048 Laplace double-layer curves, N log-uniform [2048,32768] (total "
+                                  f"{sum(ss)}), leaf 64, tol 1e-10",
+                      "mlp": {"train_boxes": int(len(yt)), "train_s": t_train, "loss": loss}}}
+    for mode in ("plain", "learned"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, kern, predictor=(P if mode == "learned" else None))
+        t1 = time.perf_counter()
+        H.set_precision("dfloat_inv")
+        G1.HSS1D_invert_nsym(H)
+        t2 = time.perf_counter()
+        f = np.random.default_rng(0).standard_normal((sum(ss), 1))
+        _, rr, it = G1.HSS1D_solve(H, f, 1e-10, 4)
+        done, full, reruns = H.id_stats()
+        out["curves"][mode] = {"compress_s": t1 - t0, "invert_s": t2 - t1, "relres": rr, "solves_used": it,
+                               "qr_steps": done, "qr_steps_full": full, "reruns": reruns}
+        del H
+    prm = workload_params("dfloat_inv", 128)
+    t0 = time.perf_counter()
+    tree = G2.HSS2D_build_tree_nsym(prm)
+    G2.HSS2D_compress_nsym(tree)
+    G2.HSS2D_invert_nsym(tree)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    F = rhs(prm.N)
+    _, rr, it = G2.HSS2D_solve(tree, F, 1e-10, 6)
+    t2 = time.perf_counter()
+    _, rr, it = G2.HSS2D_solve(tree, F, 1e-10, 6)
+    t3 = time.perf_counter()
+    out["hss2d_1024"] = {"workload": "HSS2D 1024x1024 grid (N=1048576), dfloat_inv", "compress_invert_s": t1 - t0,
+                         "solve_s_host_buffers": t3 - t2, "relres": rr, "solves_used": it,
+                         "factor_bytes_per_solve": tree.solve_bytes()}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -226,6 +280,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-curve batched HSS1D section")
     ap.add_argument("--curves", type=int, default=512)
+    ap.add_argument("--config5", action="store_true",
+                    help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
     ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv",
                     help="solve paths to measure (comma list of fp64, mixed, dfloat, dfloat_inv)")
     args = ap.parse_args()
@@ -389,6 +445,8 @@ def main():
     }
     if batched is not None:
         line["batched_hss1d"] = batched
+    if args.config5:
+        line["config5"] = bench_config5(args, L, dev)
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cores = os.cpu_count() or 1
