@@ -438,7 +438,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{pTup + (size_t)i * k * nr, W1.p + (size_t)i * n * n + k, W1.p + (size_t)i * n * n, k, n,
                              nr, k, n, n});
-      run_gemm<R>(P, false, false, R(1), R(1), stream, gscratch, dfinv());
+      run_gemm<R>(P, false, false, R(1), R(1), stream, gscratch, dfgemm());
     }
     // (3) W2 = RFI[:, J]   (k x n, ld k)
     k_gather_cols<R><<<grid_for((long long)nb * k * n), 256, 0, stream>>>(nb, k, n, d.J.p, W1.p, (long long)n * n, n,
@@ -449,7 +449,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{W2.p + (size_t)i * k * n + (size_t)k * k, pTdn + (size_t)i * k * nr,
                              W2.p + (size_t)i * k * n, k, k, nr, k, k, k});
-      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfinv());
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfgemm());
     }
     // (5) E = inv(EI)
     auto& Eb = d.fac<R>(1);
@@ -464,7 +464,7 @@ void HSS2D::invert_impl() {
     for (int i = 0; i < nb; ++i)
       P.push_back(GemmP<R>{Eb.p + (size_t)i * k * k, W1.p + (size_t)i * n * n, Ub.p + (size_t)i * k * n, k, n, k, k,
                            n, k});
-    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfinv());
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfgemm());
     // (7) FIc = FI[:, J]
     k_gather_cols<R><<<grid_for((long long)nb * n * n), 256, 0, stream>>>(nb, n, n, d.J.p, FI, (long long)n * n, n,
                                                                           W1.p, (long long)n * n, n);
@@ -474,7 +474,7 @@ void HSS2D::invert_impl() {
       for (int i = 0; i < nb; ++i)
         P.push_back(GemmP<R>{W1.p + (size_t)i * n * n + (size_t)k * n, pTdn + (size_t)i * k * nr,
                              W1.p + (size_t)i * n * n, n, k, nr, n, k, n});
-      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfinv());
+      run_gemm<R>(P, false, true, R(1), R(1), stream, gscratch, dfgemm());
     }
     auto& Gb = d.fac<R>(3);
     Gb.alloc((size_t)nb * n * k);
@@ -487,7 +487,7 @@ void HSS2D::invert_impl() {
     for (int i = 0; i < nb; ++i)
       P.push_back(GemmP<R>{Gb.p + (size_t)i * n * k, Eb.p + (size_t)i * k * k, GEb.p + (size_t)i * n * k, n, k, k, n,
                            k, n});
-    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfinv());
+    run_gemm<R>(P, false, false, R(1), R(0), stream, gscratch, dfgemm());
     check_launch("invert level");
     HSS_CUDA(cudaStreamSynchronize(stream));
   }

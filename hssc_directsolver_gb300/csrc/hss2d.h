@@ -90,9 +90,13 @@ struct HSS2D {
     return prm.precision == HSS_PREC_DFLOAT || prm.precision == HSS_PREC_DFLOAT_INV ||
            prm.precision == HSS_PREC_MIXED;
   }
-  // double-float inversion updates and products
+  // double-float Gauss-Jordan updates of the block inverses
   bool dfinv() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
-  // double-float trailing updates in the interpolation least squares
+  // double-float products of the inversion (E, U, G, GE)
+  bool dfgemm() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
+  // double-float trailing updates in the interpolation least squares (backward stable:
+  // the compressed operator keeps the compression tolerance, but T is not the FP64 T,
+  // so HSS_PREC_DFLOAT keeps the FP64 operator)
   bool dftree() const { return prm.precision == HSS_PREC_DFLOAT_INV || prm.precision == HSS_PREC_MIXED; }
   void make_df_forward();
   void make_df_inverse();
