@@ -406,27 +406,67 @@ __device__ __forceinline__ void df_madd_x2(f32x2& sh, f32x2& sl, f32x2 ah, f32x2
   sh = s;
 }
 
+// Operand access of the double-float skinny kernel for a plain or a segmented product.
+__device__ __forceinline__ int dfd_K(const GemmP<double>& p) { return p.K; }
+__device__ __forceinline__ const float2* dfd_col(const GemmP<double>& p, int k) {
+  return reinterpret_cast<const float2*>(p.A) + (size_t)k * p.lda;
+}
+__device__ __forceinline__ double dfd_b(const GemmP<double>& p, int k, int c) { return p.B[k + (size_t)c * p.ldb]; }
+__device__ __forceinline__ bool dfd_vec_ok(const GemmP<double>& p) {
+  return (p.lda % 2) == 0 && (reinterpret_cast<uintptr_t>(p.A) & 15) == 0;
+}
+__device__ __forceinline__ int dfd_K(const SegGemmP& p) { return p.K[0] + p.K[1] + p.K[2]; }
+__device__ __forceinline__ int dfd_seg(const SegGemmP& p, int& k) {
+  if (k < p.K[0]) return 0;
+  k -= p.K[0];
+  if (k < p.K[1]) return 1;
+  k -= p.K[1];
+  return 2;
+}
+// (selects rather than an indexed member array: a dynamic index would put the
+// descriptor in local memory)
+__device__ __forceinline__ const float2* dfd_col(const SegGemmP& p, int k) {
+  const int sg = dfd_seg(p, k);
+  const double* a = sg == 0 ? p.A[0] : (sg == 1 ? p.A[1] : p.A[2]);
+  const int ld = sg == 0 ? p.lda[0] : (sg == 1 ? p.lda[1] : p.lda[2]);
+  return reinterpret_cast<const float2*>(a) + (size_t)k * ld;
+}
+__device__ __forceinline__ double dfd_b(const SegGemmP& p, int k, int c) {
+  const int sg = dfd_seg(p, k);
+  const double* b = sg == 0 ? p.B[0] : (sg == 1 ? p.B[1] : p.B[2]);
+  const int ld = sg == 0 ? p.ldb[0] : (sg == 1 ? p.ldb[1] : p.ldb[2]);
+  const double sn = sg == 0 ? p.sign[0] : (sg == 1 ? p.sign[1] : p.sign[2]);
+  return sn * b[k + (size_t)c * ld];
+}
+__device__ __forceinline__ bool dfd_vec_ok(const SegGemmP& p) {
+  bool ok = true;
+#pragma unroll
+  for (int sg = 0; sg < 3; ++sg)
+    if (p.K[sg] > 0) ok = ok && (p.lda[sg] % 2) == 0 && (reinterpret_cast<uintptr_t>(p.A[sg]) & 15) == 0;
+  return ok;
+}
+
 constexpr int SKD_STAGES = 4;  // cp.async columns in flight per thread (<= 4 right-hand sides)
 
-template <int NR>
-__global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP<double>* __restrict__ P, double alpha, double beta,
+template <int NR, typename D>
+__global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __restrict__ P, double alpha, double beta,
                                                    int ksplit, double* __restrict__ part, int mmax) {
   constexpr int V = 2;  // one 16-byte load = two (hi, lo) pairs
   constexpr int KC = (NR > 4) ? SK_KC / 2 : SK_KC;  // static shared memory under 48 KB
   constexpr int ROWS = 32 * V;
-  const GemmP<double> p = P[blockIdx.z];
+  const D p = P[blockIdx.z];
   const int row0 = blockIdx.x * ROWS;
   if (row0 >= p.M) return;
-  const float2* A = reinterpret_cast<const float2*>(p.A);
   const int N = p.N;
-  const int kper = (((p.K + ksplit - 1) / ksplit) + 7) & ~7;
-  const int kb = blockIdx.y * kper, ke = min(p.K, kb + kper);
+  const int Kt = dfd_K(p);
+  const int kper = (((Kt + ksplit - 1) / ksplit) + 7) & ~7;
+  const int kb = blockIdx.y * kper, ke = min(Kt, kb + kper);
   __shared__ f32x2 Bh2[KC][NR], Bhn2[KC][NR], Bln2[KC][NR];
   __shared__ float2 red[8][NR][ROWS];
   __shared__ __align__(16) float4 ring[(NR <= 4) ? SKD_STAGES : 1][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int r = row0 + lane * V;
-  const bool vec_ok = ((p.lda % V) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  const bool vec_ok = dfd_vec_ok(p);
   f32x2 sh[NR], sl[NR];  // {row r, row r+1} accumulators
 #pragma unroll
   for (int c = 0; c < NR; ++c) { sh[c] = 0ULL; sl[c] = 0ULL; }
@@ -435,7 +475,7 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP
     __syncthreads();
     for (int e = threadIdx.x; e < KC * NR; e += 256) {
       const int kk = e % KC, c = e / KC;
-      const double x = (kk < kn && c < N) ? p.B[(size_t)(kc + kk) + (size_t)c * p.ldb] : 0.0;
+      const double x = (kk < kn && c < N) ? dfd_b(p, kc + kk, c) : 0.0;
       float xh, xl;
       split_d2f(x, xh, xl);
       Bh2[kk][c] = x2_pack(xh, xh);
@@ -453,7 +493,7 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP
         auto issue = [&](int it) {
           const int kk = w + 8 * it;
           const bool live = it < niter;
-          const float2* src = live ? A + (size_t)(kc + kk) * p.lda + (nv ? r : 0) : A;
+          const float2* src = live ? dfd_col(p, kc + kk) + (nv ? r : 0) : dfd_col(p, kc);
           const unsigned dst = (unsigned)__cvta_generic_to_shared(&ring[it % SKD_STAGES][threadIdx.x]);
           const int bytes = live ? nv : 0;
           asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes));
@@ -476,7 +516,7 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP
     }
     // software-pipelined: the next column's 16 bytes are in flight during this column's math
     auto load = [&](int kk) -> float4 {
-      const float2* col = A + (size_t)(kc + kk) * p.lda;
+      const float2* col = dfd_col(p, kc + kk);
       if (vec_ok && r + V <= p.M) return __ldg(reinterpret_cast<const float4*>(col + r));
       const float2 q0 = (r < p.M) ? __ldg(col + r) : make_float2(0.f, 0.f);
       const float2 q1 = (r + 1 < p.M) ? __ldg(col + r + 1) : make_float2(0.f, 0.f);
@@ -522,10 +562,11 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const GemmP
 }
 
 // split-K partials of k_skinny_df (float pairs) summed in double-float arithmetic
-__global__ void __launch_bounds__(256) k_skinny_reduce_df(const GemmP<double>* __restrict__ P, double alpha,
+template <typename D>
+__global__ void __launch_bounds__(256) k_skinny_reduce_df(const D* __restrict__ P, double alpha,
                                                           double beta, int ksplit, const double* __restrict__ part,
                                                           int mmax) {
-  const GemmP<double> p = P[blockIdx.y];
+  const D p = P[blockIdx.y];
   const float2* pp = reinterpret_cast<const float2*>(part);
   float alh, all;
   split_d2f(alpha, alh, all);
@@ -709,20 +750,31 @@ int skinny_ksplit_df(int batch, int maxM, int maxK) {
   return ks;
 }
 
-void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
-                          int ksplit, double* part, cudaStream_t s) {
+template <typename D>
+static void skinny_df_launch(const D* dP, int batch, int maxM, int maxN, double alpha, double beta, int ksplit,
+                             double* part, cudaStream_t s) {
   if (batch <= 0 || maxM <= 0) return;
   HSS_REQUIRE(batch <= 65535 && maxN <= 8, HSS_ERR_ARG, "skinny gemm: batch <= 65535 and N <= 8");
   HSS_REQUIRE(ksplit == 1 || part != nullptr, HSS_ERR_ARG, "skinny gemm: split-K needs a workspace");
   dim3 grid(ceil_div(maxM, 64), ksplit, batch);
-  if (maxN <= 4) k_skinny_df<4><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
-  else k_skinny_df<8><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  if (maxN <= 4) k_skinny_df<4, D><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+  else k_skinny_df<8, D><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
   check_launch("k_skinny_df");
   if (ksplit > 1) {
     const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 256));
-    k_skinny_reduce_df<<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+    k_skinny_reduce_df<D><<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
     check_launch("k_skinny_reduce_df");
   }
+}
+
+void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
+                          int ksplit, double* part, cudaStream_t s) {
+  skinny_df_launch(dP, batch, maxM, maxN, alpha, beta, ksplit, part, s);
+}
+
+void gemm_skinny_split_df(const SegGemmP* dP, int batch, int maxM, int maxN, double alpha, double beta,
+                          int ksplit, double* part, cudaStream_t s) {
+  skinny_df_launch(dP, batch, maxM, maxN, alpha, beta, ksplit, part, s);
 }
 
 template <typename R>

@@ -20,6 +20,19 @@ struct GemmP {
   int lda, ldb, ldc;
 };
 
+// C = sum_s sign_s A_s B_s over up to three K segments (A_s: M x K_s, ld lda_s; B_s:
+// K_s x N, ld ldb_s): one launch for a sum of products that share their rows, e.g.
+// FI q - G phi_up + GE phi_dn of the inverse apply's downward pass.
+struct SegGemmP {
+  const double* A[3];
+  const double* B[3];
+  double* C;
+  int K[3];
+  int lda[3], ldb[3];
+  double sign[3];
+  int M, N, ldc;
+};
+
 // Double-float ("FP64 x FP32 pairs") skinny product: A holds every FP64 element
 // as a float pair (hi, lo) with hi + lo equal to it to 2^-48 (same 8 bytes per
 // element), B and C are FP64.  Each multiply-add runs on the FP32 pipes: an exact
@@ -27,6 +40,9 @@ struct GemmP {
 // accumulator with TwoSum and a Fast2Sum renormalisation.  GB300 issues FP32 at
 // 64x its FP64 rate, so this outruns native FP64 for matrix-vector products.
 void gemm_skinny_split_df(const GemmP<double>* dP, int batch, int maxM, int maxN, double alpha, double beta,
+                          int ksplit, double* part, cudaStream_t s);
+// the segmented form (A_s as float pairs; C = alpha * sum + beta * C)
+void gemm_skinny_split_df(const SegGemmP* dP, int batch, int maxM, int maxN, double alpha, double beta,
                           int ksplit, double* part, cudaStream_t s);
 // gemm_batched in double-float arithmetic (FP64 in and out, ~2^-47 per product)
 void gemm_batched_df(const GemmP<double>* dP, int batch, int maxM, int maxN, bool tA, bool tB, double alpha,

@@ -229,9 +229,33 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
 }
 
 template <typename R>
+void SolvePlan<R>::add_seg(const std::vector<SegGemmP>& P, R alpha, R beta, cudaStream_t s) {
+  HSS_REQUIRE(df, HSS_ERR_STATE, "segmented plan steps need double-float operands");
+  Step st;
+  st.batch = (int)P.size();
+  int maxK = 0;
+  for (auto& p : P) {
+    st.maxM = std::max(st.maxM, p.M);
+    st.maxN = std::max(st.maxN, p.N);
+    maxK = std::max(maxK, p.K[0] + p.K[1] + p.K[2]);
+  }
+  st.alpha = alpha;
+  st.beta = beta;
+  st.ksplit = skinny_ksplit_df(st.batch, st.maxM, maxK);
+  if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
+  st.dseg.alloc(P.size());
+  HSS_CUDA(cudaMemcpyAsync(st.dseg.p, P.data(), P.size() * sizeof(SegGemmP), cudaMemcpyHostToDevice, s));
+  steps.push_back(std::move(st));
+}
+
+template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
   for (auto& st : steps) {
     if constexpr (std::is_same<R, double>::value) {
+      if (df && st.dseg.p) {
+        gemm_skinny_split_df(st.dseg.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+        continue;
+      }
       if (df) {
         gemm_skinny_split_df(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
         continue;
@@ -614,6 +638,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
     std::vector<GemmP<R>> P1, P2, P3;
+    std::vector<SegGemmP> PS;
     for (int i = 0; i < g.nb; ++i) {
       R* out;
       int ldo;
@@ -629,6 +654,36 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
+      if constexpr (std::is_same<R, double>::value) {
+        if (use_df && lev > 0) {
+          // FI q - G phi_up + GE phi_dn as one double-float sum
+          SegGemmP sp{};
+          sp.A[0] = F(d, 0) + fo(i) * g.n * g.n;
+          sp.B[0] = q;
+          sp.K[0] = g.n;
+          sp.lda[0] = g.n;
+          sp.ldb[0] = ldq;
+          sp.sign[0] = 1.0;
+          sp.A[1] = F(d, 3) + fo(i) * g.n * g.k;
+          sp.B[1] = d.vec<R>(0).p + (size_t)i * g.k;
+          sp.K[1] = g.k;
+          sp.lda[1] = g.n;
+          sp.ldb[1] = g.nb * g.k;
+          sp.sign[1] = -1.0;
+          sp.A[2] = F(d, 4) + fo(i) * g.n * g.k;
+          sp.B[2] = d.vec<R>(1).p + (size_t)i * g.k;
+          sp.K[2] = g.k;
+          sp.lda[2] = g.n;
+          sp.ldb[2] = g.nb * g.k;
+          sp.sign[2] = 1.0;
+          sp.C = out;
+          sp.M = g.n;
+          sp.N = r;
+          sp.ldc = ldo;
+          PS.push_back(sp);
+          continue;
+        }
+      }
       P1.push_back(GemmP<R>{F(d, 0) + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
       if (lev > 0) {
         P2.push_back(GemmP<R>{F(d, 3) + fo(i) * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
@@ -636,6 +691,10 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
         P3.push_back(GemmP<R>{F(d, 4) + fo(i) * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
                               g.k, g.n, g.nb * g.k, ldo});
       }
+    }
+    if (!PS.empty()) {
+      pl.add_seg(PS, R(1), R(0), stream);
+      continue;
     }
     pl.add(P1, R(1), R(0), stream);
     if (lev > 0) {

@@ -17,6 +17,7 @@ template <typename R>
 struct SolvePlan {
   struct Step {
     DevBuf<GemmP<R>> d;
+    DevBuf<SegGemmP> dseg;  // segmented products (df plans only)
     DevBuf<R> part;  // split-K partial sums
     int batch = 0, maxM = 0, maxN = 0, ksplit = 1;
     R alpha = R(1), beta = R(0);
@@ -24,6 +25,8 @@ struct SolvePlan {
   std::vector<Step> steps;
   bool df = false;  // FP64 operands stored as float pairs, products on the FP32 pipes
   void add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s);
+  // C = alpha * sum_s sign_s A_s B_s + beta * C in one launch (df plans only)
+  void add_seg(const std::vector<SegGemmP>& P, R alpha, R beta, cudaStream_t s);
   void run(cudaStream_t s) const;
   int launches() const {
     int n = 0;
