@@ -28,6 +28,10 @@ ERR_NAMES = {0: "HSS_OK", 1: "HSS_ERR_ARG", 2: "HSS_ERR_CUDA", 3: "HSS_ERR_SINGU
 
 HSS_SL_L_2D = 0
 HSS_DL_L_2D = 1
+HSS_SL_H_2D = 2
+HSS_MOD_GAUSS = 0
+HSS_MOD_BUMP = 1
+HSS_MOD_SQRT_BUMP = 2
 HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_PREC_DFLOAT = 2
@@ -39,7 +43,9 @@ HSS_INTER_LOWRANK = 1
 class hss_kernel_params(C.Structure):
     _fields_ = [("flag", C.c_int32), ("pad_", C.c_int32), ("h", C.c_double),
                 ("b_alpha", C.c_double), ("b_x0", C.c_double), ("b_y0", C.c_double), ("b_isig", C.c_double),
-                ("c_alpha", C.c_double), ("c_x0", C.c_double), ("c_y0", C.c_double), ("c_isig", C.c_double)]
+                ("c_alpha", C.c_double), ("c_x0", C.c_double), ("c_y0", C.c_double), ("c_isig", C.c_double),
+                ("kh", C.c_double), ("dr_re", C.c_double), ("dr_im", C.c_double),
+                ("b_kind", C.c_int32), ("c_kind", C.c_int32)]
 
 
 class hss2d_params(C.Structure):
@@ -67,6 +73,10 @@ SIGNATURES = {
     "hss_device_count": (C.c_int, [_I32P]),
     "hss1d_compress": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                  C.POINTER(hss_kernel_params), C.c_uint64]),
+    "hss_kernel_eval": (C.c_int, [C.POINTER(hss_kernel_params), _DP, C.c_int64, _DP, C.c_int64, _DP]),
+    "hss_dr_corrections": (C.c_int, [C.c_double, C.c_double, C.c_double, _DP]),
+    "hss_dr_stencil": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int64, C.c_int32, _I32P, _I64P, _DP,
+                                 _I32P]),
     "hss1d_compress_fsym": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                       C.POINTER(hss_kernel_params), C.c_uint64]),
     "hss1d_compress_batch": (C.c_int, [C.POINTER(_P), C.c_int32, _I64P, C.POINTER(C.c_void_p), _I64P, C.c_int32,

@@ -10,8 +10,16 @@
 #include "hss2d.h"
 #include "mlp.h"
 
+#include <complex>
+#include <numeric>
+
+#include "kgen.cuh"
+
 namespace hss {
 void batched_inverse_noalloc(double* d_A, int n, int batch, int* d_info, cudaStream_t s);
+void dr_corrections(double h, std::complex<double> k, std::complex<double>& corr0, std::complex<double>& corr1);
+void dr_stencil(double h, std::complex<double> k, long long n, int order, std::vector<long long>& J,
+                std::vector<std::complex<double>>& w, std::vector<int>& stencil);
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace hss
@@ -67,6 +75,80 @@ extern "C" {
 const char* hss_last_error(void) { return hss::g_last_error.c_str(); }
 
 int hss_version(void) { return 100; }
+
+int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, const double* X2, int64_t n,
+                    double* A) {
+  HSS_TRY
+  HSS_REQUIRE(kp && X1 && X2 && A && m > 0 && n > 0, HSS_ERR_ARG, "kernel_eval: bad arguments");
+  HSS_REQUIRE(m + n <= (int64_t)INT32_MAX, HSS_ERR_ARG, "kernel_eval: too many points");
+  const bool cplx = kp->flag == HSS_SL_H_2D;
+  HSS_REQUIRE(kp->flag == HSS_SL_L_2D || cplx, HSS_ERR_ARG,
+              "kernel_eval: HSS_SL_L_2D or HSS_SL_H_2D (the double layer needs normals and weights)");
+  HSS_REQUIRE(std::isfinite(kp->h) && kp->h > 0, HSS_ERR_ARG, "kernel_eval: h must be positive");
+  if (cplx)
+    HSS_REQUIRE(std::isfinite(kp->kh) && kp->kh > 0 && std::isfinite(kp->dr_re) && std::isfinite(kp->dr_im),
+                HSS_ERR_ARG, "kernel_eval: kh must be positive and the DR weight finite");
+  require_device();
+  struct Stream {
+    cudaStream_t s = nullptr;
+    Stream() { HSS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~Stream() { cudaStreamDestroy(s); }
+  } st;
+  const size_t np = (size_t)(m + n);
+  std::vector<double> hx(np), hy(np), zero(np, 0.0);
+  for (int64_t i = 0; i < m; ++i) { hx[i] = X1[i]; hy[i] = X1[m + i]; }
+  for (int64_t j = 0; j < n; ++j) { hx[m + j] = X2[j]; hy[m + j] = X2[n + j]; }
+  PointTable T;
+  T.upload(hx, hy, zero, zero, zero, zero, *kp, st.s);
+  std::vector<int> ids(np);
+  std::iota(ids.begin(), ids.end(), 0);
+  DevBuf<int> dids(np);
+  dids.upload(ids, st.s);
+  const size_t cnt = (size_t)m * (size_t)n * (cplx ? 2 : 1);
+  DevBuf<double> out(cnt);
+  if (cplx) {
+    KgenCP P{dids.p, dids.p + m, (int)m, (int)n, out.p, (long long)m};
+    DevBuf<KgenCP> dP(1);
+    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, st.s));
+    kgen_complex_batched(dP.p, 1, m * n, view(T), make_helm_dev(*kp), st.s);
+  } else {
+    HSS_REQUIRE(m <= (int64_t)INT32_MAX, HSS_ERR_ARG, "kernel_eval: m too large");
+    KgenP<double> P{dids.p, dids.p + m, (int)m, (int)n, out.p, (int)m, 0};
+    DevBuf<KgenP<double>> dP(1);
+    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, st.s));
+    kgen_batched<double>(dP.p, 1, m * n, view(T), make_kernel_dev(*kp), st.s);
+  }
+  HSS_CUDA(cudaMemcpyAsync(A, out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, st.s));
+  HSS_CUDA(cudaStreamSynchronize(st.s));
+  HSS_CATCH
+}
+
+int hss_dr_corrections(double h, double k_re, double k_im, double* corr) {
+  HSS_TRY
+  HSS_REQUIRE(corr != nullptr, HSS_ERR_ARG, "corr is NULL");
+  std::complex<double> c0, c1;
+  dr_corrections(h, std::complex<double>(k_re, k_im), c0, c1);
+  corr[0] = c0.real(); corr[1] = c0.imag(); corr[2] = c1.real(); corr[3] = c1.imag();
+  HSS_CATCH
+}
+
+int hss_dr_stencil(double h, double k_re, double k_im, int64_t n, int32_t order, int32_t* count, int64_t* J,
+                   double* w, int32_t* stencil) {
+  HSS_TRY
+  HSS_REQUIRE(count && J && w && stencil && n > 0, HSS_ERR_ARG, "DR_stencil: bad arguments");
+  std::vector<long long> j;
+  std::vector<std::complex<double>> wv;
+  std::vector<int> st;
+  dr_stencil(h, std::complex<double>(k_re, k_im), n, order, j, wv, st);
+  *count = (int32_t)j.size();
+  for (size_t e = 0; e < j.size(); ++e) {
+    J[e] = j[e];
+    w[2 * e] = wv[e].real();
+    w[2 * e + 1] = wv[e].imag();
+    for (int r = 0; r < 3; ++r) stencil[3 * e + r] = st[3 * e + r];
+  }
+  HSS_CATCH
+}
 
 int hss_device_count(int* count) {
   HSS_TRY

@@ -17,6 +17,35 @@ double modulation(double alpha, double x0, double y0, double isig, double px, do
   return 1.0 + alpha * std::exp(-s);
 }
 
+// Bump_function option 4 (Common/Bump_function.m:53-63): a product of two
+// 0.5 tanh(10 (1 - shift - |x_d|)) + 0.5 ramps
+static double bump4(double px, double py, double shift) {
+  const double D = 1.0 / 0.1;
+  const double f1 = 0.5 * std::tanh(D * (-std::fabs(px) + 1.0 - shift)) + 0.5;
+  const double f2 = 0.5 * std::tanh(D * (-std::fabs(py) + 1.0 - shift)) + 0.5;
+  return f1 * f2;
+}
+
+double modulation(const hss_kernel_params& kp, int which, double px, double py) {
+  const int kind = which ? kp.c_kind : kp.b_kind;
+  if (kind == HSS_MOD_BUMP) return bump4(px, py, 0.0);
+  if (kind == HSS_MOD_SQRT_BUMP) return std::sqrt(bump4(px, py, 4.0 * kp.h));
+  HSS_REQUIRE(kind == HSS_MOD_GAUSS, HSS_ERR_ARG, "unknown modulation form");
+  return which ? modulation(kp.c_alpha, kp.c_x0, kp.c_y0, kp.c_isig, px, py)
+               : modulation(kp.b_alpha, kp.b_x0, kp.b_y0, kp.b_isig, px, py);
+}
+
+HelmDev make_helm_dev(const hss_kernel_params& kp) {
+  // Kernel_Eval.m:47-49 forms (h^2) kh^2 (0.25 i) and 1 + kh^2 (0.25 i) dr
+  HelmDev k;
+  k.kh = kp.kh;
+  k.s = ((kp.h * kp.h) * (kp.kh * kp.kh)) * 0.25;
+  const double q = (kp.kh * kp.kh) * 0.25;
+  k.w_re = 1.0 - q * kp.dr_im;
+  k.w_im = q * kp.dr_re;
+  return k;
+}
+
 void PointTable::upload(const std::vector<double>& hx, const std::vector<double>& hy,
                         const std::vector<double>& hnx, const std::vector<double>& hny,
                         const std::vector<double>& hw, const std::vector<double>& hkap,
@@ -24,8 +53,8 @@ void PointTable::upload(const std::vector<double>& hx, const std::vector<double>
   const size_t n = hx.size();
   std::vector<double> b(n), c(n);
   for (size_t i = 0; i < n; ++i) {
-    b[i] = modulation(kp.b_alpha, kp.b_x0, kp.b_y0, kp.b_isig, hx[i], hy[i]);
-    c[i] = modulation(kp.c_alpha, kp.c_x0, kp.c_y0, kp.c_isig, hx[i], hy[i]);
+    b[i] = modulation(kp, 0, hx[i], hy[i]);
+    c[i] = modulation(kp, 1, hx[i], hy[i]);
   }
   x.upload(hx, s); y.upload(hy, s); nx.upload(hnx, s); ny.upload(hny, s);
   w.upload(hw, s); kap.upload(hkap, s); bval.upload(b, s); cval.upload(c, s);
@@ -45,8 +74,8 @@ void PointTable::upload_range(size_t first, size_t n, const double* hx, const do
   if (n == 0) return;
   std::vector<double> b(n), c(n);
   for (size_t i = 0; i < n; ++i) {
-    b[i] = modulation(kp.b_alpha, kp.b_x0, kp.b_y0, kp.b_isig, hx[i], hy[i]);
-    c[i] = modulation(kp.c_alpha, kp.c_x0, kp.c_y0, kp.c_isig, hx[i], hy[i]);
+    b[i] = modulation(kp, 0, hx[i], hy[i]);
+    c[i] = modulation(kp, 1, hx[i], hy[i]);
   }
   const size_t bytes = n * sizeof(double);
   const double* src[8] = {hx, hy, hnx, hny, hw, hkap, b.data(), c.data()};
@@ -85,6 +114,113 @@ __global__ void __launch_bounds__(256) k_kgen(const KgenP<R>* __restrict__ D, Po
     else { j = (int)(e % d.n); i = (int)(e / d.n); o = j + (size_t)i * d.ld; }
     d.out[o] = (R)kernel_entry(k, P, d.ti[i], d.si[j]);
   }
+}
+
+// H0^(1)(x) = J0(x) + i Y0(x) for x > 0 to ~2e-16 absolute accuracy.
+//  x < 3.5: the ascending series
+//    J0 = sum_k (-1)^k q^k / (k!)^2,  Y0 = (2/pi) [(log(x/2) + gamma) J0 + sum_k (-1)^(k+1) H_k q^k / (k!)^2],
+//    q = x^2 / 4, H_k the harmonic numbers.
+//  x >= 3.5: Hankel's integral (Watson, Theory of Bessel Functions, sec. 7.2), for nu = 0
+//    H0^(1)(x) = sqrt(2 / (pi x)) e^{i (x - pi/4)} / sqrt(pi) * int_{-inf}^{inf} e^{-s^2} (1 + i s^2 / (2x))^(-1/2) ds,
+//  by the trapezoidal rule with step 0.3 on |s| <= 6.3, which converges geometrically for
+//  this analytic integrand (Trefethen & Weideman, SIAM Review 56, 2014).  The factor
+//  (1 + i v)^(-1/2) = r^(-1/2) (cos(t/2) - i sin(t/2)), r = |1 + i v|, t = arg(1 + i v),
+//  with sin(t/2) = (v / r) / (2 cos(t/2)) to avoid cancellation at small v.
+constexpr int kHankelNodes = 21;
+constexpr double kHankelStep = 0.3;
+__constant__ double c_hankel_w[kHankelNodes + 1];  // 2 exp(-(j step)^2), j = 0..21 (j = 0 unused)
+
+__device__ __forceinline__ void hankel0(double x, double& J, double& Y) {
+  constexpr double kGamma = 0.57721566490153286061, kTwoOverPi = 0.63661977236758134308;
+  if (x < 3.5) {
+    const double q = 0.25 * x * x;
+    double t = 1.0, j = 1.0, ys = 0.0, hk = 0.0;
+    for (int k = 1; k < 40; ++k) {
+      t *= -q / ((double)k * k);
+      hk += 1.0 / k;
+      j += t;
+      ys -= t * hk;
+      if (fabs(t) < 1e-18) break;
+    }
+    J = j;
+    Y = kTwoOverPi * ((log(0.5 * x) + kGamma) * j + ys);
+    return;
+  }
+  double ir = 1.0, ii = 0.0;
+  const double i2x = 0.5 / x;
+#pragma unroll 3
+  for (int k = 1; k <= kHankelNodes; ++k) {
+    const double sk = k * kHankelStep;
+    const double v = sk * sk * i2x;
+    const double r = sqrt(1.0 + v * v);
+    const double ch = sqrt(0.5 * (1.0 + 1.0 / r));
+    const double sh = (v / r) / (2.0 * ch);
+    const double rs = 1.0 / sqrt(r);
+    ir += c_hankel_w[k] * (ch * rs);
+    ii -= c_hankel_w[k] * (sh * rs);
+  }
+  const double norm = kHankelStep * 0.56418958354775628695;  // step / sqrt(pi)
+  ir *= norm;
+  ii *= norm;
+  double sx, cx;
+  sincos(x, &sx, &cx);
+  const double c = (cx + sx) * 0.70710678118654752440;  // cos(x - pi/4)
+  const double sn = (sx - cx) * 0.70710678118654752440; // sin(x - pi/4)
+  const double f = sqrt(kTwoOverPi / x);
+  J = f * (c * ir - sn * ii);
+  Y = f * (c * ii + sn * ir);
+}
+
+static void upload_hankel_weights() {
+  static bool done = false;
+  if (done) return;
+  double w[kHankelNodes + 1];
+  for (int k = 0; k <= kHankelNodes; ++k) {
+    const double sk = k * kHankelStep;
+    w[k] = 2.0 * std::exp(-sk * sk);
+  }
+  HSS_CUDA(cudaMemcpyToSymbol(c_hankel_w, w, sizeof(w)));
+  done = true;
+}
+
+// Helmholtz entry (Kernel_Eval.m:44-49): w on the diagonal, else
+// (0, s) * b(x) * (J0 + i Y0)(kh r) * c(y) with the products in MATLAB's order, which
+// for the purely imaginary (0, s b) factor is Re = -((s b) Y0) c, Im = ((s b) J0) c.
+__global__ void __launch_bounds__(256) k_kgen_complex(const KgenCP* __restrict__ D, PointView P, HelmDev k) {
+  const KgenCP d = D[blockIdx.y];
+  const long long tot = (long long)d.m * d.n;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int i = (int)(e % d.m), j = (int)(e / d.m);
+    const int t = d.ti[i], s = d.si[j];
+    const double dx = __dadd_rn(P.x[t], -P.x[s]);
+    const double dy = __dadd_rn(P.y[t], -P.y[s]);
+    const double den = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    double re, im;
+    if (den == 0.0) {
+      re = k.w_re;
+      im = k.w_im;
+    } else {
+      const double x = __dmul_rn(k.kh, sqrt(den));
+      const double sb = __dmul_rn(k.s, P.bval[t]);
+      double hj, hy;
+      hankel0(x, hj, hy);
+      re = -__dmul_rn(__dmul_rn(sb, hy), P.cval[s]);
+      im = __dmul_rn(__dmul_rn(sb, hj), P.cval[s]);
+    }
+    const size_t o = 2 * ((size_t)i + (size_t)j * d.ld);
+    d.out[o] = re;
+    d.out[o + 1] = im;
+  }
+}
+
+void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, const PointView& pts,
+                          const HelmDev& k, cudaStream_t s) {
+  if (batch <= 0 || maxEntries <= 0) return;
+  HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "kgen batch too large");
+  upload_hankel_weights();
+  const int gx = std::max(1, std::min(ceil_div(maxEntries, 256), 4096));
+  k_kgen_complex<<<dim3(gx, batch), 256, 0, s>>>(dP, pts, k);
+  check_launch("k_kgen_complex");
 }
 
 template <typename R>

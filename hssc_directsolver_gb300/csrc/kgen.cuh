@@ -44,6 +44,25 @@ inline PointView view(const PointTable& t) {
 
 // modulation f(p) = 1 + alpha*exp(-isig*|p-p0|^2) evaluated on the host
 double modulation(double alpha, double x0, double y0, double isig, double px, double py);
+// b(p) (which = 0) or c(p) (which = 1) of the kernel parameters, any HSS_MOD_* form
+double modulation(const hss_kernel_params& kp, int which, double px, double py);
+
+// Complex blocks (HSS_SL_H_2D): out[2 (i + j ld)] = Re, [+1] = Im of K(ti[i], si[j])
+struct KgenCP {
+  const int* ti;
+  const int* si;
+  int m, n;
+  double* out;
+  long long ld;
+};
+// Helmholtz constants: s = h^2 kh^2 / 4 (the imaginary factor of the off-diagonal
+// entries), w = 1 + kh^2 (i/4) dr (the diagonal)
+struct HelmDev {
+  double kh, s, w_re, w_im;
+};
+HelmDev make_helm_dev(const hss_kernel_params& kp);
+void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, const PointView& pts,
+                          const HelmDev& k, cudaStream_t s);
 
 template <typename R>
 void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const PointView& pts,

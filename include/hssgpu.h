@@ -37,6 +37,16 @@ extern "C" {
 /* ---- kernels (Common/Kernel_Eval.m) ------------------------------------ */
 #define HSS_SL_L_2D 0 /* Kernel_Eval.m:60-61, (den==0) + h^2/2 b(x) log(den) c(y) */
 #define HSS_DL_L_2D 1 /* custom-kernel slot Kernel_Eval.m:75-79: Laplace double layer */
+#define HSS_SL_H_2D 2 /* Kernel_Eval.m:44-53, complex: w (den==0) + h^2 kh^2 (i/4) b(x) H0(kh r) c(y),
+                         w = 1 + kh^2 (i/4) dr (dr = the order-4 Duan-Rokhlin weight; 0 = order 0).
+                         Evaluated by hss_kernel_eval; the HSS solvers take the real kernels. */
+
+/* modulation forms of b(x) / c(y) (hss_kernel_params.b_kind / c_kind) */
+#define HSS_MOD_GAUSS 0     /* 1 + alpha exp(-isig |p - p0|^2); alpha = 0: 1 (b_func, Kernel_Eval.m:99-108) */
+#define HSS_MOD_BUMP 1      /* Bump_function option 4 called without h (Common/Bump_function.m:53-63,
+                               shift 0): the nonsymmetric Lippmann-Schwinger b, Kernel_Eval.m:115-119 */
+#define HSS_MOD_SQRT_BUMP 2 /* sqrt(Bump_function option 4 with shift 4h): the symmetric
+                               Lippmann-Schwinger b and c, Kernel_Eval.m:129-140 */
 
 /* precision modes */
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
@@ -53,14 +63,37 @@ extern "C" {
 #define HSS_INTER_LOWRANK 1
 
 /* b(x) = 1 + b_alpha*exp(-b_isig*|x-(b_x0,b_y0)|^2), c(y) likewise; alpha = 0
- * switches a modulation off (LOCAL_get_bc, Kernel_Eval.m:98-159). */
+ * switches a modulation off (LOCAL_get_bc, Kernel_Eval.m:98-159).  b_kind / c_kind
+ * select the Lippmann-Schwinger bump forms instead (HSS_MOD_*; 0 for the Laplace kernels). */
 typedef struct hss_kernel_params {
   int32_t flag;
   int32_t pad_;
   double h;
   double b_alpha, b_x0, b_y0, b_isig;
   double c_alpha, c_x0, c_y0, c_isig;
+  double kh;           /* wavenumber (params.kh) of HSS_SL_H_2D */
+  double dr_re, dr_im; /* params.dr_weights (order 4) of HSS_SL_H_2D */
+  int32_t b_kind, c_kind; /* HSS_MOD_* */
 } hss_kernel_params;
+
+/* A = Kernel_Eval(X1, X2, params) (Common/Kernel_Eval.m:1-96) on the device, host
+ * buffers.  X1: m targets, X2: n sources, each column-major (x column, then y column).
+ * A: m x n column-major, doubles for HSS_SL_L_2D, interleaved (re, im) pairs for
+ * HSS_SL_H_2D (2 m n doubles).  HSS_DL_L_2D needs normals and weights and is not
+ * evaluated here (HSS_ERR_ARG). */
+int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, const double* X2, int64_t n,
+                    double* A);
+
+/* Duan-Rokhlin corrections of the punctured trapezoidal rule for H0(k |x|) on the grid
+ * h Z^2, host computation (the corr0 and corr1 lines of Common/FORTRAN_get_DR_weights.f,
+ * corr_hank :85-): corr = {Re corr0, Im corr0, Re corr1, Im corr1}.  |k| h < 2 pi. */
+int hss_dr_corrections(double h, double k_re, double k_im, double* corr);
+/* [J, dr_weights, iistencil] = DR_stencil(h, rk, n, order) (Common/DR_stencil.m:1-53) for
+ * order 0, 4 and 6 (8 and 10 need corr2..corr5: HSS_ERR_ARG).  *count entries (<= 5):
+ * J[e] (offset i2 + n i1), w[2e], w[2e+1] (complex weight), stencil[3e..3e+2] (the
+ * column of iistencil). */
+int hss_dr_stencil(double h, double k_re, double k_im, int64_t n, int32_t order, int32_t* count, int64_t* J,
+                   double* w, int32_t* stencil);
 
 const char* hss_last_error(void);
 int hss_version(void);
