@@ -448,10 +448,43 @@ __device__ __forceinline__ bool dfd_vec_ok(const SegGemmP& p) {
 
 constexpr int SKD_STAGES = 4;  // cp.async columns in flight per thread (<= 4 right-hand sides)
 
+// One element of a double-float copy in the pair-interleaved layout of split_df: the
+// 16-byte block holding elements (2i, 2i+1) of the array is (h_2i, h_2i+1, l_2i, l_2i+1).
+// Arrays start on 16-byte boundaries, so an element's slot follows from its address.
+__device__ __forceinline__ void dfd_elem(const float2* e, float& h, float& l) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(e);
+  const float* blk = reinterpret_cast<const float*>(a & ~(uintptr_t)15);
+  const int par = (int)((a >> 3) & 1);
+  h = __ldg(blk + par);
+  l = __ldg(blk + 2 + par);
+}
+
+// Column step of the cp.async ring: GemmP columns advance by a fixed stride, segmented
+// columns are looked up (they may cross into the next segment).
+template <typename D>
+struct DfCols {
+  const char* base;
+  size_t step;
+  __device__ __forceinline__ DfCols(const D& p, int k0, int r) {
+    if constexpr (std::is_same<D, GemmP<double>>::value) {
+      base = reinterpret_cast<const char*>(dfd_col(p, k0) + r);
+      step = (size_t)8 * p.lda * sizeof(float2);
+    } else {
+      base = nullptr;
+      step = 0;
+    }
+  }
+  // address of row r of column k0 + 8 it
+  __device__ __forceinline__ const void* at(const D& p, int k0, int it, int r) const {
+    if constexpr (std::is_same<D, GemmP<double>>::value) return base + (size_t)it * step;
+    else return dfd_col(p, k0 + 8 * it) + r;
+  }
+};
+
 template <int NR, typename D>
 __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __restrict__ P, double alpha, double beta,
                                                    int ksplit, double* __restrict__ part, int mmax) {
-  constexpr int V = 2;  // one 16-byte load = two (hi, lo) pairs
+  constexpr int V = 2;  // one 16-byte load = the (hi, hi, lo, lo) block of two rows
   constexpr int KC = (NR > 4) ? SK_KC / 2 : SK_KC;  // static shared memory under 48 KB
   constexpr int ROWS = 32 * V;
   const D p = P[blockIdx.z];
@@ -461,15 +494,27 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __
   const int Kt = dfd_K(p);
   const int kper = (((Kt + ksplit - 1) / ksplit) + 7) & ~7;
   const int kb = blockIdx.y * kper, ke = min(Kt, kb + kper);
-  __shared__ f32x2 Bh2[KC][NR], Bhn2[KC][NR], Bln2[KC][NR];
+  // per column: (bh, bh) x NR, (-bh, -bh) x NR, (-bl, -bl) x NR, read two right-hand sides
+  // per 16-byte load
+  __shared__ __align__(16) f32x2 Bs[KC][3][NR];
   __shared__ float2 red[8][NR][ROWS];
-  __shared__ __align__(16) float4 ring[(NR <= 4) ? SKD_STAGES : 1][256];
+  __shared__ __align__(16) ulonglong2 ring[(NR <= 4) ? SKD_STAGES : 1][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int r = row0 + lane * V;
   const bool vec_ok = dfd_vec_ok(p);
   f32x2 sh[NR], sl[NR];  // {row r, row r+1} accumulators
 #pragma unroll
   for (int c = 0; c < NR; ++c) { sh[c] = 0ULL; sl[c] = 0ULL; }
+  auto madd = [&](f32x2 ah, f32x2 al, const f32x2* b) {
+#pragma unroll
+    for (int c = 0; c < NR; c += 2) {
+      const ulonglong2 bh = *reinterpret_cast<const ulonglong2*>(b + c);
+      const ulonglong2 bn = *reinterpret_cast<const ulonglong2*>(b + NR + c);
+      const ulonglong2 bl = *reinterpret_cast<const ulonglong2*>(b + 2 * NR + c);
+      df_madd_x2(sh[c], sl[c], ah, al, bh.x, bn.x, bl.x);
+      df_madd_x2(sh[c + 1], sl[c + 1], ah, al, bh.y, bn.y, bl.y);
+    }
+  };
   for (int kc = kb; kc < ke; kc += KC) {
     const int kn = min(KC, ke - kc);
     __syncthreads();
@@ -478,36 +523,36 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __
       const double x = (kk < kn && c < N) ? dfd_b(p, kc + kk, c) : 0.0;
       float xh, xl;
       split_d2f(x, xh, xl);
-      Bh2[kk][c] = x2_pack(xh, xh);
-      Bhn2[kk][c] = x2_pack(-xh, -xh);
-      Bln2[kk][c] = x2_pack(-xl, -xl);
+      Bs[kk][0][c] = x2_pack(xh, xh);
+      Bs[kk][1][c] = x2_pack(-xh, -xh);
+      Bs[kk][2][c] = x2_pack(-xl, -xl);
     }
     __syncthreads();
     if constexpr (NR <= 4) {
       if (vec_ok) {
         // cp.async ring: each thread keeps its next SKD_STAGES columns' 16 bytes in
         // flight into its own shared-memory slots (it reads only what it copied, so
-        // the per-thread group wait is the only synchronisation needed)
+        // the per-thread group wait is the only synchronisation needed).  With even
+        // leading dimensions a row pair inside the matrix is a whole 16-byte block
+        // (for odd M the partner of the last row is padding of the same column).
         const int niter = (w < kn) ? (kn - w + 7) / 8 : 0;
-        const int nv = (r + V <= p.M) ? 16 : (r < p.M ? 8 : 0);
+        const int nv = (r < p.M) ? 16 : 0;
+        const DfCols<D> cols(p, kc + w, nv ? r : 0);
+        const void* dummy = dfd_col(p, kc);
+        const unsigned ring0 = (unsigned)__cvta_generic_to_shared(&ring[0][threadIdx.x]);
         auto issue = [&](int it) {
-          const int kk = w + 8 * it;
           const bool live = it < niter;
-          const float2* src = live ? dfd_col(p, kc + kk) + (nv ? r : 0) : dfd_col(p, kc);
-          const unsigned dst = (unsigned)__cvta_generic_to_shared(&ring[it % SKD_STAGES][threadIdx.x]);
-          const int bytes = live ? nv : 0;
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes));
+          const void* src = live ? cols.at(p, kc + w, it, nv ? r : 0) : dummy;
+          const unsigned dst = ring0 + (unsigned)((it % SKD_STAGES) * 256 * sizeof(ulonglong2));
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(live ? nv : 0));
           asm volatile("cp.async.commit_group;\n" ::);
         };
 #pragma unroll
         for (int it = 0; it < SKD_STAGES; ++it) issue(it);
         for (int it = 0; it < niter; ++it) {
           asm volatile("cp.async.wait_group %0;\n" ::"n"(SKD_STAGES - 1));
-          const float4 cur = ring[it % SKD_STAGES][threadIdx.x];
-          const int kk = w + 8 * it;
-          const f32x2 ah = x2_pack(cur.x, cur.z), al = x2_pack(cur.y, cur.w);
-#pragma unroll
-          for (int c = 0; c < NR; ++c) df_madd_x2(sh[c], sl[c], ah, al, Bh2[kk][c], Bhn2[kk][c], Bln2[kk][c]);
+          const ulonglong2 a = ring[it % SKD_STAGES][threadIdx.x];
+          madd(a.x, a.y, &Bs[w + 8 * it][0][0]);
           issue(it + SKD_STAGES);
         }
         asm volatile("cp.async.wait_all;\n" ::);
@@ -515,19 +560,18 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __
       }
     }
     // software-pipelined: the next column's 16 bytes are in flight during this column's math
-    auto load = [&](int kk) -> float4 {
+    auto load = [&](int kk) -> ulonglong2 {
       const float2* col = dfd_col(p, kc + kk);
-      if (vec_ok && r + V <= p.M) return __ldg(reinterpret_cast<const float4*>(col + r));
-      const float2 q0 = (r < p.M) ? __ldg(col + r) : make_float2(0.f, 0.f);
-      const float2 q1 = (r + 1 < p.M) ? __ldg(col + r + 1) : make_float2(0.f, 0.f);
-      return make_float4(q0.x, q0.y, q1.x, q1.y);
+      if (vec_ok && r < p.M) return __ldg(reinterpret_cast<const ulonglong2*>(col + r));
+      float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+      if (r < p.M) dfd_elem(col + r, h0, l0);
+      if (r + 1 < p.M) dfd_elem(col + r + 1, h1, l1);
+      return make_ulonglong2(x2_pack(h0, h1), x2_pack(l0, l1));
     };
-    float4 cur = (w < kn) ? load(w) : make_float4(0.f, 0.f, 0.f, 0.f);
+    ulonglong2 cur = (w < kn) ? load(w) : make_ulonglong2(0ULL, 0ULL);
     for (int kk = w; kk < kn; kk += 8) {
-      const float4 nxt = (kk + 8 < kn) ? load(kk + 8) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const f32x2 ah = x2_pack(cur.x, cur.z), al = x2_pack(cur.y, cur.w);
-#pragma unroll
-      for (int c = 0; c < NR; ++c) df_madd_x2(sh[c], sl[c], ah, al, Bh2[kk][c], Bhn2[kk][c], Bln2[kk][c]);
+      const ulonglong2 nxt = (kk + 8 < kn) ? load(kk + 8) : make_ulonglong2(0ULL, 0ULL);
+      madd(cur.x, cur.y, &Bs[kk][0][0]);
       cur = nxt;
     }
   }
@@ -594,17 +638,25 @@ __global__ void __launch_bounds__(256) k_skinny_reduce_df(const D* __restrict__ 
   }
 }
 
-__global__ void k_split_df(const double* __restrict__ src, float2* __restrict__ dst, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double x = src[i];
-    const float h = __double2float_rn(x);
-    dst[i] = make_float2(h, __double2float_rn(__dsub_rn(x, (double)h)));
+// Pair-interleaved float-pair copy: elements (2i, 2i+1) become the 16-byte block
+// (h_2i, h_2i+1, l_2i, l_2i+1), so a row pair of a column is one load whose halves are
+// the paired-FP32 operands directly.  An odd count leaves a zero partner in the last
+// block (dst holds n rounded up to even elements).
+__global__ void k_split_df(const double* __restrict__ src, float4* __restrict__ dst, long long n) {
+  const long long npair = (n + 1) / 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npair; i += (long long)gridDim.x * blockDim.x) {
+    const double x0 = src[2 * i];
+    const double x1 = (2 * i + 1 < n) ? src[2 * i + 1] : 0.0;
+    const float h0 = __double2float_rn(x0), h1 = __double2float_rn(x1);
+    dst[i] = make_float4(h0, h1, __double2float_rn(__dsub_rn(x0, (double)h0)), __double2float_rn(__dsub_rn(x1, (double)h1)));
   }
 }
 
 void split_df(const double* src, double* dst, long long n, cudaStream_t s) {
   if (n <= 0) return;
-  k_split_df<<<std::min(ceil_div(n, 256), 4096), 256, 0, s>>>(src, reinterpret_cast<float2*>(dst), n);
+  HSS_REQUIRE((reinterpret_cast<uintptr_t>(dst) & 15) == 0, HSS_ERR_ARG, "split_df: destination not 16-byte aligned");
+  const long long npair = (n + 1) / 2;
+  k_split_df<<<std::min(ceil_div(npair, 256), 4096), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n);
   check_launch("k_split_df");
 }
 

@@ -50,7 +50,8 @@ void gemm_batched_df(const GemmP<double>* dP, int batch, int maxM, int maxN, boo
 // K slices for gemm_skinny_split_df: enough CTAs for several waves on 152 SMs
 // (the double-float kernel does ~15x the arithmetic per byte of the FP64 one)
 int skinny_ksplit_df(int batch, int maxM, int maxK);
-// dst[i] = (hi, lo) float pair of src[i], stored in the 8 bytes of dst[i]
+// FP64 -> pair-interleaved float pairs (hi, hi, lo, lo per element pair); dst holds
+// n rounded up to even elements and starts on a 16-byte boundary
 void split_df(const double* src, double* dst, long long n, cudaStream_t s);
 
 template <typename R>

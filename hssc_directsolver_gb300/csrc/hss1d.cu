@@ -1116,7 +1116,7 @@ Plan1& HSS1D::inv_plan(int r) {
 }
 
 static void split_into(const DevBuf<double>& src, DevBuf<double>& dst, cudaStream_t s) {
-  dst.alloc(std::max<size_t>(src.n, 1));
+  dst.alloc(std::max<size_t>((src.n + 1) & ~(size_t)1, 2));  // whole (hi, hi, lo, lo) blocks
   split_df(src.p, dst.p, (long long)src.n, s);
 }
 

@@ -539,7 +539,7 @@ void HSS2D::invert_level(R* A, int n, int nb) {
 }
 
 static void split_copy(const DevBuf<double>& src, DevBuf<double>& dst, cudaStream_t s) {
-  dst.alloc(std::max<size_t>(src.n, 1));
+  dst.alloc(std::max<size_t>((src.n + 1) & ~(size_t)1, 2));  // whole (hi, hi, lo, lo) blocks
   split_df(src.p, dst.p, (long long)src.n, s);
 }
 
