@@ -605,37 +605,40 @@ __global__ void __launch_bounds__(256, (NR > 4) ? 3 : 4) k_skinny_df(const D* __
   }
 }
 
-// split-K partials of k_skinny_df (float pairs) summed in double-float arithmetic
+// split-K partials of k_skinny_df (float pairs) summed in double-float arithmetic.
+// Block (64 rows of one right-hand side of one product) x 4 slice groups: group g sums
+// the slices y = g mod 4 in order, and the four group sums are combined as
+// (0 + 1) + (2 + 3).
 template <typename D>
 __global__ void __launch_bounds__(256) k_skinny_reduce_df(const D* __restrict__ P, double alpha,
                                                           double beta, int ksplit, const double* __restrict__ part,
                                                           int mmax) {
-  const D p = P[blockIdx.y];
+  const D p = P[blockIdx.z];
+  const int c = blockIdx.y;
+  if (c >= p.N || (int)blockIdx.x * 64 >= p.M) return;
   const float2* pp = reinterpret_cast<const float2*>(part);
+  const int g = threadIdx.x >> 6, rr = threadIdx.x & 63;
+  const int row = blockIdx.x * 64 + rr;
+  __shared__ float2 gs[4][64];
+  float th = 0.f, tl = 0.f;
+  if (row < p.M) {
+#pragma unroll 4
+    for (int y = g; y < ksplit; y += 4) {
+      const float2 q = pp[(((size_t)blockIdx.z * ksplit + y) * 8 + c) * mmax + row];
+      df_add(th, tl, q.x, q.y);
+    }
+  }
+  gs[g][rr] = make_float2(th, tl);
+  __syncthreads();
+  if (g != 0 || row >= p.M) return;
+  float h0 = gs[0][rr].x, l0 = gs[0][rr].y, h2 = gs[2][rr].x, l2 = gs[2][rr].y;
+  df_add(h0, l0, gs[1][rr].x, gs[1][rr].y);
+  df_add(h2, l2, gs[3][rr].x, gs[3][rr].y);
+  df_add(h0, l0, h2, l2);
   float alh, all;
   split_d2f(alpha, alh, all);
-  for (int e = blockIdx.x * 256 + threadIdx.x; e < p.M * p.N; e += gridDim.x * 256) {
-    const int row = e % p.M, c = e / p.M;
-    // four independent running sums (slices y = j mod 4), combined in a fixed order
-    float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
-    int y = 0;
-    for (; y + 4 <= ksplit; y += 4) {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float2 q = pp[(((size_t)blockIdx.y * ksplit + y + j) * 8 + c) * mmax + row];
-        df_add(th[j], tl[j], q.x, q.y);
-      }
-    }
-    for (; y < ksplit; ++y) {
-      const float2 q = pp[(((size_t)blockIdx.y * ksplit + y) * 8 + c) * mmax + row];
-      df_add(th[y & 3], tl[y & 3], q.x, q.y);
-    }
-    df_add(th[0], tl[0], th[1], tl[1]);
-    df_add(th[2], tl[2], th[3], tl[3]);
-    df_add(th[0], tl[0], th[2], tl[2]);
-    double* cp = p.C + row + (size_t)c * p.ldc;
-    *cp = df_epilogue(th[0], tl[0], alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
-  }
+  double* cp = p.C + row + (size_t)c * p.ldc;
+  *cp = df_epilogue(h0, l0, alh, all, beta, (beta == 0.0) ? 0.0 : *cp);
 }
 
 // Pair-interleaved float-pair copy: elements (2i, 2i+1) become the 16-byte block
@@ -813,8 +816,7 @@ static void skinny_df_launch(const D* dP, int batch, int maxM, int maxN, double 
   else k_skinny_df<8, D><<<grid, 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
   check_launch("k_skinny_df");
   if (ksplit > 1) {
-    const int gx = std::max(1, std::min(ceil_div((long long)maxM * maxN, 256), 256));
-    k_skinny_reduce_df<D><<<dim3(gx, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
+    k_skinny_reduce_df<D><<<dim3(ceil_div(maxM, 64), maxN, batch), 256, 0, s>>>(dP, alpha, beta, ksplit, part, maxM);
     check_launch("k_skinny_reduce_df");
   }
 }
