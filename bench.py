@@ -373,8 +373,15 @@ def main():
         torch.cuda.synchronize()
         fwd_ms = e0.elapsed_time(e1) / args.steps
         # end to end through the C ABI with host buffers (H2D of f, D2H of x each step)
-        Fh = np.asfortranarray(F)
-        Xh = np.zeros_like(Fh)
+        # pinned host buffers: (nrhs, N) row-major storage viewed as the N x nrhs
+        # column-major arrays the C ABI takes
+        Fp = torch.empty((F.shape[1], F.shape[0]), dtype=torch.float64, pin_memory=True)
+        Xp = torch.empty((F.shape[1], F.shape[0]), dtype=torch.float64, pin_memory=True)
+        Fp.numpy()[:] = np.asarray(F).T
+        Xp.zero_()
+        Fh = Fp.numpy().T
+        Xh = Xp.numpy().T
+        assert Fh.flags.f_contiguous and Xh.flags.f_contiguous
         rr2 = C.c_double()
         it2 = C.c_int32()
         for _ in range(2):
@@ -432,7 +439,8 @@ def main():
         "applyinv_ms": {p: results[p]["applyinv_ms"] for p in results},
         "apply_fp64_ms": {p: results[p]["apply_ms"] for p in results},
         "e2e": {"value": 1.0 / r["e2e_s"] * world, "unit": "solves/s",
-                "h2d_bytes_per_step": int(N * nrhs * 8), "d2h_bytes_per_step": int(N * nrhs * 8)},
+                "h2d_bytes_per_step": int(N * nrhs * 8), "d2h_bytes_per_step": int(N * nrhs * 8),
+                "host_buffers": "pinned", "call": "hss2d_solve"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_PER_APPLYINV.get(best),
                      "kernel": {"dfloat": "k_skinny_df", "dfloat_inv": "k_skinny_df",

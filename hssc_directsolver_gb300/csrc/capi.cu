@@ -413,11 +413,12 @@ int hss1d_invert(hss1d_matrix* H) {
 static void host_roundtrip1(HSS1D* h, const double* X, double* Y, int nrhs, bool inv) {
   HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
   const size_t cnt = (size_t)h->Ntot * nrhs;
-  DevBuf<double> dX(cnt), dY(cnt);
-  HSS_CUDA(cudaMemcpyAsync(dX.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  if (inv) h->applyinv_device(dX.p, dY.p, nrhs);
-  else h->apply_device(dX.p, dY.p, nrhs);
-  HSS_CUDA(cudaMemcpyAsync(Y, dY.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  h->io_in.ensure(cnt);
+  h->io_out.ensure(cnt);
+  HSS_CUDA(cudaMemcpyAsync(h->io_in.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (inv) h->applyinv_device(h->io_in.p, h->io_out.p, nrhs);
+  else h->apply_device(h->io_in.p, h->io_out.p, nrhs);
+  HSS_CUDA(cudaMemcpyAsync(Y, h->io_out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   HSS_CUDA(cudaStreamSynchronize(h->stream));
 }
 
@@ -458,11 +459,12 @@ int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
   HSS_REQUIRE(H && H->impl && f && x && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
   HSS1D* h = H->impl;
   const size_t cnt = (size_t)h->Ntot * nrhs;
-  DevBuf<double> dF(cnt), dX(cnt);
-  HSS_CUDA(cudaMemcpyAsync(dF.p, f, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  h->io_in.ensure(cnt);
+  h->io_out.ensure(cnt);
+  HSS_CUDA(cudaMemcpyAsync(h->io_in.p, f, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int it = 0;
-  h->solve_device(dF.p, dX.p, nrhs, tol, maxit, relres, &it);
-  HSS_CUDA(cudaMemcpyAsync(x, dX.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  h->solve_device(h->io_in.p, h->io_out.p, nrhs, tol, maxit, relres, &it);
+  HSS_CUDA(cudaMemcpyAsync(x, h->io_out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   HSS_CUDA(cudaStreamSynchronize(h->stream));
   if (iters) *iters = it;
   HSS_CATCH
@@ -565,12 +567,13 @@ static void host_roundtrip(HSS2D* h, const double* X, double* Y, int nrhs, int w
                            double* relres, int* iters) {
   HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
   const size_t cnt = (size_t)h->geo.N * nrhs;
-  DevBuf<double> dX(cnt), dY(cnt);
-  HSS_CUDA(cudaMemcpyAsync(dX.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  if (which == 0) h->apply_device(dX.p, dY.p, nrhs, h->stream);
-  else if (which == 1) h->applyinv_device(dX.p, dY.p, nrhs, h->stream);
-  else h->solve_device(dX.p, dY.p, nrhs, tol, maxit, relres, iters, h->stream);
-  HSS_CUDA(cudaMemcpyAsync(Y, dY.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  h->io_in.ensure(cnt);
+  h->io_out.ensure(cnt);
+  HSS_CUDA(cudaMemcpyAsync(h->io_in.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (which == 0) h->apply_device(h->io_in.p, h->io_out.p, nrhs, h->stream);
+  else if (which == 1) h->applyinv_device(h->io_in.p, h->io_out.p, nrhs, h->stream);
+  else h->solve_device(h->io_in.p, h->io_out.p, nrhs, tol, maxit, relres, iters, h->stream);
+  HSS_CUDA(cudaMemcpyAsync(Y, h->io_out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   HSS_CUDA(cudaStreamSynchronize(h->stream));
 }
 

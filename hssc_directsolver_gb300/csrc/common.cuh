@@ -119,6 +119,26 @@ struct DevBuf {
   }
 };
 
+// Grow-only pinned host block (small device->host reads without pageable staging).
+struct PinnedBuf {
+  double* p = nullptr;
+  size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void ensure(size_t cnt) {
+    if (n >= cnt) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    HSS_CUDA(cudaMallocHost(&p, cnt * sizeof(double)));
+    n = cnt;
+  }
+};
+
 template <typename T>
 inline void download(std::vector<T>& h, const T* d, size_t cnt, cudaStream_t s) {
   h.resize(cnt);

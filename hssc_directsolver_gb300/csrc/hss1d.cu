@@ -1305,16 +1305,18 @@ void HSS1D::solve_device(const double* df, double* dx, int nrhs, double tol, int
   DevBuf<double>& res = ir_res;
   DevBuf<double>& dd = ir_dd;
   const int gx = 256;
-  DevBuf<double> part((size_t)gx * nrhs * 2);
+  ir_part.ensure((size_t)gx * nrhs * 2);
+  ir_host.ensure((size_t)gx * nrhs * 2);
+  const double* hp = ir_host.p;
   applyinv_device(df, dx, nrhs);
   int used = 1;
   double worst = 0.0;
   while (true) {
     apply_device(dx, y.p, nrhs);
-    k_res1<<<gx, 256, 0, stream>>>(Ntot, nrhs, df, y.p, res.p, part.p);
+    k_res1<<<gx, 256, 0, stream>>>(Ntot, nrhs, df, y.p, res.p, ir_part.p);
     check_launch("k_res1");
-    std::vector<double> hp;
-    download(hp, part.p, (size_t)gx * nrhs * 2, stream);
+    HSS_CUDA(cudaMemcpyAsync(ir_host.p, ir_part.p, (size_t)gx * nrhs * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                             stream));
     HSS_CUDA(cudaStreamSynchronize(stream));
     worst = 0.0;
     for (int c = 0; c < nrhs; ++c) {

@@ -76,6 +76,9 @@ struct HSS1D {
   bool inverted = false;
   // solve workspaces, staging (Ntot x 8) and cached plans / graphs per RHS count
   DevBuf<double> v1, v2, v3, Xs, Ys, ir_y, ir_res, ir_dd;
+  // host-buffer entry points: device copies of the caller's vectors; refinement partials
+  DevBuf<double> io_in, io_out, ir_part;
+  PinnedBuf ir_host;
   std::map<int, Plan1> inv_plans, fwd_plans;
   GraphCache g_inv, g_fwd;
   bool use_graphs = true;

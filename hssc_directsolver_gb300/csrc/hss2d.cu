@@ -884,7 +884,10 @@ void HSS2D::solve_device(const double* df, double* dx, int nrhs, double tol, int
   Rd.ensure((size_t)N * 8);
   Dd.ensure((size_t)N * 8);
   const int gx = 256;
-  DevBuf<double> part((size_t)gx * 8 * 2);
+  ir_part.ensure((size_t)gx * 8 * 2);
+  ir_host.ensure((size_t)gx * 8 * 2);
+  double* part_d = ir_part.p;
+  const double* hp = ir_host.p;
   double worst_all = 0.0;
   int used_all = 0;
   for (int c0 = 0; c0 < nrhs; c0 += 8) {
@@ -899,9 +902,9 @@ void HSS2D::solve_device(const double* df, double* dx, int nrhs, double tol, int
       // res = f - A x
       HSS_CUDA(cudaMemcpyAsync(Xd.p, x, (size_t)N * r * sizeof(double), cudaMemcpyDeviceToDevice, stream));
       apply_stage(r);
-      k_residual<<<gx, 256, 0, stream>>>(N, r, f, N, Yd.p, N, Rd.p, N, part.p);
-      std::vector<double> hp;
-      download(hp, part.p, (size_t)gx * r * 2, stream);
+      k_residual<<<gx, 256, 0, stream>>>(N, r, f, N, Yd.p, N, Rd.p, N, part_d);
+      HSS_CUDA(cudaMemcpyAsync(ir_host.p, part_d, (size_t)gx * r * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                               stream));
       HSS_CUDA(cudaStreamSynchronize(stream));
       worst = 0.0;
       for (int c = 0; c < r; ++c) {

@@ -81,6 +81,9 @@ struct HSS2D {
   bool tree_built = false, compressed = false, inverted = false;
   // staging (N x 8): FP64 in/out, FP32 in/out, residual, correction
   DevBuf<double> Xd, Yd, Rd, Dd;
+  // host-buffer entry points: device copies of the caller's vectors; refinement partials
+  DevBuf<double> io_in, io_out, ir_part;
+  PinnedBuf ir_host;
   DevBuf<float> Xf, Yf;
   std::map<int, SolvePlan<double>> inv_plans_d;
   std::map<int, SolvePlan<float>> inv_plans_f;
