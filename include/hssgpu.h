@@ -52,8 +52,9 @@ extern "C" {
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
 #define HSS_PREC_MIXED 1 /* FP32 inverse factors; least-squares updates and the refinement's
                             forward products in double-float; FP64 refinement residual */
-#define HSS_PREC_DFLOAT 2 /* FP64 factors; solve products in paired FP32 arithmetic (~2^-48),
-                             FP64 refinement against the forward operator */
+#define HSS_PREC_DFLOAT 2 /* FP64 inversion; the interpolation least squares' trailing updates and
+                             the solve products in paired FP32 arithmetic (~2^-48); FP64
+                             refinement against the forward operator */
 #define HSS_PREC_DFLOAT_INV 3 /* HSS_PREC_DFLOAT plus the inversion's and the least squares'
                                  trailing updates and products in paired FP32 (factors ~5 bits
                                  short of FP64; refinement restores the residual) */
