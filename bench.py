@@ -216,6 +216,37 @@ def bench_batched(args, L, dev):
             "solve_ms_by_path": {p: out[p][0] for p in out}, "dtype": "f64"}
 
 
+def bench_kernel_gen(L, dev, m=8192, n=8192, reps=3):
+    """Kernel_Eval throughput (entries/s) on device buffers: the Laplace log kernel and the
+    complex Lippmann-Schwinger kernel (H0 with the order-4 Duan-Rokhlin diagonal)."""
+    import torch
+    from hssc_directsolver_gb300 import kernels as GK
+    rng = np.random.default_rng(0)
+    X1 = torch.tensor(rng.uniform(-1, 1, (2, m)), dtype=torch.float64, device=dev)  # x row, y row
+    X2 = torch.tensor(rng.uniform(-1, 1, (2, n)), dtype=torch.float64, device=dev)
+    out = {}
+    for name, k in (("SL_L_2D", GK.Kernel("SL_L_2D", 2.0 / 256, GK.Modulation(0.25, 0.3, 0.6, 1.0))),
+                    ("SL_H_2D", GK.helmholtz_kernel(20.0, 0, 8, 32, 0))):
+        A = torch.empty((2 if name == "SL_H_2D" else 1) * m * n, dtype=torch.float64, device=dev)
+        kp = k.to_c()
+        sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        call = lambda: L.check(L.lib().hss_kernel_eval_device(C.byref(kp), L.ptr(X1), m, L.ptr(X2), n,  # noqa: E731
+                                                             L.ptr(A), sp))
+        call()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        out[name] = {"entries_per_s": m * n / dt, "ms": dt * 1e3,
+                     "bytes_written_gbs": A.numel() * 8 / dt / 1e9}
+        del A
+    out["block"] = f"{m} x {n} random points in [-1,1]^2, kh = 20 for SL_H_2D, FP64 entries"
+    out["bound"] = "fp64 pipe (log / series and Hankel-integral H0 in FP64); call includes the point upload"
+    return out
+
+
 def bench_config5(args, L, dev):
     """The learned-rank configuration at scale: 2048 double-layer curves (N log-uniform in
     [2048, 32768], ~23 M points) compressed plainly and with the rank MLP trained on the
@@ -405,6 +436,7 @@ def main():
     batched = None
     if not args.no_batched:
         batched = bench_batched(args, L, dev)
+    kgen = bench_kernel_gen(L, dev) if rank == 0 else None
 
     ok = [p for p in results if results[p]["relres"] <= 1e-10]
     best = min(ok, key=lambda p: results[p]["solve_ms"]) if ok else next(iter(results))
@@ -453,6 +485,8 @@ def main():
     }
     if batched is not None:
         line["batched_hss1d"] = batched
+    if kgen is not None:
+        line["kernel_gen"] = kgen
     if args.config5:
         line["config5"] = bench_config5(args, L, dev)
     if rank == 0 and not args.no_cpu_baseline:

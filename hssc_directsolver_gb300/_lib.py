@@ -74,6 +74,7 @@ SIGNATURES = {
     "hss1d_compress": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                  C.POINTER(hss_kernel_params), C.c_uint64]),
     "hss_kernel_eval": (C.c_int, [C.POINTER(hss_kernel_params), _DP, C.c_int64, _DP, C.c_int64, _DP]),
+    "hss_kernel_eval_device": (C.c_int, [C.POINTER(hss_kernel_params), _P, C.c_int64, _P, C.c_int64, _P, _P]),
     "hss_dr_corrections": (C.c_int, [C.c_double, C.c_double, C.c_double, _DP]),
     "hss_dr_stencil": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int64, C.c_int32, _I32P, _I64P, _DP,
                                  _I32P]),

@@ -76,10 +76,10 @@ const char* hss_last_error(void) { return hss::g_last_error.c_str(); }
 
 int hss_version(void) { return 100; }
 
-int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, const double* X2, int64_t n,
-                    double* A) {
-  HSS_TRY
-  HSS_REQUIRE(kp && X1 && X2 && A && m > 0 && n > 0, HSS_ERR_ARG, "kernel_eval: bad arguments");
+// Kernel_Eval on device buffers: points (x column, y column) already on the device.
+static void kernel_eval_device(const hss_kernel_params* kp, const double* dX1, int64_t m, const double* dX2,
+                               int64_t n, double* dA, cudaStream_t s) {
+  HSS_REQUIRE(kp && dX1 && dX2 && dA && m > 0 && n > 0, HSS_ERR_ARG, "kernel_eval: bad arguments");
   HSS_REQUIRE(m + n <= (int64_t)INT32_MAX, HSS_ERR_ARG, "kernel_eval: too many points");
   const bool cplx = kp->flag == HSS_SL_H_2D;
   HSS_REQUIRE(kp->flag == HSS_SL_L_2D || cplx, HSS_ERR_ARG,
@@ -89,37 +89,60 @@ int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, co
     HSS_REQUIRE(std::isfinite(kp->kh) && kp->kh > 0 && std::isfinite(kp->dr_re) && std::isfinite(kp->dr_im),
                 HSS_ERR_ARG, "kernel_eval: kh must be positive and the DR weight finite");
   require_device();
+  const size_t np = (size_t)(m + n);
+  std::vector<double> hx(np), hy(np), zero(np, 0.0);
+  HSS_CUDA(cudaMemcpyAsync(hx.data(), dX1, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaMemcpyAsync(hy.data(), dX1 + m, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaMemcpyAsync(hx.data() + m, dX2, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaMemcpyAsync(hy.data() + m, dX2 + n, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaStreamSynchronize(s));
+  // the point table carries the modulations b(x), c(y), evaluated on the host
+  PointTable T;
+  T.upload(hx, hy, zero, zero, zero, zero, *kp, s);
+  std::vector<int> ids(np);
+  std::iota(ids.begin(), ids.end(), 0);
+  DevBuf<int> dids(np);
+  dids.upload(ids, s);
+  if (cplx) {
+    KgenCP P{dids.p, dids.p + m, (int)m, (int)n, dA, (long long)m};
+    DevBuf<KgenCP> dP(1);
+    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, s));
+    kgen_complex_batched(dP.p, 1, m * n, view(T), make_helm_dev(*kp), s);
+  } else {
+    KgenP<double> P{dids.p, dids.p + m, (int)m, (int)n, dA, (int)m, 0};
+    DevBuf<KgenP<double>> dP(1);
+    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, s));
+    kgen_batched<double>(dP.p, 1, m * n, view(T), make_kernel_dev(*kp), s);
+  }
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, const double* X2, int64_t n,
+                    double* A) {
+  HSS_TRY
+  HSS_REQUIRE(kp && X1 && X2 && A && m > 0 && n > 0, HSS_ERR_ARG, "kernel_eval: bad arguments");
+  HSS_REQUIRE(kp->flag == HSS_SL_L_2D || kp->flag == HSS_SL_H_2D, HSS_ERR_ARG,
+              "kernel_eval: HSS_SL_L_2D or HSS_SL_H_2D (the double layer needs normals and weights)");
+  require_device();
   struct Stream {
     cudaStream_t s = nullptr;
     Stream() { HSS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
     ~Stream() { cudaStreamDestroy(s); }
   } st;
-  const size_t np = (size_t)(m + n);
-  std::vector<double> hx(np), hy(np), zero(np, 0.0);
-  for (int64_t i = 0; i < m; ++i) { hx[i] = X1[i]; hy[i] = X1[m + i]; }
-  for (int64_t j = 0; j < n; ++j) { hx[m + j] = X2[j]; hy[m + j] = X2[n + j]; }
-  PointTable T;
-  T.upload(hx, hy, zero, zero, zero, zero, *kp, st.s);
-  std::vector<int> ids(np);
-  std::iota(ids.begin(), ids.end(), 0);
-  DevBuf<int> dids(np);
-  dids.upload(ids, st.s);
-  const size_t cnt = (size_t)m * (size_t)n * (cplx ? 2 : 1);
-  DevBuf<double> out(cnt);
-  if (cplx) {
-    KgenCP P{dids.p, dids.p + m, (int)m, (int)n, out.p, (long long)m};
-    DevBuf<KgenCP> dP(1);
-    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, st.s));
-    kgen_complex_batched(dP.p, 1, m * n, view(T), make_helm_dev(*kp), st.s);
-  } else {
-    HSS_REQUIRE(m <= (int64_t)INT32_MAX, HSS_ERR_ARG, "kernel_eval: m too large");
-    KgenP<double> P{dids.p, dids.p + m, (int)m, (int)n, out.p, (int)m, 0};
-    DevBuf<KgenP<double>> dP(1);
-    HSS_CUDA(cudaMemcpyAsync(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice, st.s));
-    kgen_batched<double>(dP.p, 1, m * n, view(T), make_kernel_dev(*kp), st.s);
-  }
+  const size_t cnt = (size_t)m * (size_t)n * (kp->flag == HSS_SL_H_2D ? 2 : 1);
+  DevBuf<double> dX1(2 * (size_t)m), dX2(2 * (size_t)n), out(cnt);
+  HSS_CUDA(cudaMemcpyAsync(dX1.p, X1, 2 * m * sizeof(double), cudaMemcpyHostToDevice, st.s));
+  HSS_CUDA(cudaMemcpyAsync(dX2.p, X2, 2 * n * sizeof(double), cudaMemcpyHostToDevice, st.s));
+  kernel_eval_device(kp, dX1.p, m, dX2.p, n, out.p, st.s);
   HSS_CUDA(cudaMemcpyAsync(A, out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, st.s));
   HSS_CUDA(cudaStreamSynchronize(st.s));
+  HSS_CATCH
+}
+
+int hss_kernel_eval_device(const hss_kernel_params* kp, const double* d_X1, int64_t m, const double* d_X2, int64_t n,
+                           double* d_A, void* stream) {
+  HSS_TRY
+  kernel_eval_device(kp, d_X1, m, d_X2, n, d_A, as_stream(stream));
   HSS_CATCH
 }
 

@@ -84,6 +84,9 @@ typedef struct hss_kernel_params {
  * evaluated here (HSS_ERR_ARG). */
 int hss_kernel_eval(const hss_kernel_params* kp, const double* X1, int64_t m, const double* X2, int64_t n,
                     double* A);
+/* the same on device buffers (d_A: m n or 2 m n doubles); returns after the stream's work */
+int hss_kernel_eval_device(const hss_kernel_params* kp, const double* d_X1, int64_t m, const double* d_X2, int64_t n,
+                           double* d_A, void* stream);
 
 /* Duan-Rokhlin corrections of the punctured trapezoidal rule for H0(k |x|) on the grid
  * h Z^2, host computation (the corr0 and corr1 lines of Common/FORTRAN_get_DR_weights.f,

@@ -85,3 +85,23 @@ def test_kernel_eval_argument_errors():
         GK.Kernel_Eval(T, S, GK.Kernel("SL_H_2D", 0.1, kh=0.0))
     with pytest.raises(L.HSSError):
         GK.Kernel_Eval(T, S, GK.Kernel("SL_H_2D", 0.1, kh=5.0, b=GK.Modulation(kind=7)))
+
+
+def test_kernel_eval_device_matches_host_entry():
+    import torch
+    from hssc_directsolver_gb300 import _lib as L, kernels as GK
+    T, S = _points()
+    for k in (GK.Kernel("SL_L_2D", 2.0 / 32, GK.Modulation(0.25, 0.3, 0.6, 1.0)),
+              GK.helmholtz_kernel(8 * math.pi, 0, 8, 4, 0)):
+        A = GK.Kernel_Eval(T, S, k)
+        d1 = torch.tensor(np.ascontiguousarray(T.T), device="cuda")
+        d2 = torch.tensor(np.ascontiguousarray(S.T), device="cuda")
+        cplx = k.flag_pot == "SL_H_2D"
+        dA = torch.empty((2 if cplx else 1) * len(T) * len(S), dtype=torch.float64, device="cuda")
+        kp = k.to_c()
+        import ctypes as C
+        L.check(L.lib().hss_kernel_eval_device(C.byref(kp), L.ptr(d1), len(T), L.ptr(d2), len(S), L.ptr(dA),
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        got = dA.cpu().numpy()
+        got = got.view(np.complex128).reshape(A.shape, order="F") if cplx else got.reshape(A.shape, order="F")
+        assert np.array_equal(got, A)
