@@ -528,6 +528,37 @@ int hss1d_transforminv(hss1d_matrix* H, hss1d_matrix** out) {
   HSS_CATCH
 }
 
+int hss1d_transpose(const hss1d_matrix* H, hss1d_matrix** out) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && out, HSS_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* k = new hss1d_matrix{nullptr};
+  try {
+    k->impl = new HSS1D();
+    H->impl->transpose(*k->impl);
+  } catch (...) {
+    delete k->impl;
+    delete k;
+    throw;
+  }
+  *out = k;
+  HSS_CATCH
+}
+
+int hss1d_scalarmult(hss1d_matrix* H, double c) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->scalarmult(c);
+  HSS_CATCH
+}
+
+int hss1d_dense_matrix(hss1d_matrix* H, int32_t prob, double* Kd) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->dense_matrix(prob, Kd);
+  HSS_CATCH
+}
+
 int hss1d_set_precision(hss1d_matrix* H, int32_t precision) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

@@ -680,6 +680,103 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
 // Linv/Rinv become [I; T] form through P = Linv(J_UP(1:k),:) and Q = Rinv(:,J_DN(1:k)), whose
 // factors move into the parent's rows and columns (:83-125); (3) the parents' off-diagonal
 // blocks become sibling matrices and the leaves' Dinv the self blocks (:128-161).
+// ---------------------------------------------------------------------------
+// HSS1D algebra (HSS1D/HSS1D_transpose.m, HSS1D_scalarmult.m, HSS1D_dense_matrix.m)
+// ---------------------------------------------------------------------------
+// A^T in the same format: the up and down skeletons and interpolation matrices trade
+// places, every leaf's M_SELF is transposed, and each sibling pair's M_SIB blocks are
+// swapped and transposed (HSS1D_transpose.m:24-50).
+void HSS1D::transpose(HSS1D& K) const {
+  K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;
+  K.pN = pN; K.pbase = pbase; K.proot = proot; K.pseed = pseed;
+  K.prob = prob; K.level = level; K.parent = parent; K.c1 = c1; K.c2 = c2; K.off = off; K.cnt = cnt;
+  K.nskel = nskel; K.kskel = kskel;
+  K.I_SKUP = I_SKDN; K.I_SKDN = I_SKUP;
+  K.J_UP = J_DN; K.J_DN = J_UP;
+  K.X = X; K.kp = kp; K.kdev = kdev; K.census = census;
+  K.oT = oT; K.oSelf = oSelf; K.oSib = oSib; K.oJ = oJ;
+  K.inverted = false;
+  const cudaStream_t st = stream;
+  auto copy = [&](DevBuf<double>& dst, const DevBuf<double>& src) {
+    dst.alloc(std::max<size_t>(src.n, 1));
+    if (src.n) HSS_CUDA(cudaMemcpyAsync(dst.p, src.p, src.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  };
+  copy(K.T_UP, T_DN);
+  copy(K.T_DN, T_UP);
+  K.TDNT.alloc(std::max<size_t>(TDNT.n, 1));
+  K.M_SELF.alloc(std::max<size_t>(M_SELF.n, 1));
+  K.M_SIB.alloc(std::max<size_t>(M_SIB.n, 1));
+  K.JUPd.alloc(std::max<size_t>(JDNd.n, 1));
+  K.JDNd.alloc(std::max<size_t>(JUPd.n, 1));
+  if (JDNd.n) HSS_CUDA(cudaMemcpyAsync(K.JUPd.p, JDNd.p, JDNd.n * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  if (JUPd.n) HSS_CUDA(cudaMemcpyAsync(K.JDNd.p, JUPd.p, JUPd.n * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  std::vector<MoveP> mv;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0) {
+      const int n = nskel[b], k = kskel[b];
+      // the transposed operator's T_DN^T is this operator's T_UP^T
+      if (k > 0 && n - k > 0) mv.push_back(MoveP{T_UP.p + oT[b], K.TDNT.p + oT[b], nullptr, k, n - k, k, n - k, 3, 0});
+      if (is_leaf(b)) mv.push_back(MoveP{M_SELF.p + oSelf[b], K.M_SELF.p + oSelf[b], nullptr, cnt[b], cnt[b], cnt[b],
+                                         cnt[b], 3, 0});
+    }
+    if (c1[b] >= 0 && c2[b] >= 0) {
+      const int s1 = c1[b], s2 = c2[b], k1 = kskel[s1], k2 = kskel[s2];
+      if (k1 > 0 && k2 > 0) {
+        mv.push_back(MoveP{M_SIB.p + oSib[s2], K.M_SIB.p + oSib[s1], nullptr, k2, k1, k2, k1, 3, 0});
+        mv.push_back(MoveP{M_SIB.p + oSib[s1], K.M_SIB.p + oSib[s2], nullptr, k1, k2, k1, k2, 3, 0});
+      }
+    }
+  }
+  run_moves(mv, st);
+  HSS_CUDA(cudaStreamSynchronize(st));
+}
+
+// E(row0 + c, c) = 1 for c < r (E: ld x r, zeroed)
+__global__ void k_unit_cols(double* __restrict__ E, long long ld, long long row0, int r) {
+  for (int c = threadIdx.x; c < r; c += blockDim.x) E[(size_t)c * ld + row0 + c] = 1.0;
+}
+
+__global__ void k_scale(double* __restrict__ p, long long n, double c) {
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += (long long)gridDim.x * 256) p[i] *= c;
+}
+
+// c * A: the leaf self blocks and the sibling blocks scale, the interpolation matrices
+// do not (HSS1D_scalarmult.m:19-33).  The inverse factors no longer apply.
+void HSS1D::scalarmult(double c) {
+  HSS_REQUIRE(std::isfinite(c), HSS_ERR_ARG, "scalarmult: c must be finite");
+  for (DevBuf<double>* b : {&M_SELF, &M_SIB}) {
+    if (b->n == 0) continue;
+    k_scale<<<std::max(1, std::min(ceil_div((long long)b->n, 256), 4096)), 256, 0, stream>>>(b->p, (long long)b->n, c);
+    check_launch("k_scale");
+  }
+  inverted = false;
+  clear_plans();
+  if (dfm()) make_df();
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+// The dense matrix the compressed form represents, column block by column block: the
+// forward apply of identity columns, the rows of problem p kept.  (The reference builds
+// it from the telescoping factors, HSS1D_dense_matrix.m:17-92; both are the same matrix.)
+void HSS1D::dense_matrix(int p, double* Kd) {
+  HSS_REQUIRE(p >= 0 && p < nprob, HSS_ERR_ARG, "dense_matrix: problem index out of range");
+  HSS_REQUIRE(Kd != nullptr, HSS_ERR_ARG, "dense_matrix: NULL output");
+  const long long Np = pN[p], base = pbase[p];
+  const int blk = 64;
+  DevBuf<double> E((size_t)Ntot * blk), Y((size_t)Ntot * blk);
+  for (long long j0 = 0; j0 < Np; j0 += blk) {
+    const int r = (int)std::min<long long>(blk, Np - j0);
+    HSS_CUDA(cudaMemsetAsync(E.p, 0, (size_t)Ntot * r * sizeof(double), stream));
+    k_unit_cols<<<1, 64, 0, stream>>>(E.p, Ntot, base + j0, r);
+    check_launch("k_unit_cols");
+    apply_device(E.p, Y.p, r);
+    HSS_CUDA(cudaMemcpy2DAsync(Kd + (size_t)j0 * Np, (size_t)Np * sizeof(double), Y.p + base,
+                               (size_t)Ntot * sizeof(double), (size_t)Np * sizeof(double), (size_t)r,
+                               cudaMemcpyDeviceToHost, stream));
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+}
+
 void HSS1D::transforminv(HSS1D& K) {
   HSS_REQUIRE(inverted, HSS_ERR_STATE, "transforminv needs the inverse factors (call invert first)");
   K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;

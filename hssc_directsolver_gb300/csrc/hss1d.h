@@ -120,6 +120,12 @@ struct HSS1D {
   void invert();
   // K = the inverse in compressed format (HSS1D_transforminv_nsym)
   void transforminv(HSS1D& K);
+  // K = the transpose in compressed format (HSS1D_transpose)
+  void transpose(HSS1D& K) const;
+  // M_SELF and M_SIB scaled by c in place (HSS1D_scalarmult); the inverse is dropped
+  void scalarmult(double c);
+  // the dense N_p x N_p matrix of problem p, column-major host array (HSS1D_dense_matrix)
+  void dense_matrix(int p, double* Kd);
   void applyinv_device(const double* dX, double* dY, int nrhs);
   void apply_device(const double* dX, double* dY, int nrhs);
   void solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres, int* iters);

@@ -196,6 +196,35 @@ def HSS1D_transforminv_nsym(K_HSS: HSS1DMatrix, HSSinv=None, FTinv=None) -> HSS1
     return K
 
 
+def HSS1D_transpose(A_HSS: HSS1DMatrix) -> HSS1DMatrix:
+    """At_HSS = HSS1D_transpose(A_HSS) (HSS1D/HSS1D_transpose.m:1): the transpose in compressed
+    form, as a new (not inverted) matrix."""
+    h = C.c_void_p()
+    L.check(L.lib().hss1d_transpose(A_HSS._h, C.byref(h)))
+    K = HSS1DMatrix(h, A_HSS.N)
+    if hasattr(A_HSS, "sizes"):
+        K.sizes = A_HSS.sizes
+    return K
+
+
+def HSS1D_scalarmult(c: float, A_HSS: HSS1DMatrix) -> HSS1DMatrix:
+    """A = HSS1D_scalarmult(c, A) (HSS1D/HSS1D_scalarmult.m:1).  The matrix is scaled in place
+    (and returned); its inverse factors are dropped, so invert again before applyinv."""
+    L.check(L.lib().hss1d_scalarmult(A_HSS._h, float(c)))
+    A_HSS.inverted = False
+    return A_HSS
+
+
+def HSS1D_dense_matrix(K_HSS: HSS1DMatrix, sym: int = 0, prob: int = 0) -> np.ndarray:
+    """Kd = HSS1D_dense_matrix(K_HSS, sym) (HSS1D/HSS1D_dense_matrix.m:1): the dense matrix of
+    problem ``prob`` (0 for a single curve).  ``sym`` is implied by the handle."""
+    sizes = getattr(K_HSS, "sizes", [K_HSS.N])
+    n = sizes[prob]
+    Kd = np.zeros((n, n), order="F")
+    L.check(L.lib().hss1d_dense_matrix(K_HSS._h, int(prob), L.ptr(Kd)))
+    return Kd
+
+
 def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
     q = _as_f64(qq)
     vec = q.ndim == 1

@@ -159,6 +159,16 @@ int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
                 double* relres, int32_t* iters);
 int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
+/* At_HSS = HSS1D_transpose(A_HSS) (HSS1D/HSS1D_transpose.m:1): a new handle holding the
+ * transpose in compressed form (up/down skeletons and T swapped, M_SELF transposed, sibling
+ * blocks swapped and transposed); not inverted. */
+int hss1d_transpose(const hss1d_matrix* A, hss1d_matrix** At);
+/* A = HSS1D_scalarmult(c, A) (HSS1D/HSS1D_scalarmult.m:1), in place: M_SELF and M_SIB are
+ * scaled by c; the handle's inverse is dropped (invert again before applyinv). */
+int hss1d_scalarmult(hss1d_matrix* A, double c);
+/* Kd = HSS1D_dense_matrix(K_HSS) (HSS1D/HSS1D_dense_matrix.m:1) for problem prob of the
+ * handle: N_p x N_p column-major host array (N_p from hss1d_forest_info). */
+int hss1d_dense_matrix(hss1d_matrix* A, int32_t prob, double* Kd);
 /* arithmetic of the solve products: HSS_PREC_FP64 (default), HSS_PREC_DFLOAT (float-pair
  * copies of the FP64 operators, products on the FP32 pipes, ~2^-48 per product) or
  * HSS_PREC_DFLOAT_INV (also the following hss1d_invert's updates and products) */

@@ -527,3 +527,78 @@ def transforminv_nsym(H: HSS1DMatrix, inv: dict) -> HSS1DMatrix:
 
 def dense_from_points(X, kp):
     return kernel_eval(X, X, kp)
+
+
+def transpose(H: HSS1DMatrix) -> HSS1DMatrix:
+    """At_HSS = HSS1D_transpose(A_HSS), HSS1D/HSS1D_transpose.m:24-50: up/down skeletons and
+    interpolation matrices swap, M_SELF is transposed, sibling blocks swap and transpose."""
+    t = H.tree
+    nb = t.nboxes
+    At = HSS1DMatrix(tree=t, nskel=list(H.nskel), kskel=list(H.kskel),
+                     I_SKUP=list(H.I_SKDN), I_SKDN=list(H.I_SKUP),
+                     T_UP=list(H.T_DN), J_UP=list(H.J_DN), T_DN=list(H.T_UP), J_DN=list(H.J_UP),
+                     M_SELF=[None if m is None else np.array(m).T.copy() for m in H.M_SELF],
+                     M_SIB=list(H.M_SIB), census=list(H.census))
+    for b in range(nb):
+        s1, s2 = t.c1[b], t.c2[b]
+        if s1 >= 0 and s2 >= 0:
+            At.M_SIB[s1] = np.array(H.M_SIB[s2]).T.copy()
+            At.M_SIB[s2] = np.array(H.M_SIB[s1]).T.copy()
+    return At
+
+
+def scalarmult(c: float, H: HSS1DMatrix) -> HSS1DMatrix:
+    """A = HSS1D_scalarmult(c, A), HSS1D/HSS1D_scalarmult.m:19-33 (a scaled copy)."""
+    t = H.tree
+    A = HSS1DMatrix(tree=t, nskel=list(H.nskel), kskel=list(H.kskel), I_SKUP=list(H.I_SKUP),
+                    I_SKDN=list(H.I_SKDN), T_UP=list(H.T_UP), J_UP=list(H.J_UP), T_DN=list(H.T_DN),
+                    J_DN=list(H.J_DN), M_SELF=list(H.M_SELF), M_SIB=list(H.M_SIB), census=list(H.census))
+    for b in range(t.nboxes):
+        s1, s2 = t.c1[b], t.c2[b]
+        if s1 >= 0 and s2 >= 0:
+            A.M_SIB[s1] = c * np.asarray(H.M_SIB[s1])
+            A.M_SIB[s2] = c * np.asarray(H.M_SIB[s2])
+        if t.is_leaf(b) and H.M_SELF[b] is not None:
+            A.M_SELF[b] = c * np.asarray(H.M_SELF[b])
+    return A
+
+
+def dense_matrix(H: HSS1DMatrix) -> np.ndarray:
+    """Kd = HSS1D_dense_matrix(K_HSS, sym), HSS1D/HSS1D_dense_matrix.m:17-92: leaves to root,
+    Rho_b (k x points) maps a box's points to its up skeleton and Lambda_b (points x k) its
+    down skeleton to its points; each sibling pair fills Kd(ind1, ind2) =
+    Lambda_1 M_SIB_1 Rho_2 and Kd(ind2, ind1) = Lambda_2 M_SIB_2 Rho_1.
+
+    A parent's Lambda uses the down interpolation (T_DN, J_DN); the reference's nsym branch
+    (:58-61) passes T_UP / J_UP there, which only agrees when T_DN = T_UP (fsym)."""
+    t = H.tree
+    nb = t.nboxes
+    Rho = [None] * nb
+    Lam = [None] * nb
+    sl = lambda b: slice(int(t.off[b]), int(t.off[b] + t.cnt[b]))  # noqa: E731
+    Kd = np.zeros((int(t.cnt[0]), int(t.cnt[0])))
+    for b in range(nb - 1, -1, -1):
+        if t.is_leaf(b):
+            Kd[sl(b), sl(b)] = H.M_SELF[b]
+            if b == 0:
+                continue
+            I = np.eye(int(t.cnt[b]))
+            Rho[b] = _skel_proj(H.T_UP[b], H.J_UP[b], I)
+            Lam[b] = _skel_proj(H.T_DN[b], H.J_DN[b], I).T
+            continue
+        s1, s2 = t.c1[b], t.c2[b]
+        Kd[sl(s1), sl(s2)] = Lam[s1] @ H.M_SIB[s1] @ Rho[s2]
+        Kd[sl(s2), sl(s1)] = Lam[s2] @ H.M_SIB[s2] @ Rho[s1]
+        if b == 0:
+            continue
+        n1, n2 = Rho[s1].shape[1], Rho[s2].shape[1]
+        k1, k2 = Rho[s1].shape[0], Rho[s2].shape[0]
+        Rc = np.zeros((k1 + k2, n1 + n2))
+        Rc[:k1, :n1] = Rho[s1]
+        Rc[k1:, n1:] = Rho[s2]
+        Lc = np.zeros((n1 + n2, k1 + k2))
+        Lc[:n1, :k1] = Lam[s1]
+        Lc[n1:, k1:] = Lam[s2]
+        Rho[b] = _skel_proj(H.T_UP[b], H.J_UP[b], Rc)
+        Lam[b] = _skel_proj(H.T_DN[b], H.J_DN[b], Lc.T).T
+    return Kd

@@ -247,3 +247,56 @@ def test_dfloat_inv_forest(gpu):
     x, rr, it = G1.HSS1D_solve(H, F, 1e-10, 4)
     assert rr <= 1e-10
     assert np.linalg.norm(x - x64) <= 1e-9 * np.linalg.norm(x64)
+
+
+def test_dense_matrix_transpose_scalarmult(star):
+    """HSS1D_dense_matrix / HSS1D_transpose / HSS1D_scalarmult against the oracle's
+    telescoping restatements (HSS1D/HSS1D_dense_matrix.m, HSS1D_transpose.m,
+    HSS1D_scalarmult.m)."""
+    G1, g, X, H, Ho = star
+    N = X.shape[0]
+    Kd = G1.HSS1D_dense_matrix(H)
+    Kdo = O1.dense_matrix(Ho)
+    scale = np.abs(Kdo).max()
+    assert Kd.shape == (N, N)
+    assert np.abs(Kd - Kdo).max() <= 1e-12 * scale
+    # the compressed matrix is the kernel matrix to the compression tolerance
+    A = OK.kernel_eval(X, X, OK.KernelParams(flag=OK.DL_L_2D))
+    assert np.abs(Kd - A).max() <= 1e-9 * np.abs(A).max()
+    # transpose: a new handle whose apply and dense form are A^T
+    At = G1.HSS1D_transpose(H)
+    q = np.random.default_rng(11).standard_normal((N, 3))
+    assert np.linalg.norm(G1.HSS1D_apply_nsym(At, q) - Kd.T @ q) <= 1e-13 * np.linalg.norm(Kd.T @ q)
+    assert np.linalg.norm(G1.HSS1D_apply_nsym(At, q) - O1.apply_nsym(O1.transpose(Ho), q)) <= 1e-12 * np.linalg.norm(q)
+    assert np.abs(G1.HSS1D_dense_matrix(At) - Kd.T).max() <= 1e-14 * scale
+    # the transpose inverts and solves like the dense transpose
+    G1.HSS1D_invert_nsym(At)
+    f = np.random.default_rng(12).standard_normal(N)
+    x = G1.HSS1D_applyinv_nsym(At, None, None, f)
+    assert np.linalg.norm(Kd.T @ x - f) <= 1e-11 * np.linalg.norm(f)
+    # scalar multiple (in place; the inverse is dropped until re-inverted)
+    G1.HSS1D_invert_nsym(At)
+    G1.HSS1D_scalarmult(-2.5, At)
+    assert np.linalg.norm(G1.HSS1D_apply_nsym(At, q) + 2.5 * (Kd.T @ q)) <= 1e-13 * np.linalg.norm(Kd.T @ q)
+    from hssc_directsolver_gb300 import _lib
+    with pytest.raises(_lib.HSSError):
+        G1.HSS1D_applyinv_nsym(At, None, None, f)
+    G1.HSS1D_invert_nsym(At)
+    x2 = G1.HSS1D_applyinv_nsym(At, None, None, f)
+    assert np.linalg.norm(x2 + x / 2.5) <= 1e-11 * np.linalg.norm(x)
+    out = np.zeros(4)
+    assert _lib.lib().hss1d_dense_matrix(H._h, 3, _lib.ptr(out)) == _lib.HSS_ERR_ARG
+
+
+def test_dense_matrix_of_a_forest_problem(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    rng = np.random.default_rng(3)
+    curves = [geometry.fourier_curve(n, rng.uniform(0, 0.3 / np.arange(1, 5)), rng.uniform(0, 2 * np.pi, 4))
+              for n in (700, 1300)]
+    F = G1.HSS1D_compress_batch(curves, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    for p, X in enumerate(curves):
+        Hs = G1.HSS1D_compress_nsym("green", X, 64, 1e-10, GK.Kernel("DL_L_2D"))
+        Kf = G1.HSS1D_dense_matrix(F, prob=p)
+        Ks = G1.HSS1D_dense_matrix(Hs)
+        assert Kf.shape == (X.shape[0], X.shape[0])
+        assert np.abs(Kf - Ks).max() <= 1e-12 * np.abs(Ks).max()

@@ -197,3 +197,21 @@ def test_levhss_rule():
         lev = next((l for l in range(1, tree.depth) if ks[l] <= n_cut), tree.depth - 1)
         want = -1 if max(ks[0], ks[1]) <= n_cut else (lev - 1 if lev % 2 else lev)
         assert hss2d.lev_hss(tree, n_cut) == want
+
+
+def test_hss1d_dense_matrix_transpose_scalarmult():
+    """The oracle's HSS1D_dense_matrix (telescoping) equals its apply on identity columns;
+    the transpose's dense form is the transpose; scalarmult scales the operator."""
+    from oracle import hss1d as O
+    X = geometry.star_curve(512)
+    kp = kernels.KernelParams(flag=kernels.DL_L_2D)
+    H = O.compress_nsym(X, 64, 1e-10, kp)
+    I = np.eye(512)
+    Ka = O.apply_nsym(H, I)
+    Kd = O.dense_matrix(H)
+    s = np.abs(Ka).max()
+    assert np.abs(Kd - Ka).max() <= 1e-14 * s
+    assert np.abs(O.dense_matrix(O.transpose(H)) - Kd.T).max() <= 1e-14 * s
+    assert np.abs(O.apply_nsym(O.transpose(H), I) - Ka.T).max() <= 1e-14 * s
+    assert np.abs(O.apply_nsym(O.scalarmult(-3.0, H), I) + 3.0 * Ka).max() <= 1e-14 * s
+    assert np.abs(Kd - O.dense_from_points(X, kp)).max() <= 1e-9 * s
