@@ -96,6 +96,8 @@ SIGNATURES = {
     "hss1d_transpose": (C.c_int, [_P, C.POINTER(_P)]),
     "hss1d_scalarmult": (C.c_int, [_P, C.c_double]),
     "hss1d_dense_matrix": (C.c_int, [_P, C.c_int32, _P]),
+    "hss1d_apply_submatrix": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P]),
+    "hss1d_apply_submatrix_boxes": (C.c_int, [_P, _P, _P, _P, _P]),
     "hss1d_destroy": (C.c_int, [_P]),
     "hss_mlp_create": (C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32, C.c_uint64]),
     "hss_mlp_nparams": (C.c_int, [_P, _I32P]),

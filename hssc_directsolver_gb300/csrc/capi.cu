@@ -559,6 +559,50 @@ int hss1d_dense_matrix(hss1d_matrix* H, int32_t prob, double* Kd) {
   HSS_CATCH
 }
 
+int hss1d_apply_submatrix(hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I_up, const double* qq, int32_t nrhs,
+                          double* uu) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && I_dn && I_up && qq && uu && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
+  HSS1D* h = H->impl;
+  const size_t N = (size_t)h->Ntot;
+  // K(I_dn, I_up) qq(I_up) = rows I_dn of K (qq with the columns outside I_up zeroed)
+  std::vector<double> q(N * nrhs), y(N * nrhs);
+  for (int c = 0; c < nrhs; ++c)
+    for (size_t i = 0; i < N; ++i) q[i + c * N] = I_up[i] ? qq[i + c * N] : 0.0;
+  host_roundtrip1(h, q.data(), y.data(), nrhs, false);
+  size_t m = 0;
+  for (size_t i = 0; i < N; ++i) m += I_dn[i] ? 1 : 0;
+  for (int c = 0; c < nrhs; ++c) {
+    size_t r = 0;
+    for (size_t i = 0; i < N; ++i)
+      if (I_dn[i]) uu[r++ + c * m] = y[i + c * N];
+  }
+  HSS_CATCH
+}
+
+int hss1d_apply_submatrix_boxes(const hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I_up, uint8_t* Box_dn,
+                                uint8_t* Box_up) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && I_dn && I_up && Box_dn && Box_up, HSS_ERR_ARG, "NULL argument");
+  const HSS1D* h = H->impl;
+  // children have larger ids than their parents: one pass from the leaves up
+  for (int b = h->nboxes - 1; b >= 0; --b) {
+    bool dn = false, up = false;
+    if (h->is_leaf(b)) {
+      for (int i = 0; i < h->cnt[b]; ++i) {
+        dn = dn || I_dn[h->off[b] + i];
+        up = up || I_up[h->off[b] + i];
+      }
+    } else {
+      for (int s : {h->c1[b], h->c2[b]})
+        if (s >= 0) { dn = dn || Box_dn[s]; up = up || Box_up[s]; }
+    }
+    Box_dn[b] = dn ? 1 : 0;
+    Box_up[b] = up ? 1 : 0;
+  }
+  HSS_CATCH
+}
+
 int hss1d_set_precision(hss1d_matrix* H, int32_t precision) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

@@ -225,6 +225,35 @@ def HSS1D_dense_matrix(K_HSS: HSS1DMatrix, sym: int = 0, prob: int = 0) -> np.nd
     return Kd
 
 
+def HSS1D_apply_submatrix_boxes(TREE: HSS1DMatrix, I_dn, I_up):
+    """[Box_dn, Box_up] = HSS1D_apply_submatrix_boxes(TREE, I_dn, I_up)
+    (HSS1D/HSS1D_apply_submatrix_boxes.m:1): boolean masks over the boxes."""
+    dn = np.ascontiguousarray(np.asarray(I_dn, dtype=bool).astype(np.uint8))
+    up = np.ascontiguousarray(np.asarray(I_up, dtype=bool).astype(np.uint8))
+    nb = TREE.info()["nboxes"]
+    bd = np.zeros(nb, np.uint8)
+    bu = np.zeros(nb, np.uint8)
+    L.check(L.lib().hss1d_apply_submatrix_boxes(TREE._h, L.ptr(dn), L.ptr(up), L.ptr(bd), L.ptr(bu)))
+    return bd.astype(bool), bu.astype(bool)
+
+
+def HSS1D_apply_submatrix_nsym(K_HSS: HSS1DMatrix, Box_dn, Box_up, I_dn, I_up, qq) -> np.ndarray:
+    """uu = HSS1D_apply_submatrix_nsym(K_HSS, Box_dn, Box_up, I_dn, I_up, qq)
+    (HSS1D/HSS1D_apply_submatrix_nsym.m:1): uu = K(I_dn, I_up) qq(I_up), qq of full length N.
+    Box_dn / Box_up are accepted for the reference's signature and not needed."""
+    dn = np.ascontiguousarray(np.asarray(I_dn, dtype=bool).astype(np.uint8))
+    up = np.ascontiguousarray(np.asarray(I_up, dtype=bool).astype(np.uint8))
+    q = _as_f64(qq)
+    vec = q.ndim == 1
+    q2 = q.reshape(K_HSS.N, -1, order="F")
+    out = np.zeros((int(dn.sum()), q2.shape[1]), order="F")
+    L.check(L.lib().hss1d_apply_submatrix(K_HSS._h, L.ptr(dn), L.ptr(up), L.ptr(q2), q2.shape[1], L.ptr(out)))
+    return out[:, 0] if vec else out
+
+
+HSS1D_apply_submatrix_fsym = HSS1D_apply_submatrix_nsym
+
+
 def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
     q = _as_f64(qq)
     vec = q.ndim == 1

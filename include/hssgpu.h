@@ -169,6 +169,17 @@ int hss1d_scalarmult(hss1d_matrix* A, double c);
 /* Kd = HSS1D_dense_matrix(K_HSS) (HSS1D/HSS1D_dense_matrix.m:1) for problem prob of the
  * handle: N_p x N_p column-major host array (N_p from hss1d_forest_info). */
 int hss1d_dense_matrix(hss1d_matrix* A, int32_t prob, double* Kd);
+/* uu = HSS1D_apply_submatrix_nsym(K_HSS, Box_dn, Box_up, I_dn, I_up, qq)
+ * (HSS1D/HSS1D_apply_submatrix_nsym.m:1, _fsym likewise): uu = K(I_dn, I_up) qq(I_up).
+ * I_dn, I_up: N flags (0/1) over the handle's (stacked) points; qq: N x nrhs; uu:
+ * (count of I_dn) x nrhs, column-major.  The box masks are not needed here. */
+int hss1d_apply_submatrix(hss1d_matrix* K, const uint8_t* I_dn, const uint8_t* I_up, const double* qq, int32_t nrhs,
+                          double* uu);
+/* [Box_dn, Box_up] = HSS1D_apply_submatrix_boxes(TREE, I_dn, I_up)
+ * (HSS1D/HSS1D_apply_submatrix_boxes.m:1): per box (hss1d_info numbering), 1 if it holds
+ * rows (Box_dn) / columns (Box_up) of the submatrix. */
+int hss1d_apply_submatrix_boxes(const hss1d_matrix* K, const uint8_t* I_dn, const uint8_t* I_up, uint8_t* Box_dn,
+                                uint8_t* Box_up);
 /* arithmetic of the solve products: HSS_PREC_FP64 (default), HSS_PREC_DFLOAT (float-pair
  * copies of the FP64 operators, products on the FP32 pipes, ~2^-48 per product) or
  * HSS_PREC_DFLOAT_INV (also the following hss1d_invert's updates and products) */

@@ -602,3 +602,33 @@ def dense_matrix(H: HSS1DMatrix) -> np.ndarray:
         Rho[b] = _skel_proj(H.T_UP[b], H.J_UP[b], Rc)
         Lam[b] = _skel_proj(H.T_DN[b], H.J_DN[b], Lc.T).T
     return Kd
+
+
+def apply_submatrix_boxes(tree: HSS1DTree, I_dn, I_up):
+    """[Box_dn, Box_up] = HSS1D_apply_submatrix_boxes(TREE, I_dn, I_up),
+    HSS1D/HSS1D_apply_submatrix_boxes.m:19-62: a leaf is marked when it holds any selected
+    row / column, a parent when a child is marked."""
+    I_dn = np.asarray(I_dn, dtype=bool)
+    I_up = np.asarray(I_up, dtype=bool)
+    nb = tree.nboxes
+    bd = np.zeros(nb, bool)
+    bu = np.zeros(nb, bool)
+    for b in range(nb - 1, -1, -1):
+        if tree.is_leaf(b):
+            ind = _leaf_range(tree, b)
+            bd[b] = I_dn[ind].any()
+            bu[b] = I_up[ind].any()
+        else:
+            kids = [s for s in (tree.c1[b], tree.c2[b]) if s >= 0]
+            bd[b] = any(bd[s] for s in kids)
+            bu[b] = any(bu[s] for s in kids)
+    return bd, bu
+
+
+def apply_submatrix(H: HSS1DMatrix, I_dn, I_up, qq):
+    """uu = K(I_dn, I_up) qq(I_up) (HSS1D_apply_submatrix_nsym.m output), through the dense
+    form of the compressed matrix."""
+    I_dn = np.asarray(I_dn, dtype=bool)
+    I_up = np.asarray(I_up, dtype=bool)
+    Kd = dense_matrix(H)
+    return Kd[np.ix_(I_dn, I_up)] @ np.asarray(qq)[I_up]

@@ -300,3 +300,24 @@ def test_dense_matrix_of_a_forest_problem(gpu):
         Ks = G1.HSS1D_dense_matrix(Hs)
         assert Kf.shape == (X.shape[0], X.shape[0])
         assert np.abs(Kf - Ks).max() <= 1e-12 * np.abs(Ks).max()
+
+
+def test_apply_submatrix(star):
+    """HSS1D_apply_submatrix_nsym / _boxes (HSS1D/HSS1D_apply_submatrix_*.m) against the
+    oracle: K(I_dn, I_up) qq(I_up) through the dense form, and the box masks."""
+    G1, g, X, H, Ho = star
+    N = X.shape[0]
+    rng = np.random.default_rng(21)
+    I_dn = np.zeros(N, bool)
+    I_dn[100:900] = True
+    I_dn[rng.choice(N, 200, replace=False)] = True
+    I_up = np.zeros(N, bool)
+    I_up[2000:3100] = True
+    q = rng.standard_normal((N, 2))
+    bd, bu = G1.HSS1D_apply_submatrix_boxes(H, I_dn, I_up)
+    bdo, buo = O1.apply_submatrix_boxes(Ho.tree, I_dn, I_up)
+    assert np.array_equal(bd, bdo) and np.array_equal(bu, buo)
+    uu = G1.HSS1D_apply_submatrix_nsym(H, bd, bu, I_dn, I_up, q)
+    ref = O1.apply_submatrix(Ho, I_dn, I_up, q)
+    assert uu.shape == (I_dn.sum(), 2)
+    assert np.linalg.norm(uu - ref) <= 1e-12 * np.linalg.norm(ref)
