@@ -321,3 +321,29 @@ def test_apply_submatrix(star):
     ref = O1.apply_submatrix(Ho, I_dn, I_up, q)
     assert uu.shape == (I_dn.sum(), 2)
     assert np.linalg.norm(uu - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("N,leaf", [(50, 64), (64, 64), (65, 64), (129, 32), (1000, 17)])
+def test_small_and_ragged_trees(gpu, N, leaf):
+    """N <= leaf (no split: rejected with HSS_ERR_ARG, a dense solve needs no HSS form), the
+    first split (65 = 33 + 32), a split into uneven halves and an odd leaf size, FP64 and
+    double-float: the solve against the dense kernel matrix and the oracle's ranks."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, _lib as L
+    X = geometry.star_curve(N)
+    kp = OK.KernelParams(flag=OK.DL_L_2D)
+    if N <= leaf:
+        with pytest.raises(L.HSSError) as e:
+            G1.HSS1D_compress_nsym("green", X, leaf, 1e-10, GK.Kernel("DL_L_2D"))
+        assert e.value.code == L.HSS_ERR_ARG
+        return
+    H = G1.HSS1D_compress_nsym("green", X, leaf, 1e-10, GK.Kernel("DL_L_2D"))
+    Ho = O1.compress_nsym(X, leaf, 1e-10, kp)
+    assert np.array_equal(H.info()["kskel"][1:], np.array(Ho.kskel[1:], dtype=np.int32))
+    G1.HSS1D_invert_nsym(H)
+    A = OK.kernel_eval(X, X, kp)
+    f = np.random.default_rng(N).standard_normal((N, 3))
+    for prec in ("fp64", "dfloat"):
+        H.set_precision(prec)
+        x, rr, it = G1.HSS1D_solve(H, f, 1e-12, 4)
+        assert rr <= 1e-12
+        assert np.linalg.norm(A @ x - f) <= 1e-9 * np.linalg.norm(f)

@@ -315,3 +315,18 @@ def test_krylov_argument_errors(gpu):
     with pytest.raises(L.HSSError) as e:
         G2.HSS2D_bicgstab(A, f, 1e-10, 10, PRECOND=M)   # sizes differ
     assert e.value.code == L.HSS_ERR_ARG
+
+
+@pytest.mark.parametrize("precision", ["fp64", "dfloat", "dfloat_inv"])
+def test_smallest_grid_and_rhs_chunks(gpu, precision):
+    """npan = 2 (a depth-2 tree), 1 and 17 right-hand sides (two full 8-column chunks and a
+    ragged one), every precision: solves to 1e-11 against the oracle's forward operator."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(params(2, precision)))
+    prm, ot, blk, inv = oracle(2)
+    for nrhs in (1, 17):
+        f = np.random.default_rng(nrhs).standard_normal((prm.N, nrhs))
+        x, rr, it = G2.HSS2D_solve(t, f, 1e-11, 4)
+        assert rr <= 1e-11
+        r = f - O2.apply_nsym(ot, blk, x)
+        assert np.linalg.norm(r, axis=0).max() / np.linalg.norm(f, axis=0).min() < 1e-10
