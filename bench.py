@@ -173,12 +173,20 @@ def bench_batched(args, L, dev):
     from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
     Xs, sizes = GG.batched_curves(args.curves, seed=0)
     torch.cuda.synchronize()
+    # the IDs' pivoted QR in FP64 (the reference's arithmetic), then in double-float; the
+    # second forest is the one inverted and solved
+    tf0 = time.perf_counter()
+    H64 = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    compress_fp64_id = time.perf_counter() - tf0
+    k64 = H64.info()["kskel"]
+    del H64
     t0 = time.perf_counter()
-    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"), id_precision="dfloat")
     t1 = time.perf_counter()
     G1.HSS1D_invert_nsym(H)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    rank_agree = float((H.info()["kskel"] == k64).mean())
     Nt = sum(sizes)
     F = np.random.default_rng(0).standard_normal((8, Nt))
     dF = torch.from_numpy(F).to(dev)
@@ -212,6 +220,8 @@ def bench_batched(args, L, dev):
     return {"workload": f"{args.curves} Laplace double-layer curves, N log-uniform [1024,16384] "
                         f"(total {Nt}), leaf 64, tol 1e-10, 8 RHS each, one forest",
             "compress_s": t1 - t0, "invert_s": t2 - t1, "compress_invert_s": t2 - t0,
+            "id_precision": "dfloat", "compress_s_fp64_id": compress_fp64_id,
+            "ranks_equal_to_fp64_id": rank_agree,
             "solve_ms": ms, "solves_per_s": 1e3 / ms, "relres": rel, "solves_used": used, "path": best,
             "solve_ms_by_path": {p: out[p][0] for p in out}, "dtype": "f64"}
 

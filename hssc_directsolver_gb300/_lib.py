@@ -80,6 +80,9 @@ SIGNATURES = {
                                  _I32P]),
     "hss1d_compress_fsym": (C.c_int, [C.POINTER(_P), _P, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                       C.POINTER(hss_kernel_params), C.c_uint64]),
+    "hss1d_compress_batch_ex": (C.c_int, [C.POINTER(_P), C.c_int32, _I64P, C.POINTER(C.c_void_p), _I64P, C.c_int32,
+                                          C.c_double, C.POINTER(hss_kernel_params), C.POINTER(C.c_uint64), _P,
+                                          C.c_int32]),
     "hss1d_compress_batch": (C.c_int, [C.POINTER(_P), C.c_int32, _I64P, C.POINTER(C.c_void_p), _I64P, C.c_int32,
                                        C.c_double, C.POINTER(hss_kernel_params), C.POINTER(C.c_uint64)]),
     "hss1d_forest_info": (C.c_int, [_P, _I32P, _I64P, _I32P, _I64P]),

@@ -186,13 +186,17 @@ int hss_device_count(int* count) {
 // ---------------------------------------------------------------- HSS1D --
 static void hss1d_make(hss1d_matrix** out, int nprob, const long long* N, const double* const* X,
                        const long long* ldx, int leaf, double acc, const hss_kernel_params* kp,
-                       const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false) {
+                       const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false,
+                       int id_prec = HSS_PREC_FP64) {
   HSS_REQUIRE(out && X && kp && N && ldx, HSS_ERR_ARG, "NULL argument");
+  HSS_REQUIRE(id_prec == HSS_PREC_FP64 || id_prec == HSS_PREC_DFLOAT, HSS_ERR_ARG,
+              "ID precision: HSS_PREC_FP64 or HSS_PREC_DFLOAT");
   require_device();
   *out = nullptr;
   auto* h = new hss1d_matrix{nullptr};
   try {
     h->impl = new HSS1D();
+    h->impl->id_df = (id_prec == HSS_PREC_DFLOAT);
     h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds, mlp, sym);
   } catch (...) {
     delete h->impl;
@@ -243,6 +247,20 @@ int hss1d_compress_batch_learned(hss1d_matrix** out, int32_t nprob, const int64_
   if (seeds)
     for (int p = 0; p < nprob; ++p) sd[p] = seeds[p];
   hss1d_make(out, nprob, n.data(), X, l.data(), leaf, acc, kp, sd.data(), M->impl);
+  HSS_CATCH
+}
+
+int hss1d_compress_batch_ex(hss1d_matrix** out, int32_t nprob, const int64_t* N, const double* const* X,
+                            const int64_t* ldx, int32_t leaf, double acc, const hss_kernel_params* kp,
+                            const uint64_t* seeds, hss_mlp* M, int32_t id_precision) {
+  HSS_TRY
+  HSS_REQUIRE(nprob >= 1 && N && ldx && (!M || M->impl), HSS_ERR_ARG, "bad batch arguments");
+  std::vector<long long> n(N, N + nprob), l(ldx, ldx + nprob);
+  std::vector<unsigned long long> sd(nprob, 0ULL);
+  if (seeds)
+    for (int p = 0; p < nprob; ++p) sd[p] = seeds[p];
+  hss1d_make(out, nprob, n.data(), X, l.data(), leaf, acc, kp, sd.data(), M ? M->impl : nullptr, false,
+             id_precision);
   HSS_CATCH
 }
 

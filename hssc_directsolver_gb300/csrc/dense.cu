@@ -1911,9 +1911,85 @@ __device__ double id_rand_error(const IdP& p, int k, const double* T, const doub
   return sqrt(sqrt(z2));
 }
 
+// Rank, interpolation matrix and randomized check of the ID (Common/ID.m:40-86) once the
+// pivoted QR has left R in W (FP64); jdone = QR steps done, l = min(m, n).
+__device__ void id_finish(const IdP& p, double acc, int l, int jdone, double* sh, int* shi) {
+  const unsigned long long seed = p.seed;
+  const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  double* W = p.W;
+  if (p.steps_hint == ID_QR_ONLY) {  // pivoted QR for a fixed-rank ID of the caller
+    if (tid == 0) {
+      *p.rank = l;
+      if (p.stat) { p.stat[0] = 0; p.stat[1] = l; }
+    }
+    return;
+  }
+  // rank detection (Common/ID.m:51-52) over the computed diagonal
+  double Rmx = (l > 0) ? fabs(W[0]) * acc : 0.0;
+  auto count_rank = [&](double thr) {
+    int cnt = 0;
+    for (int i = tid; i < jdone; i += 256) cnt += (fabs(W[i + (size_t)i * m]) > thr) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    __syncthreads();
+    if (lane == 0) shi[w] = cnt;
+    __syncthreads();
+    int t = 0;
+    for (int i = 0; i < 8; ++i) t += shi[i];
+    __syncthreads();
+    return t;
+  };
+  int k = (l > 0) ? count_rank(Rmx) : 0;
+  id_trisolve(W, m, n, k, p.T);
+  __syncthreads();
+  int draw = 0;
+  double* x = p.x;
+  double* y = p.y;
+  double* t1 = p.y + m;
+  while (k < l) {
+    const int r = n - k;
+    const unsigned long long st0 = ((unsigned long long)p.problem << 8) | (unsigned)(draw & 0xFF);
+    const unsigned long long st1 = ((unsigned long long)p.problem << 8) | (unsigned)((draw + 1) & 0xFF);
+    // two unit random vectors: x[0:r] for the error, x[n:n+r] for the norm; entry i is
+    // drawn at the residual column's own index, independent of the residual order
+    double pa = 0.0, pb = 0.0;
+    for (int i = tid; i < r; i += 256) {
+      const int c = p.perm[k + i];
+      const double a = rng_uniform(seed, st0, c), b = rng_uniform(seed, st1, c);
+      x[i] = a; x[n + i] = b;
+      pa += a * a; pb += b * b;
+    }
+    const double na = sqrt(block_sum256(pa, sh));
+    const double nb = sqrt(block_sum256(pb, sh));
+    for (int i = tid; i < r; i += 256) { x[i] /= na; x[n + i] /= nb; }
+    __syncthreads();
+    draw += 2;
+    const double e = id_rand_error(p, k, p.T, x, y, t1, sh);
+    const double nr = id_rand_norm(p, k, x + n, y, sh);
+    if (!(e > nr * acc)) break;
+    Rmx = 0.75 * Rmx;
+    if (jdone < l && !(fabs(W[(size_t)(jdone - 1) * (m + 1)]) <= Rmx)) {
+      // the relaxed threshold reaches past the truncated factorization: rerun in full
+      if (tid == 0 && p.stat) p.stat[0] = 2;
+      if (tid == 0) *p.rank = k;
+      return;
+    }
+    k = count_rank(Rmx);
+    id_trisolve(W, m, n, k, p.T);
+    __syncthreads();
+    if (draw > 250) break;
+  }
+  if (tid == 0) {
+    *p.rank = k;
+    if (p.stat) {
+      p.stat[0] = (jdone < l) ? 1 : 0;
+      p.stat[1] = jdone;
+    }
+  }
+}
+
+
 __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, double acc) {
   const IdP p = P[blockIdx.x];
-  const unsigned long long seed = p.seed;
   const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int l = min(m, n);
   double* W = p.W;
@@ -1996,79 +2072,169 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     }
     __syncthreads();
   }
-  if (p.steps_hint == ID_QR_ONLY) {  // pivoted QR for a fixed-rank ID of the caller
-    if (tid == 0) {
-      *p.rank = l;
-      if (p.stat) { p.stat[0] = 0; p.stat[1] = l; }
-    }
-    return;
+  id_finish(p, acc, l, jdone, sh, shi);
+}
+
+// Sum of a double-float value over a 256-thread block (xor butterfly, then the eight
+// warp sums in order); every thread gets the same (h, l).
+__device__ __forceinline__ void block_sum256_df(float& h, float& l, float* shh, float* shl) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    df_add(h, l, oh, ol);
   }
-  // rank detection (Common/ID.m:51-52) over the computed diagonal
-  double Rmx = (l > 0) ? fabs(W[0]) * acc : 0.0;
-  auto count_rank = [&](double thr) {
-    int cnt = 0;
-    for (int i = tid; i < jdone; i += 256) cnt += (fabs(W[i + (size_t)i * m]) > thr) ? 1 : 0;
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    __syncthreads();
-    if (lane == 0) shi[w] = cnt;
-    __syncthreads();
-    int t = 0;
-    for (int i = 0; i < 8; ++i) t += shi[i];
-    __syncthreads();
-    return t;
-  };
-  int k = (l > 0) ? count_rank(Rmx) : 0;
-  id_trisolve(W, m, n, k, p.T);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __syncthreads();
-  int draw = 0;
-  double* x = p.x;
-  double* y = p.y;
-  double* t1 = p.y + m;
-  while (k < l) {
-    const int r = n - k;
-    const unsigned long long st0 = ((unsigned long long)p.problem << 8) | (unsigned)(draw & 0xFF);
-    const unsigned long long st1 = ((unsigned long long)p.problem << 8) | (unsigned)((draw + 1) & 0xFF);
-    // two unit random vectors: x[0:r] for the error, x[n:n+r] for the norm; entry i is
-    // drawn at the residual column's own index, independent of the residual order
-    double pa = 0.0, pb = 0.0;
-    for (int i = tid; i < r; i += 256) {
-      const int c = p.perm[k + i];
-      const double a = rng_uniform(seed, st0, c), b = rng_uniform(seed, st1, c);
-      x[i] = a; x[n + i] = b;
-      pa += a * a; pb += b * b;
-    }
-    const double na = sqrt(block_sum256(pa, sh));
-    const double nb = sqrt(block_sum256(pb, sh));
-    for (int i = tid; i < r; i += 256) { x[i] /= na; x[n + i] /= nb; }
-    __syncthreads();
-    draw += 2;
-    const double e = id_rand_error(p, k, p.T, x, y, t1, sh);
-    const double nr = id_rand_norm(p, k, x + n, y, sh);
-    if (!(e > nr * acc)) break;
-    Rmx = 0.75 * Rmx;
-    if (jdone < l && !(fabs(W[(size_t)(jdone - 1) * (m + 1)]) <= Rmx)) {
-      // the relaxed threshold reaches past the truncated factorization: rerun in full
-      if (tid == 0 && p.stat) p.stat[0] = 2;
-      if (tid == 0) *p.rank = k;
-      return;
-    }
-    k = count_rank(Rmx);
-    id_trisolve(W, m, n, k, p.T);
-    __syncthreads();
-    if (draw > 250) break;
-  }
-  if (tid == 0) {
-    *p.rank = k;
-    if (p.stat) {
-      p.stat[0] = (jdone < l) ? 1 : 0;
-      p.stat[1] = jdone;
-    }
+  if (lane == 0) { shh[w] = h; shl[w] = l; }
+  __syncthreads();
+  h = shh[0];
+  l = shl[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i) df_add(h, l, shh[i], shl[i]);
+  __syncthreads();
+}
+
+__device__ __forceinline__ void warp_sum_df(float& h, float& l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    df_add(h, l, oh, ol);
   }
 }
 
-void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s) {
+__device__ __forceinline__ double df_val(float2 v) { return (double)v.x + (double)v.y; }
+
+// The ID with its pivoted QR in double-float arithmetic (FP64 data held as float pairs in
+// W's own storage, every product and sum on the FP32 pipes, ~2^-48 relative): the same
+// pivot rule (exact trailing column norms), Householder steps and learned-rank stop as
+// k_id_adaptive.  The per-step Householder scalars are formed in FP64.  R is then
+// widened to FP64 in place and the rank, T and the randomized check run as in FP64.
+__global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ P, double acc) {
+  const IdP p = P[blockIdx.x];
+  const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int l = min(m, n);
+  float2* W = reinterpret_cast<float2*>(p.W);
+  extern __shared__ double s_dyn[];
+  float2* norms = reinterpret_cast<float2*>(s_dyn);  // n
+  __shared__ double sh[8];
+  __shared__ double shv[8];
+  __shared__ int shi[8];
+  __shared__ float shh[8], shl[8];
+  for (long long e = tid; e < (long long)m * n; e += 256) {
+    float h, lo;
+    split_d2f(p.A[e], h, lo);
+    W[e] = make_float2(h, lo);
+  }
+  for (int c = tid; c < n; c += 256) p.perm[c] = c;
+  __syncthreads();
+  for (int c = w; c < n; c += 8) {
+    float nh = 0.f, nl = 0.f;
+    for (int i = lane; i < m; i += 32) { const float2 v = W[i + (size_t)c * m]; df_madd(nh, nl, v.x, v.y, v.x, v.y); }
+    warp_sum_df(nh, nl);
+    if (lane == 0) norms[c] = make_float2(nh, nl);
+  }
+  __syncthreads();
+  int s_hint = (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
+  int jdone = l;
+  for (int j = 0; j < l; ++j) {
+    if (j == s_hint && j > 0) {
+      if (fabs(df_val(W[(size_t)(j - 1) * (m + 1)])) <= fabs(df_val(W[0])) * acc * 0.5625) {
+        jdone = j;
+        break;
+      }
+      s_hint = min(l, j + max(4, j / 2));
+    }
+    double best = -1.0;
+    int bi = INT_MAX;
+    for (int c = j + tid; c < n; c += 256) {
+      const double v = df_val(norms[c]);
+      if (v > best) { best = v; bi = c; }
+    }
+    block_argmax256(best, bi, shv, shi);
+    if (bi == INT_MAX) bi = j;
+    if (bi != j) {
+      for (int i = tid; i < m; i += 256) {
+        const float2 t = W[i + (size_t)j * m];
+        W[i + (size_t)j * m] = W[i + (size_t)bi * m];
+        W[i + (size_t)bi * m] = t;
+      }
+      if (tid == 0) {
+        const int t = p.perm[j]; p.perm[j] = p.perm[bi]; p.perm[bi] = t;
+        const float2 u = norms[j]; norms[j] = norms[bi]; norms[bi] = u;
+      }
+    }
+    __syncthreads();
+    float xh = 0.f, xl = 0.f;
+    for (int i = j + 1 + tid; i < m; i += 256) { const float2 v = W[i + (size_t)j * m]; df_madd(xh, xl, v.x, v.y, v.x, v.y); }
+    block_sum256_df(xh, xl, shh, shl);
+    const double xn2 = (double)xh + (double)xl;
+    const double alpha = df_val(W[j + (size_t)j * m]);
+    double tau = 0.0, beta = alpha, scal = 0.0;
+    if (xn2 != 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      tau = (beta - alpha) / beta;
+      scal = 1.0 / (alpha - beta);
+    }
+    float sch, scl, tah, tal;
+    split_d2f(scal, sch, scl);
+    split_d2f(tau, tah, tal);
+    for (int i = j + 1 + tid; i < m; i += 256) {
+      float2 v = W[i + (size_t)j * m];
+      df_mul(v.x, v.y, sch, scl);
+      W[i + (size_t)j * m] = v;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      float bh, bl;
+      split_d2f(beta, bh, bl);
+      W[j + (size_t)j * m] = make_float2(bh, bl);
+    }
+    for (int c = j + 1 + w; c < n; c += 8) {
+      float dh = 0.f, dl = 0.f;
+      if (lane == 0) { const float2 v = W[j + (size_t)c * m]; dh = v.x; dl = v.y; }
+      for (int i = j + 1 + lane; i < m; i += 32) {
+        const float2 v = W[i + (size_t)j * m], a = W[i + (size_t)c * m];
+        df_madd(dh, dl, v.x, v.y, a.x, a.y);
+      }
+      warp_sum_df(dh, dl);
+      df_mul(dh, dl, tah, tal);
+      if (lane == 0) {
+        float2 v = W[j + (size_t)c * m];
+        df_add(v.x, v.y, -dh, -dl);
+        W[j + (size_t)c * m] = v;
+      }
+      float nh = 0.f, nl = 0.f;
+      for (int i = j + 1 + lane; i < m; i += 32) {
+        const float2 v = W[i + (size_t)j * m];
+        float2 a = W[i + (size_t)c * m];
+        df_madd(a.x, a.y, -dh, -dl, v.x, v.y);
+        W[i + (size_t)c * m] = a;
+        df_madd(nh, nl, a.x, a.y, a.x, a.y);
+      }
+      warp_sum_df(nh, nl);
+      if (lane == 0) norms[c] = make_float2(nh, nl);
+    }
+    __syncthreads();
+  }
+  // widen R (and the reflectors) to FP64 in place: element e's float pair and its double
+  // share the same 8 bytes
+  double* Wd = p.W;
+  for (long long e = tid; e < (long long)m * n; e += 256) {
+    const float2 v = W[e];
+    Wd[e] = df_to_double(v.x, v.y);
+  }
+  __syncthreads();
+  id_finish(p, acc, l, jdone, sh, shi);
+}
+
+void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s, bool df) {
   if (batch <= 0) return;
-  // dynamic shared memory: norms (n doubles); the host guarantees n <= 4096
+  // dynamic shared memory: norms (n doubles or float pairs); the host guarantees n <= 4096
+  if (df) {
+    k_id_adaptive_df<<<batch, 256, 4096 * sizeof(double), s>>>(dP, acc);
+    check_launch("k_id_adaptive_df");
+    return;
+  }
   k_id_adaptive<<<batch, 256, 4096 * sizeof(double), s>>>(dP, acc);
   check_launch("k_id_adaptive");
 }

@@ -132,7 +132,8 @@ struct IdP {
 
 constexpr int ID_QR_ONLY = -2;
 
-void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s);
+// df: the pivoted QR in double-float arithmetic (k_id_adaptive_df), rank / T / check in FP64
+void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s, bool df = false);
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s);
 
 // Householder QR with column pivoting of W (m x l, ld ldw; overwritten) and the

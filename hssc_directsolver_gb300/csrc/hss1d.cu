@@ -495,7 +495,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     }
     DevBuf<IdP> dip;
     upload_vec(dip, ip, stream);
-    id_adaptive_batched(dip.p, nprob2, acc, stream);
+    id_adaptive_batched(dip.p, nprob2, acc, stream, id_df);
     std::vector<int> hr, hs;
     download(hr, rank.p, nprob2, stream);
     download(hs, stat.p, (size_t)2 * nprob2, stream);
@@ -509,7 +509,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       if (!redo.empty()) {
         DevBuf<IdP> dr;
         upload_vec(dr, redo, stream);
-        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream);
+        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream, id_df);
         download(hr, rank.p, nprob2, stream);
         download(hs, stat.p, (size_t)2 * nprob2, stream);
         HSS_CUDA(cudaStreamSynchronize(stream));
@@ -544,7 +544,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       if (!redo.empty()) {
         DevBuf<IdP> dr;
         upload_vec(dr, redo, stream);
-        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream);
+        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream, id_df);
         HSS_CUDA(cudaStreamSynchronize(stream));
         reruns += (int)redo.size();
       }

@@ -52,6 +52,7 @@ struct HSS1D {
   int nprob = 0, nboxes = 0, leaf = 0, maxlev = 0;
   double acc = 0;
   bool sym = false;  // fsym compression: one ID per box, incoming skeletons = outgoing
+  bool id_df = false;  // the IDs' pivoted QR in double-float arithmetic (k_id_adaptive_df)
   std::vector<long long> pN, pbase;   // points per problem, first global point
   std::vector<int> proot;              // root box of each problem
   std::vector<unsigned long long> pseed;

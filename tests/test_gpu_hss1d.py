@@ -347,3 +347,27 @@ def test_small_and_ragged_trees(gpu, N, leaf):
         x, rr, it = G1.HSS1D_solve(H, f, 1e-12, 4)
         assert rr <= 1e-12
         assert np.linalg.norm(A @ x - f) <= 1e-9 * np.linalg.norm(f)
+
+
+def test_dfloat_id_compress(gpu):
+    """The IDs' pivoted QR in double-float arithmetic: ranks as the FP64 ID (ties in the
+    pivot order may move a rank by one in a few boxes), the same compression accuracy and
+    a solve to 1e-12 against the FP64-compressed operator's dense form."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    Xs, sizes = GG.batched_curves(16, nmin=1024, nmax=4096, seed=4)
+    k = GK.Kernel("DL_L_2D")
+    A = G1.HSS1D_compress_batch(Xs, 64, 1e-10, k)
+    B = G1.HSS1D_compress_batch(Xs, 64, 1e-10, k, id_precision="dfloat")
+    ka, kb = A.info()["kskel"], B.info()["kskel"]
+    assert (ka == kb).mean() >= 0.98 and np.abs(ka - kb).max() <= 2
+    for p in (0, 7):
+        X = Xs[p]
+        Kx = OK.kernel_eval(X, X, OK.KernelParams(flag=OK.DL_L_2D))
+        Kb = G1.HSS1D_dense_matrix(B, prob=p)
+        assert np.abs(Kb - Kx).max() <= 1e-9 * np.abs(Kx).max()
+    G1.HSS1D_invert_nsym(B)
+    f = np.random.default_rng(2).standard_normal((sum(sizes), 2))
+    x, rr, it = G1.HSS1D_solve(B, f, 1e-12, 4)
+    assert rr <= 1e-12
+    with pytest.raises(ValueError):
+        G1.HSS1D_compress_batch(Xs[:1], 64, 1e-10, k, id_precision="fp32")
