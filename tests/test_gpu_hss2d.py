@@ -330,3 +330,32 @@ def test_smallest_grid_and_rhs_chunks(gpu, precision):
         assert rr <= 1e-11
         r = f - O2.apply_nsym(ot, blk, x)
         assert np.linalg.norm(r, axis=0).max() / np.linalg.norm(f, axis=0).min() < 1e-10
+
+
+@pytest.mark.parametrize("inter", ["dense", "lowrank"])
+def test_skeleton_interpolation_error(gpu, inter):
+    """Test_HSS2D_skeletons.m on the GPU tree (exported J, T_up per box): the per-level
+    interpolation error on a 2*layers box proxy is below 1e-8 and within 2x of the
+    oracle tree's."""
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    from test_oracle import skeleton_errors
+    npan = 8
+    prm = G2.HSS2DParams(Ng=8, npan=npan, kernel=GK.Kernel("SL_L_2D", 2.0 / 64, GK.Modulation(),
+                                                             GK.Modulation(0.5, 0, 0, 20.0)), INTERform=inter)
+    t = G2.HSS2D_build_tree_nsym(prm)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / 64, c=OK.Modulation(0.5, 0, 0, 20.0))
+    oprm = O2.HSS2DParams(Ng=8, npan=npan, kp=kp, INTERform=inter)
+    ot = O2.build_tree_nsym(oprm)
+    cent = O2.box_centers(ot.depth)
+    n, k, _ = t.box_sizes()
+
+    def gbox(b):
+        e = t.export_box(b)
+        return e["I_src"], e["J"], int(k[b]), e["T_up"], cent[b]
+
+    X = oprm.X_source()
+    eg = skeleton_errors(X, oprm.h, oprm.layers, ot.depth, kp, gbox)
+    eo = skeleton_errors(X, oprm.h, oprm.layers, ot.depth, kp,
+                         lambda b: (np.asarray(ot.I_src[b]), np.asarray(ot.J[b]), ot.k[b], ot.T_up[b], ot.cent[b]))
+    assert max(eg) < 1e-8, eg
+    assert all(g <= 2 * o + 1e-12 for g, o in zip(eg, eo)), (eg, eo)

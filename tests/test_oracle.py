@@ -215,3 +215,35 @@ def test_hss1d_dense_matrix_transpose_scalarmult():
     assert np.abs(O.apply_nsym(O.transpose(H), I) - Ka.T).max() <= 1e-14 * s
     assert np.abs(O.apply_nsym(O.scalarmult(-3.0, H), I) + 3.0 * Ka).max() <= 1e-14 * s
     assert np.abs(Kd - O.dense_from_points(X, kp)).max() <= 1e-9 * s
+
+
+def skeleton_errors(X, h, layers, depth, kp, box):
+    """Test_HSS2D_skeletons.m:20-68: per level, the mean over boxes of
+    ||K(Xp, X_rs) - K(Xp, X_sk) T|| / ||K(Xp, X_rs)|| on a box proxy of 2*layers layers.
+    box(b) -> (I_src, J, k, T_up, centre)."""
+    errs = []
+    for lev in range(1, depth + 1):
+        colrad, rowrad = hss2d.box_radii(lev)
+        e = []
+        for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
+            I, J, k, T, cB = box(b)
+            if len(J) - k == 0:
+                continue
+            Xsk, Xrs = X[I[J[:k]]], X[I[J[k:]]]
+            Xp = hss2d.build_box_proxy(cB, colrad, rowrad, 2 * layers, h)
+            A = kernels.kernel_eval(Xp, Xrs, kp)
+            e.append(np.linalg.norm(A - kernels.kernel_eval(Xp, Xsk, kp) @ T, 2) / np.linalg.norm(A, 2))
+        errs.append(float(np.mean(e)))
+    return errs
+
+
+@pytest.mark.parametrize("inter", ["dense", "lowrank"])
+def test_hss2d_skeleton_interpolation_error(inter):
+    """The reference's skeleton test (Test_HSS2D_skeletons.m) on the oracle tree, NTI,
+    8x8 panels, tol 1e-10: every level interpolates the wider proxy to 1e-8."""
+    kp = kernels.KernelParams(flag=kernels.SL_L_2D, h=2.0 / 64, c=kernels.Modulation(0.5, 0, 0, 20.0))
+    prm = hss2d.HSS2DParams(Ng=8, npan=8, kp=kp, INTERform=inter)
+    t = hss2d.build_tree_nsym(prm)
+    errs = skeleton_errors(prm.X_source(), prm.h, prm.layers, t.depth, kp,
+                           lambda b: (np.asarray(t.I_src[b]), np.asarray(t.J[b]), t.k[b], t.T_up[b], t.cent[b]))
+    assert max(errs) < 1e-8, errs
