@@ -168,7 +168,9 @@ def run_reference(args):
 def bench_batched(args, L, dev):
     """The batched-curves workload: 512 double-layer curves r = 1 + sum_k a_k cos(k t + phi_k)
     (a_k ~ U(0, 0.3/k), k <= 8), N log-uniform in [1024, 16384], leaf 64, tol 1e-10, 8 RHS per
-    curve, all curves compressed / inverted / solved as one forest (FP64)."""
+    curve, all curves compressed / inverted / solved as one forest: the IDs' QR in FP64 and in
+    double-float (timed; the second forest is kept), the inversion in FP64 and in double-float,
+    every solve refined to 1e-10 against the FP64 forward operator."""
     import torch
     from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
     Xs, sizes = GG.batched_curves(args.curves, seed=0)
@@ -183,10 +185,14 @@ def bench_batched(args, L, dev):
     t0 = time.perf_counter()
     H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"), id_precision="dfloat")
     t1 = time.perf_counter()
+    rank_agree = float((H.info()["kskel"] == k64).mean())
+    # FP64 inversion (timed solves in the fp64 and dfloat paths), then the double-float
+    # inversion the dfloat_inv path solves with (both refine to 1e-10 in two solves)
+    H.set_precision("fp64")
+    ti0 = time.perf_counter()
     G1.HSS1D_invert_nsym(H)
     torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    rank_agree = float((H.info()["kskel"] == k64).mean())
+    invert_fp64 = time.perf_counter() - ti0
     Nt = sum(sizes)
     F = np.random.default_rng(0).standard_normal((8, Nt))
     dF = torch.from_numpy(F).to(dev)
@@ -200,8 +206,15 @@ def bench_batched(args, L, dev):
         L.check(L.lib().hss1d_solve_device(H._h, L.ptr(dF), L.ptr(dX), 8, 1e-10, 4, C.byref(rr), C.byref(it), sp))
 
     out = {}
-    for prec in ("fp64", "dfloat"):
+    inv_s = {"fp64": invert_fp64, "dfloat": invert_fp64}
+    for prec in ("fp64", "dfloat", "dfloat_inv"):
         H.set_precision(prec)
+        if prec == "dfloat_inv":
+            torch.cuda.synchronize()
+            ti0 = time.perf_counter()
+            G1.HSS1D_invert_nsym(H)
+            torch.cuda.synchronize()
+            inv_s[prec] = time.perf_counter() - ti0
         for _ in range(2):
             solve()
         torch.cuda.synchronize()
@@ -215,11 +228,13 @@ def bench_batched(args, L, dev):
         torch.cuda.synchronize()
         out[prec] = (e0.elapsed_time(e1) / steps, rr.value, it.value)
     ok = [p for p in out if out[p][1] <= 1e-10]
-    best = min(ok, key=lambda p: out[p][0]) if ok else "fp64"
+    # fastest solve, then the cheaper inversion among equally fast solves
+    best = min(ok, key=lambda p: (round(out[p][0], 1), inv_s[p])) if ok else "fp64"
     ms, rel, used = out[best]
     return {"workload": f"{args.curves} Laplace double-layer curves, N log-uniform [1024,16384] "
                         f"(total {Nt}), leaf 64, tol 1e-10, 8 RHS each, one forest",
-            "compress_s": t1 - t0, "invert_s": t2 - t1, "compress_invert_s": t2 - t0,
+            "compress_s": t1 - t0, "invert_s": inv_s[best], "compress_invert_s": t1 - t0 + inv_s[best],
+            "invert_s_by_path": inv_s,
             "id_precision": "dfloat", "compress_s_fp64_id": compress_fp64_id,
             "ranks_equal_to_fp64_id": rank_agree,
             "solve_ms": ms, "solves_per_s": 1e3 / ms, "relres": rel, "solves_used": used, "path": best,
