@@ -97,6 +97,7 @@ SIGNATURES = {
     "hss1d_solve_device": (C.c_int, [_P, _P, _P, C.c_int32, C.c_double, C.c_int32, _DP, _I32P, _P]),
     "hss1d_set_precision": (C.c_int, [_P, C.c_int32]),
     "hss1d_transpose": (C.c_int, [_P, C.POINTER(_P)]),
+    "hss2d_set_autotune": (C.c_int, [_P, C.c_int32]),
     "hss1d_scalarmult": (C.c_int, [_P, C.c_double]),
     "hss1d_dense_matrix": (C.c_int, [_P, C.c_int32, _P]),
     "hss1d_apply_submatrix": (C.c_int, [_P, _P, _P, _P, C.c_int32, _P]),

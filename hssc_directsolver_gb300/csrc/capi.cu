@@ -741,6 +741,13 @@ int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t 
   HSS_CATCH
 }
 
+int hss2d_set_autotune(hss2d_matrix* H, int32_t on) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  H->impl->set_autotune(on != 0);
+  HSS_CATCH
+}
+
 int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

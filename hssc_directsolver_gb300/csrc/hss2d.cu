@@ -221,6 +221,7 @@ void SolvePlan<R>::add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStre
   for (auto& p : P) { st.maxM = std::max(st.maxM, p.M); st.maxN = std::max(st.maxN, p.N); maxK = std::max(maxK, p.K); }
   st.alpha = alpha;
   st.beta = beta;
+  st.maxK = maxK;
   st.ksplit = df ? skinny_ksplit_df(st.batch, st.maxM, maxK) : skinny_ksplit<R>(st.batch, st.maxM, maxK);
   if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
   st.d.alloc(P.size());
@@ -241,6 +242,7 @@ void SolvePlan<R>::add_seg(const std::vector<SegGemmP>& P, R alpha, R beta, cuda
   }
   st.alpha = alpha;
   st.beta = beta;
+  st.maxK = maxK;
   st.ksplit = skinny_ksplit_df(st.batch, st.maxM, maxK);
   if (st.ksplit > 1) st.part.alloc((size_t)st.batch * st.ksplit * st.maxM * 8);
   st.dseg.alloc(P.size());
@@ -249,20 +251,71 @@ void SolvePlan<R>::add_seg(const std::vector<SegGemmP>& P, R alpha, R beta, cuda
 }
 
 template <typename R>
-void SolvePlan<R>::run(cudaStream_t s) const {
-  for (auto& st : steps) {
-    if constexpr (std::is_same<R, double>::value) {
-      if (df && st.dseg.p) {
-        gemm_skinny_split_df(st.dseg.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
-        continue;
-      }
-      if (df) {
-        gemm_skinny_split_df(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
-        continue;
-      }
+void SolvePlan<R>::run_step(const Step& st, cudaStream_t s) const {
+  if constexpr (std::is_same<R, double>::value) {
+    if (df && st.dseg.p) {
+      gemm_skinny_split_df(st.dseg.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+      return;
     }
-    gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+    if (df) {
+      gemm_skinny_split_df(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+      return;
+    }
   }
+  gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
+}
+
+template <typename R>
+void SolvePlan<R>::run(cudaStream_t s) const {
+  for (auto& st : steps) run_step(st, s);
+}
+
+// The steps run on the plan's own buffers: a step's output is rewritten by the next real
+// apply before anything reads it (accumulating steps follow an overwriting one), so the
+// timing runs leave no trace.
+template <typename R>
+void SolvePlan<R>::tune(cudaStream_t s) {
+  cudaEvent_t e0, e1;
+  HSS_CUDA(cudaEventCreate(&e0));
+  HSS_CUDA(cudaEventCreate(&e1));
+  try {
+    for (auto& st : steps) {
+      const int cap = std::max(1, std::min(32, st.maxK / 64));
+      if (st.maxK < 128 || cap <= 1) continue;
+      std::vector<int> cand;
+      const int around[4] = {st.ksplit, st.ksplit / 2, st.ksplit * 2, st.ksplit * 4};
+      for (int c : around) {
+        const int cc = std::max(1, std::min(cap, c));
+        if (std::find(cand.begin(), cand.end(), cc) == cand.end()) cand.push_back(cc);
+      }
+      if (cand.size() <= 1) continue;
+      const int kmax = *std::max_element(cand.begin(), cand.end());
+      if (kmax > 1) st.part.ensure((size_t)st.batch * kmax * st.maxM * 8);
+      float best = 0.f;
+      int bestc = cand[0];
+      for (size_t i = 0; i < cand.size(); ++i) {
+        st.ksplit = cand[i];
+        run_step(st, s);
+        HSS_CUDA(cudaEventRecord(e0, s));
+        for (int rep = 0; rep < 3; ++rep) run_step(st, s);
+        HSS_CUDA(cudaEventRecord(e1, s));
+        HSS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        HSS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (i == 0 || ms < 0.98f * best) {
+          best = ms;
+          bestc = cand[i];
+        }
+      }
+      st.ksplit = bestc;
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
 }
 
 template struct SolvePlan<double>;
@@ -703,7 +756,18 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
     }
   }
   HSS_CUDA(cudaStreamSynchronize(stream));
+  if (autotune) pl.tune(stream);
   return pl;
+}
+
+void HSS2D::set_autotune(bool on) {
+  autotune = on;
+  g_inv_d.clear();
+  g_inv_f.clear();
+  g_fwd.clear();
+  inv_plans_d.clear();
+  inv_plans_f.clear();
+  fwd_plans.clear();
 }
 
 template <typename R>
@@ -813,6 +877,12 @@ void HSS2D::fwd_prepare(int r) {
     }
   }
   HSS_CUDA(cudaStreamSynchronize(stream));
+  if (autotune)
+    for (int lev = 0; lev <= depth; ++lev) {
+      fp.up[lev].tune(stream);
+      fp.lam[lev].tune(stream);
+      fp.eta[lev].tune(stream);
+    }
 }
 
 void HSS2D::apply_stage(int r) {

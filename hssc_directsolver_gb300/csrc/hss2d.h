@@ -19,11 +19,15 @@ struct SolvePlan {
     DevBuf<GemmP<R>> d;
     DevBuf<SegGemmP> dseg;  // segmented products (df plans only)
     DevBuf<R> part;  // split-K partial sums
-    int batch = 0, maxM = 0, maxN = 0, ksplit = 1;
+    int batch = 0, maxM = 0, maxN = 0, maxK = 0, ksplit = 1;
     R alpha = R(1), beta = R(0);
   };
   std::vector<Step> steps;
   bool df = false;  // FP64 operands stored as float pairs, products on the FP32 pipes
+  void run_step(const Step& st, cudaStream_t s) const;
+  // time each step at K-split counts around the heuristic's and keep the fastest
+  // (a step must run at least 2% faster than the heuristic's choice to replace it)
+  void tune(cudaStream_t s);
   void add(const std::vector<GemmP<R>>& P, R alpha, R beta, cudaStream_t s);
   // C = alpha * sum_s sign_s A_s B_s + beta * C in one launch (df plans only)
   void add_seg(const std::vector<SegGemmP>& P, R alpha, R beta, cudaStream_t s);
@@ -90,6 +94,8 @@ struct HSS2D {
   std::map<int, FwdPlan> fwd_plans;
   GraphCache g_inv_d, g_inv_f, g_fwd;
   bool use_graphs = true;
+  bool autotune = false;  // tune the K split of every solve-plan step when the plan is built
+  void set_autotune(bool on);
   // double-float solve products (the inverse apply when its factors are FP64, the
   // forward apply of the refinement always in these modes)
   bool dfm() const {

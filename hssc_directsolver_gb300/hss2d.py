@@ -119,6 +119,11 @@ class InfoTree:
         L.check(L.lib().hss2d_phase_times(self._h, t.ctypes.data_as(L._DP)))
         return t
 
+    def set_autotune(self, on: bool = True):
+        """Tune the K split of every batched solve product when a solve plan is built
+        (``hss2d_set_autotune``)."""
+        L.check(L.lib().hss2d_set_autotune(self._h, 1 if on else 0))
+
     def interp_ranks(self):
         """(q_up, q_dn): rank of each box's low-rank T_up / T_dn, -1 where T is dense."""
         qu = np.zeros(self.nboxes, np.int32)

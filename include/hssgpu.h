@@ -278,6 +278,12 @@ int hss2d_solve(hss2d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
 int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
 /* tree sizes: depth, box count, N */
+/* on != 0: when a solve plan is built (first apply / inverse apply per column count), time
+ * every batched product at K-split counts around the built-in heuristic's and keep the
+ * fastest (2% hysteresis).  Solves then replay the tuned plan; results are reproducible
+ * within a plan but may differ in the last bits between tuned and untuned plans.  No
+ * reference counterpart (a GPU launch-shape choice). */
+int hss2d_set_autotune(hss2d_matrix* H, int32_t on);
 /* [x,flag,relres,iter] = bicgstab(Mapp, f, tol, maxit, Iapp) of the reference's iterative
  * solution (HSS2D/Test/Test_HSS2D_InverseCompression.m:201-228): Mapp = forward apply of
  * the compressed operator A, Iapp = inverse apply of the inverted handle M (e.g. a

@@ -359,3 +359,20 @@ def test_skeleton_interpolation_error(gpu, inter):
                          lambda b: (np.asarray(ot.I_src[b]), np.asarray(ot.J[b]), ot.k[b], ot.T_up[b], ot.cent[b]))
     assert max(eg) < 1e-8, eg
     assert all(g <= 2 * o + 1e-12 for g, o in zip(eg, eo)), (eg, eo)
+
+
+def test_autotuned_plans(gpu):
+    """hss2d_set_autotune: tuned solve plans give the untuned solution to rounding, the same
+    refinement count, and bit-identical results from one tuned solve to the next."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(params(16, "dfloat")))
+    f = np.random.default_rng(9).standard_normal((t.N, 5))
+    x0, r0, i0 = G2.HSS2D_solve(t, f, 1e-10, 4)
+    t.set_autotune(True)
+    x1, r1, i1 = G2.HSS2D_solve(t, f, 1e-10, 4)
+    x2, r2, i2 = G2.HSS2D_solve(t, f, 1e-10, 4)
+    assert i1 == i0 and r1 <= 1e-10
+    assert np.linalg.norm(x1 - x0) <= 1e-12 * np.linalg.norm(x0)
+    assert np.array_equal(x1, x2)
+    y = G2.HSS2D_apply_nsym(t, None, x1)
+    assert np.linalg.norm(y - f, axis=0).max() / np.linalg.norm(f, axis=0).min() <= 1e-10
