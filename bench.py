@@ -37,7 +37,8 @@ sys.path.insert(0, HERE)
 METRIC = "compress+invert s and solves/s at 1e-10 residual: mixed/batched vs plain FP64"
 
 # DRAM bytes (read + write) of the skinny-product kernels of one inverse apply at this
-# workload, from the ncu capture summarised in profiles/skinny_hss2d_n65536.md
+# workload, summed over the kernels of one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum per launch)
 TRAFFIC_PER_APPLYINV = {"dfloat": 2.0057e9, "dfloat_inv": 2.0057e9, "fp64": 1.9471e9}
 WORKLOAD = "HSS2D 256x256 grid (Ng=8, 32x32 panels, N=65536), leaf 8x8, tol 1e-10, 4 RHS"
 
@@ -277,7 +278,7 @@ def bench_config5(args, L, dev):
     [2048, 32768], ~23 M points) compressed plainly and with the rank MLP trained on the
     ranks of a 256-curve batched compress, plus the 1024 x 1024 HSS2D grid
     (N = 1,048,576) in the double-float inversion mode.  Reports seconds and the QR steps
-    the network saved; the adaptive ID stays the judge of every rank."""
+    the network saved; the adaptive ID still decides every rank."""
     import torch
     from hssc_directsolver_gb300 import hss1d as G1, hss2d as G2, kernels as GK, geometry as GG
     from hssc_directsolver_gb300.rank_mlp import RankPredictor, training_set
