@@ -1792,6 +1792,29 @@ __device__ __forceinline__ double rng_uniform(unsigned long long seed, unsigned 
   return (double)(z >> 11) * 0x1.0p-53;
 }
 
+// Householder scalars of one QR step: beta = -sign(alpha) sqrt(alpha^2 + xn2),
+// tau = (beta - alpha) / beta, scal = 1 / (alpha - beta) (tau = scal = 0, beta = alpha when
+// the column below the diagonal is zero).  Formed once by thread 0 and shared through s3,
+// so the block pays one FP64 square root and two divisions per step instead of 256.
+__device__ __forceinline__ void householder_scalars(double alpha, double xn2, double* s3, double& tau,
+                                                    double& beta, double& scal) {
+  if (threadIdx.x == 0) {
+    double t = 0.0, b = alpha, sc = 0.0;
+    if (xn2 != 0.0) {
+      b = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      t = (b - alpha) / b;
+      sc = 1.0 / (alpha - b);
+    }
+    s3[0] = t;
+    s3[1] = b;
+    s3[2] = sc;
+  }
+  __syncthreads();
+  tau = s3[0];
+  beta = s3[1];
+  scal = s3[2];
+}
+
 // T(0:k, 0:n-k) = R(0:k,0:k) \ R(0:k, k:n); T has leading dimension n.
 // Back substitution R(0:r0+1, 0:r0+1) x = b for one column held by a warp in
 // registers (tv[q] = row lane + 32 q, rows < 128).  Same operations in the same
@@ -1996,6 +2019,7 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
   extern __shared__ double s_dyn[];
   double* norms = s_dyn;  // n
   __shared__ double sh[8];
+  __shared__ double hs3[3];
   __shared__ double shv[8];
   __shared__ int shi[8];
   for (long long e = tid; e < (long long)m * n; e += 256) W[e] = p.A[e];
@@ -2046,13 +2070,8 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     double part = 0.0;
     for (int i = j + 1 + tid; i < m; i += 256) { const double v = W[i + (size_t)j * m]; part += v * v; }
     const double xn2 = block_sum256(part, sh);
-    const double alpha = W[j + (size_t)j * m];
-    double tau = 0.0, beta = alpha, scal = 0.0;
-    if (xn2 != 0.0) {
-      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-      tau = (beta - alpha) / beta;
-      scal = 1.0 / (alpha - beta);
-    }
+    double tau, beta, scal;
+    householder_scalars(W[j + (size_t)j * m], xn2, hs3, tau, beta, scal);
     for (int i = j + 1 + tid; i < m; i += 256) W[i + (size_t)j * m] *= scal;
     __syncthreads();
     if (tid == 0) W[j + (size_t)j * m] = beta;
@@ -2117,9 +2136,9 @@ __global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ 
   extern __shared__ double s_dyn[];
   float2* norms = reinterpret_cast<float2*>(s_dyn);  // n
   __shared__ double sh[8];
-  __shared__ double shv[8];
   __shared__ int shi[8];
   __shared__ float shh[8], shl[8];
+  __shared__ float hsf[6];
   for (long long e = tid; e < (long long)m * n; e += 256) {
     float h, lo;
     split_d2f(p.A[e], h, lo);
@@ -2144,13 +2163,29 @@ __global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ 
       }
       s_hint = min(l, j + max(4, j / 2));
     }
-    double best = -1.0;
+    // arg-max of the normalised float-pair norms (hi, then lo), lowest index among equals
+    float bh = -1.f, bl = 0.f;
     int bi = INT_MAX;
     for (int c = j + tid; c < n; c += 256) {
-      const double v = df_val(norms[c]);
-      if (v > best) { best = v; bi = c; }
+      const float2 v = norms[c];
+      if (v.x > bh || (v.x == bh && v.y > bl)) { bh = v.x; bl = v.y; bi = c; }
     }
-    block_argmax256(best, bi, shv, shi);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, bh, o), ol = __shfl_xor_sync(0xffffffffu, bl, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (oh > bh || (oh == bh && (ol > bl || (ol == bl && oi < bi)))) { bh = oh; bl = ol; bi = oi; }
+    }
+    __syncthreads();
+    if (lane == 0) { shh[w] = bh; shl[w] = bl; shi[w] = bi; }
+    __syncthreads();
+    bh = shh[0]; bl = shl[0]; bi = shi[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q)
+      if (shh[q] > bh || (shh[q] == bh && (shl[q] > bl || (shl[q] == bl && shi[q] < bi)))) {
+        bh = shh[q]; bl = shl[q]; bi = shi[q];
+      }
+    __syncthreads();
     if (bi == INT_MAX) bi = j;
     if (bi != j) {
       for (int i = tid; i < m; i += 256) {
@@ -2167,28 +2202,29 @@ __global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ 
     float xh = 0.f, xl = 0.f;
     for (int i = j + 1 + tid; i < m; i += 256) { const float2 v = W[i + (size_t)j * m]; df_madd(xh, xl, v.x, v.y, v.x, v.y); }
     block_sum256_df(xh, xl, shh, shl);
-    const double xn2 = (double)xh + (double)xl;
-    const double alpha = df_val(W[j + (size_t)j * m]);
-    double tau = 0.0, beta = alpha, scal = 0.0;
-    if (xn2 != 0.0) {
-      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-      tau = (beta - alpha) / beta;
-      scal = 1.0 / (alpha - beta);
+    // the step's scalars in FP64 by thread 0, shared as float pairs
+    if (tid == 0) {
+      const double xn2 = (double)xh + (double)xl;
+      const double alpha = df_val(W[j + (size_t)j * m]);
+      double tau = 0.0, beta = alpha, scal = 0.0;
+      if (xn2 != 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      split_d2f(scal, hsf[0], hsf[1]);
+      split_d2f(tau, hsf[2], hsf[3]);
+      split_d2f(beta, hsf[4], hsf[5]);
     }
-    float sch, scl, tah, tal;
-    split_d2f(scal, sch, scl);
-    split_d2f(tau, tah, tal);
+    __syncthreads();
+    const float sch = hsf[0], scl = hsf[1], tah = hsf[2], tal = hsf[3];
     for (int i = j + 1 + tid; i < m; i += 256) {
       float2 v = W[i + (size_t)j * m];
       df_mul(v.x, v.y, sch, scl);
       W[i + (size_t)j * m] = v;
     }
     __syncthreads();
-    if (tid == 0) {
-      float bh, bl;
-      split_d2f(beta, bh, bl);
-      W[j + (size_t)j * m] = make_float2(bh, bl);
-    }
+    if (tid == 0) W[j + (size_t)j * m] = make_float2(hsf[4], hsf[5]);
     for (int c = j + 1 + w; c < n; c += 8) {
       float dh = 0.f, dl = 0.f;
       if (lane == 0) { const float2 v = W[j + (size_t)c * m]; dh = v.x; dl = v.y; }
@@ -2359,6 +2395,7 @@ __global__ void __launch_bounds__(256) k_pqr_q(const PqrP* __restrict__ P) {
   double* W = p.W;
   extern __shared__ double s_dyn[];
   double* norms = s_dyn;  // n
+  __shared__ double hs3[3];
   __shared__ double sh[8];
   __shared__ double shv[8];
   __shared__ int shi[8];
@@ -2390,13 +2427,8 @@ __global__ void __launch_bounds__(256) k_pqr_q(const PqrP* __restrict__ P) {
     double part = 0.0;
     for (int i = j + 1 + tid; i < m; i += 256) { const double v = W[i + (size_t)j * ld]; part += v * v; }
     const double xn2 = block_sum256(part, sh);
-    const double alpha = W[j + (size_t)j * ld];
-    double tau = 0.0, beta = alpha, scal = 0.0;
-    if (xn2 != 0.0) {
-      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-      tau = (beta - alpha) / beta;
-      scal = 1.0 / (alpha - beta);
-    }
+    double tau, beta, scal;
+    householder_scalars(W[j + (size_t)j * ld], xn2, hs3, tau, beta, scal);
     for (int i = j + 1 + tid; i < m; i += 256) W[i + (size_t)j * ld] *= scal;
     __syncthreads();
     if (tid == 0) {
