@@ -943,10 +943,15 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_panel_cl(const InvP<R>* __res
       rowP[tid] = *cl.map_shared_rank(&pan[(bi - ob * rows_per) + tid * rows_per], ob);
     }
     cl.sync();  // every CTA holds rows j and bi before any CTA rewrites them
-    const R rp = R(1) / rowP[jj];
-    if (tid < nbk) s_row[tid] = (tid == jj) ? rp : rowP[tid] * rp;
+    // the pivot reciprocal is formed by the nbk threads that scale the pivot row only
+    // (an FP64 division in every thread would cost more than the column's update)
+    if (tid < nbk) {
+      const R rpt = R(1) / rowP[jj];
+      s_row[tid] = (tid == jj) ? rpt : rowP[tid] * rpt;
+    }
     if (crank == 0 && tid == 0) p.ipiv[j] = bi;
     __syncthreads();
+    const R rp = s_row[jj];
     for (int i = r0 + tid; i < r1; i += nt) {
       R* row = pan + (i - r0);
       if (i == j) {
@@ -1319,6 +1324,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __rest
   __shared__ R slot1[2];
   __shared__ R slot2[QR_NB];
   __shared__ R s_dot[QR_NB];
+  __shared__ R s_hh[2];
   __shared__ R s_tau[QR_NB];
   __shared__ R sh[32];
   __shared__ R s_gram[QR_NB][QR_NB + 1];
@@ -1356,18 +1362,26 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __rest
       if (j >= r0 && j < r1) slot1[1] = pan[(j - r0) + jj * rows_per];
     }
     cl.sync();
+    // the column's Householder scalars: thread 0 gathers the cluster's partial norms and
+    // forms them once (not one FP64 square root and two divisions per thread)
     const int oj = (j - j0) / rows_per;
-    R xn2 = R(0);
-    for (int q = 0; q < C; ++q) xn2 += *cl.map_shared_rank(&slot1[0], q);
-    const R alpha = *cl.map_shared_rank(&slot1[1], oj);
-    R tau, beta, scal;
-    if (xn2 == R(0)) { tau = R(0); beta = alpha; scal = R(0); }
-    else {
-      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-      tau = (beta - alpha) / beta;
-      scal = R(1) / (alpha - beta);
+    if (tid == 0) {
+      R xn2 = R(0);
+      for (int q = 0; q < C; ++q) xn2 += *cl.map_shared_rank(&slot1[0], q);
+      const R alpha = *cl.map_shared_rank(&slot1[1], oj);
+      R tau0, beta0, scal0;
+      if (xn2 == R(0)) { tau0 = R(0); beta0 = alpha; scal0 = R(0); }
+      else {
+        beta0 = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tau0 = (beta0 - alpha) / beta0;
+        scal0 = R(1) / (alpha - beta0);
+      }
+      s_tau[jj] = tau0;
+      s_hh[0] = beta0;
+      s_hh[1] = scal0;
     }
-    if (tid == 0) s_tau[jj] = tau;
+    __syncthreads();
+    const R tau = s_tau[jj], beta = s_hh[0], scal = s_hh[1];
     // reflector into the panel column (v_j = 1 on the diagonal row)
     for (int i = r0 + tid; i < r1; i += nt) {
       R* x = pan + (i - r0) + jj * rows_per;
