@@ -2352,10 +2352,21 @@ __global__ void __launch_bounds__(256) k_id_fixed(const IdP* __restrict__ P) {
           al += u * u; be += v * v; ga += u * v;
         }
         al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
-        if (ga != 0.0 && fabs(ga) > 1e-15 * sqrt(al * be)) {
+        // the rotation is formed by lane 0 and broadcast (its FP64 square roots and
+        // divisions would otherwise run in all 32 lanes and outweigh the update itself)
+        double c = 1.0, s = 0.0;
+        int rot = 0;
+        if (lane == 0 && ga != 0.0 && fabs(ga) > 1e-15 * sqrt(al * be)) {
           const double zeta = (be - al) / (2.0 * ga);
           const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = c * t;
+          rot = 1;
+        }
+        rot = __shfl_sync(0xffffffffu, rot, 0);
+        if (rot) {
+          c = __shfl_sync(0xffffffffu, c, 0);
+          s = __shfl_sync(0xffffffffu, s, 0);
           for (int i = lane; i < k; i += 32) {
             const double u = U[i + (size_t)a * k], v = U[i + (size_t)b * k];
             U[i + (size_t)a * k] = c * u - s * v;

@@ -106,9 +106,6 @@ struct HSS2D {
   bool dfinv() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
   // double-float products of the inversion (E, U, G, GE)
   bool dfgemm() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
-  // double-float trailing updates in the interpolation least squares (backward stable:
-  // the compressed operator keeps the compression tolerance, but T is not the FP64 T,
-  // so HSS_PREC_DFLOAT keeps the FP64 operator)
   // least squares for T with double-float trailing updates: the forward operator and the
   // inverse factors share the same T, so the solve's refinement is unaffected
   bool dftree() const { return prm.precision != HSS_PREC_FP64; }
