@@ -432,14 +432,51 @@ int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_
   HSS_REQUIRE(box >= 0 && box < h->nboxes && h->parent[box] >= 0, HSS_ERR_ARG,
               "box out of range (a root has no skeleton)");
   const int n = h->nskel[box], k = h->kskel[box];
+  const int nd = h->rn()[box], kd = h->rk()[box];
   if (I_skup) std::memcpy(I_skup, h->I_SKUP[box].data(), k * sizeof(int32_t));
-  if (I_skdn) std::memcpy(I_skdn, h->I_SKDN[box].data(), k * sizeof(int32_t));
+  if (I_skdn)  // rectangular handles: row indices into Xin
+    for (int t = 0; t < kd; ++t) I_skdn[t] = h->I_SKDN[box][t] - (h->rect ? (int)h->Ntot : 0);
   if (J_up) std::memcpy(J_up, h->J_UP[box].data(), n * sizeof(int32_t));
-  if (J_dn) std::memcpy(J_dn, h->J_DN[box].data(), n * sizeof(int32_t));
-  const size_t tc = (size_t)k * (n - k);
-  if (tc > 0) {
-    if (T_up) HSS_CUDA(cudaMemcpy(T_up, h->T_UP.p + h->oT[box], tc * sizeof(double), cudaMemcpyDeviceToHost));
-    if (T_dn) HSS_CUDA(cudaMemcpy(T_dn, h->T_DN.p + h->oT[box], tc * sizeof(double), cudaMemcpyDeviceToHost));
+  if (J_dn) std::memcpy(J_dn, h->J_DN[box].data(), nd * sizeof(int32_t));
+  const size_t tc = (size_t)k * (n - k), tcd = (size_t)kd * (nd - kd);
+  if (tc > 0 && T_up)
+    HSS_CUDA(cudaMemcpy(T_up, h->T_UP.p + h->oT[box], tc * sizeof(double), cudaMemcpyDeviceToHost));
+  if (tcd > 0 && T_dn)
+    HSS_CUDA(cudaMemcpy(T_dn, h->T_DN.p + h->roT()[box], tcd * sizeof(double), cudaMemcpyDeviceToHost));
+  HSS_CATCH
+}
+
+int hss1d_compress_rect(hss1d_matrix** out, const double* Xin, int64_t M, int64_t ldin, const double* Xout,
+                        int64_t N, int64_t ldout, int32_t leaf, double acc, const hss_kernel_params* kp,
+                        uint64_t seed) {
+  HSS_TRY
+  HSS_REQUIRE(out && kp, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *out = nullptr;
+  auto* h = new hss1d_matrix{nullptr};
+  try {
+    h->impl = new HSS1D();
+    h->impl->compress_rect(M, Xin, ldin, N, Xout, ldout, leaf, acc, *kp, seed);
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *out = h;
+  HSS_CATCH
+}
+
+int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t* cnt_in, int32_t* nskel_in,
+                    int32_t* kskel_in) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
+  const HSS1D* h = H->impl;
+  if (M) *M = h->rows();
+  for (int b = 0; b < h->nboxes; ++b) {
+    if (off_in) off_in[b] = h->roff()[b];
+    if (cnt_in) cnt_in[b] = h->rcnt()[b];
+    if (nskel_in) nskel_in[b] = h->rn()[b];
+    if (kskel_in) kskel_in[b] = h->rk()[b];
   }
   HSS_CATCH
 }
@@ -453,13 +490,13 @@ int hss1d_invert(hss1d_matrix* H) {
 
 static void host_roundtrip1(HSS1D* h, const double* X, double* Y, int nrhs, bool inv) {
   HSS_REQUIRE(X && Y && nrhs >= 1, HSS_ERR_ARG, "bad vector arguments");
-  const size_t cnt = (size_t)h->Ntot * nrhs;
+  const size_t cnt = (size_t)h->Ntot * nrhs, cnt_out = (size_t)h->rows() * nrhs;
   h->io_in.ensure(cnt);
-  h->io_out.ensure(cnt);
+  h->io_out.ensure(cnt_out);
   HSS_CUDA(cudaMemcpyAsync(h->io_in.p, X, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   if (inv) h->applyinv_device(h->io_in.p, h->io_out.p, nrhs);
   else h->apply_device(h->io_in.p, h->io_out.p, nrhs);
-  HSS_CUDA(cudaMemcpyAsync(Y, h->io_out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaMemcpyAsync(Y, h->io_out.p, cnt_out * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   HSS_CUDA(cudaStreamSynchronize(h->stream));
 }
 
@@ -582,6 +619,7 @@ int hss1d_apply_submatrix(hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I
   HSS_TRY
   HSS_REQUIRE(H && H->impl && I_dn && I_up && qq && uu && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
   HSS1D* h = H->impl;
+  HSS_REQUIRE(!h->rect, HSS_ERR_ARG, "apply_submatrix is defined for square handles only");
   const size_t N = (size_t)h->Ntot;
   // K(I_dn, I_up) qq(I_up) = rows I_dn of K (qq with the columns outside I_up zeroed)
   std::vector<double> q(N * nrhs), y(N * nrhs);
@@ -601,6 +639,7 @@ int hss1d_apply_submatrix(hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I
 int hss1d_apply_submatrix_boxes(const hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I_up, uint8_t* Box_dn,
                                 uint8_t* Box_up) {
   HSS_TRY
+  HSS_REQUIRE(H && H->impl && !H->impl->rect, HSS_ERR_ARG, "square handle required");
   HSS_REQUIRE(H && H->impl && I_dn && I_up && Box_dn && Box_up, HSS_ERR_ARG, "NULL argument");
   const HSS1D* h = H->impl;
   // children have larger ids than their parents: one pass from the leaves up

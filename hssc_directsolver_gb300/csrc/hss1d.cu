@@ -16,6 +16,7 @@
 #include <chrono>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <numeric>
 
@@ -175,6 +176,42 @@ static void circum_circle(const std::vector<double>& X, const std::vector<int>& 
   }
 }
 
+// LOCAL_get_tree (HSS1D_compress_nsym.m:277-334): problem p's tree over n points from
+// point `base`, built breadth first by halving (son1 takes ceil(n/2)) while a box holds
+// more than `leaf` points; global box ids continue the forest's numbering.
+void HSS1D::append_tree(int p, int base, int n) {
+  const int g0 = (int)level.size();
+  prob.push_back(p); level.push_back(0); parent.push_back(-1); c1.push_back(-1); c2.push_back(-1);
+  off.push_back(base); cnt.push_back(n);
+  int last = g0 - 1, created = 1, ilev = 0;
+  while (created > 0) {
+    const int first = last + 1;
+    last = last + created;
+    created = 0;
+    for (int b = first; b <= last; ++b) {
+      const int nbx = cnt[b];
+      if (nbx > leaf) {
+        const int half = (nbx + 1) / 2;
+        const int s1 = last + created + 1;
+        c1[b] = s1;
+        c2[b] = s1 + 1;
+        for (int t = 0; t < 2; ++t) {
+          prob.push_back(p);
+          level.push_back(ilev + 1);
+          parent.push_back(b);
+          c1.push_back(-1);
+          c2.push_back(-1);
+          off.push_back(t == 0 ? off[b] : off[b] + half);
+          cnt.push_back(t == 0 ? half : nbx - half);
+        }
+        created += 2;
+      }
+    }
+    ++ilev;
+  }
+  HSS_REQUIRE((int)level.size() - g0 >= 3, HSS_ERR_ARG, "each problem must exceed the leaf size (one split)");
+}
+
 HSS1D::HSS1D() { HSS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); }
 HSS1D::~HSS1D() {
   if (stream) cudaStreamDestroy(stream);
@@ -217,37 +254,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
   prob.clear(); level.clear(); parent.clear(); c1.clear(); c2.clear(); off.clear(); cnt.clear();
   proot.assign(nprob, 0);
   for (int p = 0; p < nprob; ++p) {
-    const int g0 = (int)level.size();
-    proot[p] = g0;
-    prob.push_back(p); level.push_back(0); parent.push_back(-1); c1.push_back(-1); c2.push_back(-1);
-    off.push_back((int)pbase[p]); cnt.push_back((int)pN[p]);
-    int last = g0 - 1, created = 1, ilev = 0;
-    while (created > 0) {
-      const int first = last + 1;
-      last = last + created;
-      created = 0;
-      for (int b = first; b <= last; ++b) {
-        const int nbx = cnt[b];
-        if (nbx > leaf) {
-          const int half = (nbx + 1) / 2;
-          const int s1 = last + created + 1;
-          c1[b] = s1;
-          c2[b] = s1 + 1;
-          for (int t = 0; t < 2; ++t) {
-            prob.push_back(p);
-            level.push_back(ilev + 1);
-            parent.push_back(b);
-            c1.push_back(-1);
-            c2.push_back(-1);
-            off.push_back(t == 0 ? off[b] : off[b] + half);
-            cnt.push_back(t == 0 ? half : nbx - half);
-          }
-          created += 2;
-        }
-      }
-      ++ilev;
-    }
-    HSS_REQUIRE((int)level.size() - g0 >= 3, HSS_ERR_ARG, "each problem must exceed the leaf size (one split)");
+    proot[p] = (int)level.size();
+    append_tree(p, (int)pbase[p], (int)pN[p]);
   }
   nboxes = (int)level.size();
   maxlev = *std::max_element(level.begin(), level.end());
@@ -672,6 +680,364 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
 }
 
 // ---------------------------------------------------------------------------
+// K_HSS = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params),
+// HSS1D/HSS1D_compress_rectangular_nsym.m:70-266: the M x N matrix K(Xin, Xout).  The
+// columns follow the halving tree over Xout; the rows a tree of the same shape over Xin
+// whose parents split their rows ceil(m/2) | rest (LOCAL_get_tree_in, :325-356).  Per box
+// one circle around its row and column candidates carries one proxy ring (:116-140), and
+// A_out = [K(rows inside, cols); K(ring, cols)] and A_in^T = [K(rows, cols inside),
+// K(rows, ring)]^T are IDed level-batched with independent ranks (:209-236; no rank
+// equalisation).  Point table: Xout at [0, N), Xin at [N, N + M), the rings after.
+void HSS1D::compress_rect(long long M, const double* Xin, long long ldin, long long N, const double* Xout,
+                          long long ldout, int leaf_, double acc_, const hss_kernel_params& kp_,
+                          unsigned long long seed) {
+  HSS_REQUIRE(Xin && Xout && M >= 2 && N >= 2 && ldin >= M && ldout >= N && leaf_ >= 1 && acc_ > 0 && acc_ < 1,
+              HSS_ERR_ARG, "bad rectangular compress args");
+  HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
+  HSS_REQUIRE(M + N < (1LL << 30), HSS_ERR_ARG, "total points too large");
+  std::fill(phase_s, phase_s + NPHASE, 0.0);
+  rect = true;
+  sym = false;
+  nprob = 1; leaf = leaf_; acc = acc_; kp = kp_;
+  kdev = make_kernel_dev(kp);
+  Ntot = N;
+  Mtot = M;
+  pN = {N}; pbase = {0}; pseed = {seed};
+  proot.assign(1, 0);
+  const long long NP = N + M;
+  X.resize(6 * (size_t)NP);
+  for (long long i = 0; i < N; ++i)
+    for (int c = 0; c < 6; ++c) X[6 * i + c] = Xout[i + c * ldout];
+  for (long long i = 0; i < M; ++i)
+    for (int c = 0; c < 6; ++c) X[6 * (N + i) + c] = Xin[i + c * ldin];
+  prob.clear(); level.clear(); parent.clear(); c1.clear(); c2.clear(); off.clear(); cnt.clear();
+  append_tree(0, 0, (int)N);
+  nboxes = (int)level.size();
+  maxlev = *std::max_element(level.begin(), level.end());
+  // ---- row tree (LOCAL_get_tree_in): parents come before their sons
+  off_in.assign(nboxes, 0);
+  cnt_in.assign(nboxes, 0);
+  cnt_in[0] = (int)M;
+  for (int b = 0; b < nboxes; ++b) {
+    if (c1[b] < 0 || c2[b] < 0) continue;
+    const int half = (cnt_in[b] + 1) / 2;
+    off_in[c1[b]] = off_in[b]; cnt_in[c1[b]] = half;
+    off_in[c2[b]] = off_in[b] + half; cnt_in[c2[b]] = cnt_in[b] - half;
+  }
+  for (int b = 0; b < nboxes; ++b)
+    HSS_REQUIRE(cnt_in[b] >= 1, HSS_ERR_ARG, "every box of the row tree needs a point (M too small for the tree)");
+  auto rows_of = [&](int b) {  // table indices of box b's rows
+    std::vector<int> r(cnt_in[b]);
+    std::iota(r.begin(), r.end(), (int)N + off_in[b]);
+    return r;
+  };
+  auto cols_of = [&](int b) {
+    std::vector<int> r(cnt[b]);
+    std::iota(r.begin(), r.end(), off[b]);
+    return r;
+  };
+  // ---- neighbour lists (:397-462): one circle per box around its rows and columns;
+  // nei_in keeps the boxes whose columns come inside it, nei_out those whose rows do
+  std::vector<std::vector<int>> nei_in(nboxes), nei_out(nboxes);
+  nei_in[0] = {0};
+  nei_out[0] = {0};
+  for (int b = 1; b < nboxes; ++b) {
+    std::vector<int> r = rows_of(b);
+    const std::vector<int> c = cols_of(b);
+    r.insert(r.end(), c.begin(), c.end());
+    double xc, yc, R;
+    circum_circle(X, r, xc, yc, R);
+    const double rr = RADIUS_REL * RADIUS_REL * R * R;
+    for (int side = 0; side < 2; ++side) {
+      auto& lst = side == 0 ? nei_in : nei_out;
+      std::vector<int> pot;
+      for (int j : lst[parent[b]]) {
+        if (c1[j] >= 0) pot.push_back(c1[j]);
+        if (c2[j] >= 0) pot.push_back(c2[j]);
+      }
+      for (int j : pot) {
+        const long long o = side == 0 ? off[j] : N + off_in[j];
+        const int n = side == 0 ? cnt[j] : cnt_in[j];
+        double mn = INFINITY;
+        for (long long i = o; i < o + n; ++i) {
+          const double dx = X[6 * (size_t)i] - xc, dy = X[6 * (size_t)i + 1] - yc;
+          mn = std::min(mn, dx * dx + dy * dy);
+        }
+        if (n > 0 && mn < rr) lst[b].push_back(j);
+      }
+    }
+  }
+  for (auto* lst : {&nei_in, &nei_out})
+    for (int b = 1; b < nboxes; ++b) {
+      auto& l = (*lst)[b];
+      l.erase(std::remove(l.begin(), l.end(), b), l.end());
+      std::sort(l.begin(), l.end());
+    }
+  // ---- point table with one proxy ring per non-root box, in the order levels run
+  std::vector<int> pslot(nboxes, -1);
+  int nslot = 0;
+  for (int L = maxlev; L >= 1; --L)
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == L) pslot[b] = nslot++;
+  const size_t npts = (size_t)NP + (size_t)NPROXY * nslot;
+  HSS_REQUIRE(npts < (1ULL << 31), HSS_ERR_ARG, "point table exceeds 2^31 entries");
+  std::vector<double> hx(npts, 0.0), hy(npts, 0.0), hnx(npts, 0.0), hny(npts, 0.0), hw(npts, 0.0),
+      hk(npts, 0.0);
+  for (long long i = 0; i < NP; ++i) {
+    hx[i] = X[6 * i]; hy[i] = X[6 * i + 1]; hnx[i] = X[6 * i + 2]; hny[i] = X[6 * i + 3];
+    hw[i] = X[6 * i + 4]; hk[i] = X[6 * i + 5];
+  }
+  pts.reserve(npts);
+  pts.upload_range(0, (size_t)NP, hx.data(), hy.data(), hnx.data(), hny.data(), hw.data(), hk.data(), kp, stream);
+  nskel.assign(nboxes, 0); kskel.assign(nboxes, 0);
+  nskel_in.assign(nboxes, 0); kskel_in.assign(nboxes, 0);
+  I_SKUP.assign(nboxes, {}); I_SKDN.assign(nboxes, {});
+  J_UP.assign(nboxes, {}); J_DN.assign(nboxes, {});
+  census.assign(4 * (size_t)nboxes, 0);
+  feat.assign((size_t)NFEAT * nboxes, 0.f);
+  qr_steps = qr_steps_full = 0;
+  reruns = 0;
+  std::vector<DevBuf<double>> Tkeep;
+  std::vector<std::array<long long, 2>> Toff(nboxes);
+  std::vector<int> Tlev(nboxes, -1);
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<int> boxes;
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == L) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    const int nbL = (int)boxes.size();
+    // problem 2q: A_out (rows_out x outs), problem 2q+1: A_in^T (rows_in x inns)
+    std::vector<std::vector<int>> outs(nbL), inns(nbL), rows_out(nbL), rows_in(nbL);
+    parallel_for(nbL, [&](int q) {
+      const int b = boxes[q];
+      if (is_leaf(b)) {
+        outs[q] = cols_of(b);
+        inns[q] = rows_of(b);
+      } else {
+        HSS_REQUIRE(c1[b] >= 0 && c2[b] >= 0, HSS_ERR_ARG, "one-child boxes are not produced by the halving tree");
+        outs[q] = I_SKUP[c1[b]];
+        outs[q].insert(outs[q].end(), I_SKUP[c2[b]].begin(), I_SKUP[c2[b]].end());
+        inns[q] = I_SKDN[c1[b]];
+        inns[q].insert(inns[q].end(), I_SKDN[c2[b]].begin(), I_SKDN[c2[b]].end());
+      }
+      // circle around [Xin(sort(rows)); Xout(sort(cols))] (:125-126)
+      std::vector<int> both = inns[q], so = outs[q];
+      std::sort(both.begin(), both.end());
+      std::sort(so.begin(), so.end());
+      both.insert(both.end(), so.begin(), so.end());
+      double xc, yc, R;
+      circum_circle(X, both, xc, yc, R);
+      const double Rp = RADIUS_REL * R;
+      const double stop = 2.0 * M_PI * (1.0 - 1.0 / NPROXY);
+      const double step = stop / (double)(NPROXY - 1);
+      const size_t pb = (size_t)NP + (size_t)NPROXY * pslot[b];
+      for (int t = 0; t < NPROXY; ++t) {
+        const double tt = (t == NPROXY - 1) ? stop : (double)t * step;
+        const double c = std::cos(tt), s = std::sin(tt);
+        hx[pb + t] = xc + Rp * c;
+        hy[pb + t] = yc + Rp * s;
+        hnx[pb + t] = c;
+        hny[pb + t] = s;
+        hw[pb + t] = 2.0 * M_PI * Rp / NPROXY;
+        hk[pb + t] = 1.0 / Rp;
+      }
+      std::vector<int> out_maybe, in_maybe;
+      for (int j : nei_in[b]) {
+        if (is_leaf(j)) {
+          const std::vector<int> r = cols_of(j);
+          out_maybe.insert(out_maybe.end(), r.begin(), r.end());
+        } else {
+          for (int s : {c1[j], c2[j]}) out_maybe.insert(out_maybe.end(), I_SKUP[s].begin(), I_SKUP[s].end());
+        }
+      }
+      for (int j : nei_out[b]) {
+        if (is_leaf(j)) {
+          const std::vector<int> r = rows_of(j);
+          in_maybe.insert(in_maybe.end(), r.begin(), r.end());
+        } else {
+          for (int s : {c1[j], c2[j]}) in_maybe.insert(in_maybe.end(), I_SKDN[s].begin(), I_SKDN[s].end());
+        }
+      }
+      const double rr = Rp * Rp;
+      auto inside = [&](int i) {
+        const double dx = X[6 * (size_t)i] - xc, dy = X[6 * (size_t)i + 1] - yc;
+        return dx * dx + dy * dy < rr;
+      };
+      for (int i : in_maybe)
+        if (inside(i)) rows_out[q].push_back(i);
+      for (int i : out_maybe)
+        if (inside(i)) rows_in[q].push_back(i);
+      for (int t = 0; t < NPROXY; ++t) {
+        rows_out[q].push_back((int)(pb + t));
+        rows_in[q].push_back((int)(pb + t));
+      }
+      HSS_REQUIRE(outs[q].size() <= 4096 && inns[q].size() <= 4096, HSS_ERR_RANK,
+                  "skeleton set exceeds 4096 points");
+      HSS_REQUIRE(!outs[q].empty() && !inns[q].empty(), HSS_ERR_RANK, "empty skeleton set (rank 0 children)");
+    }, 16);
+    {
+      const size_t p0 = (size_t)NP + (size_t)NPROXY * pslot[boxes[0]];
+      pts.upload_range(p0, (size_t)NPROXY * nbL, hx.data() + p0, hy.data() + p0, hnx.data() + p0, hny.data() + p0,
+                       hw.data() + p0, hk.data() + p0, kp, stream);
+    }
+    std::vector<int> idx;
+    std::vector<long long> o_ro(nbL), o_ri(nbL), o_out(nbL), o_in(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      o_ro[q] = idx.size(); idx.insert(idx.end(), rows_out[q].begin(), rows_out[q].end());
+      o_ri[q] = idx.size(); idx.insert(idx.end(), rows_in[q].begin(), rows_in[q].end());
+      o_out[q] = idx.size(); idx.insert(idx.end(), outs[q].begin(), outs[q].end());
+      o_in[q] = idx.size(); idx.insert(idx.end(), inns[q].begin(), inns[q].end());
+    }
+    DevBuf<int> didx;
+    upload_vec(didx, idx, stream);
+    const int nprob2 = 2 * nbL;
+    std::vector<long long> oA(nprob2), oT2(nprob2), oX(nprob2), oY(nprob2), oP(nprob2);
+    std::vector<int> pm(nprob2), pn(nprob2);
+    long long tA = 0, tT = 0, tX = 0, tY = 0, tP = 0;
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int q = pr / 2;
+      pm[pr] = (int)(pr % 2 == 0 ? rows_out[q].size() : rows_in[q].size());
+      pn[pr] = (int)(pr % 2 == 0 ? outs[q].size() : inns[q].size());
+      oA[pr] = tA; tA += (long long)pm[pr] * pn[pr];
+      oT2[pr] = tT; tT += (long long)pn[pr] * pn[pr];
+      oX[pr] = tX; tX += 2LL * pn[pr];
+      oY[pr] = tY; tY += (long long)pm[pr] + pn[pr];
+      oP[pr] = tP; tP += pn[pr];
+    }
+    DevBuf<double> A(tA), W(tA), SW(tT), SV(tT), xw(tX), yw(tY);
+    Tkeep.emplace_back(tT);
+    DevBuf<double>& Tb = Tkeep.back();
+    DevBuf<int> perm(tP), rank(nprob2);
+    std::vector<KgenP<double>> kg(nprob2);
+    std::vector<IdP> ip(nprob2);
+    for (int q = 0; q < nbL; ++q) {
+      const int po = 2 * q, pi = po + 1;
+      kg[po] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[po], pn[po], A.p + oA[po], pm[po], 0};
+      kg[pi] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], pn[pi], pm[pi], A.p + oA[pi], pm[pi], 1};
+    }
+    for (int pr = 0; pr < nprob2; ++pr)
+      ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], pm[pr], pn[pr], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * boxes[pr / 2] + pr % 2, -1,
+                   seed, nullptr};
+    long long maxe = 0;
+    for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
+    DevBuf<KgenP<double>> dkg;
+    upload_vec(dkg, kg, stream);
+    for (int o = 0; o < nprob2; o += 65535)
+      kgen_batched<double>(dkg.p + o, std::min(65535, nprob2 - o), maxe, view(pts), kdev, stream);
+    DevBuf<IdP> dip;
+    upload_vec(dip, ip, stream);
+    id_adaptive_batched(dip.p, nprob2, acc, stream, id_df);
+    std::vector<int> hr, hp;
+    download(hr, rank.p, nprob2, stream);
+    download(hp, perm.p, tP, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], po = 2 * q, pi = po + 1;
+      const int ko = hr[po], ki = hr[pi];
+      nskel[b] = pn[po]; kskel[b] = ko;
+      nskel_in[b] = pn[pi]; kskel_in[b] = ki;
+      J_UP[b].assign(hp.begin() + oP[po], hp.begin() + oP[po] + pn[po]);
+      J_DN[b].assign(hp.begin() + oP[pi], hp.begin() + oP[pi] + pn[pi]);
+      I_SKUP[b].resize(ko);
+      I_SKDN[b].resize(ki);
+      for (int t = 0; t < ko; ++t) I_SKUP[b][t] = outs[q][J_UP[b][t]];
+      for (int t = 0; t < ki; ++t) I_SKDN[b][t] = inns[q][J_DN[b][t]];
+      Toff[b] = {oT2[po], oT2[pi]};
+      Tlev[b] = (int)Tkeep.size() - 1;
+      census[4 * b] = pm[po]; census[4 * b + 1] = pm[pi]; census[4 * b + 2] = pn[po]; census[4 * b + 3] = ko;
+    }
+  }
+  // ---- compact T_UP (k_out x (n_out - k_out)), T_DN / T_DN^T (row side) and the J arenas
+  oT.assign(nboxes, 0); oTd.assign(nboxes, 0);
+  oJ.assign(nboxes, 0); oJd.assign(nboxes, 0);
+  long long tu = 0, td = 0, ju = 0, jd = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    oT[b] = tu; tu += (long long)kskel[b] * (nskel[b] - kskel[b]);
+    oTd[b] = td; td += (long long)kskel_in[b] * (nskel_in[b] - kskel_in[b]);
+    oJ[b] = ju; ju += nskel[b];
+    oJd[b] = jd; jd += nskel_in[b];
+  }
+  T_UP.alloc(std::max(tu, 1LL)); T_DN.alloc(std::max(td, 1LL)); TDNT.alloc(std::max(td, 1LL));
+  std::vector<MoveP> mv;
+  std::vector<int> hJU(std::max(ju, 1LL)), hJD(std::max(jd, 1LL));
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
+    std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJd[b]);
+    const double* Tl = Tkeep[Tlev[b]].p;
+    const int n = nskel[b], k = kskel[b], ni = nskel_in[b], ki = kskel_in[b];
+    if (n - k > 0 && k > 0) mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    if (ni - ki > 0 && ki > 0) {
+      mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oTd[b], nullptr, ki, ni - ki, ni, ki, 0, 0});
+      mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oTd[b], nullptr, ki, ni - ki, ni, ni - ki, 3, 0});
+    }
+  }
+  run_moves(mv, stream);
+  upload_vec(JUPd, hJU, stream);
+  upload_vec(JDNd, hJD, stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  Tkeep.clear();
+  // ---- M_SELF = K(Xin(rows), Xout(cols)) on leaves, M_SIB{s1} = K(Xin(I_SKDN{s1}),
+  // Xout(I_SKUP{s2})) (:240-266)
+  oSelf.assign(nboxes, -1);
+  oSib.assign(nboxes, -1);
+  long long ts = 0, tb = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0 && is_leaf(b)) { oSelf[b] = ts; ts += (long long)cnt_in[b] * cnt[b]; }
+    if (!is_leaf(b)) {
+      const int s1 = c1[b], s2 = c2[b];
+      oSib[s1] = tb; tb += (long long)kskel_in[s1] * kskel[s2];
+      oSib[s2] = tb; tb += (long long)kskel_in[s2] * kskel[s1];
+    }
+  }
+  M_SELF.alloc(std::max(ts, 1LL));
+  M_SIB.alloc(std::max(tb, 1LL));
+  std::vector<int> idx;
+  std::vector<long long> io;
+  auto push = [&](const std::vector<int>& v) { io.push_back(idx.size()); idx.insert(idx.end(), v.begin(), v.end()); };
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0 && is_leaf(b)) { push(rows_of(b)); push(cols_of(b)); }
+    if (!is_leaf(b)) {
+      push(I_SKDN[c1[b]]); push(I_SKUP[c2[b]]);
+      push(I_SKDN[c2[b]]); push(I_SKUP[c1[b]]);
+    }
+  }
+  DevBuf<int> didx;
+  upload_vec(didx, idx, stream);
+  std::vector<KgenP<double>> kg;
+  size_t q = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0 && is_leaf(b)) {
+      const int* r = didx.p + io[q++];
+      const int* c = didx.p + io[q++];
+      kg.push_back(KgenP<double>{r, c, cnt_in[b], cnt[b], M_SELF.p + oSelf[b], cnt_in[b], 0});
+    }
+    if (!is_leaf(b)) {
+      const int s1 = c1[b], s2 = c2[b];
+      const int* a = didx.p + io[q++];
+      const int* bb = didx.p + io[q++];
+      const int* c = didx.p + io[q++];
+      const int* d = didx.p + io[q++];
+      kg.push_back(KgenP<double>{a, bb, kskel_in[s1], kskel[s2], M_SIB.p + oSib[s1], std::max(kskel_in[s1], 1), 0});
+      kg.push_back(KgenP<double>{c, d, kskel_in[s2], kskel[s1], M_SIB.p + oSib[s2], std::max(kskel_in[s2], 1), 0});
+    }
+  }
+  long long maxe = 0;
+  for (auto& g : kg) maxe = std::max(maxe, (long long)g.m * g.n);
+  DevBuf<KgenP<double>> dkg;
+  upload_vec(dkg, kg, stream);
+  for (size_t o = 0; o < kg.size(); o += 65535) {
+    const int c = (int)std::min<size_t>(65535, kg.size() - o);
+    kgen_batched<double>(dkg.p + o, c, maxe, view(pts), kdev, stream);
+  }
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  inverted = false;
+  clear_plans();
+}
+
+// ---------------------------------------------------------------------------
 // Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv), HSS1D/HSS1D_transforminv_nsym.m:38-161.
 // Rewrites the inverse factors as an HSS1D matrix in the compressed format, so that the
 // forward apply of K applies the inverse.  Three tree sweeps, each level batched over every
@@ -687,6 +1053,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
 // places, every leaf's M_SELF is transposed, and each sibling pair's M_SIB blocks are
 // swapped and transposed (HSS1D_transpose.m:24-50).
 void HSS1D::transpose(HSS1D& K) const {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "transpose is defined for square handles only");
   K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;
   K.pN = pN; K.pbase = pbase; K.proot = proot; K.pseed = pseed;
   K.prob = prob; K.level = level; K.parent = parent; K.c1 = c1; K.c2 = c2; K.off = off; K.cnt = cnt;
@@ -759,6 +1126,7 @@ void HSS1D::scalarmult(double c) {
 // forward apply of identity columns, the rows of problem p kept.  (The reference builds
 // it from the telescoping factors, HSS1D_dense_matrix.m:17-92; both are the same matrix.)
 void HSS1D::dense_matrix(int p, double* Kd) {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "dense_matrix is defined for square handles only");
   HSS_REQUIRE(p >= 0 && p < nprob, HSS_ERR_ARG, "dense_matrix: problem index out of range");
   HSS_REQUIRE(Kd != nullptr, HSS_ERR_ARG, "dense_matrix: NULL output");
   const long long Np = pN[p], base = pbase[p];
@@ -778,6 +1146,7 @@ void HSS1D::dense_matrix(int p, double* Kd) {
 }
 
 void HSS1D::transforminv(HSS1D& K) {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "transforminv is defined for square handles only");
   HSS_REQUIRE(inverted, HSS_ERR_STATE, "transforminv needs the inverse factors (call invert first)");
   K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;
   K.pN = pN; K.pbase = pbase; K.proot = proot; K.pseed = pseed;
@@ -947,6 +1316,7 @@ void HSS1D::transforminv(HSS1D& K) {
 
 // ---------------------------------------------------------------------------
 void HSS1D::invert() {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "invert is defined for square handles only");
   clear_plans();
   oL.assign(nboxes, 0); oR.assign(nboxes, 0); oD.assign(nboxes, 0); oE.assign(nboxes, 0);
   long long tl = 0, td = 0, te = 0;
@@ -1080,7 +1450,9 @@ struct Stack1 {
   std::vector<long long> row;   // per box: row offset within its level
 };
 
-static Stack1 make_stack(const HSS1D& H, int width) {
+// k: skeleton size of each box (the column side's kskel, or the row side's on a
+// rectangular handle)
+static Stack1 make_stack(const HSS1D& H, int width, const std::vector<int>& k) {
   Stack1 s;
   s.base.assign(H.maxlev + 2, 0);
   s.ld.assign(H.maxlev + 2, 0);
@@ -1088,7 +1460,7 @@ static Stack1 make_stack(const HSS1D& H, int width) {
   for (int b = 0; b < H.nboxes; ++b) {
     if (H.parent[b] < 0) continue;
     s.row[b] = s.ld[H.level[b]];
-    s.ld[H.level[b]] += H.kskel[b];
+    s.ld[H.level[b]] += k[b];
   }
   long long acc = 0;
   for (int L = 0; L <= H.maxlev + 1; ++L) { s.base[L] = acc; acc += (long long)s.ld[L] * width; }
@@ -1138,15 +1510,15 @@ int Plan1::launches() const {
 }
 
 void HSS1D::ensure_work() {
-  const Stack1 S = make_stack(*this, 8);
+  const Stack1 S = make_stack(*this, 8, kskel), Sd = make_stack(*this, 8, rk());
   v1.ensure(std::max(S.base.back(), 1LL));
-  v2.ensure(std::max(S.base.back(), 1LL));
+  v2.ensure(std::max(Sd.base.back(), 1LL));
   long long ts = 0;
   for (int b = 0; b < nboxes; ++b)
-    if (parent[b] >= 0) ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8;
+    if (parent[b] >= 0) ts += (long long)std::max({nskel[b] - kskel[b], rn()[b] - rk()[b], 1}) * 8;
   v3.ensure(std::max(ts, 1LL));
   Xs.ensure((size_t)Ntot * 8);
-  Ys.ensure((size_t)Ntot * 8);
+  Ys.ensure((size_t)rows() * 8);
 }
 
 // inverse apply of r columns Xs -> Ys (HSS1D_applyinv_nsym.m:43-86): up Rinv, top FTinv,
@@ -1161,7 +1533,7 @@ Plan1& HSS1D::inv_plan(int r) {
   const double* LI = dfm() ? Linv_df.p : Linv.p;
   const double* DI = dfm() ? Dinv_df.p : Dinv.p;
   const double* FT = dfm() ? FTinv_df.p : FTinv.p;
-  const Stack1 S = make_stack(*this, 8);
+  const Stack1 S = make_stack(*this, 8, kskel);
   const double* ff = Xs.p;
   double* xx = Ys.p;
   auto vin = [&](int b, const double*& p, int& ld) {
@@ -1241,6 +1613,7 @@ void HSS1D::set_precision(int prec) {
 }
 
 void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "applyinv is defined for square handles only");
   HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_applyinv before hss1d_invert");
   for (int c0 = 0; c0 < nrhs; c0 += 8) {
     const int r = std::min(8, nrhs - c0);
@@ -1254,7 +1627,9 @@ void HSS1D::applyinv_device(const double* dX, double* dY, int nrhs) {
 }
 
 // forward apply of r columns Xs -> Ys (HSS1D_apply_nsym.m:38-100): up projections
-// q(J(1:k)) + T_UP q(J(k+1:n)), top siblings, down evaluations with M_SIB / M_SELF
+// q(J(1:k)) + T_UP q(J(k+1:n)), top siblings, down evaluations with M_SIB / M_SELF.  On a
+// rectangular handle (HSS1D_apply_rect_nsym.m:30-106) the down pass runs on the row tree:
+// its stack, T_DN, J_DN and the leaves' rows come from the row side (rk(), roff() ...).
 Plan1& HSS1D::fwd_plan(int r) {
   auto it = fwd_plans.find(r);
   if (it != fwd_plans.end()) return it->second;
@@ -1265,13 +1640,16 @@ Plan1& HSS1D::fwd_plan(int r) {
   const double* TD = dfm() ? TDNT_df.p : TDNT.p;
   const double* MS = dfm() ? M_SELF_df.p : M_SELF.p;
   const double* MB = dfm() ? M_SIB_df.p : M_SIB.p;
-  const Stack1 S = make_stack(*this, 8);
+  const std::vector<int>&kd = rk(), &nd = rn(), &od = roff(), &cd = rcnt();
+  const std::vector<long long>&oTdn = roT(), &oJdn = roJ();
+  const int ldu = (int)rows();
+  const Stack1 S = make_stack(*this, 8, kskel), Sd = make_stack(*this, 8, kd);
   std::vector<long long> oS(nboxes, 0);
   long long ts = 0;
   for (int b = 0; b < nboxes; ++b) {
     if (parent[b] < 0) continue;
     oS[b] = ts;
-    ts += (long long)std::max(nskel[b] - kskel[b], 1) * 8;
+    ts += (long long)std::max({nskel[b] - kskel[b], nd[b] - kd[b], 1}) * 8;
   }
   const double* qq = Xs.p;
   double* uu = Ys.p;
@@ -1304,10 +1682,10 @@ Plan1& HSS1D::fwd_plan(int r) {
     std::vector<GemmP<double>> P;
     for (int p = 0; p < nprob; ++p) {
       const int a = c1[proot[p]], b = c2[proot[p]];
-      P.push_back(GemmP<double>{MB + oSib[a], v1.p + S.base[1] + S.row[b], v2.p + S.base[1] + S.row[a],
-                                kskel[a], r, kskel[b], kskel[a], S.ld[1], S.ld[1]});
-      P.push_back(GemmP<double>{MB + oSib[b], v1.p + S.base[1] + S.row[a], v2.p + S.base[1] + S.row[b],
-                                kskel[b], r, kskel[a], kskel[b], S.ld[1], S.ld[1]});
+      P.push_back(GemmP<double>{MB + oSib[a], v1.p + S.base[1] + S.row[b], v2.p + Sd.base[1] + Sd.row[a],
+                                kd[a], r, kskel[b], std::max(kd[a], 1), S.ld[1], Sd.ld[1]});
+      P.push_back(GemmP<double>{MB + oSib[b], v1.p + S.base[1] + S.row[a], v2.p + Sd.base[1] + Sd.row[b],
+                                kd[b], r, kskel[a], std::max(kd[b], 1), S.ld[1], Sd.ld[1]});
     }
     pl.gemm(P, 1.0, 0.0, stream);
   }
@@ -1315,24 +1693,24 @@ Plan1& HSS1D::fwd_plan(int r) {
     std::vector<GemmP<double>> PT, PS;
     std::vector<MoveP> mv;
     for (int b : bylev[L]) {
-      const int n = nskel[b], k = kskel[b], nr = n - k;
-      const double* dn = v2.p + S.base[L] + S.row[b];
+      const int n = nd[b], k = kd[b], nr = n - k;
+      const double* dn = v2.p + Sd.base[L] + Sd.row[b];
       double* out;
       int ldo;
-      if (is_leaf(b)) { out = uu + off[b]; ldo = (int)Ntot; }
-      else { out = v2.p + S.base[L + 1] + S.row[c1[b]]; ldo = S.ld[L + 1]; }
-      if (nr > 0) PT.push_back(GemmP<double>{TD + oT[b], dn, v3.p + oS[b], nr, r, k, nr, S.ld[L], nr});
-      mv.push_back(MoveP{dn, out, JDNd.p + oJ[b], k, r, S.ld[L], ldo, 2, 0});
-      if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJ[b] + k, nr, r, nr, ldo, 2, 0});
+      if (is_leaf(b)) { out = uu + od[b]; ldo = ldu; }
+      else { out = v2.p + Sd.base[L + 1] + Sd.row[c1[b]]; ldo = Sd.ld[L + 1]; }
+      if (nr > 0) PT.push_back(GemmP<double>{TD + oTdn[b], dn, v3.p + oS[b], nr, r, k, nr, Sd.ld[L], nr});
+      mv.push_back(MoveP{dn, out, JDNd.p + oJdn[b], k, r, Sd.ld[L], ldo, 2, 0});
+      if (nr > 0) mv.push_back(MoveP{v3.p + oS[b], out, JDNd.p + oJdn[b] + k, nr, r, nr, ldo, 2, 0});
       if (is_leaf(b)) {
-        PS.push_back(GemmP<double>{MS + oSelf[b], qq + off[b], out, n, r, n, n, (int)Ntot, ldo});
+        PS.push_back(GemmP<double>{MS + oSelf[b], qq + off[b], out, cd[b], r, cnt[b], cd[b], (int)Ntot, ldo});
       } else {
         const int s1 = c1[b], s2 = c2[b];
         const double* up1 = v1.p + S.base[L + 1] + S.row[s1];
         const double* up2 = v1.p + S.base[L + 1] + S.row[s2];
-        PS.push_back(GemmP<double>{MB + oSib[s1], up2, out, kskel[s1], r, kskel[s2], kskel[s1], S.ld[L + 1],
-                                   ldo});
-        PS.push_back(GemmP<double>{MB + oSib[s2], up1, out + kskel[s1], kskel[s2], r, kskel[s1], kskel[s2],
+        PS.push_back(GemmP<double>{MB + oSib[s1], up2, out, kd[s1], r, kskel[s2], std::max(kd[s1], 1),
+                                   S.ld[L + 1], ldo});
+        PS.push_back(GemmP<double>{MB + oSib[s2], up1, out + kd[s1], kd[s2], r, kskel[s1], std::max(kd[s2], 1),
                                    S.ld[L + 1], ldo});
       }
     }
@@ -1351,7 +1729,7 @@ void HSS1D::apply_device(const double* dX, double* dY, int nrhs) {
     HSS_CUDA(cudaMemcpyAsync(Xs.p, dX + (size_t)c0 * Ntot, (size_t)Ntot * r * sizeof(double),
                              cudaMemcpyDeviceToDevice, stream));
     run_graph(g_fwd, r, stream, use_graphs, [&] { pl.run(stream); });
-    HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * Ntot, Ys.p, (size_t)Ntot * r * sizeof(double),
+    HSS_CUDA(cudaMemcpyAsync(dY + (size_t)c0 * rows(), Ys.p, (size_t)rows() * r * sizeof(double),
                              cudaMemcpyDeviceToDevice, stream));
   }
 }
@@ -1392,6 +1770,7 @@ __global__ void k_axpy1(long long n, const double* __restrict__ d, double* __res
 
 void HSS1D::solve_device(const double* df, double* dx, int nrhs, double tol, int maxit, double* relres,
                          int* iters) {
+  HSS_REQUIRE(!rect, HSS_ERR_ARG, "solve is defined for square handles only");
   HSS_REQUIRE(inverted, HSS_ERR_STATE, "hss1d_solve before hss1d_invert");
   HSS_REQUIRE(nrhs >= 1 && maxit >= 1, HSS_ERR_ARG, "nrhs and maxit must be >= 1");
   const long long cnt = Ntot * nrhs;

@@ -52,6 +52,22 @@ struct HSS1D {
   int nprob = 0, nboxes = 0, leaf = 0, maxlev = 0;
   double acc = 0;
   bool sym = false;  // fsym compression: one ID per box, incoming skeletons = outgoing
+  // rectangular K(Xin, Xout) (HSS1D_compress_rectangular_nsym): the columns follow the tree
+  // of off/cnt over the Ntot points of Xout, the rows a tree of the same shape with
+  // off_in/cnt_in over the Mtot points of Xin (K_HSS rows 16:17) and row-side skeleton sizes
+  // nskel_in/kskel_in (rows 18:19).  In the point table Xin follows Xout, so I_SKDN holds
+  // Ntot + (row index).  Square handles keep these empty and read the column side.
+  bool rect = false;
+  long long Mtot = 0;
+  std::vector<int> off_in, cnt_in, nskel_in, kskel_in;
+  std::vector<long long> oTd, oJd;  // T_DN / TDNT and J_DN arena offsets of the row side
+  const std::vector<int>& rk() const { return rect ? kskel_in : kskel; }
+  const std::vector<int>& rn() const { return rect ? nskel_in : nskel; }
+  const std::vector<int>& roff() const { return rect ? off_in : off; }
+  const std::vector<int>& rcnt() const { return rect ? cnt_in : cnt; }
+  const std::vector<long long>& roT() const { return rect ? oTd : oT; }
+  const std::vector<long long>& roJ() const { return rect ? oJd : oJ; }
+  long long rows() const { return rect ? Mtot : Ntot; }
   bool id_df = false;  // the IDs' pivoted QR in double-float arithmetic (k_id_adaptive_df)
   std::vector<long long> pN, pbase;   // points per problem, first global point
   std::vector<int> proot;              // root box of each problem
@@ -119,6 +135,11 @@ struct HSS1D {
   void compress(int nprob, const long long* N, const double* const* Xp, const long long* ldx, int leaf, double acc,
                 const hss_kernel_params& kp, const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false);
   void invert();
+  // the M x N matrix K(Xin, Xout) (HSS1D_compress_rectangular_nsym); Xin / Xout are M x 6 /
+  // N x 6 column-major blocks [x y nx ny w kappa]
+  void append_tree(int p, int base, int n);
+  void compress_rect(long long M, const double* Xin, long long ldin, long long N, const double* Xout,
+                     long long ldout, int leaf, double acc, const hss_kernel_params& kp, unsigned long long seed);
   // K = the inverse in compressed format (HSS1D_transforminv_nsym)
   void transforminv(HSS1D& K);
   // K = the transpose in compressed format (HSS1D_transpose)

@@ -4,9 +4,11 @@
     [HSSinv,FTinv] = HSS1D_invert_nsym(K_HSS, acc)
     uu             = HSS1D_apply_nsym(K_HSS, qq)
     xx             = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff)
+    K_HSS          = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params)
+    uu             = HSS1D_apply_rect_nsym(K_HSS, qq)
 
 (HSS1D/HSS1D_compress_nsym.m:1, HSS1D_invert_nsym.m:1, HSS1D_apply_nsym.m:1,
-HSS1D_applyinv_nsym.m:1).  All work runs in libhssgpu.so on the GPU; the
+HSS1D_applyinv_nsym.m:1, HSS1D_compress_rectangular_nsym.m:1, HSS1D_apply_rect_nsym.m:1).  All work runs in libhssgpu.so on the GPU; the
 returned K_HSS object owns the device factors.
 """
 from __future__ import annotations
@@ -51,12 +53,26 @@ class HSS1DMatrix:
         arrs["nboxes"] = n
         return arrs
 
+    def rect_info(self):
+        """Row side (K_HSS rows 16:19): M and per box off_in, cnt_in, nskel_in, kskel_in
+        (the column side again on a square matrix)."""
+        n = self.info()["nboxes"]
+        M = C.c_int64()
+        arrs = {k: np.zeros(n, dtype=np.int32) for k in ("off_in", "cnt_in", "nskel_in", "kskel_in")}
+        p = lambda a: a.ctypes.data_as(L._I32P)
+        L.check(L.lib().hss1d_rect_info(self._h, C.byref(M), p(arrs["off_in"]), p(arrs["cnt_in"]),
+                                        p(arrs["nskel_in"]), p(arrs["kskel_in"])))
+        arrs["M"] = M.value
+        return arrs
+
     def export_box(self, box: int):
         inf = self.info()
+        rinf = self.rect_info()
         n, k = int(inf["nskel"][box]), int(inf["kskel"][box])
-        out = dict(I_SKUP=np.zeros(k, np.int32), I_SKDN=np.zeros(k, np.int32),
-                   J_UP=np.zeros(n, np.int32), J_DN=np.zeros(n, np.int32),
-                   T_UP=np.zeros((k, n - k), order="F"), T_DN=np.zeros((k, n - k), order="F"))
+        nd, kd = int(rinf["nskel_in"][box]), int(rinf["kskel_in"][box])
+        out = dict(I_SKUP=np.zeros(k, np.int32), I_SKDN=np.zeros(kd, np.int32),
+                   J_UP=np.zeros(n, np.int32), J_DN=np.zeros(nd, np.int32),
+                   T_UP=np.zeros((k, n - k), order="F"), T_DN=np.zeros((kd, nd - kd), order="F"))
         ip = lambda a: a.ctypes.data_as(L._I32P)
         dp = lambda a: a.ctypes.data_as(L._DP)
         L.check(L.lib().hss1d_export_box(self._h, box, ip(out["I_SKUP"]), ip(out["I_SKDN"]), ip(out["J_UP"]),
@@ -133,6 +149,46 @@ def HSS1D_compress_fsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel
     L.check(L.lib().hss1d_compress_fsym(C.byref(h), L.ptr(Xf), Xf.shape[0], Xf.shape[0], int(TREE), float(acc),
                                         C.byref(kp), int(seed)))
     return HSS1DMatrix(h, Xf.shape[0])
+
+
+def _points6(X):
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim != 2 or X.shape[1] not in (2, 6):
+        raise ValueError("points must be n x 2 or n x 6 ([x y nx ny w kappa])")
+    if X.shape[1] == 2:
+        X6 = np.zeros((X.shape[0], 6))
+        X6[:, :2] = X
+        X = X6
+    return np.asfortranarray(X)
+
+
+def HSS1D_compress_rectangular_nsym(type_: str, Xin, Xout, TREE: int, acc: float, params: Kernel,
+                                    seed: int = 0) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params)
+    (HSS1D/HSS1D_compress_rectangular_nsym.m:1): the M x N matrix K(Xin, Xout) with a
+    column tree over Xout and a row tree of the same shape over Xin.  Apply it with
+    ``HSS1D_apply_rect_nsym``."""
+    if type_ != "green":
+        raise ValueError("only the 'green' construction is implemented on the GPU")
+    Xi, Xo = _points6(Xin), _points6(Xout)
+    h = C.c_void_p()
+    kp = params.to_c()
+    L.check(L.lib().hss1d_compress_rect(C.byref(h), L.ptr(Xi), Xi.shape[0], Xi.shape[0], L.ptr(Xo), Xo.shape[0],
+                                        Xo.shape[0], int(TREE), float(acc), C.byref(kp), int(seed)))
+    K = HSS1DMatrix(h, Xo.shape[0])
+    K.M = Xi.shape[0]
+    return K
+
+
+def HSS1D_apply_rect_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
+    """uu = HSS1D_apply_rect_nsym(K_HSS, qq) (HSS1D/HSS1D_apply_rect_nsym.m:1): qq has N rows
+    (Xout), uu has M rows (Xin)."""
+    q = _as_f64(qq)
+    vec = q.ndim == 1
+    q2 = q.reshape(K_HSS.N, -1, order="F")
+    out = np.zeros((getattr(K_HSS, "M", K_HSS.N), q2.shape[1]), order="F")
+    L.check(L.lib().hss1d_apply(K_HSS._h, L.ptr(q2), L.ptr(out), q2.shape[1]))
+    return out[:, 0] if vec else out
 
 
 def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None,
@@ -265,7 +321,7 @@ def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
     q = _as_f64(qq)
     vec = q.ndim == 1
     q2 = q.reshape(K_HSS.N, -1, order="F")
-    out = np.zeros_like(q2, order="F")
+    out = np.zeros((getattr(K_HSS, "M", K_HSS.N), q2.shape[1]), order="F")
     L.check(L.lib().hss1d_apply(K_HSS._h, L.ptr(q2), L.ptr(out), q2.shape[1]))
     return out[:, 0] if vec else out
 

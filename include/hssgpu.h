@@ -139,6 +139,24 @@ int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* 
  * T_* are k x (n-k) column-major; any pointer may be NULL. */
 int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_t* I_skdn,
                      int32_t* J_up, int32_t* J_dn, double* T_up, double* T_dn);
+/* K_HSS = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params)
+ *   HSS1D/HSS1D_compress_rectangular_nsym.m:1 (trees :70-88 with LOCAL_get_tree_in :325-356,
+ *   neighbour lists :397-462, skeletons :112-236, self/sibling blocks :238-266): the M x N
+ *   matrix K(Xin, Xout).  Xin: M x 6 and Xout: N x 6 column-major [x y nx ny w kappa].  The
+ *   columns follow the halving tree over Xout (leaf = nbox_max), the rows a tree of the same
+ *   shape over Xin (each of its boxes must keep at least one point).  Outgoing and incoming
+ *   ranks are independent.  hss1d_apply then computes uu (M x nrhs) = K qq (qq: N x nrhs),
+ *   HSS1D/HSS1D_apply_rect_nsym.m:1; hss1d_info gives the column tree, hss1d_rect_info the
+ *   row side, and hss1d_export_box returns I_SKDN as row indices into Xin.  invert,
+ *   applyinv, solve, transforminv, transpose, dense_matrix and apply_submatrix return
+ *   HSS_ERR_ARG on such a handle. */
+int hss1d_compress_rect(hss1d_matrix** out, const double* Xin, int64_t M, int64_t ldin, const double* Xout,
+                        int64_t N, int64_t ldout, int32_t leaf, double acc, const hss_kernel_params* kp,
+                        uint64_t seed);
+/* row side of a handle (K_HSS rows 16:19): M, and per box the first row and row count in
+ * Xin and the incoming skeleton sizes (a square handle reports its column side) */
+int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t* cnt_in, int32_t* nskel_in,
+                    int32_t* kskel_in);
 /* [HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D/HSS1D_invert_nsym.m:44-91 */
 int hss1d_invert(hss1d_matrix* H);
 /* Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv),

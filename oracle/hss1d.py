@@ -7,6 +7,7 @@ Follows, function by function:
   HSS1D/HSS1D_apply_nsym.m      (:38-130)
   HSS1D/HSS1D_applyinv_nsym.m   (:43-86)
   HSS1D/HSS1D_transforminv_nsym.m (:38-161)
+  HSS1D/HSS1D_compress_rectangular_nsym.m, HSS1D/HSS1D_apply_rect_nsym.m (rectangular K(Xin, Xout))
 
 The cell array ``K_HSS{row, ibox}`` of Common/box_constants.m:33-52 becomes an
 ``HSS1DMatrix`` whose per-box lists are indexed by the 0-based box id (box 0 is
@@ -632,3 +633,173 @@ def apply_submatrix(H: HSS1DMatrix, I_dn, I_up, qq):
     I_up = np.asarray(I_up, dtype=bool)
     Kd = dense_matrix(H)
     return Kd[np.ix_(I_dn, I_up)] @ np.asarray(qq)[I_up]
+
+
+# ---------------------------------------------------------------------------
+# Rectangular HSS1D: K(Xin, Xout), HSS1D/HSS1D_compress_rectangular_nsym.m and
+# HSS1D/HSS1D_apply_rect_nsym.m
+# ---------------------------------------------------------------------------
+@dataclass
+class HSS1DRectMatrix(HSS1DMatrix):
+    """K_HSS of HSS1D_compress_rectangular_nsym: ``tree`` is the column (out) tree over
+    Xout; the row (in) tree has the same shape with offsets/counts ``off_in``/``cnt_in``
+    over Xin (K_HSS rows 16:17) and skeleton sizes ``nskel_in``/``kskel_in`` (rows 18:19).
+    I_SKUP indexes Xout, I_SKDN indexes Xin."""
+    off_in: np.ndarray = None
+    cnt_in: np.ndarray = None
+    nskel_in: list = field(default_factory=list)
+    kskel_in: list = field(default_factory=list)
+    mtot: int = 0
+
+
+def get_tree_in(mtot: int, tree: HSS1DTree):
+    """LOCAL_get_tree_in, HSS1D_compress_rectangular_nsym.m:325-356: the row tree takes the
+    column tree's shape; a parent's rows split as ceil(m/2) | rest (parents come first)."""
+    nb = tree.nboxes
+    off = np.zeros(nb, dtype=np.int64)
+    cnt = np.zeros(nb, dtype=np.int64)
+    cnt[0] = mtot
+    for b in range(nb):
+        s1, s2 = tree.c1[b], tree.c2[b]
+        if s1 >= 0 and s2 >= 0:
+            half = (cnt[b] + 1) // 2
+            off[s1], cnt[s1] = off[b], half
+            off[s2], cnt[s2] = off[b] + half, cnt[b] - half
+    return off, cnt
+
+
+def neighbor_list_rect(Xin, Xout, tree: HSS1DTree, off_in, cnt_in, radius_rel=RADIUS_REL):
+    """LOCAL_construct_potential_neighborlist, HSS1D_compress_rectangular_nsym.m:397-462.
+    One circle per box around its rows and columns; nei_in keeps the boxes whose COLUMN
+    points come inside it, nei_out those whose ROW points do."""
+    nb = tree.nboxes
+    nei_in = [[] for _ in range(nb)]
+    nei_out = [[] for _ in range(nb)]
+    nei_in[0] = [0]
+    nei_out[0] = [0]
+    for ibox in range(1, nb):
+        P = np.vstack([Xin[off_in[ibox]:off_in[ibox] + cnt_in[ibox]],
+                       Xout[tree.off[ibox]:tree.off[ibox] + tree.cnt[ibox]]])
+        xxc, R = circum_circle(P)
+        rr = radius_rel * radius_rel * R * R
+        for lst, pts, offs, cnts in ((nei_in, Xout, tree.off, tree.cnt), (nei_out, Xin, off_in, cnt_in)):
+            pot = []
+            for jbox in lst[tree.parent[ibox]]:
+                if tree.c1[jbox] >= 0:
+                    pot.append(int(tree.c1[jbox]))
+                if tree.c2[jbox] >= 0:
+                    pot.append(int(tree.c2[jbox]))
+            for jbox in pot:
+                o, c = offs[jbox], cnts[jbox]
+                d = (pts[o:o + c, 0] - xxc[0]) ** 2 + (pts[o:o + c, 1] - xxc[1]) ** 2
+                if c > 0 and np.min(d) < rr:
+                    lst[ibox].append(jbox)
+    for lst in (nei_in, nei_out):
+        for ibox in range(1, nb):
+            l = list(lst[ibox])
+            if ibox in l:
+                l.remove(ibox)
+            lst[ibox] = sorted(l)
+    return nei_in, nei_out
+
+
+def compress_rectangular_nsym(Xin: np.ndarray, Xout: np.ndarray, leaf: int, acc: float, kp: KernelParams,
+                              seed: int = 0) -> HSS1DRectMatrix:
+    """K_HSS = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params) for the
+    M x N matrix K(Xin, Xout), HSS1D_compress_rectangular_nsym.m:70-266.
+
+    Per box (fine to coarse, :112-236): one circle around the box's row and column
+    skeleton candidates, one proxy ring on it (50 points for Laplace kernels),
+    A_out = [K(rows inside, cols); K(ring, cols)] and A_in = [K(rows, cols inside),
+    K(rows, ring)], then ID(A_out) and ID(A_in.') with independent ranks (no rank
+    equalisation, unlike the square compress).  Problem numbers of the shared RNG:
+    2*b (outgoing) and 2*b+1 (incoming), as in compress_nsym.  Leaves keep
+    M_SELF = K(Xin(rows), Xout(cols)); siblings M_SIB{s1} = K(Xin(I_SKDN{s1}),
+    Xout(I_SKUP{s2})) (:240-266)."""
+    Xin = np.asarray(Xin, dtype=np.float64)
+    Xout = np.asarray(Xout, dtype=np.float64)
+    mtot, ntot = Xin.shape[0], Xout.shape[0]
+    t = get_tree(ntot, leaf)
+    off_in, cnt_in = get_tree_in(mtot, t)
+    nb = t.nboxes
+    H = HSS1DRectMatrix(t, off_in=off_in, cnt_in=cnt_in, mtot=mtot)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census", "nskel_in", "kskel_in"):
+        setattr(H, name, [None] * nb)
+    nei_in, nei_out = neighbor_list_rect(Xin, Xout, t, off_in, cnt_in)
+    cat = lambda L: np.concatenate(L) if L else np.zeros(0, dtype=np.int64)
+    in_range = lambda b: np.arange(off_in[b], off_in[b] + cnt_in[b])
+    for ibox in range(nb - 1, 0, -1):
+        if t.is_leaf(ibox):
+            out, inn = _leaf_range(t, ibox), in_range(ibox)
+        else:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            out = np.concatenate([H.I_SKUP[s1], H.I_SKUP[s2]])
+            inn = np.concatenate([H.I_SKDN[s1], H.I_SKDN[s2]])
+        xxc, R = circum_circle(np.vstack([Xin[np.sort(inn, kind="stable")], Xout[np.sort(out, kind="stable")]]))
+        Cp = proxy_circle(xxc, RADIUS_REL * R, NPROXY)
+        out_maybe, in_maybe = [], []
+        for j in nei_in[ibox]:
+            out_maybe += [_leaf_range(t, j)] if t.is_leaf(j) else [H.I_SKUP[t.c1[j]], H.I_SKUP[t.c2[j]]]
+        for j in nei_out[ibox]:
+            in_maybe += [in_range(j)] if t.is_leaf(j) else [H.I_SKDN[t.c1[j]], H.I_SKDN[t.c2[j]]]
+        out_maybe, in_maybe = cat(out_maybe), cat(in_maybe)
+        rr = (RADIUS_REL * R) ** 2
+        out_inside = out_maybe[(Xout[out_maybe, 0] - xxc[0]) ** 2 + (Xout[out_maybe, 1] - xxc[1]) ** 2 < rr]
+        in_inside = in_maybe[(Xin[in_maybe, 0] - xxc[0]) ** 2 + (Xin[in_maybe, 1] - xxc[1]) ** 2 < rr]
+        A_out = np.vstack([kernel_eval(Xin[in_inside], Xout[out], kp), kernel_eval(Cp, Xout[out], kp)])
+        A_in = np.hstack([kernel_eval(Xin[inn], Xout[out_inside], kp), kernel_eval(Xin[inn], Cp, kp)])
+        Tout, Jout, kout, _ = idecomp.id_adaptive(A_out, acc, seed, 2 * ibox)
+        Tin, Jin, kin, _ = idecomp.id_adaptive(A_in.T, acc, seed, 2 * ibox + 1)
+        H.I_SKUP[ibox] = out[Jout[:kout]]
+        H.T_UP[ibox] = Tout
+        H.J_UP[ibox] = Jout
+        H.I_SKDN[ibox] = inn[Jin[:kin]]
+        H.T_DN[ibox] = Tin
+        H.J_DN[ibox] = Jin
+        H.nskel[ibox], H.kskel[ibox] = len(out), kout
+        H.nskel_in[ibox], H.kskel_in[ibox] = len(inn), kin
+        H.census[ibox] = (A_out.shape[0], A_in.shape[1], len(out), len(inn), kout, kin)
+    for ibox in range(nb - 1, -1, -1):
+        if t.is_leaf(ibox):
+            H.M_SELF[ibox] = kernel_eval(Xin[in_range(ibox)], Xout[_leaf_range(t, ibox)], kp)
+        elif t.c1[ibox] >= 0 and t.c2[ibox] >= 0:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            H.M_SIB[s1] = kernel_eval(Xin[H.I_SKDN[s1]], Xout[H.I_SKUP[s2]], kp)
+            H.M_SIB[s2] = kernel_eval(Xin[H.I_SKDN[s2]], Xout[H.I_SKUP[s1]], kp)
+    return H
+
+
+def apply_rect_nsym(H: HSS1DRectMatrix, qq: np.ndarray) -> np.ndarray:
+    """uu = HSS1D_apply_rect_nsym(K_HSS, qq), HSS1D_apply_rect_nsym.m:30-106: the upward
+    projections run on the column tree, the downward evaluations on the row tree, and
+    the leaves add M_SELF qq(cols) into uu(rows) (uu has mtot rows)."""
+    t = H.tree
+    nb = t.nboxes
+    qq = np.asarray(qq, dtype=np.float64)
+    vec = qq.ndim == 1
+    if vec:
+        qq = qq[:, None]
+    up = [None] * nb
+    dn = [None] * nb
+    for b in range(nb - 1, 0, -1):
+        if t.is_leaf(b):
+            up[b] = _skel_proj(H.T_UP[b], H.J_UP[b], qq[_leaf_range(t, b)])
+    for b in range(nb - 1, 0, -1):
+        if not t.is_leaf(b):
+            up[b] = _skel_proj(H.T_UP[b], H.J_UP[b], np.vstack([up[t.c1[b]], up[t.c2[b]]]))
+    dn[1] = H.M_SIB[1] @ up[2]
+    dn[2] = H.M_SIB[2] @ up[1]
+    for b in range(1, nb):
+        if not t.is_leaf(b):
+            s1, s2 = t.c1[b], t.c2[b]
+            n1 = len(H.I_SKDN[s1])
+            u = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b])
+            dn[s1] = u[:n1] + H.M_SIB[s1] @ up[s2]
+            dn[s2] = u[n1:] + H.M_SIB[s2] @ up[s1]
+    uu = np.zeros((H.mtot, qq.shape[1]))
+    for b in range(nb - 1, 0, -1):
+        if t.is_leaf(b):
+            rows = np.arange(H.off_in[b], H.off_in[b] + H.cnt_in[b])
+            uu[rows] = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b]) + H.M_SELF[b] @ qq[_leaf_range(t, b)]
+    return uu[:, 0] if vec else uu

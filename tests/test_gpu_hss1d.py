@@ -371,3 +371,72 @@ def test_dfloat_id_compress(gpu):
     assert rr <= 1e-12
     with pytest.raises(ValueError):
         G1.HSS1D_compress_batch(Xs[:1], 64, 1e-10, k, id_precision="fp32")
+
+
+def _outer_star(M, s):
+    P = geometry.star_curve(M).copy()
+    P[:, :2] *= s
+    P[:, 4] *= s
+    P[:, 5] /= s
+    return P
+
+
+def _rect_parity(G1, H, Ho, Xin, Xout, kpo, nrhs=11, tol=1e-9):
+    """Trees, ranks and skeletons equal the oracle's; the apply equals the oracle's to 1e-12
+    and the dense K(Xin, Xout) to the compression tolerance."""
+    inf, ri = H.info(), H.rect_info()
+    nb = inf["nboxes"]
+    assert ri["M"] == Xin.shape[0]
+    assert np.array_equal(ri["off_in"], Ho.off_in) and np.array_equal(ri["cnt_in"], Ho.cnt_in)
+    assert np.array_equal(inf["kskel"][1:], Ho.kskel[1:])
+    assert np.array_equal(ri["kskel_in"][1:], Ho.kskel_in[1:])
+    for b in range(1, nb):
+        e = H.export_box(b)
+        assert np.array_equal(e["I_SKUP"], Ho.I_SKUP[b]) and np.array_equal(e["I_SKDN"], Ho.I_SKDN[b])
+    q = np.random.default_rng(3).standard_normal((Xout.shape[0], nrhs))   # more than one 8-column chunk
+    u = G1.HSS1D_apply_rect_nsym(H, q)
+    uo = O1.apply_rect_nsym(Ho, q)
+    assert u.shape == (Xin.shape[0], nrhs)
+    assert np.linalg.norm(u - uo) <= 1e-12 * np.linalg.norm(uo)
+    K = OK.kernel_eval(Xin, Xout, kpo)
+    assert np.linalg.norm(u - K @ q) <= tol * np.linalg.norm(K @ q)
+    return u, q
+
+
+@pytest.mark.parametrize("N,M,leaf,s", [(1500, 1100, 64, 1.2), (700, 1000, 50, 0.85)])
+def test_rect_compress_apply_matches_oracle(gpu, N, M, leaf, s):
+    """HSS1D_compress_rectangular_nsym + HSS1D_apply_rect_nsym on two curves (M < N and
+    M > N); the double-float apply agrees with the FP64 one; square-only calls refuse."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    Xout, Xin = geometry.star_curve(N), _outer_star(M, s)
+    kpo = OK.KernelParams(flag=OK.DL_L_2D)
+    H = G1.HSS1D_compress_rectangular_nsym("green", Xin, Xout, leaf, 1e-10, GK.Kernel("DL_L_2D"))
+    Ho = O1.compress_rectangular_nsym(Xin, Xout, leaf, 1e-10, kpo)
+    u, q = _rect_parity(G1, H, Ho, Xin, Xout, kpo)
+    H.set_precision("dfloat")
+    ud = G1.HSS1D_apply_rect_nsym(H, q)
+    assert np.linalg.norm(ud - u) <= 1e-12 * np.linalg.norm(u)
+    for call in (lambda: G1.HSS1D_invert_nsym(H), lambda: G1.HSS1D_transpose(H),
+                 lambda: G1.HSS1D_dense_matrix(H)):
+        with pytest.raises(Exception):
+            call()
+
+
+def test_rect_reference_call_site(gpu):
+    """The reference's use (interpolation_operator_HSS.m:64): K(X_proxy, X1) between a level-1
+    box's proxy layers and its skeleton (Ng=8, np=16, SL_L_2D), nbox_max 108, acc/10."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    Ng, npan = 8, 16
+    h = 2.0 / (Ng * npan)
+    b, c = OK.reference_modulations(sym=0, proxy=1, transinv=0)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=h, b=b, c=c)
+    prm = O2.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    tree = O2.build_tree_nsym(prm, with_T=False)
+    X1 = prm.X_source()[tree.I_sk[1]]
+    colrad, rowrad = O2.box_radii(1)
+    Xp = O2.build_box_proxy(tree.cent[1], colrad, rowrad, O2.lay_prox(prm, 1), h)
+    Xp = Xp[np.argsort(np.arctan2(Xp[:, 1] - tree.cent[1][1], Xp[:, 0] - tree.cent[1][0]), kind="stable")]
+    gk = GK.Kernel("SL_L_2D", h, GK.Modulation(b.alpha, b.x0, b.y0, b.isig), GK.Modulation(c.alpha, c.x0, c.y0, c.isig))
+    H = G1.HSS1D_compress_rectangular_nsym("green", Xp, X1, 108, 1e-11, gk)
+    Ho = O1.compress_rectangular_nsym(Xp, X1, 108, 1e-11, kp)
+    _rect_parity(G1, H, Ho, Xp, X1, kp, nrhs=4, tol=1e-9)

@@ -247,3 +247,35 @@ def test_hss2d_skeleton_interpolation_error(inter):
     errs = skeleton_errors(prm.X_source(), prm.h, prm.layers, t.depth, kp,
                            lambda b: (np.asarray(t.I_src[b]), np.asarray(t.J[b]), t.k[b], t.T_up[b], t.cent[b]))
     assert max(errs) < 1e-8, errs
+
+
+def _outer_star(M, s):
+    """The star curve scaled by s (normals kept, weights and curvature rescaled)."""
+    P = geometry.star_curve(M).copy()
+    P[:, :2] *= s
+    P[:, 4] *= s
+    P[:, 5] /= s
+    return P
+
+
+@pytest.mark.parametrize("N,M,leaf,s", [(600, 450, 64, 1.2), (500, 700, 50, 0.85)])
+def test_hss1d_rectangular_compress_apply(N, M, leaf, s):
+    """HSS1D_compress_rectangular_nsym / HSS1D_apply_rect_nsym restated: the row tree has
+    the column tree's shape with ceil halving of the rows, and the compressed K(Xin, Xout)
+    applies within the ID tolerance of the dense matrix."""
+    from oracle import hss1d as O
+    Xout, Xin = geometry.star_curve(N), _outer_star(M, s)
+    kp = kernels.KernelParams(flag=kernels.DL_L_2D)
+    H = O.compress_rectangular_nsym(Xin, Xout, leaf, 1e-10, kp)
+    t = H.tree
+    assert H.cnt_in[0] == M and H.off_in[0] == 0
+    for b in range(t.nboxes):
+        if not t.is_leaf(b):
+            s1, s2 = t.c1[b], t.c2[b]
+            assert H.cnt_in[s1] == (H.cnt_in[b] + 1) // 2 and H.off_in[s2] == H.off_in[b] + H.cnt_in[s1]
+    assert any(H.kskel[b] != H.kskel_in[b] for b in range(1, t.nboxes))   # ranks are not equalised
+    K = kernels.kernel_eval(Xin, Xout, kp)
+    q = np.random.default_rng(1).standard_normal((N, 3))
+    u = O.apply_rect_nsym(H, q)
+    assert u.shape == (M, 3)
+    assert np.linalg.norm(u - K @ q) <= 1e-9 * np.linalg.norm(K @ q)
