@@ -481,6 +481,24 @@ int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t*
   HSS_CATCH
 }
 
+int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_matrix** C) {
+  HSS_TRY
+  HSS_REQUIRE(A && A->impl && B && B->impl && C, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *C = nullptr;
+  auto* h = new hss1d_matrix{nullptr};
+  try {
+    h->impl = new HSS1D();
+    h->impl->sum(*A->impl, *B->impl, acc);
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *C = h;
+  HSS_CATCH
+}
+
 int hss1d_invert(hss1d_matrix* H) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

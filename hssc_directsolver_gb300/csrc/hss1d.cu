@@ -1813,4 +1813,297 @@ void HSS1D::solve_device(const double* df, double* dx, int nrhs, double tol, int
   if (iters) *iters = used;
 }
 
+// ---------------------------------------------------------------------------
+// C_HSS = HSS1D_sum_nsym(A_HSS, B_HSS, acc), HSS1D/HSS1D_sum_nsym.m:30-160: *this = A + B for
+// two square handles on one forest.  Level by level (deepest first), every box of every
+// problem stacks the operands' outgoing bases RC = [R_A P_A; R_B P_B] and incoming bases
+// LC^T (R(:, J) = [I T] from a box's (T, J); P the sons' RHO, the identity on a leaf), IDs
+// both in one batched launch with the rank equalised by the fixed-rank ID (:57-66), and keeps
+// RHO = RC(:, J_out(1:k)) and LAMBDA^T = LC^T(:, J_in(1:k)).  Sibling blocks become
+// LAMBDA_s1 [M_SIB_A 0; 0 M_SIB_B] RHO_s2 (:79-86); self blocks add.
+struct RformP {
+  const double* T;  // k x (n - k), ld k
+  const int* J;     // n, a permutation
+  double* R;        // k x n, ld ldr: R(:, J) = [I T]
+  int k, n, ldr;
+};
+
+__global__ void __launch_bounds__(256) k_rform(const RformP* __restrict__ P) {
+  const RformP p = P[blockIdx.x];
+  const long long tot = (long long)p.k * p.n;
+  for (long long e = threadIdx.x; e < tot; e += 256) {
+    const int r = (int)(e % p.k), c = (int)(e / p.k);
+    const double v = (c < p.k) ? (r == c ? 1.0 : 0.0) : p.T[r + (size_t)(c - p.k) * p.k];
+    p.R[r + (size_t)p.J[c] * p.ldr] = v;
+  }
+}
+
+void HSS1D::sum(const HSS1D& A, const HSS1D& B, double acc_) {
+  HSS_REQUIRE(!A.rect && !B.rect, HSS_ERR_ARG, "sum is defined for square handles only");
+  HSS_REQUIRE(A.nboxes == B.nboxes && A.level == B.level && A.parent == B.parent && A.c1 == B.c1 && A.c2 == B.c2 &&
+                  A.off == B.off && A.cnt == B.cnt && A.M_SELF.n == B.M_SELF.n,
+              HSS_ERR_ARG, "HSS1D sum needs both operands on one tree");
+  HSS_REQUIRE(acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad sum tolerance");
+  std::fill(phase_s, phase_s + NPHASE, 0.0);
+  Ntot = A.Ntot; nprob = A.nprob; nboxes = A.nboxes; leaf = A.leaf; maxlev = A.maxlev; acc = acc_;
+  sym = false; rect = false; id_df = false;
+  pN = A.pN; pbase = A.pbase; proot = A.proot; pseed = A.pseed;
+  prob = A.prob; level = A.level; parent = A.parent; c1 = A.c1; c2 = A.c2; off = A.off; cnt = A.cnt;
+  X = A.X; kp = A.kp; kdev = A.kdev;
+  precision = HSS_PREC_FP64;
+  inverted = false;
+  clear_plans();
+  nskel.assign(nboxes, 0); kskel.assign(nboxes, 0);
+  I_SKUP.assign(nboxes, {}); I_SKDN.assign(nboxes, {});
+  J_UP.assign(nboxes, {}); J_DN.assign(nboxes, {});
+  census.assign(4 * (size_t)nboxes, 0);
+  feat.assign((size_t)NFEAT * nboxes, 0.f);
+  qr_steps = qr_steps_full = 0;
+  reruns = 0;
+  const cudaStream_t st = stream;
+  std::vector<DevBuf<double>> keep;  // per level: RHO and LAMBDA^T of its boxes
+  std::vector<DevBuf<double>> Tkeep;
+  std::vector<std::array<long long, 2>> Toff(nboxes);
+  std::vector<int> Tlev(nboxes, -1), mR(nboxes, 0);
+  std::vector<const double*> rho(nboxes, nullptr), sig(nboxes, nullptr);
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<int> boxes;
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == L) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    const int nbL = (int)boxes.size(), nprob2 = 2 * nbL;
+    // problem 2q: RC (m x n), 2q+1: LC^T (m x n); parents stage R_A, R_B, L_A^T, L_B^T in Y
+    std::vector<int> m(nbL), n(nbL);
+    std::vector<long long> oZ(nprob2), oY(nbL);
+    long long tZ = 0, tY = 0;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q];
+      m[q] = A.kskel[b] + B.kskel[b];
+      n[q] = is_leaf(b) ? cnt[b] : kskel[c1[b]] + kskel[c2[b]];
+      HSS_REQUIRE(m[q] >= 1 && n[q] >= 1 && n[q] <= 4096, HSS_ERR_RANK, "sum: empty or oversized skeleton basis");
+      oZ[2 * q] = tZ; tZ += (long long)m[q] * n[q];
+      oZ[2 * q + 1] = tZ; tZ += (long long)m[q] * n[q];
+      oY[q] = tY;
+      if (!is_leaf(b)) tY += 2LL * ((long long)A.kskel[b] * A.nskel[b] + (long long)B.kskel[b] * B.nskel[b]);
+    }
+    DevBuf<double> Z(std::max(tZ, 1LL)), Y(std::max(tY, 1LL));
+    Z.zero(st);
+    std::vector<RformP> rf;
+    std::vector<GemmP<double>> gp;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], kA = A.kskel[b], kB = B.kskel[b], mm = m[q];
+      double* RC = Z.p + oZ[2 * q];
+      double* LC = Z.p + oZ[2 * q + 1];
+      const double *TUa = A.T_UP.p + A.oT[b], *TDa = A.T_DN.p + A.oT[b];
+      const double *TUb = B.T_UP.p + B.oT[b], *TDb = B.T_DN.p + B.oT[b];
+      const int *JUa = A.JUPd.p + A.oJ[b], *JDa = A.JDNd.p + A.oJ[b];
+      const int *JUb = B.JUPd.p + B.oJ[b], *JDb = B.JDNd.p + B.oJ[b];
+      if (is_leaf(b)) {
+        const int nn = cnt[b];
+        rf.push_back(RformP{TUa, JUa, RC, kA, nn, mm});
+        rf.push_back(RformP{TUb, JUb, RC + kA, kB, nn, mm});
+        rf.push_back(RformP{TDa, JDa, LC, kA, nn, mm});
+        rf.push_back(RformP{TDb, JDb, LC + kA, kB, nn, mm});
+        continue;
+      }
+      const int s1 = c1[b], s2 = c2[b];
+      const int nA = A.nskel[b], nB = B.nskel[b];
+      const int kA1 = A.kskel[s1], kA2 = A.kskel[s2], kB1 = B.kskel[s1], kB2 = B.kskel[s2];
+      const int kC1 = kskel[s1], kC2 = kskel[s2], m1 = mR[s1], m2 = mR[s2];
+      HSS_REQUIRE(nA == kA1 + kA2 && nB == kB1 + kB2, HSS_ERR_ARG, "sum: operand skeleton sets do not follow the tree");
+      double* RA = Y.p + oY[q];
+      double* RB = RA + (size_t)kA * nA;
+      double* LA = RB + (size_t)kB * nB;
+      double* LB = LA + (size_t)kA * nA;
+      rf.push_back(RformP{TUa, JUa, RA, kA, nA, std::max(kA, 1)});
+      rf.push_back(RformP{TUb, JUb, RB, kB, nB, std::max(kB, 1)});
+      rf.push_back(RformP{TDa, JDa, LA, kA, nA, std::max(kA, 1)});
+      rf.push_back(RformP{TDb, JDb, LB, kB, nB, std::max(kB, 1)});
+      for (int side = 0; side < 2; ++side) {
+        const double* XA = side == 0 ? RA : LA;
+        const double* XB = side == 0 ? RB : LB;
+        const double* P1 = side == 0 ? rho[s1] : sig[s1];
+        const double* P2 = side == 0 ? rho[s2] : sig[s2];
+        double* D = side == 0 ? RC : LC;
+        const int la = std::max(kA, 1), lb = std::max(kB, 1);
+        gp.push_back(GemmP<double>{XA, P1, D, kA, kC1, kA1, la, m1, mm});
+        gp.push_back(GemmP<double>{XA + (size_t)kA1 * kA, P2, D + (size_t)kC1 * mm, kA, kC2, kA2, la, m2, mm});
+        gp.push_back(GemmP<double>{XB, P1 + kA1, D + kA, kB, kC1, kB1, lb, m1, mm});
+        gp.push_back(GemmP<double>{XB + (size_t)kB1 * kB, P2 + kA2, D + kA + (size_t)kC1 * mm, kB, kC2, kB2, lb, m2,
+                                   mm});
+      }
+    }
+    if (!rf.empty()) {
+      DevBuf<RformP> drf;
+      upload_vec(drf, rf, st);
+      for (size_t o = 0; o < rf.size(); o += 65535) {
+        const int c = (int)std::min<size_t>(65535, rf.size() - o);
+        k_rform<<<c, 256, 0, st>>>(drf.p + o);
+        check_launch("k_rform");
+      }
+      HSS_CUDA(cudaStreamSynchronize(st));
+    }
+    run_gemms(gp, false, false, 1.0, 0.0, st);
+    // IDs of RC and LC^T (problems 2 * local box + side of the shared random stream)
+    std::vector<long long> oT2(nprob2), oX(nprob2), oYw(nprob2), oP(nprob2);
+    long long tT = 0, tX = 0, tYw = 0, tP = 0;
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int q = pr / 2;
+      oT2[pr] = tT; tT += (long long)n[q] * n[q];
+      oX[pr] = tX; tX += 2LL * n[q];
+      oYw[pr] = tYw; tYw += (long long)m[q] + n[q];
+      oP[pr] = tP; tP += n[q];
+    }
+    DevBuf<double> W(std::max(tZ, 1LL)), SW(tT), SV(tT), xw(tX), yw(tYw);
+    Tkeep.emplace_back(tT);
+    DevBuf<double>& Tb = Tkeep.back();
+    DevBuf<int> perm(tP), rank(nprob2);
+    std::vector<IdP> ip(nprob2);
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int q = pr / 2, b = boxes[q];
+      const int lb = b - proot[prob[b]];
+      ip[pr] = IdP{Z.p + oZ[pr], W.p + oZ[pr], m[q], n[q], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oYw[pr], 2 * lb + pr % 2, -1,
+                   pseed[prob[b]], nullptr};
+    }
+    DevBuf<IdP> dip;
+    upload_vec(dip, ip, st);
+    id_adaptive_batched(dip.p, nprob2, acc, st, false);
+    std::vector<int> hr;
+    download(hr, rank.p, nprob2, st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    bool any = false;
+    std::vector<int> kbox(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      const int ko = hr[2 * q], ki = hr[2 * q + 1], k = std::max(ko, ki);
+      kbox[q] = k;
+      if (k != ko) { ip[2 * q].force_k = k; any = true; }
+      else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; }
+      HSS_REQUIRE(k <= std::min(m[q], n[q]), HSS_ERR_RANK, "fixed rank exceeds block size");
+    }
+    if (any) {
+      HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob2 * sizeof(IdP), cudaMemcpyHostToDevice, st));
+      id_fixed_batched(dip.p, nprob2, st);
+    }
+    std::vector<int> hp;
+    download(hp, perm.p, tP, st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    // RHO and LAMBDA^T: the ID's skeleton columns of RC and LC^T
+    long long tK = 0;
+    std::vector<long long> oK(nbL);
+    for (int q = 0; q < nbL; ++q) { oK[q] = tK; tK += 2LL * m[q] * kbox[q]; }
+    keep.emplace_back(std::max(tK, 1LL));
+    DevBuf<double>& Kb = keep.back();
+    std::vector<MoveP> mv;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], k = kbox[q], nn = n[q];
+      double* r = Kb.p + oK[q];
+      double* s = r + (size_t)m[q] * k;
+      mv.push_back(MoveP{Z.p + oZ[2 * q], r, perm.p + oP[2 * q], m[q], k, m[q], m[q], 1, 0});
+      mv.push_back(MoveP{Z.p + oZ[2 * q + 1], s, perm.p + oP[2 * q + 1], m[q], k, m[q], m[q], 1, 0});
+      rho[b] = r;
+      sig[b] = s;
+      mR[b] = m[q];
+      std::vector<int> outs, inns;
+      if (is_leaf(b)) {
+        outs.resize(cnt[b]);
+        std::iota(outs.begin(), outs.end(), off[b]);
+        inns = outs;
+      } else {
+        outs = I_SKUP[c1[b]];
+        outs.insert(outs.end(), I_SKUP[c2[b]].begin(), I_SKUP[c2[b]].end());
+        inns = I_SKDN[c1[b]];
+        inns.insert(inns.end(), I_SKDN[c2[b]].begin(), I_SKDN[c2[b]].end());
+      }
+      nskel[b] = nn;
+      kskel[b] = k;
+      J_UP[b].assign(hp.begin() + oP[2 * q], hp.begin() + oP[2 * q] + nn);
+      J_DN[b].assign(hp.begin() + oP[2 * q + 1], hp.begin() + oP[2 * q + 1] + nn);
+      I_SKUP[b].resize(k);
+      I_SKDN[b].resize(k);
+      for (int t = 0; t < k; ++t) {
+        I_SKUP[b][t] = outs[J_UP[b][t]];
+        I_SKDN[b][t] = inns[J_DN[b][t]];
+      }
+      Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
+      Tlev[b] = (int)Tkeep.size() - 1;
+      census[4 * b] = m[q]; census[4 * b + 1] = m[q]; census[4 * b + 2] = nn; census[4 * b + 3] = k;
+    }
+    run_moves(mv, st);
+  }
+  // ---- T_UP / T_DN / T_DN^T and J arenas
+  oT.assign(nboxes, 0);
+  oJ.assign(nboxes, 0);
+  long long tt = 0, tj = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    oT[b] = tt; tt += (long long)kskel[b] * (nskel[b] - kskel[b]);
+    oJ[b] = tj; tj += nskel[b];
+  }
+  T_UP.alloc(std::max(tt, 1LL)); T_DN.alloc(std::max(tt, 1LL)); TDNT.alloc(std::max(tt, 1LL));
+  std::vector<MoveP> mv;
+  std::vector<int> hJU(std::max(tj, 1LL)), hJD(std::max(tj, 1LL));
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    const int n = nskel[b], k = kskel[b];
+    std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
+    std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJ[b]);
+    if (n - k <= 0 || k == 0) continue;
+    const double* Tl = Tkeep[Tlev[b]].p;
+    mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, 3, 0});
+  }
+  run_moves(mv, st);
+  upload_vec(JUPd, hJU, st);
+  upload_vec(JDNd, hJD, st);
+  // ---- sibling blocks LAMBDA_s1 [M_SIB_A 0; 0 M_SIB_B] RHO_s2, through P = M_SIB_X RHO_s2(rows of X)
+  oSib.assign(nboxes, -1);
+  long long tb = 0, tw = 0;
+  std::vector<long long> oW(nboxes, 0);
+  for (int b = 0; b < nboxes; ++b) {
+    if (is_leaf(b)) continue;
+    HSS_REQUIRE(c1[b] >= 0 && c2[b] >= 0, HSS_ERR_ARG, "one-child boxes are not produced by the halving tree");
+    for (int t = 0; t < 2; ++t) {
+      const int s = t == 0 ? c1[b] : c2[b], o = t == 0 ? c2[b] : c1[b];
+      oSib[s] = tb; tb += (long long)kskel[s] * kskel[o];
+      oW[s] = tw; tw += (long long)(A.kskel[s] + B.kskel[s]) * kskel[o];
+    }
+  }
+  M_SIB.alloc(std::max(tb, 1LL));
+  DevBuf<double> Wsib(std::max(tw, 1LL));
+  std::vector<GemmP<double>> g1, g2, g3;
+  for (int b = 0; b < nboxes; ++b) {
+    if (is_leaf(b)) continue;
+    for (int t = 0; t < 2; ++t) {
+      const int s = t == 0 ? c1[b] : c2[b], o = t == 0 ? c2[b] : c1[b];
+      const int kAs = A.kskel[s], kBs = B.kskel[s], kAo = A.kskel[o], kBo = B.kskel[o];
+      const int ks = kskel[s], ko = kskel[o];
+      double* PA = Wsib.p + oW[s];
+      double* PB = PA + (size_t)kAs * ko;
+      g1.push_back(GemmP<double>{A.M_SIB.p + A.oSib[s], rho[o], PA, kAs, ko, kAo, std::max(kAs, 1), mR[o],
+                                 std::max(kAs, 1)});
+      g1.push_back(GemmP<double>{B.M_SIB.p + B.oSib[s], rho[o] + kAo, PB, kBs, ko, kBo, std::max(kBs, 1), mR[o],
+                                 std::max(kBs, 1)});
+      g2.push_back(GemmP<double>{sig[s], PA, M_SIB.p + oSib[s], ks, ko, kAs, mR[s], std::max(kAs, 1),
+                                 std::max(ks, 1)});
+      g3.push_back(GemmP<double>{sig[s] + kAs, PB, M_SIB.p + oSib[s], ks, ko, kBs, mR[s], std::max(kBs, 1),
+                                 std::max(ks, 1)});
+    }
+  }
+  run_gemms(g1, false, false, 1.0, 0.0, st);
+  run_gemms(g2, true, false, 1.0, 0.0, st);
+  run_gemms(g3, true, false, 1.0, 1.0, st);
+  // ---- self blocks
+  oSelf = A.oSelf;
+  M_SELF.alloc(std::max<size_t>(A.M_SELF.n, 1));
+  if (A.M_SELF.n) {
+    HSS_CUDA(cudaMemcpyAsync(M_SELF.p, A.M_SELF.p, A.M_SELF.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    const long long ne = (long long)A.M_SELF.n;
+    k_axpy1<<<std::min(ceil_div(ne, 256), 4096), 256, 0, st>>>(ne, B.M_SELF.p, M_SELF.p);
+    check_launch("k_axpy1");
+  }
+  HSS_CUDA(cudaStreamSynchronize(st));
+}
+
 }  // namespace hss

@@ -140,6 +140,8 @@ struct HSS1D {
   void append_tree(int p, int base, int n);
   void compress_rect(long long M, const double* Xin, long long ldin, long long N, const double* Xout,
                      long long ldout, int leaf, double acc, const hss_kernel_params& kp, unsigned long long seed);
+  // *this = A + B for two square handles on one forest (HSS1D_sum_nsym)
+  void sum(const HSS1D& A, const HSS1D& B, double acc);
   // K = the inverse in compressed format (HSS1D_transforminv_nsym)
   void transforminv(HSS1D& K);
   // K = the transpose in compressed format (HSS1D_transpose)

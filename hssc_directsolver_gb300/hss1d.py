@@ -270,6 +270,17 @@ def HSS1D_transpose(A_HSS: HSS1DMatrix) -> HSS1DMatrix:
     return K
 
 
+def HSS1D_sum_nsym(A_HSS: HSS1DMatrix, B_HSS: HSS1DMatrix, acc: float) -> HSS1DMatrix:
+    """C_HSS = HSS1D_sum_nsym(A_HSS, B_HSS, acc) (HSS1D/HSS1D_sum_nsym.m:1): A + B as a new
+    compressed matrix on the operands' common tree, re-skeletonized at tolerance acc."""
+    h = C.c_void_p()
+    L.check(L.lib().hss1d_sum(A_HSS._h, B_HSS._h, float(acc), C.byref(h)))
+    K = HSS1DMatrix(h, A_HSS.N)
+    if hasattr(A_HSS, "sizes"):
+        K.sizes = A_HSS.sizes
+    return K
+
+
 def HSS1D_scalarmult(c: float, A_HSS: HSS1DMatrix) -> HSS1DMatrix:
     """A = HSS1D_scalarmult(c, A) (HSS1D/HSS1D_scalarmult.m:1).  The matrix is scaled in place
     (and returned); its inverse factors are dropped, so invert again before applyinv."""

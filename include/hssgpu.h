@@ -157,6 +157,13 @@ int hss1d_compress_rect(hss1d_matrix** out, const double* Xin, int64_t M, int64_
  * Xin and the incoming skeleton sizes (a square handle reports its column side) */
 int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t* cnt_in, int32_t* nskel_in,
                     int32_t* kskel_in);
+/* C_HSS = HSS1D_sum_nsym(A_HSS, B_HSS, acc), HSS1D/HSS1D_sum_nsym.m:1: a new handle holding
+ * A + B, for two square handles on one tree (the same curves, leaf size and forest).  Each
+ * box re-skeletonizes the stacked bases of A and B by the ID at tolerance acc (rank raised
+ * to max(k_out, k_in) as in the compress); sibling blocks are projected, self blocks added.
+ * The result is an ordinary handle (invert, apply, solve ...); fsym operands are accepted
+ * and give an nsym result. */
+int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_matrix** C);
 /* [HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D/HSS1D_invert_nsym.m:44-91 */
 int hss1d_invert(hss1d_matrix* H);
 /* Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv),

@@ -8,6 +8,7 @@ Follows, function by function:
   HSS1D/HSS1D_applyinv_nsym.m   (:43-86)
   HSS1D/HSS1D_transforminv_nsym.m (:38-161)
   HSS1D/HSS1D_compress_rectangular_nsym.m, HSS1D/HSS1D_apply_rect_nsym.m (rectangular K(Xin, Xout))
+  HSS1D/HSS1D_sum_nsym.m        (C = A + B on one tree)
 
 The cell array ``K_HSS{row, ibox}`` of Common/box_constants.m:33-52 becomes an
 ``HSS1DMatrix`` whose per-box lists are indexed by the 0-based box id (box 0 is
@@ -803,3 +804,84 @@ def apply_rect_nsym(H: HSS1DRectMatrix, qq: np.ndarray) -> np.ndarray:
             rows = np.arange(H.off_in[b], H.off_in[b] + H.cnt_in[b])
             uu[rows] = _skel_eval(H.T_DN[b], H.J_DN[b], dn[b]) + H.M_SELF[b] @ qq[_leaf_range(t, b)]
     return uu[:, 0] if vec else uu
+
+
+# ---------------------------------------------------------------------------
+# C = A + B on one tree, HSS1D/HSS1D_sum_nsym.m
+# ---------------------------------------------------------------------------
+def _rform(T, J, k, n):
+    """R with R(:, J) = [I T] (k x n), HSS1D_sum_nsym.m:40-43; for the incoming side the
+    same form of (T_DN, J_DN) is L^T."""
+    R = np.zeros((k, n))
+    R[:, np.asarray(J)] = np.hstack([np.eye(k), np.asarray(T).reshape(k, n - k)])
+    return R
+
+
+def sum_nsym(A: HSS1DMatrix, B: HSS1DMatrix, acc: float, seed: int = 0) -> HSS1DMatrix:
+    """C_HSS = HSS1D_sum_nsym(A_HSS, B_HSS, acc), HSS1D_sum_nsym.m:30-160, for A and B on
+    one tree.  Bottom-up, each box stacks the two operands' outgoing bases
+    RC = [R_A P_A; R_B P_B] and incoming bases LC^T (P: the sons' RHO, the identity on a
+    leaf), IDs both (problems 2*b and 2*b+1 of the shared RNG) with the rank equalised to
+    k = max(k_out, k_in) by the fixed-rank ID (:57-66), and keeps RHO = RC(:, J_out(1:k)),
+    LAMBDA = LC(J_in(1:k), :).  Sibling blocks become
+    LAMBDA_s1 [M_SIB_A 0; 0 M_SIB_B] RHO_s2 (:79-86) and self blocks add."""
+    t = A.tree
+    for f in ("level", "parent", "c1", "c2", "off", "cnt"):
+        if not np.array_equal(getattr(t, f), getattr(B.tree, f)):
+            raise ValueError("HSS1D_sum_nsym needs both operands on one tree")
+    nb = t.nboxes
+    C = HSS1DMatrix(t)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census"):
+        setattr(C, name, [None] * nb)
+    rho = [None] * nb
+    sig = [None] * nb   # LAMBDA^T
+    for ibox in range(nb - 1, -1, -1):
+        if t.is_leaf(ibox):
+            ind = _leaf_range(t, ibox)
+            n = len(ind)
+            C.M_SELF[ibox] = A.M_SELF[ibox] + B.M_SELF[ibox]
+            if ibox == 0:
+                continue
+            kA, kB = A.kskel[ibox], B.kskel[ibox]
+            RC = np.vstack([_rform(A.T_UP[ibox], A.J_UP[ibox], kA, n), _rform(B.T_UP[ibox], B.J_UP[ibox], kB, n)])
+            LCt = np.vstack([_rform(A.T_DN[ibox], A.J_DN[ibox], kA, n), _rform(B.T_DN[ibox], B.J_DN[ibox], kB, n)])
+            out_set = in_set = ind
+        else:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            kA1, kA2 = A.kskel[s1], A.kskel[s2]
+            C.M_SIB[s1] = sig[s1][:kA1].T @ A.M_SIB[s1] @ rho[s2][:kA2] + sig[s1][kA1:].T @ B.M_SIB[s1] @ rho[s2][kA2:]
+            C.M_SIB[s2] = sig[s2][:kA2].T @ A.M_SIB[s2] @ rho[s1][:kA1] + sig[s2][kA2:].T @ B.M_SIB[s2] @ rho[s1][kA1:]
+            if ibox == 0:
+                continue
+            kB1, kB2 = B.kskel[s1], B.kskel[s2]
+            kA, kB = A.kskel[ibox], B.kskel[ibox]
+            out_set = np.concatenate([C.I_SKUP[s1], C.I_SKUP[s2]])
+            in_set = np.concatenate([C.I_SKDN[s1], C.I_SKDN[s2]])
+
+            def stack(TA, JA, TB, JB, P):
+                RA = _rform(TA, JA, kA, kA1 + kA2)
+                RB = _rform(TB, JB, kB, kB1 + kB2)
+                return np.vstack([np.hstack([RA[:, :kA1] @ P[s1][:kA1], RA[:, kA1:] @ P[s2][:kA2]]),
+                                  np.hstack([RB[:, :kB1] @ P[s1][kA1:], RB[:, kB1:] @ P[s2][kA2:]])])
+            RC = stack(A.T_UP[ibox], A.J_UP[ibox], B.T_UP[ibox], B.J_UP[ibox], rho)
+            LCt = stack(A.T_DN[ibox], A.J_DN[ibox], B.T_DN[ibox], B.J_DN[ibox], sig)
+        Tout, Jout, kout, Rout = idecomp.id_adaptive(RC, acc, seed, 2 * ibox)
+        Tin, Jin, kin, Rin = idecomp.id_adaptive(LCt, acc, seed, 2 * ibox + 1)
+        k = max(kout, kin)
+        if k != kout:
+            Tout = idecomp.id_fixed_from_qr(Rout, Jout, k)
+        elif k != kin:
+            Tin = idecomp.id_fixed_from_qr(Rin, Jin, k)
+        C.I_SKUP[ibox] = out_set[Jout[:k]]
+        C.T_UP[ibox] = Tout
+        C.J_UP[ibox] = Jout
+        C.I_SKDN[ibox] = in_set[Jin[:k]]
+        C.T_DN[ibox] = Tin
+        C.J_DN[ibox] = Jin
+        C.nskel[ibox] = len(out_set)
+        C.kskel[ibox] = k
+        C.census[ibox] = (RC.shape[0], LCt.shape[0], len(out_set), k, kout, kin)
+        rho[ibox] = RC[:, Jout[:k]]
+        sig[ibox] = LCt[:, Jin[:k]]
+    return C

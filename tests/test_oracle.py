@@ -279,3 +279,20 @@ def test_hss1d_rectangular_compress_apply(N, M, leaf, s):
     u = O.apply_rect_nsym(H, q)
     assert u.shape == (M, 3)
     assert np.linalg.norm(u - K @ q) <= 1e-9 * np.linalg.norm(K @ q)
+
+
+def test_hss1d_sum():
+    """HSS1D_sum_nsym restated: A + A^T re-skeletonized equals the dense sum to the tolerance;
+    A + 2A keeps A's ranks."""
+    from oracle import hss1d as O
+    X = geometry.star_curve(768)
+    kp = kernels.KernelParams(flag=kernels.DL_L_2D)
+    A = O.compress_nsym(X, 64, 1e-10, kp)
+    I = np.eye(768)
+    Ka = O.apply_nsym(A, I)
+    C = O.sum_nsym(A, O.transpose(A), 1e-10)
+    assert np.abs(O.apply_nsym(C, I) - (Ka + Ka.T)).max() <= 1e-10 * np.abs(Ka).max()
+    assert max(C.kskel[1:]) > max(A.kskel[1:])
+    S = O.sum_nsym(A, O.scalarmult(2.0, A), 1e-10)
+    assert S.kskel[1:] == A.kskel[1:]
+    assert np.abs(O.apply_nsym(S, I) - 3.0 * Ka).max() <= 1e-12 * np.abs(Ka).max()
