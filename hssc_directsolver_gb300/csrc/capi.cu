@@ -499,6 +499,25 @@ int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_ma
   HSS_CATCH
 }
 
+int hss1d_compress_lr(hss1d_matrix** out, const double* U, const double* V, int64_t N, int32_t r, int64_t ldu,
+                      int64_t ldv, int32_t leaf, double acc, uint64_t seed) {
+  HSS_TRY
+  HSS_REQUIRE(out, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *out = nullptr;
+  auto* h = new hss1d_matrix{nullptr};
+  try {
+    h->impl = new HSS1D();
+    h->impl->compress_lr(N, r, U, ldu, V, ldv, leaf, acc, seed);
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *out = h;
+  HSS_CATCH
+}
+
 int hss1d_invert(hss1d_matrix* H) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

@@ -2031,32 +2031,7 @@ void HSS1D::sum(const HSS1D& A, const HSS1D& B, double acc_) {
     }
     run_moves(mv, st);
   }
-  // ---- T_UP / T_DN / T_DN^T and J arenas
-  oT.assign(nboxes, 0);
-  oJ.assign(nboxes, 0);
-  long long tt = 0, tj = 0;
-  for (int b = 0; b < nboxes; ++b) {
-    if (parent[b] < 0) continue;
-    oT[b] = tt; tt += (long long)kskel[b] * (nskel[b] - kskel[b]);
-    oJ[b] = tj; tj += nskel[b];
-  }
-  T_UP.alloc(std::max(tt, 1LL)); T_DN.alloc(std::max(tt, 1LL)); TDNT.alloc(std::max(tt, 1LL));
-  std::vector<MoveP> mv;
-  std::vector<int> hJU(std::max(tj, 1LL)), hJD(std::max(tj, 1LL));
-  for (int b = 0; b < nboxes; ++b) {
-    if (parent[b] < 0) continue;
-    const int n = nskel[b], k = kskel[b];
-    std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
-    std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJ[b]);
-    if (n - k <= 0 || k == 0) continue;
-    const double* Tl = Tkeep[Tlev[b]].p;
-    mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
-    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
-    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, 3, 0});
-  }
-  run_moves(mv, st);
-  upload_vec(JUPd, hJU, st);
-  upload_vec(JDNd, hJD, st);
+  pack_T(Tkeep, Toff, Tlev);
   // ---- sibling blocks LAMBDA_s1 [M_SIB_A 0; 0 M_SIB_B] RHO_s2, through P = M_SIB_X RHO_s2(rows of X)
   oSib.assign(nboxes, -1);
   long long tb = 0, tw = 0;
@@ -2104,6 +2079,232 @@ void HSS1D::sum(const HSS1D& A, const HSS1D& B, double acc_) {
     check_launch("k_axpy1");
   }
   HSS_CUDA(cudaStreamSynchronize(st));
+}
+
+// T_UP / T_DN / T_DN^T and J arenas from the per-level ID outputs (T of box b: k x (n - k),
+// ld n, at Tkeep[Tlev[b]] + Toff[b][side])
+void HSS1D::pack_T(const std::vector<DevBuf<double>>& Tkeep, const std::vector<std::array<long long, 2>>& Toff,
+                   const std::vector<int>& Tlev) {
+  oT.assign(nboxes, 0);
+  oJ.assign(nboxes, 0);
+  long long tt = 0, tj = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    oT[b] = tt; tt += (long long)kskel[b] * (nskel[b] - kskel[b]);
+    oJ[b] = tj; tj += nskel[b];
+  }
+  T_UP.alloc(std::max(tt, 1LL)); T_DN.alloc(std::max(tt, 1LL)); TDNT.alloc(std::max(tt, 1LL));
+  std::vector<MoveP> mv;
+  std::vector<int> hJU(std::max(tj, 1LL)), hJD(std::max(tj, 1LL));
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    const int n = nskel[b], k = kskel[b];
+    std::copy(J_UP[b].begin(), J_UP[b].end(), hJU.begin() + oJ[b]);
+    std::copy(J_DN[b].begin(), J_DN[b].end(), hJD.begin() + oJ[b]);
+    if (n - k <= 0 || k == 0) continue;
+    const double* Tl = Tkeep[Tlev[b]].p;
+    mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, 3, 0});
+  }
+  run_moves(mv, stream);
+  upload_vec(JUPd, hJU, stream);
+  upload_vec(JDNd, hJD, stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+// ---------------------------------------------------------------------------
+// K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc), HSS1D/HSS1D_compressLR_nsym.m:25-88: the
+// N x N matrix U V^T on the halving tree.  Per level (deepest first) every box IDs
+// V(out,:).' and U(in,:).' (r x n, gathered and transposed on the device) in one batched
+// launch, with the rank equalised by the fixed-rank ID; M_SELF = U(ind,:) V(ind,:).' and
+// M_SIB{s1} = U(I_SKDN{s1},:) V(I_SKUP{s2},:).' are batched products.
+void HSS1D::compress_lr(long long N, int r, const double* U, long long ldu, const double* V, long long ldv,
+                        int leaf_, double acc_, unsigned long long seed) {
+  HSS_REQUIRE(U && V && N >= 2 && N < (1LL << 30) && r >= 1 && r <= 4096 && ldu >= N && ldv >= N && leaf_ >= 1 &&
+                  acc_ > 0 && acc_ < 1,
+              HSS_ERR_ARG, "bad low-rank compress args");
+  std::fill(phase_s, phase_s + NPHASE, 0.0);
+  rect = false; sym = false; id_df = false;
+  nprob = 1; leaf = leaf_; acc = acc_;
+  kp = hss_kernel_params{};
+  Ntot = N;
+  pN = {N}; pbase = {0}; pseed = {seed};
+  proot.assign(1, 0);
+  X.assign(6 * (size_t)N, 0.0);
+  prob.clear(); level.clear(); parent.clear(); c1.clear(); c2.clear(); off.clear(); cnt.clear();
+  append_tree(0, 0, (int)N);
+  nboxes = (int)level.size();
+  maxlev = *std::max_element(level.begin(), level.end());
+  precision = HSS_PREC_FP64;
+  inverted = false;
+  clear_plans();
+  const cudaStream_t st = stream;
+  DevBuf<double> Ud((size_t)N * r), Vd((size_t)N * r);
+  HSS_CUDA(cudaMemcpy2DAsync(Ud.p, N * sizeof(double), U, ldu * sizeof(double), N * sizeof(double), r,
+                             cudaMemcpyHostToDevice, st));
+  HSS_CUDA(cudaMemcpy2DAsync(Vd.p, N * sizeof(double), V, ldv * sizeof(double), N * sizeof(double), r,
+                             cudaMemcpyHostToDevice, st));
+  nskel.assign(nboxes, 0); kskel.assign(nboxes, 0);
+  I_SKUP.assign(nboxes, {}); I_SKDN.assign(nboxes, {});
+  J_UP.assign(nboxes, {}); J_DN.assign(nboxes, {});
+  census.assign(4 * (size_t)nboxes, 0);
+  feat.assign((size_t)NFEAT * nboxes, 0.f);
+  qr_steps = qr_steps_full = 0;
+  reruns = 0;
+  std::vector<DevBuf<double>> Tkeep;
+  std::vector<std::array<long long, 2>> Toff(nboxes);
+  std::vector<int> Tlev(nboxes, -1);
+  for (int L = maxlev; L >= 1; --L) {
+    std::vector<int> boxes;
+    for (int b = 0; b < nboxes; ++b)
+      if (level[b] == L) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    const int nbL = (int)boxes.size(), nprob2 = 2 * nbL;
+    std::vector<std::vector<int>> outs(nbL), inns(nbL);
+    std::vector<int> idx;
+    std::vector<long long> oI(nprob2), oA(nprob2), oT2(nprob2), oX(nprob2), oY(nprob2), oP(nprob2);
+    long long tA = 0, tT = 0, tX = 0, tY = 0, tP = 0;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q];
+      if (is_leaf(b)) {
+        outs[q].resize(cnt[b]);
+        std::iota(outs[q].begin(), outs[q].end(), off[b]);
+        inns[q] = outs[q];
+      } else {
+        outs[q] = I_SKUP[c1[b]];
+        outs[q].insert(outs[q].end(), I_SKUP[c2[b]].begin(), I_SKUP[c2[b]].end());
+        inns[q] = I_SKDN[c1[b]];
+        inns[q].insert(inns[q].end(), I_SKDN[c2[b]].begin(), I_SKDN[c2[b]].end());
+      }
+      const int n = (int)outs[q].size();
+      HSS_REQUIRE(n >= 1 && n <= 4096, HSS_ERR_RANK, "empty or oversized skeleton set");
+      for (int s = 0; s < 2; ++s) {
+        const int pr = 2 * q + s;
+        oI[pr] = idx.size();
+        const auto& v = s == 0 ? outs[q] : inns[q];
+        idx.insert(idx.end(), v.begin(), v.end());
+        oA[pr] = tA; tA += (long long)r * n;
+        oT2[pr] = tT; tT += (long long)n * n;
+        oX[pr] = tX; tX += 2LL * n;
+        oY[pr] = tY; tY += (long long)r + n;
+        oP[pr] = tP; tP += n;
+      }
+    }
+    DevBuf<int> didx;
+    upload_vec(didx, idx, st);
+    // A = V(out,:).' / U(in,:).': row gather (n x r) then transpose (r x n)
+    DevBuf<double> G(std::max(tA, 1LL)), A(std::max(tA, 1LL)), W(std::max(tA, 1LL)), SW(tT), SV(tT), xw(tX), yw(tY);
+    std::vector<MoveP> g, tr;
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int n = (int)outs[pr / 2].size();
+      g.push_back(MoveP{pr % 2 == 0 ? Vd.p : Ud.p, G.p + oA[pr], didx.p + oI[pr], n, r, (int)N, n, 0, 0});
+      tr.push_back(MoveP{G.p + oA[pr], A.p + oA[pr], nullptr, n, r, n, r, 3, 0});
+    }
+    run_moves(g, st);
+    run_moves(tr, st);
+    Tkeep.emplace_back(tT);
+    DevBuf<double>& Tb = Tkeep.back();
+    DevBuf<int> perm(tP), rank(nprob2);
+    std::vector<IdP> ip(nprob2);
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int n = (int)outs[pr / 2].size();
+      ip[pr] = IdP{A.p + oA[pr], W.p + oA[pr], r, n, perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oX[pr], yw.p + oY[pr], 2 * boxes[pr / 2] + pr % 2, -1,
+                   seed, nullptr};
+    }
+    DevBuf<IdP> dip;
+    upload_vec(dip, ip, st);
+    id_adaptive_batched(dip.p, nprob2, acc, st, false);
+    std::vector<int> hr;
+    download(hr, rank.p, nprob2, st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    bool any = false;
+    std::vector<int> kbox(nbL);
+    for (int q = 0; q < nbL; ++q) {
+      const int ko = hr[2 * q], ki = hr[2 * q + 1], k = std::max(ko, ki);
+      kbox[q] = k;
+      if (k != ko) { ip[2 * q].force_k = k; any = true; }
+      else if (k != ki) { ip[2 * q + 1].force_k = k; any = true; }
+    }
+    if (any) {
+      HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob2 * sizeof(IdP), cudaMemcpyHostToDevice, st));
+      id_fixed_batched(dip.p, nprob2, st);
+    }
+    std::vector<int> hp;
+    download(hp, perm.p, tP, st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], k = kbox[q], n = (int)outs[q].size();
+      nskel[b] = n;
+      kskel[b] = k;
+      J_UP[b].assign(hp.begin() + oP[2 * q], hp.begin() + oP[2 * q] + n);
+      J_DN[b].assign(hp.begin() + oP[2 * q + 1], hp.begin() + oP[2 * q + 1] + n);
+      I_SKUP[b].resize(k);
+      I_SKDN[b].resize(k);
+      for (int t = 0; t < k; ++t) {
+        I_SKUP[b][t] = outs[q][J_UP[b][t]];
+        I_SKDN[b][t] = inns[q][J_DN[b][t]];
+      }
+      Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
+      Tlev[b] = (int)Tkeep.size() - 1;
+      census[4 * b] = r; census[4 * b + 1] = r; census[4 * b + 2] = n; census[4 * b + 3] = k;
+    }
+  }
+  pack_T(Tkeep, Toff, Tlev);
+  Tkeep.clear();
+  // ---- M_SELF = U(ind,:) V(ind,:).', M_SIB{s1} = U(I_SKDN{s1},:) V(I_SKUP{s2},:).'
+  oSelf.assign(nboxes, -1);
+  oSib.assign(nboxes, -1);
+  long long ts = 0, tb = 0, tg = 0;
+  std::vector<long long> oG(nboxes, 0);
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0 && is_leaf(b)) { oSelf[b] = ts; ts += (long long)cnt[b] * cnt[b]; }
+    if (!is_leaf(b)) {
+      const int s1 = c1[b], s2 = c2[b];
+      oSib[s1] = tb; tb += (long long)kskel[s1] * kskel[s2];
+      oSib[s2] = tb; tb += (long long)kskel[s2] * kskel[s1];
+      for (int s : {s1, s2}) { oG[s] = tg; tg += 2LL * kskel[s] * r; }
+    }
+  }
+  M_SELF.alloc(std::max(ts, 1LL));
+  M_SIB.alloc(std::max(tb, 1LL));
+  // per son s: U(I_SKDN{s},:) and V(I_SKUP{s},:) (k_s x r each)
+  std::vector<int> idx;
+  std::vector<long long> oIx(nboxes, 0);
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] < 0) continue;
+    oIx[b] = idx.size();
+    idx.insert(idx.end(), I_SKDN[b].begin(), I_SKDN[b].end());
+    idx.insert(idx.end(), I_SKUP[b].begin(), I_SKUP[b].end());
+  }
+  DevBuf<int> didx;
+  upload_vec(didx, idx, st);
+  DevBuf<double> Gs(std::max(tg, 1LL));
+  std::vector<MoveP> mv;
+  std::vector<GemmP<double>> P;
+  for (int b = 0; b < nboxes; ++b) {
+    if (parent[b] >= 0 && is_leaf(b))
+      P.push_back(GemmP<double>{Ud.p + off[b], Vd.p + off[b], M_SELF.p + oSelf[b], cnt[b], cnt[b], r, (int)N, (int)N,
+                                cnt[b]});
+    if (parent[b] >= 0 && kskel[b] > 0) {
+      const int k = kskel[b];
+      mv.push_back(MoveP{Ud.p, Gs.p + oG[b], didx.p + oIx[b], k, r, (int)N, k, 0, 0});
+      mv.push_back(MoveP{Vd.p, Gs.p + oG[b] + (size_t)k * r, didx.p + oIx[b] + k, k, r, (int)N, k, 0, 0});
+    }
+  }
+  run_moves(mv, st);
+  for (int b = 0; b < nboxes; ++b) {
+    if (is_leaf(b)) continue;
+    for (int t = 0; t < 2; ++t) {
+      const int s = t == 0 ? c1[b] : c2[b], o = t == 0 ? c2[b] : c1[b];
+      const int ks = kskel[s], ko = kskel[o];
+      if (ks == 0 || ko == 0) continue;
+      P.push_back(GemmP<double>{Gs.p + oG[s], Gs.p + oG[o] + (size_t)ko * r, M_SIB.p + oSib[s], ks, ko, r, ks, ko,
+                                ks});
+    }
+  }
+  run_gemms(P, false, true, 1.0, 0.0, st);
 }
 
 }  // namespace hss

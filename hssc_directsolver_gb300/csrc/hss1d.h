@@ -5,6 +5,7 @@
 // arenas, so every level of every problem is processed by the same launches.
 #pragma once
 
+#include <array>
 #include <map>
 #include <vector>
 
@@ -140,6 +141,11 @@ struct HSS1D {
   void append_tree(int p, int base, int n);
   void compress_rect(long long M, const double* Xin, long long ldin, long long N, const double* Xout,
                      long long ldout, int leaf, double acc, const hss_kernel_params& kp, unsigned long long seed);
+  // U V^T (U, V: N x r column-major) on the halving tree (HSS1D_compressLR_nsym)
+  void compress_lr(long long N, int r, const double* U, long long ldu, const double* V, long long ldv, int leaf,
+                   double acc, unsigned long long seed);
+  void pack_T(const std::vector<DevBuf<double>>& Tkeep, const std::vector<std::array<long long, 2>>& Toff,
+              const std::vector<int>& Tlev);
   // *this = A + B for two square handles on one forest (HSS1D_sum_nsym)
   void sum(const HSS1D& A, const HSS1D& B, double acc);
   // K = the inverse in compressed format (HSS1D_transforminv_nsym)

@@ -281,6 +281,19 @@ def HSS1D_sum_nsym(A_HSS: HSS1DMatrix, B_HSS: HSS1DMatrix, acc: float) -> HSS1DM
     return K
 
 
+def HSS1D_compressLR_nsym(U, V, TREE: int, acc: float, seed: int = 0) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc) (HSS1D/HSS1D_compressLR_nsym.m:1): the
+    N x N matrix U V^T in compressed form on the halving tree of leaf size TREE."""
+    Uf = np.asfortranarray(np.asarray(U, dtype=np.float64))
+    Vf = np.asfortranarray(np.asarray(V, dtype=np.float64))
+    if Uf.ndim != 2 or Uf.shape != Vf.shape:
+        raise ValueError("U and V must both be N x r")
+    h = C.c_void_p()
+    L.check(L.lib().hss1d_compress_lr(C.byref(h), L.ptr(Uf), L.ptr(Vf), Uf.shape[0], Uf.shape[1], Uf.shape[0],
+                                      Vf.shape[0], int(TREE), float(acc), int(seed)))
+    return HSS1DMatrix(h, Uf.shape[0])
+
+
 def HSS1D_scalarmult(c: float, A_HSS: HSS1DMatrix) -> HSS1DMatrix:
     """A = HSS1D_scalarmult(c, A) (HSS1D/HSS1D_scalarmult.m:1).  The matrix is scaled in place
     (and returned); its inverse factors are dropped, so invert again before applyinv."""

@@ -164,6 +164,12 @@ int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t*
  * The result is an ordinary handle (invert, apply, solve ...); fsym operands are accepted
  * and give an nsym result. */
 int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_matrix** C);
+/* K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc), HSS1D/HSS1D_compressLR_nsym.m:1: the N x N
+ * matrix U V^T (U, V: N x r column-major, ld ldu / ldv) on the halving tree with leaf size
+ * `leaf`; every box IDs V(out,:).' and U(in,:).' at tolerance acc (seed keys the rank check).
+ * With hss1d_sum this forms low-rank updates of a compressed matrix. */
+int hss1d_compress_lr(hss1d_matrix** out, const double* U, const double* V, int64_t N, int32_t r, int64_t ldu,
+                      int64_t ldv, int32_t leaf, double acc, uint64_t seed);
 /* [HSSinv, FTinv] = HSS1D_invert_nsym(K_HSS, acc), HSS1D/HSS1D_invert_nsym.m:44-91 */
 int hss1d_invert(hss1d_matrix* H);
 /* Kinv_HSS = HSS1D_transforminv_nsym(K_HSS, HSSinv, FTinv),

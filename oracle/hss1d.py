@@ -9,6 +9,7 @@ Follows, function by function:
   HSS1D/HSS1D_transforminv_nsym.m (:38-161)
   HSS1D/HSS1D_compress_rectangular_nsym.m, HSS1D/HSS1D_apply_rect_nsym.m (rectangular K(Xin, Xout))
   HSS1D/HSS1D_sum_nsym.m        (C = A + B on one tree)
+  HSS1D/HSS1D_compressLR_nsym.m (U V^T in compressed form)
 
 The cell array ``K_HSS{row, ibox}`` of Common/box_constants.m:33-52 becomes an
 ``HSS1DMatrix`` whose per-box lists are indexed by the 0-based box id (box 0 is
@@ -885,3 +886,51 @@ def sum_nsym(A: HSS1DMatrix, B: HSS1DMatrix, acc: float, seed: int = 0) -> HSS1D
         rho[ibox] = RC[:, Jout[:k]]
         sig[ibox] = LCt[:, Jin[:k]]
     return C
+
+
+# ---------------------------------------------------------------------------
+# K = U V^T in compressed form, HSS1D/HSS1D_compressLR_nsym.m
+# ---------------------------------------------------------------------------
+def compress_lr_nsym(U: np.ndarray, V: np.ndarray, leaf: int, acc: float, seed: int = 0) -> HSS1DMatrix:
+    """K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc), HSS1D_compressLR_nsym.m:25-88: the
+    N x N matrix U V^T on the halving tree.  Per box (fine to coarse) ID(V(out,:).') and
+    ID(U(in,:).') (problems 2*b and 2*b+1 of the shared RNG), rank equalised by the
+    fixed-rank ID; M_SELF = U(ind,:) V(ind,:).' and M_SIB{s1} = U(I_SKDN{s1},:)
+    V(I_SKUP{s2},:).'."""
+    U = np.asarray(U, dtype=np.float64)
+    V = np.asarray(V, dtype=np.float64)
+    t = get_tree(U.shape[0], leaf)
+    nb = t.nboxes
+    H = HSS1DMatrix(t)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census"):
+        setattr(H, name, [None] * nb)
+    for ibox in range(nb - 1, 0, -1):
+        out, inn = _box_skel_sets(H, ibox)
+        A21 = V[out].T
+        A12t = U[inn].T
+        Tout, Jout, kout, Rout = idecomp.id_adaptive(A21, acc, seed, 2 * ibox)
+        Tin, Jin, kin, Rin = idecomp.id_adaptive(A12t, acc, seed, 2 * ibox + 1)
+        k = max(kout, kin)
+        if k != kout:
+            Tout = idecomp.id_fixed_from_qr(Rout, Jout, k)
+        elif k != kin:
+            Tin = idecomp.id_fixed_from_qr(Rin, Jin, k)
+        H.I_SKUP[ibox] = out[Jout[:k]]
+        H.T_UP[ibox] = Tout
+        H.J_UP[ibox] = Jout
+        H.I_SKDN[ibox] = inn[Jin[:k]]
+        H.T_DN[ibox] = Tin
+        H.J_DN[ibox] = Jin
+        H.nskel[ibox] = len(out)
+        H.kskel[ibox] = k
+        H.census[ibox] = (A21.shape[0], A12t.shape[0], len(out), k, kout, kin)
+    for ibox in range(nb - 1, -1, -1):
+        if t.is_leaf(ibox):
+            ind = _leaf_range(t, ibox)
+            H.M_SELF[ibox] = U[ind] @ V[ind].T
+        elif t.c1[ibox] >= 0 and t.c2[ibox] >= 0:
+            s1, s2 = t.c1[ibox], t.c2[ibox]
+            H.M_SIB[s1] = U[H.I_SKDN[s1]] @ V[H.I_SKUP[s2]].T
+            H.M_SIB[s2] = U[H.I_SKDN[s2]] @ V[H.I_SKUP[s1]].T
+    return H

@@ -504,3 +504,35 @@ def test_sum_forest(gpu):
         uo = O1.apply_nsym(Co, q[r0:r0 + X.shape[0]])
         assert np.linalg.norm(u[r0:r0 + X.shape[0]] - uo) <= 1e-9 * np.linalg.norm(uo)
         r0 += X.shape[0]
+
+
+def test_compress_lr_and_low_rank_update(gpu):
+    """HSS1D_compressLR_nsym: the IDs read exact copies of U and V rows, so ranks, skeletons
+    and the apply equal the oracle's; K + U V^T (HSS1D_sum_nsym of a kernel compression and
+    the low-rank one) inverts and solves to 1e-10 against the dense matrix."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    rng = np.random.default_rng(4)
+    N, r = 2000, 11
+    U, V = rng.standard_normal((N, r)), rng.standard_normal((N, r))
+    H = G1.HSS1D_compressLR_nsym(U, V, 64, 1e-10)
+    Ho = O1.compress_lr_nsym(U, V, 64, 1e-10)
+    inf = H.info()
+    assert np.array_equal(inf["kskel"][1:], Ho.kskel[1:])
+    for b in range(1, inf["nboxes"]):
+        e = H.export_box(b)
+        assert np.array_equal(e["I_SKUP"], Ho.I_SKUP[b]) and np.array_equal(e["I_SKDN"], Ho.I_SKDN[b])
+    q = rng.standard_normal((N, 3))
+    u = G1.HSS1D_apply_nsym(H, q)
+    assert np.linalg.norm(u - O1.apply_nsym(Ho, q)) <= 1e-12 * np.linalg.norm(u)
+    assert np.linalg.norm(u - U @ (V.T @ q)) <= 1e-12 * np.linalg.norm(u)
+    X = geometry.star_curve(N)
+    kpo = OK.KernelParams(flag=OK.DL_L_2D)
+    A = G1.HSS1D_compress_nsym("green", X, 64, 1e-10, GK.Kernel("DL_L_2D"))
+    Cg = G1.HSS1D_sum_nsym(A, G1.HSS1D_scalarmult(1e-3, H), 1e-10)
+    Kd = OK.kernel_eval(X, X, kpo) + 1e-3 * U @ V.T
+    f = rng.standard_normal(N)
+    G1.HSS1D_invert_nsym(Cg)
+    x, rr, _ = G1.HSS1D_solve(Cg, f, tol=1e-10)
+    assert rr < 1e-10
+    xd = np.linalg.solve(Kd, f)
+    assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)

@@ -296,3 +296,21 @@ def test_hss1d_sum():
     S = O.sum_nsym(A, O.scalarmult(2.0, A), 1e-10)
     assert S.kskel[1:] == A.kskel[1:]
     assert np.abs(O.apply_nsym(S, I) - 3.0 * Ka).max() <= 1e-12 * np.abs(Ka).max()
+
+
+def test_hss1d_compress_lr():
+    """HSS1D_compressLR_nsym restated: U V^T is represented exactly (ranks r) and a low-rank
+    update of a compressed kernel matrix is formed by HSS1D_sum_nsym."""
+    from oracle import hss1d as O
+    rng = np.random.default_rng(0)
+    N, r = 800, 9
+    U, V = rng.standard_normal((N, r)), rng.standard_normal((N, r))
+    H = O.compress_lr_nsym(U, V, 64, 1e-10)
+    assert all(k == r for k in H.kskel[1:])
+    q = rng.standard_normal((N, 2))
+    assert np.linalg.norm(O.apply_nsym(H, q) - U @ (V.T @ q)) <= 1e-13 * np.linalg.norm(U @ (V.T @ q))
+    X = geometry.star_curve(N)
+    kp = kernels.KernelParams(flag=kernels.DL_L_2D)
+    C = O.sum_nsym(O.compress_nsym(X, 64, 1e-10, kp), H, 1e-10)
+    Kd = kernels.kernel_eval(X, X, kp) + U @ V.T
+    assert np.linalg.norm(O.apply_nsym(C, q) - Kd @ q) <= 1e-10 * np.linalg.norm(Kd @ q)
