@@ -273,6 +273,50 @@ def bench_kernel_gen(L, dev, m=8192, n=8192, reps=3):
     return out
 
 
+def bench_hss1d_algebra(N=32768, M=24576, r=16, leaf=64, acc=1e-10):
+    """Seconds of the HSS1D algebra entry points on one star curve (Laplace double layer):
+    compress, transpose, A + A^T (HSS1D_sum_nsym), U V^T (HSS1D_compressLR_nsym), the
+    low-rank update A + U V^T, and the rectangular K(Xin, Xout) between the curve and the
+    curve scaled by 1.2 (HSS1D_compress_rectangular_nsym) with its 8-column apply."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    rng = np.random.default_rng(0)
+    X = GG.star_curve(N)
+    Xin = GG.star_curve(M).copy()
+    Xin[:, :2] *= 1.2
+    Xin[:, 4] *= 1.2
+    Xin[:, 5] /= 1.2
+    U, V = rng.standard_normal((N, r)), rng.standard_normal((N, r))
+    k = GK.Kernel("DL_L_2D")
+    out = {"workload": f"star curve N={N} (rows of the rectangular case: M={M}, the curve scaled by 1.2), "
+                       f"leaf {leaf}, tol {acc:g}, U V^T of rank {r}; host wall seconds per call"}
+    t = time.perf_counter
+    t0 = t()
+    A = G1.HSS1D_compress_nsym("green", X, leaf, acc, k)
+    t1 = t()
+    At = G1.HSS1D_transpose(A)
+    t2 = t()
+    S = G1.HSS1D_sum_nsym(A, At, acc)
+    t3 = t()
+    H = G1.HSS1D_compressLR_nsym(U, V, leaf, acc)
+    t4 = t()
+    C2 = G1.HSS1D_sum_nsym(A, H, acc)
+    t5 = t()
+    R = G1.HSS1D_compress_rectangular_nsym("green", Xin, X, leaf, acc, k)
+    t6 = t()
+    q = rng.standard_normal((N, 8))
+    G1.HSS1D_apply_rect_nsym(R, q)
+    t7 = t()
+    G1.HSS1D_apply_rect_nsym(R, q)
+    t8 = t()
+    out.update(compress_s=t1 - t0, transpose_s=t2 - t1, sum_AAt_s=t3 - t2, compress_lr_s=t4 - t3,
+               sum_lowrank_update_s=t5 - t4, compress_rect_s=t6 - t5, apply_rect_8rhs_ms=(t8 - t7) * 1e3,
+               max_rank={"A": int(A.info()["kskel"][1:].max()), "A+A^T": int(S.info()["kskel"][1:].max()),
+                         "A+UV^T": int(C2.info()["kskel"][1:].max()),
+                         "rect_in": int(R.rect_info()["kskel_in"][1:].max())})
+    del A, At, S, H, C2, R
+    return out
+
+
 def bench_config5(args, L, dev):
     """The learned-rank configuration at scale: 2048 double-layer curves (N log-uniform in
     [2048, 32768], ~23 M points) compressed plainly and with the rank MLP trained on the
@@ -337,6 +381,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-curve batched HSS1D section")
     ap.add_argument("--curves", type=int, default=512)
+    ap.add_argument("--no-algebra", action="store_true", help="skip the HSS1D algebra section")
     ap.add_argument("--config5", action="store_true",
                     help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
     ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv",
@@ -465,6 +510,12 @@ def main():
     if not args.no_batched:
         batched = bench_batched(args, L, dev)
     kgen = bench_kernel_gen(L, dev) if rank == 0 else None
+    algebra = None
+    if rank == 0 and not args.no_algebra:
+        try:
+            algebra = bench_hss1d_algebra()
+        except Exception as e:  # the section is reported, never allowed to drop the bench line
+            algebra = {"error": str(e)}
 
     ok = [p for p in results if results[p]["relres"] <= 1e-10]
     best = min(ok, key=lambda p: results[p]["solve_ms"]) if ok else next(iter(results))
@@ -515,6 +566,8 @@ def main():
         line["batched_hss1d"] = batched
     if kgen is not None:
         line["kernel_gen"] = kgen
+    if algebra is not None:
+        line["hss1d_algebra"] = algebra
     if args.config5:
         line["config5"] = bench_config5(args, L, dev)
     if rank == 0 and not args.no_cpu_baseline:
