@@ -341,6 +341,34 @@ def HSS1D_apply_submatrix_nsym(K_HSS: HSS1DMatrix, Box_dn, Box_up, I_dn, I_up, q
 HSS1D_apply_submatrix_fsym = HSS1D_apply_submatrix_nsym
 
 
+def BHSS1D_apply_nsym(K11, K12, K21, K22, B_dn, B_up, I_dn, I_up, X) -> np.ndarray:
+    """Y = BHSS1D_apply_nsym(K11,K12,K21,K22,B_dn,B_up,I_dn,I_up,X) (HSS1D/BHSS1D_apply_nsym.m:1):
+    Y = A X for the submatrix A = [K11(I_dn{1,1},I_up{1,1}) K12(I_dn{1,2},I_up{1,2});
+    K21(I_dn{2,1},I_up{2,1}) K22(I_dn{2,2},I_up{2,2})] of a 2 x 2 block matrix of compressed
+    matrices, through four submatrix applies on the GPU.  I_dn / I_up are 2 x 2 nested lists
+    of boolean masks over each block's points; B_dn / B_up (box masks) are accepted for the
+    reference's signature and not needed.  X stacks X1 (sum of I_up{1,1} rows) over X2."""
+    X = np.asarray(X, dtype=np.float64)
+    vec = X.ndim == 1
+    X2d = X.reshape(X.shape[0], -1)
+    r1 = int(np.count_nonzero(I_up[0][0]))
+    parts = (X2d[:r1], X2d[r1:])
+    rows = []
+    for i, (Ka, Kb) in enumerate(((K11, K12), (K21, K22))):
+        y = 0.0
+        for j, K in enumerate((Ka, Kb)):
+            up = np.asarray(I_up[i][j], dtype=bool)
+            v = np.zeros((up.size, X2d.shape[1]), order="F")
+            v[up] = parts[j]
+            y = y + HSS1D_apply_submatrix_nsym(K, None, None, I_dn[i][j], up, v)
+        rows.append(y)
+    Y = np.vstack(rows)
+    return Y[:, 0] if vec else Y
+
+
+BHSS1D_apply_fsym = BHSS1D_apply_nsym
+
+
 def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
     q = _as_f64(qq)
     vec = q.ndim == 1

@@ -64,3 +64,32 @@ def test_product_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(ImportError):
         _lib.lib()
+
+
+def test_block_submatrix_apply_composition(monkeypatch):
+    """BHSS1D_apply_nsym's host composition (HSS1D/BHSS1D_apply_nsym.m:38-73): four submatrix
+    applies, X split after the first block column's selected rows.  The GPU submatrix apply is
+    replaced by its dense definition here; the GPU path is tested on a GB300."""
+    import numpy as np
+    from hssc_directsolver_gb300 import hss1d as G1
+
+    class Dense:
+        def __init__(self, A):
+            self.A, self.N = A, A.shape[0]
+
+    def sub(K, bd, bu, dn, up, q):
+        dn, up = np.asarray(dn, bool), np.asarray(up, bool)
+        return K.A[np.ix_(dn, up)] @ np.asarray(q)[up]
+
+    monkeypatch.setattr(G1, "HSS1D_apply_submatrix_nsym", sub)
+    rng = np.random.default_rng(0)
+    K = [Dense(rng.standard_normal((n, n))) for n in (7, 6, 6, 9)]
+    dn1 = np.array([1, 0, 1, 0, 1, 0, 1], bool)
+    dn2 = np.array([1, 1, 0, 0, 1, 0, 0, 1, 0], bool)
+    I_dn = [[dn1, np.array([1, 1, 0, 1, 0, 1], bool)], [np.array([1, 0, 1, 1, 0, 1], bool), dn2]]
+    I_up = [[~dn1, np.array([1, 1, 1, 0, 1, 1], bool)], [np.array([0, 1, 1, 1, 0, 0], bool), ~dn2]]
+    X = rng.standard_normal(((~dn1).sum() + (~dn2).sum(), 2))
+    Y = G1.BHSS1D_apply_nsym(K[0], K[1], K[2], K[3], None, None, I_dn, I_up, X)
+    A = np.block([[K[0].A[np.ix_(I_dn[0][0], I_up[0][0])], K[1].A[np.ix_(I_dn[0][1], I_up[0][1])]],
+                  [K[2].A[np.ix_(I_dn[1][0], I_up[1][0])], K[3].A[np.ix_(I_dn[1][1], I_up[1][1])]]])
+    assert np.abs(Y - A @ X).max() <= 1e-14

@@ -536,3 +536,36 @@ def test_compress_lr_and_low_rank_update(gpu):
     assert rr < 1e-10
     xd = np.linalg.solve(Kd, f)
     assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
+
+
+def test_block_submatrix_apply(gpu):
+    """BHSS1D_apply_nsym: the submatrix of a 2 x 2 block matrix whose blocks are four
+    compressed curves, applied through four GPU submatrix applies, equals the dense product."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    rng = np.random.default_rng(12)
+    kpo = OK.KernelParams(flag=OK.DL_L_2D)
+    n1, n2 = 700, 900
+    Xa, Xb = geometry.star_curve(n1), geometry.star_curve(n2, eps=0.2, m=3)
+    Xc, Xd = geometry.star_curve(800), geometry.star_curve(800, eps=0.1, m=4)
+    Ks = [G1.HSS1D_compress_nsym("green", X, 64, 1e-10, GK.Kernel("DL_L_2D")) for X in (Xa, Xc, Xd, Xb)]
+    Kd = [OK.kernel_eval(X, X, kpo) for X in (Xa, Xc, Xd, Xb)]
+    sizes = [n1, 800, 800, n2]
+    # row masks of the block row i and column masks of the block column j: K11 rows/cols split
+    # into complementary parts as in the reference's use (k1 + r1 = n1)
+    dn1 = rng.random(n1) < 0.5
+    up1 = ~dn1
+    dn2 = rng.random(n2) < 0.4
+    up2 = ~dn2
+    k1, r1, k2, r2 = dn1.sum(), up1.sum(), dn2.sum(), up2.sum()
+    def mask(n, cnt, seed):
+        m = np.zeros(n, bool)
+        m[np.random.default_rng(seed).choice(n, cnt, replace=False)] = True
+        return m
+    I_dn = [[dn1, mask(800, k1, 1)], [mask(800, k2, 2), dn2]]
+    I_up = [[up1, mask(800, r2, 3)], [mask(800, r1, 4), up2]]
+    X = rng.standard_normal((r1 + r2, 2))
+    Y = G1.BHSS1D_apply_nsym(Ks[0], Ks[1], Ks[2], Ks[3], None, None, I_dn, I_up, X)
+    A = np.block([[Kd[0][np.ix_(I_dn[0][0], I_up[0][0])], Kd[1][np.ix_(I_dn[0][1], I_up[0][1])]],
+                  [Kd[2][np.ix_(I_dn[1][0], I_up[1][0])], Kd[3][np.ix_(I_dn[1][1], I_up[1][1])]]])
+    assert Y.shape == (k1 + k2, 2)
+    assert np.linalg.norm(Y - A @ X) <= 1e-9 * np.linalg.norm(A @ X)
