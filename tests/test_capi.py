@@ -52,10 +52,18 @@ def test_status_paths_without_gpu(lib):
     assert lib.hss2d_compress(None) == _lib.HSS_ERR_ARG
     assert lib.hss1d_invert(None) == _lib.HSS_ERR_ARG
     assert b"NULL" in lib.hss_last_error()
+    assert lib.hss1d_sum(None, None, 1e-10, None) == _lib.HSS_ERR_ARG
+    assert lib.hss1d_compress_rect(None, None, 0, 0, None, 0, 0, 64, 1e-10, None, 0) == _lib.HSS_ERR_ARG
+    assert lib.hss1d_rect_info(None, None, None, None, None, None) == _lib.HSS_ERR_ARG
     if n.value == 0:
         h = C.c_void_p()
         p = _lib.hss2d_params(8, 4, 2, 0, 0, 0, 0, 0, 1e-10, _lib.hss_kernel_params())
         assert lib.hss2d_build_tree(C.byref(h), C.byref(p)) == _lib.HSS_ERR_CUDA
+        # the HSS1D constructors need the device before they look at their inputs' values
+        U = (C.c_double * 8)()
+        assert lib.hss1d_compress_lr(C.byref(h), U, U, 4, 2, 4, 4, 2, 1e-10, 0) == _lib.HSS_ERR_CUDA
+        kp = _lib.hss_kernel_params()
+        assert lib.hss1d_compress_rect(C.byref(h), U, 4, 4, U, 4, 4, 2, 1e-10, C.byref(kp), 0) == _lib.HSS_ERR_CUDA
 
 
 def test_product_fails_loudly_without_library(monkeypatch, tmp_path):
