@@ -1,0 +1,121 @@
+"""Complex interpolative decomposition through the real 2 x 2 embedding (oracle; test
+infrastructure).
+
+The Helmholtz / Lippmann-Schwinger path (Common/Kernel_Eval.m:44-53) needs the ID of
+complex blocks (Common/ID.m:40-65 on complex A).  The route planned for the GPU keeps every
+dense kernel real: a complex m x n block A acts as the real 2m x 2n block E(A) with
+E[2i:2i+2, 2j:2j+2] = [[Re a, -Im a], [Im a, Re a]], and the pivoted QR pivots on column
+pairs (2j, 2j+1) -- point j -- instead of single columns.
+
+Why the pair QR reproduces the complex one: the two columns of a pair are c and Jc with J
+the rotation by 90 degrees in every (re, im) row pair, so c' Jc = 0 and |Jc| = |c|.  After
+the reflector of c, the partner's first component vanishes and its trailing norm is |c|,
+so both diagonal entries of a pair equal |R_tt| of the complex QR.  The span of a pair is
+J-invariant, hence the projection onto its complement commutes with J and every remaining
+pair keeps two columns of equal norm: the pivot order over pairs is the complex pivot
+order, the rank counted in pairs is the complex rank, and T = R11 \\ R12 of the pair QR is
+E(T) of the complex ID.  ``pivoted_qr_complex`` restates the complex QR with the same
+exact-norm pivot rule as ``idecomp.pivoted_qr`` (reflectors as LAPACK zlarfg: beta real,
+H = I - tau v v^H)."""
+from __future__ import annotations
+
+import numpy as np
+from scipy.linalg import solve_triangular
+
+
+def embed(A: np.ndarray) -> np.ndarray:
+    """E(A): the real 2m x 2n form of complex A, (re, im) interleaved in rows and columns."""
+    A = np.asarray(A, dtype=np.complex128)
+    m, n = A.shape
+    E = np.empty((2 * m, 2 * n))
+    E[0::2, 0::2] = A.real
+    E[1::2, 0::2] = A.imag
+    E[0::2, 1::2] = -A.imag
+    E[1::2, 1::2] = A.real
+    return E
+
+
+def pivoted_qr_complex(A: np.ndarray):
+    """(R, perm) with A[:, perm] = Q R for complex A: Householder QR choosing, at each step,
+    the remaining column of largest exact trailing norm (lowest index on ties)."""
+    A = np.array(A, dtype=np.complex128, order="F", copy=True)
+    m, n = A.shape
+    perm = np.arange(n)
+    l = min(m, n)
+    norms = np.einsum("ij,ij->j", A.conj(), A).real
+    for j in range(l):
+        p = j + int(np.argmax(norms[j:]))
+        if p != j:
+            A[:, [j, p]] = A[:, [p, j]]
+            perm[[j, p]] = perm[[p, j]]
+        x = A[j:, j]
+        alpha = x[0]
+        xn2 = float(np.vdot(x[1:], x[1:]).real) if x.shape[0] > 1 else 0.0
+        if xn2 != 0.0 or alpha.imag != 0.0:
+            beta = -np.copysign(np.sqrt(abs(alpha) ** 2 + xn2), alpha.real)
+            tau = (beta - alpha) / beta
+            v = x / (alpha - beta)
+            v[0] = 1.0
+            A[j, j] = beta
+            A[j + 1:, j] = 0.0
+            if j + 1 < n:
+                w = v.conj() @ A[j:, j + 1:]
+                A[j:, j + 1:] -= np.conj(tau) * np.outer(v, w)
+        if j + 1 < n:
+            tail = A[j + 1:, j + 1:]
+            norms[j + 1:] = np.einsum("ij,ij->j", tail.conj(), tail).real
+    return np.triu(A[:l, :]), perm
+
+
+def pivoted_qr_pairs(E: np.ndarray):
+    """(R, pair_perm) for a real 2m x 2n block pivoted on column pairs: the pair whose first
+    column has the largest exact trailing norm moves to the front (lowest pair on ties),
+    then one reflector per column of the pair."""
+    A = np.array(E, dtype=np.float64, order="F", copy=True)
+    m2, n2 = A.shape
+    npair = n2 // 2
+    perm = np.arange(npair)
+    l = min(m2, n2) // 2
+    for t in range(l):
+        c0 = 2 * t
+        tail = A[c0:, c0::2]
+        norms = np.einsum("ij,ij->j", tail, tail)
+        p = t + int(np.argmax(norms))
+        if p != t:
+            A[:, [c0, c0 + 1, 2 * p, 2 * p + 1]] = A[:, [2 * p, 2 * p + 1, c0, c0 + 1]]
+            perm[[t, p]] = perm[[p, t]]
+        for j in (c0, c0 + 1):
+            x = A[j:, j]
+            alpha = x[0]
+            xn2 = float(np.dot(x[1:], x[1:])) if x.shape[0] > 1 else 0.0
+            if xn2 == 0.0:
+                continue
+            beta = -np.copysign(np.sqrt(alpha * alpha + xn2), alpha)
+            tau = (beta - alpha) / beta
+            v = x * (1.0 / (alpha - beta))
+            v[0] = 1.0
+            A[j, j] = beta
+            A[j + 1:, j] = 0.0
+            if j + 1 < n2:
+                w = v @ A[j:, j + 1:]
+                A[j:, j + 1:] -= tau * np.outer(v, w)
+    return np.triu(A[:2 * l, :]), perm
+
+
+def id_rank_complex(A: np.ndarray, acc: float):
+    """ID.m's rank rule (k = #{|R_ii| > |R_11| acc}) and T = R11 \\ R12 for complex A."""
+    R, perm = pivoted_qr_complex(A)
+    d = np.abs(np.diag(R))
+    k = int(np.count_nonzero(d > d[0] * acc)) if d.size else 0
+    T = solve_triangular(R[:k, :k], R[:k, k:]) if k else np.zeros((0, A.shape[1]))
+    return T, perm, k
+
+
+def id_rank_pairs(A: np.ndarray, acc: float):
+    """The same on E(A) through the pair QR: rank in pairs, T real (2k x 2(n-k))."""
+    R, perm = pivoted_qr_pairs(embed(A))
+    d = np.abs(np.diag(R))
+    k2 = int(np.count_nonzero(d > d[0] * acc)) if d.size else 0
+    k = k2 // 2
+    T = solve_triangular(R[:2 * k, :2 * k], R[:2 * k, 2 * k:]) if k else np.zeros((0, R.shape[1]))
+    return T, perm, k, k2

@@ -314,3 +314,28 @@ def test_hss1d_compress_lr():
     C = O.sum_nsym(O.compress_nsym(X, 64, 1e-10, kp), H, 1e-10)
     Kd = kernels.kernel_eval(X, X, kp) + U @ V.T
     assert np.linalg.norm(O.apply_nsym(C, q) - Kd @ q) <= 1e-10 * np.linalg.norm(Kd @ q)
+
+
+def test_complex_id_through_real_pairs():
+    """The planned route for the complex (Helmholtz) IDs: the pair-pivoted QR of the real
+    2 x 2 embedding picks the complex pivoted QR's skeleton points, rank, and (with residual
+    columns matched by point) T = E(T_complex) to cond(R11) eps; both IDs have the same error."""
+    from oracle import cid
+    rng = np.random.default_rng(3)
+    kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=2.0 / 128, kh=20.0, dr=0.1 + 0.2j)
+    for _ in range(3):
+        Xs = rng.uniform(-0.1, 0.1, (64, 2))
+        th, r = rng.uniform(0, 2 * np.pi, 150), rng.uniform(0.2, 0.3, 150)
+        A = kernels.kernel_eval(np.stack([r * np.cos(th), r * np.sin(th)], 1), Xs, kp)
+        Tc, pc, kc = cid.id_rank_complex(A, 1e-10)
+        Tr, pr, k, k2 = cid.id_rank_pairs(A, 1e-10)
+        assert k == kc and k2 == 2 * k and np.array_equal(pc[:k], pr[:k])
+        pos = {p: j for j, p in enumerate(pr[k:])}
+        cols = np.ravel([[2 * pos[p], 2 * pos[p] + 1] for p in pc[k:]])
+        E = cid.embed(Tc)
+        assert np.abs(Tr[:, cols] - E).max() <= 1e-5 * np.abs(E).max()
+        ec = np.linalg.norm(A[:, pc[k:]] - A[:, pc[:k]] @ Tc)
+        Ea = cid.embed(A)
+        pair = lambda P: np.ravel([[2 * p, 2 * p + 1] for p in P])
+        er = np.linalg.norm(Ea[:, pair(pr[k:])] - Ea[:, pair(pr[:k])] @ Tr)
+        assert abs(er - ec) <= 1e-4 * ec
