@@ -119,3 +119,52 @@ def id_rank_pairs(A: np.ndarray, acc: float):
     k = k2 // 2
     T = solve_triangular(R[:2 * k, :2 * k], R[:2 * k, 2 * k:]) if k else np.zeros((0, R.shape[1]))
     return T, perm, k, k2
+
+
+def _rand_unit(seed, problem, draw, cols):
+    from .idecomp import _rand_unit as ru
+    return ru(seed, problem, draw, cols)
+
+
+def id_adaptive_complex(A: np.ndarray, acc: float, seed: int = 0, problem: int = 0):
+    """[T, I] = ID(A, acc) (Common/ID.m:40-65) on complex A: the complex pivoted QR, the rank
+    rule |R_ii| > |R_11| acc, and the randomized posterior check of rand_norm / rand_error
+    (:68-86, ' is the conjugate transpose) with real unit vectors from the shared counter
+    RNG, lowering the threshold by 0.75 while the estimate misses acc.  Returns (T, I, k, R)."""
+    A = np.asarray(A, dtype=np.complex128)
+    m, n = A.shape
+    R, I = pivoted_qr_complex(A)
+    Rdg = np.abs(np.diag(R))
+    if Rdg.size == 0:
+        return np.zeros((0, n), dtype=np.complex128), I, 0, R
+
+    def tri(k):
+        if k == 0:
+            return np.zeros((0, n), dtype=np.complex128)
+        return solve_triangular(R[:k, :k], R[:k, k:])
+
+    def rnorm(k, x):
+        Ars = A[:, I[k:]]
+        return np.sqrt(np.linalg.norm(Ars.conj().T @ (Ars @ x)))
+
+    def rerr(T, k, x):
+        Ask, Ars = A[:, I[:k]], A[:, I[k:]]
+        y = Ask @ (T @ x) - Ars @ x
+        y = T.conj().T @ (Ask.conj().T @ y) - Ars.conj().T @ y
+        return np.sqrt(np.linalg.norm(y))
+
+    Rmx = Rdg[0] * acc
+    k = int(np.sum(Rdg > Rmx))
+    T = tri(k)
+    l = min(m, n)
+    draw = 0
+    while k < l:
+        xe = _rand_unit(seed, problem, draw, I[k:])
+        xn = _rand_unit(seed, problem, draw + 1, I[k:])
+        draw += 2
+        if not (rerr(T, k, xe) > rnorm(k, xn) * acc):
+            break
+        Rmx = 0.75 * Rmx
+        k = int(np.sum(Rdg > Rmx))
+        T = tri(k)
+    return T, I, k, R

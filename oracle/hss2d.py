@@ -28,7 +28,7 @@ import math
 
 import numpy as np
 
-from .kernels import KernelParams, kernel_eval, SL_L_2D
+from .kernels import KernelParams, kernel_eval, SL_L_2D, SL_H_2D
 from . import geometry
 from . import idecomp
 
@@ -244,12 +244,21 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             if 2 * b + 1 < nb:
                 I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
             X_src = X[I_src[b]]
+            Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
+            proxy[b] = Xp
+            if prm.kp.flag == SL_H_2D and lev >= depth - 1:
+                # :399-412 -- kh > 0: skeletons by the ID on the two finest levels
+                Tb, Jb, kb = non_preset_skeleton(prm, Xp, X_src, cent[b], lev, b)
+                Js[b] = Jb
+                ks[b] = kb
+                I_sk[b] = I_src[b][Jb[:kb]]
+                T_up[b] = T_dn[b] = Tb
+                qlev = max(qlev, Tb.shape[1])
+                continue
             Jb, kb = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
             Js[b] = Jb
             ks[b] = kb
             I_sk[b] = I_src[b][Jb[:kb]]
-            Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
-            proxy[b] = Xp
             if with_T and lev > 0:
                 X_sk, X_rs = X_src[Jb[:kb]], X_src[Jb[kb:]]
                 if uses_lowrank(prm, lev, depth, kb, X_rs.shape[0]):
@@ -269,11 +278,30 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
     return tree
 
 
+def non_preset_skeleton(prm: HSS2DParams, X_ext, X_src, cB, lev, box):
+    """LOCAL_Non_Preset_Skeleton_Info, HSS2D_build_tree_nsym.m:614-657: [T, J] = ID of
+    K(X_ext, X_src) (the complex ID, problem 2*box of the shared RNG), skeleton points
+    sorted around the box centre and residual points along the interface; T = T(Js, Jr)
+    serves both directions (T_dn = T_up).  Returns (T, J, k)."""
+    from . import cid
+    A21 = kernel_eval(X_ext, X_src, prm.kp)
+    Ttmp, J, k, _ = cid.id_adaptive_complex(A21, prm.acc, prm.seed, 2 * box)
+    if lev % 2 == 0:
+        nrm, tan, th0 = 0, 1, math.pi / 2
+    else:
+        nrm, tan, th0 = 1, 0, 0.0
+    I_sk, I_rs = J[:k], J[k:]
+    Jr = orient_residual(X_src[I_rs], nrm, tan)
+    Js = orient_skeleton(X_src[I_sk], cB, th0)
+    return Ttmp[np.ix_(Js, Jr)], np.concatenate([I_sk[Js], I_rs[Jr]]), k
+
+
 def uses_lowrank(prm: HSS2DParams, lev: int, depth: int, k: int, nr: int) -> bool:
     """LOCAL_Interpolation_Operators (HSS2D_build_tree_nsym.m:842-846): the low-rank T of
     INTERform 'lowrank' on levels above the leaves' parents with k < k_cut (the k >= k_cut
     branch, interpolation_operator_HSS, is the compressed-block path and is not built)."""
-    return prm.INTERform == "lowrank" and lev < depth - 1 and k < prm.k_cut and k > 0 and nr > 0
+    return (prm.INTERform == "lowrank" and prm.kp.flag != SL_H_2D and lev < depth - 1 and k < prm.k_cut and k > 0
+            and nr > 0)
 
 
 def sample_guess(q, lev, m, n, up: bool):
@@ -323,12 +351,13 @@ def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):
         z = np.zeros((k, X_rs.shape[0]))
         return z, z
     kp = prm.kp
+    ls = idecomp.lstsq_qr if kp.flag != SL_H_2D else (lambda A, B: np.linalg.lstsq(A, B, rcond=None)[0])
     K11 = kernel_eval(Xp, X_sk, kp)
     K21 = kernel_eval(Xp, X_rs, kp)
-    Tu = idecomp.lstsq_qr(K11, K21)
+    Tu = ls(K11, K21)
     K11d = kernel_eval(X_sk, Xp, kp).T
     K21d = kernel_eval(X_rs, Xp, kp).T
-    Td = idecomp.lstsq_qr(K11d, K21d)
+    Td = ls(K11d, K21d)
     return Tu, Td
 
 
@@ -337,6 +366,13 @@ class HSS2DBlocks:
     Bself: dict
     B12: dict
     B21: dict
+
+
+def _as_vectors(Xv, tree):
+    """Right-hand sides in the tree's arithmetic: complex when its T are (Helmholtz)."""
+    Xv = np.asarray(Xv)
+    cplx = any(t is not None and np.iscomplexobj(t) for t in tree.T_up)
+    return Xv.astype(np.complex128 if cplx or np.iscomplexobj(Xv) else np.float64, copy=False)
 
 
 def compress_nsym(tree: HSS2DTree, prm: HSS2DParams) -> HSS2DBlocks:
@@ -361,9 +397,10 @@ def _R_L(tree, b):
     k = tree.k[b]
     Jb = tree.J[b]
     n = len(Jb)
-    R = np.zeros((k, n))
+    dt = np.result_type(tree.T_up[b], tree.T_dn[b])
+    R = np.zeros((k, n), dtype=dt)
     R[:, Jb] = np.hstack([np.eye(k), tree.T_up[b]])
-    L = np.zeros((n, k))
+    L = np.zeros((n, k), dtype=dt)
     L[Jb, :] = np.hstack([np.eye(k), tree.T_dn[b]]).T
     return R, L
 
@@ -401,7 +438,7 @@ def invert_nsym(tree: HSS2DTree, prm: HSS2DParams, blocks: HSS2DBlocks | None = 
 
 def apply_nsym(tree: HSS2DTree, blocks: HSS2DBlocks, Xv: np.ndarray) -> np.ndarray:
     """Y = HSS2D_apply_nsym(INFO_TREE, A_HSS, X, params), :74-218 (LR = 0)."""
-    Xv = np.asarray(Xv, dtype=np.float64)
+    Xv = _as_vectors(Xv, tree)
     vec = Xv.ndim == 1
     if vec:
         Xv = Xv[:, None]
@@ -451,7 +488,7 @@ def apply_nsym(tree: HSS2DTree, blocks: HSS2DBlocks, Xv: np.ndarray) -> np.ndarr
 
 def applyinv_nsym(tree: HSS2DTree, inv: dict, Xv: np.ndarray) -> np.ndarray:
     """Y = HSS2D_applyinv_nsym(INFO_TREE, A_HSS, X, params), :74-243 (dense, LR = 0)."""
-    Xv = np.asarray(Xv, dtype=np.float64)
+    Xv = _as_vectors(Xv, tree)
     vec = Xv.ndim == 1
     if vec:
         Xv = Xv[:, None]
@@ -484,7 +521,7 @@ def applyinv_nsym(tree: HSS2DTree, inv: dict, Xv: np.ndarray) -> np.ndarray:
                 lam = np.vstack([up[1], up[2]])
                 eta = np.zeros_like(lam)
             else:
-                tmp = np.zeros((n, Xv.shape[1]))
+                tmp = np.zeros((n, Xv.shape[1]), dtype=Xv.dtype)
                 if k < n:
                     tmp[Jb] = np.vstack([up[b], tree.T_dn[b].T @ up[b]])
                 else:
@@ -515,7 +552,7 @@ def applyinv_nsym(tree: HSS2DTree, inv: dict, Xv: np.ndarray) -> np.ndarray:
 def kernel_matvec(prm: HSS2DParams, Xv: np.ndarray, block: int = 4096) -> np.ndarray:
     """A @ Xv for the dense kernel matrix A = K[X_source, X_source], blockwise."""
     X = prm.X_source()
-    Xv = np.asarray(Xv, dtype=np.float64)
+    Xv = _as_vectors(Xv, tree)
     out = np.zeros_like(Xv)
     for i in range(0, X.shape[0], block):
         out[i:i + block] = kernel_eval(X[i:i + block], X, prm.kp) @ Xv

@@ -339,3 +339,30 @@ def test_complex_id_through_real_pairs():
         pair = lambda P: np.ravel([[2 * p, 2 * p + 1] for p in P])
         er = np.linalg.norm(Ea[:, pair(pr[k:])] - Ea[:, pair(pr[:k])] @ Tr)
         assert abs(er / np.sqrt(2.0) - ec) <= 1e-4 * ec   # |E(M)|_F = sqrt(2) |M|_F
+
+
+def test_hss2d_helmholtz_oracle():
+    """The complex Lippmann-Schwinger HSS2D restated (kh > 0: ID skeletons on the two finest
+    levels, HSS2D_build_tree_nsym.m:399-412 and :614-657; preset boundary skeletons and dense
+    T above; symmetric contrast sqrt(bump) on both sides as the reference's paper test uses):
+    the compressed operator and its direct inverse agree with the dense complex matrix."""
+    from oracle import drweights
+    Ng, npan, kh = 8, 4, 10.0
+    h = 2.0 / (Ng * npan)
+    _, w, _ = drweights.dr_stencil(h, kh, npan * Ng, 4)
+    b, c = kernels.reference_modulations(1, 0, 0, kh)
+    kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=h, b=b, c=c, kh=kh, dr=complex(w[0]))
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense")
+    tree = hss2d.build_tree_nsym(prm)
+    blk = hss2d.compress_nsym(tree, prm)
+    inv = hss2d.invert_nsym(tree, prm, blk)
+    X = prm.X_source()
+    K = kernels.kernel_eval(X, X, kp)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((prm.N, 2)) + 1j * rng.standard_normal((prm.N, 2))
+    f = K @ x
+    assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
+    z = hss2d.applyinv_nsym(tree, inv, f)
+    assert np.linalg.norm(K @ z - f) <= 1e-9 * np.linalg.norm(f)
+    # the ID levels give each box its own rank
+    assert len({tree.k[b] for b in range(2 ** tree.depth - 1, 2 ** (tree.depth + 1) - 1)}) > 1
