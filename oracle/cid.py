@@ -168,3 +168,14 @@ def id_adaptive_complex(A: np.ndarray, acc: float, seed: int = 0, problem: int =
         k = int(np.sum(Rdg > Rmx))
         T = tri(k)
     return T, I, k, R
+
+
+def id_fixed_complex(R: np.ndarray, I: np.ndarray, k: int):
+    """skel_col_fixed (Common/ID.m:106-113) on a complex pivoted QR: T = V_q D_q^-1 U_q^H
+    R(1:k, k+1:end), q = #{sigma > 1e-12}."""
+    n = R.shape[1]
+    if k == 0:
+        return np.zeros((0, n), dtype=np.complex128)
+    U, sv, Vh = np.linalg.svd(R[:k, :k])
+    q = int(np.sum(sv > 1e-12))
+    return Vh.conj().T[:, :q] @ ((U[:, :q].conj().T @ R[:k, k:]) / sv[:q, None])

@@ -47,6 +47,9 @@ class HSS2DParams:
     sym: int = 0
     k_cut: int = 2500
     seed: int = 0
+    # ID levels of the Helmholtz tree: raise every box to the level's largest rank (the
+    # uniform level layout of the GPU build); the reference keeps per-box ranks
+    uniform_ranks: bool = False
 
     @property
     def h(self):
@@ -240,6 +243,7 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
         colrad, rowrad = box_radii(lev)
         lp = lay_prox(prm, lev)
         qlev = 0
+        ids = {}
         for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
             if 2 * b + 1 < nb:
                 I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
@@ -248,12 +252,7 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             proxy[b] = Xp
             if prm.kp.flag == SL_H_2D and lev >= depth - 1:
                 # :399-412 -- kh > 0: skeletons by the ID on the two finest levels
-                Tb, Jb, kb = non_preset_skeleton(prm, Xp, X_src, cent[b], lev, b)
-                Js[b] = Jb
-                ks[b] = kb
-                I_sk[b] = I_src[b][Jb[:kb]]
-                T_up[b] = T_dn[b] = Tb
-                qlev = max(qlev, Tb.shape[1])
+                ids[b] = (X_src, id_box(prm, Xp, X_src, b))
                 continue
             Jb, kb = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
             Js[b] = Jb
@@ -270,6 +269,20 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 else:
                     T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_sk, X_rs)
                     qlev = max(qlev, T_up[b].shape[1])
+        if ids:
+            # the ID level's skeletons; with uniform_ranks every box keeps the level's
+            # largest rank (the fixed-rank ID promotes its next pivoted points)
+            kl = max(r[2] for _, r in ids.values())
+            for b, (X_src, (Tt, J, k, R)) in ids.items():
+                if prm.uniform_ranks and k < kl:
+                    from . import cid
+                    Tt, k = cid.id_fixed_complex(R, J, kl), kl
+                Tb, Jb, kb = orient_id(Tt, J, k, X_src, cent[b], lev)
+                Js[b] = Jb
+                ks[b] = kb
+                I_sk[b] = I_src[b][Jb[:kb]]
+                T_up[b] = T_dn[b] = Tb
+                qlev = max(qlev, Tb.shape[1])
         if lev > 0:
             q[lev] = qlev
     tree = HSS2DTree(depth, cent, I_src, I_sk, Js, ks, T_up, T_dn, proxy, lop)
@@ -278,14 +291,18 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
     return tree
 
 
-def non_preset_skeleton(prm: HSS2DParams, X_ext, X_src, cB, lev, box):
-    """LOCAL_Non_Preset_Skeleton_Info, HSS2D_build_tree_nsym.m:614-657: [T, J] = ID of
-    K(X_ext, X_src) (the complex ID, problem 2*box of the shared RNG), skeleton points
-    sorted around the box centre and residual points along the interface; T = T(Js, Jr)
-    serves both directions (T_dn = T_up).  Returns (T, J, k)."""
+def id_box(prm: HSS2DParams, X_ext, X_src, box):
+    """The ID of LOCAL_Non_Preset_Skeleton_Info (HSS2D_build_tree_nsym.m:614-627): [T, J] =
+    ID(K(X_ext, X_src), acc), the complex ID with problem 2*box of the shared RNG.
+    Returns (T, J, k, R)."""
     from . import cid
-    A21 = kernel_eval(X_ext, X_src, prm.kp)
-    Ttmp, J, k, _ = cid.id_adaptive_complex(A21, prm.acc, prm.seed, 2 * box)
+    return cid.id_adaptive_complex(kernel_eval(X_ext, X_src, prm.kp), prm.acc, prm.seed, 2 * box)
+
+
+def orient_id(Ttmp, J, k, X_src, cB, lev):
+    """The rest of LOCAL_Non_Preset_Skeleton_Info (:629-656): skeleton points sorted around
+    the box centre, residual points along the interface, T = T(Js, Jr), which serves both
+    directions (T_dn = T_up).  Returns (T, J, k)."""
     if lev % 2 == 0:
         nrm, tan, th0 = 0, 1, math.pi / 2
     else:

@@ -352,17 +352,22 @@ def test_hss2d_helmholtz_oracle():
     _, w, _ = drweights.dr_stencil(h, kh, npan * Ng, 4)
     b, c = kernels.reference_modulations(1, 0, 0, kh)
     kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=h, b=b, c=c, kh=kh, dr=complex(w[0]))
-    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense")
-    tree = hss2d.build_tree_nsym(prm)
-    blk = hss2d.compress_nsym(tree, prm)
-    inv = hss2d.invert_nsym(tree, prm, blk)
-    X = prm.X_source()
+    X = hss2d.HSS2DParams(Ng=Ng, npan=npan).X_source()
     K = kernels.kernel_eval(X, X, kp)
     rng = np.random.default_rng(0)
-    x = rng.standard_normal((prm.N, 2)) + 1j * rng.standard_normal((prm.N, 2))
+    x = rng.standard_normal((K.shape[0], 2)) + 1j * rng.standard_normal((K.shape[0], 2))
     f = K @ x
-    assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
-    z = hss2d.applyinv_nsym(tree, inv, f)
-    assert np.linalg.norm(K @ z - f) <= 1e-9 * np.linalg.norm(f)
-    # the ID levels give each box its own rank
-    assert len({tree.k[b] for b in range(2 ** tree.depth - 1, 2 ** (tree.depth + 1) - 1)}) > 1
+    for uniform in (False, True):
+        # uniform: every box of an ID level raised to the level's largest rank by the
+        # fixed-rank ID (the uniform level layout a GPU build keeps); the reference keeps
+        # per-box ranks
+        prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense",
+                                uniform_ranks=uniform)
+        tree = hss2d.build_tree_nsym(prm)
+        blk = hss2d.compress_nsym(tree, prm)
+        inv = hss2d.invert_nsym(tree, prm, blk)
+        assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
+        z = hss2d.applyinv_nsym(tree, inv, f)
+        assert np.linalg.norm(K @ z - f) <= 1e-9 * np.linalg.norm(f)
+        leaf_ranks = {tree.k[b] for b in range(2 ** tree.depth - 1, 2 ** (tree.depth + 1) - 1)}
+        assert (len(leaf_ranks) == 1) == uniform
