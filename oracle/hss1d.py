@@ -10,6 +10,7 @@ Follows, function by function:
   HSS1D/HSS1D_compress_rectangular_nsym.m, HSS1D/HSS1D_apply_rect_nsym.m (rectangular K(Xin, Xout))
   HSS1D/HSS1D_sum_nsym.m        (C = A + B on one tree)
   HSS1D/HSS1D_compressLR_nsym.m (U V^T in compressed form)
+  HSS1D/HSS1D_recompress_nsym.m (rank reduction by SVDs of the far-field blocks)
 
 The cell array ``K_HSS{row, ibox}`` of Common/box_constants.m:33-52 becomes an
 ``HSS1DMatrix`` whose per-box lists are indexed by the 0-based box id (box 0 is
@@ -934,3 +935,101 @@ def compress_lr_nsym(U: np.ndarray, V: np.ndarray, leaf: int, acc: float, seed: 
             H.M_SIB[s1] = U[H.I_SKDN[s1]] @ V[H.I_SKUP[s2]].T
             H.M_SIB[s2] = U[H.I_SKDN[s2]] @ V[H.I_SKUP[s1]].T
     return H
+
+
+# ---------------------------------------------------------------------------
+# Rank reduction of a compressed matrix, HSS1D/HSS1D_recompress_nsym.m
+# ---------------------------------------------------------------------------
+def recompress_nsym(A: HSS1DMatrix, acc: float) -> HSS1DMatrix:
+    """A_NEW = HSS1D_recompress_nsym(A, acc), HSS1D_recompress_nsym.m:26-247.
+
+    Top-down (:30-146): the root's sibling blocks are truncated by their SVDs (singular
+    values above the absolute acc); every other parent stacks its sons' sibling blocks with
+    the parent's far-field factors (Sson = [B, Lp S], Tson = [B; T Rp]) and truncates them
+    by SVD, giving each son a reduced row basis Q' R and column basis L P.  Bottom-up
+    (:148-246): each box IDs its reduced bases at full rank (ID(RNEW, k), k = min(size)),
+    keeps RHO / LAMBDA, and the sibling blocks become LAMBDA_s1 M_SIB RHO_s2."""
+    t = A.tree
+    nb = t.nboxes
+    sv = lambda M: np.linalg.svd(M, full_matrices=False)
+    Rf = lambda b: _rform(A.T_UP[b], A.J_UP[b], A.kskel[b], A.nskel[b])
+    Lf = lambda b: _rform(A.T_DN[b], A.J_DN[b], A.kskel[b], A.nskel[b]).T
+    Tp, Sp, Rp, Lp = {}, {}, {}, {}
+    sib = {}
+    for ib in range(nb):
+        s1, s2 = t.c1[ib], t.c2[ib]
+        if s1 < 0 or s2 < 0:
+            continue
+        k1, k2 = A.kskel[s1], A.kskel[s2]
+        R1, R2, L1, L2 = Rf(s1), Rf(s2), Lf(s1), Lf(s2)
+        B1, B2 = A.M_SIB[s1], A.M_SIB[s2]
+        if ib == 0:
+            P1, D1, Q2h = sv(B1)
+            P2, D2, Q1h = sv(B2)
+            k1n, k2n = int(np.sum(D1 > acc)), int(np.sum(D2 > acc))
+            Q1, Q2 = Q1h.conj().T[:, :k1n], Q2h.conj().T[:, :k2n]
+            P1, P2 = P1[:, :k1n], P2[:, :k2n]
+            D1m = np.diag(D1)[:k1n, :k2n]
+            D2m = np.diag(D2)[:k2n, :k1n]
+            sib[s1], sib[s2] = D1m, D2m
+            Tp[s1], Tp[s2] = D2m, D1m
+            Sp[s1], Sp[s2] = D1m, D2m
+        else:
+            T0, S0, R0, L0 = Tp.pop(ib), Sp.pop(ib), Rp[ib], Lp[ib]
+            Sson1 = np.hstack([B1, L0[:k1] @ S0])
+            Sson2 = np.hstack([B2, L0[k1:] @ S0])
+            Tson2 = np.vstack([B1, T0 @ R0[:, k1:]])
+            Tson1 = np.vstack([B2, T0 @ R0[:, :k1]])
+            Y2, DT2, Q2h = sv(Tson2)
+            Y1, DT1, Q1h = sv(Tson1)
+            P1, DS1, _ = sv(Sson1)
+            P2, DS2, _ = sv(Sson2)
+            k2n = max(int(np.sum(DT2 > acc)), int(np.sum(DS2 > acc)))
+            k1n = max(int(np.sum(DT1 > acc)), int(np.sum(DS1 > acc)))
+            Y1, Y2 = Y1[:, :k1n], Y2[:, :k2n]
+            Q1, Q2 = Q1h.conj().T[:, :k1n], Q2h.conj().T[:, :k2n]
+            P1, P2 = P1[:, :k1n], P2[:, :k2n]
+            DT1m, DT2m = np.diag(DT1[:k1n]), np.diag(DT2[:k2n])
+            sib[s1] = P1.conj().T @ Y2[:k1] @ DT2m
+            sib[s2] = P2.conj().T @ Y1[:k2] @ DT1m
+            Tp[s1], Tp[s2] = DT1m, DT2m
+            Sp[s1], Sp[s2] = np.diag(DS1[:k1n]), np.diag(DS2[:k2n])
+            Rp[ib] = np.hstack([R0[:, :k1] @ Q1, R0[:, k1:] @ Q2])
+            Lp[ib] = np.vstack([P1.conj().T @ L0[:k1], P2.conj().T @ L0[k1:]])
+        Rp[s1], Rp[s2] = Q1.conj().T @ R1, Q2.conj().T @ R2
+        Lp[s1], Lp[s2] = L1 @ P1, L2 @ P2
+    N = HSS1DMatrix(t)
+    for name in ("nskel", "kskel", "I_SKUP", "I_SKDN", "T_UP", "J_UP", "T_DN", "J_DN",
+                 "M_SELF", "M_SIB", "census"):
+        setattr(N, name, [None] * nb)
+    rho, lam = [None] * nb, [None] * nb
+    for ib in range(nb - 1, -1, -1):
+        if t.is_leaf(ib):
+            out = inn = _leaf_range(t, ib)
+            N.M_SELF[ib] = A.M_SELF[ib]
+            RNEW, LNEW = Rp.get(ib), Lp.get(ib)
+        else:
+            s1, s2 = t.c1[ib], t.c2[ib]
+            out = np.concatenate([N.I_SKUP[s1], N.I_SKUP[s2]])
+            inn = np.concatenate([N.I_SKDN[s1], N.I_SKDN[s2]])
+            N.M_SIB[s1] = lam[s1] @ sib[s1] @ rho[s2]
+            N.M_SIB[s2] = lam[s2] @ sib[s2] @ rho[s1]
+            if ib > 0:
+                RA, LA = Rp[ib], Lp[ib]
+                ka1 = rho[s1].shape[0]
+                RNEW = np.hstack([RA[:, :ka1] @ rho[s1], RA[:, ka1:] @ rho[s2]])
+                LNEW = np.vstack([lam[s1] @ LA[:ka1], lam[s2] @ LA[ka1:]])
+        if ib == 0:
+            continue
+        k = min(RNEW.shape)
+        Rq, Jout = idecomp.pivoted_qr(RNEW)
+        Tout = idecomp.id_fixed_from_qr(Rq, Jout, k)
+        Rq2, Jin = idecomp.pivoted_qr(LNEW.T)
+        Tin = idecomp.id_fixed_from_qr(Rq2, Jin, k)
+        N.I_SKUP[ib], N.T_UP[ib], N.J_UP[ib] = out[Jout[:k]], Tout, Jout
+        N.I_SKDN[ib], N.T_DN[ib], N.J_DN[ib] = inn[Jin[:k]], Tin, Jin
+        N.nskel[ib], N.kskel[ib] = len(out), k
+        N.census[ib] = (RNEW.shape[0], LNEW.shape[1], len(out), k, k, k)
+        rho[ib] = RNEW[:, Jout[:k]]
+        lam[ib] = LNEW[Jin[:k], :]
+    return N

@@ -371,3 +371,19 @@ def test_hss2d_helmholtz_oracle():
         assert np.linalg.norm(K @ z - f) <= 1e-9 * np.linalg.norm(f)
         leaf_ranks = {tree.k[b] for b in range(2 ** tree.depth - 1, 2 ** (tree.depth + 1) - 1)}
         assert (len(leaf_ranks) == 1) == uniform
+
+
+def test_hss1d_recompress():
+    """HSS1D_recompress_nsym restated: a compression at 1e-14 recompressed at acc keeps the
+    operator to ~acc with much smaller ranks (SVD truncation of the far-field blocks)."""
+    from oracle import hss1d as O
+    X = geometry.star_curve(768)
+    kp = kernels.KernelParams(flag=kernels.DL_L_2D)
+    A = O.compress_nsym(X, 64, 1e-14, kp)
+    I = np.eye(768)
+    Ka = O.apply_nsym(A, I)
+    for acc in (1e-6, 1e-10):
+        R = O.recompress_nsym(A, acc)
+        assert max(R.kskel[1:]) < max(A.kskel[1:])
+        Kr = O.apply_nsym(R, I)
+        assert np.linalg.norm(Kr - Ka, 2) <= 20 * acc * np.linalg.norm(Ka, 2)
