@@ -142,6 +142,22 @@ def cpu_sample(npan: int = 32, nrhs: int = 4, budget_s: float = 20.0):
     return float(np.median(times)), len(times)
 
 
+def cpu_compress_invert(npan: int = 32):
+    """Seconds of the oracle's tree build (interpolation operators), compress and invert
+    (HSS2D_build_tree_nsym / HSS2D_compress_nsym / HSS2D_invert_nsym restated in NumPy,
+    dense T) on the workload's grid and kernel, on the host cores: the CPU side of the
+    metric's compress+invert comparison."""
+    from oracle import hss2d as O2, kernels as OK
+    h = 2.0 / (8 * npan)
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=h, c=OK.Modulation(0.5, 0.0, 0.0, 20.0))
+    prm = O2.HSS2DParams(Ng=8, npan=npan, kp=kp, layers=2, acc=1e-10, INTERform="dense")
+    t0 = time.perf_counter()
+    tree = O2.build_tree_nsym(prm)
+    blk = O2.compress_nsym(tree, prm)
+    O2.invert_nsym(tree, prm, blk)
+    return time.perf_counter() - t0
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -151,6 +167,7 @@ def run_reference(args):
     steps = []
     t_solve, n = cpu_sample(budget_s=max(5.0, 2.0 * (args.steps + args.warmup)))
     value = 1.0 / t_solve
+    t_ci = cpu_compress_invert(args.npan) if not args.no_cpu_ci else None
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": True,
@@ -161,6 +178,11 @@ def run_reference(args):
                                    f"shapes, {n} timed solves of 4 RHS, median"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if t_ci is not None:
+        line["compress_invert_s"] = {"fp64": t_ci}
+        line["cpu_baseline"]["compress_invert_s"] = t_ci
+        line["cpu_baseline"]["compress_invert_sample"] = ("oracle build_tree (dense T) + compress + invert at the "
+                                                          "full workload, once")
     print(json.dumps(line), flush=True)
     return 0
 
@@ -382,6 +404,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-curve batched HSS1D section")
     ap.add_argument("--curves", type=int, default=512)
     ap.add_argument("--no-algebra", action="store_true", help="skip the HSS1D algebra section")
+    ap.add_argument("--no-cpu-ci", action="store_true",
+                    help="skip the CPU oracle's compress+invert (about a minute at the full workload)")
     ap.add_argument("--config5", action="store_true",
                     help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
     ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv",
@@ -577,6 +601,14 @@ def main():
             line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": cores, "kind": "port",
                                     "sample": f"oracle HSS2D_applyinv_nsym over factors of the workload's shapes, "
                                               f"{n_cpu} solves of 4 RHS, median"}
+            if not args.no_cpu_ci:
+                try:
+                    t_ci = cpu_compress_invert(args.npan)
+                    line["cpu_baseline"]["compress_invert_s"] = t_ci
+                    line["cpu_baseline"]["compress_invert_sample"] = ("oracle build_tree (dense T) + compress + "
+                                                                      "invert at the full workload, once")
+                except Exception as e:  # reported, never required
+                    line["cpu_baseline"]["compress_invert_sample"] = f"failed: {e}"
         except Exception as e:  # the CPU baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                                     "sample": f"failed: {e}"}

@@ -11,7 +11,8 @@ ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 def _run(env_extra):
     env = dict(os.environ, **env_extra)
     p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+                        "--warmup", "0", "--no-cpu-ci"], cwd=ROOT, env=env, capture_output=True, text=True,
+                       timeout=600)
     assert p.returncode == 0, p.stderr[-2000:]
     return [l for l in p.stdout.splitlines() if l.strip()]
 
@@ -30,3 +31,12 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_are_silent():
     assert _run({"RANK": "1"}) == []
+
+
+def test_cpu_compress_invert_runs():
+    """The CPU side of the compress+invert comparison (oracle tree + compress + invert) on a
+    small grid."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.cpu_compress_invert(npan=4)
+    assert t > 0
