@@ -594,7 +594,7 @@ def main():
         line["hss1d_algebra"] = algebra
     if args.config5:
         line["config5"] = bench_config5(args, L, dev)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         try:
             cores = os.cpu_count() or 1
             t_cpu, n_cpu = cpu_sample(args.npan, nrhs, budget_s=15.0)
