@@ -219,8 +219,9 @@ def leaf_sources(prm: HSS2DParams, cent):
 
 
 def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
-    """INFO_TREE = HSS2D_build_tree_nsym(params), 'uniform'/'bdry'/'bdry', NTI."""
-    assert prm.transinv == 0
+    """INFO_TREE = HSS2D_build_tree_nsym(params), 'uniform'/'bdry'/'bdry'.  With transinv
+    (:421-438, :507-548) the first box of each level computes (J, k, T) and every other
+    box of the level takes them over on its own source set."""
     depth = prm.depth
     h = prm.h
     X = prm.X_source()
@@ -244,12 +245,17 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
         lp = lay_prox(prm, lev)
         qlev = 0
         ids = {}
+        first = 2 ** lev - 1
+        followers = []
         for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
             if 2 * b + 1 < nb:
                 I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
             X_src = X[I_src[b]]
             Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
             proxy[b] = Xp
+            if prm.transinv and b != first:
+                followers.append(b)
+                continue
             if prm.kp.flag == SL_H_2D and lev >= depth - 1:
                 # :399-412 -- kh > 0: skeletons by the ID on the two finest levels
                 ids[b] = (X_src, id_box(prm, Xp, X_src, b))
@@ -273,16 +279,19 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             # the ID level's skeletons; with uniform_ranks every box keeps the level's
             # largest rank (the fixed-rank ID promotes its next pivoted points)
             kl = max(r[2] for _, r in ids.values())
-            for b, (X_src, (Tt, J, k, R)) in ids.items():
+            for b, (X_src, (Tt, Jp, k, R)) in ids.items():
                 if prm.uniform_ranks and k < kl:
                     from . import cid
-                    Tt, k = cid.id_fixed_complex(R, J, kl), kl
-                Tb, Jb, kb = orient_id(Tt, J, k, X_src, cent[b], lev)
+                    Tt, k = cid.id_fixed_complex(R, Jp, kl), kl
+                Tb, Jb, kb = orient_id(Tt, Jp, k, X_src, cent[b], lev)
                 Js[b] = Jb
                 ks[b] = kb
                 I_sk[b] = I_src[b][Jb[:kb]]
                 T_up[b] = T_dn[b] = Tb
                 qlev = max(qlev, Tb.shape[1])
+        for b in followers:   # transinv: the level's first box's skeleton data
+            Js[b], ks[b], T_up[b], T_dn[b] = Js[first], ks[first], T_up[first], T_dn[first]
+            I_sk[b] = I_src[b][Js[first][:ks[first]]]
         if lev > 0:
             q[lev] = qlev
     tree = HSS2DTree(depth, cent, I_src, I_sk, Js, ks, T_up, T_dn, proxy, lop)

@@ -387,3 +387,29 @@ def test_hss1d_recompress():
         assert max(R.kskel[1:]) < max(A.kskel[1:])
         Kr = O.apply_nsym(R, I)
         assert np.linalg.norm(Kr - Ka, 2) <= 20 * acc * np.linalg.norm(Ka, 2)
+
+
+def test_hss2d_translation_invariant_oracle():
+    """transinv = 1 in the oracle tree (the level's first box computes (J, k, T), the other
+    boxes take them over): on the unmodulated Helmholtz kernel with its Duan-Rokhlin diagonal
+    (the reference's TI case 5.3) the operator and its solve match the dense matrix."""
+    from oracle import drweights
+    Ng, npan, kh = 8, 4, 10.0
+    h = 2.0 / (Ng * npan)
+    _, w, _ = drweights.dr_stencil(h, kh, npan * Ng, 4)
+    kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=h, kh=kh, dr=complex(w[0]))
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense", transinv=1)
+    tree = hss2d.build_tree_nsym(prm)
+    for lev in range(1, tree.depth + 1):
+        boxes = range(2 ** lev - 1, 2 ** (lev + 1) - 1)
+        assert len({tree.k[b] for b in boxes}) == 1
+        assert all(tree.T_up[b] is tree.T_up[2 ** lev - 1] for b in boxes)
+    blk = hss2d.compress_nsym(tree, prm)
+    inv = hss2d.invert_nsym(tree, prm, blk)
+    X = prm.X_source()
+    K = kernels.kernel_eval(X, X, kp)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((prm.N, 2)) + 1j * rng.standard_normal((prm.N, 2))
+    f = K @ x
+    assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
+    assert np.linalg.norm(K @ hss2d.applyinv_nsym(tree, inv, f) - f) <= 1e-9 * np.linalg.norm(f)
