@@ -413,3 +413,41 @@ def test_hss2d_translation_invariant_oracle():
     f = K @ x
     assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
     assert np.linalg.norm(K @ hss2d.applyinv_nsym(tree, inv, f) - f) <= 1e-9 * np.linalg.norm(f)
+
+
+def test_gmres_restated():
+    """GMRES(m) with restarts on real and complex systems reaches its tolerance."""
+    from oracle import krylov
+    rng = np.random.default_rng(1)
+    A = np.eye(200) * 4 + (rng.standard_normal((200, 200)) + 1j * rng.standard_normal((200, 200))) / 10
+    b = rng.standard_normal(200) + 1j * rng.standard_normal(200)
+    x, rr, _ = krylov.gmres(lambda v: A @ v, lambda v: v, b, tol=1e-12, restart=10)
+    assert rr <= 1e-12 and np.linalg.norm(A @ x - b) <= 1e-11 * np.linalg.norm(b)
+    Ar = np.eye(150) * 3 + rng.standard_normal((150, 150)) / 8
+    br = rng.standard_normal(150)
+    x, rr, _ = krylov.gmres(lambda v: Ar @ v, lambda v: v, br, tol=1e-12, restart=7)
+    assert rr <= 1e-12
+
+
+def test_lippmann_schwinger_gmres_with_complex64_inverse():
+    """The Lippmann-Schwinger configuration's solve: complex128 GMRES on the operator,
+    preconditioned by the HSS inverse held in complex64, reaches 1e-8 in a few iterations
+    (69 without the preconditioner)."""
+    from oracle import drweights, krylov
+    Ng, npan, kh = 8, 4, 10.0
+    h = 2.0 / (Ng * npan)
+    _, w, _ = drweights.dr_stencil(h, kh, npan * Ng, 4)
+    b, c = kernels.reference_modulations(1, 0, 0, kh)
+    kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=h, b=b, c=c, kh=kh, dr=complex(w[0]))
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense")
+    tree = hss2d.build_tree_nsym(prm)
+    inv = hss2d.invert_nsym(tree, prm, hss2d.compress_nsym(tree, prm))
+    inv32 = {k: [None if a is None else a.astype(np.complex64) for a in v] for k, v in inv.items()}
+    X = prm.X_source()
+    K = kernels.kernel_eval(X, X, kp)
+    rng = np.random.default_rng(0)
+    f = rng.standard_normal(prm.N) + 1j * rng.standard_normal(prm.N)
+    M = lambda v: hss2d.applyinv_nsym(tree, inv32, v.astype(np.complex64)[:, None])[:, 0].astype(np.complex128)
+    x, rr, its = krylov.gmres(lambda v: K @ v, M, f, tol=1e-8)
+    assert rr <= 1e-8 and its <= 3
+    assert np.linalg.norm(K @ x - f) <= 1e-8 * np.linalg.norm(f)
