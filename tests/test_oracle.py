@@ -451,3 +451,30 @@ def test_lippmann_schwinger_gmres_with_complex64_inverse():
     x, rr, its = krylov.gmres(lambda v: K @ v, M, f, tol=1e-8)
     assert rr <= 1e-8 and its <= 3
     assert np.linalg.norm(K @ x - f) <= 1e-8 * np.linalg.norm(f)
+
+
+def test_reference_sum_test_workflow():
+    """Test_HSS1D_SUM.m restated on the oracle: A on the skeleton of box 7 (level 2) of the
+    Run_HSS1D_tests.m geometry (SL_L_2D, Ng=7, np=16, lay=2, nbox_max 56), B the same points
+    with h -> 100 h, C = HSS1D_sum_nsym(A, B), CR = HSS1D_recompress_nsym(C); the test's
+    Err_sum = |uC - (uA + uB)| / |uA + uB| and Err_rec = |uC - uCR| / |uA + uB| on 10 normal
+    columns."""
+    from oracle import hss1d as O
+    Ng, npan, acc = 7, 16, 1e-10
+    h = 2.0 / (Ng * npan)
+    b, c = kernels.reference_modulations(sym=0, proxy=1, transinv=0)
+    kp = kernels.KernelParams(flag=kernels.SL_L_2D, h=h, b=b, c=c)
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp)
+    X = prm.X_source()[hss2d.build_tree_nsym(prm, with_T=False).I_sk[6]]
+    kpB = kernels.KernelParams(flag=kernels.SL_L_2D, h=100 * h, b=b, c=c)
+    A = O.compress_nsym(X, 56, acc, kp)
+    B = O.compress_nsym(X, 56, acc, kpB)
+    C = O.sum_nsym(A, B, acc)
+    CR = O.recompress_nsym(C, acc)
+    q = np.random.default_rng(0).standard_normal((X.shape[0], 10))
+    u_sum = O.apply_nsym(A, q) + O.apply_nsym(B, q)
+    uC = O.apply_nsym(C, q)
+    err_sum = np.linalg.norm(uC - u_sum) / np.linalg.norm(u_sum)
+    err_rec = np.linalg.norm(uC - O.apply_nsym(CR, q)) / np.linalg.norm(u_sum)
+    assert err_sum < 1e-9 and err_rec < 1e-8
+    assert max(CR.kskel[1:]) <= max(C.kskel[1:])
