@@ -478,3 +478,20 @@ def test_reference_sum_test_workflow():
     err_rec = np.linalg.norm(uC - O.apply_nsym(CR, q)) / np.linalg.norm(u_sum)
     assert err_sum < 1e-9 and err_rec < 1e-8
     assert max(CR.kskel[1:]) <= max(C.kskel[1:])
+
+
+def test_reference_lowrank_test_workflow():
+    """Test_LowRank_HSS1D.m restated on the oracle: U, V of 800 x 50 normal entries scaled by
+    their 2-norms, HSS1D_compressLR_nsym with n_max = 2k = 100, and the apply against
+    U (V' q) on 10 normal columns (its Err_Apply, over the exact product's norm)."""
+    from oracle import hss1d as O
+    rng = np.random.default_rng(0)
+    M, k = 800, 50
+    U = rng.standard_normal((M, k))
+    U /= np.linalg.norm(U, 2)
+    V = rng.standard_normal((M, k))
+    V /= np.linalg.norm(V, 2)
+    T = O.compress_lr_nsym(U, V, 2 * k, 1e-10)
+    q = rng.standard_normal((M, 10))
+    ut = U @ (V.T @ q)
+    assert np.linalg.norm(O.apply_nsym(T, q) - ut) <= 1e-12 * np.linalg.norm(ut)
