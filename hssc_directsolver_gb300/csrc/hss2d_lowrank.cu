@@ -8,8 +8,8 @@
 // stored in the dense T arrays, so compress, invert and the applies read one T format.
 //
 // Every step runs batched over all 2*nb ID problems of the level:
-//   round 0   G (p x k0) Gaussian, Y = K21^T G, pivoted QR of Y -> Q, |diag R|
-//   round r   problems whose last |R_jj| still exceeds acc draw C more columns:
+//   sample 0  G (p x k0) Gaussian, Y = K21^T G, pivoted QR of Y -> Q, |diag R|
+//   sample s  problems whose last |R_jj| still exceeds acc draw C more columns:
 //             Ynew = K21^T G, M = Ynew - Q Q^T Ynew, pivoted QR of M -> Qc,
 //             Qc -= Q Q^T Qc, Q = [Q Qc]  (the host counts |R_jj| > acc per problem)
 //   then      pivoted QR of Z = Y(:,1:q)^T and the fixed-rank ID (1e-12 pseudo-inverse cut),
@@ -160,7 +160,7 @@ void HSS2D::lowrank_T(int lev, const double* A, DevBuf<double>& Vw, DevBuf<doubl
     for (int b : act)
       gs.push_back(GemmP<double>{A2(b), Gp(b), Yp(b) + (size_t)krank[b] * nr, nr, num[b], p, p, p, nr});
     run_gemm_list(gs, true, false, 1.0, 0.0, st);
-    // M = Ynew (round 0) or Ynew - Q Q^T Ynew
+    // M = Ynew (first sample block) or Ynew - Q Q^T Ynew
     std::vector<MoveP> mv;
     for (int b : act)
       mv.push_back(MoveP{Yp(b) + (size_t)krank[b] * nr, Mp(b), nullptr, nr, num[b], nr, nr, 0, 0});
