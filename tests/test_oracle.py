@@ -483,7 +483,9 @@ def test_reference_sum_test_workflow():
 def test_reference_lowrank_test_workflow():
     """Test_LowRank_HSS1D.m restated on the oracle: U, V of 800 x 50 normal entries scaled by
     their 2-norms, HSS1D_compressLR_nsym with n_max = 2k = 100, and the apply against
-    U (V' q) on 10 normal columns (its Err_Apply, over the exact product's norm)."""
+    U (V' q) on 10 normal columns (its Err_Apply, over the exact product's norm).  The
+    reference's sample output for this test is 6.4e-16 (INSTALL.txt:36-43); rounding-level
+    agreement is the criterion here."""
     from oracle import hss1d as O
     rng = np.random.default_rng(0)
     M, k = 800, 50
@@ -494,4 +496,4 @@ def test_reference_lowrank_test_workflow():
     T = O.compress_lr_nsym(U, V, 2 * k, 1e-10)
     q = rng.standard_normal((M, 10))
     ut = U @ (V.T @ q)
-    assert np.linalg.norm(O.apply_nsym(T, q) - ut) <= 1e-12 * np.linalg.norm(ut)
+    assert np.linalg.norm(O.apply_nsym(T, q) - ut) <= 1e-14 * np.linalg.norm(ut)
