@@ -578,7 +578,9 @@ def applyinv_nsym(tree: HSS2DTree, inv: dict, Xv: np.ndarray) -> np.ndarray:
 def kernel_matvec(prm: HSS2DParams, Xv: np.ndarray, block: int = 4096) -> np.ndarray:
     """A @ Xv for the dense kernel matrix A = K[X_source, X_source], blockwise."""
     X = prm.X_source()
-    Xv = _as_vectors(Xv, tree)
+    Xv = np.asarray(Xv)
+    cplx = np.iscomplexobj(Xv) or prm.kp.flag == SL_H_2D
+    Xv = Xv.astype(np.complex128 if cplx else np.float64, copy=False)
     out = np.zeros_like(Xv)
     for i in range(0, X.shape[0], block):
         out[i:i + block] = kernel_eval(X[i:i + block], X, prm.kp) @ Xv

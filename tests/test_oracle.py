@@ -125,6 +125,7 @@ def test_hss2d_small_against_dense():
     X = prm.X_source()
     A = kernels.kernel_eval(X, X, kp)
     q = np.random.default_rng(2).standard_normal((prm.N, 3))
+    assert np.abs(hss2d.kernel_matvec(prm, q, block=100) - A @ q).max() <= 1e-12 * np.abs(A @ q).max()
     assert np.linalg.norm(hss2d.apply_nsym(tree, blk, q) - A @ q) / np.linalg.norm(A @ q) < 1e-8
     y = hss2d.applyinv_nsym(tree, inv, q)
     yd = np.linalg.solve(A, q)
@@ -411,6 +412,7 @@ def test_hss2d_translation_invariant_oracle():
     rng = np.random.default_rng(0)
     x = rng.standard_normal((prm.N, 2)) + 1j * rng.standard_normal((prm.N, 2))
     f = K @ x
+    assert np.abs(hss2d.kernel_matvec(prm, x, block=300) - f).max() <= 1e-12 * np.abs(f).max()
     assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
     assert np.linalg.norm(K @ hss2d.applyinv_nsym(tree, inv, f) - f) <= 1e-9 * np.linalg.norm(f)
 
