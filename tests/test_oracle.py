@@ -499,3 +499,21 @@ def test_reference_lowrank_test_workflow():
     q = rng.standard_normal((M, 10))
     ut = U @ (V.T @ q)
     assert np.linalg.norm(O.apply_nsym(T, q) - ut) <= 1e-14 * np.linalg.norm(ut)
+
+
+def test_reference_hss2d_test_configuration():
+    """Run_HSS2D_tests.m's configuration (SL_L_2D, kh = 0, sym = 1, Ng = 16, np = 8,
+    acc = 1e-10, lay = 2, TI = 1: N = 16384, translation-invariant tree) through
+    Test_HSS2D_InverseCompression's checks: the HSS inverse application's residual against
+    the dense kernel and the residual after one refinement step against the dense kernel.
+    The reference's sample output is 3.0e-11 and 7.5e-16 (INSTALL.txt:61-63)."""
+    kp = kernels.KernelParams(flag=kernels.SL_L_2D, h=2.0 / (16 * 8))
+    prm = hss2d.HSS2DParams(Ng=16, npan=8, kp=kp, layers=2, acc=1e-10, transinv=1, INTERform="dense")
+    tree = hss2d.build_tree_nsym(prm)
+    inv = hss2d.invert_nsym(tree, prm, hss2d.compress_nsym(tree, prm))
+    f = np.random.default_rng(0).standard_normal((prm.N, 2))
+    x = hss2d.applyinv_nsym(tree, inv, f)
+    r = f - hss2d.kernel_matvec(prm, x)
+    assert np.linalg.norm(r) / np.linalg.norm(f) < 1e-10
+    x1 = x + hss2d.applyinv_nsym(tree, inv, r)
+    assert np.linalg.norm(f - hss2d.kernel_matvec(prm, x1)) / np.linalg.norm(f) < 1e-14
