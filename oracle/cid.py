@@ -179,3 +179,85 @@ def id_fixed_complex(R: np.ndarray, I: np.ndarray, k: int):
     U, sv, Vh = np.linalg.svd(R[:k, :k])
     q = int(np.sum(sv > 1e-12))
     return Vh.conj().T[:, :q] @ ((U[:, :q].conj().T @ R[:k, k:]) / sv[:q, None])
+
+
+def _pivoted_qr_q_complex(Y: np.ndarray):
+    """Complex Householder QR with column pivoting (exact trailing norms, lowest index on
+    ties) returning the explicit thin Q, |diag R| and the pivots."""
+    A = np.array(Y, dtype=np.complex128, order="F", copy=True)
+    m, n = A.shape
+    l = min(m, n)
+    perm = np.arange(n)
+    vs, taus = [], []
+    norms = np.einsum("ij,ij->j", A.conj(), A).real
+    for j in range(l):
+        p = j + int(np.argmax(norms[j:]))
+        if p != j:
+            A[:, [j, p]] = A[:, [p, j]]
+            perm[[j, p]] = perm[[p, j]]
+        x = A[j:, j]
+        alpha = x[0]
+        xn2 = float(np.vdot(x[1:], x[1:]).real) if x.shape[0] > 1 else 0.0
+        if xn2 == 0.0 and alpha.imag == 0.0:
+            vs.append(None)
+            taus.append(0.0)
+        else:
+            beta = -np.copysign(np.sqrt(abs(alpha) ** 2 + xn2), alpha.real)
+            tau = (beta - alpha) / beta
+            v = x / (alpha - beta)
+            v[0] = 1.0
+            A[j, j] = beta
+            A[j + 1:, j] = 0.0
+            if j + 1 < n:
+                A[j:, j + 1:] -= np.conj(tau) * np.outer(v, v.conj() @ A[j:, j + 1:])
+            vs.append(v)
+            taus.append(tau)
+        if j + 1 < n:
+            tail = A[j + 1:, j + 1:]
+            norms[j + 1:] = np.einsum("ij,ij->j", tail.conj(), tail).real
+    Q = np.zeros((m, l), dtype=np.complex128)
+    Q[:l, :l] = np.eye(l)
+    for j in range(l - 1, -1, -1):   # Q = H_0 ... H_{l-1} [I; 0], H = I - tau v v^H
+        if vs[j] is None:
+            continue
+        v, tau = vs[j], taus[j]
+        Q[j:, :] -= tau * np.outer(v, v.conj() @ Q[j:, :])
+    D = np.abs(np.diag(A[:l, :l])) if l else np.zeros(0)
+    return Q, D, perm
+
+
+def id_rand_complex(A: np.ndarray, k0: int, C: int, tol: float, seed: int, problem: int):
+    """[T, J] = ID_rand(m, n, A, A.', 'norm', tol, k0, C) (Common/ID_rand.m:26-49 over
+    QR_findrank.m:45-91) for complex A: real Gaussian sketches Y = A.' G from the shared
+    counter RNG (as the real oracle draws them), the adaptive range finder with absolute
+    tolerance, then the pivoted QR of Z = Y.' and the fixed-rank ID.  Returns (T, J, k)."""
+    from .randid import gauss
+    from . import rng
+    A = np.asarray(A, dtype=np.complex128)
+    m, n = A.shape
+    mn = min(m, n)
+    k0 = max(1, min(k0, mn))
+    draw = 0
+    Y = A.T @ gauss(seed, rng.id_stream(problem, draw), m, k0)
+    draw += 1
+    Q, D, _ = _pivoted_qr_q_complex(Y)
+    residual = D[-1] if D.size else 0.0
+    krank = int(np.sum(D > tol))
+    while residual > tol and krank < mn:
+        num = min(C, mn - krank)
+        if num <= 0:
+            break
+        Ynew = A.T @ gauss(seed, rng.id_stream(problem, draw), m, num)
+        draw += 1
+        if Y.shape[1] < krank + num:
+            Y = np.hstack([Y, np.zeros((n, krank + num - Y.shape[1]), dtype=np.complex128)])
+        Y[:, krank:krank + num] = Ynew
+        M = Ynew - Q @ (Q.conj().T @ Ynew)
+        Qc, D, _ = _pivoted_qr_q_complex(M)
+        residual = D[-1] if D.size else 0.0
+        krank += int(np.sum(D > tol))
+        Qc = Qc - Q @ (Q.conj().T @ Qc)
+        Q = np.hstack([Q, Qc])
+    Z = Y[:, :krank].T
+    R, J = pivoted_qr_complex(Z)
+    return id_fixed_complex(R, J, krank), J, krank

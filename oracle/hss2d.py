@@ -50,6 +50,10 @@ class HSS2DParams:
     # ID levels of the Helmholtz tree: raise every box to the level's largest rank (the
     # uniform level layout of the GPU build); the reference keeps per-box ranks
     uniform_ranks: bool = False
+    # params.proxy_rule / lambda / skel_extra_pts (HSS_tree_parameters.m:121-124)
+    proxy_rule: str = "bdry"
+    lambda_: float = 2.0
+    skel_extra_pts: int = 0
 
     @property
     def h(self):
@@ -252,6 +256,8 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 I_src[b] = np.concatenate([I_sk[2 * b + 1], I_sk[2 * b + 2]])
             X_src = X[I_src[b]]
             Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
+            if prm.proxy_rule == "rand":
+                Xp = random_proxy(Xp, len(I_src[b]), cent[b], colrad, rowrad, lev, prm)
             proxy[b] = Xp
             if prm.transinv and b != first:
                 followers.append(b)
@@ -275,6 +281,11 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 else:
                     T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_sk, X_rs)
                     qlev = max(qlev, T_up[b].shape[1])
+                if prm.skel_extra_pts and b not in lowrank and len(Jb) - kb > 0:
+                    T_up[b], T_dn[b], Jb, kb = extra_points(prm, T_up[b], T_dn[b], Jb, kb, Xp, X_src, cent[b],
+                                                            lev, b)
+                    Js[b], ks[b] = Jb, kb
+                    I_sk[b] = I_src[b][Jb[:kb]]
         if ids:
             # the ID level's skeletons; with uniform_ranks every box keeps the level's
             # largest rank (the fixed-rank ID promotes its next pivoted points)
@@ -298,6 +309,77 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
     tree.lowrank = lowrank
     tree.q = q
     return tree
+
+
+def random_sampler(X, cB, colrad, rowrad, lam, lay, h):
+    """LOCAL_random_sampler, HSS2D_build_tree_nsym.m:964-1001: points within lay*h of the
+    box are kept, farther ones with probability 2^(-lam * l) by dyadic distance band l.
+    The reference resets MATLAB's generator (rng('default'): the Mersenne Twister with its
+    default seed, 5489) on every call; numpy's RandomState(5489) is that generator, so the
+    same uniforms are drawn (not verified against MATLAB here)."""
+    D = np.abs(np.minimum(colrad - np.abs(X[:, 0] - cB[0]), rowrad - np.abs(X[:, 1] - cB[1])))
+    width = lay * h
+    rad = D.max()
+    sz = -math.floor(math.log2(width / rad)) + 1
+    prob = 2.0 ** (-lam * np.arange(sz - 1, -1, -1, dtype=np.float64))
+    B = D < width
+    with np.errstate(divide="ignore"):
+        Ld = np.minimum(-np.ceil(np.log2(D / rad)), sz - 2) + 1
+    Ld[B] = sz
+    if sz > 0:
+        P = prob[Ld.astype(np.int64) - 1]
+        B = np.random.RandomState(5489).random_sample(P.shape[0]) < P
+    return X[B]
+
+
+def random_proxy(X_ext, n_skel, cB, colrad, rowrad, lev, prm: HSS2DParams):
+    """LOCAL_Build_Proxy, 'rand' rule (:883-905): the 'bdry' layers sampled until at least
+    k0 = ceil(2/3 n) (even levels) or ceil(3/4 n) (odd) points remain; each retry samples
+    the previous sample again with a wider target and 0.9 lambda, as the reference does."""
+    k0 = math.ceil((2 / 3) * n_skel) if lev % 2 == 0 else math.ceil((3 / 4) * n_skel)
+    k0 = min(k0, X_ext.shape[0])
+    lam, k, c = prm.lambda_, 0, 0
+    while k0 > k and c < 10:
+        X_ext = random_sampler(X_ext, cB, colrad, rowrad, lam, prm.layers, prm.h)
+        k = X_ext.shape[0]
+        if k0 > k:
+            lam = 0.9 * lam
+        c += 1
+    return X_ext
+
+
+def extra_points(prm: HSS2DParams, Tu0, Td0, J0, k0, X_ext, X_src, cB, lev, box):
+    """LOCAL_ID_rand_update (:1069-1124) with dense T, and the re-orientation of the NTI
+    branch (:468-487): a randomized ID of the interpolation residual
+    [K(X_ext, X_rs) - K(X_ext, X_sk) T_up; K(X_rs, X_ext).' - K(X_sk, X_ext).' T_dn]
+    (2p x n_rs, q0 = 8 layers ceil(log2 k0), C = q0/2, problem 2*box of the shared RNG)
+    promotes k1 residual points to skeletons; T = [T(:, J1_rs) - T(:, J1_sk) T1; T1].
+    (The reference's Res_apply stacks the full A_sk twice; only its transpose, which
+    splits A_sk correctly, enters the randomized ID.)  Returns (T_up, T_dn, J, k)."""
+    from . import cid, randid
+    kp = prm.kp
+    J0_sk, J0_rs = J0[:k0], J0[k0:]
+    Xrs, Xsk = X_src[J0_rs], X_src[J0_sk]
+    p = X_ext.shape[0]
+    A_rs = np.vstack([kernel_eval(X_ext, Xrs, kp), kernel_eval(Xrs, X_ext, kp).T])
+    A_sk = np.vstack([kernel_eval(X_ext, Xsk, kp), kernel_eval(Xsk, X_ext, kp).T])
+    Res = A_rs - np.vstack([A_sk[:p] @ Tu0, A_sk[p:] @ Td0])
+    q0 = 8 * prm.layers * math.ceil(math.log2(k0))
+    if np.iscomplexobj(Res):
+        T1, J1, k1 = cid.id_rand_complex(Res, q0, q0 // 2, prm.acc, prm.seed, 2 * box)
+    else:
+        T1, J1, k1 = randid.id_rand(Res, q0, q0 // 2, prm.acc, prm.seed, 2 * box)
+    J1_sk, J1_rs = J1[:k1], J1[k1:]
+    kf = k0 + k1
+    Jf = np.concatenate([J0_sk, J0_rs[J1]])
+    Tfu = np.vstack([Tu0[:, J1_rs] - Tu0[:, J1_sk] @ T1, T1])
+    Tfd = np.vstack([Td0[:, J1_rs] - Td0[:, J1_sk] @ T1, T1])
+    if lev % 2 == 0:
+        th = math.pi / 2 if (box + 1) % 2 == 0 else -math.pi / 2
+    else:
+        th = 0.0 if (box + 1) % 2 == 0 else -math.pi
+    Js = orient_skeleton(X_src[Jf[:kf]], cB, th)
+    return Tfu[Js], Tfd[Js], np.concatenate([Jf[:kf][Js], Jf[kf:]]), kf
 
 
 def id_box(prm: HSS2DParams, X_ext, X_src, box):
