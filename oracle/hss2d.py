@@ -350,7 +350,7 @@ def random_proxy(X_ext, n_skel, cB, colrad, rowrad, lev, prm: HSS2DParams):
 
 def extra_points(prm: HSS2DParams, Tu0, Td0, J0, k0, X_ext, X_src, cB, lev, box):
     """LOCAL_ID_rand_update (:1069-1124) with dense T, and the re-orientation of the NTI
-    branch (:468-487): a randomized ID of the interpolation residual
+    (:468-487) or TI (:516-528) branch: a randomized ID of the interpolation residual
     [K(X_ext, X_rs) - K(X_ext, X_sk) T_up; K(X_rs, X_ext).' - K(X_sk, X_ext).' T_dn]
     (2p x n_rs, q0 = 8 layers ceil(log2 k0), C = q0/2, problem 2*box of the shared RNG)
     promotes k1 residual points to skeletons; T = [T(:, J1_rs) - T(:, J1_sk) T1; T1].
@@ -376,10 +376,14 @@ def extra_points(prm: HSS2DParams, Tu0, Td0, J0, k0, X_ext, X_src, cB, lev, box)
     Tfd = np.vstack([Td0[:, J1_rs] - Td0[:, J1_sk] @ T1, T1])
     if lev % 2 == 0:
         th = math.pi / 2 if (box + 1) % 2 == 0 else -math.pi / 2
+        nrm, tan = 0, 1
     else:
         th = 0.0 if (box + 1) % 2 == 0 else -math.pi
+        nrm, tan = 1, 0
     Js = orient_skeleton(X_src[Jf[:kf]], cB, th)
-    return Tfu[Js], Tfd[Js], np.concatenate([Jf[:kf][Js], Jf[kf:]]), kf
+    # the translation-invariant branch (:520-528) also orders the residual points
+    Jr = orient_residual(X_src[Jf[kf:]], nrm, tan) if prm.transinv else np.arange(len(Jf) - kf)
+    return Tfu[np.ix_(Js, Jr)], Tfd[np.ix_(Js, Jr)], np.concatenate([Jf[:kf][Js], Jf[kf:][Jr]]), kf
 
 
 def id_box(prm: HSS2DParams, X_ext, X_src, box):

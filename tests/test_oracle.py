@@ -415,6 +415,12 @@ def test_hss2d_translation_invariant_oracle():
     assert np.abs(hss2d.kernel_matvec(prm, x, block=300) - f).max() <= 1e-12 * np.abs(f).max()
     assert np.linalg.norm(hss2d.apply_nsym(tree, blk, x) - f) <= 1e-9 * np.linalg.norm(f)
     assert np.linalg.norm(K @ hss2d.applyinv_nsym(tree, inv, f) - f) <= 1e-9 * np.linalg.norm(f)
+    # the paper test's case 5.3 settings: 'rand' proxies and extra skeleton points
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense", transinv=1,
+                            proxy_rule="rand", skel_extra_pts=1)
+    tree = hss2d.build_tree_nsym(prm)
+    inv = hss2d.invert_nsym(tree, prm, hss2d.compress_nsym(tree, prm))
+    assert np.linalg.norm(K @ hss2d.applyinv_nsym(tree, inv, f) - f) <= 1e-9 * np.linalg.norm(f)
 
 
 def test_gmres_restated():
