@@ -261,3 +261,15 @@ def id_rand_complex(A: np.ndarray, k0: int, C: int, tol: float, seed: int, probl
     Z = Y[:, :krank].T
     R, J = pivoted_qr_complex(Z)
     return id_fixed_complex(R, J, krank), J, krank
+
+
+def lrid_rand_complex(A: np.ndarray, k0: int, C: int, tol: float, seed: int, problem: int):
+    """T = LRID_rand(m, n, A, A.', 'norm', params) (Common/LRID_rand.m:20-39) for complex A:
+    A ~ U V.' with U = A(:, J(1:k)) and V(J, :) = [I T].'."""
+    m, n = A.shape
+    T, J, k = id_rand_complex(A, k0, C, tol, seed, problem)
+    U = A[:, J[:k]]
+    V = np.zeros((n, k), dtype=np.complex128)
+    V[J[:k], :] = np.eye(k)
+    V[J[k:], :] = T.T
+    return U, V

@@ -281,7 +281,10 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 else:
                     T_up[b], T_dn[b] = interpolation_dense(prm, Xp, X_sk, X_rs)
                     qlev = max(qlev, T_up[b].shape[1])
-                if prm.skel_extra_pts and b not in lowrank and len(Jb) - kb > 0:
+                if prm.skel_extra_pts and len(Jb) - kb > 0:
+                    # T = T.U T.V' is kept dense after the update (the reference keeps the
+                    # factors, :1111-1121; their product is this T)
+                    lowrank.pop(b, None)
                     T_up[b], T_dn[b], Jb, kb = extra_points(prm, T_up[b], T_dn[b], Jb, kb, Xp, X_src, cent[b],
                                                             lev, b)
                     Js[b], ks[b] = Jb, kb
@@ -412,8 +415,7 @@ def uses_lowrank(prm: HSS2DParams, lev: int, depth: int, k: int, nr: int) -> boo
     """LOCAL_Interpolation_Operators (HSS2D_build_tree_nsym.m:842-846): the low-rank T of
     INTERform 'lowrank' on levels above the leaves' parents with k < k_cut (the k >= k_cut
     branch, interpolation_operator_HSS, is the compressed-block path and is not built)."""
-    return (prm.INTERform == "lowrank" and prm.kp.flag != SL_H_2D and lev < depth - 1 and k < prm.k_cut and k > 0
-            and nr > 0)
+    return prm.INTERform == "lowrank" and lev < depth - 1 and k < prm.k_cut and k > 0 and nr > 0
 
 
 def sample_guess(q, lev, m, n, up: bool):
@@ -448,8 +450,13 @@ def interpolation_lowrank(prm: HSS2DParams, Xp, X_sk, X_rs, q, lev, box):
             A = kernel_eval(X_rs, Xp, kp).T        # p x nr; matvec K21.'*x
         m, n = A.shape
         k0, C = sample_guess(q, lev, m, n, up)
-        U, V = randid.lrid_rand(A, k0, C, prm.acc, prm.seed, 2 * box + (0 if up else 1))
-        out["U" + tag] = idecomp.lstsq_qr(K11, U)
+        if np.iscomplexobj(A):
+            from . import cid
+            U, V = cid.lrid_rand_complex(A, k0, C, prm.acc, prm.seed, 2 * box + (0 if up else 1))
+            out["U" + tag] = np.linalg.lstsq(K11, U, rcond=None)[0]
+        else:
+            U, V = randid.lrid_rand(A, k0, C, prm.acc, prm.seed, 2 * box + (0 if up else 1))
+            out["U" + tag] = idecomp.lstsq_qr(K11, U)
         out["V" + tag] = V
         out["k0" + tag] = k0
         out["C" + tag] = C
