@@ -36,7 +36,7 @@ DL_L_2D = 1
 SL_H_2D = 2
 FLAG_NAMES = {"SL_L_2D": SL_L_2D, "DL_L_2D": DL_L_2D, "SL_H_2D": SL_H_2D}
 
-MOD_GAUSS, MOD_BUMP, MOD_SQRT_BUMP = 0, 1, 2
+MOD_GAUSS, MOD_BUMP, MOD_SQRT_BUMP, MOD_GAUSS0 = 0, 1, 2, 3
 
 
 @dataclass
@@ -44,7 +44,8 @@ class Modulation:
     """``f(p) = 1 + alpha*exp(-isig*((px-x0)^2 + (py-y0)^2))``; alpha=0 means f=1.
 
     ``kind`` MOD_BUMP / MOD_SQRT_BUMP select Bump_function option 4 (shift 0) and the
-    square root of option 4 with shift 4h instead (Kernel_Eval.m:115-140)."""
+    square root of option 4 with shift 4h instead (Kernel_Eval.m:115-140); MOD_GAUSS0 is
+    ``alpha*exp(-isig*|p-p0|^2)`` without the constant (a Gaussian contrast)."""
 
     alpha: float = 0.0
     x0: float = 0.0
@@ -98,6 +99,12 @@ def _modulation(m: Modulation, px: np.ndarray, py: np.ndarray, h: float = 0.0) -
         return _bump4(px, py, 0.0)
     if m.kind == MOD_SQRT_BUMP:
         return np.sqrt(_bump4(px, py, 4 * h))
+    if m.kind == MOD_GAUSS0:
+        # alpha exp(-isig |p - p0|^2) without the constant term: the Gaussian contrast of the
+        # Lippmann-Schwinger configuration (its square root is the same kind, isig / 2)
+        d1 = px - m.x0
+        d2 = py - m.y0
+        return m.alpha * np.exp(-m.isig * (d1 * d1 + d2 * d2))
     if m.alpha == 0.0:
         return np.ones_like(px)
     d1 = px - m.x0

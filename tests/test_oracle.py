@@ -558,3 +558,30 @@ def test_reference_lippmann_schwinger_case():
     y = hss2d.applyinv_nsym(tree, inv, vec[:, None])[:, 0]
     assert np.linalg.norm(y_true - y) <= 1e-8
     assert np.linalg.norm(y_true - y) <= 1e-9 * np.linalg.norm(y_true)
+
+
+def test_lippmann_schwinger_configuration_shape():
+    """The Lippmann-Schwinger configuration's kernel at a small grid: kappa = 20, Gaussian
+    contrast exp(-|x|^2/0.1) taken symmetrically (its square root, exp(-|x|^2/0.2), on both
+    sides), leaf 8 x 8, tol 1e-10, the paper test's proxy and extra-point settings; GMRES
+    preconditioned by the complex64 HSS inverse reaches 1e-8."""
+    from oracle import drweights, krylov
+    Ng, npan, kh = 8, 4, 20.0
+    h = 2.0 / (Ng * npan)
+    _, w, _ = drweights.dr_stencil(h, kh, npan * Ng, 4)
+    sq = kernels.Modulation(alpha=1.0, isig=5.0, kind=kernels.MOD_GAUSS0)
+    kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=h, b=sq, c=sq, kh=kh, dr=complex(w[0]))
+    prm = hss2d.HSS2DParams(Ng=Ng, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="lowrank", proxy_rule="rand",
+                            skel_extra_pts=1)
+    tree = hss2d.build_tree_nsym(prm)
+    blk = hss2d.compress_nsym(tree, prm)
+    inv = hss2d.invert_nsym(tree, prm, blk)
+    X = prm.X_source()
+    K = kernels.kernel_eval(X, X, kp)
+    f = np.exp(-(X[:, 0] ** 2 + X[:, 1] ** 2) / 0.2) * np.exp(1j * kh * X[:, 0])
+    inv32 = {k: [None if a is None else a.astype(np.complex64) for a in v] for k, v in inv.items()}
+    M = lambda v: hss2d.applyinv_nsym(tree, inv32, v.astype(np.complex64)[:, None])[:, 0].astype(np.complex128)
+    x, rr, its = krylov.gmres(lambda v: K @ v, M, f, tol=1e-8)
+    assert rr <= 1e-8 and its <= 4
+    y = hss2d.apply_nsym(tree, blk, x[:, None])[:, 0]
+    assert np.linalg.norm(y - K @ x) <= 1e-9 * np.linalg.norm(K @ x)
