@@ -101,3 +101,13 @@ def test_block_submatrix_apply_composition(monkeypatch):
     A = np.block([[K[0].A[np.ix_(I_dn[0][0], I_up[0][0])], K[1].A[np.ix_(I_dn[0][1], I_up[0][1])]],
                   [K[2].A[np.ix_(I_dn[1][0], I_up[1][0])], K[3].A[np.ix_(I_dn[1][1], I_up[1][1])]]])
     assert np.abs(Y - A @ X).max() <= 1e-14
+
+
+def test_binding_constants_match_header():
+    """Every #define HSS_* of the header has the same value in the Python binding."""
+    from hssc_directsolver_gb300 import _lib
+    src = open(HEADER).read()
+    consts = dict(re.findall(r"^#define\s+(HSS_\w+)\s+(-?\d+)", src, flags=re.M))
+    assert len(consts) >= 15
+    for name, val in consts.items():
+        assert getattr(_lib, name) == int(val), name
