@@ -111,3 +111,31 @@ def test_binding_constants_match_header():
     assert len(consts) >= 15
     for name, val in consts.items():
         assert getattr(_lib, name) == int(val), name
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of hss_kernel_params and hss2d_params have the C layout: sizes and
+    every field offset, from a C program compiled against the header (needs a C compiler)."""
+    import shutil
+    import subprocess
+    from hssc_directsolver_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"hss_kernel_params": _lib.hss_kernel_params, "hss2d_params": _lib.hss2d_params}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hssgpu.h"', "int main(void) {"]
+    for sname, cls in structs.items():
+        lines.append(f'printf("{sname} size %zu\\n", sizeof({sname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{sname} {f} %zu\\n", offsetof({sname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for sname, cls in structs.items():
+        assert got[(sname, "size")] == C.sizeof(cls), sname
+        for f, _ in cls._fields_:
+            assert got[(sname, f)] == getattr(cls, f).offset, (sname, f)
