@@ -139,3 +139,15 @@ def test_struct_layouts_match_header(tmp_path):
         assert got[(sname, "size")] == C.sizeof(cls), sname
         for f, _ in cls._fields_:
             assert got[(sname, f)] == getattr(cls, f).offset, (sname, f)
+
+
+def test_binding_arity_matches_header():
+    """Each ctypes signature takes as many arguments as the header's prototype declares."""
+    from hssc_directsolver_gb300 import _lib
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    protos = dict(re.findall(r"\b(hss\w+)\s*\(([^)]*)\)\s*;", src))
+    assert protos
+    for name, params in protos.items():
+        params = params.strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(_lib.SIGNATURES[name][1]) == n, name
