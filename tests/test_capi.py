@@ -151,3 +151,24 @@ def test_binding_arity_matches_header():
         params = params.strip()
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(_lib.SIGNATURES[name][1]) == n, name
+
+
+def test_binding_argument_kinds_match_header():
+    """Position by position: pointers bind as pointers, and int32_t / int64_t / uint64_t /
+    double scalars as the same ctypes scalar."""
+    from hssc_directsolver_gb300 import _lib
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    protos = dict(re.findall(r"\b(hss\w+)\s*\(([^)]*)\)\s*;", src))
+    scalars = {"int32_t": C.c_int32, "int64_t": C.c_int64, "uint64_t": C.c_uint64, "double": C.c_double,
+               "float": C.c_float, "int": C.c_int}
+    ptr_types = (C.c_void_p, C.c_char_p)
+    for name, params in protos.items():
+        params = params.strip()
+        if params in ("", "void"):
+            continue
+        for i, (decl, ct) in enumerate(zip(params.split(","), _lib.SIGNATURES[name][1])):
+            if "*" in decl:
+                assert ct in ptr_types or issubclass(ct, C._Pointer), (name, i, decl)
+            else:
+                base = decl.replace("const", "").split()[0]
+                assert ct is scalars[base], (name, i, decl)
