@@ -401,6 +401,13 @@ def HSS1D_solve(K_HSS: HSS1DMatrix, ff, tol: float = 1e-10, maxit: int = 5):
     return (out[:, 0] if vec else out), rr.value, it.value
 
 
+# HSS1D_sum_fsym / HSS1D_compressLR_fsym (one ID per box for symmetric operands,
+# HSS1D/HSS1D_sum_fsym.m, HSS1D_compressLR_fsym.m): the nsym forms accept the same
+# operands and return matrices every call here takes (incoming and outgoing skeletons
+# kept separately).
+HSS1D_sum_fsym = HSS1D_sum_nsym
+HSS1D_compressLR_fsym = HSS1D_compressLR_nsym
+
 # fsym handles carry T_DN = T_UP; the nsym algorithms are the fsym ones on them
 # (HSS1D_invert_fsym.m:47-90 with E at :79, HSS1D_apply_fsym.m:1-118, HSS1D_applyinv_fsym.m:38-86)
 HSS1D_invert_fsym = HSS1D_invert_nsym
