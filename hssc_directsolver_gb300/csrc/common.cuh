@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <map>
 #include <atomic>
+#include <mutex>
 #include <exception>
 #include <thread>
 #include <cstdint>
@@ -186,6 +187,26 @@ inline void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&&
   }
   HSS_CUDA(cudaGraphLaunch(it->second, s));
 }
+
+// One-time setup per CUDA device (function attributes, which cudaFuncSetAttribute sets for
+// the current device only).  run() calls f() the first time it is reached with a given
+// device current; the flags are per device and guarded by a mutex, so several host threads
+// and several devices in one process each get the setup exactly once.
+struct PerDeviceOnce {
+  static constexpr int kMaxDevices = 256;
+  std::mutex mu;
+  bool done[kMaxDevices] = {};
+  template <typename F>
+  void run(F&& f) {
+    int dev = 0;
+    HSS_CUDA(cudaGetDevice(&dev));
+    HSS_REQUIRE(dev >= 0 && dev < kMaxDevices, HSS_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return;
+    f();
+    done[dev] = true;
+  }
+};
 
 // Host-side parallel loop over [0, n): chunks handed out dynamically to up to
 // hardware_concurrency() threads; the first exception of any chunk is rethrown.

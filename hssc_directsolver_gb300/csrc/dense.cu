@@ -1257,12 +1257,11 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool
   const int C = gj_cluster<R>(maxn, batch, rows_per);
   const size_t smem = (size_t)rows_per * GJ_NB * sizeof(R);
   HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "block too large for the cluster panel (n > 12800)");
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;  // per R instantiation; attributes are per device
+  attr_once.run([] {
     HSS_CUDA(cudaFuncSetAttribute(k_gj_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     HSS_CUDA(cudaFuncSetAttribute(k_gj_panel_cl<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    attr_set = true;
-  }
+  });
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(batch * C, 1, 1);
   cfg.blockDim = dim3(GJ_THREADS, 1, 1);
@@ -1749,12 +1748,11 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   const int cap = (maxm + C - 1) / C;
   const size_t smem = (size_t)cap * QR_NB * sizeof(R);
   HSS_REQUIRE(smem <= 200 * 1024, HSS_ERR_ARG, "least-squares panel too tall for the cluster (m > 12800)");
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;  // per R instantiation; attributes are per device
+  attr_once.run([] {
     HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    attr_set = true;
-  }
+  });
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(batch * C, 1, 1);
   cfg.blockDim = dim3(QR_THREADS, 1, 1);

@@ -43,6 +43,10 @@ HelmDev make_helm_dev(const hss_kernel_params& kp) {
   const double q = (kp.kh * kp.kh) * 0.25;
   k.w_re = 1.0 - q * kp.dr_im;
   k.w_im = q * kp.dr_re;
+  for (int j = 0; j <= kHankelNodes; ++j) {
+    const double sj = j * kHankelStep;
+    k.hw[j] = 2.0 * std::exp(-sj * sj);
+  }
   return k;
 }
 
@@ -126,11 +130,9 @@ __global__ void __launch_bounds__(256) k_kgen(const KgenP<R>* __restrict__ D, Po
 //  this analytic integrand (Trefethen & Weideman, SIAM Review 56, 2014).  The factor
 //  (1 + i v)^(-1/2) = r^(-1/2) (cos(t/2) - i sin(t/2)), r = |1 + i v|, t = arg(1 + i v),
 //  with sin(t/2) = (v / r) / (2 cos(t/2)) to avoid cancellation at small v.
-constexpr int kHankelNodes = 21;
-constexpr double kHankelStep = 0.3;
-__constant__ double c_hankel_w[kHankelNodes + 1];  // 2 exp(-(j step)^2), j = 0..21 (j = 0 unused)
-
-__device__ __forceinline__ void hankel0(double x, double& J, double& Y) {
+// hw: the trapezoid weights 2 exp(-(j step)^2) (HelmDev::hw), indexed with constants only
+// (the loop below is unrolled) so they stay in the parameter bank.
+__device__ __forceinline__ void hankel0(double x, const double (&hw)[kHankelNodes + 1], double& J, double& Y) {
   constexpr double kGamma = 0.57721566490153286061, kTwoOverPi = 0.63661977236758134308;
   if (x < 3.5) {
     const double q = 0.25 * x * x;
@@ -148,7 +150,7 @@ __device__ __forceinline__ void hankel0(double x, double& J, double& Y) {
   }
   double ir = 1.0, ii = 0.0;
   const double i2x = 0.5 / x;
-#pragma unroll 3
+#pragma unroll
   for (int k = 1; k <= kHankelNodes; ++k) {
     const double sk = k * kHankelStep;
     const double v = sk * sk * i2x;
@@ -156,8 +158,8 @@ __device__ __forceinline__ void hankel0(double x, double& J, double& Y) {
     const double ch = sqrt(0.5 * (1.0 + 1.0 / r));
     const double sh = (v / r) / (2.0 * ch);
     const double rs = 1.0 / sqrt(r);
-    ir += c_hankel_w[k] * (ch * rs);
-    ii -= c_hankel_w[k] * (sh * rs);
+    ir += hw[k] * (ch * rs);
+    ii -= hw[k] * (sh * rs);
   }
   const double norm = kHankelStep * 0.56418958354775628695;  // step / sqrt(pi)
   ir *= norm;
@@ -169,18 +171,6 @@ __device__ __forceinline__ void hankel0(double x, double& J, double& Y) {
   const double f = sqrt(kTwoOverPi / x);
   J = f * (c * ir - sn * ii);
   Y = f * (c * ii + sn * ir);
-}
-
-static void upload_hankel_weights() {
-  static bool done = false;
-  if (done) return;
-  double w[kHankelNodes + 1];
-  for (int k = 0; k <= kHankelNodes; ++k) {
-    const double sk = k * kHankelStep;
-    w[k] = 2.0 * std::exp(-sk * sk);
-  }
-  HSS_CUDA(cudaMemcpyToSymbol(c_hankel_w, w, sizeof(w)));
-  done = true;
 }
 
 // Helmholtz entry (Kernel_Eval.m:44-49): w on the diagonal, else
@@ -203,7 +193,7 @@ __global__ void __launch_bounds__(256) k_kgen_complex(const KgenCP* __restrict__
       const double x = __dmul_rn(k.kh, sqrt(den));
       const double sb = __dmul_rn(k.s, P.bval[t]);
       double hj, hy;
-      hankel0(x, hj, hy);
+      hankel0(x, k.hw, hj, hy);
       re = -__dmul_rn(__dmul_rn(sb, hy), P.cval[s]);
       im = __dmul_rn(__dmul_rn(sb, hj), P.cval[s]);
     }
@@ -217,7 +207,6 @@ void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, con
                           const HelmDev& k, cudaStream_t s) {
   if (batch <= 0 || maxEntries <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "kgen batch too large");
-  upload_hankel_weights();
   const int gx = std::max(1, std::min(ceil_div(maxEntries, 256), 4096));
   k_kgen_complex<<<dim3(gx, batch), 256, 0, s>>>(dP, pts, k);
   check_launch("k_kgen_complex");

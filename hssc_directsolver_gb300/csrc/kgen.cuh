@@ -57,8 +57,14 @@ struct KgenCP {
 };
 // Helmholtz constants: s = h^2 kh^2 / 4 (the imaginary factor of the off-diagonal
 // entries), w = 1 + kh^2 (i/4) dr (the diagonal)
+// and the weights 2 exp(-(j 0.3)^2), j = 0..21, of the Hankel-integral trapezoid rule
+// (j = 0 unused).  The weights travel in the kernel parameters, so no per-device state
+// has to be uploaded before a launch.
+constexpr int kHankelNodes = 21;
+constexpr double kHankelStep = 0.3;
 struct HelmDev {
   double kh, s, w_re, w_im;
+  double hw[kHankelNodes + 1];
 };
 HelmDev make_helm_dev(const hss_kernel_params& kp);
 void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, const PointView& pts,

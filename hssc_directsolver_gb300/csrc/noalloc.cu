@@ -21,6 +21,10 @@
 //    zero, are cleared by each call.
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; later calls reuse it.
+//    That first call may also load this library's device code on the device
+//    (CUDA loads modules lazily), so make it before any stream capture.  A
+//    cudaDeviceReset destroys the array with the context: the cached address is
+//    then stale, so do not use this entry point after resetting a device.
 #include <mutex>
 
 #include "dense.cuh"

@@ -357,7 +357,8 @@ int hss_batched_inverse_device_f32(float* d_A, int32_t n, int32_t batch, int32_t
  * scratch comes from one fixed 16 MiB array in device global memory (held by
  * every GPU that loads the library): batch <= 256 and
  * batch*(n*n + 64*n)*8 + batch*(n + 132)*4 bytes plus descriptors must fit, else
- * HSS_ERR_ARG.  The first call on a device resolves the array's address there.
+ * HSS_ERR_ARG.  The first call on a device resolves the array's address there
+ * (make it before any stream capture); a cudaDeviceReset invalidates that address.
  * Calls share the array: overlapping calls on the GPU race and must be ordered
  * by the caller.  d_info is cleared by each call. */
 int hss_batched_inverse_noalloc_device(double* d_A, int32_t n, int32_t batch, int32_t* d_info,

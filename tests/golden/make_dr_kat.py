@@ -1,6 +1,6 @@
 """Extract the Duan-Rokhlin known-answer output published with the reference.
 
-    python tests/golden/make_dr_kat.py [path/to/HSSC_DirectSolver]
+    python tests/golden/make_dr_kat.py path/to/HSSC_DirectSolver
 
 The reference's INSTALL.txt (lines 95-115) lists the indata.txt / outdata.txt pair of
 its Fortran weight program (Common/FORTRAN_get_DR_weights.f): h, the wavenumber and
@@ -32,7 +32,9 @@ def parse(text: str) -> dict:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/HSSC_DirectSolver"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_dr_kat.py <HSSC_DirectSolver source directory (the one holding INSTALL.txt)>")
+    ref = sys.argv[1]
     kat = parse(open(os.path.join(ref, "INSTALL.txt")).read())
     kat["source"] = "HSSC_DirectSolver/INSTALL.txt:95-115 (outdata.txt of FORTRAN_get_DR_weights)"
     with open(os.path.join(HERE, "dr_weights_kat.json"), "w") as f:
