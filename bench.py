@@ -408,8 +408,10 @@ def main():
                     help="skip the CPU oracle's compress+invert (about a minute at the full workload)")
     ap.add_argument("--config5", action="store_true",
                     help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
-    ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv",
-                    help="solve paths to measure (comma list of fp64, mixed, dfloat, dfloat_inv)")
+    ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv,tc",
+                    help="solve paths to measure (comma list of fp64, mixed, dfloat, dfloat_inv, tc)")
+    ap.add_argument("--no-kernel-residual", action="store_true",
+                    help="skip the FP64 residual against the kernel matrix itself (~0.5 s per path)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -522,7 +524,12 @@ def main():
                                         C.byref(it2)))
         barrier()
         e2e_s = max_over_ranks((time.perf_counter() - te0) / args.steps)
-        results[prec] = dict(compress_invert_s=ci, tree_s=t1 - t0, compress_s=t2 - t1, invert_s=t3 - t2,
+        # the solution's residual against the kernel matrix itself (generated on the fly in
+        # FP64, never formed), outside the timed region
+        kres = None
+        if not args.no_kernel_residual:
+            kres = G2.HSS2D_kernel_residual(tree, F, np.asfortranarray(Xh))
+        results[prec] = dict(kernel_relres=kres, compress_invert_s=ci, tree_s=t1 - t0, compress_s=t2 - t1, invert_s=t3 - t2,
                              solve_ms=ms, relres=rr.value, solves_used=it.value, applyinv_ms=inv_ms,
                              apply_ms=fwd_ms,
                              solve_bytes=tree.solve_bytes(), launches=tree.solve_launches(dF.shape[0]),
@@ -562,7 +569,9 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["solve_ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": {"mixed": "f32+f64", "dfloat": "f64 (products as f32 pairs)",
-                  "dfloat_inv": "f64 (products and inversion as f32 pairs)"}.get(best, "f64"),
+                  "dfloat_inv": "f64 (products and inversion as f32 pairs)",
+                  "tc": "f64 (inverse-apply products as bf16 digit slices on tensor cores, exact fp32 "
+                        "accumulation)"}.get(best, "f64"),
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nrhs": nrhs, "path": best, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (factors %.2f GB per solve)" % (r["solve_bytes"] / 1e9)},
@@ -570,6 +579,7 @@ def main():
         "stages_s": {p: {k: results[p][k] for k in ("tree_s", "compress_s", "invert_s")} for p in results},
         "solves_per_s": {p: 1e3 / results[p]["solve_ms"] for p in results},
         "relres": {p: results[p]["relres"] for p in results},
+        "kernel_relres": {p: results[p]["kernel_relres"] for p in results},
         "solves_used": {p: results[p]["solves_used"] for p in results},
         "applyinv_ms": {p: results[p]["applyinv_ms"] for p in results},
         "apply_fp64_ms": {p: results[p]["apply_ms"] for p in results},
@@ -578,7 +588,7 @@ def main():
                 "host_buffers": "pinned", "call": "hss2d_solve"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_PER_APPLYINV.get(best),
-                     "kernel": {"dfloat": "k_skinny_df", "dfloat_inv": "k_skinny_df",
+                     "kernel": {"dfloat": "k_skinny_df", "dfloat_inv": "k_skinny_df", "tc": "k_skinny_tc",
                                 "mixed": "k_skinny<float>"}.get(best, "k_skinny<double>")
                                + " chain of one inverse apply",
                      "peak_source": peak_src,

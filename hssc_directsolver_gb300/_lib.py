@@ -36,6 +36,7 @@ HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_PREC_DFLOAT = 2
 HSS_PREC_DFLOAT_INV = 3
+HSS_PREC_TC = 4
 HSS_INTER_DENSE = 0
 HSS_INTER_LOWRANK = 1
 
@@ -148,6 +149,9 @@ SIGNATURES = {
     "hss_batched_id_device": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
                                         C.c_int32, _P, _P, _P, _P]),
     "hss_batched_gemm_device": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "hss_batched_gemv_tc_device": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "hss2d_kernel_residual": (C.c_int, [_P, _P, _P, C.c_int32, _P]),
+    "hss1d_kernel_residual": (C.c_int, [_P, _P, _P, C.c_int32, _P]),
 }
 
 _lib = None

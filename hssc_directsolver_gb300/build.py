@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libhssgpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["dense.cu", "kgen.cu", "hss2d.cu", "hss1d.cu", "hss1d_algebra.cu", "capi.cu", "noalloc.cu", "mlp.cu", "hss2d_lowrank.cu", "krylov.cu", "hss2d_tree.cpp", "drweights.cpp"]
+SOURCES = ["dense.cu", "skinny_tc.cu", "kgen.cu", "hss2d.cu", "hss1d.cu", "hss1d_algebra.cu", "capi.cu", "noalloc.cu", "mlp.cu", "hss2d_lowrank.cu", "krylov.cu", "hss2d_tree.cpp", "drweights.cpp"]
 
 
 def nvcc() -> str:

@@ -146,6 +146,48 @@ int hss_kernel_eval_device(const hss_kernel_params* kp, const double* d_X1, int6
   HSS_CATCH
 }
 
+// max over columns of ||f - u|| / ||f|| (host vectors, N x nrhs column-major)
+static double host_relres(const double* f, const double* u, long long N, int nrhs) {
+  double worst = 0.0;
+  for (int c = 0; c < nrhs; ++c) {
+    long double a = 0.0L, b = 0.0L;
+    for (long long i = 0; i < N; ++i) {
+      const long double fv = f[i + c * N], rv = fv - (long double)u[i + c * N];
+      a += rv * rv;
+      b += fv * fv;
+    }
+    const double rel = (b > 0.0L) ? (double)std::sqrt(a / b) : (double)std::sqrt(a);
+    HSS_REQUIRE(std::isfinite(rel), HSS_ERR_NONFINITE, "non-finite kernel residual");
+    worst = std::max(worst, rel);
+  }
+  return worst;
+}
+
+// u = K x on the device for the problems of a point table (one KmvP per problem), host x and u
+static void kernel_matvec_host(const PointTable& pts, const KernelDev& kd, const std::vector<KmvP>& probs0,
+                               long long Nrows, const double* x, double* u, int nrhs, cudaStream_t s) {
+  DevBuf<double> dx((size_t)Nrows * nrhs), du((size_t)Nrows * nrhs), part;
+  HSS_CUDA(cudaMemcpyAsync(dx.p, x, (size_t)Nrows * nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
+  int maxM = 0, maxN = 0;
+  for (auto& p : probs0) { maxM = std::max(maxM, p.m); maxN = std::max(maxN, p.n); }
+  DevBuf<KmvP> dP(probs0.size());
+  for (int c0 = 0; c0 < nrhs; c0 += 8) {
+    const int r = std::min(8, nrhs - c0);
+    std::vector<KmvP> P = probs0;
+    for (auto& p : P) {
+      p.q = dx.p + (size_t)c0 * Nrows + p.s0;
+      p.ldq = (int)Nrows;
+      p.u = du.p + (size_t)c0 * Nrows + p.t0;
+      p.ldu = (int)Nrows;
+    }
+    HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), P.size() * sizeof(KmvP), cudaMemcpyHostToDevice, s));
+    kernel_matvec(dP.p, (int)P.size(), maxM, maxN, r, view(pts), kd, part, s);
+    HSS_CUDA(cudaStreamSynchronize(s));
+  }
+  HSS_CUDA(cudaMemcpyAsync(u, du.p, (size_t)Nrows * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
 int hss_dr_corrections(double h, double k_re, double k_im, double* corr) {
   HSS_TRY
   HSS_REQUIRE(corr != nullptr, HSS_ERR_ARG, "corr is NULL");
@@ -724,7 +766,7 @@ int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p) {
   HSS_REQUIRE(p->transinv == 0 || (p->kp.b_alpha == 0.0 && p->kp.c_alpha == 0.0), HSS_ERR_ARG,
               "translation-invariant mode needs an unmodulated kernel (b = c = 1)");
   HSS_REQUIRE(p->precision == HSS_PREC_FP64 || p->precision == HSS_PREC_MIXED || p->precision == HSS_PREC_DFLOAT ||
-                  p->precision == HSS_PREC_DFLOAT_INV,
+                  p->precision == HSS_PREC_DFLOAT_INV || p->precision == HSS_PREC_TC,
               HSS_ERR_ARG, "bad precision");
   require_device();
   *out = nullptr;
@@ -1042,6 +1084,82 @@ int hss_batched_gemm_device(const double* d_A, const double* d_B, double* d_C, i
   if (N <= 8) gemm_skinny<double>(dP.p, batch, M, 1.0, 0.0, s);
   else gemm_batched<double>(dP.p, batch, M, N, false, false, 1.0, 0.0, s);
   HSS_CUDA(cudaStreamSynchronize(s));
+  HSS_CATCH
+}
+
+int hss_batched_gemv_tc_device(const double* d_A, const double* d_B, double* d_C, int32_t M, int32_t N, int32_t K,
+                               int32_t batch, void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(d_A && d_B && d_C && M > 0 && N >= 1 && N <= TC_NR && K > 0 && batch > 0 && batch <= 65535,
+              HSS_ERR_ARG, "tensor-core product: 1..4 columns and a positive size");
+  cudaStream_t s = as_stream(stream);
+  const size_t pb = tc_packed_bytes(M, K);
+  DevBuf<unsigned char> packed(pb * batch);
+  DevBuf<int> rexp((size_t)M * batch), err(1);
+  err.zero(s);
+  std::vector<TcPackP> P(batch);
+  std::vector<TcProd> Q(batch);
+  for (int b = 0; b < batch; ++b) {
+    TcPackP q{};
+    q.A[0] = d_A + (size_t)b * M * K;
+    q.K[0] = K;
+    q.lda[0] = M;
+    q.sign[0] = 1.0;
+    q.M = M;
+    q.out = packed.p + pb * b;
+    q.rexp = rexp.p + (size_t)b * M;
+    P[b] = q;
+    TcProd t{};
+    t.A = q.out;
+    t.rexp = q.rexp;
+    t.B[0] = d_B + (size_t)b * K * N;
+    t.K[0] = K;
+    t.ldb[0] = K;
+    t.C = d_C + (size_t)b * M * N;
+    t.ldc = M;
+    t.M = M;
+    t.r = N;
+    Q[b] = t;
+  }
+  DevBuf<TcPackP> dP(batch);
+  HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(TcPackP), cudaMemcpyHostToDevice, s));
+  tc_pack(dP.p, batch, M, K, s);
+  TcStep st;
+  st.build(Q, 1.0, 0.0, err.p, s);
+  st.run(s);
+  int herr = 0;
+  HSS_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HSS_CUDA(cudaStreamSynchronize(s));
+  HSS_REQUIRE(herr == 0, HSS_ERR_CUDA, "tensor-core product: a pipeline wait timed out");
+  HSS_CATCH
+}
+
+int hss2d_kernel_residual(hss2d_matrix* H, const double* f, const double* x, int32_t nrhs, double* relres) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && f && x && relres && nrhs >= 1, HSS_ERR_ARG, "kernel residual: bad arguments");
+  auto* h = H->impl;
+  HSS_REQUIRE(h->tree_built, HSS_ERR_STATE, "kernel residual before the tree is built");
+  const long long N = h->geo.N;
+  std::vector<double> u((size_t)N * nrhs);
+  kernel_matvec_host(h->pts, h->kdev, {KmvP{0, (int)N, 0, (int)N, nullptr, 0, nullptr, 0}}, N, x, u.data(), nrhs,
+                     h->stream);
+  *relres = host_relres(f, u.data(), N, nrhs);
+  HSS_CATCH
+}
+
+int hss1d_kernel_residual(hss1d_matrix* H, const double* f, const double* x, int32_t nrhs, double* relres) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && f && x && relres && nrhs >= 1, HSS_ERR_ARG, "kernel residual: bad arguments");
+  auto* h = H->impl;
+  HSS_REQUIRE(!h->rect, HSS_ERR_ARG, "kernel residual: square handles only");
+  HSS_REQUIRE(h->kernel_op && (h->kdev.flag == HSS_SL_L_2D || h->kdev.flag == HSS_DL_L_2D), HSS_ERR_ARG,
+              "kernel residual: the handle holds no kernel matrix of its points (a low-rank or algebra result)");
+  std::vector<KmvP> P;
+  for (size_t p = 0; p < h->pN.size(); ++p)
+    P.push_back(KmvP{(int)h->pbase[p], (int)h->pN[p], (int)h->pbase[p], (int)h->pN[p], nullptr, 0, nullptr, 0});
+  std::vector<double> u((size_t)h->Ntot * nrhs);
+  kernel_matvec_host(h->pts, h->kdev, P, h->Ntot, x, u.data(), nrhs, h->stream);
+  *relres = host_relres(f, u.data(), h->Ntot, nrhs);
   HSS_CATCH
 }
 

@@ -214,6 +214,7 @@ HSS1D::~HSS1D() {
 void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, const long long* ldx, int leaf_,
                      double acc_, const hss_kernel_params& kp_, const unsigned long long* seeds, MLP* mlp,
                      bool sym_) {
+  kernel_op = true;
   HSS_REQUIRE(np_ >= 1 && Np && Xp && ldx && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
   HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
   using clk = std::chrono::steady_clock;

@@ -85,6 +85,7 @@ __global__ void k_scale(double* __restrict__ p, long long n, double c) {
 // c * A: the leaf self blocks and the sibling blocks scale, the interpolation matrices
 // do not (HSS1D_scalarmult.m:19-33).  The inverse factors no longer apply.
 void HSS1D::scalarmult(double c) {
+  kernel_op = false;  // c K is no longer the kernel matrix of the points
   HSS_REQUIRE(std::isfinite(c), HSS_ERR_ARG, "scalarmult: c must be finite");
   for (DevBuf<double>* b : {&M_SELF, &M_SIB}) {
     if (b->n == 0) continue;

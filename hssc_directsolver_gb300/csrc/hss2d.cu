@@ -268,6 +268,7 @@ void SolvePlan<R>::run_step(const Step& st, cudaStream_t s) const {
 template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
   for (auto& st : steps) run_step(st, s);
+  for (auto& st : tc_steps) st.run(s);
 }
 
 // The steps run on the plan's own buffers: a step's output is rewritten by the next real
@@ -615,12 +616,81 @@ void HSS2D::make_df_inverse() {
   HSS_CUDA(cudaStreamSynchronize(stream));
 }
 
+// Digit slices of the FP64 inverse factors for the tensor-core inverse apply: per factor
+// box, U (k x n) for the upward products and [FI, -G, GE] (n x (n + 2k); FI alone at the
+// root) for the downward ones, in the order the solve plan reads them.
+void HSS2D::make_tc_inverse() {
+  for (int lev = 0; lev <= geo.depth; ++lev) {
+    const auto& g = geo.levels[lev];
+    auto& d = L[lev];
+    const int nbf = nf(g);
+    std::vector<TcPackP> P;
+    if (lev > 0) {
+      d.tcU_box = tc_packed_bytes(g.k, g.n);
+      d.tcU.alloc(d.tcU_box * nbf);
+      d.tcUe.alloc((size_t)g.k * nbf);
+      for (int i = 0; i < nbf; ++i) {
+        TcPackP q{};
+        q.A[0] = d.fd[2].p + (size_t)i * g.k * g.n;
+        q.K[0] = g.n;
+        q.lda[0] = g.k;
+        q.sign[0] = 1.0;
+        q.M = g.k;
+        q.out = d.tcU.p + d.tcU_box * i;
+        q.rexp = d.tcUe.p + (size_t)i * g.k;
+        P.push_back(q);
+      }
+    }
+    const int Kd = (lev > 0) ? g.n + 2 * g.k : g.n;
+    d.tcD_box = tc_packed_bytes(g.n, Kd);
+    d.tcD.alloc(d.tcD_box * nbf);
+    d.tcDe.alloc((size_t)g.n * nbf);
+    for (int i = 0; i < nbf; ++i) {
+      TcPackP q{};
+      q.A[0] = d.fd[0].p + (size_t)i * g.n * g.n;
+      q.K[0] = g.n;
+      q.lda[0] = g.n;
+      q.sign[0] = 1.0;
+      if (lev > 0) {
+        q.A[1] = d.fd[3].p + (size_t)i * g.n * g.k;
+        q.K[1] = g.k;
+        q.lda[1] = g.n;
+        q.sign[1] = -1.0;
+        q.A[2] = d.fd[4].p + (size_t)i * g.n * g.k;
+        q.K[2] = g.k;
+        q.lda[2] = g.n;
+        q.sign[2] = 1.0;
+      }
+      q.M = g.n;
+      q.out = d.tcD.p + d.tcD_box * i;
+      q.rexp = d.tcDe.p + (size_t)i * g.n;
+      P.push_back(q);
+    }
+    int maxM = 0, maxK = 0;
+    for (auto& q : P) {
+      maxM = std::max(maxM, q.M);
+      maxK = std::max(maxK, q.K[0] + q.K[1] + q.K[2]);
+    }
+    DevBuf<TcPackP> dP(P.size());
+    HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), P.size() * sizeof(TcPackP), cudaMemcpyHostToDevice, stream));
+    tc_pack(dP.p, (int)P.size(), maxM, maxK, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+}
+
 void HSS2D::invert() {
   HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_invert before hss2d_compress");
+  if (tcm() && !tc_err.p) {
+    tc_err.alloc(1);
+    tc_err.zero(stream);
+    HSS_CUDA(cudaMallocHost(&tc_err_host, sizeof(int)));
+    *tc_err_host = 0;
+  }
   const auto ti0 = std::chrono::steady_clock::now();
   if (prm.precision == HSS_PREC_MIXED) invert_impl<float>();
   else invert_impl<double>();
-  if (dfm()) make_df_inverse();
+  if (tcm()) make_tc_inverse();
+  else if (dfm()) make_df_inverse();
   HSS_CUDA(cudaStreamSynchronize(stream));
   phase_s[4] = std::chrono::duration<double>(std::chrono::steady_clock::now() - ti0).count();
   inverted = true;
@@ -672,6 +742,83 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
     }
     (void)g;
   };
+  if constexpr (std::is_same<R, double>::value) {
+    if (tcm()) {
+      // tensor-core products over the digit slices; at most 4 columns per product
+      auto outptr = [&](int lev, int i, double*& ptr, int& ld) {
+        if (lev == depth) {
+          const int b = (1 << lev) - 1 + i;
+          ptr = vout.p + (size_t)NG * geo.leaf_panel[b];
+          ld = (int)N;
+        } else {
+          const auto& gc = geo.levels[lev + 1];
+          ptr = L[lev + 1].vec<double>(1).p + (size_t)(2 * i) * gc.k;
+          ld = gc.nb * gc.k;
+        }
+      };
+      for (int lev = depth; lev >= 1; --lev) {
+        const auto& g = geo.levels[lev];
+        auto& d = L[lev];
+        std::vector<TcProd> P;
+        for (int c0 = 0; c0 < r; c0 += TC_NR)
+          for (int i = 0; i < g.nb; ++i) {
+            const double* q;
+            int ldq;
+            qptr(lev, i, q, ldq);
+            TcProd t{};
+            t.A = d.tcU.p + d.tcU_box * fo(i);
+            t.rexp = d.tcUe.p + (size_t)fo(i) * g.k;
+            t.B[0] = q + (size_t)c0 * ldq;
+            t.K[0] = g.n;
+            t.ldb[0] = ldq;
+            t.C = d.vec<double>(0).p + (size_t)i * g.k + (size_t)c0 * g.nb * g.k;
+            t.ldc = g.nb * g.k;
+            t.M = g.k;
+            t.r = std::min(TC_NR, r - c0);
+            P.push_back(t);
+          }
+        pl.tc_steps.emplace_back();
+        pl.tc_steps.back().build(P, 1.0, 0.0, tc_err.p, stream);
+      }
+      for (int lev = 0; lev <= depth; ++lev) {
+        const auto& g = geo.levels[lev];
+        auto& d = L[lev];
+        std::vector<TcProd> P;
+        for (int c0 = 0; c0 < r; c0 += TC_NR)
+          for (int i = 0; i < g.nb; ++i) {
+            const double* q;
+            int ldq;
+            qptr(lev, i, q, ldq);
+            double* out;
+            int ldo;
+            outptr(lev, i, out, ldo);
+            TcProd t{};
+            t.A = d.tcD.p + d.tcD_box * fo(i);
+            t.rexp = d.tcDe.p + (size_t)fo(i) * g.n;
+            t.B[0] = q + (size_t)c0 * ldq;
+            t.K[0] = g.n;
+            t.ldb[0] = ldq;
+            if (lev > 0) {
+              t.B[1] = d.vec<double>(0).p + (size_t)i * g.k + (size_t)c0 * g.nb * g.k;
+              t.K[1] = g.k;
+              t.ldb[1] = g.nb * g.k;
+              t.B[2] = d.vec<double>(1).p + (size_t)i * g.k + (size_t)c0 * g.nb * g.k;
+              t.K[2] = g.k;
+              t.ldb[2] = g.nb * g.k;
+            }
+            t.C = out + (size_t)c0 * ldo;
+            t.ldc = ldo;
+            t.M = g.n;
+            t.r = std::min(TC_NR, r - c0);
+            P.push_back(t);
+          }
+        pl.tc_steps.emplace_back();
+        pl.tc_steps.back().build(P, 1.0, 0.0, tc_err.p, stream);
+      }
+      HSS_CUDA(cudaStreamSynchronize(stream));
+      return pl;
+    }
+  }
   // upward pass
   for (int lev = depth; lev >= 1; --lev) {
     const auto& g = geo.levels[lev];
@@ -975,7 +1122,10 @@ void HSS2D::solve_device(const double* df, double* dx, int nrhs, double tol, int
       k_residual<<<gx, 256, 0, stream>>>(N, r, f, N, Yd.p, N, Rd.p, N, part_d);
       HSS_CUDA(cudaMemcpyAsync(ir_host.p, part_d, (size_t)gx * r * 2 * sizeof(double), cudaMemcpyDeviceToHost,
                                stream));
+      if (tcm()) HSS_CUDA(cudaMemcpyAsync(tc_err_host, tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
       HSS_CUDA(cudaStreamSynchronize(stream));
+      HSS_REQUIRE(!tcm() || *tc_err_host == 0, HSS_ERR_CUDA,
+                  "tensor-core product: a pipeline wait timed out (results invalid)");
       worst = 0.0;
       for (int c = 0; c < r; ++c) {
         double a = 0.0, b = 0.0;
@@ -1040,6 +1190,7 @@ HSS2D::~HSS2D() {
   g_inv_f.clear();
   g_fwd.clear();
   L.clear();
+  if (tc_err_host) cudaFreeHost(tc_err_host);
   if (ev) cudaEventDestroy(ev);
   if (stream) cudaStreamDestroy(stream);
 }

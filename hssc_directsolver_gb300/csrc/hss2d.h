@@ -8,6 +8,7 @@
 #include "dense.cuh"
 #include "hss2d_tree.h"
 #include "kgen.cuh"
+#include "skinny_tc.cuh"
 
 namespace hss {
 
@@ -23,6 +24,7 @@ struct SolvePlan {
     R alpha = R(1), beta = R(0);
   };
   std::vector<Step> steps;
+  std::vector<TcStep> tc_steps;  // tensor-core products (HSS_PREC_TC inverse applies)
   bool df = false;  // FP64 operands stored as float pairs, products on the FP32 pipes
   void run_step(const Step& st, cudaStream_t s) const;
   // time each step at K-split counts around the heuristic's and keep the fastest
@@ -35,6 +37,7 @@ struct SolvePlan {
   int launches() const {
     int n = 0;
     for (auto& st : steps) n += (st.ksplit > 1) ? 2 : 1;
+    for (auto& st : tc_steps) n += st.launches();
     return n;
   }
 };
@@ -51,6 +54,11 @@ struct Level2Dev {
   // HSS_PREC_DFLOAT: the same FP64 factors and forward blocks as float pairs (8 bytes each)
   DevBuf<double> fdf[5];
   DevBuf<double> Tup_df, TdnT_df, Bself_df, B12_df, B21_df;
+  // HSS_PREC_TC: bf16 digit slices (tc_pack) of U (upward products) and of
+  // [FI, -G, GE] (downward products, FI alone at the root), per factor box, with row exponents
+  DevBuf<unsigned char> tcU, tcD;
+  DevBuf<int> tcUe, tcDe;
+  size_t tcU_box = 0, tcD_box = 0;  // packed bytes per factor box
   // inverse-apply vectors: 0 phi_up, 1 phi_dn (nb*k x 8)
   DevBuf<double> vd[2];
   DevBuf<float> vf[2];
@@ -100,8 +108,13 @@ struct HSS2D {
   // forward apply of the refinement always in these modes)
   bool dfm() const {
     return prm.precision == HSS_PREC_DFLOAT || prm.precision == HSS_PREC_DFLOAT_INV ||
-           prm.precision == HSS_PREC_MIXED;
+           prm.precision == HSS_PREC_MIXED || prm.precision == HSS_PREC_TC;
   }
+  // inverse apply on the tensor cores over digit slices of the FP64 factors
+  bool tcm() const { return prm.precision == HSS_PREC_TC; }
+  void make_tc_inverse();
+  DevBuf<int> tc_err;           // error word of the tensor-core products (0: none)
+  int* tc_err_host = nullptr;   // pinned copy, read with the refinement's residual
   // double-float Gauss-Jordan updates of the block inverses
   bool dfinv() const { return prm.precision == HSS_PREC_DFLOAT_INV; }
   // double-float products of the inversion (E, U, G, GE)

@@ -222,6 +222,85 @@ void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const Poi
   check_launch("k_kgen");
 }
 
+// One thread per target; the target's data and h^2/2 b(x) are held in registers, every
+// entry is formed with kernel_entry's operations in kernel_entry's order.
+template <int NR>
+__global__ void __launch_bounds__(256) k_kmatvec(const KmvP* __restrict__ D, PointView P, KernelDev k, int nsplit,
+                                                 double* __restrict__ part, int mmax, int nrhs) {
+  const KmvP d = D[blockIdx.z];
+  if ((int)blockIdx.x * 256 >= d.m) return;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  const int per = (d.n + nsplit - 1) / nsplit;
+  const int jb = blockIdx.y * per, je = min(d.n, jb + per);
+  double acc[NR];
+#pragma unroll
+  for (int c = 0; c < NR; ++c) acc[c] = 0.0;
+  if (i < d.m) {
+    const int t = d.t0 + i;
+    const double tx = P.x[t], ty = P.y[t];
+    const double hb = __dmul_rn(k.h2half, P.bval[t]);
+    for (int j = jb; j < je; ++j) {
+      const int sj = d.s0 + j;
+      const double dx = __dadd_rn(tx, -P.x[sj]);
+      const double dy = __dadd_rn(ty, -P.y[sj]);
+      const double den = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      const bool z = (den == 0.0);
+      double v;
+      if (k.flag == HSS_SL_L_2D) {
+        v = __dmul_rn(__dmul_rn(hb, log(z ? 1.0 : den)), P.cval[sj]);
+        v = __dadd_rn(v, z ? 1.0 : 0.0);
+      } else {
+        const double w = P.w[sj];
+        if (z) {
+          v = __dadd_rn(-0.5, -__dmul_rn(__dmul_rn(w, P.kap[sj]), 0.07957747154594767));
+        } else {
+          const double num = __dadd_rn(__dmul_rn(P.nx[sj], dx), __dmul_rn(P.ny[sj], dy));
+          v = __ddiv_rn(__dmul_rn(__dmul_rn(w, 0.15915494309189535), num), den);
+        }
+      }
+      const double* qj = d.q + j;
+#pragma unroll
+      for (int c = 0; c < NR; ++c)
+        if (c < nrhs) acc[c] = fma(v, qj[(size_t)c * d.ldq], acc[c]);
+    }
+    double* pp = part + (((size_t)blockIdx.z * nsplit + blockIdx.y) * mmax + i) * NR;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) pp[c] = acc[c];
+  }
+}
+
+template <int NR>
+__global__ void k_kmatvec_reduce(const KmvP* __restrict__ D, int nsplit, const double* __restrict__ part, int mmax,
+                                 int nrhs) {
+  const KmvP d = D[blockIdx.y];
+  const int tot = d.m * nrhs;
+  for (int e = blockIdx.x * 256 + threadIdx.x; e < tot; e += gridDim.x * 256) {
+    const int i = e % d.m, c = e / d.m;
+    double s = 0.0;
+    for (int y = 0; y < nsplit; ++y) s += part[(((size_t)blockIdx.y * nsplit + y) * mmax + i) * NR + c];
+    d.u[i + (size_t)c * d.ldu] = s;
+  }
+}
+
+void kernel_matvec(const KmvP* dP, int batch, int maxM, int maxN, int nrhs, const PointView& pts, const KernelDev& k,
+                   DevBuf<double>& part, cudaStream_t s) {
+  if (batch <= 0 || maxM <= 0) return;
+  HSS_REQUIRE(batch <= 65535 && nrhs >= 1 && nrhs <= 8, HSS_ERR_ARG, "kernel matvec: batch <= 65535, 1..8 columns");
+  HSS_REQUIRE(k.flag == HSS_SL_L_2D || k.flag == HSS_DL_L_2D, HSS_ERR_ARG, "kernel matvec: real kernels only");
+  const int tiles = ceil_div(maxM, 256);
+  const int nsplit = std::max(1, std::min(64, std::min(ceil_div(1216, (long long)tiles * batch), std::max(1, maxN / 256))));
+  const int NR = nrhs <= 4 ? 4 : 8;
+  part.ensure((size_t)batch * nsplit * maxM * NR);
+  const dim3 grid(tiles, nsplit, batch);
+  if (NR == 4) k_kmatvec<4><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
+  else k_kmatvec<8><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
+  check_launch("k_kmatvec");
+  const int gx = std::max(1, std::min(ceil_div((long long)maxM * nrhs, 256), 256));
+  if (NR == 4) k_kmatvec_reduce<4><<<dim3(gx, batch), 256, 0, s>>>(dP, nsplit, part.p, maxM, nrhs);
+  else k_kmatvec_reduce<8><<<dim3(gx, batch), 256, 0, s>>>(dP, nsplit, part.p, maxM, nrhs);
+  check_launch("k_kmatvec_reduce");
+}
+
 template void kgen_batched<double>(const KgenP<double>*, int, long long, const PointView&,
                                    const KernelDev&, cudaStream_t);
 template void kgen_batched<float>(const KgenP<float>*, int, long long, const PointView&,

@@ -74,4 +74,19 @@ template <typename R>
 void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const PointView& pts,
                   const KernelDev& k, cudaStream_t s);
 
+// Kernel matrix times vectors without forming the matrix, in FP64 (the refinement residual
+// of Common/Iterative_Refinement.m:20-35 against the kernel matrix itself): problem b
+// computes u(i, c) = sum_j K(t0 + i, s0 + j) q(j, c), i < m, j < n, c < nrhs (<= 8), over
+// the point table, with the entries of kernel_entry (SL_L_2D or DL_L_2D).  The sources are
+// split over blocks; the partial sums are added in a fixed order.
+struct KmvP {
+  int t0, m, s0, n;
+  const double* q;
+  int ldq;
+  double* u;
+  int ldu;
+};
+void kernel_matvec(const KmvP* dP, int batch, int maxM, int maxN, int nrhs, const PointView& pts, const KernelDev& k,
+                   DevBuf<double>& part, cudaStream_t s);
+
 }  // namespace hss

@@ -1,0 +1,616 @@
+// Skinny products on the tensor cores (tcgen05): digit packing, the persistent product
+// kernel and its split-K reduction.  Format and accuracy are described in skinny_tc.cuh.
+//
+// Kernel structure (one CTA per SM, 192 threads):
+//   warp 4, lane 0  producer: streams each work item's packed A blocks into a ring of
+//                   TC_STAGES shared-memory stages with bulk copies (cp.async.bulk, the TMA
+//                   engine) completing on per-stage mbarriers;
+//   warp 5, lane 0  MMA issuer: one tcgen05.mma (M = 128, N = 32, K = 16, bf16 -> fp32) per
+//                   digit slice and stage into the item's TMEM accumulators; tcgen05.commit
+//                   frees the stage and, after the item's last stage, signals the epilogue;
+//   warps 0-3       cut the right-hand sides of the next items into bf16 digits (the B
+//                   operand, two buffers), then read the accumulators of the finished item
+//                   (one TMEM lane per row), add the digit pairs in integers and write FP64.
+// Accumulators are double-buffered in TMEM (2 x 256 columns), so the epilogue of one item
+// overlaps the loads and MMAs of the next.  Every wait is bounded by the global timer; a
+// wait that gives up sets the error word, and the CTA drains its copies in flight and
+// frees its TMEM before it exits.
+#include <algorithm>
+#include <queue>
+
+#include "skinny_tc.cuh"
+
+namespace hss {
+
+namespace {
+
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TC_BBYTES = (TC_KITEM / 8) * 512;  // 32 K cores x 4 row groups x 128 B
+template <int S>
+constexpr uint32_t tc_abytes() { return (uint32_t)S * (TC_ROWS / 8) * 256; }
+template <int S>
+constexpr size_t tc_smem() { return 2 * TC_BBYTES + TC_STAGES * tc_abytes<S>() + 512; }
+constexpr unsigned long long TC_WAIT_NS = 2000000000ULL;  // 2 s per wait
+
+// instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both K-major,
+// N = 32 (bits 17-22 hold N/8), M = 128 (bits 24-28 hold M/16)
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(32 >> 3) << 17) |
+                              ((uint32_t)(TC_ROWS >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase of `bar` with the given parity.  Gives up (false) when another role
+// aborted the CTA or after TC_WAIT_NS, which sets the abort flag and the error word.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_f, int* err) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  for (unsigned it = 1;; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 63) == 0) {
+      if (*abort_f) return false;
+      if (gtimer() - t0 > TC_WAIT_NS) {
+        *abort_f = 1;
+        atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+}
+// bounded wait that ignores the abort flag (draining copies before exit)
+__device__ __forceinline__ void mbar_wait_drain(uint32_t bar, uint32_t parity) {
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try(bar, parity))
+    if (gtimer() - t0 > TC_WAIT_NS) return;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor, no swizzle: start, leading-dimension byte offset (the
+// K-direction step between core matrices), stride byte offset (the M/N-direction step
+// between 8-row groups), descriptor version 1 (bits 46-48)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(TC_IDESC), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 24 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld24(uint32_t taddr, uint32_t (&v)[24]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+               : "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+                 "=r"(v[23])
+               : "r"(taddr + 16));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void named_sync128() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// true on all of warps 0-3 iff `ok` holds on all of them (named barrier 1, 128 threads)
+__device__ __forceinline__ bool all128(bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)ok)
+      : "memory");
+  return r != 0;
+}
+
+// Row / column exponent: |x| < 2^(e - 1) for every x whose biased exponent field is <= ef.
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+__device__ __forceinline__ int scale_exp(int ef) { return ef == 0 ? -1021 : ef - 1021; }
+
+// round(x * 2^(8S - e)) for |x| < 2^(e - 1), from the bits of x (no FP64 arithmetic)
+template <int S>
+__device__ __forceinline__ long long tc_fixed(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  if (ef == 0) return 0;  // zero or subnormal: below every scale in use
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = e - 8 * S + 1075 - ef;  // x 2^(8S - e) = m 2^-sh
+  long long v;
+  if (sh >= 60) v = 0;
+  else if (sh > 0) v = (long long)((m + (1ull << (sh - 1))) >> sh);
+  else v = (long long)(m << (-sh));
+  return (b >> 63) ? -v : v;
+}
+
+// v = sum_j d[j] 256^(S-1-j): the low S-1 digits balanced in [-128, 127], the top digit
+// takes the rest (|d[0]| <= 128 for |v| <= 2^(8S-1))
+template <int S>
+__device__ __forceinline__ void tc_digits(long long v, int (&d)[S]) {
+#pragma unroll
+  for (int j = S - 1; j >= 1; --j) {
+    const int q = (int)(((v + 128) & 255) - 128);
+    d[j] = q;
+    v = (v - q) >> 8;
+  }
+  d[0] = (int)v;
+}
+
+// bf16 bits of a small integer (exact: at most 8 significant bits)
+__device__ __forceinline__ uint32_t bf16_digit(int q) {
+  const float f = __int_as_float(0x4B400000 + q) - 12582912.0f;
+  return __float_as_uint(f) >> 16;
+}
+
+__device__ __forceinline__ double seg_val(const TcPackP& p, int r, int k) {
+  if (k < p.K[0]) return p.sign[0] * p.A[0][r + (size_t)k * p.lda[0]];
+  k -= p.K[0];
+  if (k < p.K[1]) return p.sign[1] * p.A[1][r + (size_t)k * p.lda[1]];
+  k -= p.K[1];
+  return p.sign[2] * p.A[2][r + (size_t)k * p.lda[2]];
+}
+
+__device__ __forceinline__ double b_val(const TcProd& p, int k, int c) {
+  if (k < p.K[0]) return p.B[0][k + (size_t)c * p.ldb[0]];
+  k -= p.K[0];
+  if (k < p.K[1]) return p.B[1][k + (size_t)c * p.ldb[1]];
+  k -= p.K[1];
+  return p.B[2][k + (size_t)c * p.ldb[2]];
+}
+
+__global__ void k_tc_rexp(const TcPackP* __restrict__ P) {
+  const TcPackP p = P[blockIdx.y];
+  const int Kt = p.K[0] + p.K[1] + p.K[2];
+  for (int r = blockIdx.x * 256 + threadIdx.x; r < p.M; r += gridDim.x * 256) {
+    int ef = 0;
+    for (int k = 0; k < Kt; ++k) ef = max(ef, exp_field(seg_val(p, r, k)));
+    p.rexp[r] = scale_exp(ef);
+  }
+}
+
+template <int S>
+__global__ void k_tc_pack(const TcPackP* __restrict__ P) {
+  const TcPackP p = P[blockIdx.y];
+  const int Kt = p.K[0] + p.K[1] + p.K[2];
+  const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
+  const long long work = (long long)(Kp / 8) * Mp;
+  for (long long w = blockIdx.x * 256LL + threadIdx.x; w < work; w += (long long)gridDim.x * 256) {
+    const int r = (int)(w % Mp), cc = (int)(w / Mp);
+    const int e = (r < p.M) ? p.rexp[r] : 0;
+    uint32_t pk[S][4];
+#pragma unroll
+    for (int j = 0; j < S; ++j) pk[j][0] = pk[j][1] = pk[j][2] = pk[j][3] = 0u;
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      const int k = cc * 8 + kk;
+      const double a = (r < p.M && k < Kt) ? seg_val(p, r, k) : 0.0;
+      int d[S];
+      tc_digits<S>(tc_fixed<S>(a, e), d);
+#pragma unroll
+      for (int j = 0; j < S; ++j) pk[j][kk >> 1] |= bf16_digit(d[j]) << (16 * (kk & 1));
+    }
+    const int t = r / TC_ROWS, rt = min(TC_ROWS, Mp - TC_ROWS * t);
+    const int q = cc >> 1, c = cc & 1, g = (r % TC_ROWS) >> 3, rr = r & 7;
+    const size_t base = (size_t)t * (Kp / TC_KS) * S * (TC_ROWS / 8) * 256 + (size_t)q * S * (rt / 8) * 256;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      uint4 v = make_uint4(pk[j][0], pk[j][1], pk[j][2], pk[j][3]);
+      *reinterpret_cast<uint4*>(p.out + base + (size_t)j * (rt / 8) * 256 + g * 256 + c * 128 + rr * 16) = v;
+    }
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_skinny_tc(const TcProd* __restrict__ P, const int4* __restrict__ items, const int* __restrict__ cta_off,
+                double alpha, double beta, double* __restrict__ part, int* __restrict__ err) {
+  constexpr uint32_t AB = tc_abytes<S>();
+  constexpr int TMAX = S + 1;          // digit pairs kept: weight 256^-t, t <= S + 1
+  constexpr int TMID = (TMAX + 1) / 2; // pairs t <= TMID in the high integer, the rest in the low one
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* Bbuf = sm;
+  unsigned char* Abuf = sm + 2 * TC_BBYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Abuf + TC_STAGES * AB);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 6);
+  volatile int* abort_f = reinterpret_cast<volatile int*>(tslot + 1);
+  int* xexp = reinterpret_cast<int*>(tslot + 2);  // [2][4]
+  int* red = xexp + 8;                            // [2][4 warps][4 columns]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int i0 = cta_off[blockIdx.x], nit = cta_off[blockIdx.x + 1] - i0;
+  const uint32_t bar0 = smem_u32(bars);
+  auto FULL = [&](int s) { return bar0 + 8u * s; };
+  auto EMPTY = [&](int s) { return bar0 + 8u * (TC_STAGES + s); };
+  auto BREADY = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + a); };
+  auto DONE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + 2 + a); };
+  auto TFREE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + 4 + a); };
+
+  if (tid == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(FULL(s), 1);
+      mbar_init(EMPTY(s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(BREADY(a), 128);
+      mbar_init(DONE(a), 1);
+      mbar_init(TFREE(a), 128);
+    }
+    *abort_f = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // rows 24..31 of both B buffers (no right-hand side) stay zero
+  for (int e = tid; e < 2 * 32 * 8; e += TC_THREADS) {
+    const int buf = e >> 8, kc = (e >> 3) & 31, part16 = e & 7;
+    *reinterpret_cast<uint4*>(Bbuf + buf * TC_BBYTES + kc * 512 + 3 * 128 + part16 * 16) = make_uint4(0, 0, 0, 0);
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  // item geometry
+  struct Geo {
+    int prod, t, sp, rt, kb, ke, Kt, Mp, nks;
+  };
+  auto geo = [&](int j) {
+    const int4 w = items[i0 + j];
+    const TcProd& p = P[w.x];
+    Geo g;
+    g.prod = w.x;
+    g.t = w.y;
+    g.sp = w.z;
+    g.Kt = p.K[0] + p.K[1] + p.K[2];
+    const int Kp = (g.Kt + 15) & ~15;
+    g.Mp = (p.M + 7) & ~7;
+    g.nks = Kp / TC_KS;
+    g.rt = min(TC_ROWS, g.Mp - TC_ROWS * g.t);
+    g.kb = g.sp * TC_KITEM;
+    g.ke = min(Kp, g.kb + TC_KITEM);
+    return g;
+  };
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer
+      int gs = 0;
+      bool ok = true;
+      for (int j = 0; j < nit && ok; ++j) {
+        const Geo g = geo(j);
+        const uint32_t bytes = (uint32_t)S * (g.rt / 8) * 256;
+        const unsigned char* tile = P[g.prod].A + (size_t)g.t * g.nks * AB;
+        for (int q = g.kb / TC_KS; q < g.ke / TC_KS; ++q, ++gs) {
+          const int s = gs % TC_STAGES;
+          if (gs >= TC_STAGES && !mbar_wait(EMPTY(s), ((gs / TC_STAGES) - 1) & 1, abort_f, err)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(FULL(s), bytes);
+          bulk_g2s(smem_u32(Abuf + s * AB), tile + (size_t)q * bytes, bytes, FULL(s));
+        }
+      }
+      if (!ok)  // let the copies in flight land before the CTA exits
+        for (int h = max(0, gs - TC_STAGES); h < gs; ++h) mbar_wait_drain(FULL(h % TC_STAGES), (h / TC_STAGES) & 1);
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer
+      int gs = 0;
+      bool ok = true;
+      for (int j = 0; j < nit && ok; ++j) {
+        const int a = j & 1;
+        if (!mbar_wait(BREADY(a), (j >> 1) & 1, abort_f, err)) break;
+        if (j >= 2 && !mbar_wait(TFREE(a), ((j - 2) >> 1) & 1, abort_f, err)) break;
+        tc_fence_after();
+        const Geo g = geo(j);
+        const uint32_t bb = smem_u32(Bbuf + a * TC_BBYTES);
+        const uint32_t dcol = tmem + (uint32_t)a * 256;
+        for (int q = 0; q < (g.ke - g.kb) / TC_KS; ++q, ++gs) {
+          const int s = gs % TC_STAGES;
+          if (!mbar_wait(FULL(s), (gs / TC_STAGES) & 1, abort_f, err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ab = smem_u32(Abuf + s * AB);
+          const uint64_t bd = sdesc(bb + (uint32_t)q * 1024, 512, 128);
+#pragma unroll
+          for (int i = 0; i < S; ++i)
+            tc_mma(dcol + (uint32_t)i * 32, sdesc(ab + (uint32_t)(i * (g.rt / 8) * 256), 128, 256), bd, q > 0 ? 1u : 0u);
+          tc_commit(EMPTY(s));
+        }
+        if (ok) tc_commit(DONE(a));
+      }
+      // MMAs in flight finish before the accumulators are freed
+      if (!ok && gs > 0) mbar_wait_drain(EMPTY((gs - 1) % TC_STAGES), ((gs - 1) / TC_STAGES) & 1);
+    }
+  } else {
+    // right-hand-side digits and epilogue (128 threads; thread = TMEM lane = tile row)
+    auto prep = [&](int j, int a) {
+      named_sync128();
+      const Geo g = geo(j);
+      const TcProd& p = P[g.prod];
+      const int c = tid & 3, oct = tid >> 2;
+      const int k0 = g.kb + oct * 8;
+      const bool live = (c < p.r) && (k0 < g.ke);
+      double xv[8];
+      int mef = 0;
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const int k = k0 + kk;
+        xv[kk] = (live && k < g.Kt) ? b_val(p, k, c) : 0.0;
+        mef = max(mef, exp_field(xv[kk]));
+      }
+      mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 4));
+      mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 8));
+      mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 16));
+      if (lane < 4) red[(a * 4 + warp) * 4 + lane] = mef;
+      named_sync128();
+      int m = 0;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) m = max(m, red[(a * 4 + w) * 4 + c]);
+      const int e = scale_exp(m);
+      if (tid < 4) xexp[a * 4 + tid] = e;
+      if (k0 < g.ke) {
+        uint32_t pk[S][4];
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) pk[jj][0] = pk[jj][1] = pk[jj][2] = pk[jj][3] = 0u;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+          int d[S];
+          tc_digits<S>(tc_fixed<S>(xv[kk], e), d);
+#pragma unroll
+          for (int jj = 0; jj < S; ++jj) pk[jj][kk >> 1] |= bf16_digit(d[jj]) << (16 * (kk & 1));
+        }
+        unsigned char* bb = Bbuf + a * TC_BBYTES + (k0 - g.kb) / 8 * 512;
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) {
+          const int n = jj * 4 + c;
+          *reinterpret_cast<uint4*>(bb + (n >> 3) * 128 + (n & 7) * 16) = make_uint4(pk[jj][0], pk[jj][1], pk[jj][2], pk[jj][3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(BREADY(a));
+    };
+    for (int j = 0; j < min(2, nit); ++j) prep(j, j & 1);
+    for (int j = 0; j < nit; ++j) {
+      const int a = j & 1;
+      // the 128 threads leave together: a thread left behind would wait in prep's barrier
+      if (!all128(mbar_wait(DONE(a), (j >> 1) & 1, abort_f, err))) break;
+      tc_fence_after();
+      const Geo g = geo(j);
+      const TcProd& p = P[g.prod];
+      int sacc[TMAX - 1][4];
+#pragma unroll
+      for (int t = 0; t < TMAX - 1; ++t) sacc[t][0] = sacc[t][1] = sacc[t][2] = sacc[t][3] = 0;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)a * 256;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        uint32_t v[24];
+        tmem_ld24(lane_base + (uint32_t)i * 32, v);
+#pragma unroll
+        for (int jx = 0; jx < S; ++jx) {
+          const int t = i + jx + 2;
+          if (t <= TMAX) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) sacc[t - 2][c] += __float2int_rn(__uint_as_float(v[jx * 4 + c]));
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(TFREE(a));
+      int xe[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) xe[c] = xexp[a * 4 + c];
+      const int row = TC_ROWS * g.t + tid;
+      double y[4] = {0.0, 0.0, 0.0, 0.0};
+      if (tid < g.rt && row < p.M) {
+        const int er = p.rexp[row];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          long long hi = 0, lo = 0;
+#pragma unroll
+          for (int t = 2; t <= TMID; ++t) hi += (long long)sacc[t - 2][c] << (8 * (TMID - t));
+#pragma unroll
+          for (int t = TMID + 1; t <= TMAX; ++t) lo += (long long)sacc[t - 2][c] << (8 * (TMAX - t));
+          const int E = er + xe[c];
+          y[c] = ldexp((double)hi, E - 8 * TMID) + ldexp((double)lo, E - 8 * TMAX);
+        }
+      }
+      if (j + 2 < nit) prep(j + 2, a);  // the MMAs of item j are done: its B buffer is free
+      if (tid < g.rt && row < p.M) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (c >= p.r) continue;
+          if (p.ksplit == 1) {
+            double* cp = p.C + row + (size_t)c * p.ldc;
+            *cp = (beta == 0.0) ? alpha * y[c] : alpha * y[c] + beta * *cp;
+          } else {
+            part[p.part_off + ((long long)g.sp * p.M + row) * 4 + c] = y[c];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 5) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+__global__ void k_tc_reduce(const TcProd* __restrict__ P, const int* __restrict__ red, double alpha, double beta,
+                            const double* __restrict__ part) {
+  const TcProd p = P[red[blockIdx.y]];
+  const int tot = p.M * p.r;
+  for (int e = blockIdx.x * 256 + threadIdx.x; e < tot; e += gridDim.x * 256) {
+    const int row = e % p.M, c = e / p.M;
+    double s = 0.0;
+    for (int sp = 0; sp < p.ksplit; ++sp) s += part[p.part_off + ((long long)sp * p.M + row) * 4 + c];
+    double* cp = p.C + row + (size_t)c * p.ldc;
+    *cp = (beta == 0.0) ? alpha * s : alpha * s + beta * *cp;
+  }
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  HSS_CUDA(cudaGetDevice(&dev));
+  HSS_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  return std::max(1, n);
+}
+
+}  // namespace
+
+size_t tc_packed_bytes(int M, int K) {
+  const size_t Mp = ((size_t)M + 7) & ~(size_t)7, Kp = ((size_t)K + 15) & ~(size_t)15;
+  return Mp * Kp * TC_S * 2;
+}
+
+void tc_pack(const TcPackP* dP, int batch, int maxM, int maxK, cudaStream_t s) {
+  if (batch <= 0 || maxM <= 0 || maxK <= 0) return;
+  HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "tc_pack: batch too large");
+  k_tc_rexp<<<dim3(std::max(1, std::min(ceil_div(maxM, 256), 64)), batch), 256, 0, s>>>(dP);
+  check_launch("k_tc_rexp");
+  const long long work = (long long)((maxK + 15) / 8) * ((maxM + 7) & ~7);
+  k_tc_pack<TC_S><<<dim3(std::max(1, std::min(ceil_div(work, 256), 2048)), batch), 256, 0, s>>>(dP);
+  check_launch("k_tc_pack");
+}
+
+void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_err, cudaStream_t s) {
+  HSS_REQUIRE(d_err != nullptr, HSS_ERR_ARG, "tensor-core product: no error word");
+  err = d_err;
+  alpha = al;
+  beta = be;
+  std::vector<TcProd> P = P0;
+  nprod = (int)P.size();
+  std::vector<int4> its;
+  std::vector<long long> cost;
+  std::vector<int> redl;
+  long long poff = 0;
+  maxM = 0;
+  for (int i = 0; i < nprod; ++i) {
+    TcProd& p = P[i];
+    HSS_REQUIRE(p.r >= 1 && p.r <= TC_NR && p.M > 0, HSS_ERR_ARG, "tensor-core product: 1..4 columns");
+    const int Kt = p.K[0] + p.K[1] + p.K[2];
+    HSS_REQUIRE(Kt > 0, HSS_ERR_ARG, "tensor-core product: empty K");
+    HSS_REQUIRE((reinterpret_cast<uintptr_t>(p.A) & 15) == 0, HSS_ERR_ARG, "tensor-core product: A not 16-byte aligned");
+    const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
+    const int nt = (Mp + TC_ROWS - 1) / TC_ROWS;
+    p.ksplit = (Kp + TC_KITEM - 1) / TC_KITEM;
+    p.part_off = 0;
+    if (p.ksplit > 1) {
+      p.part_off = poff;
+      poff += (long long)p.ksplit * p.M * 4;
+      redl.push_back(i);
+    }
+    maxM = std::max(maxM, p.M);
+    for (int t = 0; t < nt; ++t)
+      for (int sp = 0; sp < p.ksplit; ++sp) {
+        const int rt = std::min(TC_ROWS, Mp - TC_ROWS * t);
+        const int kw = std::min(Kp, (sp + 1) * TC_KITEM) - sp * TC_KITEM;
+        its.push_back(make_int4(i, t, sp, 0));
+        cost.push_back((long long)rt * kw + 128LL * 64);  // bytes streamed + a fixed item overhead
+      }
+  }
+  const int nitems = (int)its.size();
+  grid = std::min(nitems, sm_count());
+  // longest-processing-time-first assignment of items to the persistent CTAs
+  std::vector<int> order(nitems);
+  for (int i = 0; i < nitems; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  using LC = std::pair<long long, int>;
+  std::priority_queue<LC, std::vector<LC>, std::greater<LC>> pq;
+  for (int c = 0; c < grid; ++c) pq.push({0, c});
+  std::vector<std::vector<int>> per(grid);
+  for (int i : order) {
+    LC top = pq.top();
+    pq.pop();
+    per[top.second].push_back(i);
+    top.first += cost[i];
+    pq.push(top);
+  }
+  std::vector<int4> flat;
+  std::vector<int> off(grid + 1, 0);
+  for (int c = 0; c < grid; ++c) {
+    std::sort(per[c].begin(), per[c].end());
+    for (int i : per[c]) flat.push_back(its[i]);
+    off[c + 1] = (int)flat.size();
+  }
+  nred = (int)redl.size();
+  prods.alloc(P.size());
+  items.alloc(std::max<size_t>(flat.size(), 1));
+  cta_off.alloc(off.size());
+  red.alloc(std::max(nred, 1));
+  part.alloc(std::max<long long>(poff, 1));
+  HSS_CUDA(cudaMemcpyAsync(prods.p, P.data(), P.size() * sizeof(TcProd), cudaMemcpyHostToDevice, s));
+  HSS_CUDA(cudaMemcpyAsync(items.p, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  HSS_CUDA(cudaMemcpyAsync(cta_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (nred) HSS_CUDA(cudaMemcpyAsync(red.p, redl.data(), redl.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  HSS_CUDA(cudaStreamSynchronize(s));  // host vectors go out of scope
+}
+
+void TcStep::run(cudaStream_t s) const {
+  if (grid <= 0) return;
+  static PerDeviceOnce attr_once;
+  attr_once.run([] {
+    HSS_CUDA(cudaFuncSetAttribute(k_skinny_tc<TC_S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc_smem<TC_S>()));
+  });
+  k_skinny_tc<TC_S><<<grid, TC_THREADS, tc_smem<TC_S>(), s>>>(prods.p, items.p, cta_off.p, alpha, beta, part.p,
+                                                             err);
+  check_launch("k_skinny_tc");
+  if (nred) {
+    k_tc_reduce<<<dim3(std::max(1, std::min(ceil_div((long long)maxM * TC_NR, 256), 64)), nred), 256, 0, s>>>(
+        prods.p, red.p, alpha, beta, part.p);
+    check_launch("k_tc_reduce");
+  }
+}
+
+}  // namespace hss

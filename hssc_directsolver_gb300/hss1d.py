@@ -401,6 +401,18 @@ def HSS1D_solve(K_HSS: HSS1DMatrix, ff, tol: float = 1e-10, maxit: int = 5):
     return (out[:, 0] if vec else out), rr.value, it.value
 
 
+def HSS1D_kernel_residual(K_HSS: HSS1DMatrix, ff, xx) -> float:
+    """max over columns of ||f - K x|| / ||f|| with K the kernel matrix of each curve itself
+    (generated in FP64 on the GPU and applied on the fly, never formed): the dense-matrix
+    residual the reference's tests print (Common/Iterative_Refinement.m:20-35)."""
+    f2 = _as_f64(ff).reshape(K_HSS.N, -1, order="F")
+    x2 = _as_f64(xx).reshape(K_HSS.N, -1, order="F")
+    assert f2.shape == x2.shape
+    rr = C.c_double()
+    L.check(L.lib().hss1d_kernel_residual(K_HSS._h, L.ptr(f2), L.ptr(x2), f2.shape[1], C.byref(rr)))
+    return rr.value
+
+
 # HSS1D_sum_fsym / HSS1D_compressLR_fsym (one ID per box for symmetric operands,
 # HSS1D/HSS1D_sum_fsym.m, HSS1D_compressLR_fsym.m): the nsym forms accept the same
 # operands and return matrices every call here takes (incoming and outgoing skeletons

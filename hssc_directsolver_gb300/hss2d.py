@@ -38,7 +38,8 @@ class HSS2DParams:
     transinv: int = 0
     sym: int = 0
     precision: str = "fp64"   # "fp64", "mixed", "dfloat" (FP64 factors, paired-FP32 solve products)
-                              # or "dfloat_inv" (also the inversion in paired FP32)
+                              # or "dfloat_inv" (also the inversion in paired FP32) or "tc"
+                              # (FP64 factors, inverse-apply products on the tensor cores)
     n_cut: int = 400
     Fopts: str = "dense"
     k_cut: int = 2500         # low-rank T only where k < k_cut
@@ -63,7 +64,7 @@ class HSS2DParams:
         if self.Fopts != "dense":
             raise ValueError("Fopts 'dense' (HSS-D) is the implemented inverse storage")
         prec = {"fp64": L.HSS_PREC_FP64, "mixed": L.HSS_PREC_MIXED, "dfloat": L.HSS_PREC_DFLOAT,
-                "dfloat_inv": L.HSS_PREC_DFLOAT_INV}[self.precision]
+                "dfloat_inv": L.HSS_PREC_DFLOAT_INV, "tc": L.HSS_PREC_TC}[self.precision]
         k = self.kernel
         k.h = self.h
         return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,
@@ -226,6 +227,19 @@ def HSS2D_solve(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 5):
     L.check(L.lib().hss2d_solve(INFO_TREE._h, L.ptr(F2), L.ptr(Xs), F2.shape[1], tol, maxit, C.byref(rr),
                                 C.byref(it)))
     return (Xs[:, 0] if vec else Xs), rr.value, it.value
+
+
+def HSS2D_kernel_residual(INFO_TREE: InfoTree, F, X) -> float:
+    """max over columns of ||f - K x|| / ||f|| with K the kernel matrix of the grid itself
+    (Kernel_Eval entries generated in FP64 on the GPU and applied on the fly, never formed):
+    the residual of HSS2D/Test/Test_HSS2D_InverseCompression.m:300-324 against the dense
+    operator rather than the compressed one."""
+    F2, _ = _vec(INFO_TREE, F)
+    X2, _ = _vec(INFO_TREE, X)
+    assert F2.shape == X2.shape
+    rr = C.c_double()
+    L.check(L.lib().hss2d_kernel_residual(INFO_TREE._h, L.ptr(F2), L.ptr(X2), F2.shape[1], C.byref(rr)))
+    return rr.value
 
 
 def HSS2D_bicgstab(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 200, PRECOND: InfoTree | None = None):

@@ -58,6 +58,11 @@ extern "C" {
 #define HSS_PREC_DFLOAT_INV 3 /* HSS_PREC_DFLOAT plus the inversion's and the least squares'
                                  trailing updates and products in paired FP32 (factors ~5 bits
                                  short of FP64; refinement restores the residual) */
+#define HSS_PREC_TC 4 /* HSS_PREC_DFLOAT's FP64 inversion and forward products; the inverse apply's
+                         products on the tensor cores (tcgen05): each FP64 inverse factor is cut
+                         once into 6 bf16 fixed-point digit slices per row (12 bytes per entry),
+                         the right-hand sides likewise per column, and the exact digit products
+                         are summed in integers (~2^-48 of the row and column maxima) */
 
 /* HSS2D interpolation-operator storage (params.INTERform) */
 #define HSS_INTER_DENSE 0
@@ -190,6 +195,9 @@ int hss1d_solve(hss1d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
                 double* relres, int32_t* iters);
 int hss1d_solve_device(hss1d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
+/* the same residual against the kernel matrix of each curve of the handle (block diagonal over
+ * a forest; stacked vectors); handles from hss1d_compress* only (HSS_ERR_ARG otherwise) */
+int hss1d_kernel_residual(hss1d_matrix* H, const double* f, const double* x, int32_t nrhs, double* relres);
 /* At_HSS = HSS1D_transpose(A_HSS) (HSS1D/HSS1D_transpose.m:1): a new handle holding the
  * transpose in compressed form (up/down skeletons and T swapped, M_SELF transposed, sibling
  * blocks swapped and transposed); not inverted. */
@@ -308,6 +316,13 @@ int hss2d_solve(hss2d_matrix* H, const double* f, double* x, int32_t nrhs, doubl
                 int32_t maxit, double* relres, int32_t* iters);
 int hss2d_solve_device(hss2d_matrix* H, const double* d_f, double* d_x, int32_t nrhs, double tol,
                        int32_t maxit, double* relres, int32_t* iters, void* stream);
+/* relres = max over columns of ||f - K x|| / ||f|| with K the kernel matrix itself
+ * (Kernel_Eval over the grid, never formed: each entry is generated in FP64 and applied on
+ * the fly).  The reference measures this residual against the dense matrix
+ * (HSS2D/Test/Test_HSS2D_InverseCompression.m:300-324; Common/Iterative_Refinement.m:20-35
+ * forms f - A x); hss2d_solve's relres is against the compressed operator.  f, x: host
+ * N x nrhs column-major.  O(N^2) work per column. */
+int hss2d_kernel_residual(hss2d_matrix* H, const double* f, const double* x, int32_t nrhs, double* relres);
 /* tree sizes: depth, box count, N */
 /* on != 0: when a solve plan is built (first apply / inverse apply per column count), time
  * every batched product at K-split counts around the built-in heuristic's and keep the
@@ -376,6 +391,14 @@ int hss_batched_id_device(const double* d_A, int32_t m, int32_t n, int32_t batch
 /* C = A*B for `batch` column-major blocks back to back (device), FP64. */
 int hss_batched_gemm_device(const double* d_A, const double* d_B, double* d_C, int32_t M,
                             int32_t N, int32_t K, int32_t batch, void* stream);
+/* C = A*B for `batch` column-major blocks back to back (device, FP64 in and out, N <= 4
+ * columns) on the tensor cores: each A is cut into 6 bf16 fixed-point digit slices per row,
+ * B likewise per column, and the exact digit products are summed in integers (error
+ * ~2^-47 of max_k |A(i,k)| * max_k |B(k,j)| per term).  The skinny products of the inverse
+ * apply of HSS2D_applyinv_nsym (HSS2D/HSS2D_applyinv_nsym.m:74-243, HSS2D_applyFinv_nsym.m:30-31)
+ * in the HSS_PREC_TC mode run on this kernel. */
+int hss_batched_gemv_tc_device(const double* d_A, const double* d_B, double* d_C, int32_t M,
+                               int32_t N, int32_t K, int32_t batch, void* stream);
 
 #ifdef __cplusplus
 }
