@@ -24,7 +24,7 @@ namespace hss {
 
 namespace {
 
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 320;  // 4 epilogue warps, 4 digit warps, producer, MMA issuer
 constexpr uint32_t TC_BBYTES = (TC_KITEM / 8) * 512;  // 32 K cores x 4 row groups x 128 B
 template <int S>
 constexpr uint32_t tc_abytes() { return (uint32_t)S * (TC_ROWS / 8) * 256; }
@@ -116,8 +116,8 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// 24 consecutive accumulator columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld24(uint32_t taddr, uint32_t (&v)[24]) {
+// 24 consecutive accumulator columns of this thread's TMEM lane (completed by tmem_ld_wait)
+__device__ __forceinline__ void tmem_ld24_issue(uint32_t taddr, uint32_t (&v)[24]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15}, [%16];\n"
@@ -128,19 +128,24 @@ __device__ __forceinline__ void tmem_ld24(uint32_t taddr, uint32_t (&v)[24]) {
                : "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
                  "=r"(v[23])
                : "r"(taddr + 16));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void named_sync128() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-// true on all of warps 0-3 iff `ok` holds on all of them (named barrier 1, 128 threads)
-__device__ __forceinline__ bool all128(bool ok) {
+// named barrier `id` over one 128-thread role group (four warps)
+__device__ __forceinline__ void named_sync128(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+// true on every thread of the group iff `ok` holds on all of them (named barrier `id`)
+__device__ __forceinline__ bool all128(int id, bool ok) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %2, 0;\n bar.red.and.pred q, %1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
       : "=r"(r)
-      : "r"((uint32_t)ok)
+      : "r"(id), "r"((uint32_t)ok)
       : "memory");
   return r != 0;
+}
+// an FP32 holding an integer of magnitude < 2^22, as an int (exact; adds 1.5 * 2^23)
+__device__ __forceinline__ int exact_f32_int(uint32_t bits) {
+  return __float_as_int(__uint_as_float(bits) + 12582912.0f) - 0x4B400000;
 }
 
 // Row / column exponent: |x| < 2^(e - 1) for every x whose biased exponent field is <= ef.
@@ -181,6 +186,33 @@ __device__ __forceinline__ void tc_digits(long long v, int (&d)[S]) {
 __device__ __forceinline__ uint32_t bf16_digit(int q) {
   const float f = __int_as_float(0x4B400000 + q) - 12582912.0f;
   return __float_as_uint(f) >> 16;
+}
+
+// v * 2^e as a double, rounded to nearest (ties to even), from integer operations only:
+// GB300 runs int -> double conversions and FP64 arithmetic at a small fraction of its
+// integer rate.  Results outside the normal range take the FP64 path.
+__device__ __forceinline__ double int_scaled(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
+  unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int nb = 64 - __clzll(u);  // significant bits
+  unsigned long long m;
+  int top = nb - 1;                // exponent of the leading bit
+  if (nb <= 53) {
+    m = u << (53 - nb);
+  } else {
+    const int sh = nb - 53;
+    m = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (m & 1ull))) ++m;
+    if (m == (1ull << 53)) {
+      m >>= 1;
+      ++top;
+    }
+  }
+  const int be = top + e + 1023;
+  if (be <= 0 || be >= 2047) return ldexp((double)v, e);
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
 __device__ __forceinline__ double seg_val(const TcPackP& p, int r, int k) {
@@ -244,18 +276,21 @@ __global__ void k_tc_pack(const TcPackP* __restrict__ P) {
 template <int S>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_skinny_tc(const TcProd* __restrict__ P, const int4* __restrict__ items, const int* __restrict__ cta_off,
-                double alpha, double beta, double* __restrict__ part, int* __restrict__ err) {
+                double alpha, double beta, long long* __restrict__ part, int* __restrict__ err) {
   constexpr uint32_t AB = tc_abytes<S>();
   constexpr int TMAX = S + 1;          // digit pairs kept: weight 256^-t, t <= S + 1
   constexpr int TMID = (TMAX + 1) / 2; // pairs t <= TMID in the high integer, the rest in the low one
+  constexpr int UP = 20, DOWN = 8 * (TMAX - TMID) - UP;
+  static_assert(DOWN >= 0, "digit pair split");
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* Bbuf = sm;
   unsigned char* Abuf = sm + 2 * TC_BBYTES;
   uint64_t* bars = reinterpret_cast<uint64_t*>(Abuf + TC_STAGES * AB);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 6);
   volatile int* abort_f = reinterpret_cast<volatile int*>(tslot + 1);
-  int* xexp = reinterpret_cast<int*>(tslot + 2);  // [2][4]
-  int* red = xexp + 8;                            // [2][4 warps][4 columns]
+  volatile int* last_f = reinterpret_cast<volatile int*>(tslot + 2);
+  int* xexp = reinterpret_cast<int*>(tslot + 4);  // [4 item slots][4 columns]
+  int* red = xexp + 16;                           // [2][4 prep warps][4 columns]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = cta_off[blockIdx.x], nit = cta_off[blockIdx.x + 1] - i0;
   const uint32_t bar0 = smem_u32(bars);
@@ -283,7 +318,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int buf = e >> 8, kc = (e >> 3) & 31, part16 = e & 7;
     *reinterpret_cast<uint4*>(Bbuf + buf * TC_BBYTES + kc * 512 + 3 * 128 + part16 * 16) = make_uint4(0, 0, 0, 0);
   }
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -315,7 +350,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     return g;
   };
 
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {
       // producer
       int gs = 0;
@@ -337,7 +372,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (!ok)  // let the copies in flight land before the CTA exits
         for (int h = max(0, gs - TC_STAGES); h < gs; ++h) mbar_wait_drain(FULL(h % TC_STAGES), (h / TC_STAGES) & 1);
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     if (lane == 0) {
       // MMA issuer
       int gs = 0;
@@ -369,13 +404,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // MMAs in flight finish before the accumulators are freed
       if (!ok && gs > 0) mbar_wait_drain(EMPTY((gs - 1) % TC_STAGES), ((gs - 1) / TC_STAGES) & 1);
     }
-  } else {
-    // right-hand-side digits and epilogue (128 threads; thread = TMEM lane = tile row)
-    auto prep = [&](int j, int a) {
-      named_sync128();
+  } else if (warp >= 4) {
+    // right-hand-side digits of item j into B buffer j & 1 once the MMAs of item j - 2 are done
+    const int ptid = tid - 128, pw = warp - 4;
+    for (int j = 0; j < nit; ++j) {
+      const int a = j & 1;
+      if (j >= 2 && !all128(1, mbar_wait(DONE(a), ((j - 2) >> 1) & 1, abort_f, err))) break;
+      named_sync128(1);
       const Geo g = geo(j);
       const TcProd& p = P[g.prod];
-      const int c = tid & 3, oct = tid >> 2;
+      const int c = ptid & 3, oct = ptid >> 2;
       const int k0 = g.kb + oct * 8;
       const bool live = (c < p.r) && (k0 < g.ke);
       double xv[8];
@@ -389,13 +427,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 4));
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 8));
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 16));
-      if (lane < 4) red[(a * 4 + warp) * 4 + lane] = mef;
-      named_sync128();
+      if (lane < 4) red[(a * 4 + pw) * 4 + lane] = mef;
+      named_sync128(1);
       int m = 0;
 #pragma unroll
       for (int w = 0; w < 4; ++w) m = max(m, red[(a * 4 + w) * 4 + c]);
       const int e = scale_exp(m);
-      if (tid < 4) xexp[a * 4 + tid] = e;
+      if (ptid < 4) xexp[(j & 3) * 4 + ptid] = e;
       if (k0 < g.ke) {
         uint32_t pk[S][4];
 #pragma unroll
@@ -416,86 +454,125 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(BREADY(a));
-    };
-    for (int j = 0; j < min(2, nit); ++j) prep(j, j & 1);
+    }
+  } else {
+    // epilogue (128 threads; thread = TMEM lane = tile row)
     for (int j = 0; j < nit; ++j) {
       const int a = j & 1;
-      // the 128 threads leave together: a thread left behind would wait in prep's barrier
-      if (!all128(mbar_wait(DONE(a), (j >> 1) & 1, abort_f, err))) break;
+      // the 128 threads leave together: a thread left behind would wait in a barrier
+      if (!all128(2, mbar_wait(DONE(a), (j >> 1) & 1, abort_f, err))) break;
       tc_fence_after();
       const Geo g = geo(j);
       const TcProd& p = P[g.prod];
+      int xe[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) xe[c] = xexp[(j & 3) * 4 + c];
       int sacc[TMAX - 1][4];
 #pragma unroll
       for (int t = 0; t < TMAX - 1; ++t) sacc[t][0] = sacc[t][1] = sacc[t][2] = sacc[t][3] = 0;
       const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)a * 256;
 #pragma unroll
-      for (int i = 0; i < S; ++i) {
-        uint32_t v[24];
-        tmem_ld24(lane_base + (uint32_t)i * 32, v);
+      for (int i0s = 0; i0s < S; i0s += 3) {
+        uint32_t v[3][24];
 #pragma unroll
-        for (int jx = 0; jx < S; ++jx) {
-          const int t = i + jx + 2;
-          if (t <= TMAX) {
+        for (int u = 0; u < 3; ++u)
+          if (i0s + u < S) tmem_ld24_issue(lane_base + (uint32_t)(i0s + u) * 32, v[u]);
+        tmem_ld_wait();
 #pragma unroll
-            for (int c = 0; c < 4; ++c) sacc[t - 2][c] += __float2int_rn(__uint_as_float(v[jx * 4 + c]));
+        for (int u = 0; u < 3; ++u) {
+          const int i = i0s + u;
+          if (i >= S) continue;
+#pragma unroll
+          for (int jx = 0; jx < S; ++jx) {
+            const int t = i + jx + 2;
+            if (t <= TMAX) {
+#pragma unroll
+              for (int c = 0; c < 4; ++c) sacc[t - 2][c] += exact_f32_int(v[u][jx * 4 + c]);
+            }
           }
         }
       }
       tc_fence_before();
       mbar_arrive(TFREE(a));
-      int xe[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) xe[c] = xexp[a * 4 + c];
       const int row = TC_ROWS * g.t + tid;
-      double y[4] = {0.0, 0.0, 0.0, 0.0};
-      if (tid < g.rt && row < p.M) {
-        const int er = p.rexp[row];
+      const bool mine = tid < g.rt && row < p.M;
+      long long tot[4];
+      int E[4];
+      const int er = mine ? p.rexp[row] : 0;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          long long hi = 0, lo = 0;
+      for (int c = 0; c < 4; ++c) {
+        long long hi = 0, lo = 0;
 #pragma unroll
-          for (int t = 2; t <= TMID; ++t) hi += (long long)sacc[t - 2][c] << (8 * (TMID - t));
+        for (int t = 2; t <= TMID; ++t) hi += (long long)sacc[t - 2][c] << (8 * (TMID - t));
 #pragma unroll
-          for (int t = TMID + 1; t <= TMAX; ++t) lo += (long long)sacc[t - 2][c] << (8 * (TMAX - t));
-          const int E = er + xe[c];
-          y[c] = ldexp((double)hi, E - 8 * TMID) + ldexp((double)lo, E - 8 * TMAX);
-        }
+        for (int t = TMID + 1; t <= TMAX; ++t) lo += (long long)sacc[t - 2][c] << (8 * (TMAX - t));
+        // one integer: |hi| < 2^42 moves up by UP bits, lo (weight 2^(8 (TMID - TMAX)) of hi's)
+        // down by DOWN bits, dropping < 2^-52 of the product's scale
+        tot[c] = (hi << UP) + (lo >> DOWN);
+        E[c] = er + xe[c] - 8 * TMID - UP;
       }
-      if (j + 2 < nit) prep(j + 2, a);  // the MMAs of item j are done: its B buffer is free
-      if (tid < g.rt && row < p.M) {
+      if (p.ksplit == 1) {
+        if (mine) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          if (c >= p.r) continue;
-          if (p.ksplit == 1) {
+          for (int c = 0; c < 4; ++c) {
+            if (c >= p.r) continue;
+            const double y = int_scaled(tot[c], E[c]);
             double* cp = p.C + row + (size_t)c * p.ldc;
-            *cp = (beta == 0.0) ? alpha * y[c] : alpha * y[c] + beta * *cp;
-          } else {
-            part[p.part_off + ((long long)g.sp * p.M + row) * 4 + c] = y[c];
+            if (alpha == 1.0 && beta == 0.0) *cp = y;  // no FP64 arithmetic on the common path
+            else *cp = (beta == 0.0) ? alpha * y : alpha * y + beta * *cp;
           }
+        }
+      } else {
+        // split K: publish (integer, exponent); the CTA finishing the tile's last part adds all
+        if (mine) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (c >= p.r) continue;
+            long long* pp = part + p.part_off + (((long long)g.sp * p.M + row) * 4 + c) * 2;
+            pp[0] = tot[c];
+            pp[1] = E[c];
+          }
+        }
+        __threadfence();
+        named_sync128(2);
+        if (tid == 0) *last_f = (atomicAdd(p.cnt + g.t, 1) == p.ksplit - 1) ? 1 : 0;
+        named_sync128(2);
+        if (*last_f) {
+          __threadfence();
+          if (mine) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c >= p.r) continue;
+              const long long* pp = part + p.part_off + ((long long)row * 4 + c) * 2;
+              const long long step = (long long)p.M * 8;
+              int emax = -100000;
+              for (int sp = 0; sp < p.ksplit; ++sp) emax = max(emax, (int)__ldcg(pp + sp * step + 1));
+              // each |value| < 2^61 is aligned to emax and lowered by 7 bits, so <= 128 parts
+              // add without overflow (53 bits of the largest part are kept)
+              long long sum = 0;
+              for (int sp = 0; sp < p.ksplit; ++sp) {
+                const int sh = emax - (int)__ldcg(pp + sp * step + 1) + 7;
+                const long long v = __ldcg(pp + sp * step);
+                if (sh < 62) sum += (v + (1LL << (sh - 1))) >> sh;
+              }
+              const double y = int_scaled(sum, emax + 7);
+              double* cp = p.C + row + (size_t)c * p.ldc;
+              if (alpha == 1.0 && beta == 0.0) *cp = y;
+              else *cp = (beta == 0.0) ? alpha * y : alpha * y + beta * *cp;
+            }
+          }
+          named_sync128(2);
+          if (tid == 0) p.cnt[g.t] = 0;  // every part has been counted: ready for the next launch
         }
       }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 5) {
+  if (warp == 9) {
     __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
-  }
-}
-
-__global__ void k_tc_reduce(const TcProd* __restrict__ P, const int* __restrict__ red, double alpha, double beta,
-                            const double* __restrict__ part) {
-  const TcProd p = P[red[blockIdx.y]];
-  const int tot = p.M * p.r;
-  for (int e = blockIdx.x * 256 + threadIdx.x; e < tot; e += gridDim.x * 256) {
-    const int row = e % p.M, c = e / p.M;
-    double s = 0.0;
-    for (int sp = 0; sp < p.ksplit; ++sp) s += part[p.part_off + ((long long)sp * p.M + row) * 4 + c];
-    double* cp = p.C + row + (size_t)c * p.ldc;
-    *cp = (beta == 0.0) ? alpha * s : alpha * s + beta * *cp;
   }
 }
 
@@ -532,8 +609,9 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
   nprod = (int)P.size();
   std::vector<int4> its;
   std::vector<long long> cost;
-  std::vector<int> redl;
+  std::vector<std::pair<int, int>> cnt_of;  // (product, first counter)
   long long poff = 0;
+  int ncnt = 0;
   maxM = 0;
   for (int i = 0; i < nprod; ++i) {
     TcProd& p = P[i];
@@ -544,11 +622,14 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
     const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
     const int nt = (Mp + TC_ROWS - 1) / TC_ROWS;
     p.ksplit = (Kp + TC_KITEM - 1) / TC_KITEM;
+    HSS_REQUIRE(p.ksplit <= 128, HSS_ERR_ARG, "tensor-core product: K above 128 parts");
     p.part_off = 0;
+    p.cnt = nullptr;
     if (p.ksplit > 1) {
       p.part_off = poff;
-      poff += (long long)p.ksplit * p.M * 4;
-      redl.push_back(i);
+      poff += (long long)p.ksplit * p.M * 4 * 2;
+      cnt_of.push_back({i, ncnt});
+      ncnt += nt;
     }
     maxM = std::max(maxM, p.M);
     for (int t = 0; t < nt; ++t)
@@ -559,6 +640,9 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
         cost.push_back((long long)rt * kw + 128LL * 64);  // bytes streamed + a fixed item overhead
       }
   }
+  cnt.alloc(std::max(ncnt, 1));
+  cnt.zero(s);
+  for (auto& pc : cnt_of) P[pc.first].cnt = cnt.p + pc.second;
   const int nitems = (int)its.size();
   grid = std::min(nitems, sm_count());
   // longest-processing-time-first assignment of items to the persistent CTAs
@@ -583,16 +667,13 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
     for (int i : per[c]) flat.push_back(its[i]);
     off[c + 1] = (int)flat.size();
   }
-  nred = (int)redl.size();
   prods.alloc(P.size());
   items.alloc(std::max<size_t>(flat.size(), 1));
   cta_off.alloc(off.size());
-  red.alloc(std::max(nred, 1));
   part.alloc(std::max<long long>(poff, 1));
   HSS_CUDA(cudaMemcpyAsync(prods.p, P.data(), P.size() * sizeof(TcProd), cudaMemcpyHostToDevice, s));
   HSS_CUDA(cudaMemcpyAsync(items.p, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   HSS_CUDA(cudaMemcpyAsync(cta_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  if (nred) HSS_CUDA(cudaMemcpyAsync(red.p, redl.data(), redl.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   HSS_CUDA(cudaStreamSynchronize(s));  // host vectors go out of scope
 }
 
@@ -606,11 +687,6 @@ void TcStep::run(cudaStream_t s) const {
   k_skinny_tc<TC_S><<<grid, TC_THREADS, tc_smem<TC_S>(), s>>>(prods.p, items.p, cta_off.p, alpha, beta, part.p,
                                                              err);
   check_launch("k_skinny_tc");
-  if (nred) {
-    k_tc_reduce<<<dim3(std::max(1, std::min(ceil_div((long long)maxM * TC_NR, 256), 64)), nred), 256, 0, s>>>(
-        prods.p, red.p, alpha, beta, part.p);
-    check_launch("k_tc_reduce");
-  }
 }
 
 }  // namespace hss

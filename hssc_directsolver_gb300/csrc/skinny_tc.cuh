@@ -8,7 +8,7 @@
 //     a = 2^e_r * sum_{i=1..S} alpha_i 256^-i,   alpha_i integers in [-128, 127],
 // (the Ozaki splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59 (2012), with
 // fixed-point digits), and the right-hand sides are cut the same way per column inside the
-// kernel.  Every digit product is exact in bf16 x bf16 -> fp32, and a sum of at most 256
+// kernel.  Every digit product is exact in bf16 x bf16 -> fp32, and a sum of at most 240
 // of them (|alpha beta| <= 2^14) stays below 2^22, so the tensor-core accumulation in
 // FP32 is exact.  The kernel keeps the digit pairs of weight 256^-t, t <= S + 1, adds
 // them in 64-bit integers and converts once to FP64: the product carries ~2^-48 of the
@@ -28,7 +28,7 @@ namespace hss {
 constexpr int TC_S = 6;          // digit slices per entry (8 bits each)
 constexpr int TC_ROWS = 128;     // rows per tile (the MMA's M)
 constexpr int TC_KS = 16;        // K per pipeline stage (one bf16 MMA step)
-constexpr int TC_KITEM = 256;    // K per work item: exact FP32 accumulation bound
+constexpr int TC_KITEM = 240;    // K per work item: |sum of digit products| < 240 * 2^14 < 2^22
 constexpr int TC_NR = 4;         // right-hand sides per product
 constexpr int TC_STAGES = 6;     // shared-memory pipeline depth
 
@@ -56,23 +56,25 @@ struct TcProd {
   double* C;
   int ldc, M, r;
   int ksplit;           // work items along K (TC_KITEM columns each)
-  long long part_off;   // first entry of this product's split-K partial sums (ksplit * M * 4)
+  long long part_off;   // first entry of this product's split-K partials (ksplit * M * 4 (value, exponent) pairs)
+  int* cnt;             // per row tile: split items finished (the last one adds the partials; reset to 0)
 };
 
 // One launch over a list of products: work items (product, tile, K part), balanced over
-// persistent CTAs on the host; the split-K partial sums are added in a fixed order.
+// persistent CTAs on the host.  Split-K partials are exact integers with an exponent; the
+// CTA that finishes a tile's last part adds them in a fixed order (no second launch).
 struct TcStep {
   DevBuf<TcProd> prods;
-  DevBuf<int4> items;   // (product, tile, K part, 0)
-  DevBuf<int> cta_off;  // item range of each CTA
-  DevBuf<int> red;      // products with ksplit > 1
-  DevBuf<double> part;
-  int* err = nullptr;   // device word set by a wait that gave up (owned by the caller)
-  int grid = 0, nred = 0, maxM = 0, nprod = 0;
+  DevBuf<int4> items;     // (product, tile, K part, 0)
+  DevBuf<int> cta_off;    // item range of each CTA
+  DevBuf<long long> part; // split-K partials: (integer sum, exponent) per row and column
+  DevBuf<int> cnt;        // tile counters of the split products
+  int* err = nullptr;     // device word set by a wait that gave up (owned by the caller)
+  int grid = 0, maxM = 0, nprod = 0;
   double alpha = 1.0, beta = 0.0;
   void build(const std::vector<TcProd>& P, double alpha, double beta, int* d_err, cudaStream_t s);
   void run(cudaStream_t s) const;
-  int launches() const { return (grid > 0 ? 1 : 0) + (nred > 0 ? 1 : 0); }
+  int launches() const { return grid > 0 ? 1 : 0; }
 };
 
 }  // namespace hss

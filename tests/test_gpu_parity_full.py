@@ -1,0 +1,113 @@
+"""GPU against the oracle at the benchmarked sizes (GPU).
+
+* The HSS2D 256 x 256 workload (N = 65536, 2047 boxes): the oracle's own tree, compress and
+  invert (about a minute on the host) against the GPU's: skeletons J, source sets I_src and
+  ranks k equal in every box, the FP64 inverse apply, and the solutions of every precision
+  path.
+* 64 curves of the batched configuration (N log-uniform in [1024, 16384], ~380 K points) as
+  one GPU forest against the oracle run on each curve alone: ranks equal in every box of every
+  tree, the inverse apply per curve.  The per-curve oracle runs go to a pool of spawned
+  processes (started fresh, so the GPU context of this process is never forked).
+"""
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+from oracle import hss2d as O2, kernels as OK
+
+pytestmark = pytest.mark.gpu
+
+NPAN = 32
+
+
+def _params(precision):
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    h = 2.0 / (8 * NPAN)
+    return G2.HSS2DParams(Ng=8, npan=NPAN, acc=1e-10, layers=2,
+                          kernel=GK.Kernel("SL_L_2D", h, GK.Modulation(), GK.Modulation(0.5, 0, 0, 20.0)),
+                          precision=precision)
+
+
+@pytest.fixture(scope="module")
+def full(gpu):
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / (8 * NPAN), c=OK.Modulation(0.5, 0, 0, 20.0))
+    prm = O2.HSS2DParams(Ng=8, npan=NPAN, kp=kp, layers=2, acc=1e-10, INTERform="dense")
+    tree = O2.build_tree_nsym(prm)
+    blk = O2.compress_nsym(tree, prm)
+    inv = O2.invert_nsym(tree, prm, blk)
+    F = np.random.default_rng(0).standard_normal((prm.N, 4))
+    F /= np.linalg.norm(F, axis=0)
+    return prm, tree, blk, inv, F, O2.applyinv_nsym(tree, inv, F)
+
+
+def test_full_size_tree_equals_oracle(full):
+    from hssc_directsolver_gb300 import hss2d as G2
+    prm, ot, blk, inv, F, xo = full
+    p = _params("fp64")
+    p.INTERform = "dense"
+    t = G2.HSS2D_build_tree_nsym(p)
+    assert t.N == prm.N == 65536 and t.nboxes == len(ot.k)
+    n, k, px = t.box_sizes()
+    for b in range(t.nboxes):
+        e = t.export_box(b)
+        assert np.array_equal(e["J"], ot.J[b]) and np.array_equal(e["I_src"], ot.I_src[b]), b
+        assert k[b] == ot.k[b] and px[b] == ot.proxy[b].shape[0], b
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("dfloat", 1e-10), ("dfloat_inv", 1e-10),
+                                           ("tc", 1e-10)])
+def test_full_size_solution_equals_oracle(full, precision, tol):
+    """The FP64 inverse apply, and every path's refined solve, against the oracle's FP64 inverse
+    apply of its own factorization (dense T in both)."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    prm, ot, blk, inv, F, xo = full
+    p = _params(precision)
+    p.INTERform = "dense"
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(p))
+    if precision == "fp64":
+        x = G2.HSS2D_applyinv_nsym(t, None, F)
+    else:
+        x, rr, it = G2.HSS2D_solve(t, F, 1e-10, 6)
+        assert rr <= 1e-10
+    d = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+    print(f"{precision}: relative difference from the oracle {d:.2e}")
+    assert d <= tol
+
+
+def _oracle_curve(args):
+    """Per-curve oracle run (in a spawned worker): ranks of every box and the inverse apply."""
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import hss1d as O1, kernels as OK1
+    X, seed, F = args
+    H = O1.compress_nsym(X, 64, 1e-10, OK1.KernelParams(flag=OK1.DL_L_2D), seed=seed)
+    return np.array(H.kskel[1:]), O1.applyinv_nsym(H, O1.invert_nsym(H), F)
+
+
+def test_batched_curves_equal_per_curve_oracle(gpu):
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK, geometry as GG
+    ncurve = 64
+    Xs, sizes = GG.batched_curves(ncurve, seed=0)
+    assert max(sizes) > 12000 and sum(sizes) > 300000
+    seeds = [7 * p + 1 for p in range(ncurve)]
+    F = np.random.default_rng(9).standard_normal((sum(sizes), 2))
+    H = G1.HSS1D_compress_batch(Xs, 64, 1e-10, GK.Kernel("DL_L_2D"), seeds=seeds)
+    roots, base = G1.forest_info(H)
+    kall = H.info()["kskel"]
+    G1.HSS1D_invert_nsym(H)
+    X = G1.HSS1D_applyinv_nsym(H, None, None, F)
+    jobs = [(Xs[p], seeds[p], F[base[p]:base[p] + sizes[p]]) for p in range(ncurve)]
+    order = sorted(range(ncurve), key=lambda p: -sizes[p])
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:
+        res = dict(zip(order, pool.map(_oracle_curve, [jobs[p] for p in order], chunksize=1)))
+    boxes = 0
+    for p in range(ncurve):
+        kq, xo = res[p]
+        kg = kall[roots[p] + 1:roots[p] + 1 + len(kq)]
+        assert np.array_equal(kg, kq), p
+        boxes += len(kq)
+        sl = slice(base[p], base[p] + sizes[p])
+        assert np.linalg.norm(X[sl] - xo) <= 1e-12 * np.linalg.norm(xo), p
+    assert boxes > 10000
