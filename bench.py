@@ -106,12 +106,35 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+def cpu_model() -> str:
+    """The host CPU's model name (the CPU baseline's hardware)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=5).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                return v.strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                    return v.strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(npan: int = 32, nrhs: int = 4, budget_s: float = 20.0):
-    """The oracle's inverse apply (HSS2D_applyinv_nsym restated in NumPy) over
-    factors of the workload's exact shapes, timed on the host cores.  The
-    factors are random (the apply's cost does not depend on their values), so
-    the sample is bounded by the solve itself rather than the oracle's ~70 s
-    factorization."""
+    """One step of the GPU arm on the host cores: the oracle's inverse apply
+    (HSS2D_applyinv_nsym restated in NumPy), its forward apply (HSS2D_apply_nsym, the
+    refinement's residual operator) and the residual norms, over factors and blocks of the
+    workload's exact shapes.  Factors and blocks are random (the applies' cost does not
+    depend on their values), so the sample is bounded by the solve itself rather than the
+    oracle's ~60 s factorization."""
     from oracle import hss2d as O2, kernels as OK
     prm = O2.HSS2DParams(Ng=8, npan=npan, acc=1e-10, layers=2,
                          kp=OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / (8 * npan)))
@@ -129,13 +152,29 @@ def cpu_sample(npan: int = 32, nrhs: int = 4, budget_s: float = 20.0):
         inv["FI"][b] = rng.standard_normal((n, n)) * (1.0 / n)
         if b > 0:
             inv["E"][b] = rng.standard_normal((k, k)) * (1.0 / k)
+    Bs, B12, B21 = {}, {}, {}
+    for b in range(nb):
+        if tree.is_leaf(b):
+            n = len(tree.I_src[b])
+            Bs[b] = rng.standard_normal((n, n)) * (1.0 / n)
+        else:
+            c1, c2 = tree.children(b)
+            B12[b] = rng.standard_normal((tree.k[c1], tree.k[c2])) * 1e-3
+            B21[b] = rng.standard_normal((tree.k[c2], tree.k[c1])) * 1e-3
+    blk = O2.HSS2DBlocks(Bs, B12, B21)
     F = rhs(prm.N, nrhs)
-    O2.applyinv_nsym(tree, inv, F)  # warm
+
+    def step():
+        x = O2.applyinv_nsym(tree, inv, F)
+        r = F - O2.apply_nsym(tree, blk, x)
+        return np.linalg.norm(r, axis=0).max() / np.linalg.norm(F, axis=0).min()
+
+    step()  # warm
     times = []
     t_end = time.perf_counter() + budget_s
     while time.perf_counter() < t_end or len(times) < 2:
         t0 = time.perf_counter()
-        O2.applyinv_nsym(tree, inv, F)
+        step()
         times.append(time.perf_counter() - t0)
         if len(times) >= 50:
             break
@@ -173,9 +212,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nrhs": 4, "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"oracle HSS2D_applyinv_nsym (NumPy/OpenBLAS) over factors of the workload's "
-                                   f"shapes, {n} timed solves of 4 RHS, median"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
+                         "sample": f"oracle HSS2D_applyinv_nsym + HSS2D_apply_nsym residual (NumPy/OpenBLAS) over "
+                                   f"factors and blocks of the workload's shapes, {n} timed steps of 4 RHS, median"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if t_ci is not None:
@@ -609,8 +648,9 @@ def main():
             cores = os.cpu_count() or 1
             t_cpu, n_cpu = cpu_sample(args.npan, nrhs, budget_s=15.0)
             line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": cores, "kind": "port",
-                                    "sample": f"oracle HSS2D_applyinv_nsym over factors of the workload's shapes, "
-                                              f"{n_cpu} solves of 4 RHS, median"}
+                                    "cpu": cpu_model(),
+                                    "sample": f"oracle HSS2D_applyinv_nsym + HSS2D_apply_nsym residual over factors "
+                                              f"and blocks of the workload's shapes, {n_cpu} steps of 4 RHS, median"}
             if not args.no_cpu_ci:
                 try:
                     t_ci = cpu_compress_invert(args.npan)

@@ -215,6 +215,29 @@ __device__ __forceinline__ double int_scaled(long long v, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
+// x >> sh rounded to nearest (ties up), sh >= 1; 0 when the shift removes every bit
+__device__ __forceinline__ long long shr_round(long long x, int sh) {
+  if (sh >= 62) return 0;
+  return (x + (1LL << (sh - 1))) >> sh;
+}
+
+// Running sum (at, ae) += t 2^e of integer products with exponents: the sum is held 2^hb
+// below its largest term's scale, so <= 2^hb terms of magnitude < 2^61 add without overflow
+// (hb = 0 keeps a single term exact).
+__device__ __forceinline__ void acc_add(long long& at, int& ae, long long t, int e, bool first, int hb) {
+  const int e7 = e + hb;
+  if (first) {
+    at = hb ? shr_round(t, hb) : t;
+    ae = e7;
+    return;
+  }
+  if (e7 > ae) {
+    at = shr_round(at, e7 - ae);
+    ae = e7;
+  }
+  at += shr_round(t, ae - e);
+}
+
 __device__ __forceinline__ double seg_val(const TcPackP& p, int r, int k) {
   if (k < p.K[0]) return p.sign[0] * p.A[0][r + (size_t)k * p.lda[0]];
   k -= p.K[0];
@@ -457,6 +480,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {
     // epilogue (128 threads; thread = TMEM lane = tile row)
+    long long acc_t[4] = {0, 0, 0, 0};  // running sum of the current part
+    int acc_e[4] = {0, 0, 0, 0};
     for (int j = 0; j < nit; ++j) {
       const int a = j & 1;
       // the 128 threads leave together: a thread left behind would wait in a barrier
@@ -511,51 +536,62 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tot[c] = (hi << UP) + (lo >> DOWN);
         E[c] = er + xe[c] - 8 * TMID - UP;
       }
-      if (p.ksplit == 1) {
+      const int flags = items[i0 + j].w;
+      const bool first = flags & 1, last = (flags >> 1) & 1;
+      const int hb = (flags >> 2) & 7, part_q = flags >> 5;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc_add(acc_t[c], acc_e[c], tot[c], E[c], first, hb);
+      if (!last) continue;  // the next chunk of this part follows on this CTA
+      if (p.nparts == 1) {
         if (mine) {
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
             if (c >= p.r) continue;
-            const double y = int_scaled(tot[c], E[c]);
+            const double y = int_scaled(acc_t[c], acc_e[c]);
             double* cp = p.C + row + (size_t)c * p.ldc;
             if (alpha == 1.0 && beta == 0.0) *cp = y;  // no FP64 arithmetic on the common path
             else *cp = (beta == 0.0) ? alpha * y : alpha * y + beta * *cp;
           }
         }
       } else {
-        // split K: publish (integer, exponent); the CTA finishing the tile's last part adds all
+        // several parts: publish (integer, exponent); the CTA finishing the tile's last part adds all
         if (mine) {
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
             if (c >= p.r) continue;
-            long long* pp = part + p.part_off + (((long long)g.sp * p.M + row) * 4 + c) * 2;
-            pp[0] = tot[c];
-            pp[1] = E[c];
+            long long* pp = part + p.part_off + (((long long)part_q * p.M + row) * 4 + c) * 2;
+            pp[0] = acc_t[c];
+            pp[1] = acc_e[c];
           }
         }
         __threadfence();
         named_sync128(2);
-        if (tid == 0) *last_f = (atomicAdd(p.cnt + g.t, 1) == p.ksplit - 1) ? 1 : 0;
+        if (tid == 0) *last_f = (atomicAdd(p.cnt + g.t, 1) == p.nparts - 1) ? 1 : 0;
         named_sync128(2);
         if (*last_f) {
           __threadfence();
           if (mine) {
+            const long long step = (long long)p.M * 8;
+            const int pb = 32 - __clz(p.nparts - 1);  // headroom bits for nparts terms
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
               if (c >= p.r) continue;
               const long long* pp = part + p.part_off + ((long long)row * 4 + c) * 2;
-              const long long step = (long long)p.M * 8;
-              int emax = -100000;
-              for (int sp = 0; sp < p.ksplit; ++sp) emax = max(emax, (int)__ldcg(pp + sp * step + 1));
-              // each |value| < 2^61 is aligned to emax and lowered by 7 bits, so <= 128 parts
-              // add without overflow (53 bits of the largest part are kept)
-              long long sum = 0;
-              for (int sp = 0; sp < p.ksplit; ++sp) {
-                const int sh = emax - (int)__ldcg(pp + sp * step + 1) + 7;
-                const long long v = __ldcg(pp + sp * step);
-                if (sh < 62) sum += (v + (1LL << (sh - 1))) >> sh;
+              long long vt[8];
+              int ve[8];
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {  // every load issued before any is used
+                vt[q] = q < p.nparts ? __ldcg(pp + q * step) : 0;
+                ve[q] = q < p.nparts ? (int)__ldcg(pp + q * step + 1) : -100000;
               }
-              const double y = int_scaled(sum, emax + 7);
+              int emax = ve[0];
+#pragma unroll
+              for (int q = 1; q < 8; ++q) emax = max(emax, ve[q]);
+              long long sum = 0;
+#pragma unroll
+              for (int q = 0; q < 8; ++q)
+                if (q < p.nparts) sum += shr_round(vt[q], emax - ve[q] + pb);
+              const double y = int_scaled(sum, emax + pb);
               double* cp = p.C + row + (size_t)c * p.ldc;
               if (alpha == 1.0 && beta == 0.0) *cp = y;
               else *cp = (beta == 0.0) ? alpha * y : alpha * y + beta * *cp;
@@ -607,48 +643,64 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
   beta = be;
   std::vector<TcProd> P = P0;
   nprod = (int)P.size();
-  std::vector<int4> its;
-  std::vector<long long> cost;
-  std::vector<std::pair<int, int>> cnt_of;  // (product, first counter)
-  long long poff = 0;
-  int ncnt = 0;
-  maxM = 0;
-  for (int i = 0; i < nprod; ++i) {
-    TcProd& p = P[i];
+  const int nsm = sm_count();
+  // chunks of every product and tile, then the chunks per part: about two parts per CTA
+  long long total_chunks = 0;
+  for (auto& p : P) {
     HSS_REQUIRE(p.r >= 1 && p.r <= TC_NR && p.M > 0, HSS_ERR_ARG, "tensor-core product: 1..4 columns");
     const int Kt = p.K[0] + p.K[1] + p.K[2];
     HSS_REQUIRE(Kt > 0, HSS_ERR_ARG, "tensor-core product: empty K");
     HSS_REQUIRE((reinterpret_cast<uintptr_t>(p.A) & 15) == 0, HSS_ERR_ARG, "tensor-core product: A not 16-byte aligned");
     const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
-    const int nt = (Mp + TC_ROWS - 1) / TC_ROWS;
     p.ksplit = (Kp + TC_KITEM - 1) / TC_KITEM;
-    HSS_REQUIRE(p.ksplit <= 128, HSS_ERR_ARG, "tensor-core product: K above 128 parts");
+    HSS_REQUIRE(p.ksplit <= 128, HSS_ERR_ARG, "tensor-core product: K above 128 chunks");
+    total_chunks += (long long)((Mp + TC_ROWS - 1) / TC_ROWS) * p.ksplit;
+  }
+  const int psize = (int)std::max<long long>(1, (total_chunks + 2LL * nsm - 1) / (2LL * nsm));
+  struct Part { int prod, t, c0, c1, q; long long cost; };
+  std::vector<Part> parts;
+  long long poff = 0;
+  int ncnt = 0;
+  std::vector<std::pair<int, int>> cnt_of;  // (product, first counter)
+  maxM = 0;
+  for (int i = 0; i < nprod; ++i) {
+    TcProd& p = P[i];
+    const int Kt = p.K[0] + p.K[1] + p.K[2];
+    const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
+    const int nt = (Mp + TC_ROWS - 1) / TC_ROWS;
+    int np = (p.ksplit + psize - 1) / psize;
+    np = std::max(1, std::min(8, np));
+    const int cs = (p.ksplit + np - 1) / np;
+    np = (p.ksplit + cs - 1) / cs;  // no empty part
+    p.nparts = np;
     p.part_off = 0;
     p.cnt = nullptr;
-    if (p.ksplit > 1) {
+    if (np > 1) {
       p.part_off = poff;
-      poff += (long long)p.ksplit * p.M * 4 * 2;
+      poff += (long long)np * p.M * 4 * 2;
       cnt_of.push_back({i, ncnt});
       ncnt += nt;
     }
     maxM = std::max(maxM, p.M);
-    for (int t = 0; t < nt; ++t)
-      for (int sp = 0; sp < p.ksplit; ++sp) {
-        const int rt = std::min(TC_ROWS, Mp - TC_ROWS * t);
-        const int kw = std::min(Kp, (sp + 1) * TC_KITEM) - sp * TC_KITEM;
-        its.push_back(make_int4(i, t, sp, 0));
-        cost.push_back((long long)rt * kw + 128LL * 64);  // bytes streamed + a fixed item overhead
+    for (int t = 0; t < nt; ++t) {
+      const int rt = std::min(TC_ROWS, Mp - TC_ROWS * t);
+      for (int q = 0; q < np; ++q) {
+        const int c0 = q * cs, c1 = std::min(p.ksplit, c0 + cs);
+        const int kw = std::min(Kp, c1 * TC_KITEM) - c0 * TC_KITEM;
+        // bytes streamed + a fixed overhead per chunk
+        parts.push_back(Part{i, t, c0, c1, q, (long long)rt * kw + 128LL * 64 * (c1 - c0)});
       }
+    }
   }
   cnt.alloc(std::max(ncnt, 1));
   cnt.zero(s);
   for (auto& pc : cnt_of) P[pc.first].cnt = cnt.p + pc.second;
-  const int nitems = (int)its.size();
-  grid = std::min(nitems, sm_count());
-  // longest-processing-time-first assignment of items to the persistent CTAs
-  std::vector<int> order(nitems);
-  for (int i = 0; i < nitems; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  const int nparts_all = (int)parts.size();
+  grid = std::min(nparts_all, nsm);
+  // longest-processing-time-first assignment of parts to the persistent CTAs
+  std::vector<int> order(nparts_all);
+  for (int i = 0; i < nparts_all; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return parts[a].cost > parts[b].cost; });
   using LC = std::pair<long long, int>;
   std::priority_queue<LC, std::vector<LC>, std::greater<LC>> pq;
   for (int c = 0; c < grid; ++c) pq.push({0, c});
@@ -657,14 +709,21 @@ void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_e
     LC top = pq.top();
     pq.pop();
     per[top.second].push_back(i);
-    top.first += cost[i];
+    top.first += parts[i].cost;
     pq.push(top);
   }
   std::vector<int4> flat;
   std::vector<int> off(grid + 1, 0);
   for (int c = 0; c < grid; ++c) {
     std::sort(per[c].begin(), per[c].end());
-    for (int i : per[c]) flat.push_back(its[i]);
+    for (int i : per[c]) {
+      const Part& pt = parts[i];
+      int hb = 0;  // headroom bits of the part's running sum: 2^hb >= its chunk count
+      while ((1 << hb) < pt.c1 - pt.c0) ++hb;
+      for (int ch = pt.c0; ch < pt.c1; ++ch)
+        flat.push_back(make_int4(pt.prod, pt.t, ch,
+                                 (pt.q << 5) | (hb << 2) | ((ch == pt.c1 - 1) ? 2 : 0) | ((ch == pt.c0) ? 1 : 0)));
+    }
     off[c + 1] = (int)flat.size();
   }
   prods.alloc(P.size());

@@ -55,17 +55,19 @@ struct TcProd {
   int K[3], ldb[3];
   double* C;
   int ldc, M, r;
-  int ksplit;           // work items along K (TC_KITEM columns each)
-  long long part_off;   // first entry of this product's split-K partials (ksplit * M * 4 (value, exponent) pairs)
-  int* cnt;             // per row tile: split items finished (the last one adds the partials; reset to 0)
+  int ksplit;           // K chunks of TC_KITEM columns
+  int nparts;           // parts per row tile: runs of consecutive chunks, each summed by one CTA (<= 8)
+  long long part_off;   // first entry of this product's part sums (nparts * M * 4 (value, exponent) pairs)
+  int* cnt;             // per row tile: parts finished (the last one adds the part sums; reset to 0)
 };
 
-// One launch over a list of products: work items (product, tile, K part), balanced over
-// persistent CTAs on the host.  Split-K partials are exact integers with an exponent; the
-// CTA that finishes a tile's last part adds them in a fixed order (no second launch).
+// One launch over a list of products: work items (product, tile, K chunk), grouped into
+// parts (runs of consecutive chunks of one tile) that the host balances over persistent
+// CTAs.  A CTA adds the chunks of a part in 64-bit integers; when a tile has several parts,
+// the CTA finishing its last part adds the part sums in a fixed order (no second launch).
 struct TcStep {
   DevBuf<TcProd> prods;
-  DevBuf<int4> items;     // (product, tile, K part, 0)
+  DevBuf<int4> items;     // (product, tile, K chunk, part << 5 | headroom << 2 | last << 1 | first)
   DevBuf<int> cta_off;    // item range of each CTA
   DevBuf<long long> part; // split-K partials: (integer sum, exponent) per row and column
   DevBuf<int> cnt;        // tile counters of the split products

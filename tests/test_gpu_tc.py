@@ -95,6 +95,10 @@ def test_tc_inverse_apply_matches_oracle(gpu, npan):
     x = G2.HSS2D_applyinv_nsym(t, None, q)
     xo = O2.applyinv_nsym(ot, inv, q)
     assert np.linalg.norm(x - xo) <= 1e-11 * np.linalg.norm(xo)
+    # the forward apply's products (T_up, T_dn^T, Bself, B12, B21) on the tensor cores too
+    u = G2.HSS2D_apply_nsym(t, None, q)
+    uo = O2.apply_nsym(ot, O2.compress_nsym(ot, prm), q)
+    assert np.linalg.norm(u - uo) <= 1e-12 * np.linalg.norm(uo)
     xs, rr, it = G2.HSS2D_solve(t, q[:, :4], 1e-10, 3)
     assert rr <= 1e-10 and it == 1
 
