@@ -454,8 +454,7 @@ void HSS2D::compress() {
     kgen_batched<double>(dkg.p, cnt, maxe, view(pts), kdev, stream);
     HSS_CUDA(cudaStreamSynchronize(stream));
   }
-  if (tcm()) make_tc_forward();
-  else if (dfm()) make_df_forward();
+  if (dfm()) make_df_forward();  // the tensor-core mode's forward apply runs on double-float products
   HSS_CUDA(cudaStreamSynchronize(stream));
   phase_s[3] = std::chrono::duration<double>(std::chrono::steady_clock::now() - tc0).count();
   compressed = true;
@@ -687,55 +686,6 @@ void HSS2D::ensure_tc_err() {
   *tc_err_host = 0;
 }
 
-// Digit slices of the forward operator's blocks (T_up, T_dn^T, leaf Bself, sibling B12 / B21)
-// for the tensor-core forward apply.
-void HSS2D::make_tc_forward() {
-  ensure_tc_err();
-  for (int lev = 0; lev <= geo.depth; ++lev) {
-    const auto& g = geo.levels[lev];
-    auto& d = L[lev];
-    const int nbf = nf(g);
-    const int nr = g.n - g.k;
-    const int kc = (lev < geo.depth) ? geo.levels[lev + 1].k : 0;
-    // (source, rows, cols, ld) of each block kind on this level
-    struct Kind { const double* A; int m, k, ld; bool on; };
-    const Kind kinds[5] = {
-        {d.Tup.p, g.k, nr, g.k, lev > 0 && nr > 0},
-        {d.TdnT.p, nr, g.k, nr, lev > 0 && nr > 0},
-        {d.Bself.p, g.n, g.n, g.n, lev == geo.depth},
-        {d.B12.p, kc, kc, kc, lev < geo.depth},
-        {d.B21.p, kc, kc, kc, lev < geo.depth}};
-    std::vector<TcPackP> P;
-    int maxM = 0, maxK = 0;
-    for (int t = 0; t < 5; ++t) {
-      const Kind& kd = kinds[t];
-      if (!kd.on) continue;
-      d.tcF_m[t] = kd.m;
-      d.tcF_box[t] = tc_packed_bytes(kd.m, kd.k);
-      d.tcF[t].alloc(d.tcF_box[t] * nbf);
-      d.tcFe[t].alloc((size_t)kd.m * nbf);
-      for (int i = 0; i < nbf; ++i) {
-        TcPackP q{};
-        q.A[0] = kd.A + (size_t)i * kd.m * kd.k;
-        q.K[0] = kd.k;
-        q.lda[0] = kd.ld;
-        q.sign[0] = 1.0;
-        q.M = kd.m;
-        q.out = d.tcF[t].p + d.tcF_box[t] * i;
-        q.rexp = d.tcFe[t].p + (size_t)i * kd.m;
-        P.push_back(q);
-      }
-      maxM = std::max(maxM, kd.m);
-      maxK = std::max(maxK, kd.k);
-    }
-    if (P.empty()) continue;
-    DevBuf<TcPackP> dP(P.size());
-    HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), P.size() * sizeof(TcPackP), cudaMemcpyHostToDevice, stream));
-    tc_pack(dP.p, (int)P.size(), maxM, maxK, stream);
-    HSS_CUDA(cudaStreamSynchronize(stream));
-  }
-}
-
 void HSS2D::invert() {
   HSS_REQUIRE(compressed, HSS_ERR_STATE, "hss2d_invert before hss2d_compress");
   if (tcm()) ensure_tc_err();
@@ -809,6 +759,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
           ld = gc.nb * gc.k;
         }
       };
+      std::vector<std::vector<TcProd>> phases;
       for (int lev = depth; lev >= 1; --lev) {
         const auto& g = geo.levels[lev];
         auto& d = L[lev];
@@ -830,8 +781,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
             t.r = std::min(TC_NR, r - c0);
             P.push_back(t);
           }
-        pl.tc_steps.emplace_back();
-        pl.tc_steps.back().build(P, 1.0, 0.0, tc_err.p, stream);
+        phases.push_back(std::move(P));
       }
       for (int lev = 0; lev <= depth; ++lev) {
         const auto& g = geo.levels[lev];
@@ -865,9 +815,11 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
             t.r = std::min(TC_NR, r - c0);
             P.push_back(t);
           }
-        pl.tc_steps.emplace_back();
-        pl.tc_steps.back().build(P, 1.0, 0.0, tc_err.p, stream);
+        phases.push_back(std::move(P));
       }
+      // the whole apply, up and down the tree, as one chain of phases (one launch)
+      pl.tc_steps.emplace_back();
+      pl.tc_steps.back().build(phases, 1.0, 0.0, tc_err.p, stream);
       HSS_CUDA(cudaStreamSynchronize(stream));
       return pl;
     }
@@ -1028,69 +980,6 @@ void HSS2D::fwd_prepare(int r) {
   fp.eta.resize(depth + 1);
   const bool df = dfm();
   for (int lev = 0; lev <= depth; ++lev) fp.up[lev].df = fp.lam[lev].df = fp.eta[lev].df = df;
-  if (tcm()) {
-    // tensor-core products over the digit slices of the forward blocks, <= 4 columns each
-    auto tcp = [&](Level2Dev& d, int kind, int i, const double* B, int K, int ldb, double* C, int ldc, int c0) {
-      TcProd t{};
-      t.A = d.tcF[kind].p + d.tcF_box[kind] * fo(i);
-      t.rexp = d.tcFe[kind].p + (size_t)fo(i) * d.tcF_m[kind];
-      t.B[0] = B + (size_t)c0 * ldb;
-      t.K[0] = K;
-      t.ldb[0] = ldb;
-      t.C = C + (size_t)c0 * ldc;
-      t.ldc = ldc;
-      t.M = d.tcF_m[kind];
-      t.r = std::min(TC_NR, r - c0);
-      return t;
-    };
-    for (int lev = depth; lev >= 1; --lev) {
-      const auto& g = geo.levels[lev];
-      auto& d = L[lev];
-      const int nr = g.n - g.k;
-      if (nr <= 0) continue;
-      std::vector<TcProd> P;
-      for (int c0 = 0; c0 < r; c0 += TC_NR)
-        for (int i = 0; i < g.nb; ++i)
-          P.push_back(tcp(d, 0, i, d.rsF.p + (size_t)i * nr, nr, g.nb * nr, d.upF.p + (size_t)i * g.k, g.nb * g.k,
-                          c0));
-      fp.up[lev].tc_steps.emplace_back();
-      fp.up[lev].tc_steps.back().build(P, 1.0, 1.0, tc_err.p, stream);
-    }
-    for (int lev = 0; lev <= depth; ++lev) {
-      const auto& g = geo.levels[lev];
-      auto& d = L[lev];
-      std::vector<TcProd> P;
-      for (int c0 = 0; c0 < r; c0 += TC_NR)
-        for (int i = 0; i < g.nb; ++i) {
-          if (lev == depth) {
-            const int b = (1 << lev) - 1 + i;
-            P.push_back(tcp(d, 2, i, Xd.p + (size_t)NG * geo.leaf_panel[b], g.n, (int)N,
-                            Yd.p + (size_t)NG * geo.leaf_panel[b], (int)N, c0));
-          } else {
-            const auto& gc = geo.levels[lev + 1];
-            auto& dc = L[lev + 1];
-            const int kc = gc.k;
-            double* out = dc.dnF.p + (size_t)(2 * i) * kc;
-            P.push_back(tcp(d, 3, i, dc.upF.p + (size_t)(2 * i + 1) * kc, kc, gc.nb * kc, out, gc.nb * kc, c0));
-            P.push_back(tcp(d, 4, i, dc.upF.p + (size_t)(2 * i) * kc, kc, gc.nb * kc, out + kc, gc.nb * kc, c0));
-          }
-        }
-      fp.lam[lev].tc_steps.emplace_back();
-      fp.lam[lev].tc_steps.back().build(P, 1.0, 0.0, tc_err.p, stream);
-      const int nr = g.n - g.k;
-      if (lev > 0 && nr > 0) {
-        std::vector<TcProd> Q;
-        for (int c0 = 0; c0 < r; c0 += TC_NR)
-          for (int i = 0; i < g.nb; ++i)
-            Q.push_back(tcp(d, 1, i, d.dnF.p + (size_t)i * g.k, g.k, g.nb * g.k, d.tmF.p + (size_t)i * nr, g.nb * nr,
-                            c0));
-        fp.eta[lev].tc_steps.emplace_back();
-        fp.eta[lev].tc_steps.back().build(Q, 1.0, 0.0, tc_err.p, stream);
-      }
-    }
-    HSS_CUDA(cudaStreamSynchronize(stream));
-    return;
-  }
   auto pick = [&](DevBuf<double>& a, DevBuf<double>& b) -> const double* { return df ? b.p : a.p; };
   for (int lev = depth; lev >= 1; --lev) {
     const auto& g = geo.levels[lev];

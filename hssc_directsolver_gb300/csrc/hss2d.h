@@ -59,11 +59,6 @@ struct Level2Dev {
   DevBuf<unsigned char> tcU, tcD;
   DevBuf<int> tcUe, tcDe;
   size_t tcU_box = 0, tcD_box = 0;  // packed bytes per factor box
-  // HSS_PREC_TC forward operator: digit slices of 0 T_up, 1 T_dn^T, 2 Bself, 3 B12, 4 B21
-  DevBuf<unsigned char> tcF[5];
-  DevBuf<int> tcFe[5];
-  size_t tcF_box[5] = {};
-  int tcF_m[5] = {};  // rows of each packed block
   // inverse-apply vectors: 0 phi_up, 1 phi_dn (nb*k x 8)
   DevBuf<double> vd[2];
   DevBuf<float> vf[2];
@@ -118,7 +113,6 @@ struct HSS2D {
   // inverse apply on the tensor cores over digit slices of the FP64 factors
   bool tcm() const { return prm.precision == HSS_PREC_TC; }
   void make_tc_inverse();
-  void make_tc_forward();
   void ensure_tc_err();
   DevBuf<int> tc_err;           // error word of the tensor-core products (0: none)
   int* tc_err_host = nullptr;   // pinned copy, read with the refinement's residual

@@ -16,6 +16,7 @@
 // wait that gives up sets the error word, and the CTA drains its copies in flight and
 // frees its TMEM before it exits.
 #include <algorithm>
+#include <climits>
 #include <queue>
 
 #include "skinny_tc.cuh"
@@ -25,11 +26,14 @@ namespace hss {
 namespace {
 
 constexpr int TC_THREADS = 320;  // 4 epilogue warps, 4 digit warps, producer, MMA issuer
-constexpr uint32_t TC_BBYTES = (TC_KITEM / 8) * 512;  // 32 K cores x 4 row groups x 128 B
+constexpr uint32_t TC_BBYTES = (TC_KITEM / 8) * 512;  // 30 K cores x 4 row groups x 128 B
+constexpr int TC_BDEPTH = 2;  // right-hand-side digit buffers: items prepared ahead of the MMAs
+constexpr int TC_MAXIT = 512; // work items per CTA: their geometry is staged in shared memory
+constexpr int TC_MAXPART = 16; // parts of one row tile (CTAs sharing its K range)
 template <int S>
 constexpr uint32_t tc_abytes() { return (uint32_t)S * (TC_ROWS / 8) * 256; }
 template <int S>
-constexpr size_t tc_smem() { return 2 * TC_BBYTES + TC_STAGES * tc_abytes<S>() + 512; }
+constexpr size_t tc_smem() { return TC_BDEPTH * TC_BBYTES + TC_STAGES * tc_abytes<S>() + 512 + TC_MAXIT * 16; }
 constexpr unsigned long long TC_WAIT_NS = 2000000000ULL;  // 2 s per wait
 
 // instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both K-major,
@@ -246,12 +250,36 @@ __device__ __forceinline__ double seg_val(const TcPackP& p, int r, int k) {
   return p.sign[2] * p.A[2][r + (size_t)k * p.lda[2]];
 }
 
+// right-hand-side entries come from L2 (__ldcg): in a chained launch they were written by
+// other CTAs during an earlier phase
 __device__ __forceinline__ double b_val(const TcProd& p, int k, int c) {
-  if (k < p.K[0]) return p.B[0][k + (size_t)c * p.ldb[0]];
+  if (k < p.K[0]) return __ldcg(p.B[0] + k + (size_t)c * p.ldb[0]);
   k -= p.K[0];
-  if (k < p.K[1]) return p.B[1][k + (size_t)c * p.ldb[1]];
+  if (k < p.K[1]) return __ldcg(p.B[1] + k + (size_t)c * p.ldb[1]);
   k -= p.K[1];
-  return p.B[2][k + (size_t)c * p.ldb[2]];
+  return __ldcg(p.B[2] + k + (size_t)c * p.ldb[2]);
+}
+
+// Wait (one thread) until every CTA has finished phase `cnt` (the counter reaches n), bounded
+// by the global timer like the mbarrier waits.
+__device__ __forceinline__ bool phase_wait(const int* cnt, int n, volatile int* abort_f, int* err) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+  if (v >= n) return true;
+  const unsigned long long t0 = gtimer();
+  for (unsigned it = 1;; ++it) {
+    __nanosleep(64);
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+    if (v >= n) return true;
+    if ((it & 63) == 0) {
+      if (*abort_f) return false;
+      if (gtimer() - t0 > TC_WAIT_NS) {
+        *abort_f = 1;
+        atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
 }
 
 __global__ void k_tc_rexp(const TcPackP* __restrict__ P) {
@@ -299,7 +327,8 @@ __global__ void k_tc_pack(const TcPackP* __restrict__ P) {
 template <int S>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_skinny_tc(const TcProd* __restrict__ P, const int4* __restrict__ items, const int* __restrict__ cta_off,
-                double alpha, double beta, long long* __restrict__ part, int* __restrict__ err) {
+                double alpha, double beta, long long* __restrict__ part, int* __restrict__ err, int nphase,
+                int* __restrict__ pdone) {
   constexpr uint32_t AB = tc_abytes<S>();
   constexpr int TMAX = S + 1;          // digit pairs kept: weight 256^-t, t <= S + 1
   constexpr int TMID = (TMAX + 1) / 2; // pairs t <= TMID in the high integer, the rest in the low one
@@ -307,21 +336,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   static_assert(DOWN >= 0, "digit pair split");
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* Bbuf = sm;
-  unsigned char* Abuf = sm + 2 * TC_BBYTES;
+  unsigned char* Abuf = sm + TC_BDEPTH * TC_BBYTES;
   uint64_t* bars = reinterpret_cast<uint64_t*>(Abuf + TC_STAGES * AB);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 6);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 4 + 2 * TC_BDEPTH);
   volatile int* abort_f = reinterpret_cast<volatile int*>(tslot + 1);
   volatile int* last_f = reinterpret_cast<volatile int*>(tslot + 2);
-  int* xexp = reinterpret_cast<int*>(tslot + 4);  // [4 item slots][4 columns]
-  int* red = xexp + 16;                           // [2][4 prep warps][4 columns]
+  int* xexp = reinterpret_cast<int*>(tslot + 4);  // [8 item slots][4 columns]
+  int* red = xexp + 32;                           // [2][4 prep warps][4 columns]
+  // per item: product, tile | rows << 16, first | end K << 16, K steps | flags << 16
+  int4* gtab = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(bars) + 512);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = cta_off[blockIdx.x], nit = cta_off[blockIdx.x + 1] - i0;
   const uint32_t bar0 = smem_u32(bars);
   auto FULL = [&](int s) { return bar0 + 8u * s; };
   auto EMPTY = [&](int s) { return bar0 + 8u * (TC_STAGES + s); };
-  auto BREADY = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + a); };
-  auto DONE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + 2 + a); };
-  auto TFREE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + 4 + a); };
+  // per accumulator set a (item j % 2): DONE (MMAs finished), TFREE (accumulators read);
+  // per B buffer b (item j % TC_BDEPTH): BREADY (digits written), BFREE (MMAs reading it done)
+  auto DONE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + a); };
+  auto TFREE = [&](int a) { return bar0 + 8u * (2 * TC_STAGES + 2 + a); };
+  auto BREADY = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + 4 + b); };
+  auto BFREE = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + 4 + TC_BDEPTH + b); };
 
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
@@ -329,17 +363,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(EMPTY(s), 1);
     }
     for (int a = 0; a < 2; ++a) {
-      mbar_init(BREADY(a), 128);
       mbar_init(DONE(a), 1);
       mbar_init(TFREE(a), 128);
+    }
+    for (int b = 0; b < TC_BDEPTH; ++b) {
+      mbar_init(BREADY(b), 128);
+      mbar_init(BFREE(b), 1);
     }
     *abort_f = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // rows 24..31 of both B buffers (no right-hand side) stay zero
-  for (int e = tid; e < 2 * 32 * 8; e += TC_THREADS) {
-    const int buf = e >> 8, kc = (e >> 3) & 31, part16 = e & 7;
+  // rows 24..31 of every B buffer (no right-hand side) stay zero
+  constexpr int KC = TC_KITEM / 8;  // K cores of a B buffer
+  for (int e = tid; e < TC_BDEPTH * KC * 8; e += TC_THREADS) {
+    const int buf = e / (KC * 8), kc = (e / 8) % KC, part16 = e & 7;
     *reinterpret_cast<uint4*>(Bbuf + buf * TC_BBYTES + kc * 512 + 3 * 128 + part16 * 16) = make_uint4(0, 0, 0, 0);
+  }
+  for (int e = tid; e < nit; e += TC_THREADS) {  // item geometry, once (global loads off the pipeline)
+    const int4 w = items[i0 + e];
+    const TcProd& p = P[w.x];
+    const int Kp = (p.K[0] + p.K[1] + p.K[2] + 15) & ~15, Mp = (p.M + 7) & ~7;
+    const int rt = min(TC_ROWS, Mp - TC_ROWS * (w.y & 1023));
+    gtab[e] = make_int4(w.x, w.y | (rt << 16), w.z, (Kp / TC_KS) | (w.w << 16));
   }
   if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
@@ -354,22 +399,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   // item geometry
   struct Geo {
-    int prod, t, sp, rt, kb, ke, Kt, Mp, nks;
+    int prod, t, ph, rt, kb, ke, nks;
   };
   auto geo = [&](int j) {
-    const int4 w = items[i0 + j];
-    const TcProd& p = P[w.x];
+    const int4 w = gtab[j];
     Geo g;
     g.prod = w.x;
-    g.t = w.y;
-    g.sp = w.z;
-    g.Kt = p.K[0] + p.K[1] + p.K[2];
-    const int Kp = (g.Kt + 15) & ~15;
-    g.Mp = (p.M + 7) & ~7;
-    g.nks = Kp / TC_KS;
-    g.rt = min(TC_ROWS, g.Mp - TC_ROWS * g.t);
-    g.kb = g.sp * TC_KITEM;
-    g.ke = min(Kp, g.kb + TC_KITEM);
+    g.t = w.y & 1023;
+    g.ph = (w.y >> 10) & 63;
+    g.rt = w.y >> 16;
+    g.kb = w.z & 0xFFFF;
+    g.ke = w.z >> 16;
+    g.nks = w.w & 0xFFFF;
     return g;
   };
 
@@ -380,16 +421,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool ok = true;
       for (int j = 0; j < nit && ok; ++j) {
         const Geo g = geo(j);
-        const uint32_t bytes = (uint32_t)S * (g.rt / 8) * 256;
+        // a stage holds spp consecutive K steps (one contiguous copy): 128 rows' worth
+        const uint32_t step_bytes = (uint32_t)S * (g.rt / 8) * 256;
+        const int spp = TC_ROWS / g.rt, q0 = g.kb / TC_KS, q1 = g.ke / TC_KS;
         const unsigned char* tile = P[g.prod].A + (size_t)g.t * g.nks * AB;
-        for (int q = g.kb / TC_KS; q < g.ke / TC_KS; ++q, ++gs) {
+        for (int q = q0; q < q1; q += spp, ++gs) {
           const int s = gs % TC_STAGES;
           if (gs >= TC_STAGES && !mbar_wait(EMPTY(s), ((gs / TC_STAGES) - 1) & 1, abort_f, err)) {
             ok = false;
             break;
           }
+          const uint32_t bytes = step_bytes * (uint32_t)min(spp, q1 - q);
           mbar_expect_tx(FULL(s), bytes);
-          bulk_g2s(smem_u32(Abuf + s * AB), tile + (size_t)q * bytes, bytes, FULL(s));
+          bulk_g2s(smem_u32(Abuf + s * AB), tile + (size_t)q * step_bytes, bytes, FULL(s));
         }
       }
       if (!ok)  // let the copies in flight land before the CTA exits
@@ -401,42 +445,60 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int gs = 0;
       bool ok = true;
       for (int j = 0; j < nit && ok; ++j) {
-        const int a = j & 1;
-        if (!mbar_wait(BREADY(a), (j >> 1) & 1, abort_f, err)) break;
+        const int a = j & 1, bi = j % TC_BDEPTH;
+        if (!mbar_wait(BREADY(bi), (j / TC_BDEPTH) & 1, abort_f, err)) break;
         if (j >= 2 && !mbar_wait(TFREE(a), ((j - 2) >> 1) & 1, abort_f, err)) break;
         tc_fence_after();
         const Geo g = geo(j);
-        const uint32_t bb = smem_u32(Bbuf + a * TC_BBYTES);
+        const uint32_t bb = smem_u32(Bbuf + bi * TC_BBYTES);
         const uint32_t dcol = tmem + (uint32_t)a * 256;
-        for (int q = 0; q < (g.ke - g.kb) / TC_KS; ++q, ++gs) {
+        const uint32_t step_bytes = (uint32_t)S * (g.rt / 8) * 256;
+        const int spp = TC_ROWS / g.rt, nq = (g.ke - g.kb) / TC_KS;
+        for (int q = 0; q < nq; q += spp, ++gs) {
           const int s = gs % TC_STAGES;
           if (!mbar_wait(FULL(s), (gs / TC_STAGES) & 1, abort_f, err)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t ab = smem_u32(Abuf + s * AB);
-          const uint64_t bd = sdesc(bb + (uint32_t)q * 1024, 512, 128);
+          const int nst = min(spp, nq - q);
+          for (int u = 0; u < nst; ++u) {
+            const uint32_t ab = smem_u32(Abuf + s * AB) + (uint32_t)u * step_bytes;
+            const uint64_t bd = sdesc(bb + (uint32_t)(q + u) * 1024, 512, 128);
 #pragma unroll
-          for (int i = 0; i < S; ++i)
-            tc_mma(dcol + (uint32_t)i * 32, sdesc(ab + (uint32_t)(i * (g.rt / 8) * 256), 128, 256), bd, q > 0 ? 1u : 0u);
+            for (int i = 0; i < S; ++i)
+              tc_mma(dcol + (uint32_t)i * 32, sdesc(ab + (uint32_t)(i * (g.rt / 8) * 256), 128, 256), bd,
+                     (q + u) > 0 ? 1u : 0u);
+          }
           tc_commit(EMPTY(s));
         }
-        if (ok) tc_commit(DONE(a));
+        if (ok) {
+          tc_commit(DONE(a));
+          tc_commit(BFREE(bi));
+        }
       }
       // MMAs in flight finish before the accumulators are freed
       if (!ok && gs > 0) mbar_wait_drain(EMPTY((gs - 1) % TC_STAGES), ((gs - 1) / TC_STAGES) & 1);
     }
   } else if (warp >= 4) {
-    // right-hand-side digits of item j into B buffer j & 1 once the MMAs of item j - 2 are done
+    // right-hand-side digits of item j into B buffer j % TC_BDEPTH once the MMAs of item
+    // j - TC_BDEPTH (the buffer's previous reader) are done
     const int ptid = tid - 128, pw = warp - 4;
     for (int j = 0; j < nit; ++j) {
-      const int a = j & 1;
-      if (j >= 2 && !all128(1, mbar_wait(DONE(a), ((j - 2) >> 1) & 1, abort_f, err))) break;
-      named_sync128(1);
+      const int a = j % TC_BDEPTH;
+      if (j >= TC_BDEPTH && !all128(1, mbar_wait(BFREE(a), ((j - TC_BDEPTH) / TC_BDEPTH) & 1, abort_f, err)))
+        break;
       const Geo g = geo(j);
+      if (g.ph > 0 && (j == 0 || geo(j - 1).ph != g.ph)) {
+        // the right-hand sides of phase ph are the outputs of phase ph - 1 on every CTA
+        bool ok = true;
+        if (ptid == 0) ok = phase_wait(pdone + g.ph - 1, (int)gridDim.x, abort_f, err);
+        if (!all128(1, ok)) break;
+      }
+      named_sync128(1);
       const TcProd& p = P[g.prod];
       const int c = ptid & 3, oct = ptid >> 2;
+      const int Kt = p.K[0] + p.K[1] + p.K[2];
       const int k0 = g.kb + oct * 8;
       const bool live = (c < p.r) && (k0 < g.ke);
       double xv[8];
@@ -444,19 +506,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk) {
         const int k = k0 + kk;
-        xv[kk] = (live && k < g.Kt) ? b_val(p, k, c) : 0.0;
+        xv[kk] = (live && k < Kt) ? b_val(p, k, c) : 0.0;
         mef = max(mef, exp_field(xv[kk]));
       }
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 4));
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 8));
       mef = max(mef, __shfl_xor_sync(0xffffffffu, mef, 16));
-      if (lane < 4) red[(a * 4 + pw) * 4 + lane] = mef;
+      if (lane < 4) red[((j & 1) * 4 + pw) * 4 + lane] = mef;
       named_sync128(1);
       int m = 0;
 #pragma unroll
-      for (int w = 0; w < 4; ++w) m = max(m, red[(a * 4 + w) * 4 + c]);
+      for (int w = 0; w < 4; ++w) m = max(m, red[((j & 1) * 4 + w) * 4 + c]);
       const int e = scale_exp(m);
-      if (ptid < 4) xexp[(j & 3) * 4 + ptid] = e;
+      if (ptid < 4) xexp[(j & 7) * 4 + ptid] = e;
       if (k0 < g.ke) {
         uint32_t pk[S][4];
 #pragma unroll
@@ -482,6 +544,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // epilogue (128 threads; thread = TMEM lane = tile row)
     long long acc_t[4] = {0, 0, 0, 0};  // running sum of the current part
     int acc_e[4] = {0, 0, 0, 0};
+    // phases [arrived, upto) are finished on this CTA: publish its outputs and count it in
+    int arrived = 0;
+    auto arrive = [&](int upto) {
+      if (upto <= arrived) return;
+      __threadfence();
+      named_sync128(2);
+      if (tid == 0)
+        for (int ph = arrived; ph < upto; ++ph) atomicAdd(pdone + ph, 1);
+      arrived = upto;
+    };
+    arrive(nit > 0 ? geo(0).ph : nphase);  // phases without items on this CTA
     for (int j = 0; j < nit; ++j) {
       const int a = j & 1;
       // the 128 threads leave together: a thread left behind would wait in a barrier
@@ -491,7 +564,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const TcProd& p = P[g.prod];
       int xe[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) xe[c] = xexp[(j & 3) * 4 + c];
+      for (int c = 0; c < 4; ++c) xe[c] = xexp[(j & 7) * 4 + c];
       int sacc[TMAX - 1][4];
 #pragma unroll
       for (int t = 0; t < TMAX - 1; ++t) sacc[t][0] = sacc[t][1] = sacc[t][2] = sacc[t][3] = 0;
@@ -536,13 +609,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tot[c] = (hi << UP) + (lo >> DOWN);
         E[c] = er + xe[c] - 8 * TMID - UP;
       }
-      const int flags = items[i0 + j].w;
+      const int flags = gtab[j].w >> 16;
       const bool first = flags & 1, last = (flags >> 1) & 1;
-      const int hb = (flags >> 2) & 7, part_q = flags >> 5;
+      const int hb = (flags >> 2) & 7, part_q = (flags >> 5) & 15, np = (flags >> 9) & 31;
 #pragma unroll
       for (int c = 0; c < 4; ++c) acc_add(acc_t[c], acc_e[c], tot[c], E[c], first, hb);
-      if (!last) continue;  // the next chunk of this part follows on this CTA
-      if (p.nparts == 1) {
+      if (!last) continue;  // the next chunk of this part follows on this CTA (same phase)
+      if (np == 1) {
         if (mine) {
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
@@ -566,31 +639,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         __threadfence();
         named_sync128(2);
-        if (tid == 0) *last_f = (atomicAdd(p.cnt + g.t, 1) == p.nparts - 1) ? 1 : 0;
+        if (tid == 0) *last_f = (atomicAdd(p.cnt + g.t, 1) == np - 1) ? 1 : 0;
         named_sync128(2);
         if (*last_f) {
           __threadfence();
           if (mine) {
             const long long step = (long long)p.M * 8;
-            const int pb = 32 - __clz(p.nparts - 1);  // headroom bits for nparts terms
+            const int pb = 32 - __clz(np - 1);  // headroom bits for np terms
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
               if (c >= p.r) continue;
               const long long* pp = part + p.part_off + ((long long)row * 4 + c) * 2;
-              long long vt[8];
-              int ve[8];
+              long long vt[TC_MAXPART];
+              int ve[TC_MAXPART];
 #pragma unroll
-              for (int q = 0; q < 8; ++q) {  // every load issued before any is used
-                vt[q] = q < p.nparts ? __ldcg(pp + q * step) : 0;
-                ve[q] = q < p.nparts ? (int)__ldcg(pp + q * step + 1) : -100000;
+              for (int q = 0; q < TC_MAXPART; ++q) {  // every load issued before any is used
+                vt[q] = q < np ? __ldcg(pp + q * step) : 0;
+                ve[q] = q < np ? (int)__ldcg(pp + q * step + 1) : -100000;
               }
               int emax = ve[0];
 #pragma unroll
-              for (int q = 1; q < 8; ++q) emax = max(emax, ve[q]);
+              for (int q = 1; q < TC_MAXPART; ++q) emax = max(emax, ve[q]);
               long long sum = 0;
 #pragma unroll
-              for (int q = 0; q < 8; ++q)
-                if (q < p.nparts) sum += shr_round(vt[q], emax - ve[q] + pb);
+              for (int q = 0; q < TC_MAXPART; ++q)
+                if (q < np) sum += shr_round(vt[q], emax - ve[q] + pb);
               const double y = int_scaled(sum, emax + pb);
               double* cp = p.C + row + (size_t)c * p.ldc;
               if (alpha == 1.0 && beta == 0.0) *cp = y;
@@ -601,6 +674,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           if (tid == 0) p.cnt[g.t] = 0;  // every part has been counted: ready for the next launch
         }
       }
+      arrive(j + 1 < nit ? geo(j + 1).ph : nphase);
+    }
+    arrive(nphase);
+    // the last CTA to finish every phase resets the phase counters for the next launch (every
+    // CTA's digit warps have passed all their phase waits by now)
+    if (tid == 0 && atomicAdd(pdone + nphase, 1) == (int)gridDim.x - 1) {
+      for (int ph = 0; ph <= nphase; ++ph) atomicExch(pdone + ph, 0);
     }
   }
   tc_fence_before();
@@ -637,95 +717,138 @@ void tc_pack(const TcPackP* dP, int batch, int maxM, int maxK, cudaStream_t s) {
 }
 
 void TcStep::build(const std::vector<TcProd>& P0, double al, double be, int* d_err, cudaStream_t s) {
+  build(std::vector<std::vector<TcProd>>{P0}, al, be, d_err, s);
+}
+
+void TcStep::build(const std::vector<std::vector<TcProd>>& phases, double al, double be, int* d_err,
+                   cudaStream_t s) {
   HSS_REQUIRE(d_err != nullptr, HSS_ERR_ARG, "tensor-core product: no error word");
+  HSS_REQUIRE(!phases.empty() && phases.size() <= 63, HSS_ERR_ARG, "tensor-core product: 1..63 phases");
   err = d_err;
   alpha = al;
   beta = be;
-  std::vector<TcProd> P = P0;
+  nphase = (int)phases.size();
+  std::vector<TcProd> P;
+  std::vector<int> phase_of;
+  for (int ph = 0; ph < nphase; ++ph)
+    for (auto& q : phases[ph]) {
+      P.push_back(q);
+      phase_of.push_back(ph);
+    }
   nprod = (int)P.size();
   const int nsm = sm_count();
-  // chunks of every product and tile, then the chunks per part: about two parts per CTA
-  long long total_chunks = 0;
-  for (auto& p : P) {
-    HSS_REQUIRE(p.r >= 1 && p.r <= TC_NR && p.M > 0, HSS_ERR_ARG, "tensor-core product: 1..4 columns");
-    const int Kt = p.K[0] + p.K[1] + p.K[2];
-    HSS_REQUIRE(Kt > 0, HSS_ERR_ARG, "tensor-core product: empty K");
-    HSS_REQUIRE((reinterpret_cast<uintptr_t>(p.A) & 15) == 0, HSS_ERR_ARG, "tensor-core product: A not 16-byte aligned");
-    const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
-    p.ksplit = (Kp + TC_KITEM - 1) / TC_KITEM;
-    HSS_REQUIRE(p.ksplit <= 128, HSS_ERR_ARG, "tensor-core product: K above 128 chunks");
-    total_chunks += (long long)((Mp + TC_ROWS - 1) / TC_ROWS) * p.ksplit;
-  }
-  const int psize = (int)std::max<long long>(1, (total_chunks + 2LL * nsm - 1) / (2LL * nsm));
-  struct Part { int prod, t, c0, c1, q; long long cost; };
-  std::vector<Part> parts;
-  long long poff = 0;
-  int ncnt = 0;
-  std::vector<std::pair<int, int>> cnt_of;  // (product, first counter)
+  // row tiles of every product, in product order; cost = rows x K steps (+ a fixed cost per chunk)
+  struct Tile { int prod, t, rt, nks, ph; };
+  std::vector<Tile> tiles;
+  std::vector<long long> ptotal(nphase, 0);
   maxM = 0;
   for (int i = 0; i < nprod; ++i) {
     TcProd& p = P[i];
+    HSS_REQUIRE(p.r >= 1 && p.r <= TC_NR && p.M > 0, HSS_ERR_ARG, "tensor-core product: 1..4 columns");
     const int Kt = p.K[0] + p.K[1] + p.K[2];
+    HSS_REQUIRE(Kt > 0 && Kt < 65536 - 16, HSS_ERR_ARG, "tensor-core product: K outside 1..65519");
+    HSS_REQUIRE((reinterpret_cast<uintptr_t>(p.A) & 15) == 0, HSS_ERR_ARG, "tensor-core product: A not 16-byte aligned");
     const int Kp = (Kt + 15) & ~15, Mp = (p.M + 7) & ~7;
     const int nt = (Mp + TC_ROWS - 1) / TC_ROWS;
-    int np = (p.ksplit + psize - 1) / psize;
-    np = std::max(1, std::min(8, np));
-    const int cs = (p.ksplit + np - 1) / np;
-    np = (p.ksplit + cs - 1) / cs;  // no empty part
-    p.nparts = np;
-    p.part_off = 0;
-    p.cnt = nullptr;
-    if (np > 1) {
-      p.part_off = poff;
-      poff += (long long)np * p.M * 4 * 2;
-      cnt_of.push_back({i, ncnt});
-      ncnt += nt;
-    }
+    HSS_REQUIRE(nt <= 1024, HSS_ERR_ARG, "tensor-core product: more than 1024 row tiles");
+    p.ksplit = (Kp + TC_KITEM - 1) / TC_KITEM;
     maxM = std::max(maxM, p.M);
     for (int t = 0; t < nt; ++t) {
       const int rt = std::min(TC_ROWS, Mp - TC_ROWS * t);
-      for (int q = 0; q < np; ++q) {
-        const int c0 = q * cs, c1 = std::min(p.ksplit, c0 + cs);
-        const int kw = std::min(Kp, c1 * TC_KITEM) - c0 * TC_KITEM;
-        // bytes streamed + a fixed overhead per chunk
-        parts.push_back(Part{i, t, c0, c1, q, (long long)rt * kw + 128LL * 64 * (c1 - c0)});
-      }
+      tiles.push_back(Tile{i, t, rt, Kp / TC_KS, phase_of[i]});
+      ptotal[phase_of[i]] += (long long)rt * (Kp / TC_KS);
     }
   }
-  cnt.alloc(std::max(ncnt, 1));
-  cnt.zero(s);
-  for (auto& pc : cnt_of) P[pc.first].cnt = cnt.p + pc.second;
-  const int nparts_all = (int)parts.size();
-  grid = std::min(nparts_all, nsm);
-  // longest-processing-time-first assignment of parts to the persistent CTAs
-  std::vector<int> order(nparts_all);
-  for (int i = 0; i < nparts_all; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return parts[a].cost > parts[b].cost; });
-  using LC = std::pair<long long, int>;
-  std::priority_queue<LC, std::vector<LC>, std::greater<LC>> pq;
-  for (int c = 0; c < grid; ++c) pq.push({0, c});
-  std::vector<std::vector<int>> per(grid);
-  for (int i : order) {
-    LC top = pq.top();
-    pq.pop();
-    per[top.second].push_back(i);
-    top.first += parts[i].cost;
-    pq.push(top);
+  // Linear partition: every CTA takes an equal share of rows x K steps.  Whole tiles go to
+  // the current CTA while they fit; a tile larger than a quarter of the share is cut at a K
+  // step so that the CTA is filled (at most TC_MAXPART parts per tile); the CTAs of one tile
+  // meet in the in-kernel reduction.
+  const int ntile = (int)tiles.size();
+  // Per phase, cut the tiles' K steps, in order and weighted by their rows, into runs of
+  // equal weight, one per CTA; a run boundary may fall inside a tile (its parts then meet in
+  // the kernel's final add).  A tile of weight w spans at most w / share + 2 runs, so a
+  // phase uses fewer CTAs when needed to keep every tile within TC_MAXPART parts.  A chain
+  // of phases runs on every SM (one CTA each, all resident: a cooperative launch).
+  grid = nphase > 1 ? nsm : std::max(1, std::min(nsm, ntile * TC_MAXPART));
+  struct Seg { int tile, s0, s1; };
+  std::vector<std::vector<Seg>> per(grid);
+  {
+    int tb = 0;
+    for (int ph = 0; ph < nphase; ++ph) {
+      int te = tb;
+      long long maxw = 1;
+      while (te < ntile && tiles[te].ph == ph) {
+        maxw = std::max(maxw, (long long)tiles[te].rt * tiles[te].nks);
+        ++te;
+      }
+      if (te == tb) continue;
+      const long long total = ptotal[ph];
+      const int g = std::max(1, std::min(grid, (int)std::min<long long>((long long)(te - tb) * TC_MAXPART,
+                                                                        (TC_MAXPART - 2) * total / maxw)));
+      const long long share = (total + g - 1) / g;
+      long long w0 = 0;  // weight before the current tile
+      for (int ti = tb; ti < te; ++ti) {
+        const Tile& T = tiles[ti];
+        int s0 = 0;
+        while (s0 < T.nks) {
+          const long long pos = w0 + (long long)s0 * T.rt;  // weight at step s0
+          const int c = (int)std::min<long long>(g - 1, pos / share);
+          const long long end = (c == g - 1) ? LLONG_MAX : (long long)(c + 1) * share;
+          const long long room = end - pos;  // steps of this tile before the run's end (at least one)
+          const int take = (int)std::max<long long>(1, std::min<long long>(T.nks - s0, (room + T.rt - 1) / T.rt));
+          per[c].push_back(Seg{ti, s0, s0 + take});
+          s0 += take;
+        }
+        w0 += (long long)T.rt * T.nks;
+      }
+      tb = te;
+    }
   }
+  if (nphase == 1)
+    while (grid > 1 && per[grid - 1].empty()) --grid;
+  // parts per tile, counters and part-sum slots
+  std::vector<int> tparts(ntile, 0);
+  for (auto& v : per)
+    for (auto& sg : v) ++tparts[sg.tile];
+  std::vector<int> pslots(nprod, 1), tfirst(nprod, -1);
+  for (int ti = 0; ti < ntile; ++ti) {
+    HSS_REQUIRE(tparts[ti] >= 1 && tparts[ti] <= TC_MAXPART, HSS_ERR_ARG, "tensor-core product: tile split too far");
+    pslots[tiles[ti].prod] = std::max(pslots[tiles[ti].prod], tparts[ti]);
+    if (tfirst[tiles[ti].prod] < 0) tfirst[tiles[ti].prod] = ti;
+  }
+  long long poff = 0;
+  for (int i = 0; i < nprod; ++i) {
+    P[i].nparts = pslots[i];
+    P[i].part_off = poff;
+    if (pslots[i] > 1) poff += (long long)pslots[i] * P[i].M * 4 * 2;
+  }
+  cnt.alloc(std::max(ntile, 1));
+  cnt.zero(s);
+  for (int i = 0; i < nprod; ++i) P[i].cnt = cnt.p + tfirst[i];  // tiles of a product are consecutive
+  // items: chunks of <= TC_KITEM columns of each segment, in segment order per CTA
+  std::vector<int> qnext(ntile, 0);
   std::vector<int4> flat;
   std::vector<int> off(grid + 1, 0);
+  constexpr int CH = TC_KITEM / TC_KS;  // K steps per chunk
   for (int c = 0; c < grid; ++c) {
-    std::sort(per[c].begin(), per[c].end());
-    for (int i : per[c]) {
-      const Part& pt = parts[i];
+    for (auto& sg : per[c]) {
+      const Tile& T = tiles[sg.tile];
+      const int q = qnext[sg.tile]++;
+      const int nch = (sg.s1 - sg.s0 + CH - 1) / CH;
       int hb = 0;  // headroom bits of the part's running sum: 2^hb >= its chunk count
-      while ((1 << hb) < pt.c1 - pt.c0) ++hb;
-      for (int ch = pt.c0; ch < pt.c1; ++ch)
-        flat.push_back(make_int4(pt.prod, pt.t, ch,
-                                 (pt.q << 5) | (hb << 2) | ((ch == pt.c1 - 1) ? 2 : 0) | ((ch == pt.c0) ? 1 : 0)));
+      while ((1 << hb) < nch) ++hb;
+      HSS_REQUIRE(hb <= 7, HSS_ERR_ARG, "tensor-core product: part of more than 128 chunks");
+      for (int ch = 0; ch < nch; ++ch) {
+        const int a0 = sg.s0 + ch * CH, a1 = std::min(sg.s1, a0 + CH);
+        const int flags = ((ch == 0) ? 1 : 0) | ((ch == nch - 1) ? 2 : 0) | (hb << 2) | (q << 5) | (tparts[sg.tile] << 9);
+        flat.push_back(make_int4(T.prod, T.t | (T.ph << 10), (a0 * TC_KS) | ((a1 * TC_KS) << 16), flags));
+      }
     }
+    HSS_REQUIRE((int)flat.size() - off[c] <= TC_MAXIT, HSS_ERR_ARG, "tensor-core product: too many work items for one launch");
     off[c + 1] = (int)flat.size();
   }
+  pdone.alloc(nphase + 1);
+  pdone.zero(s);
   prods.alloc(P.size());
   items.alloc(std::max<size_t>(flat.size(), 1));
   cta_off.alloc(off.size());
@@ -743,8 +866,18 @@ void TcStep::run(cudaStream_t s) const {
     HSS_CUDA(cudaFuncSetAttribute(k_skinny_tc<TC_S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)tc_smem<TC_S>()));
   });
-  k_skinny_tc<TC_S><<<grid, TC_THREADS, tc_smem<TC_S>(), s>>>(prods.p, items.p, cta_off.p, alpha, beta, part.p,
-                                                             err);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(TC_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = tc_smem<TC_S>();
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // the phases of a chain wait on every CTA
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = nphase > 1 ? 1 : 0;
+  HSS_CUDA(cudaLaunchKernelEx(&cfg, k_skinny_tc<TC_S>, prods.p, items.p, cta_off.p, alpha, beta, part.p, err,
+                              nphase, pdone.p));
   check_launch("k_skinny_tc");
 }
 

@@ -30,7 +30,7 @@ constexpr int TC_ROWS = 128;     // rows per tile (the MMA's M)
 constexpr int TC_KS = 16;        // K per pipeline stage (one bf16 MMA step)
 constexpr int TC_KITEM = 240;    // K per work item: |sum of digit products| < 240 * 2^14 < 2^22
 constexpr int TC_NR = 4;         // right-hand sides per product
-constexpr int TC_STAGES = 6;     // shared-memory pipeline depth
+constexpr int TC_STAGES = 7;     // shared-memory pipeline depth (24 KB stages)
 
 // bytes of the packed digit slices of an M x K product
 size_t tc_packed_bytes(int M, int K);
@@ -71,10 +71,15 @@ struct TcStep {
   DevBuf<int> cta_off;    // item range of each CTA
   DevBuf<long long> part; // split-K partials: (integer sum, exponent) per row and column
   DevBuf<int> cnt;        // tile counters of the split products
+  DevBuf<int> pdone;      // per phase: CTAs finished with it (and a final count that resets them)
   int* err = nullptr;     // device word set by a wait that gave up (owned by the caller)
-  int grid = 0, maxM = 0, nprod = 0;
+  int grid = 0, maxM = 0, nprod = 0, nphase = 1;
   double alpha = 1.0, beta = 0.0;
   void build(const std::vector<TcProd>& P, double alpha, double beta, int* d_err, cudaStream_t s);
+  // a chain: phase ph + 1 reads what phase ph writes; one cooperative launch runs them all,
+  // every CTA waiting (bounded) for the previous phase before it reads its right-hand sides
+  void build(const std::vector<std::vector<TcProd>>& phases, double alpha, double beta, int* d_err,
+             cudaStream_t s);
   void run(cudaStream_t s) const;
   int launches() const { return grid > 0 ? 1 : 0; }
 };
