@@ -32,6 +32,9 @@ HSS_SL_H_2D = 2
 HSS_MOD_GAUSS = 0
 HSS_MOD_BUMP = 1
 HSS_MOD_SQRT_BUMP = 2
+HSS_MOD_GAUSS0 = 3
+HSS_PROXY_BDRY = 0
+HSS_PROXY_RAND = 1
 HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_PREC_DFLOAT = 2
@@ -53,7 +56,7 @@ class hss2d_params(C.Structure):
     _fields_ = [("Ng", C.c_int32), ("npan", C.c_int32), ("layers", C.c_int32), ("interform", C.c_int32),
                 ("transinv", C.c_int32), ("sym", C.c_int32), ("precision", C.c_int32), ("pad_", C.c_int32),
                 ("acc", C.c_double), ("kp", hss_kernel_params), ("k_cut", C.c_int32), ("pad2_", C.c_int32),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("proxy_rule", C.c_int32), ("pad3_", C.c_int32), ("lambda", C.c_double)]
 
 
 class HSSError(RuntimeError):
@@ -139,6 +142,9 @@ SIGNATURES = {
     "hss2d_interp_ranks": (C.c_int, [_P, _I32P, _I32P]),
     "hss2d_phase_times": (C.c_int, [_P, _DP]),
     "hss2d_bicgstab": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_double, C.c_int32, _DP, _I32P]),
+    "hss2d_gmres": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_double, C.c_int32, C.c_int32, _DP, _I32P]),
+    "hss2d_kernel_residual_rows": (C.c_int, [_P, C.c_int64, C.c_int64, _P, _P, C.c_int32, _P]),
+    "hss2d_proxy_points": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _DP, C.c_int32, _I32P]),
     "hss2d_solve_bytes": (C.c_int, [_P, _I64P]),
     "hss2d_solve_launches": (C.c_int, [_P, C.c_int32, _I32P]),
     "hss2d_destroy": (C.c_int, [_P]),

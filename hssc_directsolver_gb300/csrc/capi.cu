@@ -871,7 +871,7 @@ int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* 
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
   if (depth) *depth = H->impl->geo.depth;
   if (nboxes) *nboxes = H->impl->geo.nboxes;
-  if (N) *N = H->impl->geo.N;
+  if (N) *N = H->impl->cplx ? H->impl->geo.N / 2 : H->impl->geo.N;
   HSS_CATCH
 }
 
@@ -879,13 +879,14 @@ int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* npro
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
   const auto& g = H->impl->geo;
+  const int u = H->impl->cplx ? 2 : 1;  // complex trees report points, not embedded entries
   for (int lev = 0; lev <= g.depth; ++lev) {
     const auto& L = g.levels[lev];
     for (int i = 0; i < L.nb; ++i) {
       const int b = (1 << lev) - 1 + i;
-      if (n) n[b] = L.n;
-      if (k) k[b] = L.k;
-      if (nproxy) nproxy[b] = L.p;
+      if (n) n[b] = L.n / u;
+      if (k) k[b] = L.k / u;
+      if (nproxy) nproxy[b] = (L.poff[i + 1] - L.poff[i]) / u;
     }
   }
   HSS_CATCH
@@ -900,9 +901,36 @@ int hss2d_export_box(const hss2d_matrix* H, int32_t box, int32_t* I_src, int32_t
   while (((1 << (lev + 1)) - 1) <= box) ++lev;
   const auto& g = h->geo.levels[lev];
   const int i = box - ((1 << lev) - 1);
+  const size_t tcnt = (size_t)g.k * (g.n - g.k);
+  if (h->cplx) {
+    // points (every other embedded entry) and T as interleaved complex (k x (n - k) points)
+    const int nc = g.n / 2, kc = g.k / 2;
+    for (int q = 0; q < nc; ++q) {
+      if (I_src) I_src[q] = g.Isrc[(size_t)i * g.n + 2 * q] / 2;
+      if (J) J[q] = g.J[(size_t)i * g.n + 2 * q] / 2;
+    }
+    if (lev > 0 && tcnt > 0) {
+      auto& d = h->L[lev];
+      const size_t fi = h->fo(i);
+      std::vector<double> t(tcnt);
+      double* outs[2] = {T_up, T_dn};
+      const double* srcs[2] = {d.Tup.p, d.Tdn.p};
+      for (int w = 0; w < 2; ++w) {
+        if (!outs[w]) continue;
+        HSS_CUDA(cudaMemcpy(t.data(), srcs[w] + fi * tcnt, tcnt * sizeof(double), cudaMemcpyDeviceToHost));
+        // T_dn is held conjugated (its real transpose is then the embedded plain transpose)
+        const double sg = (w == 1) ? -1.0 : 1.0;
+        for (int c = 0; c < (g.n - g.k) / 2; ++c)
+          for (int r = 0; r < kc; ++r) {
+            outs[w][2 * (r + (size_t)c * kc)] = t[2 * r + (size_t)(2 * c) * g.k];
+            outs[w][2 * (r + (size_t)c * kc) + 1] = sg * t[2 * r + 1 + (size_t)(2 * c) * g.k];
+          }
+      }
+    }
+    return HSS_OK;
+  }
   if (I_src) std::memcpy(I_src, g.Isrc.data() + (size_t)i * g.n, g.n * sizeof(int32_t));
   if (J) std::memcpy(J, g.J.data() + (size_t)i * g.n, g.n * sizeof(int32_t));
-  const size_t tcnt = (size_t)g.k * (g.n - g.k);
   if (lev > 0 && tcnt > 0) {
     auto& d = h->L[lev];
     const size_t fi = h->fo(i);
@@ -934,6 +962,22 @@ int hss2d_export_inverse(const hss2d_matrix* H, int32_t box, double* FI, double*
       HSS_CUDA(cudaMemcpy(dst, d.fd[which].p + fi * cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost));
     }
   };
+  if (h->cplx) {
+    // the complex blocks (interleaved) out of their real embeddings
+    auto fetch_c = [&](int which, int nn, double* dst) {
+      if (!dst) return;
+      std::vector<double> t((size_t)nn * nn);
+      fetch(which, t.size(), t.data());
+      for (int c = 0; c < nn / 2; ++c)
+        for (int r = 0; r < nn / 2; ++r) {
+          dst[2 * (r + (size_t)c * (nn / 2))] = t[2 * r + (size_t)(2 * c) * nn];
+          dst[2 * (r + (size_t)c * (nn / 2)) + 1] = t[2 * r + 1 + (size_t)(2 * c) * nn];
+        }
+    };
+    fetch_c(0, g.n, FI);
+    if (lev > 0) fetch_c(1, g.k, E);
+    return HSS_OK;
+  }
   fetch(0, (size_t)g.n * g.n, FI);
   if (lev > 0) fetch(1, (size_t)g.k * g.k, E);
   HSS_CATCH
@@ -953,6 +997,73 @@ int hss2d_bicgstab(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x,
   HSS_CUDA(cudaMemcpyAsync(x, dx.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   HSS_CUDA(cudaStreamSynchronize(h->stream));
   if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss2d_gmres(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x, int32_t nrhs, double tol,
+                int32_t restart, int32_t maxit, double* relres, int32_t* iters) {
+  HSS_TRY
+  HSS_REQUIRE(A && A->impl && f && x, HSS_ERR_ARG, "NULL argument");
+  HSS_REQUIRE(nrhs >= 1, HSS_ERR_ARG, "nrhs must be >= 1");
+  HSS2D* h = A->impl;
+  const size_t cnt = (size_t)h->geo.N * nrhs;
+  DevBuf<double> df(cnt), dx(cnt);
+  HSS_CUDA(cudaMemcpyAsync(df.p, f, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int it = 0;
+  gmres_device(*h, M ? M->impl : nullptr, df.p, dx.p, nrhs, tol, restart, maxit, relres, &it);
+  HSS_CUDA(cudaMemcpyAsync(x, dx.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  HSS_CUDA(cudaStreamSynchronize(h->stream));
+  if (iters) *iters = it;
+  HSS_CATCH
+}
+
+int hss2d_proxy_points(const hss2d_params* p, int32_t box, int32_t n_src, double* xy, int32_t cap, int32_t* count) {
+  HSS_TRY
+  HSS_REQUIRE(p && xy && count && cap >= 0 && n_src >= 0, HSS_ERR_ARG, "proxy points: bad arguments");
+  HSS_REQUIRE(p->Ng > 0 && p->npan > 1 && (p->npan & (p->npan - 1)) == 0, HSS_ERR_ARG,
+              "npan must be a power of two >= 2 and Ng > 0");
+  const int depth = (int)std::lround(2.0 * (std::log((double)p->npan) / std::log(2.0) - 1.0) + 3.0) - 1;
+  HSS_REQUIRE(box >= 0 && box < (1 << (depth + 1)) - 1, HSS_ERR_ARG, "box out of range");
+  int lev = 0;
+  while (((1 << (lev + 1)) - 1) <= box) ++lev;
+  // the box centre by the alternating bisection (x split on even levels, y on odd)
+  double cx = 0.0, cy = 0.0;
+  int path[32], np = 0;
+  for (int b = box; b > 0; b = (b - 1) / 2) path[np++] = b;
+  for (int l = 0, q = np - 1; q >= 0; ++l, --q) {
+    const double d = 0.5 * std::ldexp(1.0, -(l / 2));
+    const bool first = (path[q] % 2) == 1;  // child 2b + 1
+    if (l % 2 == 0) cx += first ? -d : d;
+    else cy += first ? d : -d;
+  }
+  std::vector<double> px, py;
+  level_proxy(*p, lev, cx, cy, n_src, px, py);
+  *count = (int32_t)px.size();
+  HSS_REQUIRE((int)px.size() <= cap, HSS_ERR_ARG, "proxy points: more points than cap");
+  for (size_t q = 0; q < px.size(); ++q) {
+    xy[q] = px[q];
+    xy[cap + q] = py[q];
+  }
+  HSS_CATCH
+}
+
+int hss2d_kernel_residual_rows(hss2d_matrix* H, int64_t row0, int64_t nrows, const double* f, const double* x,
+                               int32_t nrhs, double* relres) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && f && x && relres && nrhs >= 1, HSS_ERR_ARG, "kernel residual: bad arguments");
+  auto* h = H->impl;
+  HSS_REQUIRE(h->tree_built, HSS_ERR_STATE, "kernel residual before the tree is built");
+  const int u = h->cplx ? 2 : 1;
+  const long long N = h->geo.N;
+  HSS_REQUIRE(row0 >= 0 && nrows >= 1 && (row0 + nrows) * u <= N, HSS_ERR_ARG, "kernel residual: rows out of range");
+  std::vector<double> ufull((size_t)N * nrhs, 0.0);
+  kernel_matvec_host(h->pts, h->kdev, {KmvP{(int)(u * row0), (int)(u * nrows), 0, (int)N, nullptr, 0, nullptr, 0}}, N,
+                     x, ufull.data(), nrhs, h->stream);
+  const long long m = u * nrows;
+  std::vector<double> ur((size_t)m * nrhs);
+  for (int c = 0; c < nrhs; ++c)
+    std::memcpy(ur.data() + (size_t)c * m, ufull.data() + (size_t)c * N + u * row0, m * sizeof(double));
+  *relres = host_relres(f, ur.data(), m, nrhs);
   HSS_CATCH
 }
 

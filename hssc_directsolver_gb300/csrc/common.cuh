@@ -48,12 +48,28 @@ inline void check_launch(const char* what) {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-// Device copy of hss_kernel_params with derived constants.
+// Helmholtz constants: s = h^2 kh^2 / 4 (the imaginary factor of the off-diagonal
+// entries), w = 1 + kh^2 (i/4) dr (the diagonal) and the weights 2 exp(-(j 0.3)^2),
+// j = 0..21, of the Hankel-integral trapezoid rule (j = 0 unused).  The weights travel in
+// the kernel parameters, so no per-device state has to be uploaded before a launch.
+constexpr int kHankelNodes = 21;
+constexpr double kHankelStep = 0.3;
+struct HelmDev {
+  double kh, s, w_re, w_im;
+  double hw[kHankelNodes + 1];
+};
+HelmDev make_helm_dev(const hss_kernel_params& kp);
+
+// Device copy of hss_kernel_params with derived constants.  HSS_SL_H_2D blocks of the HSS
+// solvers are generated in the real 2 x 2 embedding (point-table entries 2i and 2i + 1 are
+// the real and imaginary components of point i): entry (t, s) is Re K for (even, even) and
+// (odd, odd), Im K for (odd, even) and -Im K for (even, odd).
 struct KernelDev {
   int flag;
   double h2half;  // h*h*0.5
   double b_alpha, b_x0, b_y0, b_isig;
   double c_alpha, c_x0, c_y0, c_isig;
+  HelmDev helm;
 };
 
 inline KernelDev make_kernel_dev(const hss_kernel_params& p) {
@@ -62,6 +78,7 @@ inline KernelDev make_kernel_dev(const hss_kernel_params& p) {
   k.h2half = p.h * p.h * 0.5;
   k.b_alpha = p.b_alpha; k.b_x0 = p.b_x0; k.b_y0 = p.b_y0; k.b_isig = p.b_isig;
   k.c_alpha = p.c_alpha; k.c_x0 = p.c_x0; k.c_y0 = p.c_y0; k.c_isig = p.c_isig;
+  k.helm = make_helm_dev(p);
   return k;
 }
 

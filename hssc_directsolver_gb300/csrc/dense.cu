@@ -2106,6 +2106,161 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
   id_finish(p, acc, l, jdone, sh, shi);
 }
 
+// The ID of a complex block through its real 2 x 2 embedding E(A) (m = 2 x rows, n = 2 x
+// columns, column pairs (2c, 2c + 1) = complex column c): the pivoted QR moves the pair whose
+// first column has the largest exact trailing norm to the front (the lowest pair within a
+// factor 1 - 2^-14 of the largest: ties of mirror-symmetric boxes resolve by index, not by
+// rounding) and reflects both columns.  The two columns of a pair are a and i a, orthogonal and of equal
+// norm, so the pivot order over pairs, the rank counted in pairs (|R_{2t,2t}| = |R_tt| of the
+// complex QR) and T = R11 \ R12 = E(T) are those of the complex ID (Common/ID.m:40-65 on a
+// complex A).  perm is the real column permutation (pairs kept together), *rank is in real
+// columns (twice the complex rank).  The randomized posterior check draws its real unit
+// vectors over complex columns (entry of complex column c at counter c), which E maps to
+// (x_c, 0) pairs.
+__device__ void id_finish_pairs(const IdP& p, double acc, int lp, double* sh, int* shi) {
+  const unsigned long long seed = p.seed;
+  const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  double* W = p.W;
+  double Rmx = (lp > 0) ? fabs(W[0]) * acc : 0.0;
+  auto count_pairs = [&](double thr) {
+    int cnt = 0;
+    for (int t = tid; t < lp; t += 256) cnt += (fabs(W[2 * t + (size_t)(2 * t) * m]) > thr) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    __syncthreads();
+    if (lane == 0) shi[w] = cnt;
+    __syncthreads();
+    int t = 0;
+    for (int i = 0; i < 8; ++i) t += shi[i];
+    __syncthreads();
+    return t;
+  };
+  int kc = (lp > 0) ? count_pairs(Rmx) : 0;
+  id_trisolve(W, m, n, 2 * kc, p.T);
+  __syncthreads();
+  int draw = 0;
+  double* x = p.x;
+  double* y = p.y;
+  double* t1 = p.y + m;
+  while (kc < lp) {
+    const int k = 2 * kc, r = n - k;
+    const unsigned long long st0 = ((unsigned long long)p.problem << 8) | (unsigned)(draw & 0xFF);
+    const unsigned long long st1 = ((unsigned long long)p.problem << 8) | (unsigned)((draw + 1) & 0xFF);
+    double pa = 0.0, pb = 0.0;
+    for (int i = tid; i < r; i += 256) {
+      double a = 0.0, b = 0.0;
+      if ((i & 1) == 0) {
+        const int c = p.perm[k + i] >> 1;
+        a = rng_uniform(seed, st0, c);
+        b = rng_uniform(seed, st1, c);
+      }
+      x[i] = a; x[n + i] = b;
+      pa += a * a; pb += b * b;
+    }
+    const double na = sqrt(block_sum256(pa, sh));
+    const double nb = sqrt(block_sum256(pb, sh));
+    for (int i = tid; i < r; i += 256) { x[i] /= na; x[n + i] /= nb; }
+    __syncthreads();
+    draw += 2;
+    const double e = id_rand_error(p, k, p.T, x, y, t1, sh);
+    const double nr = id_rand_norm(p, k, x + n, y, sh);
+    if (!(e > nr * acc)) break;
+    Rmx = 0.75 * Rmx;
+    kc = count_pairs(Rmx);
+    id_trisolve(W, m, n, 2 * kc, p.T);
+    __syncthreads();
+    if (draw > 250) break;
+  }
+  if (tid == 0) {
+    *p.rank = 2 * kc;
+    if (p.stat) {
+      p.stat[0] = 0;
+      p.stat[1] = 2 * lp;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_id_pairs(const IdP* __restrict__ P, double acc) {
+  const IdP p = P[blockIdx.x];
+  const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int lp = min(m, n) / 2;
+  double* W = p.W;
+  extern __shared__ double s_dyn[];
+  double* norms = s_dyn;  // n
+  __shared__ double sh[8];
+  __shared__ double hs3[3];
+  __shared__ double shv[8];
+  __shared__ int shi[8];
+  for (long long e = tid; e < (long long)m * n; e += 256) W[e] = p.A[e];
+  for (int c = tid; c < n; c += 256) p.perm[c] = c;
+  __syncthreads();
+  for (int c = w; c < n; c += 8) {
+    double d = 0.0;
+    for (int i = lane; i < m; i += 32) { const double v = W[i + (size_t)c * m]; d += v * v; }
+    d = warp_sum(d);
+    if (lane == 0) norms[c] = d;
+  }
+  __syncthreads();
+  for (int t = 0; t < lp; ++t) {
+    double best = -1.0;
+    int bi = INT_MAX;
+    for (int q = t + tid; q < n / 2; q += 256) {
+      const double v = norms[2 * q];
+      if (v > best) { best = v; bi = q; }
+    }
+    block_argmax256(best, bi, shv, shi);
+    // pivot ties: the lowest pair whose norm is within a factor 1 - 2^-14 of the largest
+    // (mirror-symmetric boxes have pairs of equal norm up to rounding)
+    const double thr = __dadd_rn(best, -__dmul_rn(best, 0x1.0p-14));
+    double cand = -1.0;
+    int ci = INT_MAX;
+    for (int q = t + tid; q < n / 2; q += 256)
+      if (norms[2 * q] >= thr) { cand = 1.0; ci = q; break; }
+    block_argmax256(cand, ci, shv, shi);
+    bi = (ci == INT_MAX) ? t : ci;
+    if (bi != t) {
+      for (int e = tid; e < 2 * m; e += 256) {
+        const int i = e % m, h = e / m;
+        const size_t a = i + (size_t)(2 * t + h) * m, b = i + (size_t)(2 * bi + h) * m;
+        const double u = W[a];
+        W[a] = W[b];
+        W[b] = u;
+      }
+      if (tid < 2) {
+        const int a = 2 * t + tid, b = 2 * bi + tid;
+        const int u = p.perm[a]; p.perm[a] = p.perm[b]; p.perm[b] = u;
+        const double v = norms[a]; norms[a] = norms[b]; norms[b] = v;
+      }
+    }
+    __syncthreads();
+    for (int j = 2 * t; j < 2 * t + 2; ++j) {
+      double part = 0.0;
+      for (int i = j + 1 + tid; i < m; i += 256) { const double v = W[i + (size_t)j * m]; part += v * v; }
+      const double xn2 = block_sum256(part, sh);
+      double tau, beta, scal;
+      householder_scalars(W[j + (size_t)j * m], xn2, hs3, tau, beta, scal);
+      for (int i = j + 1 + tid; i < m; i += 256) W[i + (size_t)j * m] *= scal;
+      __syncthreads();
+      if (tid == 0) W[j + (size_t)j * m] = beta;
+      for (int c = j + 1 + w; c < n; c += 8) {
+        double d = W[j + (size_t)c * m] * (lane == 0 ? 1.0 : 0.0);
+        for (int i = j + 1 + lane; i < m; i += 32) d += W[i + (size_t)j * m] * W[i + (size_t)c * m];
+        d = warp_sum(d) * tau;
+        if (lane == 0) W[j + (size_t)c * m] -= d;
+        double nn = 0.0;
+        for (int i = j + 1 + lane; i < m; i += 32) {
+          const double v = W[i + (size_t)c * m] - d * W[i + (size_t)j * m];
+          W[i + (size_t)c * m] = v;
+          nn += v * v;
+        }
+        nn = warp_sum(nn);
+        if (lane == 0) norms[c] = nn;
+      }
+      __syncthreads();
+    }
+  }
+  id_finish_pairs(p, acc, lp, sh, shi);
+}
+
 // Sum of a double-float value over a 256-thread block (xor butterfly, then the eight
 // warp sums in order); every thread gets the same (h, l).
 __device__ __forceinline__ void block_sum256_df(float& h, float& l, float* shh, float* shl) {
@@ -2523,6 +2678,13 @@ void gauss_batched(const GaussP* dP, int batch, long long maxEntries, cudaStream
   const int gx = std::min(ceil_div(maxEntries, 256), 1024);
   k_gauss<<<dim3(gx, batch), 256, 0, s>>>(dP, maxEntries);
   check_launch("k_gauss");
+}
+
+void id_pairs_batched(const IdP* dP, int batch, int maxn, double acc, cudaStream_t s) {
+  if (batch <= 0) return;
+  HSS_REQUIRE(maxn <= 4096 && maxn % 2 == 0, HSS_ERR_ARG, "pair ID: at most 4096 real columns, even");
+  k_id_pairs<<<batch, 256, 4096 * sizeof(double), s>>>(dP, acc);
+  check_launch("k_id_pairs");
 }
 
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {

@@ -135,6 +135,9 @@ constexpr int ID_QR_ONLY = -2;
 // df: the pivoted QR in double-float arithmetic (k_id_adaptive_df), rank / T / check in FP64
 void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s, bool df = false);
 void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s);
+// The complex ID through the real 2 x 2 embedding (m, n real, pairs of columns pivoted
+// together; *rank and T in real columns); maxn <= 4096 real columns.
+void id_pairs_batched(const IdP* dP, int batch, int maxn, double acc, cudaStream_t s);
 
 // Householder QR with column pivoting of W (m x l, ld ldw; overwritten) and the
 // explicit thin Q (m x min(m,l), ld ldq); D = |diag R|.  Same pivots and

@@ -93,6 +93,34 @@ __global__ void k_copy2d(int nb, int m, int n, const S* __restrict__ src, long l
   }
 }
 
+// Tikhonov rows of a complex tree's interpolation least squares (one block per problem):
+// below the p proxy rows of [K11 | K21] the k x n block [lam I | 0], lam = 2^-40 ||K11||_F
+// (K11 = the first k columns; the embedding doubles the squared Frobenius norm).
+struct TikP {
+  double* A;
+  int p, n, k, ld;
+};
+__global__ void k_tikhonov_rows(const TikP* __restrict__ P) {
+  const TikP q = P[blockIdx.x];
+  __shared__ double sh[256];
+  double ss = 0.0;
+  for (long long e = threadIdx.x; e < (long long)q.p * q.k; e += 256) {
+    const double v = q.A[(e % q.p) + (size_t)(e / q.p) * q.ld];
+    ss += v * v;
+  }
+  sh[threadIdx.x] = ss;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double lam = 0x1.0p-40 * sqrt(0.5 * sh[0]);
+  for (long long e = threadIdx.x; e < (long long)q.k * q.n; e += 256) {
+    const int r = (int)(e % q.k), c = (int)(e / q.k);
+    q.A[q.p + r + (size_t)c * q.ld] = (c == r) ? lam : 0.0;
+  }
+}
+
 // transpose copy: dst_b(j, i) = src_b(i, j), src m x n
 __global__ void k_transpose(int nb, int m, int n, const double* __restrict__ src, long long sstride, int lds,
                             double* __restrict__ dst, long long dstride, int ldd) {
@@ -325,18 +353,196 @@ template struct SolvePlan<float>;
 // ---------------------------------------------------------------------------
 // build_tree
 // ---------------------------------------------------------------------------
+// The ID step of a kh > 0 tree level (LOCAL_Non_Preset_Skeleton_Info,
+// HSS2D_build_tree_nsym.m:614-627): per box, the complex ID of K(proxies, box) at tolerance acc
+// through the pair-pivoted QR of its real embedding, problem 2 box of the shared random
+// stream.  Returns the complex column order and the rank per box; the raw T of each box
+// (2k x 2(n - k) real, the embedding of the complex T) is kept in id_T[lev].
+void HSS2D::id_level(int lev, const std::vector<std::vector<int>>& boxes, const std::vector<std::vector<double>>& px,
+                     const std::vector<std::vector<double>>& py, std::vector<std::vector<int>>& perm_out,
+                     std::vector<int>& k_out) {
+  const int nb = (int)boxes.size();
+  const int n = (int)boxes[0].size(), n2 = 2 * n;
+  HSS_REQUIRE(n2 <= 4096, HSS_ERR_ARG, "ID level: more than 2048 points in a box");
+  // temporary point table: per box its sources, then its proxies; each point twice (the two
+  // components of the embedding)
+  std::vector<long long> soff(nb + 1, 0), qoff(nb + 1, 0);
+  long long npt = 0;
+  for (int i = 0; i < nb; ++i) {
+    HSS_REQUIRE((int)boxes[i].size() == n, HSS_ERR_ARG, "ID level: non-uniform box sizes");
+    HSS_REQUIRE((int)px[i].size() >= 1, HSS_ERR_ARG, "ID level: box without proxies");
+    soff[i] = npt;
+    npt += n;
+    qoff[i] = npt;
+    npt += (long long)px[i].size();
+  }
+  HSS_REQUIRE(2 * npt < (1LL << 31), HSS_ERR_ARG, "ID level: point table exceeds 2^31 entries");
+  std::vector<double> hx(2 * npt), hy(2 * npt), zero(2 * npt, 0.0);
+  std::vector<int> ti, si;
+  std::vector<long long> aoff(nb + 1, 0);
+  for (int i = 0; i < nb; ++i) {
+    for (int j = 0; j < n; ++j)
+      for (int a = 0; a < 2; ++a) {
+        const size_t e = 2 * (size_t)(soff[i] + j) + a;
+        hx[e] = geo.X[2 * (size_t)boxes[i][j]];
+        hy[e] = geo.X[2 * (size_t)boxes[i][j] + 1];
+      }
+    const int p = (int)px[i].size();
+    for (int q = 0; q < p; ++q)
+      for (int a = 0; a < 2; ++a) {
+        const size_t e = 2 * (size_t)(qoff[i] + q) + a;
+        hx[e] = px[i][q];
+        hy[e] = py[i][q];
+      }
+    aoff[i + 1] = aoff[i] + (long long)(2 * p) * n2;
+  }
+  // index arrays: rows (proxies) then columns (sources) per box, in embedded entries
+  std::vector<long long> ioff(nb + 1, 0);
+  std::vector<int> idx;
+  for (int i = 0; i < nb; ++i) {
+    ioff[i] = (long long)idx.size();
+    for (long long q = 0; q < (long long)px[i].size(); ++q)
+      for (int a = 0; a < 2; ++a) idx.push_back((int)(2 * (qoff[i] + q) + a));
+    for (int j = 0; j < n; ++j)
+      for (int a = 0; a < 2; ++a) idx.push_back((int)(2 * (soff[i] + j) + a));
+  }
+  PointTable tp;
+  tp.upload(hx, hy, zero, zero, zero, zero, prm.kp, stream);
+  DevBuf<int> didx;
+  didx.upload(idx, stream);
+  DevBuf<double> A(aoff[nb]), W(aoff[nb]);
+  std::vector<KgenP<double>> kg(nb);
+  long long maxe = 0;
+  int maxm = 0;
+  for (int i = 0; i < nb; ++i) {
+    const int m2 = 2 * (int)px[i].size();
+    kg[i] = KgenP<double>{didx.p + ioff[i], didx.p + ioff[i] + m2, m2, n2, A.p + aoff[i], m2, 0};
+    maxe = std::max(maxe, (long long)m2 * n2);
+    maxm = std::max(maxm, m2);
+  }
+  for (int off = 0; off < nb; off += 65535) {
+    const int cnt = std::min(65535, nb - off);
+    DevBuf<KgenP<double>> dkg(cnt);
+    HSS_CUDA(cudaMemcpyAsync(dkg.p, kg.data() + off, cnt * sizeof(KgenP<double>), cudaMemcpyHostToDevice, stream));
+    kgen_batched<double>(dkg.p, cnt, maxe, view(tp), kdev, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+  // adaptive pair ID of every box
+  DevBuf<int> perm((size_t)nb * n2), rank(nb);
+  DevBuf<double> T((size_t)nb * n2 * n2), xw((size_t)nb * 2 * n2), yw((size_t)nb * (maxm + n2));
+  std::vector<IdP> ip(nb);
+  for (int i = 0; i < nb; ++i) {
+    IdP q{};
+    q.A = A.p + aoff[i];
+    q.W = W.p + aoff[i];
+    q.m = 2 * (int)px[i].size();
+    q.n = n2;
+    q.perm = perm.p + (size_t)i * n2;
+    q.rank = rank.p + i;
+    q.T = T.p + (size_t)i * n2 * n2;
+    q.force_k = -1;
+    q.x = xw.p + (size_t)i * 2 * n2;
+    q.y = yw.p + (size_t)i * (maxm + n2);
+    q.problem = 2 * ((1 << lev) - 1 + i);  // 2 * box (heap index) of the shared random stream
+    q.steps_hint = 0;
+    q.seed = prm.seed;
+    ip[i] = q;
+  }
+  for (int off = 0; off < nb; off += 65535) {
+    const int cnt = std::min(65535, nb - off);
+    DevBuf<IdP> dip(cnt);
+    HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data() + off, cnt * sizeof(IdP), cudaMemcpyHostToDevice, stream));
+    id_pairs_batched(dip.p, cnt, n2, prm.acc, stream);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+  std::vector<int> hr, hp;
+  download(hr, rank.p, nb, stream);
+  download(hp, perm.p, (size_t)nb * n2, stream);
+  std::vector<double> ht;
+  download(ht, T.p, (size_t)nb * n2 * n2, stream);
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  perm_out.assign(nb, std::vector<int>(n));
+  k_out.assign(nb, 0);
+  // raw T per box (2k x 2(n - k), ld 2k), packed
+  std::vector<double>& keep = id_T[lev];
+  std::vector<long long>& toff = id_Toff[lev];
+  keep.clear();
+  toff.assign(nb + 1, 0);
+  for (int i = 0; i < nb; ++i) {
+    const int k2 = hr[i], nr2 = n2 - k2;
+    HSS_REQUIRE(k2 % 2 == 0 && k2 >= 0 && k2 <= n2, HSS_ERR_CUDA, "pair ID: odd rank");
+    for (int q = 0; q < n; ++q) {
+      const int c = hp[(size_t)i * n2 + 2 * q];
+      HSS_REQUIRE(c % 2 == 0 && hp[(size_t)i * n2 + 2 * q + 1] == c + 1, HSS_ERR_CUDA, "pair ID split a pair");
+      perm_out[i][q] = c / 2;
+    }
+    k_out[i] = k2 / 2;
+    toff[i + 1] = toff[i] + (long long)k2 * nr2;
+    for (int c = 0; c < nr2; ++c)
+      for (int r = 0; r < k2; ++r) keep.push_back(ht[(size_t)i * n2 * n2 + r + (size_t)c * n2]);
+  }
+}
+
+// The real 2 x 2 embedding of a complex tree level: point i becomes the entries 2i, 2i + 1
+// (real and imaginary components), so n, k and the proxy counts double and every index
+// array interleaves the two components.
+static void embed_level(Level2Geom& g) {
+  auto dbl = [](std::vector<int>& v) {
+    std::vector<int> o(2 * v.size());
+    for (size_t q = 0; q < v.size(); ++q) {
+      o[2 * q] = 2 * v[q];
+      o[2 * q + 1] = 2 * v[q] + 1;
+    }
+    v.swap(o);
+  };
+  dbl(g.J);
+  dbl(g.Isrc);
+  dbl(g.IsrcJ);
+  dbl(g.proxy);
+  for (auto& o : g.poff) o *= 2;
+  g.n *= 2;
+  g.k *= 2;
+  g.p *= 2;
+}
+
 void HSS2D::build_tree() {
   using clk = std::chrono::steady_clock;
   auto t0 = clk::now();
-  build_tree_geometry(prm, geo);
+  cplx = (prm.kp.flag == HSS_SL_H_2D);
+  kdev = make_kernel_dev(prm.kp);
+  if (cplx) {
+    HSS_REQUIRE(prm.interform == HSS_INTER_DENSE, HSS_ERR_ARG, "kh > 0: dense interpolation operators only");
+    HSS_REQUIRE(prm.transinv == 0, HSS_ERR_ARG, "kh > 0: transinv 0 only");
+    HSS_REQUIRE(prm.precision == HSS_PREC_FP64 || prm.precision == HSS_PREC_MIXED, HSS_ERR_ARG,
+                "kh > 0: HSS_PREC_FP64 or HSS_PREC_MIXED");
+  }
+  if (prm.proxy_rule == HSS_PROXY_RAND)
+    HSS_REQUIRE(prm.interform == HSS_INTER_DENSE, HSS_ERR_ARG, "'rand' proxies: dense interpolation operators only");
+  id_T.clear();
+  id_Toff.clear();
+  IdLevelFn fn = [this](int lev, const std::vector<std::vector<int>>& b, const std::vector<std::vector<double>>& x,
+                        const std::vector<std::vector<double>>& y, std::vector<std::vector<int>>& perm,
+                        std::vector<int>& k) { id_level(lev, b, x, y, perm, k); };
+  build_tree_geometry(prm, geo, cplx ? fn : IdLevelFn());
   auto t1 = clk::now();
   phase_s[0] = std::chrono::duration<double>(t1 - t0).count();
-  kdev = make_kernel_dev(prm.kp);
   const long long N = geo.N;
   const size_t npts = (size_t)N + geo.proxy_x.size();
-  std::vector<double> hx(npts), hy(npts), zero(npts, 0.0);
-  for (long long i = 0; i < N; ++i) { hx[i] = geo.X[2 * i]; hy[i] = geo.X[2 * i + 1]; }
-  for (size_t i = 0; i < geo.proxy_x.size(); ++i) { hx[N + i] = geo.proxy_x[i]; hy[N + i] = geo.proxy_y[i]; }
+  const int rep = cplx ? 2 : 1;  // table entries per point
+  std::vector<double> hx(rep * npts), hy(rep * npts), zero(rep * npts, 0.0);
+  for (size_t i = 0; i < npts; ++i) {
+    const double x = i < (size_t)N ? geo.X[2 * i] : geo.proxy_x[i - N];
+    const double y = i < (size_t)N ? geo.X[2 * i + 1] : geo.proxy_y[i - N];
+    for (int a = 0; a < rep; ++a) {
+      hx[rep * i + a] = x;
+      hy[rep * i + a] = y;
+    }
+  }
+  if (cplx) {
+    for (auto& g : geo.levels) embed_level(g);
+    geo.N = 2 * N;
+  }
+  ng_pts = rep * prm.Ng * prm.Ng;
   pts.upload(hx, hy, zero, zero, zero, zero, prm.kp, stream);
   L.clear();
   L.resize(geo.depth + 1);
@@ -354,10 +560,58 @@ void HSS2D::build_tree() {
   qrank_dn.assign(geo.depth + 1, {});
   auto t2 = clk::now();
   phase_s[1] = std::chrono::duration<double>(t2 - t1).count();
-  for (int lev = geo.depth; lev >= 1; --lev) compute_T(lev);
+  for (int lev = geo.depth; lev >= 1; --lev) {
+    if (geo.levels[lev].id_level) id_T_level(lev);
+    else compute_T(lev);
+  }
   HSS_CUDA(cudaStreamSynchronize(stream));
+  id_T.clear();
+  id_Toff.clear();
   phase_s[2] = std::chrono::duration<double>(clk::now() - t2).count();
   tree_built = true;
+}
+
+// T of an ID level: rows and columns of each box's raw ID T in the tree's order (complex
+// indices, each an embedded 2 x 2 block; zero rows for promoted points); T_dn = T_up
+// (LOCAL_Non_Preset_Skeleton_Info :656).  A complex tree keeps T_dn conjugated, E(conj T_dn)
+// (entries of odd row xor odd column negated), as the least squares of the other levels leave
+// it: its real transpose is then E(T_dn^T), the plain transpose the HSS formulas apply.
+void HSS2D::id_T_level(int lev) {
+  auto& g = geo.levels[lev];
+  auto& d = L[lev];
+  const int nb = g.nb, k = g.k, nr = g.n - g.k, kc = k / 2, nrc = nr / 2;
+  d.Tup.alloc((size_t)nb * k * std::max(nr, 1));
+  d.Tdn.alloc((size_t)nb * k * std::max(nr, 1));
+  d.TdnT.alloc((size_t)nb * k * std::max(nr, 1));
+  if (nr == 0 || k == 0) return;
+  const std::vector<double>& raw = id_T.at(lev);
+  const std::vector<long long>& toff = id_Toff.at(lev);
+  std::vector<double> tu((size_t)nb * k * nr), td((size_t)nb * k * nr), tt((size_t)nb * k * nr);
+  for (int i = 0; i < nb; ++i) {
+    const int* rows = g.id_rows.data() + (size_t)i * kc;
+    const int* cols = g.id_cols.data() + (size_t)i * nrc;
+    const double* src = raw.data() + toff[i];
+    // rows of the raw T: twice the box's own rank (the rows that are not promoted points)
+    const int kraw = 2 * (int)std::count_if(rows, rows + kc, [](int v) { return v >= 0; });
+    HSS_REQUIRE((long long)kraw * (g.n - kraw) == toff[i + 1] - toff[i], HSS_ERR_ARG, "ID level: raw T size");
+    double* dst = tu.data() + (size_t)i * k * nr;
+    double* ddn = td.data() + (size_t)i * k * nr;
+    double* dtt = tt.data() + (size_t)i * k * nr;
+    for (int c = 0; c < nr; ++c)
+      for (int r = 0; r < k; ++r) {
+        const int rr = rows[r / 2];
+        const double v = (rr < 0) ? 0.0 : src[(2 * rr + (r & 1)) + (size_t)(2 * cols[c / 2] + (c & 1)) * kraw];
+        const double vc = ((r ^ c) & 1) ? -v : v;  // E(conj T)
+        dst[r + (size_t)c * k] = v;
+        ddn[r + (size_t)c * k] = vc;
+        dtt[c + (size_t)r * nr] = vc;
+      }
+  }
+  HSS_CUDA(cudaMemcpyAsync(d.Tup.p, tu.data(), tu.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  HSS_CUDA(cudaMemcpyAsync(d.Tdn.p, td.data(), td.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  HSS_CUDA(cudaMemcpyAsync(d.TdnT.p, tt.data(), tt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  HSS_CUDA(cudaStreamSynchronize(stream));
+  qlev[lev] = nr;
 }
 
 void HSS2D::compute_T(int lev) {
@@ -368,34 +622,56 @@ void HSS2D::compute_T(int lev) {
   d.Tdn.alloc((size_t)nb * k * std::max(nr, 1));
   d.TdnT.alloc((size_t)nb * k * std::max(nr, 1));
   if (nr == 0 || k == 0) return;
-  HSS_REQUIRE(p >= k, HSS_ERR_ARG, "proxy set smaller than skeleton: least squares is underdetermined");
+  // per factor box: its proxy count (the 'rand' rule samples a different set per box); a
+  // complex tree's systems carry k Tikhonov rows under the proxy rows (k_tikhonov_rows)
+  const int tk = cplx ? k : 0;
+  std::vector<int> pb(nb);
+  std::vector<long long> aoff(2 * nb + 1, 0);
+  for (int i = 0; i < nb; ++i) {
+    pb[i] = g.poff[i + 1] - g.poff[i];
+    HSS_REQUIRE(pb[i] >= k, HSS_ERR_ARG, "proxy set smaller than skeleton: least squares is underdetermined");
+    aoff[2 * i + 1] = aoff[2 * i] + (long long)(pb[i] + tk) * n;
+    aoff[2 * i + 2] = aoff[2 * i + 1] + (long long)(pb[i] + tk) * n;
+  }
   const int batch = 2 * nb;
-  DevBuf<double> A((size_t)batch * p * n);
-  // kernel blocks: problem 2i = [K(Xp, X_sk) | K(Xp, X_rs)], 2i+1 = K(X_src[J], Xp)^T
+  DevBuf<double> A(aoff[batch]);
+  // kernel blocks: problem 2i = [K(Xp, X_sk) | K(Xp, X_rs)], 2i+1 = K(X_src[J], Xp)^T (the real
+  // transpose: of a complex tree's embedded blocks E(K)^T = E(K^H), so its T_dn comes out
+  // conjugated, E(conj T_dn), whose real transpose is the E(T_dn^T) the HSS formulas use)
   std::vector<KgenP<double>> kg(batch);
   for (int i = 0; i < nb; ++i) {
-    kg[2 * i] = KgenP<double>{d.proxy.p + (size_t)i * p, d.IsrcJ.p + (size_t)i * n, p, n,
-                              A.p + (size_t)(2 * i) * p * n, p, 0};
-    kg[2 * i + 1] = KgenP<double>{d.IsrcJ.p + (size_t)i * n, d.proxy.p + (size_t)i * p, n, p,
-                                  A.p + (size_t)(2 * i + 1) * p * n, p, 1};
+    const int* pr = d.proxy.p + g.poff[i];
+    kg[2 * i] = KgenP<double>{pr, d.IsrcJ.p + (size_t)i * n, pb[i], n, A.p + aoff[2 * i], pb[i] + tk, 0};
+    kg[2 * i + 1] = KgenP<double>{d.IsrcJ.p + (size_t)i * n, pr, n, pb[i], A.p + aoff[2 * i + 1], pb[i] + tk, 1};
   }
   DevBuf<KgenP<double>> dkg(batch);
   HSS_CUDA(cudaMemcpyAsync(dkg.p, kg.data(), batch * sizeof(KgenP<double>), cudaMemcpyHostToDevice, stream));
   kgen_batched<double>(dkg.p, batch, (long long)p * n, view(pts), kdev, stream);
-  DevBuf<double> V((size_t)batch * p * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * k);
+  if (tk > 0) {
+    std::vector<TikP> tp(batch);
+    for (int b = 0; b < batch; ++b) tp[b] = TikP{A.p + aoff[b], pb[b / 2], n, k, pb[b / 2] + tk};
+    DevBuf<TikP> dtp(batch);
+    HSS_CUDA(cudaMemcpyAsync(dtp.p, tp.data(), batch * sizeof(TikP), cudaMemcpyHostToDevice, stream));
+    k_tikhonov_rows<<<batch, 256, 0, stream>>>(dtp.p);
+    check_launch("k_tikhonov_rows");
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  }
+  DevBuf<double> V((size_t)batch * (p + tk) * QR_NB), Tf((size_t)batch * QR_NB * QR_NB), diag((size_t)batch * k);
   if (uses_lowrank(lev)) {
+    HSS_REQUIRE(g.p_uniform, HSS_ERR_ARG, "low-rank T needs the same proxy count in every box");
     diag.zero(stream);
     lowrank_T(lev, A.p, V, Tf, diag);
   } else {
     std::vector<QrP<double>> qp(batch);
     for (int b = 0; b < batch; ++b) {
       double* X = ((b & 1) ? d.Tdn.p : d.Tup.p) + (size_t)(b / 2) * k * nr;
-      qp[b] = QrP<double>{A.p + (size_t)b * p * n, p, n, k, p, V.p + (size_t)b * p * QR_NB,
+      const int pm = pb[b / 2] + tk;
+      qp[b] = QrP<double>{A.p + aoff[b], pm, n, k, pm, V.p + (size_t)b * (p + tk) * QR_NB,
                           Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k, X, k};
     }
     DevBuf<QrP<double>> dqp(batch);
     HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
-    lstsq_batched<double>(dqp.p, batch, p, n, k, stream, dftree());
+    lstsq_batched<double>(dqp.p, batch, p + tk, n, k, stream, dftree());
     HSS_CUDA(cudaStreamSynchronize(stream));
     qlev[lev] = nr;  // a dense T.U is k x nr
   }
@@ -725,7 +1001,7 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
   };
   auto& vin = stage_in<R>();
   auto& vout = stage_out<R>();
-  const int NG = prm.Ng * prm.Ng;
+  const int NG = ng_pts;
   for (int lev = 0; lev <= depth; ++lev) {
     auto& d = L[lev];
     const auto& g = geo.levels[lev];
@@ -966,7 +1242,7 @@ void HSS2D::fwd_prepare(int r) {
   FwdPlan& fp = fwd_plans[r];
   const int depth = geo.depth;
   const long long N = geo.N;
-  const int NG = prm.Ng * prm.Ng;
+  const int NG = ng_pts;
   for (int lev = 0; lev <= depth; ++lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];

@@ -138,6 +138,15 @@ struct HSS2D {
   std::vector<int> qlev;
   std::vector<std::vector<int>> qrank_up, qrank_dn;
 
+  // complex (HSS_SL_H_2D) tree: every block in the real 2 x 2 embedding, vectors interleaved
+  bool cplx = false;
+  int ng_pts = 0;  // vector rows of one leaf panel (Ng^2, twice that for a complex tree)
+  // raw ID T per level while the tree is built (box i at id_Toff[lev][i], 2k x 2(n - k))
+  std::map<int, std::vector<double>> id_T;
+  std::map<int, std::vector<long long>> id_Toff;
+  void id_level(int lev, const std::vector<std::vector<int>>& boxes, const std::vector<std::vector<double>>& px,
+                const std::vector<std::vector<double>>& py, std::vector<std::vector<int>>& perm, std::vector<int>& k);
+  void id_T_level(int lev);
   void build_tree();
   void compute_T(int lev);
   bool uses_lowrank(int lev) const;
@@ -194,6 +203,10 @@ struct HSS2D {
   }
 };
 
+// x = A^-1 f by restarted GMRES right-preconditioned with M^-1 (krylov.cu); complex on a
+// complex tree
+void gmres_device(HSS2D& A, HSS2D* M, const double* f, double* x, int nrhs, double tol, int restart, int maxit,
+                  double* relres, int* iters);
 // x = A^-1 f by BiCGSTAB preconditioned with M^-1 (krylov.cu)
 void bicgstab_device(HSS2D& A, HSS2D* M, const double* f, double* x, int nrhs, double tol, int maxit,
                      double* relres, int* iters);

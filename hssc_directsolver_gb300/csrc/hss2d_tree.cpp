@@ -8,11 +8,14 @@
 //   skeletons          LOCAL_Preset_Skeleton_Info 'bdry' :732-792, orient :794-811
 //   proxies            HSS2D/build_box_proxy.m:52-88 via LOCAL_Build_Proxy :945-949
 //   proxy layers       :360-368
+//   'rand' proxies     LOCAL_Build_Proxy :883-905, LOCAL_random_sampler :964-1001
+//   ID skeletons       :399-412, LOCAL_Non_Preset_Skeleton_Info :614-657 (kh > 0)
 #include "hss2d_tree.h"
 
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <random>
 
 namespace hss {
 
@@ -87,6 +90,48 @@ void box_proxy(double cx, double cy, double colrad, double rowrad, int layers, d
   }
 }
 
+// LOCAL_orient_residual (:805-811): order of points (x[i], y[i]) by the normal coordinate,
+// then stably by the negated tangential one
+static std::vector<int> orient_residual(const std::vector<double>& x, const std::vector<double>& y, int nrm) {
+  const std::vector<double>& a = nrm == 0 ? x : y;
+  const std::vector<double>& b = nrm == 0 ? y : x;
+  std::vector<int> J1, J2;
+  stable_argsort(a, J1);
+  std::vector<double> key2(J1.size());
+  for (size_t i = 0; i < J1.size(); ++i) key2[i] = -b[J1[i]];
+  stable_argsort(key2, J2);
+  std::vector<int> out(J1.size());
+  for (size_t i = 0; i < J1.size(); ++i) out[i] = J1[J2[i]];
+  return out;
+}
+
+// LOCAL_orient_skeleton (:794-802): polar order around (cx, cy) from angle th0, ties by radius
+static std::vector<int> orient_skeleton(const std::vector<double>& x, const std::vector<double>& y, double cx,
+                                        double cy, double th0) {
+  const size_t n = x.size();
+  std::vector<double> th(n), rho(n);
+  for (size_t i = 0; i < n; ++i) {
+    const double dx = x[i] - cx, dy = y[i] - cy;
+    double t = std::atan2(dy, dx);
+    if (t < th0) t = t + 2.0 * M_PI;
+    th[i] = t;
+    rho[i] = std::hypot(dx, dy);
+  }
+  std::vector<int> J1, J2;
+  stable_argsort(rho, J1);
+  std::vector<double> th1(n);
+  for (size_t i = 0; i < n; ++i) th1[i] = th[J1[i]];
+  stable_argsort(th1, J2);
+  std::vector<int> out(n);
+  for (size_t i = 0; i < n; ++i) out[i] = J1[J2[i]];
+  return out;
+}
+
+static void level_orientation(int lev, int& nrm, double& th0) {
+  if (lev % 2 == 0) { nrm = 0; th0 = M_PI / 2; }
+  else { nrm = 1; th0 = 0.0; }
+}
+
 // J (local permutation, skeleton first) and k of one box.
 static void preset_skeleton(const std::vector<double>& X, const std::vector<int>& I_src, double cx,
                             double cy, int lev, double colrad, double rowrad, int layers, double h,
@@ -99,46 +144,99 @@ static void preset_skeleton(const std::vector<double>& X, const std::vector<int>
     const bool b = (std::fabs(x - cx) > (colrad - width)) || (std::fabs(y - cy) > (rowrad - width));
     (b ? sk : rs).push_back(i);
   }
-  int nrm, tan;
+  int nrm;
   double th0;
-  if (lev % 2 == 0) { nrm = 0; tan = 1; th0 = M_PI / 2; }
-  else { nrm = 1; tan = 0; th0 = 0.0; }
-  // residual: sort by normal coordinate, then stably by -tangential
-  std::vector<int> J1, J2;
-  {
-    std::vector<double> key(rs.size());
-    for (size_t i = 0; i < rs.size(); ++i) key[i] = X[2 * (size_t)I_src[rs[i]] + nrm];
-    stable_argsort(key, J1);
-    std::vector<double> key2(rs.size());
-    for (size_t i = 0; i < rs.size(); ++i) key2[i] = -X[2 * (size_t)I_src[rs[J1[i]]] + tan];
-    stable_argsort(key2, J2);
-  }
-  std::vector<int> rs_sorted(rs.size());
-  for (size_t i = 0; i < rs.size(); ++i) rs_sorted[i] = rs[J1[J2[i]]];
-  // skeleton: polar sort around the centre
-  std::vector<double> th(sk.size()), rho(sk.size());
-  for (size_t i = 0; i < sk.size(); ++i) {
-    const double dx = X[2 * (size_t)I_src[sk[i]]] - cx, dy = X[2 * (size_t)I_src[sk[i]] + 1] - cy;
-    double t = std::atan2(dy, dx);
-    if (t < th0) t = t + 2.0 * M_PI;
-    th[i] = t;
-    rho[i] = std::hypot(dx, dy);
-  }
-  stable_argsort(rho, J1);
-  std::vector<double> th1(sk.size());
-  for (size_t i = 0; i < sk.size(); ++i) th1[i] = th[J1[i]];
-  stable_argsort(th1, J2);
+  level_orientation(lev, nrm, th0);
+  std::vector<double> rx(rs.size()), ry(rs.size()), sx(sk.size()), sy(sk.size());
+  for (size_t i = 0; i < rs.size(); ++i) { rx[i] = X[2 * (size_t)I_src[rs[i]]]; ry[i] = X[2 * (size_t)I_src[rs[i]] + 1]; }
+  for (size_t i = 0; i < sk.size(); ++i) { sx[i] = X[2 * (size_t)I_src[sk[i]]]; sy[i] = X[2 * (size_t)I_src[sk[i]] + 1]; }
+  const std::vector<int> Jr = orient_residual(rx, ry, nrm);
+  const std::vector<int> Js = orient_skeleton(sx, sy, cx, cy, th0);
   J.clear();
-  for (size_t i = 0; i < sk.size(); ++i) J.push_back(sk[J1[J2[i]]]);
+  for (int v : Js) J.push_back(sk[v]);
   k = (int)sk.size();
-  for (int v : rs_sorted) J.push_back(v);
+  for (int v : Jr) J.push_back(rs[v]);
 }
 
-void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
+// LOCAL_random_sampler (:964-1001): points within lay h of the box are kept, the others with
+// probability 2^(-lam l) by dyadic distance band l.  The reference resets MATLAB's generator
+// (the Mersenne Twister with its default seed 5489) on every call; the uniforms are that
+// generator's 53-bit doubles (two 32-bit draws, a >> 5 and b >> 6, (a 2^26 + b) 2^-53).
+static void random_sampler(std::vector<double>& px, std::vector<double>& py, double cx, double cy, double colrad,
+                           double rowrad, double lam, int lay, double h) {
+  const size_t n = px.size();
+  if (n == 0) return;
+  std::vector<double> D(n);
+  double rad = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    D[i] = std::fabs(std::min(colrad - std::fabs(px[i] - cx), rowrad - std::fabs(py[i] - cy)));
+    rad = std::max(rad, D[i]);
+  }
+  const double width = lay * h;
+  const int sz = -(int)std::floor(std::log2(width / rad)) + 1;
+  std::vector<char> keep(n);
+  for (size_t i = 0; i < n; ++i) keep[i] = D[i] < width;
+  if (sz > 0) {
+    std::mt19937 gen(5489u);
+    for (size_t i = 0; i < n; ++i) {
+      double Ld;
+      if (D[i] < width) Ld = sz;
+      else Ld = std::min(-std::ceil(std::log2(D[i] / rad)), (double)(sz - 2)) + 1.0;
+      const double P = std::pow(2.0, -lam * (double)(sz - (int)Ld));  // prob(Ld) of :985-990
+      const uint32_t a = gen() >> 5, b = gen() >> 6;
+      const double u = ((double)a * 67108864.0 + (double)b) * (1.0 / 9007199254740992.0);
+      keep[i] = u < P;
+    }
+  }
+  size_t o = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (keep[i]) { px[o] = px[i]; py[o] = py[i]; ++o; }
+  px.resize(o);
+  py.resize(o);
+}
+
+// LOCAL_Build_Proxy 'rand' (:883-905): the box's proxy layers sampled until at least
+// k0 = ceil(2/3 n) (even levels) or ceil(3/4 n) (odd) points remain, each retry sampling the
+// previous sample again with 0.9 lambda.
+static void random_proxy(std::vector<double>& px, std::vector<double>& py, int n_src, double cx, double cy,
+                         double colrad, double rowrad, int lev, int layers, double h, double lambda) {
+  int k0 = (lev % 2 == 0) ? (int)std::ceil((2.0 / 3.0) * n_src) : (int)std::ceil((3.0 / 4.0) * n_src);
+  k0 = std::min(k0, (int)px.size());
+  double lam = lambda;
+  int k = 0, c = 0;
+  while (k0 > k && c < 10) {
+    random_sampler(px, py, cx, cy, colrad, rowrad, lam, layers, h);
+    k = (int)px.size();
+    if (k0 > k) lam = 0.9 * lam;
+    ++c;
+  }
+}
+
+// proxy layers of a level (:360-368): layers + 1 for the Laplace kernel, 2 round(min radius / h)
+// for kh > 0; the root keeps params.layers
+static int proxy_layers(const hss2d_params& prm, int lev, double colrad, double rowrad, double h) {
+  if (lev == 0) return prm.layers;
+  if (prm.kp.flag == HSS_SL_H_2D) return 2 * (int)std::lround(std::min(colrad, rowrad) / h);
+  return prm.layers + 1;
+}
+
+void level_proxy(const hss2d_params& prm, int lev, double cx, double cy, int n_src, std::vector<double>& px,
+                 std::vector<double>& py) {
+  double colrad, rowrad;
+  box_radii(lev, colrad, rowrad);
+  const double h = 2.0 / (double)(prm.Ng * prm.npan);
+  box_proxy(cx, cy, colrad, rowrad, proxy_layers(prm, lev, colrad, rowrad, h), h, px, py);
+  if (prm.proxy_rule == HSS_PROXY_RAND)
+    random_proxy(px, py, n_src, cx, cy, colrad, rowrad, lev, prm.layers, h, prm.lambda > 0 ? prm.lambda : 2.0);
+}
+
+void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id_level) {
   HSS_REQUIRE(prm.Ng > 0 && prm.npan > 1 && (prm.npan & (prm.npan - 1)) == 0, HSS_ERR_ARG,
               "npan must be a power of two >= 2 and Ng > 0");
   HSS_REQUIRE(prm.layers >= 1, HSS_ERR_ARG, "layers must be >= 1");
-  HSS_REQUIRE(prm.kp.flag == HSS_SL_L_2D, HSS_ERR_ARG, "HSS2D supports the SL_L_2D kernel family");
+  HSS_REQUIRE(prm.kp.flag == HSS_SL_L_2D || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
+              "HSS2D takes the SL_L_2D and SL_H_2D kernels");
+  HSS_REQUIRE(prm.proxy_rule == HSS_PROXY_BDRY || prm.proxy_rule == HSS_PROXY_RAND, HSS_ERR_ARG, "unknown proxy rule");
   const int Ng = prm.Ng, np = prm.npan;
   const double hh = 2.0 / (double)(Ng * np);
   const double hp = 2.0 / (double)np;
@@ -195,6 +293,7 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
     T.leaf_panel[b] = pi;
   }
   // upward skeleton pass
+  const bool helm = (prm.kp.flag == HSS_SL_H_2D);
   T.levels.assign(depth + 1, Level2Geom{});
   std::vector<std::vector<int>> I_sk(nb);
   std::vector<std::vector<int>> I_src(nb);
@@ -206,10 +305,11 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
     L.lev = lev;
     L.nb = 1 << lev;
     box_radii(lev, L.colrad, L.rowrad);
-    int lay = prm.layers;
-    if (lev > 0) lay = prm.layers + 1;  // SL_L_2D rule of :360-368
-    L.lay_prox = lay;
+    L.lay_prox = proxy_layers(prm, lev, L.colrad, L.rowrad, hh);
     const int b0 = (1 << lev) - 1;
+    std::vector<std::vector<double>> PX(L.nb), PY(L.nb);
+    std::vector<std::vector<int>> Jall(L.nb);
+    std::vector<int> kall(L.nb, 0);
     for (int i = 0; i < L.nb; ++i) {
       const int b = b0 + i;
       if (lev == depth) {
@@ -221,19 +321,119 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
         I_src[b] = I_sk[2 * b + 1];
         I_src[b].insert(I_src[b].end(), I_sk[2 * b + 2].begin(), I_sk[2 * b + 2].end());
       }
-      std::vector<int> Jb;
-      int kb = 0;
-      if (prm.transinv && i > 0) {
-        // translation-invariant mode: every box of the level uses box 0's J and k
-        // (INFO_TREE.LEV(l) of HSS2D_build_tree_nsym.m:438-449, 499-540)
-        Jb.assign(L.J.begin(), L.J.begin() + L.n);
-        kb = L.k;
-      } else {
-        preset_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad,
-                        prm.layers, hh, Jb, kb);
+      level_proxy(prm, lev, T.cent[2 * b], T.cent[2 * b + 1], (int)I_src[b].size(), PX[i], PY[i]);
+    }
+    // kh > 0: the two finest levels take their skeletons from the ID of K(proxies, box)
+    L.id_level = helm && lev >= depth - 1;
+    if (L.id_level) {
+      HSS_REQUIRE(id_level != nullptr, HSS_ERR_ARG, "kh > 0 tree without an ID step");
+      std::vector<std::vector<int>> boxes(I_src.begin() + b0, I_src.begin() + b0 + L.nb);
+      std::vector<std::vector<int>> perm;
+      std::vector<int> kb;
+      id_level(lev, boxes, PX, PY, perm, kb);
+      HSS_REQUIRE((int)perm.size() == L.nb && (int)kb.size() == L.nb, HSS_ERR_ARG, "ID step: one result per box");
+      const int kl = *std::max_element(kb.begin(), kb.end());
+      int nrm;
+      double th0;
+      level_orientation(lev, nrm, th0);
+      for (int i = 0; i < L.nb; ++i) {
+        const int b = b0 + i, n = (int)I_src[b].size(), k = kb[i];
+        HSS_REQUIRE((int)perm[i].size() == n && k >= 0 && kl <= n, HSS_ERR_ARG, "ID permutation size");
+        const double cx = T.cent[2 * b], cy = T.cent[2 * b + 1];
+        auto X_of = [&](int pos, int dim) { return T.X[2 * (size_t)I_src[b][perm[i][pos]] + dim]; };
+        // the uniform level layout: the kl - k residual points nearest the boundary join the
+        // skeleton with zero rows of T (ties in the ID's residual order)
+        std::vector<double> d(n - k);
+        for (int q = k; q < n; ++q)
+          d[q - k] = std::min(L.colrad - std::fabs(X_of(q, 0) - cx), L.rowrad - std::fabs(X_of(q, 1) - cy));
+        std::vector<int> o;
+        stable_argsort(d, o);
+        std::vector<char> take(n - k, 0);
+        std::vector<int> skp, rsp;  // positions in perm
+        std::vector<int> rows, cols;  // raw T row / column of each
+        for (int q = 0; q < k; ++q) { skp.push_back(q); rows.push_back(q); }
+        for (int q = 0; q < kl - k; ++q) { take[o[q]] = 1; skp.push_back(k + o[q]); rows.push_back(-1); }
+        for (int q = 0; q < n - k; ++q)
+          if (!take[q]) { rsp.push_back(k + q); cols.push_back(q); }
+        // LOCAL_Non_Preset_Skeleton_Info :629-656: skeleton points around the centre,
+        // residual points along the interface; T = T(Js, Jr)
+        std::vector<double> sx(kl), sy(kl), rx(n - kl), ry(n - kl);
+        for (int q = 0; q < kl; ++q) { sx[q] = X_of(skp[q], 0); sy[q] = X_of(skp[q], 1); }
+        for (int q = 0; q < n - kl; ++q) { rx[q] = X_of(rsp[q], 0); ry[q] = X_of(rsp[q], 1); }
+        const std::vector<int> Js = orient_skeleton(sx, sy, cx, cy, th0);
+        const std::vector<int> Jr = orient_residual(rx, ry, nrm);
+        for (int v : Js) { Jall[i].push_back(perm[i][skp[v]]); L.id_rows.push_back(rows[v]); }
+        for (int v : Jr) { Jall[i].push_back(perm[i][rsp[v]]); L.id_cols.push_back(cols[v]); }
+        kall[i] = kl;
       }
+    } else {
+      for (int i = 0; i < L.nb; ++i) {
+        const int b = b0 + i;
+        if (prm.transinv && i > 0) {
+          // translation-invariant mode: every box of the level uses box 0's J and k
+          // (INFO_TREE.LEV(l) of HSS2D_build_tree_nsym.m:438-449, 499-540)
+          Jall[i] = Jall[0];
+          kall[i] = kall[0];
+        } else {
+          preset_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad, prm.layers,
+                          hh, Jall[i], kall[i]);
+        }
+      }
+      // above the ID levels of a kh > 0 tree the boundary-layer counts differ from box to
+      // box; every box takes the level's largest count, promoting the residual points
+      // nearest its boundary (ties in the residual order), then both sets are ordered as the
+      // preset rule orders them
+      const int kl = *std::max_element(kall.begin(), kall.end());
+      int nrm;
+      double th0;
+      level_orientation(lev, nrm, th0);
+      for (int i = 0; i < L.nb; ++i) {
+        if (kall[i] == kl) continue;
+        const int b = b0 + i, kb = kall[i], n = (int)I_src[b].size();
+        HSS_REQUIRE(n >= kl, HSS_ERR_ARG, "box smaller than its level's skeleton");
+        const double cx = T.cent[2 * b], cy = T.cent[2 * b + 1];
+        std::vector<int> rs(Jall[i].begin() + kb, Jall[i].end());
+        std::vector<double> d(rs.size());
+        for (size_t q = 0; q < rs.size(); ++q) {
+          const size_t g = (size_t)I_src[b][rs[q]];
+          d[q] = std::min(L.colrad - std::fabs(T.X[2 * g] - cx), L.rowrad - std::fabs(T.X[2 * g + 1] - cy));
+        }
+        std::vector<int> o;
+        stable_argsort(d, o);
+        std::vector<char> take(rs.size(), 0);
+        std::vector<int> sk(Jall[i].begin(), Jall[i].begin() + kb), rest;
+        for (int q = 0; q < kl - kb; ++q) {
+          take[o[q]] = 1;
+          sk.push_back(rs[o[q]]);
+        }
+        for (size_t q = 0; q < rs.size(); ++q)
+          if (!take[q]) rest.push_back(rs[q]);
+        auto coords = [&](const std::vector<int>& v, std::vector<double>& x, std::vector<double>& y) {
+          x.resize(v.size());
+          y.resize(v.size());
+          for (size_t q = 0; q < v.size(); ++q) {
+            x[q] = T.X[2 * (size_t)I_src[b][v[q]]];
+            y[q] = T.X[2 * (size_t)I_src[b][v[q]] + 1];
+          }
+        };
+        std::vector<double> x, y;
+        coords(sk, x, y);
+        const std::vector<int> Js = orient_skeleton(x, y, cx, cy, th0);
+        coords(rest, x, y);
+        const std::vector<int> Jr = orient_residual(x, y, nrm);
+        Jall[i].clear();
+        for (int v : Js) Jall[i].push_back(sk[v]);
+        for (int v : Jr) Jall[i].push_back(rest[v]);
+        kall[i] = kl;
+      }
+    }
+    L.poff.assign(1, 0);
+    for (int i = 0; i < L.nb; ++i) {
+      const int b = b0 + i;
+      const std::vector<int>& Jb = Jall[i];
+      const int kb = kall[i];
       const int n = (int)I_src[b].size();
-      if (i == 0) { L.n = n; L.k = kb; }
+      if (i == 0) { L.n = n; L.k = kb; L.p = 0; }
       HSS_REQUIRE(n == L.n && kb == L.k, HSS_ERR_ARG, "non-uniform level sizes");
       I_sk[b].resize(kb);
       for (int q = 0; q < kb; ++q) I_sk[b][q] = I_src[b][Jb[q]];
@@ -242,16 +442,18 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T) {
         L.Isrc.push_back(I_src[b][q]);
         L.IsrcJ.push_back(I_src[b][Jb[q]]);
       }
-      std::vector<double> px, py;
-      box_proxy(T.cent[2 * b], T.cent[2 * b + 1], L.colrad, L.rowrad, lay, hh, px, py);
-      if (i == 0) L.p = (int)px.size();
-      HSS_REQUIRE((int)px.size() == L.p, HSS_ERR_ARG, "non-uniform proxy sizes");
+      const std::vector<double>& px = PX[i];
+      const std::vector<double>& py = PY[i];
+      L.p = std::max(L.p, (int)px.size());
+      L.poff.push_back(L.poff.back() + (int)px.size());
       for (size_t q = 0; q < px.size(); ++q) {
         L.proxy.push_back((int)(proxy_base + (long long)T.proxy_x.size()));
         T.proxy_x.push_back(px[q]);
         T.proxy_y.push_back(py[q]);
       }
     }
+    L.p_uniform = true;
+    for (int i = 0; i < L.nb; ++i) L.p_uniform = L.p_uniform && (L.poff[i + 1] - L.poff[i] == L.p);
   }
   HSS_REQUIRE(proxy_base + (long long)T.proxy_x.size() < (1LL << 31), HSS_ERR_ARG,
               "point table exceeds 2^31 entries");

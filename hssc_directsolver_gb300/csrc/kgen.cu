@@ -30,6 +30,13 @@ double modulation(const hss_kernel_params& kp, int which, double px, double py) 
   const int kind = which ? kp.c_kind : kp.b_kind;
   if (kind == HSS_MOD_BUMP) return bump4(px, py, 0.0);
   if (kind == HSS_MOD_SQRT_BUMP) return std::sqrt(bump4(px, py, 4.0 * kp.h));
+  if (kind == HSS_MOD_GAUSS0) {
+    // alpha exp(-isig |p - p0|^2), no constant term
+    const double a = which ? kp.c_alpha : kp.b_alpha, x0 = which ? kp.c_x0 : kp.b_x0;
+    const double y0 = which ? kp.c_y0 : kp.b_y0, is = which ? kp.c_isig : kp.b_isig;
+    const double d1 = px - x0, d2 = py - y0;
+    return a * std::exp(-is * (d1 * d1 + d2 * d2));
+  }
   HSS_REQUIRE(kind == HSS_MOD_GAUSS, HSS_ERR_ARG, "unknown modulation form");
   return which ? modulation(kp.c_alpha, kp.c_x0, kp.c_y0, kp.c_isig, px, py)
                : modulation(kp.b_alpha, kp.b_x0, kp.b_y0, kp.b_isig, px, py);
@@ -87,37 +94,6 @@ void PointTable::upload_range(size_t first, size_t n, const double* hx, const do
   for (int a = 0; a < 8; ++a)
     HSS_CUDA(cudaMemcpyAsync(dst[a] + first, src[a], bytes, cudaMemcpyHostToDevice, s));
   HSS_CUDA(cudaStreamSynchronize(s));
-}
-
-__device__ __forceinline__ double kernel_entry(const KernelDev& k, const PointView& P, int t, int s) {
-  const double dx = __dadd_rn(P.x[t], -P.x[s]);
-  const double dy = __dadd_rn(P.y[t], -P.y[s]);
-  const double den = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-  const bool z = (den == 0.0);
-  if (k.flag == HSS_SL_L_2D) {
-    double v = __dmul_rn(k.h2half, P.bval[t]);
-    v = __dmul_rn(v, log(z ? 1.0 : den));
-    v = __dmul_rn(v, P.cval[s]);
-    return __dadd_rn(v, z ? 1.0 : 0.0);
-  }
-  // double layer: w/(2 pi) n_y.(x-y)/|x-y|^2 ; diagonal -1/2 - w kappa/(4 pi)
-  const double w = P.w[s];
-  if (z) return __dadd_rn(-0.5, -__dmul_rn(__dmul_rn(w, P.kap[s]), 0.07957747154594767));
-  const double num = __dadd_rn(__dmul_rn(P.nx[s], dx), __dmul_rn(P.ny[s], dy));
-  return __ddiv_rn(__dmul_rn(__dmul_rn(w, 0.15915494309189535), num), den);
-}
-
-template <typename R>
-__global__ void __launch_bounds__(256) k_kgen(const KgenP<R>* __restrict__ D, PointView P, KernelDev k) {
-  const KgenP<R> d = D[blockIdx.y];
-  const long long tot = (long long)d.m * d.n;
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
-    int i, j;
-    size_t o;
-    if (!d.trans) { i = (int)(e % d.m); j = (int)(e / d.m); o = i + (size_t)j * d.ld; }
-    else { j = (int)(e % d.n); i = (int)(e / d.n); o = j + (size_t)i * d.ld; }
-    d.out[o] = (R)kernel_entry(k, P, d.ti[i], d.si[j]);
-  }
 }
 
 // H0^(1)(x) = J0(x) + i Y0(x) for x > 0 to ~2e-16 absolute accuracy.
@@ -203,6 +179,89 @@ __global__ void __launch_bounds__(256) k_kgen_complex(const KgenCP* __restrict__
   }
 }
 
+// Complex Helmholtz entry K(t, s) of the point table (the operations of k_kgen_complex).
+__device__ __forceinline__ void helm_entry(const HelmDev& k, const PointView& P, int t, int s, double& re,
+                                           double& im) {
+  const double dx = __dadd_rn(P.x[t], -P.x[s]);
+  const double dy = __dadd_rn(P.y[t], -P.y[s]);
+  const double den = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  if (den == 0.0) {
+    re = k.w_re;
+    im = k.w_im;
+    return;
+  }
+  const double x = __dmul_rn(k.kh, sqrt(den));
+  const double sb = __dmul_rn(k.s, P.bval[t]);
+  double hj, hy;
+  hankel0(x, k.hw, hj, hy);
+  re = -__dmul_rn(__dmul_rn(sb, hy), P.cval[s]);
+  im = __dmul_rn(__dmul_rn(sb, hj), P.cval[s]);
+}
+
+// entry (a, b) of the real 2 x 2 embedding [[re, -im], [im, re]]
+__device__ __forceinline__ double emb_entry(double re, double im, int a, int b) {
+  return (a == b) ? re : (a ? im : -im);
+}
+
+__device__ __forceinline__ double kernel_entry(const KernelDev& k, const PointView& P, int t, int s) {
+  const double dx = __dadd_rn(P.x[t], -P.x[s]);
+  const double dy = __dadd_rn(P.y[t], -P.y[s]);
+  const double den = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  const bool z = (den == 0.0);
+  if (k.flag == HSS_SL_H_2D) {  // embedded complex entry
+    double re, im;
+    helm_entry(k.helm, P, t & ~1, s & ~1, re, im);
+    return emb_entry(re, im, t & 1, s & 1);
+  }
+  if (k.flag == HSS_SL_L_2D) {
+    double v = __dmul_rn(k.h2half, P.bval[t]);
+    v = __dmul_rn(v, log(z ? 1.0 : den));
+    v = __dmul_rn(v, P.cval[s]);
+    return __dadd_rn(v, z ? 1.0 : 0.0);
+  }
+  // double layer: w/(2 pi) n_y.(x-y)/|x-y|^2 ; diagonal -1/2 - w kappa/(4 pi)
+  const double w = P.w[s];
+  if (z) return __dadd_rn(-0.5, -__dmul_rn(__dmul_rn(w, P.kap[s]), 0.07957747154594767));
+  const double num = __dadd_rn(__dmul_rn(P.nx[s], dx), __dmul_rn(P.ny[s], dy));
+  return __ddiv_rn(__dmul_rn(__dmul_rn(w, 0.15915494309189535), num), den);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_kgen(const KgenP<R>* __restrict__ D, PointView P, KernelDev k) {
+  const KgenP<R> d = D[blockIdx.y];
+  const long long tot = (long long)d.m * d.n;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    int i, j;
+    size_t o;
+    if (!d.trans) { i = (int)(e % d.m); j = (int)(e / d.m); o = i + (size_t)j * d.ld; }
+    else { j = (int)(e % d.n); i = (int)(e / d.n); o = j + (size_t)i * d.ld; }
+    d.out[o] = (R)kernel_entry(k, P, d.ti[i], d.si[j]);
+  }
+}
+
+// Embedded Helmholtz blocks: one thread per complex entry (index pairs 2i, 2i + 1 of ti and
+// si address the two components of one point), the four real entries of its 2 x 2 block
+// written together; m and n are even.
+template <typename R>
+__global__ void __launch_bounds__(256) k_kgen_emb(const KgenP<R>* __restrict__ D, PointView P, HelmDev k) {
+  const KgenP<R> d = D[blockIdx.y];
+  const int mc = d.m / 2, nc = d.n / 2;
+  const long long tot = (long long)mc * nc;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int i = (int)(e % mc), j = (int)(e / mc);
+    double re, im;
+    helm_entry(k, P, d.ti[2 * i], d.si[2 * j], re, im);
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const int r = 2 * i + a, c = 2 * j + b;
+        const size_t o = d.trans ? (c + (size_t)r * d.ld) : (r + (size_t)c * d.ld);
+        d.out[o] = (R)emb_entry(re, im, a, b);
+      }
+  }
+}
+
 void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, const PointView& pts,
                           const HelmDev& k, cudaStream_t s) {
   if (batch <= 0 || maxEntries <= 0) return;
@@ -217,6 +276,12 @@ void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const Poi
                   const KernelDev& k, cudaStream_t s) {
   if (batch <= 0 || maxEntries <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "kgen batch too large");
+  if (k.flag == HSS_SL_H_2D) {
+    const int gx = std::max(1, std::min(ceil_div(maxEntries / 4, 256), 2048));
+    k_kgen_emb<R><<<dim3(gx, batch), 256, 0, s>>>(dP, pts, k.helm);
+    check_launch("k_kgen_emb");
+    return;
+  }
   const int gx = std::max(1, std::min(ceil_div(maxEntries, 256), 2048));
   k_kgen<R><<<dim3(gx, batch), 256, 0, s>>>(dP, pts, k);
   check_launch("k_kgen");
@@ -269,6 +334,44 @@ __global__ void __launch_bounds__(256) k_kmatvec(const KmvP* __restrict__ D, Poi
   }
 }
 
+// Embedded complex kernel (HSS_SL_H_2D): one thread per complex target (real rows 2i, 2i + 1
+// of the embedded system), each complex entry formed once and applied to the interleaved
+// (re, im) source vector: complex128 arithmetic.
+template <int NR>
+__global__ void __launch_bounds__(256) k_kmatvec_c(const KmvP* __restrict__ D, PointView P, HelmDev k, int nsplit,
+                                                   double* __restrict__ part, int mmax, int nrhs) {
+  const KmvP d = D[blockIdx.z];
+  const int mc = d.m / 2, nc = d.n / 2;
+  if ((int)blockIdx.x * 256 >= mc) return;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  const int per = (nc + nsplit - 1) / nsplit;
+  const int jb = blockIdx.y * per, je = min(nc, jb + per);
+  double ar[NR], ai[NR];
+#pragma unroll
+  for (int c = 0; c < NR; ++c) ar[c] = ai[c] = 0.0;
+  if (i < mc) {
+    const int t = d.t0 + 2 * i;
+    for (int j = jb; j < je; ++j) {
+      double re, im;
+      helm_entry(k, P, t, d.s0 + 2 * j, re, im);
+      const double* qj = d.q + 2 * j;
+#pragma unroll
+      for (int c = 0; c < NR; ++c)
+        if (c < nrhs) {
+          const double xr = qj[(size_t)c * d.ldq], xi = qj[(size_t)c * d.ldq + 1];
+          ar[c] = fma(re, xr, fma(-im, xi, ar[c]));
+          ai[c] = fma(re, xi, fma(im, xr, ai[c]));
+        }
+    }
+    double* pp = part + (((size_t)blockIdx.z * nsplit + blockIdx.y) * mmax + 2 * i) * NR;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+      pp[c] = ar[c];
+      pp[NR + c] = ai[c];
+    }
+  }
+}
+
 template <int NR>
 __global__ void k_kmatvec_reduce(const KmvP* __restrict__ D, int nsplit, const double* __restrict__ part, int mmax,
                                  int nrhs) {
@@ -286,14 +389,20 @@ void kernel_matvec(const KmvP* dP, int batch, int maxM, int maxN, int nrhs, cons
                    DevBuf<double>& part, cudaStream_t s) {
   if (batch <= 0 || maxM <= 0) return;
   HSS_REQUIRE(batch <= 65535 && nrhs >= 1 && nrhs <= 8, HSS_ERR_ARG, "kernel matvec: batch <= 65535, 1..8 columns");
-  HSS_REQUIRE(k.flag == HSS_SL_L_2D || k.flag == HSS_DL_L_2D, HSS_ERR_ARG, "kernel matvec: real kernels only");
-  const int tiles = ceil_div(maxM, 256);
+  const bool cplx = (k.flag == HSS_SL_H_2D);
+  const int tiles = ceil_div(cplx ? maxM / 2 : maxM, 256);
   const int nsplit = std::max(1, std::min(64, std::min(ceil_div(1216, (long long)tiles * batch), std::max(1, maxN / 256))));
   const int NR = nrhs <= 4 ? 4 : 8;
   part.ensure((size_t)batch * nsplit * maxM * NR);
   const dim3 grid(tiles, nsplit, batch);
-  if (NR == 4) k_kmatvec<4><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
-  else k_kmatvec<8><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
+  if (cplx) {
+    if (NR == 4) k_kmatvec_c<4><<<grid, 256, 0, s>>>(dP, pts, k.helm, nsplit, part.p, maxM, nrhs);
+    else k_kmatvec_c<8><<<grid, 256, 0, s>>>(dP, pts, k.helm, nsplit, part.p, maxM, nrhs);
+  } else if (NR == 4) {
+    k_kmatvec<4><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
+  } else {
+    k_kmatvec<8><<<grid, 256, 0, s>>>(dP, pts, k, nsplit, part.p, maxM, nrhs);
+  }
   check_launch("k_kmatvec");
   const int gx = std::max(1, std::min(ceil_div((long long)maxM * nrhs, 256), 256));
   if (NR == 4) k_kmatvec_reduce<4><<<dim3(gx, batch), 256, 0, s>>>(dP, nsplit, part.p, maxM, nrhs);

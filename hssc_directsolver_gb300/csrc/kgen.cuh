@@ -55,18 +55,6 @@ struct KgenCP {
   double* out;
   long long ld;
 };
-// Helmholtz constants: s = h^2 kh^2 / 4 (the imaginary factor of the off-diagonal
-// entries), w = 1 + kh^2 (i/4) dr (the diagonal)
-// and the weights 2 exp(-(j 0.3)^2), j = 0..21, of the Hankel-integral trapezoid rule
-// (j = 0 unused).  The weights travel in the kernel parameters, so no per-device state
-// has to be uploaded before a launch.
-constexpr int kHankelNodes = 21;
-constexpr double kHankelStep = 0.3;
-struct HelmDev {
-  double kh, s, w_re, w_im;
-  double hw[kHankelNodes + 1];
-};
-HelmDev make_helm_dev(const hss_kernel_params& kp);
 void kgen_complex_batched(const KgenCP* dP, int batch, long long maxEntries, const PointView& pts,
                           const HelmDev& k, cudaStream_t s);
 
@@ -78,7 +66,8 @@ void kgen_batched(const KgenP<R>* dP, int batch, long long maxEntries, const Poi
 // of Common/Iterative_Refinement.m:20-35 against the kernel matrix itself): problem b
 // computes u(i, c) = sum_j K(t0 + i, s0 + j) q(j, c), i < m, j < n, c < nrhs (<= 8), over
 // the point table, with the entries of kernel_entry (SL_L_2D or DL_L_2D).  The sources are
-// split over blocks; the partial sums are added in a fixed order.
+// split over blocks; the partial sums are added in a fixed order.  HSS_SL_H_2D: rows and
+// columns count embedded (real) entries, m, n, t0 and s0 even, q and u interleaved complex.
 struct KmvP {
   int t0, m, s0, n;
   const double* q;

@@ -44,6 +44,8 @@ class HSS2DParams:
     Fopts: str = "dense"
     k_cut: int = 2500         # low-rank T only where k < k_cut
     seed: int = 0             # key of the randomized ID's Gaussian samples
+    proxy_rule: str = "bdry"  # params.proxy_rule: "bdry" or "rand" (sampled proxy layers)
+    lambda_: float = 2.0      # params.lambda of the "rand" rule
 
     @property
     def h(self) -> float:
@@ -67,15 +69,28 @@ class HSS2DParams:
                 "dfloat_inv": L.HSS_PREC_DFLOAT_INV, "tc": L.HSS_PREC_TC}[self.precision]
         k = self.kernel
         k.h = self.h
+        rules = {"bdry": L.HSS_PROXY_BDRY, "rand": L.HSS_PROXY_RAND}
+        if self.proxy_rule not in rules:
+            raise ValueError("proxy_rule must be 'bdry' or 'rand'")
         return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,
-                              0, float(self.acc), k.to_c(), int(self.k_cut), 0, int(self.seed))
+                              0, float(self.acc), k.to_c(), int(self.k_cut), 0, int(self.seed),
+                              rules[self.proxy_rule], 0, float(self.lambda_))
+
+    @property
+    def complex(self) -> bool:
+        """The Helmholtz / Lippmann-Schwinger operator (SL_H_2D) is complex."""
+        return self.kernel.flag_pot == "SL_H_2D"
 
 
 def HSS_tree_parameters(pot: str, kh: float, sym: int, Ng: int, npan: int, acc: float, lay: int, n_cut: int,
                         TI: int, proxy: int = 0) -> HSS2DParams:
-    """Common/HSS_tree_parameters.m:108-139 for the Laplace kernel (kh = 0)."""
+    """Common/HSS_tree_parameters.m:108-139.  kh > 0: the Lippmann-Schwinger kernel SL_H_2D
+    with the order-4 Duan-Rokhlin diagonal and the bump contrast of LOCAL_get_bc, dense T
+    (the complex GPU tree's interpolation form)."""
     if kh != 0:
-        raise ValueError("the oscillatory kernels are not part of the GPU path")
+        from .kernels import helmholtz_kernel
+        return HSS2DParams(Ng=Ng, npan=npan, acc=acc, layers=lay, kernel=helmholtz_kernel(kh, sym, Ng, npan, TI, proxy),
+                           transinv=TI, sym=sym, n_cut=n_cut, INTERform="dense")
     # transinv = 1 keeps one factor set per tree level (INFO_TREE.LEV); the kernel has b = c = 1
     b, c = reference_modulations(sym, proxy, TI)
     # INTERform 'lowrank' and k_cut 2500 are the reference's defaults (HSS_tree_parameters.m:131-134)
@@ -94,6 +109,7 @@ class InfoTree:
         d, nb, n = C.c_int32(), C.c_int32(), C.c_int64()
         L.check(L.lib().hss2d_info(self._h, C.byref(d), C.byref(nb), C.byref(n)))
         self.depth, self.nboxes, self.N = d.value, nb.value, n.value
+        self.complex = params.complex
         self.compressed = False
         self.inverted = False
 
@@ -135,8 +151,9 @@ class InfoTree:
     def export_box(self, box: int):
         n, k, _ = self.box_sizes()
         nb, kb = int(n[box]), int(k[box])
+        dt = np.complex128 if self.complex else np.float64
         out = dict(I_src=np.zeros(nb, np.int32), J=np.zeros(nb, np.int32),
-                   T_up=np.zeros((kb, nb - kb), order="F"), T_dn=np.zeros((kb, nb - kb), order="F"))
+                   T_up=np.zeros((kb, nb - kb), dtype=dt, order="F"), T_dn=np.zeros((kb, nb - kb), dtype=dt, order="F"))
         ip = lambda a: a.ctypes.data_as(L._I32P)
         dp = lambda a: a.ctypes.data_as(L._DP)
         L.check(L.lib().hss2d_export_box(self._h, box, ip(out["I_src"]), ip(out["J"]), dp(out["T_up"]),
@@ -146,8 +163,9 @@ class InfoTree:
     def export_inverse(self, box: int):
         n, k, _ = self.box_sizes()
         nb, kb = int(n[box]), int(k[box])
-        FI = np.zeros((nb, nb), order="F")
-        E = np.zeros((kb, kb), order="F")
+        dt = np.complex128 if self.complex else np.float64
+        FI = np.zeros((nb, nb), dtype=dt, order="F")
+        E = np.zeros((kb, kb), dtype=dt, order="F")
         L.check(L.lib().hss2d_export_inverse(self._h, box, FI.ctypes.data_as(L._DP), E.ctypes.data_as(L._DP)))
         return FI, E
 
@@ -196,24 +214,74 @@ def HSS2D_invert_nsym(INFO_TREE: InfoTree, params: HSS2DParams | None = None) ->
 
 
 def _vec(INFO_TREE, X):
-    X = np.asfortranarray(np.asarray(X, dtype=np.float64))
+    """Column-major N x r vectors in the tree's arithmetic: complex128 for a complex tree
+    (passed to the library as interleaved (re, im) doubles), float64 otherwise."""
+    dt = np.complex128 if INFO_TREE.complex else np.float64
+    X = np.asfortranarray(np.asarray(X, dtype=dt))
     vec = X.ndim == 1
     X2 = X.reshape(INFO_TREE.N, -1, order="F")
     return X2, vec
+
+
+def _out(X2, vec):
+    return X2[:, 0] if vec else X2
 
 
 def HSS2D_apply_nsym(INFO_TREE: InfoTree, A_HSS, X, params=None) -> np.ndarray:
     X2, vec = _vec(INFO_TREE, X)
     Y = np.zeros_like(X2, order="F")
     L.check(L.lib().hss2d_apply(INFO_TREE._h, L.ptr(X2), L.ptr(Y), X2.shape[1]))
-    return Y[:, 0] if vec else Y
+    return _out(Y, vec)
 
 
 def HSS2D_applyinv_nsym(INFO_TREE: InfoTree, A_HSS, X, params=None) -> np.ndarray:
     X2, vec = _vec(INFO_TREE, X)
     Y = np.zeros_like(X2, order="F")
     L.check(L.lib().hss2d_applyinv(INFO_TREE._h, L.ptr(X2), L.ptr(Y), X2.shape[1]))
-    return Y[:, 0] if vec else Y
+    return _out(Y, vec)
+
+
+def HSS2D_gmres(INFO_TREE: InfoTree, F, tol: float = 1e-8, restart: int = 30, maxit: int = 200,
+                PRECOND: InfoTree | None = None):
+    """x = A^-1 f by restarted GMRES on INFO_TREE's forward operator, right-preconditioned by
+    the inverse apply of PRECOND (an inverted tree; INFO_TREE itself in "mixed" precision is
+    the Lippmann-Schwinger configuration's complex64 inverse), complex128 on a complex tree
+    (the reference's Krylov solves: HSS2D/Test/Test_HSS2D_InverseCompression.m:201-228).
+    Returns (x, relres, iterations)."""
+    F2, vec = _vec(INFO_TREE, F)
+    Xs = np.zeros_like(F2, order="F")
+    rr = C.c_double()
+    it = C.c_int32()
+    L.check(L.lib().hss2d_gmres(INFO_TREE._h, PRECOND._h if PRECOND is not None else None, L.ptr(F2), L.ptr(Xs),
+                                F2.shape[1], float(tol), int(restart), int(maxit), C.byref(rr), C.byref(it)))
+    return _out(Xs, vec), rr.value, it.value
+
+
+def HSS2D_kernel_residual_rows(INFO_TREE: InfoTree, row0: int, F_rows, X) -> float:
+    """max over columns of ||f - K x|| / ||f|| over the rows row0 .. row0 + len(F_rows) only:
+    the kernel-matrix residual on a sample of rows (O(rows N) work)."""
+    dt = np.complex128 if INFO_TREE.complex else np.float64
+    Fr = np.asfortranarray(np.asarray(F_rows, dtype=dt))
+    Fr = Fr.reshape(Fr.shape[0], -1, order="F")
+    X2, _ = _vec(INFO_TREE, X)
+    assert Fr.shape[1] == X2.shape[1]
+    rr = C.c_double()
+    L.check(L.lib().hss2d_kernel_residual_rows(INFO_TREE._h, int(row0), Fr.shape[0], L.ptr(Fr), L.ptr(X2),
+                                               X2.shape[1], C.byref(rr)))
+    return rr.value
+
+
+def proxy_points(params: HSS2DParams, box: int, n_src: int) -> np.ndarray:
+    """LOCAL_Build_Proxy of one box (host computation): the proxy points (p x 2) of heap box
+    ``box`` with ``n_src`` sources under params' proxy rule."""
+    cp = params.to_c()
+    cap = 1 << 22
+    xy = np.zeros(2 * cap)
+    cnt = C.c_int32()
+    L.check(L.lib().hss2d_proxy_points(C.byref(cp), int(box), int(n_src), xy.ctypes.data_as(L._DP), cap,
+                                       C.byref(cnt)))
+    n = cnt.value
+    return np.stack([xy[:n], xy[cap:cap + n]], axis=1)
 
 
 def HSS2D_solve(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 5):
@@ -226,7 +294,7 @@ def HSS2D_solve(INFO_TREE: InfoTree, F, tol: float = 1e-10, maxit: int = 5):
     it = C.c_int32()
     L.check(L.lib().hss2d_solve(INFO_TREE._h, L.ptr(F2), L.ptr(Xs), F2.shape[1], tol, maxit, C.byref(rr),
                                 C.byref(it)))
-    return (Xs[:, 0] if vec else Xs), rr.value, it.value
+    return _out(Xs, vec), rr.value, it.value
 
 
 def HSS2D_kernel_residual(INFO_TREE: InfoTree, F, X) -> float:

@@ -11,7 +11,7 @@ from . import _lib as L
 from ._lib import hss_kernel_params, HSS_SL_L_2D, HSS_DL_L_2D, HSS_SL_H_2D
 
 KERNELS = {"SL_L_2D": HSS_SL_L_2D, "DL_L_2D": HSS_DL_L_2D, "SL_H_2D": HSS_SL_H_2D}
-MOD_GAUSS, MOD_BUMP, MOD_SQRT_BUMP = L.HSS_MOD_GAUSS, L.HSS_MOD_BUMP, L.HSS_MOD_SQRT_BUMP
+MOD_GAUSS, MOD_BUMP, MOD_SQRT_BUMP, MOD_GAUSS0 = L.HSS_MOD_GAUSS, L.HSS_MOD_BUMP, L.HSS_MOD_SQRT_BUMP, L.HSS_MOD_GAUSS0
 
 
 @dataclass
@@ -19,7 +19,8 @@ class Modulation:
     """``1 + alpha*exp(-isig*|p - (x0, y0)|^2)``; alpha = 0 switches it off.
 
     ``kind`` = MOD_BUMP / MOD_SQRT_BUMP selects the Lippmann-Schwinger bumps of
-    LOCAL_get_bc (Kernel_Eval.m:115-140) instead."""
+    LOCAL_get_bc (Kernel_Eval.m:115-140) instead; MOD_GAUSS0 is ``alpha*exp(-isig*|p - p0|^2)``
+    without the constant (a Gaussian contrast)."""
 
     alpha: float = 0.0
     x0: float = 0.0

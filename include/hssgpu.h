@@ -39,7 +39,8 @@ extern "C" {
 #define HSS_DL_L_2D 1 /* custom-kernel slot Kernel_Eval.m:75-79: Laplace double layer */
 #define HSS_SL_H_2D 2 /* Kernel_Eval.m:44-53, complex: w (den==0) + h^2 kh^2 (i/4) b(x) H0(kh r) c(y),
                          w = 1 + kh^2 (i/4) dr (dr = the order-4 Duan-Rokhlin weight; 0 = order 0).
-                         Evaluated by hss_kernel_eval; the HSS solvers take the real kernels. */
+                         Evaluated by hss_kernel_eval and solved by HSS2D (complex vectors:
+                         interleaved (re, im) doubles); HSS1D takes the real kernels. */
 
 /* modulation forms of b(x) / c(y) (hss_kernel_params.b_kind / c_kind) */
 #define HSS_MOD_GAUSS 0     /* 1 + alpha exp(-isig |p - p0|^2); alpha = 0: 1 (b_func, Kernel_Eval.m:99-108) */
@@ -47,6 +48,14 @@ extern "C" {
                                shift 0): the nonsymmetric Lippmann-Schwinger b, Kernel_Eval.m:115-119 */
 #define HSS_MOD_SQRT_BUMP 2 /* sqrt(Bump_function option 4 with shift 4h): the symmetric
                                Lippmann-Schwinger b and c, Kernel_Eval.m:129-140 */
+#define HSS_MOD_GAUSS0 3    /* alpha exp(-isig |p - p0|^2) without the constant: a Gaussian
+                               contrast taken symmetrically (b = c = its square root, isig halved) */
+
+/* HSS2D box proxies (params.proxy_rule, HSS2D_build_tree_nsym.m:870-961) */
+#define HSS_PROXY_BDRY 0 /* every point of the box's proxy layers (build_box_proxy.m:52-88) */
+#define HSS_PROXY_RAND 1 /* the layers sampled with probability 2^(-lambda l) by dyadic distance
+                            band l until ceil(2/3 n) (even levels) or ceil(3/4 n) points remain
+                            (LOCAL_Build_Proxy :883-905, LOCAL_random_sampler :964-1001) */
 
 /* precision modes */
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
@@ -289,10 +298,20 @@ typedef struct hss2d_params {
   int32_t k_cut;     /* low-rank T only where k < k_cut (0: 2500) */
   int32_t pad2_;
   uint64_t seed;     /* key of the randomized ID's Gaussian samples */
+  int32_t proxy_rule; /* HSS_PROXY_BDRY or HSS_PROXY_RAND (params.proxy_rule) */
+  int32_t pad3_;
+  double lambda;      /* params.lambda of HSS_PROXY_RAND (0: 2) */
 } hss2d_params;
 
 /* INFO_TREE = HSS2D_build_tree_nsym(params), HSS2D/HSS2D_build_tree_nsym.m:80-610
- * ('uniform' tree, 'bdry' preset skeletons, 'bdry' proxies, dense T). */
+ * ('uniform' tree, 'bdry' preset skeletons, 'bdry' or 'rand' proxies, dense T).
+ * HSS_SL_H_2D (kh > 0, the Lippmann-Schwinger operator): the skeletons of the two finest
+ * levels come from the interpolative decomposition of K(proxies, box) (:399-412, :614-657),
+ * every box of such a level at the level's largest rank (boxes below it take the fixed-rank
+ * ID's next pivots), T_dn = T_up = the ID's T; complex arithmetic runs as the real 2 x 2
+ * embedding [[Re, -Im], [Im, Re]] of every block.  Vectors of a complex tree are N complex
+ * entries per column, interleaved (re, im); hss2d_info reports N complex rows.
+ * Dense T only (HSS_INTER_DENSE), transinv 0. */
 int hss2d_build_tree(hss2d_matrix** out, const hss2d_params* p);
 /* A_HSS = HSS2D_compress_nsym(INFO_TREE, params) dense blocks, HSS2D/HSS2D_compress_nsym.m:67-125 */
 int hss2d_compress(hss2d_matrix* H);
@@ -337,6 +356,27 @@ int hss2d_set_autotune(hss2d_matrix* H, int32_t on);
  * f, x host N x nrhs column-major; relres = max column true residual; iters = iterations. */
 int hss2d_bicgstab(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x, int32_t nrhs,
                    double tol, int32_t maxit, double* relres, int32_t* iters);
+/* x = A^-1 f by restarted GMRES(restart) with right preconditioner M^-1 (the inverse apply
+ * of the inverted handle M, e.g. A itself in HSS_PREC_MIXED: the FP32 "complex64" inverse),
+ * A the FP64 forward operator; complex for HSS_SL_H_2D trees (complex128 arithmetic,
+ * interleaved vectors).  Each column iterates on its own Krylov space until its relative
+ * residual ||f - A x|| / ||f|| <= tol; all columns share the operator applies.  f, x host
+ * N x nrhs; relres = max column residual of the returned x; iters = Arnoldi steps.
+ * The reference's Krylov use: HSS2D/Test/Test_HSS2D_InverseCompression.m:201-228. */
+int hss2d_gmres(hss2d_matrix* A, hss2d_matrix* M, const double* f, double* x, int32_t nrhs, double tol,
+                int32_t restart, int32_t maxit, double* relres, int32_t* iters);
+/* relres = max over columns of ||f - K x|| / ||f|| over the target rows [row0, row0 + nrows)
+ * only (complex rows for a complex tree): the kernel-matrix residual on a row sample when
+ * the full O(N^2) product is too long.  f: those rows of the right-hand sides (nrows x nrhs),
+ * x: the full solution (N x nrhs). */
+int hss2d_kernel_residual_rows(hss2d_matrix* H, int64_t row0, int64_t nrows, const double* f, const double* x,
+                               int32_t nrhs, double* relres);
+/* LOCAL_Build_Proxy of one box (host computation, HSS2D_build_tree_nsym.m:870-961): the
+ * proxy points of box `box` (heap numbering, 0-based) on level lev of the tree p describes,
+ * for a box of n_src sources; rule and lambda from p.  xy receives x then y columns
+ * (2 cap doubles), *count the number of points (HSS_ERR_ARG if above cap). */
+int hss2d_proxy_points(const hss2d_params* p, int32_t box, int32_t n_src, double* xy, int32_t cap,
+                       int32_t* count);
 int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N);
 /* per-box sizes: n (|I_src|), k (|I_sk|), proxy count; arrays of nboxes (NULL ok) */
 int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* nproxy);

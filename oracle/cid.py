@@ -14,13 +14,28 @@ so both diagonal entries of a pair equal |R_tt| of the complex QR.  The span of 
 J-invariant, hence the projection onto its complement commutes with J and every remaining
 pair keeps two columns of equal norm: the pivot order over pairs is the complex pivot
 order, the rank counted in pairs is the complex rank, and T = R11 \\ R12 of the pair QR is
-E(T) of the complex ID.  ``pivoted_qr_complex`` restates the complex QR with the same
-exact-norm pivot rule as ``idecomp.pivoted_qr`` (reflectors as LAPACK zlarfg: beta real,
-H = I - tau v v^H)."""
+E(T) of the complex ID.  ``pivoted_qr_complex`` restates the complex QR with exact trailing
+norms (reflectors as LAPACK zlarfg: beta real, H = I - tau v v^H).
+
+Pivot ties.  Boxes on the diagonals of the domain are mirror images of themselves under the
+radial contrast, so pairs of their columns have equal norms up to rounding, and which one a
+QR takes first depends on its rounding.  Both QRs here (and the GPU's) therefore take the
+lowest-index column among those within a factor 1 - 2^-14 of the largest trailing norm
+(PIVOT_TIE); the reference (MATLAB's qr) resolves such ties by its own rounding."""
 from __future__ import annotations
 
 import numpy as np
 from scipy.linalg import solve_triangular
+
+
+PIVOT_TIE = 2.0 ** -14
+
+
+def pick_pivot(norms) -> int:
+    """Index of the pivot: the first entry >= max - max * PIVOT_TIE."""
+    m = float(np.max(norms))
+    thr = m - m * PIVOT_TIE
+    return int(np.flatnonzero(norms >= thr)[0])
 
 
 def embed(A: np.ndarray) -> np.ndarray:
@@ -44,7 +59,7 @@ def pivoted_qr_complex(A: np.ndarray):
     l = min(m, n)
     norms = np.einsum("ij,ij->j", A.conj(), A).real
     for j in range(l):
-        p = j + int(np.argmax(norms[j:]))
+        p = j + pick_pivot(norms[j:])
         if p != j:
             A[:, [j, p]] = A[:, [p, j]]
             perm[[j, p]] = perm[[p, j]]
@@ -80,7 +95,7 @@ def pivoted_qr_pairs(E: np.ndarray):
         c0 = 2 * t
         tail = A[c0:, c0::2]
         norms = np.einsum("ij,ij->j", tail, tail)
-        p = t + int(np.argmax(norms))
+        p = t + pick_pivot(norms)
         if p != t:
             A[:, [c0, c0 + 1, 2 * p, 2 * p + 1]] = A[:, [2 * p, 2 * p + 1, c0, c0 + 1]]
             perm[[t, p]] = perm[[p, t]]

@@ -47,8 +47,9 @@ class HSS2DParams:
     sym: int = 0
     k_cut: int = 2500
     seed: int = 0
-    # ID levels of the Helmholtz tree: raise every box to the level's largest rank (the
-    # uniform level layout of the GPU build); the reference keeps per-box ranks
+    # uniform level layout of the GPU build (the reference keeps per-box ranks): on the ID
+    # levels of the Helmholtz tree every box takes the level's largest rank (promote_id), on
+    # the preset levels above them the level's largest boundary count (promote_skeleton)
     uniform_ranks: bool = False
     # params.proxy_rule / lambda / skel_extra_pts (HSS_tree_parameters.m:121-124)
     proxy_rule: str = "bdry"
@@ -249,6 +250,7 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
         lp = lay_prox(prm, lev)
         qlev = 0
         ids = {}
+        presets = {}
         first = 2 ** lev - 1
         followers = []
         for b in range(2 ** lev - 1, 2 ** (lev + 1) - 1):
@@ -266,7 +268,17 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 # :399-412 -- kh > 0: skeletons by the ID on the two finest levels
                 ids[b] = (X_src, id_box(prm, Xp, X_src, b))
                 continue
-            Jb, kb = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
+            presets[b] = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
+        if prm.uniform_ranks and presets:
+            # the boundary-layer counts of boxes above ID levels differ; every box takes the
+            # level's largest count, promoting the residual points nearest its boundary
+            kl = max(kb for _, kb in presets.values())
+            for b, (Jb, kb) in presets.items():
+                if kb < kl:
+                    presets[b] = promote_skeleton(X[I_src[b]], Jb, kb, kl, cent[b], colrad, rowrad, lev)
+        for b, (Jb, kb) in presets.items():
+            X_src = X[I_src[b]]
+            Xp = proxy[b]
             Js[b] = Jb
             ks[b] = kb
             I_sk[b] = I_src[b][Jb[:kb]]
@@ -290,13 +302,12 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                     Js[b], ks[b] = Jb, kb
                     I_sk[b] = I_src[b][Jb[:kb]]
         if ids:
-            # the ID level's skeletons; with uniform_ranks every box keeps the level's
-            # largest rank (the fixed-rank ID promotes its next pivoted points)
+            # the ID level's skeletons; with uniform_ranks every box holds the level's
+            # largest rank: residual points join the skeleton with zero rows of T
             kl = max(r[2] for _, r in ids.values())
             for b, (X_src, (Tt, Jp, k, R)) in ids.items():
                 if prm.uniform_ranks and k < kl:
-                    from . import cid
-                    Tt, k = cid.id_fixed_complex(R, Jp, kl), kl
+                    Tt, Jp, k = promote_id(Tt, Jp, k, kl, X_src, cent[b], colrad, rowrad)
                 Tb, Jb, kb = orient_id(Tt, Jp, k, X_src, cent[b], lev)
                 Js[b] = Jb
                 ks[b] = kb
@@ -312,6 +323,45 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
     tree.lowrank = lowrank
     tree.q = q
     return tree
+
+
+def promote_skeleton(X_src, J, k, kl, cB, colrad, rowrad, lev):
+    """The uniform level layout above the ID levels of a kh > 0 tree (the GPU build's; the
+    reference keeps per-box counts): a box with k < kl boundary points promotes the kl - k
+    residual points nearest its boundary (distance min(colrad - |x - cx|, rowrad - |y - cy|),
+    ties in the residual order), then orders both sets as LOCAL_Preset_Skeleton_Info does.
+    Returns (J, kl)."""
+    rs = J[k:]
+    d = np.minimum(colrad - np.abs(X_src[rs, 0] - cB[0]), rowrad - np.abs(X_src[rs, 1] - cB[1]))
+    o = np.argsort(d, kind="stable")[:kl - k]
+    take = np.zeros(len(rs), dtype=bool)
+    take[o] = True
+    sk = np.concatenate([J[:k], rs[o]])
+    rest = rs[~take]
+    if lev % 2 == 0:
+        nrm, tan, th0 = 0, 1, math.pi / 2
+    else:
+        nrm, tan, th0 = 1, 0, 0.0
+    sk = sk[orient_skeleton(X_src[sk], cB, th0)]
+    rest = rest[orient_residual(X_src[rest], nrm, tan)]
+    return np.concatenate([sk, rest]), kl
+
+
+def promote_id(T, J, k, kl, X_src, cB, colrad, rowrad):
+    """The uniform level layout of the ID levels (the GPU build's; the reference keeps
+    per-box ranks): a box of rank k < kl moves the kl - k residual points nearest its boundary
+    (distance min(colrad - |x - cx|, rowrad - |y - cy|), ties in the ID's residual order) into
+    its skeleton.  Their rows of T are zero: A(:, sk) T = A(:, rs) holds unchanged for the
+    remaining residual points, so the interpolation error is the ID's own.
+    Returns (T, J, kl) with the promoted points after the ID's skeleton."""
+    rs = J[k:]
+    d = np.minimum(colrad - np.abs(X_src[rs, 0] - cB[0]), rowrad - np.abs(X_src[rs, 1] - cB[1]))
+    o = np.argsort(d, kind="stable")[:kl - k]
+    take = np.zeros(len(rs), dtype=bool)
+    take[o] = True
+    keep = np.flatnonzero(~take)
+    Tn = np.vstack([T[:, keep], np.zeros((kl - k, len(keep)), dtype=T.dtype)])
+    return Tn, np.concatenate([J[:k], rs[o], rs[keep]]), kl
 
 
 def random_sampler(X, cB, colrad, rowrad, lam, lay, h):
@@ -463,6 +513,25 @@ def interpolation_lowrank(prm: HSS2DParams, Xp, X_sk, X_rs, q, lev, box):
     return out
 
 
+TIKHONOV_REL = 2.0 ** -40
+
+
+def lstsq_tikhonov(A, B):
+    """T = argmin ||A T - B||^2 + lam^2 ||T||^2, lam = 2^-40 ||A||_F, by the Householder QR of
+    [A; lam I] (the complex interpolation systems' rule, GPU and oracle alike).  The
+    Helmholtz proxy systems K11 of the preset levels are numerically rank deficient (cond
+    ~1e14): the reference's K11 \\ K21 takes MATLAB's basic solution from a column-pivoted
+    QR; an unpivoted QR's solution has 10-100x that norm and costs the inverse five digits.
+    The damping keeps ||T|| near the minimum-norm solution's at an interpolation error of
+    ~acc."""
+    k = A.shape[1]
+    lam = TIKHONOV_REL * np.linalg.norm(A)
+    Aa = np.vstack([A, lam * np.eye(k)])
+    Ba = np.vstack([B, np.zeros((k, B.shape[1]), dtype=np.result_type(A, B))])
+    Q, R = np.linalg.qr(Aa)
+    return np.linalg.solve(R, Q.conj().T @ Ba)
+
+
 def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):
     """interpolation_operator.m:57-77 with lr = 0: T_up (box_2_proxy), T_dn (proxy_2_box)."""
     k = X_sk.shape[0]
@@ -470,7 +539,7 @@ def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):
         z = np.zeros((k, X_rs.shape[0]))
         return z, z
     kp = prm.kp
-    ls = idecomp.lstsq_qr if kp.flag != SL_H_2D else (lambda A, B: np.linalg.lstsq(A, B, rcond=None)[0])
+    ls = idecomp.lstsq_qr if kp.flag != SL_H_2D else lstsq_tikhonov
     K11 = kernel_eval(Xp, X_sk, kp)
     K21 = kernel_eval(Xp, X_rs, kp)
     Tu = ls(K11, K21)

@@ -1,0 +1,169 @@
+"""The complex Lippmann-Schwinger HSS2D on the GPU against the oracle (GPU).
+
+kh = 20, the Gaussian contrast exp(-|x|^2/0.1) taken symmetrically (b = c = exp(-|x|^2/0.2)),
+the order-4 Duan-Rokhlin diagonal, leaf 8 x 8, acc 1e-10, dense T.  The two finest levels take
+their skeletons from the complex ID of K(proxies, box) (HSS2D_build_tree_nsym.m:399-412,
+:614-657), run on the GPU as the pair-pivoted QR of the real 2 x 2 embedding; every box of a
+level holds the level's largest rank (the oracle's uniform_ranks layout).  Checked: skeletons,
+source sets and ranks equal in every box; T, the forward and inverse applies close to the
+oracle's; GMRES preconditioned by the FP32 ("complex64") inverse reaches 1e-8 against the
+kernel matrix itself.
+"""
+import numpy as np
+import pytest
+
+from oracle import drweights, hss2d as O2, kernels as OK
+
+pytestmark = pytest.mark.gpu
+KH = 20.0
+
+
+def _params(npan, precision="fp64", rule="bdry"):
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    h = 2.0 / (8 * npan)
+    _, w, _ = drweights.dr_stencil(h, KH, npan * 8, 4)
+    sq = GK.Modulation(alpha=1.0, isig=5.0, kind=GK.MOD_GAUSS0)
+    gp = G2.HSS2DParams(Ng=8, npan=npan, layers=3, acc=1e-10, INTERform="dense", precision=precision,
+                        kernel=GK.Kernel("SL_H_2D", h, sq, sq, KH, complex(w[0])), proxy_rule=rule)
+    osq = OK.Modulation(alpha=1.0, isig=5.0, kind=OK.MOD_GAUSS0)
+    kp = OK.KernelParams(flag=OK.SL_H_2D, h=h, b=osq, c=osq, kh=KH, dr=complex(w[0]))
+    op = O2.HSS2DParams(Ng=8, npan=npan, kp=kp, layers=3, acc=1e-10, INTERform="dense", uniform_ranks=True,
+                        proxy_rule=rule)
+    return gp, op
+
+
+_CACHE = {}
+
+
+def _oracle(npan, rule="bdry"):
+    key = (npan, rule)
+    if key not in _CACHE:
+        _, op = _params(npan, rule=rule)
+        tree = O2.build_tree_nsym(op)
+        blk = O2.compress_nsym(tree, op)
+        _CACHE[key] = (op, tree, blk, O2.invert_nsym(tree, op, blk))
+    return _CACHE[key]
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+CASES = [(4, "bdry"), (8, "rand")]
+
+
+@pytest.mark.parametrize("npan,rule", CASES)
+def test_helmholtz_tree_equals_oracle(gpu, npan, rule):
+    """Skeletons, source sets, ranks and proxy counts equal in every box.  T (from an ID whose
+    R11 reaches |R_kk| ~ acc |R_11|, and from damped least squares of condition ~1e14) is
+    compared by what it does: ||K(Xp, X_sk) (T - T_o)|| / ||K(Xp, X_rs)||."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    op, ot, blk, inv = _oracle(npan, rule)
+    gp, _ = _params(npan, rule=rule)
+    t = G2.HSS2D_build_tree_nsym(gp)
+    assert t.complex and t.N == op.N
+    n, k, px = t.box_sizes()
+    X = op.X_source()
+    worst_id, worst_ls = 0.0, 0.0
+    for b in range(t.nboxes):
+        e = t.export_box(b)
+        assert k[b] == ot.k[b], (b, k[b], ot.k[b])
+        assert px[b] == ot.proxy[b].shape[0], b
+        assert np.array_equal(e["I_src"], ot.I_src[b]), b
+        assert np.array_equal(e["J"], ot.J[b]), b
+        if b == 0 or ot.T_up[b] is None or not ot.T_up[b].size:
+            continue
+        lev = int(np.floor(np.log2(b + 1)))
+        Xs = X[ot.I_src[b]][ot.J[b]]
+        kb = ot.k[b]
+        Xp = ot.proxy[b]
+        K11, K21 = OK.kernel_eval(Xp, Xs[:kb], op.kp), OK.kernel_eval(Xp, Xs[kb:], op.kp)
+        act = np.linalg.norm(K11 @ (e["T_up"] - ot.T_up[b])) / np.linalg.norm(K21)
+        if lev >= op.depth - 1:
+            assert np.array_equal(e["T_up"], e["T_dn"]), b        # T_dn = T_up on the ID levels
+            worst_id = max(worst_id, act)
+        else:
+            K11d, K21d = OK.kernel_eval(Xs[:kb], Xp, op.kp).T, OK.kernel_eval(Xs[kb:], Xp, op.kp).T
+            worst_ls = max(worst_ls, act, np.linalg.norm(K11d @ (e["T_dn"] - ot.T_dn[b])) / np.linalg.norm(K21d))
+    print(f"npan {npan} {rule}: interpolation action of T against the oracle's: ID levels {worst_id:.2e}, "
+          f"least-squares levels {worst_ls:.2e}")
+    # measured 1.4e-15 / 4.9e-15 (npan 4), 2.7e-15 / 4.8e-15 (npan 8, 'rand')
+    assert worst_id <= 1e-13 and worst_ls <= 1e-13
+
+
+@pytest.mark.parametrize("npan,rule", CASES)
+def test_helmholtz_applies_match_oracle(gpu, npan, rule):
+    from hssc_directsolver_gb300 import hss2d as G2
+    op, ot, blk, inv = _oracle(npan, rule)
+    gp, _ = _params(npan, rule=rule)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(gp))
+    r = np.random.default_rng(3)
+    x = r.standard_normal((op.N, 3)) + 1j * r.standard_normal((op.N, 3))
+    y = G2.HSS2D_apply_nsym(t, None, x)
+    yo = O2.apply_nsym(ot, blk, x)
+    z = G2.HSS2D_applyinv_nsym(t, None, y)
+    zo = O2.applyinv_nsym(ot, inv, yo)
+    da, di = _rel(y, yo), _rel(z, zo)
+    print(f"npan {npan} {rule}: apply {da:.2e}, inverse apply {di:.2e}, round trip {_rel(z, x):.2e}")
+    # measured: apply 6.4e-16 / 6.9e-16, inverse apply 1.2e-12 / 3.7e-13, round trip 9.4e-13 / 2.6e-13
+    assert da <= 1e-13 and di <= 1e-10
+    assert _rel(z, x) <= 1e-10                        # forward then inverse: the identity
+    if npan == 4:                                     # the compressed operator against K itself
+        X = op.X_source()
+        K = OK.kernel_eval(X, X, op.kp)
+        assert _rel(y, K @ x) <= 1e-9
+
+
+def test_helmholtz_kernel_residual_matches_dense(gpu):
+    """The complex kernel-matrix residual (entries generated in FP64 on the fly) against the
+    dense complex matrix of the oracle."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    gp, op = _params(4)
+    t = G2.HSS2D_build_tree_nsym(gp)
+    X = op.X_source()
+    K = OK.kernel_eval(X, X, op.kp)
+    r = np.random.default_rng(5)
+    x = r.standard_normal((op.N, 2)) + 1j * r.standard_normal((op.N, 2))
+    f = K @ x
+    assert G2.HSS2D_kernel_residual(t, f, x) <= 1e-14
+    f2 = f.copy()
+    f2[7, 1] += 1e-3 * np.linalg.norm(f2[:, 1])
+    rr = G2.HSS2D_kernel_residual(t, f2, x)
+    assert abs(rr - 1e-3) <= 1e-6
+    assert G2.HSS2D_kernel_residual_rows(t, 100, f[100:400], x) <= 1e-14
+
+
+@pytest.mark.parametrize("npan,rule", CASES)
+def test_lippmann_schwinger_gmres_complex64_preconditioner(gpu, npan, rule):
+    """GMRES (complex128) on the FP64 operator, preconditioned by the FP32 inverse factors of
+    the same tree, reaches 1e-8 in a few steps, and the solution's residual against the
+    kernel matrix is at the compression tolerance."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    gp, op = _params(npan, precision="mixed", rule=rule)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(gp))
+    X = op.X_source()
+    f = np.exp(-(X[:, 0] ** 2 + X[:, 1] ** 2) / 0.2) * np.exp(1j * KH * X[:, 0])
+    F = np.stack([f, np.random.default_rng(1).standard_normal(op.N) + 0j], axis=1)
+    x, rr, its = G2.HSS2D_gmres(t, F, tol=1e-8, restart=30, maxit=100, PRECOND=t)
+    kr = G2.HSS2D_kernel_residual(t, F, x)
+    print(f"npan {npan} {rule}: GMRES relres {rr:.2e} in {its} steps, kernel residual {kr:.2e}")
+    assert rr <= 1e-8 and its <= 8                   # measured: 3 steps at npan 4 and 8
+    assert kr <= 1e-8                                 # measured 9.6e-10 / 5.0e-10 (acc 1e-10)
+    # without the preconditioner GMRES needs many more steps
+    _, rr0, its0 = G2.HSS2D_gmres(t, F[:, :1], tol=1e-8, restart=30, maxit=30)
+    assert its0 > 3 * its or rr0 > 1e-8
+
+
+def test_gmres_real_laplace_with_fp64_inverse(gpu):
+    """GMRES on a real (Laplace) tree, preconditioned by its own FP64 inverse: one or two
+    steps to 1e-12; unpreconditioned it still converges, in more steps."""
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    h = 2.0 / 32
+    p = G2.HSS2DParams(Ng=8, npan=4, kernel=GK.Kernel("SL_L_2D", h, GK.Modulation(), GK.Modulation(0.5, 0, 0, 20.0)))
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(p))
+    F = np.random.default_rng(2).standard_normal((t.N, 3))
+    x, rr, its = G2.HSS2D_gmres(t, F, tol=1e-12, restart=20, maxit=40, PRECOND=t)
+    assert rr <= 1e-12 and its <= 3
+    assert np.linalg.norm(G2.HSS2D_apply_nsym(t, None, x) - F) <= 1e-11 * np.linalg.norm(F)
+    x0, rr0, its0 = G2.HSS2D_gmres(t, F[:, :1], tol=1e-8, restart=60, maxit=300)
+    assert rr0 <= 1e-8 and its0 > its
