@@ -1738,7 +1738,7 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
 }
 
 template <typename R>
-void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df) {
+void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df, bool solve) {
   if (batch <= 0 || maxkf <= 0) return;
   HSS_REQUIRE(batch <= 65535, HSS_ERR_ARG, "lstsq batch too large");
   int C = 1;
@@ -1782,6 +1782,7 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
       check_launch("k_qr_update");
     }
   }
+  if (!solve) return;  // factor only: R11 and (Q^T A(:, kf:n))(0:kf, :) in the top kf rows
   const int nblk = ceil_div(maxkf, 32);
   for (int blk = nblk - 1; blk >= 0; --blk) {
     const int rows_above = blk * 32;
@@ -2702,7 +2703,7 @@ void id_fixed_batched(const IdP* dP, int batch, cudaStream_t s) {
   template void gemm_skinny_split<R>(const GemmP<R>*, int, int, int, R, R, int, R*, cudaStream_t); \
   template int skinny_ksplit<R>(int, int, int);                                              \
   template void invert_batched<R>(const InvP<R>*, int, int, cudaStream_t, bool);             \
-  template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t, bool);
+  template void lstsq_batched<R>(const QrP<R>*, int, int, int, int, cudaStream_t, bool, bool);
 HSS_INST(double)
 HSS_INST(float)
 #undef HSS_INST

@@ -83,6 +83,7 @@ struct InvP {
   int* aux;   // GJ_AUX ints: row-permutation bookkeeping of the current panel
 };
 constexpr int GJ_NB = 32;
+constexpr int GJ_MAX_N = 12800;  // the cluster panel's size limit of invert_batched
 constexpr int GJ_AUX = 4 * GJ_NB + 4;
 
 template <typename R>
@@ -107,7 +108,13 @@ constexpr int QR_NB = 32;
 
 template <typename R>
 // df (FP64 only): the compact-WY trailing updates in double-float arithmetic
-void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df = false);
+// solve = false: the QR only; the top kf rows then hold R11 (upper triangle; the reflectors
+// below it) and the first kf rows of Q^T A(:, kf:n), the data a row-blocked (TSQR) solve
+// stacks onto the next block of rows.
+void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df = false,
+                   bool solve = true);
+// the cluster panel's row limit of lstsq_batched
+constexpr int LSTSQ_MAX_ROWS = 12800;
 
 // Interpolative decomposition of one m x n block per problem (the pivoted-QR
 // rank detection of the reference ID, with its randomized posterior check).

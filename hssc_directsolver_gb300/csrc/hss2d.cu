@@ -17,11 +17,25 @@
 //               operator (Iterative_Refinement.m:20-35).
 #include "hss2d.h"
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 
 namespace hss {
+
+// Size limit of the single-launch block inversion and least squares (the cluster panels);
+// larger blocks take the two-level inversion and the row-blocked least squares.  The
+// environment variable HSS2D_PANEL_LIMIT (>= 256) lowers it, so that tests reach those
+// paths at small sizes.
+static int panel_limit(int def) {
+  const char* e = std::getenv("HSS2D_PANEL_LIMIT");
+  if (!e) return def;
+  const int v = std::atoi(e);
+  return (v >= 256 && v < def) ? v : def;
+}
+
 
 // ---------------------------------------------------------------------------
 // small batched kernels
@@ -118,6 +132,31 @@ __global__ void k_tikhonov_rows(const TikP* __restrict__ P) {
   for (long long e = threadIdx.x; e < (long long)q.k * q.n; e += 256) {
     const int r = (int)(e % q.k), c = (int)(e / q.k);
     q.A[q.p + r + (size_t)c * q.ld] = (c == r) ? lam : 0.0;
+  }
+}
+
+// One stacking step of a row-blocked least squares (TSQR): in W (ld ldw) the top k rows keep
+// the previous block's R11 | Q^T B (the reflectors below R11's diagonal are cleared) and the
+// rows below take `count` rows of A starting at row `from` (clean = 0: W starts empty and
+// takes the rows from its top).
+struct TsqrP {
+  const double* A;
+  int lda;
+  double* W;
+  int ldw, k, n, from, count, clean;
+};
+__global__ void k_tsqr_fill(const TsqrP* __restrict__ P) {
+  const TsqrP q = P[blockIdx.y];
+  const int top = q.clean ? q.k : 0;
+  const long long tot = (long long)(top + q.count) * q.n;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < tot; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % (top + q.count)), c = (int)(e / (top + q.count));
+    double* w = q.W + r + (size_t)c * q.ldw;
+    if (r < top) {
+      if (c < q.k && r > c) *w = 0.0;
+    } else {
+      *w = q.A[(q.from + r - top) + (size_t)c * q.lda];
+    }
   }
 }
 
@@ -614,6 +653,60 @@ void HSS2D::id_T_level(int lev) {
   qlev[lev] = nr;
 }
 
+// Least squares taller than the cluster panel's row limit, by row blocks (TSQR): the first
+// block is factored, then the k rows of R11 | Q^T B are stacked onto the next rows of A and
+// factored again, until every row has been taken; the last step solves with the k x k R11.
+// The solution is that of the full problem (orthogonal transformations of row blocks).
+void HSS2D::lstsq_tsqr(const std::vector<QrP<double>>& qp, int n, int k) {
+  const int batch = (int)qp.size();
+  const int ldw = panel_limit(LSTSQ_MAX_ROWS), chunk = ldw - k;
+  HSS_REQUIRE(chunk >= 32, HSS_ERR_ARG, "least squares: too many columns for a row-blocked solve");
+  DevBuf<double> W((size_t)batch * ldw * n), V((size_t)batch * ldw * QR_NB), Tf((size_t)batch * QR_NB * QR_NB);
+  DevBuf<TsqrP> dtp(batch);
+  DevBuf<QrP<double>> dqp(batch);
+  std::vector<int> done(batch, 0);
+  int maxrows = 0;
+  for (auto& q : qp) maxrows = std::max(maxrows, q.m);
+  auto fill = [&](bool clean, std::vector<QrP<double>>& step) {
+    std::vector<TsqrP> tp(batch);
+    long long maxe = 1;
+    for (int b = 0; b < batch; ++b) {
+      const int take = std::min(clean ? chunk : ldw, qp[b].m - done[b]);
+      tp[b] = TsqrP{qp[b].A, qp[b].lda, W.p + (size_t)b * ldw * n, ldw, k, n, done[b], take, clean ? 1 : 0};
+      step[b] = qp[b];
+      step[b].A = tp[b].W;
+      step[b].lda = ldw;
+      step[b].m = (clean ? k : 0) + take;
+      step[b].V = V.p + (size_t)b * ldw * QR_NB;
+      step[b].Tf = Tf.p + (size_t)b * QR_NB * QR_NB;
+      done[b] += take;
+      maxe = std::max(maxe, (long long)step[b].m * n);
+    }
+    HSS_CUDA(cudaMemcpyAsync(dtp.p, tp.data(), batch * sizeof(TsqrP), cudaMemcpyHostToDevice, stream));
+    const int gx = std::max(1, std::min(ceil_div(maxe, 256), 4096));
+    k_tsqr_fill<<<dim3(gx, batch), 256, 0, stream>>>(dtp.p);
+    check_launch("k_tsqr_fill");
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  };
+  auto run = [&](std::vector<QrP<double>>& step, bool solve) {
+    int maxm = 1;
+    for (auto& q : step) maxm = std::max(maxm, q.m);
+    HSS_CUDA(cudaMemcpyAsync(dqp.p, step.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
+    lstsq_batched<double>(dqp.p, batch, maxm, n, k, stream, dftree(), solve);
+    HSS_CUDA(cudaStreamSynchronize(stream));
+  };
+  std::vector<QrP<double>> step(batch);
+  fill(false, step);
+  run(step, false);
+  bool more = true;
+  while (more) {
+    more = false;
+    for (int b = 0; b < batch; ++b) more = more || done[b] < qp[b].m;
+    fill(true, step);  // with no rows left this only clears the reflectors under R11
+    run(step, !more);
+  }
+}
+
 void HSS2D::compute_T(int lev) {
   auto& g = geo.levels[lev];
   auto& d = L[lev];
@@ -669,10 +762,14 @@ void HSS2D::compute_T(int lev) {
       qp[b] = QrP<double>{A.p + aoff[b], pm, n, k, pm, V.p + (size_t)b * (p + tk) * QR_NB,
                           Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * k, X, k};
     }
-    DevBuf<QrP<double>> dqp(batch);
-    HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
-    lstsq_batched<double>(dqp.p, batch, p + tk, n, k, stream, dftree());
-    HSS_CUDA(cudaStreamSynchronize(stream));
+    if (p + tk <= panel_limit(LSTSQ_MAX_ROWS)) {
+      DevBuf<QrP<double>> dqp(batch);
+      HSS_CUDA(cudaMemcpyAsync(dqp.p, qp.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, stream));
+      lstsq_batched<double>(dqp.p, batch, p + tk, n, k, stream, dftree());
+      HSS_CUDA(cudaStreamSynchronize(stream));
+    } else {
+      lstsq_tsqr(qp, n, k);
+    }
     qlev[lev] = nr;  // a dense T.U is k x nr
   }
   // T_up came from the even problems, T_dn from the odd ones
@@ -849,12 +946,68 @@ void HSS2D::invert_impl() {
 
 template <typename R>
 void HSS2D::invert_level(R* A, int n, int nb) {
+  if (n > panel_limit(GJ_MAX_N)) {
+    invert_level_schur<R>(A, n, nb);
+    return;
+  }
+  invert_level_ld<R>(A, n, n, nb, (size_t)n * n);
+}
+
+// Blocks above the cluster panel's size, by the 2 x 2 block inverse: with the leading n1 x n1
+// block A11 and S = A22 - A21 A11^-1 A12,
+//   A^-1 = [[A11^-1 + Z Y, -Z], [-S^-1 Y, S^-1]],  Y = A21 A11^-1, Z = A11^-1 A12 S^-1,
+// two inversions of half size and six products, in place.  A11 is a diagonal block of the
+// HSS system (at the root: the first child's E), inverted with partial pivoting.
+template <typename R>
+void HSS2D::invert_level_schur(R* A, int n, int nb) {
+  const int n1 = (n / 2) & ~1, n2 = n - n1;
+  HSS_REQUIRE(n2 <= GJ_MAX_N, HSS_ERR_ARG, "block too large for the two-level inversion");
+  HSS_REQUIRE(n1 >= 2, HSS_ERR_ARG, "two-level inversion of a tiny block");
+  DevBuf<GemmP<R>> gs;
+  DevBuf<R> Ai((size_t)nb * n1 * n1), X((size_t)nb * n1 * n2), Y((size_t)nb * n2 * n1);
+  auto blk = [&](int i, int r, int c) { return A + (size_t)i * n * n + r + (size_t)c * n; };
+  k_copy2d<R, R><<<grid_for((long long)nb * n1 * n1), 256, 0, stream>>>(nb, n1, n1, A, (long long)n * n, n, Ai.p,
+                                                                        (long long)n1 * n1, n1);
+  check_launch("schur copy");
+  invert_level_ld<R>(Ai.p, n1, n1, nb, (size_t)n1 * n1);
+  std::vector<GemmP<R>> P;
+  auto gemm = [&](auto mk, R alpha, R beta) {
+    P.clear();
+    for (int i = 0; i < nb; ++i) P.push_back(mk(i));
+    run_gemm<R>(P, false, false, alpha, beta, stream, gs, dfgemm());
+  };
+  const R* Aip = Ai.p;
+  // X = A11^-1 A12, Y = A21 A11^-1
+  gemm([&](int i) { return GemmP<R>{Aip + (size_t)i * n1 * n1, blk(i, 0, n1), X.p + (size_t)i * n1 * n2, n1, n2, n1, n1, n, n1}; },
+       R(1), R(0));
+  gemm([&](int i) { return GemmP<R>{blk(i, n1, 0), Aip + (size_t)i * n1 * n1, Y.p + (size_t)i * n2 * n1, n2, n1, n1, n, n1, n2}; },
+       R(1), R(0));
+  // S = A22 - A21 X in place, then S^-1 in place
+  gemm([&](int i) { return GemmP<R>{blk(i, n1, 0), X.p + (size_t)i * n1 * n2, blk(i, n1, n1), n2, n2, n1, n, n1, n}; },
+       R(-1), R(1));
+  invert_level_ld<R>(blk(0, n1, n1), n2, n, nb, (size_t)n * n);
+  // A12 = -Z = -X S^-1, A21 = -S^-1 Y, A11 = A11^-1 - A12 Y
+  gemm([&](int i) { return GemmP<R>{X.p + (size_t)i * n1 * n2, blk(i, n1, n1), blk(i, 0, n1), n1, n2, n2, n1, n, n}; },
+       R(-1), R(0));
+  gemm([&](int i) { return GemmP<R>{blk(i, n1, n1), Y.p + (size_t)i * n2 * n1, blk(i, n1, 0), n2, n1, n2, n, n2, n}; },
+       R(-1), R(0));
+  k_copy2d<R, R><<<grid_for((long long)nb * n1 * n1), 256, 0, stream>>>(nb, n1, n1, Ai.p, (long long)n1 * n1, n1, A,
+                                                                        (long long)n * n, n);
+  check_launch("schur copy");
+  gemm([&](int i) { return GemmP<R>{blk(i, 0, n1), Y.p + (size_t)i * n2 * n1, blk(i, 0, 0), n1, n1, n2, n, n2, n}; },
+       R(-1), R(1));
+  HSS_CUDA(cudaStreamSynchronize(stream));
+}
+
+// Gauss-Jordan inversion of nb blocks (n x n, leading dimension lda, block stride bs).
+template <typename R>
+void HSS2D::invert_level_ld(R* A, int n, int lda, int nb, size_t bs) {
   DevBuf<int> ipiv((size_t)nb * n), info(nb), aux((size_t)nb * GJ_AUX);
   DevBuf<R> W((size_t)nb * 2 * GJ_NB * n), Wf((size_t)nb * n * n);
   info.zero(stream);
   std::vector<InvP<R>> P(nb);
   for (int i = 0; i < nb; ++i)
-    P[i] = InvP<R>{A + (size_t)i * n * n, n, n, ipiv.p + (size_t)i * n, W.p + (size_t)i * 2 * GJ_NB * n,
+    P[i] = InvP<R>{A + (size_t)i * bs, n, lda, ipiv.p + (size_t)i * n, W.p + (size_t)i * 2 * GJ_NB * n,
                    Wf.p + (size_t)i * n * n, info.p + i, aux.p + (size_t)i * GJ_AUX};
   DevBuf<InvP<R>> dP(nb);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), nb * sizeof(InvP<R>), cudaMemcpyHostToDevice, stream));

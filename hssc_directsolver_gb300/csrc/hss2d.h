@@ -147,6 +147,7 @@ struct HSS2D {
   void id_level(int lev, const std::vector<std::vector<int>>& boxes, const std::vector<std::vector<double>>& px,
                 const std::vector<std::vector<double>>& py, std::vector<std::vector<int>>& perm, std::vector<int>& k);
   void id_T_level(int lev);
+  void lstsq_tsqr(const std::vector<QrP<double>>& qp, int n, int k);
   void build_tree();
   void compute_T(int lev);
   bool uses_lowrank(int lev) const;
@@ -169,6 +170,10 @@ struct HSS2D {
   void invert_impl();
   template <typename R>
   void invert_level(R* A, int n, int nb);
+  template <typename R>
+  void invert_level_schur(R* A, int n, int nb);
+  template <typename R>
+  void invert_level_ld(R* A, int n, int lda, int nb, size_t bs);
   template <typename R>
   SolvePlan<R>& inv_plan(int r);
   template <typename R>
