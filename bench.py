@@ -432,6 +432,54 @@ def bench_config5(args, L, dev):
     return out
 
 
+def bench_lippmann_schwinger(npan: int = 64, kh: float = 20.0):
+    """The Lippmann-Schwinger configuration: kh = 20, the Gaussian contrast exp(-|x|^2/0.1)
+    taken symmetrically, the order-4 Duan-Rokhlin diagonal, (8 npan)^2 grid with leaf 8 x 8,
+    tol 1e-10, 'rand' proxies, dense T; compress and invert in HSS_PREC_MIXED (FP32 inverse
+    factors: the complex64 inverse), complex128 GMRES on the compressed operator to 1e-8
+    preconditioned by that inverse.  Reports the stage seconds, GMRES steps and time, the
+    relative residual against the compressed operator and against the kernel matrix itself
+    on three samples of 4096 rows (the full O(N^2) product is not formed)."""
+    import torch
+    from hssc_directsolver_gb300 import hss2d as G2, kernels as GK
+    h = 2.0 / (8 * npan)
+    _, w, _ = GK.DR_stencil(h, kh, 8 * npan, 4)
+    sq = GK.Modulation(alpha=1.0, isig=5.0, kind=GK.MOD_GAUSS0)
+    prm = G2.HSS2DParams(Ng=8, npan=npan, layers=3, acc=1e-10, INTERform="dense", precision="mixed",
+                         kernel=GK.Kernel("SL_H_2D", h, sq, sq, kh, complex(w[0])), proxy_rule="rand")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tree = G2.HSS2D_build_tree_nsym(prm)
+    G2.HSS2D_compress_nsym(tree)
+    G2.HSS2D_invert_nsym(tree)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ph = tree.phase_times()
+    from hssc_directsolver_gb300.geometry import grid_points
+    X = grid_points(8, npan)
+    f = np.exp(-(X[:, 0] ** 2 + X[:, 1] ** 2) / 0.2) * np.exp(1j * kh * X[:, 0])
+    F = np.stack([f, np.random.default_rng(0).standard_normal(prm.N) + 0j], axis=1)
+    G2.HSS2D_gmres(tree, F[:, :1], tol=1e-8, restart=30, maxit=60, PRECOND=tree)  # warm the plans
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    x, rr, its = G2.HSS2D_gmres(tree, F, tol=1e-8, restart=30, maxit=60, PRECOND=tree)
+    t3 = time.perf_counter()
+    kr = []
+    for row0 in (0, prm.N // 2 - 2048, prm.N - 4096):
+        kr.append(G2.HSS2D_kernel_residual_rows(tree, row0, F[row0:row0 + 4096], x))
+    n, k, _ = tree.box_sizes()
+    return {"workload": f"HSS2D Lippmann-Schwinger kappa={kh:g}, contrast exp(-|x|^2/0.1) (symmetric), "
+                        f"{8 * npan}x{8 * npan} grid (N={prm.N}), leaf 8x8, tol 1e-10, 'rand' proxies, dense T",
+            "precision": "compress/invert HSS_PREC_MIXED (FP32 inverse factors), complex128 GMRES",
+            "compress_invert_s": t1 - t0,
+            "stages_s": {"tree_geometry_and_ID": float(ph[0]), "uploads": float(ph[1]),
+                         "interpolation_lstsq": float(ph[2]), "compress": float(ph[3]), "invert": float(ph[4])},
+            "gmres": {"nrhs": 2, "steps": its, "s_host_buffers": t3 - t2, "relres_compressed_operator": rr,
+                      "restart": 30, "tol": 1e-8},
+            "kernel_relres_rows": {"rows": "3 samples of 4096 rows (start, middle, end)", "values": kr},
+            "root_n": int(n[0]), "root_k_children": int(k[1])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -445,6 +493,9 @@ def main():
     ap.add_argument("--no-algebra", action="store_true", help="skip the HSS1D algebra section")
     ap.add_argument("--no-cpu-ci", action="store_true",
                     help="skip the CPU oracle's compress+invert (about a minute at the full workload)")
+    ap.add_argument("--no-ls", action="store_true",
+                    help="skip the Lippmann-Schwinger (complex HSS2D, 512 x 512) section")
+    ap.add_argument("--ls-npan", type=int, default=64)
     ap.add_argument("--config5", action="store_true",
                     help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
     ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv,tc",
@@ -641,6 +692,11 @@ def main():
         line["kernel_gen"] = kgen
     if algebra is not None:
         line["hss1d_algebra"] = algebra
+    if not args.no_ls:
+        try:
+            line["lippmann_schwinger"] = bench_lippmann_schwinger(args.ls_npan)
+        except Exception as e:  # reported, not fatal: the headline line still prints
+            line["lippmann_schwinger"] = {"error": str(e)}
     if args.config5:
         line["config5"] = bench_config5(args, L, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure

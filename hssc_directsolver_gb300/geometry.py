@@ -56,3 +56,16 @@ def batched_curves(count: int, nmin: int = 1024, nmax: int = 16384, seed: int = 
         out.append(fourier_curve(N, a, phi))
         sizes.append(N)
     return out, sizes
+
+
+def grid_points(Ng: int, npan: int) -> np.ndarray:
+    """The HSS2D grid in the solver's point order (params.X_source of
+    Common/HSS_tree_parameters.m:141-162): npan x npan panels of Ng x Ng midpoints on
+    [-1, 1]^2, panel-major (panel i at x = -1 + (i // npan) 2/npan, y = -1 + (i % npan) 2/npan),
+    y fastest inside a panel.  Returns (N, 2)."""
+    hh = 2.0 / (Ng * npan)
+    z = np.linspace(0.5 * hh, Ng * hh - 0.5 * hh, Ng)
+    corner = -1.0 + np.arange(npan) * (2.0 / npan)
+    px = np.repeat(corner, npan)[:, None] + np.repeat(z, Ng)[None, :]
+    py = np.tile(corner, npan)[:, None] + np.tile(z, Ng)[None, :]
+    return np.stack([px.ravel(), py.ravel()], axis=1)

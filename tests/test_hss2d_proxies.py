@@ -53,3 +53,10 @@ def test_rand_rule_retries_with_smaller_lambda():
         for n_src in (100, 2000):
             got = G2.proxy_points(gp, box, n_src)
             assert np.array_equal(got, _oracle_proxy(op, box, n_src))
+
+
+def test_grid_points_equal_oracle_source_points():
+    from oracle.geometry import grid_source
+    from hssc_directsolver_gb300.geometry import grid_points
+    for Ng, npan in ((8, 4), (7, 8), (8, 32)):
+        assert np.array_equal(grid_points(Ng, npan), grid_source(Ng, npan))
