@@ -2024,13 +2024,18 @@ __device__ void id_finish(const IdP& p, double acc, int l, int jdone, double* sh
 }
 
 
+constexpr double ID_TOL3Z = 1.4901161193847656e-08;  // sqrt(DBL_EPSILON), xLAQP2's threshold
+
 __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, double acc) {
   const IdP p = P[blockIdx.x];
   const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int l = min(m, n);
   double* W = p.W;
   extern __shared__ double s_dyn[];
-  double* norms = s_dyn;  // n
+  double* norms = s_dyn;  // n: trailing norms (squared), downdated
+  // n: each column's norm at its last exact computation, in the random-vector workspace
+  // (x is read only once the QR is done)
+  double* nref = p.x;
   __shared__ double sh[8];
   __shared__ double hs3[3];
   __shared__ double shv[8];
@@ -2042,7 +2047,7 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     double d = 0.0;
     for (int i = lane; i < m; i += 32) { const double v = W[i + (size_t)c * m]; d += v * v; }
     d = warp_sum(d);
-    if (lane == 0) norms[c] = d;
+    if (lane == 0) norms[c] = nref[c] = d;
   }
   __syncthreads();
   // Learned-rank mode: at step steps_hint, stop if |R_jj| is already below the
@@ -2077,6 +2082,7 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
       if (tid == 0) {
         const int t = p.perm[j]; p.perm[j] = p.perm[bi]; p.perm[bi] = t;
         const double u = norms[j]; norms[j] = norms[bi]; norms[bi] = u;
+        const double v = nref[j]; nref[j] = nref[bi]; nref[bi] = v;
       }
     }
     __syncthreads();
@@ -2089,18 +2095,35 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
     __syncthreads();
     if (tid == 0) W[j + (size_t)j * m] = beta;
     for (int c = j + 1 + w; c < n; c += 8) {
-      double d = W[j + (size_t)c * m] * (lane == 0 ? 1.0 : 0.0);
+      const double wjc = W[j + (size_t)c * m];
+      double d = wjc * (lane == 0 ? 1.0 : 0.0);
       for (int i = j + 1 + lane; i < m; i += 32) d += W[i + (size_t)j * m] * W[i + (size_t)c * m];
       d = warp_sum(d) * tau;
-      if (lane == 0) W[j + (size_t)c * m] -= d;
+      // downdate the column's trailing norm by its new row-j entry (LAPACK xLAQP2's rule,
+      // without divisions): recompute it exactly when the cancellation leaves less than
+      // sqrt(eps) of the norm last computed exactly.  Every lane takes the same decision
+      // from the same values.
+      const double nc = norms[c], r = wjc - d;
+      bool redo = false;
+      double nd = nc;
+      if (nc != 0.0) {
+        nd = fmax(0.0, __dadd_rn(nc, -__dmul_rn(r, r)));
+        redo = nd <= __dmul_rn(ID_TOL3Z, nref[c]);
+      }
+      __syncwarp();
+      if (lane == 0) W[j + (size_t)c * m] = r;
       double nn = 0.0;
       for (int i = j + 1 + lane; i < m; i += 32) {
         const double v = W[i + (size_t)c * m] - d * W[i + (size_t)j * m];
         W[i + (size_t)c * m] = v;
-        nn += v * v;
+        if (redo) nn += v * v;
       }
-      nn = warp_sum(nn);
-      if (lane == 0) norms[c] = nn;
+      if (redo) {
+        nn = warp_sum(nn);
+        if (lane == 0) norms[c] = nref[c] = nn;
+      } else if (lane == 0) {
+        norms[c] = nd;
+      }
     }
     __syncthreads();
   }
@@ -2186,7 +2209,10 @@ __global__ void __launch_bounds__(256) k_id_pairs(const IdP* __restrict__ P, dou
   const int lp = min(m, n) / 2;
   double* W = p.W;
   extern __shared__ double s_dyn[];
-  double* norms = s_dyn;  // n
+  double* norms = s_dyn;  // n: trailing norms (squared), downdated
+  // n: each column's norm at its last exact computation, in the random-vector workspace
+  // (x is read only once the QR is done)
+  double* nref = p.x;
   __shared__ double sh[8];
   __shared__ double hs3[3];
   __shared__ double shv[8];

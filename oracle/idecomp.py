@@ -1,11 +1,14 @@
 """Interpolative decomposition (oracle restatement of Common/ID.m).
 
 ``qr(A,0)`` with column pivoting (MATLAB/LAPACK xGEQP3) is restated as a
-Householder QR that, at every step, recomputes the exact 2-norms of the
-trailing parts of the remaining columns and picks the largest (lowest index on
-ties).  The CUDA kernel runs the same algorithm, so both pick the same pivots
-on the same matrix.  Reflectors follow LAPACK dlarfg:
-``beta = -sign(alpha)*||x||``, ``tau = (beta - alpha)/beta``,
+Householder QR that picks, at every step, the remaining column of largest trailing
+norm (lowest index on ties).  The trailing norms are downdated after each step as
+xGEQP3's panel routine does (LAPACK xLAQP2): with r the new row entry of column c,
+``temp = max(0, 1 - r^2 / n_c)``; if ``temp * n_c / n_ref_c <= sqrt(eps)`` the
+norm is recomputed exactly (and becomes the new reference n_ref_c), otherwise
+``n_c *= temp`` (squared norms throughout).  The CUDA kernel runs the same
+algorithm, so both pick the same pivots on the same matrix.  Reflectors follow
+LAPACK dlarfg: ``beta = -sign(alpha)*||x||``, ``tau = (beta - alpha)/beta``,
 ``v = x/(alpha - beta)`` with ``v[0] = 1``.
 """
 from __future__ import annotations
@@ -14,6 +17,8 @@ import numpy as np
 from scipy.linalg import solve_triangular
 
 from . import rng
+
+TOL3Z = float(np.sqrt(np.finfo(np.float64).eps))  # xLAQP2's recompute threshold
 
 
 def pivoted_qr(A: np.ndarray, pivot: bool = True):
@@ -25,6 +30,7 @@ def pivoted_qr(A: np.ndarray, pivot: bool = True):
     if l == 0:
         return np.zeros((0, n)), perm
     norms = np.einsum("ij,ij->j", A, A)
+    nref = norms.copy()
     for j in range(l):
         if pivot:
             p = j + int(np.argmax(norms[j:]))
@@ -32,6 +38,7 @@ def pivoted_qr(A: np.ndarray, pivot: bool = True):
                 A[:, [j, p]] = A[:, [p, j]]
                 perm[[j, p]] = perm[[p, j]]
                 norms[[j, p]] = norms[[p, j]]
+                nref[[j, p]] = nref[[p, j]]
         x = A[j:, j]
         alpha = x[0]
         xn2 = float(np.dot(x[1:], x[1:])) if x.shape[0] > 1 else 0.0
@@ -48,9 +55,20 @@ def pivoted_qr(A: np.ndarray, pivot: bool = True):
             if j + 1 < n:
                 w = v @ A[j:, j + 1:]
                 A[j:, j + 1:] -= tau * np.outer(v, w)
+        # downdate the trailing norms; recompute where cancellation has eaten the estimate
         if j + 1 < n:
-            tail = A[j + 1:, j + 1:]
-            norms[j + 1:] = np.einsum("ij,ij->j", tail, tail)
+            nc = norms[j + 1:]
+            live = nc != 0.0
+            r = A[j, j + 1:]
+            nd = np.maximum(0.0, nc - r * r)
+            redo = live & (nd <= TOL3Z * nref[j + 1:])
+            keep = live & ~redo
+            nc[keep] = nd[keep]
+            if redo.any():
+                cols = j + 1 + np.flatnonzero(redo)
+                t = A[j + 1:, cols]
+                nc[redo] = np.einsum("ij,ij->j", t, t)
+                nref[cols] = nc[redo]
     R = np.triu(A[:l, :])
     return R, perm
 
