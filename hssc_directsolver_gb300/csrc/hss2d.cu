@@ -1422,10 +1422,13 @@ void HSS2D::fwd_prepare(int r) {
       fp.up[lev].add(P, 1.0, 1.0, stream);
     }
   }
+  // every level's sibling and leaf products (lam) read only the finished upward pass and the
+  // input: one step holds them all (fp.lam[0]); the downward pass then runs eta and the
+  // scatters, which add onto what lam wrote
+  std::vector<GemmP<double>> P;
   for (int lev = 0; lev <= depth; ++lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
-    std::vector<GemmP<double>> P;
     for (int i = 0; i < g.nb; ++i) {
       double* out;
       int ldo;
@@ -1447,7 +1450,6 @@ void HSS2D::fwd_prepare(int r) {
                                   kc, gc.nb * kc, ldo});
       }
     }
-    fp.lam[lev].add(P, 1.0, 0.0, stream);
     const int nr = g.n - g.k;
     if (lev > 0 && nr > 0) {
       std::vector<GemmP<double>> Q;
@@ -1457,6 +1459,7 @@ void HSS2D::fwd_prepare(int r) {
       fp.eta[lev].add(Q, 1.0, 0.0, stream);
     }
   }
+  fp.lam[0].add(P, 1.0, 0.0, stream);
   HSS_CUDA(cudaStreamSynchronize(stream));
   if (autotune)
     for (int lev = 0; lev <= depth; ++lev) {
@@ -1489,11 +1492,10 @@ void HSS2D::apply_stage_body(int r) {
         (long long)g.nb * std::max(nr, 1));
     fp.up[lev].run(stream);
   }
-  for (int lev = 0; lev <= depth; ++lev) {
+  fp.lam[0].run(stream);  // every level's lam products
+  for (int lev = 1; lev <= depth; ++lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
-    fp.lam[lev].run(stream);
-    if (lev == 0) continue;
     const bool leaf = (lev == depth);
     const int kc = leaf ? 0 : geo.levels[lev + 1].k;
     double* dst = leaf ? Yd.p : L[lev + 1].dnF.p;
