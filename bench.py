@@ -496,6 +496,8 @@ def main():
     ap.add_argument("--no-ls", action="store_true",
                     help="skip the Lippmann-Schwinger (complex HSS2D, 512 x 512) section")
     ap.add_argument("--ls-npan", type=int, default=64)
+    ap.add_argument("--only-ls", action="store_true",
+                    help="run only the Lippmann-Schwinger section and print its JSON (profiling)")
     ap.add_argument("--config5", action="store_true",
                     help="also run the learned-rank configuration at scale (2048 curves, 1024^2 grid; ~1 min)")
     ap.add_argument("--paths", default="fp64,mixed,dfloat,dfloat_inv,tc",
@@ -505,6 +507,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_ls:
+        print(json.dumps({"lippmann_schwinger": bench_lippmann_schwinger(args.ls_npan)}), flush=True)
+        return
 
     import torch
     import torch.distributed as dist

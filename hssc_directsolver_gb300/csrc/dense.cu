@@ -1676,6 +1676,168 @@ __global__ void __launch_bounds__(256) k_qr_update_df(const QrP<double>* __restr
   }
 }
 
+// The same trailing update with the rows split over several CTAs (the top levels of a tree
+// have a few tall problems: one CTA per 32 columns leaves most SMs idle).
+// k_qr_wpart_df: CTA (x, y, z) forms the partial W = V^T A(rows of slice y, its 32 columns);
+// k_qr_apply_df: every CTA adds the slices' partials in slice order, forms W2 = Tf^T W and
+// updates its own rows.  The sums are fixed-order, so results do not depend on timing.
+__device__ __forceinline__ void qr_rows(int m, int j0, int rs, int y, int& rb, int& re) {
+  const int per = (((m - j0) + rs - 1) / rs + 31) & ~31;
+  rb = j0 + y * per;
+  re = min(m, rb + per);
+}
+
+__global__ void __launch_bounds__(256) k_qr_wpart_df(const QrP<double>* __restrict__ P, int j0, int rs,
+                                                     float2* __restrict__ wpart) {
+  const QrP<double> p = P[blockIdx.z];
+  if (j0 >= p.kf) return;
+  const int m = p.m, n = p.n, tid = threadIdx.x;
+  const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
+  const int c0 = jend + blockIdx.x * 32;
+  if (c0 >= n) return;
+  const int nc = min(32, n - c0);
+  int rb, re;
+  qr_rows(m, j0, rs, blockIdx.y, rb, re);
+  const double* A = p.A;
+  const size_t lda = p.lda;
+  const double* V = p.V;
+  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
+  __shared__ float Xh[32][33], Xl[32][33];
+  const int lo5 = tid & 31, hi3 = tid >> 5;
+  f32x2 sh[2] = {0ULL, 0ULL}, sl[2] = {0ULL, 0ULL};
+  for (int r0 = rb; r0 < re; r0 += 32) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, jj = e >> 5;
+      const int gi = r0 + i;
+      float h, l;
+      split_d2f((gi < re && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
+      Vh[i][jj] = h;
+      Vhn[i][jj] = -h;
+      Vln[i][jj] = -l;
+      split_d2f((gi < re && jj < nc) ? A[gi + (size_t)(c0 + jj) * lda] : 0.0, h, l);
+      Xh[i][jj] = h;
+      Xl[i][jj] = l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < 32; ++i) {
+      const float vh = Vh[i][lo5], vhn = Vhn[i][lo5], vln = Vln[i][lo5];
+      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int ca = hi3 + 16 * u, cb = ca + 8;
+        df_madd_x2(sh[u], sl[u], x2_pack(Xh[i][ca], Xh[i][cb]), x2_pack(Xl[i][ca], Xl[i][cb]), b2, bn2, bl2);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const f32x2 h = x2_add(sh[u], sl[u]);
+      sl[u] = x2_sub(sl[u], x2_sub(h, sh[u]));
+      sh[u] = h;
+    }
+    __syncthreads();
+  }
+  float2* wp = wpart + (((size_t)blockIdx.z * gridDim.x + blockIdx.x) * rs + blockIdx.y) * 1024;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    float h0, h1, l0, l1;
+    x2_unpack(sh[u], h0, h1);
+    x2_unpack(sl[u], l0, l1);
+    const int ca = hi3 + 16 * u, cb = ca + 8;
+    wp[lo5 * 32 + ca] = make_float2(h0, l0);
+    wp[lo5 * 32 + cb] = make_float2(h1, l1);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_qr_apply_df(const QrP<double>* __restrict__ P, int j0, int rs,
+                                                     const float2* __restrict__ wpart) {
+  const QrP<double> p = P[blockIdx.z];
+  if (j0 >= p.kf) return;
+  const int m = p.m, n = p.n, tid = threadIdx.x;
+  const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
+  const int c0 = jend + blockIdx.x * 32;
+  if (c0 >= n) return;
+  const int nc = min(32, n - c0);
+  int rb, re;
+  qr_rows(m, j0, rs, blockIdx.y, rb, re);
+  double* A = p.A;
+  const size_t lda = p.lda;
+  const double* V = p.V;
+  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
+  __shared__ float Xh[32][33], Xl[32][33];
+  __shared__ float Wh[32][33], Wl[32][33];
+  const int lo5 = tid & 31, hi3 = tid >> 5;
+  // W = the slices' partials, added in slice order
+  const float2* wp = wpart + ((size_t)blockIdx.z * gridDim.x + blockIdx.x) * rs * 1024;
+  for (int e = tid; e < 1024; e += 256) {
+    float h = 0.f, l = 0.f;
+    for (int y = 0; y < rs; ++y) {
+      const float2 v = wp[(size_t)y * 1024 + e];
+      df_add(h, l, v.x, v.y);
+    }
+    Wh[e >> 5][e & 31] = h;
+    Wl[e >> 5][e & 31] = l;
+  }
+  __syncthreads();
+  // W2[jj][cc] = sum_{a <= jj} Tf[a, jj] W[a][cc]  (Tf upper triangular)
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int cc = hi3 + 8 * q;
+    float th = 0.f, tl = 0.f;
+    if (lo5 < nbk)
+      for (int a = 0; a <= lo5; ++a) {
+        float fh, fl;
+        split_d2f(p.Tf[a + lo5 * QR_NB], fh, fl);
+        df_madd(th, tl, Wh[a][cc], Wl[a][cc], fh, fl);
+      }
+    Xh[lo5][cc] = th;
+    Xl[lo5][cc] = tl;
+  }
+  __syncthreads();
+  for (int r0 = rb; r0 < re; r0 += 32) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, jj = e >> 5;
+      const int gi = r0 + i;
+      float h, l;
+      split_d2f((gi < re && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
+      Vh[i][jj] = h;
+      Vhn[i][jj] = -h;
+      Vln[i][jj] = -l;
+    }
+    __syncthreads();
+    f32x2 ah[2] = {0ULL, 0ULL}, al[2] = {0ULL, 0ULL};
+    for (int jj = 0; jj < nbk; ++jj) {
+      const float vh = Vh[lo5][jj], vhn = Vhn[lo5][jj], vln = Vln[lo5][jj];
+      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int ca = hi3 + 16 * u, cb = ca + 8;
+        df_madd_x2(ah[u], al[u], x2_pack(Xh[jj][ca], Xh[jj][cb]), x2_pack(Xl[jj][ca], Xl[jj][cb]), b2, bn2, bl2);
+      }
+    }
+    const int gi = r0 + lo5;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const f32x2 h = x2_add(ah[u], al[u]);
+      const f32x2 l = x2_sub(al[u], x2_sub(h, ah[u]));
+      float h2[2], l2[2];
+      x2_unpack(h, h2[0], h2[1]);
+      x2_unpack(l, l2[0], l2[1]);
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int cc = hi3 + 16 * u + 8 * v;
+        if (gi >= re || cc >= nc) continue;
+        double* c = A + gi + (size_t)(c0 + cc) * lda;
+        float xh, xl;
+        split_d2f(*c, xh, xl);
+        df_add(xh, xl, -h2[v], -l2[v]);
+        *c = df_to_double(xh, xl);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One back-substitution block step: solve R[b0:b1,b0:b1] X[b0:b1, tile] =
 // C[b0:b1, tile] (C = A[0:kf, kf:n], already updated by the blocks below) and
 // update C[rows of this CTA's chunk of 0:b0, tile] -= R[.., b0:b1] X.  Every
@@ -1766,6 +1928,7 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   require_cluster_fits(k_qr_panel_cl<R>, cfg, C);
+  DevBuf<double> wpart;  // row-split partial W of the double-float update (float pairs)
   for (int j0 = 0; j0 < maxkf; j0 += QR_NB) {
     HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl<R>, dP, j0, cap));
     const int jend = std::min(j0 + QR_NB, maxkf);
@@ -1773,8 +1936,20 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
     if (ncols > 0) {
       if constexpr (std::is_same<R, double>::value) {
         if (df) {
-          k_qr_update_df<<<dim3(ceil_div(ncols, 32), batch), 256, 0, s>>>(dP, j0);
-          check_launch("k_qr_update_df");
+          const int cb = ceil_div(ncols, 32);
+          // rows split over CTAs when the problems are too few to fill the GPU twice
+          const int rs = std::max(1, std::min(std::min(16, std::max(1, (maxm - j0) / 512)),
+                                              ceil_div(2 * 4 * 152, (long long)cb * batch)));
+          if (rs == 1) {
+            k_qr_update_df<<<dim3(cb, batch), 256, 0, s>>>(dP, j0);
+            check_launch("k_qr_update_df");
+          } else {
+            wpart.ensure((size_t)batch * cb * rs * 1024 * 2);
+            k_qr_wpart_df<<<dim3(cb, rs, batch), 256, 0, s>>>(dP, j0, rs, reinterpret_cast<float2*>(wpart.p));
+            check_launch("k_qr_wpart_df");
+            k_qr_apply_df<<<dim3(cb, rs, batch), 256, 0, s>>>(dP, j0, rs, reinterpret_cast<const float2*>(wpart.p));
+            check_launch("k_qr_apply_df");
+          }
           continue;
         }
       }

@@ -63,8 +63,8 @@ def test_full_size_solution_equals_oracle(full, precision, tol):
     apply of its own factorization (dense T in both).  The two factorizations share every
     skeleton; their interpolation operators come from least squares of condition ~1e7 solved
     in different orders, so they agree to cond * eps and the FP64 inverse applies to ~2e-12
-    (measured 2.35e-12; dfloat 2.9e-12, dfloat_inv 2.2e-13; tc 1.8e-11, where one
-    tensor-core inverse apply already meets the solve tolerance)."""
+    (measured 2.35e-12 for the FP64 inverse apply; the refined solutions of the other paths
+    agree to the same level)."""
     from hssc_directsolver_gb300 import hss2d as G2
     prm, ot, blk, inv, F, xo = full
     p = _params(precision)
@@ -73,8 +73,10 @@ def test_full_size_solution_equals_oracle(full, precision, tol):
     if precision == "fp64":
         x = G2.HSS2D_applyinv_nsym(t, None, F)
     else:
-        x, rr, it = G2.HSS2D_solve(t, F, 1e-10, 6)
-        assert rr <= 1e-10
+        # refined to 1e-11 so that the comparison measures the factorizations, not where a
+        # 1e-10 stop happens to fall (a solve stopped at relres 1e-10 can sit ~1e-10 away)
+        x, rr, it = G2.HSS2D_solve(t, F, 1e-11, 6)
+        assert rr <= 1e-11
     d = np.linalg.norm(x - xo) / np.linalg.norm(xo)
     print(f"{precision}: relative difference from the oracle {d:.2e}")
     assert d <= tol
