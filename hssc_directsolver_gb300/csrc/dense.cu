@@ -1899,6 +1899,72 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
   }
 }
 
+// k_trsm_step with the update of the rows above in double-float arithmetic (the 32 x 32
+// block solve stays FP64): R(i, b0:b1) and X as float pairs, each product exact by FMA, the
+// 32-term sum in a (hi, lo) accumulator, subtracted from C in FP64.
+__global__ void __launch_bounds__(256) k_trsm_step_df(const QrP<double>* __restrict__ P, int blk) {
+  using R = double;
+  const QrP<R> p = P[blockIdx.z];
+  const int kf = p.kf, ncol = p.n - p.kf;
+  const int b0 = blk * 32;
+  if (b0 >= kf) return;
+  const int b1 = min(b0 + 32, kf), nb = b1 - b0;
+  const int c0 = blockIdx.x * 32;
+  if (c0 >= ncol) return;
+  const int rc0 = blockIdx.y * 256;
+  if (blockIdx.y > 0 && rc0 >= b0) return;
+  const int nc = min(32, ncol - c0);
+  R* A = p.A;
+  const size_t lda = p.lda;
+  R* C = A + (size_t)kf * lda;
+  __shared__ R Rs[32][33];
+  __shared__ R Xs[32][33];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int e = tid; e < 32 * 32; e += 256) {
+    const int i = e & 31, j = e >> 5;
+    Rs[i][j] = (i < nb && j < nb) ? A[(b0 + i) + (size_t)(b0 + j) * lda] : R(0);
+    Xs[i][j] = (i < nb && j < nc) ? C[(b0 + i) + (size_t)(c0 + j) * lda] : R(0);
+  }
+  __syncthreads();
+  for (int q = 0; q < 4; ++q) {
+    const int cc = w + 8 * q;
+    R x = Xs[lane][cc];
+    for (int r = nb - 1; r >= 0; --r) {
+      R xr = __shfl_sync(0xffffffffu, x, r);
+      xr = xr / Rs[r][r];
+      if (lane == r) x = xr;
+      if (lane < r) x -= Rs[lane][r] * xr;
+    }
+    Xs[lane][cc] = x;
+  }
+  __syncthreads();
+  if (blockIdx.y == 0) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int i = e & 31, j = e >> 5;
+      if (i < nb && j < nc) p.X[(b0 + i) + (size_t)(c0 + j) * p.ldx] = Xs[i][j];
+    }
+  }
+  __shared__ float Xh[32][33], Xl[32][33];
+  for (int e = tid; e < 32 * 32; e += 256) {
+    const int t = e & 31, j = e >> 5;
+    split_d2f(Xs[t][j], Xh[t][j], Xl[t][j]);
+  }
+  __syncthreads();
+  const int rend = min(b0, rc0 + 256);
+  for (int i = rc0 + tid; i < rend; i += 256) {
+    float rh[32], rl[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t) split_d2f((t < nb) ? A[i + (size_t)(b0 + t) * lda] : 0.0, rh[t], rl[t]);
+    for (int j = 0; j < nc; ++j) {
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int t = 0; t < 32; ++t) df_madd(sh, sl, rh[t], rl[t], Xh[t][j], Xl[t][j]);
+      double* c = C + i + (size_t)(c0 + j) * lda;
+      *c = (*c - (double)sh) - (double)sl;
+    }
+  }
+}
+
 template <typename R>
 void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, cudaStream_t s, bool df, bool solve) {
   if (batch <= 0 || maxkf <= 0) return;
@@ -1962,6 +2028,13 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   for (int blk = nblk - 1; blk >= 0; --blk) {
     const int rows_above = blk * 32;
     dim3 g(ceil_div(maxn, 32), std::max(1, ceil_div(rows_above, 256)), batch);
+    if constexpr (std::is_same<R, double>::value) {
+      if (df) {
+        k_trsm_step_df<<<g, 256, 0, s>>>(dP, blk);
+        check_launch("k_trsm_step_df");
+        continue;
+      }
+    }
     k_trsm_step<R><<<g, 256, 0, s>>>(dP, blk);
     check_launch("k_trsm_step");
   }
