@@ -33,6 +33,7 @@ HSS_MOD_GAUSS = 0
 HSS_MOD_BUMP = 1
 HSS_MOD_SQRT_BUMP = 2
 HSS_MOD_GAUSS0 = 3
+HSS_ID_STEP_TEST = 256
 HSS_PROXY_BDRY = 0
 HSS_PROXY_RAND = 1
 HSS_PREC_FP64 = 0

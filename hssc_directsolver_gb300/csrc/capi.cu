@@ -231,14 +231,18 @@ static void hss1d_make(hss1d_matrix** out, int nprob, const long long* N, const 
                        const unsigned long long* seeds, MLP* mlp = nullptr, bool sym = false,
                        int id_prec = HSS_PREC_FP64) {
   HSS_REQUIRE(out && X && kp && N && ldx, HSS_ERR_ARG, "NULL argument");
+  const bool step_test = (id_prec & HSS_ID_STEP_TEST) != 0;
+  id_prec &= ~HSS_ID_STEP_TEST;
   HSS_REQUIRE(id_prec == HSS_PREC_FP64 || id_prec == HSS_PREC_DFLOAT, HSS_ERR_ARG,
               "ID precision: HSS_PREC_FP64 or HSS_PREC_DFLOAT");
+  HSS_REQUIRE(!(step_test && mlp), HSS_ERR_ARG, "HSS_ID_STEP_TEST replaces the rank predictor: pass no model");
   require_device();
   *out = nullptr;
   auto* h = new hss1d_matrix{nullptr};
   try {
     h->impl = new HSS1D();
     h->impl->id_df = (id_prec == HSS_PREC_DFLOAT);
+    h->impl->id_step_test = step_test;
     h->impl->compress(nprob, N, X, ldx, leaf, acc, *kp, seeds, mlp, sym);
   } catch (...) {
     delete h->impl;

@@ -2303,7 +2303,8 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
   // look again after another half as many steps.  Pivoted QR with exact column
   // norms has non-increasing |R_jj|, so the rank count, the first k pivots and T
   // equal those of the full factorization.
-  int s_hint = (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
+  const bool every = (p.steps_hint == ID_EVERY_STEP);
+  int s_hint = every ? 1 : (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
   int jdone = l;
   for (int j = 0; j < l; ++j) {
     if (j == s_hint && j > 0) {
@@ -2311,7 +2312,7 @@ __global__ void __launch_bounds__(256) k_id_adaptive(const IdP* __restrict__ P, 
         jdone = j;
         break;
       }
-      s_hint = min(l, j + max(4, j / 2));
+      s_hint = every ? j + 1 : min(l, j + max(4, j / 2));
     }
     double best = -1.0;
     int bi = INT_MAX;
@@ -2595,7 +2596,8 @@ __global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ 
     if (lane == 0) norms[c] = make_float2(nh, nl);
   }
   __syncthreads();
-  int s_hint = (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
+  const bool every = (p.steps_hint == ID_EVERY_STEP);
+  int s_hint = every ? 1 : (p.steps_hint > 0) ? min(p.steps_hint, l) : l;
   int jdone = l;
   for (int j = 0; j < l; ++j) {
     if (j == s_hint && j > 0) {
@@ -2603,7 +2605,7 @@ __global__ void __launch_bounds__(256) k_id_adaptive_df(const IdP* __restrict__ 
         jdone = j;
         break;
       }
-      s_hint = min(l, j + max(4, j / 2));
+      s_hint = every ? j + 1 : min(l, j + max(4, j / 2));
     }
     // arg-max of the normalised float-pair norms (hi, then lo), lowest index among equals
     float bh = -1.f, bl = 0.f;

@@ -138,6 +138,9 @@ struct IdP {
 };
 
 constexpr int ID_QR_ONLY = -2;
+// steps_hint = ID_EVERY_STEP: the truncation test of the learned-rank mode at every step (the
+// plain per-step threshold rule, no model)
+constexpr int ID_EVERY_STEP = -3;
 
 // df: the pivoted QR in double-float arithmetic (k_id_adaptive_df), rank / T / check in FP64
 void id_adaptive_batched(const IdP* dP, int batch, double acc, cudaStream_t s, bool df = false);

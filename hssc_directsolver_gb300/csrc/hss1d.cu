@@ -495,6 +495,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
         const int hint = kh + std::max(4, (int)std::ceil(0.15 * kh));
         for (int s = 0; s < ps; ++s) ip[ps * q + s].steps_hint = hint;
       }
+    } else if (id_step_test) {
+      for (auto& q : ip) q.steps_hint = ID_EVERY_STEP;
     }
     DevBuf<IdP> dip;
     upload_vec(dip, ip, stream);

@@ -70,6 +70,7 @@ struct HSS1D {
   const std::vector<long long>& roJ() const { return rect ? oJd : oJ; }
   long long rows() const { return rect ? Mtot : Ntot; }
   bool id_df = false;  // the IDs' pivoted QR in double-float arithmetic (k_id_adaptive_df)
+  bool id_step_test = false;  // every ID's pivoted QR tests the truncation rule at every step
   bool kernel_op = false;  // the handle compresses the kernel matrix of its point table (compress)
   std::vector<long long> pN, pbase;   // points per problem, first global point
   std::vector<int> proot;              // root box of each problem

@@ -192,12 +192,14 @@ def HSS1D_apply_rect_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
 
 
 def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=None,
-                         predictor=None, id_precision: str = "fp64") -> HSS1DMatrix:
+                         predictor=None, id_precision: str = "fp64", step_test: bool = False) -> HSS1DMatrix:
     """Many independent curves compressed together (every level of every tree in the
     same launches).  Vectors of the returned matrix are the problems' vectors stacked.
     With a ``RankPredictor`` the IDs stop their pivoted QR early at the predicted rank;
-    the result equals the plain compress.  ``id_precision="dfloat"`` runs the IDs'
-    pivoted QR in double-float arithmetic (rank, T and the randomized check in FP64)."""
+    the result equals the plain compress.  ``step_test=True`` (no predictor) is the
+    model-free baseline: every pivoted QR tests the same stop rule at every step.
+    ``id_precision="dfloat"`` runs the IDs' pivoted QR in double-float arithmetic (rank, T
+    and the randomized check in FP64)."""
     mats = []
     for X in Xs:
         X = np.asarray(X, dtype=np.float64)
@@ -213,10 +215,12 @@ def HSS1D_compress_batch(Xs, TREE: int, acc: float, knl_params: Kernel, seeds=No
     sd = (C.c_uint64 * P)(*seeds)
     h = C.c_void_p()
     kp = knl_params.to_c()
-    if id_precision != "fp64":
-        prec = {"dfloat": L.HSS_PREC_DFLOAT}.get(id_precision)
+    if id_precision != "fp64" or step_test:
+        prec = {"fp64": L.HSS_PREC_FP64, "dfloat": L.HSS_PREC_DFLOAT}.get(id_precision)
         if prec is None:
             raise ValueError("id_precision must be 'fp64' or 'dfloat'")
+        if step_test:
+            prec |= L.HSS_ID_STEP_TEST
         L.check(L.lib().hss1d_compress_batch_ex(C.byref(h), P, N, ptrs, N, int(TREE), float(acc), C.byref(kp), sd,
                                                 predictor._h if predictor is not None else None, prec))
     elif predictor is None:

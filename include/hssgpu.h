@@ -275,7 +275,10 @@ int hss1d_compress_batch_learned(hss1d_matrix** out, int32_t nprob, const int64_
 /* hss1d_compress_batch with options: M (NULL or a rank predictor as in
  * hss1d_compress_batch_learned) and the arithmetic of the IDs' pivoted QR: HSS_PREC_FP64
  * (the reference's ID, exact-rank parity) or HSS_PREC_DFLOAT (double-float QR on the FP32
- * pipes, ~2^-48 per operation; rank, T and the randomized check stay FP64). */
+ * pipes, ~2^-48 per operation; rank, T and the randomized check stay FP64).
+ * id_precision | HSS_ID_STEP_TEST (M NULL): the model-free baseline of the learned mode,
+ * every pivoted QR testing the same stop rule at every step. */
+#define HSS_ID_STEP_TEST 256
 int hss1d_compress_batch_ex(hss1d_matrix** out, int32_t nprob, const int64_t* N, const double* const* X,
                             const int64_t* ldx, int32_t leaf, double acc, const hss_kernel_params* kp,
                             const uint64_t* seeds, hss_mlp* M, int32_t id_precision);

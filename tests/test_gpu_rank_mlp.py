@@ -136,3 +136,28 @@ def test_untrained_predictor_still_exact(curves):
     _same_compress(G1, A, B)
     done, full, _ = B.id_stats()
     assert done <= full
+
+
+def test_learned_against_the_per_step_rule(curves):
+    """The model-free baseline the learned mode must be weighed against: the same stop rule
+    tested at every step of every pivoted QR (HSS_ID_STEP_TEST).  Both give the plain
+    compress's ranks, skeletons and T; the QR steps and reruns of each are reported (the
+    per-step rule can stop no later than the hint, and pays in reruns when the randomized
+    check relaxes the threshold past where it stopped)."""
+    import time
+    G1, GK, GG, Xs, sizes, kern, H, P, loss, F, y = curves
+    Xn, sn = GG.batched_curves(6, nmin=1500, nmax=5000, seed=99)
+    t = {}
+    mats = {}
+    for name, kw in (("plain", {}), ("learned", {"predictor": P}), ("per_step", {"step_test": True})):
+        t0 = time.perf_counter()
+        mats[name] = G1.HSS1D_compress_batch(Xn, 64, 1e-10, kern, **kw)
+        t[name] = time.perf_counter() - t0
+    _same_compress(G1, mats["plain"], mats["learned"])
+    _same_compress(G1, mats["plain"], mats["per_step"])
+    done_p, full, _ = mats["plain"].id_stats()
+    done_l, _, re_l = mats["learned"].id_stats()
+    done_s, _, re_s = mats["per_step"].id_stats()
+    print(f"QR steps: full {full}, learned {done_l} ({re_l} reruns), per-step rule {done_s} ({re_s} reruns); "
+          f"compress s: plain {t['plain']:.3f}, learned {t['learned']:.3f}, per-step {t['per_step']:.3f}")
+    assert done_p == full and done_l < full and done_s < full
