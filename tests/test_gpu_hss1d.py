@@ -569,3 +569,34 @@ def test_block_submatrix_apply(gpu):
                   [Kd[2][np.ix_(I_dn[1][0], I_up[1][0])], Kd[3][np.ix_(I_dn[1][1], I_up[1][1])]]])
     assert Y.shape == (k1 + k2, 2)
     assert np.linalg.norm(Y - A @ X) <= 1e-9 * np.linalg.norm(A @ X)
+
+
+def test_fsym_sum_and_low_rank_forms(gpu):
+    """HSS1D_sum_fsym and HSS1D_compressLR_fsym (the nsym algorithms, which take fsym
+    operands, T_DN = T_UP, unchanged): the sum of two fsym compressions of symmetric kernels
+    and the compressed U U^T equal their dense matrices to the tolerance, and the sum inverts
+    and solves against its dense matrix."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    rng = np.random.default_rng(21)
+    N = 1500
+    X = geometry.star_curve(N)
+    h = 2 * np.pi / N
+    ka = GK.Kernel("SL_L_2D", np.sqrt(h))
+    A = G1.HSS1D_compress_fsym("green", X, 64, 1e-12, ka)
+    B = G1.HSS1D_scalarmult(0.5, G1.HSS1D_compress_fsym("green", X, 64, 1e-12, ka))
+    Ad = G1.HSS1D_dense_matrix(A)
+    C = G1.HSS1D_sum_fsym(A, B, 1e-10)
+    Cd = G1.HSS1D_dense_matrix(C)
+    assert np.linalg.norm(Cd - 1.5 * Ad) <= 1e-9 * np.linalg.norm(Ad)
+    U = rng.standard_normal((N, 7))
+    H = G1.HSS1D_compressLR_fsym(U, U, 64, 1e-10)
+    Hd = G1.HSS1D_dense_matrix(H)
+    assert np.linalg.norm(Hd - U @ U.T) <= 1e-10 * np.linalg.norm(U @ U.T)
+    S = G1.HSS1D_sum_fsym(C, G1.HSS1D_scalarmult(1e-4, H), 1e-10)
+    Sd = 1.5 * Ad + 1e-4 * U @ U.T
+    G1.HSS1D_invert_nsym(S)
+    f = rng.standard_normal(N)
+    x, rr, _ = G1.HSS1D_solve(S, f, tol=1e-10)
+    assert rr < 1e-10
+    xd = np.linalg.solve(Sd, f)
+    assert np.linalg.norm(x - xd) <= 1e-7 * np.linalg.norm(xd)
