@@ -34,6 +34,9 @@ HSS_MOD_BUMP = 1
 HSS_MOD_SQRT_BUMP = 2
 HSS_MOD_GAUSS0 = 3
 HSS_ID_STEP_TEST = 256
+HSS_SKEL_BDRY = 0
+HSS_SKEL_RAND = 1
+HSS_SKEL_ID = 2
 HSS_PROXY_BDRY = 0
 HSS_PROXY_RAND = 1
 HSS_PREC_FP64 = 0
@@ -57,7 +60,8 @@ class hss2d_params(C.Structure):
     _fields_ = [("Ng", C.c_int32), ("npan", C.c_int32), ("layers", C.c_int32), ("interform", C.c_int32),
                 ("transinv", C.c_int32), ("sym", C.c_int32), ("precision", C.c_int32), ("pad_", C.c_int32),
                 ("acc", C.c_double), ("kp", hss_kernel_params), ("k_cut", C.c_int32), ("pad2_", C.c_int32),
-                ("seed", C.c_uint64), ("proxy_rule", C.c_int32), ("pad3_", C.c_int32), ("lambda", C.c_double)]
+                ("seed", C.c_uint64), ("proxy_rule", C.c_int32), ("pad3_", C.c_int32), ("lambda", C.c_double),
+                ("skel_rule", C.c_int32), ("pad4_", C.c_int32)]
 
 
 class HSSError(RuntimeError):

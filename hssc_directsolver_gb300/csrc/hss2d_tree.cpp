@@ -162,10 +162,11 @@ static void preset_skeleton(const std::vector<double>& X, const std::vector<int>
 // probability 2^(-lam l) by dyadic distance band l.  The reference resets MATLAB's generator
 // (the Mersenne Twister with its default seed 5489) on every call; the uniforms are that
 // generator's 53-bit doubles (two 32-bit draws, a >> 5 and b >> 6, (a 2^26 + b) 2^-53).
-static void random_sampler(std::vector<double>& px, std::vector<double>& py, double cx, double cy, double colrad,
-                           double rowrad, double lam, int lay, double h) {
+static std::vector<char> sampler_mask(const std::vector<double>& px, const std::vector<double>& py, double cx,
+                                      double cy, double colrad, double rowrad, double lam, int lay, double h) {
   const size_t n = px.size();
-  if (n == 0) return;
+  std::vector<char> keep(n, 0);
+  if (n == 0) return keep;
   std::vector<double> D(n);
   double rad = 0.0;
   for (size_t i = 0; i < n; ++i) {
@@ -174,7 +175,6 @@ static void random_sampler(std::vector<double>& px, std::vector<double>& py, dou
   }
   const double width = lay * h;
   const int sz = -(int)std::floor(std::log2(width / rad)) + 1;
-  std::vector<char> keep(n);
   for (size_t i = 0; i < n; ++i) keep[i] = D[i] < width;
   if (sz > 0) {
     std::mt19937 gen(5489u);
@@ -188,11 +188,52 @@ static void random_sampler(std::vector<double>& px, std::vector<double>& py, dou
       keep[i] = u < P;
     }
   }
+  return keep;
+}
+
+static void random_sampler(std::vector<double>& px, std::vector<double>& py, double cx, double cy, double colrad,
+                           double rowrad, double lam, int lay, double h) {
+  const std::vector<char> keep = sampler_mask(px, py, cx, cy, colrad, rowrad, lam, lay, h);
   size_t o = 0;
-  for (size_t i = 0; i < n; ++i)
+  for (size_t i = 0; i < px.size(); ++i)
     if (keep[i]) { px[o] = px[i]; py[o] = py[i]; ++o; }
   px.resize(o);
   py.resize(o);
+}
+
+// LOCAL_Preset_Skeleton_Info 'rand' (:703-730): the box's own points sampled (each retry on
+// the full set with 0.9 lambda) until the sample reaches k0 / 1.1, k0 = ceil(2/3 n) (even
+// levels) or ceil(3/4 n); ordered as the 'bdry' rule orders its sets.
+static void random_skeleton(const std::vector<double>& X, const std::vector<int>& I_src, double cx, double cy,
+                            int lev, double colrad, double rowrad, int layers, double h, double lambda,
+                            std::vector<int>& J, int& k) {
+  const int n = (int)I_src.size();
+  std::vector<double> x(n), y(n);
+  for (int i = 0; i < n; ++i) { x[i] = X[2 * (size_t)I_src[i]]; y[i] = X[2 * (size_t)I_src[i] + 1]; }
+  const int k0 = (lev % 2 == 0) ? (int)std::ceil((2.0 / 3.0) * n) : (int)std::ceil((3.0 / 4.0) * n);
+  double lam = lambda;
+  int kk = 0;
+  std::vector<char> keep(n, 0);
+  while (k0 > 1.1 * kk) {
+    keep = sampler_mask(x, y, cx, cy, colrad, rowrad, lam, layers, h);
+    kk = 0;
+    for (char c : keep) kk += c ? 1 : 0;
+    if (k0 > 1.1 * kk) lam = 0.9 * lam;
+  }
+  std::vector<int> sk, rs;
+  for (int i = 0; i < n; ++i) (keep[i] ? sk : rs).push_back(i);
+  int nrm;
+  double th0;
+  level_orientation(lev, nrm, th0);
+  std::vector<double> rx(rs.size()), ry(rs.size()), sx(sk.size()), sy(sk.size());
+  for (size_t i = 0; i < rs.size(); ++i) { rx[i] = x[rs[i]]; ry[i] = y[rs[i]]; }
+  for (size_t i = 0; i < sk.size(); ++i) { sx[i] = x[sk[i]]; sy[i] = y[sk[i]]; }
+  const std::vector<int> Jr = orient_residual(rx, ry, nrm);
+  const std::vector<int> Js = orient_skeleton(sx, sy, cx, cy, th0);
+  J.clear();
+  for (int v : Js) J.push_back(sk[v]);
+  k = (int)sk.size();
+  for (int v : Jr) J.push_back(rs[v]);
 }
 
 // LOCAL_Build_Proxy 'rand' (:883-905): the box's proxy layers sampled until at least
@@ -237,6 +278,10 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
   HSS_REQUIRE(prm.kp.flag == HSS_SL_L_2D || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
               "HSS2D takes the SL_L_2D and SL_H_2D kernels");
   HSS_REQUIRE(prm.proxy_rule == HSS_PROXY_BDRY || prm.proxy_rule == HSS_PROXY_RAND, HSS_ERR_ARG, "unknown proxy rule");
+  HSS_REQUIRE(prm.skel_rule == HSS_SKEL_BDRY || prm.skel_rule == HSS_SKEL_RAND || prm.skel_rule == HSS_SKEL_ID,
+              HSS_ERR_ARG, "unknown skeleton rule");
+  HSS_REQUIRE(prm.skel_rule != HSS_SKEL_ID || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
+              "the 'ID' skeleton rule is built for kh > 0 trees");
   const int Ng = prm.Ng, np = prm.npan;
   const double hh = 2.0 / (double)(Ng * np);
   const double hp = 2.0 / (double)np;
@@ -324,7 +369,7 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
       level_proxy(prm, lev, T.cent[2 * b], T.cent[2 * b + 1], (int)I_src[b].size(), PX[i], PY[i]);
     }
     // kh > 0: the two finest levels take their skeletons from the ID of K(proxies, box)
-    L.id_level = helm && lev >= depth - 1;
+    L.id_level = helm && (lev >= depth - 1 || prm.skel_rule == HSS_SKEL_ID);
     if (L.id_level) {
       HSS_REQUIRE(id_level != nullptr, HSS_ERR_ARG, "kh > 0 tree without an ID step");
       std::vector<std::vector<int>> boxes(I_src.begin() + b0, I_src.begin() + b0 + L.nb);
@@ -374,6 +419,9 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
           // (INFO_TREE.LEV(l) of HSS2D_build_tree_nsym.m:438-449, 499-540)
           Jall[i] = Jall[0];
           kall[i] = kall[0];
+        } else if (prm.skel_rule == HSS_SKEL_RAND) {
+          random_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad, prm.layers,
+                          hh, prm.lambda > 0 ? prm.lambda : 2.0, Jall[i], kall[i]);
         } else {
           preset_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad, prm.layers,
                           hh, Jall[i], kall[i]);

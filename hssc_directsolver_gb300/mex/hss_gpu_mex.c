@@ -174,6 +174,14 @@ static void hss2d_params_of(const mxArray* params, hss2d_params* p) {
     else if (!strcmp(buf, "dfloat_inv")) p->precision = HSS_PREC_DFLOAT_INV;
     else if (!strcmp(buf, "tc")) p->precision = HSS_PREC_TC;
   }
+  p->proxy_rule = HSS_PROXY_BDRY;
+  if (field_str(params, "proxy_rule", buf, sizeof buf) && !strcmp(buf, "rand")) p->proxy_rule = HSS_PROXY_RAND;
+  p->skel_rule = HSS_SKEL_BDRY;
+  if (field_str(params, "skel_rule", buf, sizeof buf)) {
+    if (!strcmp(buf, "rand")) p->skel_rule = HSS_SKEL_RAND;
+    else if (!strcmp(buf, "ID")) p->skel_rule = HSS_SKEL_ID;
+  }
+  p->lambda = field_or(params, "lambda", 2.0);
   kernel_params(params, &p->kp);
 }
 

@@ -51,6 +51,14 @@ extern "C" {
 #define HSS_MOD_GAUSS0 3    /* alpha exp(-isig |p - p0|^2) without the constant: a Gaussian
                                contrast taken symmetrically (b = c = its square root, isig halved) */
 
+/* HSS2D skeleton rules (params.skel_rule, HSS2D_build_tree_nsym.m:399-412, :668-730); every
+ * box of a level then holds the level's largest count (residual points nearest the box
+ * boundary promoted) */
+#define HSS_SKEL_BDRY 0 /* the points within layers h of the box boundary */
+#define HSS_SKEL_RAND 1 /* a random sample of the box's points (LOCAL_random_sampler until
+                           ceil(2/3 n) or ceil(3/4 n) / 1.1 are kept) */
+#define HSS_SKEL_ID 2   /* the ID of K(proxies, box) on every level (kh > 0 trees) */
+
 /* HSS2D box proxies (params.proxy_rule, HSS2D_build_tree_nsym.m:870-961) */
 #define HSS_PROXY_BDRY 0 /* every point of the box's proxy layers (build_box_proxy.m:52-88) */
 #define HSS_PROXY_RAND 1 /* the layers sampled with probability 2^(-lambda l) by dyadic distance
@@ -303,7 +311,9 @@ typedef struct hss2d_params {
   uint64_t seed;     /* key of the randomized ID's Gaussian samples */
   int32_t proxy_rule; /* HSS_PROXY_BDRY or HSS_PROXY_RAND (params.proxy_rule) */
   int32_t pad3_;
-  double lambda;      /* params.lambda of HSS_PROXY_RAND (0: 2) */
+  double lambda;      /* params.lambda of the 'rand' rules (0: 2) */
+  int32_t skel_rule;  /* HSS_SKEL_BDRY, HSS_SKEL_RAND or HSS_SKEL_ID (params.skel_rule) */
+  int32_t pad4_;
 } hss2d_params;
 
 /* INFO_TREE = HSS2D_build_tree_nsym(params), HSS2D/HSS2D_build_tree_nsym.m:80-610

@@ -53,6 +53,9 @@ class HSS2DParams:
     uniform_ranks: bool = False
     # params.proxy_rule / lambda / skel_extra_pts (HSS_tree_parameters.m:121-124)
     proxy_rule: str = "bdry"
+    # params.skel_rule (HSS2D_build_tree_nsym.m:399-412, :668-730): 'bdry' boundary layers,
+    # 'rand' a random sample of the box's points, 'ID' the ID of K(proxies, box) on every level
+    skel_rule: str = "bdry"
     lambda_: float = 2.0
     skel_extra_pts: int = 0
 
@@ -264,11 +267,15 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             if prm.transinv and b != first:
                 followers.append(b)
                 continue
-            if prm.kp.flag == SL_H_2D and lev >= depth - 1:
-                # :399-412 -- kh > 0: skeletons by the ID on the two finest levels
+            if prm.skel_rule == "ID" or (prm.kp.flag == SL_H_2D and lev >= depth - 1):
+                # :399-412 -- kh > 0: skeletons by the ID on the two finest levels (on
+                # every level with skel_rule 'ID')
                 ids[b] = (X_src, id_box(prm, Xp, X_src, b))
                 continue
-            presets[b] = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
+            if prm.skel_rule == "rand":
+                presets[b] = random_skeleton(X_src, cent[b], lev, colrad, rowrad, prm)
+            else:
+                presets[b] = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
         if prm.uniform_ranks and presets:
             # the boundary-layer counts of boxes above ID levels differ; every box takes the
             # level's largest count, promoting the residual points nearest its boundary
@@ -370,6 +377,37 @@ def random_sampler(X, cB, colrad, rowrad, lam, lay, h):
     The reference resets MATLAB's generator (rng('default'): the Mersenne Twister with its
     default seed, 5489) on every call; numpy's RandomState(5489) is that generator, so the
     same uniforms are drawn (not verified against MATLAB here)."""
+    return X[sampler_mask(X, cB, colrad, rowrad, lam, lay, h)]
+
+
+def random_skeleton(X_src, cB, lev, colrad, rowrad, prm: HSS2DParams):
+    """LOCAL_Preset_Skeleton_Info 'rand' (:703-730): the box's own points sampled by
+    LOCAL_random_sampler (each retry on the full set with 0.9 lambda) until the sample
+    reaches k0 / 1.1, k0 = ceil(2/3 n) (even levels) or ceil(3/4 n); skeleton and residual
+    ordered as the 'bdry' rule orders them.  Returns (J, k)."""
+    n = X_src.shape[0]
+    k0 = math.ceil((2 / 3) * n) if lev % 2 == 0 else math.ceil((3 / 4) * n)
+    lam, k = prm.lambda_, 0
+    keep = np.zeros(n, dtype=bool)
+    while k0 > 1.1 * k:
+        keep = sampler_mask(X_src, cB, colrad, rowrad, lam, prm.layers, prm.h)
+        k = int(keep.sum())
+        if k0 > 1.1 * k:
+            lam = 0.9 * lam
+    if lev % 2 == 0:
+        nrm, tan, th0 = 0, 1, math.pi / 2
+    else:
+        nrm, tan, th0 = 1, 0, 0.0
+    idx = np.arange(n)
+    I_rs = idx[~keep]
+    I_rs = I_rs[orient_residual(X_src[~keep], nrm, tan)]
+    I_sk = idx[keep]
+    I_sk = I_sk[orient_skeleton(X_src[keep], cB, th0)]
+    return np.concatenate([I_sk, I_rs]), len(I_sk)
+
+
+def sampler_mask(X, cB, colrad, rowrad, lam, lay, h):
+    """The kept-point mask of LOCAL_random_sampler (random_sampler returns X[mask])."""
     D = np.abs(np.minimum(colrad - np.abs(X[:, 0] - cB[0]), rowrad - np.abs(X[:, 1] - cB[1])))
     width = lay * h
     rad = D.max()
@@ -382,7 +420,7 @@ def random_sampler(X, cB, colrad, rowrad, lam, lay, h):
     if sz > 0:
         P = prob[Ld.astype(np.int64) - 1]
         B = np.random.RandomState(5489).random_sample(P.shape[0]) < P
-    return X[B]
+    return B
 
 
 def random_proxy(X_ext, n_skel, cB, colrad, rowrad, lev, prm: HSS2DParams):

@@ -376,3 +376,33 @@ def test_autotuned_plans(gpu):
     assert np.array_equal(x1, x2)
     y = G2.HSS2D_apply_nsym(t, None, x1)
     assert np.linalg.norm(y - f, axis=0).max() / np.linalg.norm(f, axis=0).min() <= 1e-10
+
+
+@pytest.mark.parametrize("npan", [4, 8])
+def test_random_skeleton_rule_matches_oracle(gpu, npan):
+    """params.skel_rule = 'rand' (LOCAL_Preset_Skeleton_Info :703-730): a random sample of
+    each box's points (the Mersenne Twister reset to seed 5489 per box, as the reference's
+    rng('default')), every box of a level raised to the level's largest count by promoting
+    the residual points nearest its boundary.  Skeletons equal the oracle's; the forward
+    apply agrees to 1e-13 and the inverse apply to the FP64 parity level."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    p = params(npan, "fp64")
+    p.skel_rule = "rand"
+    p.INTERform = "dense"
+    kp = OK.KernelParams(flag=OK.SL_L_2D, h=2.0 / (8 * npan), c=OK.Modulation(0.5, 0, 0, 20.0))
+    prm = O2.HSS2DParams(Ng=8, npan=npan, kp=kp, skel_rule="rand", uniform_ranks=True)
+    ot = O2.build_tree_nsym(prm)
+    blk = O2.compress_nsym(ot, prm)
+    inv = O2.invert_nsym(ot, prm, blk)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(p))
+    _, k, _ = t.box_sizes()
+    for b in range(t.nboxes):
+        e = t.export_box(b)
+        assert k[b] == ot.k[b] and np.array_equal(e["J"], ot.J[b]) and np.array_equal(e["I_src"], ot.I_src[b]), b
+    q = np.random.default_rng(5).standard_normal((prm.N, 3))
+    y = G2.HSS2D_apply_nsym(t, None, q)
+    yo = O2.apply_nsym(ot, blk, q)
+    assert np.linalg.norm(y - yo) <= 1e-13 * np.linalg.norm(yo)
+    x = G2.HSS2D_applyinv_nsym(t, None, q)
+    xo = O2.applyinv_nsym(ot, inv, q)
+    assert np.linalg.norm(x - xo) <= 1e-11 * np.linalg.norm(xo)

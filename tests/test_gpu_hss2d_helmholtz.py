@@ -167,3 +167,26 @@ def test_gmres_real_laplace_with_fp64_inverse(gpu):
     assert np.linalg.norm(G2.HSS2D_apply_nsym(t, None, x) - F) <= 1e-11 * np.linalg.norm(F)
     x0, rr0, its0 = G2.HSS2D_gmres(t, F[:, :1], tol=1e-8, restart=60, maxit=300)
     assert rr0 <= 1e-8 and its0 > its
+
+
+def test_helmholtz_id_skeleton_rule(gpu):
+    """params.skel_rule = 'ID' (HSS2D_build_tree_nsym.m:402): the complex ID picks the
+    skeletons of every level; skeletons, sources and ranks equal the oracle's, the forward
+    and inverse applies agree with it."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    gp, op = _params(4)
+    gp.skel_rule = "ID"
+    op.skel_rule = "ID"
+    ot = O2.build_tree_nsym(op)
+    blk = O2.compress_nsym(ot, op)
+    inv = O2.invert_nsym(ot, op, blk)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(gp))
+    _, k, _ = t.box_sizes()
+    for b in range(t.nboxes):
+        e = t.export_box(b)
+        assert k[b] == ot.k[b] and np.array_equal(e["J"], ot.J[b]) and np.array_equal(e["I_src"], ot.I_src[b]), b
+    r = np.random.default_rng(8)
+    x = r.standard_normal((op.N, 2)) + 1j * r.standard_normal((op.N, 2))
+    y = G2.HSS2D_apply_nsym(t, None, x)
+    assert _rel(y, O2.apply_nsym(ot, blk, x)) <= 1e-13
+    assert _rel(G2.HSS2D_applyinv_nsym(t, None, y), O2.applyinv_nsym(ot, inv, y)) <= 1e-10
