@@ -37,6 +37,7 @@ HSS_ID_STEP_TEST = 256
 HSS_SKEL_BDRY = 0
 HSS_SKEL_RAND = 1
 HSS_SKEL_ID = 2
+HSS_SKEL_WDEC = 3
 HSS_PROXY_BDRY = 0
 HSS_PROXY_RAND = 1
 HSS_PREC_FP64 = 0

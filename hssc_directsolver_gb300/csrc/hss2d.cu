@@ -107,12 +107,13 @@ __global__ void k_copy2d(int nb, int m, int n, const S* __restrict__ src, long l
   }
 }
 
-// Tikhonov rows of a complex tree's interpolation least squares (one block per problem):
-// below the p proxy rows of [K11 | K21] the k x n block [lam I | 0], lam = 2^-40 ||K11||_F
-// (K11 = the first k columns; the embedding doubles the squared Frobenius norm).
+// Tikhonov rows of a damped interpolation least squares (one block per problem): below the p
+// proxy rows of [K11 | K21] the k x n block [lam I | 0], lam = 2^-40 ||K11||_F (K11 = the
+// first k columns; the embedding of a complex tree doubles the squared Frobenius norm).
 struct TikP {
   double* A;
   int p, n, k, ld;
+  double sq;  // ||K11||_F^2 per sum of squares of the block (1/2 for an embedded complex block)
 };
 __global__ void k_tikhonov_rows(const TikP* __restrict__ P) {
   const TikP q = P[blockIdx.x];
@@ -128,7 +129,7 @@ __global__ void k_tikhonov_rows(const TikP* __restrict__ P) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
     __syncthreads();
   }
-  const double lam = 0x1.0p-40 * sqrt(0.5 * sh[0]);
+  const double lam = 0x1.0p-40 * sqrt(q.sq * sh[0]);
   for (long long e = threadIdx.x; e < (long long)q.k * q.n; e += 256) {
     const int r = (int)(e % q.k), c = (int)(e / q.k);
     q.A[q.p + r + (size_t)c * q.ld] = (c == r) ? lam : 0.0;
@@ -716,8 +717,10 @@ void HSS2D::compute_T(int lev) {
   d.TdnT.alloc((size_t)nb * k * std::max(nr, 1));
   if (nr == 0 || k == 0) return;
   // per factor box: its proxy count (the 'rand' rule samples a different set per box); a
-  // complex tree's systems carry k Tikhonov rows under the proxy rows (k_tikhonov_rows)
-  const int tk = cplx ? k : 0;
+  // complex tree's systems, and those of the sampled and Whitney skeleton rules, carry k
+  // Tikhonov rows under the proxy rows (k_tikhonov_rows): their proxy systems are
+  // numerically rank deficient
+  const int tk = (cplx || prm.skel_rule != HSS_SKEL_BDRY) ? k : 0;
   std::vector<int> pb(nb);
   std::vector<long long> aoff(2 * nb + 1, 0);
   for (int i = 0; i < nb; ++i) {
@@ -742,7 +745,7 @@ void HSS2D::compute_T(int lev) {
   kgen_batched<double>(dkg.p, batch, (long long)p * n, view(pts), kdev, stream);
   if (tk > 0) {
     std::vector<TikP> tp(batch);
-    for (int b = 0; b < batch; ++b) tp[b] = TikP{A.p + aoff[b], pb[b / 2], n, k, pb[b / 2] + tk};
+    for (int b = 0; b < batch; ++b) tp[b] = TikP{A.p + aoff[b], pb[b / 2], n, k, pb[b / 2] + tk, cplx ? 0.5 : 1.0};
     DevBuf<TikP> dtp(batch);
     HSS_CUDA(cudaMemcpyAsync(dtp.p, tp.data(), batch * sizeof(TikP), cudaMemcpyHostToDevice, stream));
     k_tikhonov_rows<<<batch, 256, 0, stream>>>(dtp.p);

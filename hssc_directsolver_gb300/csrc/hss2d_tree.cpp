@@ -236,6 +236,61 @@ static void random_skeleton(const std::vector<double>& X, const std::vector<int>
   for (int v : Jr) J.push_back(rs[v]);
 }
 
+// LOCAL_Preset_Skeleton_Info 'wdec' (:668-701) over Common/Whitney_decomposition.m: on the
+// box's integer grid coordinates, the full boundary layers, then for each finer dyadic scale
+// i the lines at distance c_i from the box edges sampled every 2^max(i - ceil(layers/2), 0)
+// points (c_i a power of two below Ng, or Ng times one: the Ng x Ng panel grid).
+static void whitney_skeleton(const std::vector<double>& X, const std::vector<int>& I_src, double cx, double cy,
+                             int lev, double colrad, double rowrad, int layers, double h, int Ng,
+                             std::vector<int>& J, int& k) {
+  const int n = (int)I_src.size();
+  std::vector<long long> c1(n), c2(n);
+  long long max1 = 0, max2 = 0;
+  for (int i = 0; i < n; ++i) {
+    c1[i] = (long long)std::floor((-cx + (colrad - h / 2) + X[2 * (size_t)I_src[i]]) / h + 0.5);
+    c2[i] = (long long)std::floor((-cy + (rowrad - h / 2) + X[2 * (size_t)I_src[i] + 1]) / h + 0.5);
+    max1 = std::max(max1, c1[i]);
+    max2 = std::max(max2, c2[i]);
+  }
+  const long long dmax = std::max(max1, max2);
+  const int depth = (int)std::ceil(std::log2((double)dmax)) + 1;
+  const int freq = (layers + 1) / 2;
+  const int lNg = (int)std::ceil(std::log2((double)Ng));
+  std::vector<char> keep(n);
+  for (int i = 0; i < n; ++i)
+    keep[i] = c1[i] < layers || max1 - c1[i] < layers || c2[i] < layers || max2 - c2[i] < layers;
+  for (int d = 2; d <= depth; ++d) {
+    long long ci, mi;
+    if ((1LL << (d - 1)) < Ng) {
+      ci = 1LL << (d - 1);
+      mi = Ng;
+    } else {
+      ci = (long long)Ng << (d - 1 - lNg);
+      mi = 2 * ci;
+    }
+    const long long e = 1LL << std::max(d - freq, 0);
+    for (int i = 0; i < n; ++i) {
+      const bool a = (c1[i] == ci || c1[i] == max1 - ci) && (((c2[i] % mi) % e) == 0 || c2[i] == max2 - ci);
+      const bool b = (c2[i] == ci || c2[i] == max2 - ci) && (((c1[i] % mi) % e) == 0 || c1[i] == max1 - ci);
+      if (a || b) keep[i] = 1;
+    }
+  }
+  std::vector<int> sk, rs;
+  for (int i = 0; i < n; ++i) (keep[i] ? sk : rs).push_back(i);
+  int nrm;
+  double th0;
+  level_orientation(lev, nrm, th0);
+  std::vector<double> rx(rs.size()), ry(rs.size()), sx(sk.size()), sy(sk.size());
+  for (size_t i = 0; i < rs.size(); ++i) { rx[i] = X[2 * (size_t)I_src[rs[i]]]; ry[i] = X[2 * (size_t)I_src[rs[i]] + 1]; }
+  for (size_t i = 0; i < sk.size(); ++i) { sx[i] = X[2 * (size_t)I_src[sk[i]]]; sy[i] = X[2 * (size_t)I_src[sk[i]] + 1]; }
+  const std::vector<int> Jr = orient_residual(rx, ry, nrm);
+  const std::vector<int> Js = orient_skeleton(sx, sy, cx, cy, th0);
+  J.clear();
+  for (int v : Js) J.push_back(sk[v]);
+  k = (int)sk.size();
+  for (int v : Jr) J.push_back(rs[v]);
+}
+
 // LOCAL_Build_Proxy 'rand' (:883-905): the box's proxy layers sampled until at least
 // k0 = ceil(2/3 n) (even levels) or ceil(3/4 n) (odd) points remain, each retry sampling the
 // previous sample again with 0.9 lambda.
@@ -278,7 +333,8 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
   HSS_REQUIRE(prm.kp.flag == HSS_SL_L_2D || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
               "HSS2D takes the SL_L_2D and SL_H_2D kernels");
   HSS_REQUIRE(prm.proxy_rule == HSS_PROXY_BDRY || prm.proxy_rule == HSS_PROXY_RAND, HSS_ERR_ARG, "unknown proxy rule");
-  HSS_REQUIRE(prm.skel_rule == HSS_SKEL_BDRY || prm.skel_rule == HSS_SKEL_RAND || prm.skel_rule == HSS_SKEL_ID,
+  HSS_REQUIRE(prm.skel_rule == HSS_SKEL_BDRY || prm.skel_rule == HSS_SKEL_RAND || prm.skel_rule == HSS_SKEL_ID ||
+                  prm.skel_rule == HSS_SKEL_WDEC,
               HSS_ERR_ARG, "unknown skeleton rule");
   HSS_REQUIRE(prm.skel_rule != HSS_SKEL_ID || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
               "the 'ID' skeleton rule is built for kh > 0 trees");
@@ -419,6 +475,9 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
           // (INFO_TREE.LEV(l) of HSS2D_build_tree_nsym.m:438-449, 499-540)
           Jall[i] = Jall[0];
           kall[i] = kall[0];
+        } else if (prm.skel_rule == HSS_SKEL_WDEC) {
+          whitney_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad, prm.layers,
+                           hh, prm.Ng, Jall[i], kall[i]);
         } else if (prm.skel_rule == HSS_SKEL_RAND) {
           random_skeleton(T.X, I_src[b], T.cent[2 * b], T.cent[2 * b + 1], lev, L.colrad, L.rowrad, prm.layers,
                           hh, prm.lambda > 0 ? prm.lambda : 2.0, Jall[i], kall[i]);

@@ -45,7 +45,7 @@ class HSS2DParams:
     k_cut: int = 2500         # low-rank T only where k < k_cut
     seed: int = 0             # key of the randomized ID's Gaussian samples
     proxy_rule: str = "bdry"  # params.proxy_rule: "bdry" or "rand" (sampled proxy layers)
-    skel_rule: str = "bdry"   # params.skel_rule: "bdry", "rand" (sampled box points) or "ID" (kh > 0)
+    skel_rule: str = "bdry"   # params.skel_rule: "bdry", "rand" (sampled box points), "wdec" (Whitney) or "ID" (kh > 0)
     lambda_: float = 2.0      # params.lambda of the "rand" rule
 
     @property
@@ -73,9 +73,9 @@ class HSS2DParams:
         rules = {"bdry": L.HSS_PROXY_BDRY, "rand": L.HSS_PROXY_RAND}
         if self.proxy_rule not in rules:
             raise ValueError("proxy_rule must be 'bdry' or 'rand'")
-        skels = {"bdry": L.HSS_SKEL_BDRY, "rand": L.HSS_SKEL_RAND, "ID": L.HSS_SKEL_ID}
+        skels = {"bdry": L.HSS_SKEL_BDRY, "rand": L.HSS_SKEL_RAND, "ID": L.HSS_SKEL_ID, "wdec": L.HSS_SKEL_WDEC}
         if self.skel_rule not in skels:
-            raise ValueError("skel_rule must be 'bdry', 'rand' or 'ID'")
+            raise ValueError("skel_rule must be 'bdry', 'rand', 'wdec' or 'ID'")
         return L.hss2d_params(self.Ng, self.npan, self.layers, forms[self.INTERform], self.transinv, self.sym, prec,
                               0, float(self.acc), k.to_c(), int(self.k_cut), 0, int(self.seed),
                               rules[self.proxy_rule], 0, float(self.lambda_), skels[self.skel_rule], 0)

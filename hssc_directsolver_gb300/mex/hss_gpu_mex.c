@@ -180,6 +180,7 @@ static void hss2d_params_of(const mxArray* params, hss2d_params* p) {
   if (field_str(params, "skel_rule", buf, sizeof buf)) {
     if (!strcmp(buf, "rand")) p->skel_rule = HSS_SKEL_RAND;
     else if (!strcmp(buf, "ID")) p->skel_rule = HSS_SKEL_ID;
+    else if (!strcmp(buf, "wdec")) p->skel_rule = HSS_SKEL_WDEC;
   }
   p->lambda = field_or(params, "lambda", 2.0);
   kernel_params(params, &p->kp);

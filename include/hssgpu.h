@@ -58,6 +58,8 @@ extern "C" {
 #define HSS_SKEL_RAND 1 /* a random sample of the box's points (LOCAL_random_sampler until
                            ceil(2/3 n) or ceil(3/4 n) / 1.1 are kept) */
 #define HSS_SKEL_ID 2   /* the ID of K(proxies, box) on every level (kh > 0 trees) */
+#define HSS_SKEL_WDEC 3 /* a Whitney decomposition of the box (Common/Whitney_decomposition.m):
+                           boundary layers plus sampled lines at dyadic distances */
 
 /* HSS2D box proxies (params.proxy_rule, HSS2D_build_tree_nsym.m:870-961) */
 #define HSS_PROXY_BDRY 0 /* every point of the box's proxy layers (build_box_proxy.m:52-88) */
@@ -312,7 +314,7 @@ typedef struct hss2d_params {
   int32_t proxy_rule; /* HSS_PROXY_BDRY or HSS_PROXY_RAND (params.proxy_rule) */
   int32_t pad3_;
   double lambda;      /* params.lambda of the 'rand' rules (0: 2) */
-  int32_t skel_rule;  /* HSS_SKEL_BDRY, HSS_SKEL_RAND or HSS_SKEL_ID (params.skel_rule) */
+  int32_t skel_rule;  /* HSS_SKEL_BDRY, HSS_SKEL_RAND, HSS_SKEL_ID or HSS_SKEL_WDEC (params.skel_rule) */
   int32_t pad4_;
 } hss2d_params;
 

@@ -54,7 +54,8 @@ class HSS2DParams:
     # params.proxy_rule / lambda / skel_extra_pts (HSS_tree_parameters.m:121-124)
     proxy_rule: str = "bdry"
     # params.skel_rule (HSS2D_build_tree_nsym.m:399-412, :668-730): 'bdry' boundary layers,
-    # 'rand' a random sample of the box's points, 'ID' the ID of K(proxies, box) on every level
+    # 'rand' a random sample of the box's points, 'wdec' a Whitney decomposition of the box,
+    # 'ID' the ID of K(proxies, box) on every level
     skel_rule: str = "bdry"
     lambda_: float = 2.0
     skel_extra_pts: int = 0
@@ -274,6 +275,8 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
                 continue
             if prm.skel_rule == "rand":
                 presets[b] = random_skeleton(X_src, cent[b], lev, colrad, rowrad, prm)
+            elif prm.skel_rule == "wdec":
+                presets[b] = whitney_skeleton(X_src, cent[b], lev, colrad, rowrad, prm)
             else:
                 presets[b] = preset_skeleton(X_src, cent[b], lev, colrad, rowrad, prm.layers, h)
         if prm.uniform_ranks and presets:
@@ -399,6 +402,48 @@ def random_skeleton(X_src, cB, lev, colrad, rowrad, prm: HSS2DParams):
     else:
         nrm, tan, th0 = 1, 0, 0.0
     idx = np.arange(n)
+    I_rs = idx[~keep]
+    I_rs = I_rs[orient_residual(X_src[~keep], nrm, tan)]
+    I_sk = idx[keep]
+    I_sk = I_sk[orient_skeleton(X_src[keep], cB, th0)]
+    return np.concatenate([I_sk, I_rs]), len(I_sk)
+
+
+def whitney_mask(X, cB, colrad, rowrad, layers, h, Ng):
+    """Common/Whitney_decomposition.m: on the box's integer grid coordinates, the full
+    boundary layers, then for each finer dyadic scale i the lines at distance c_i from the
+    box edges sampled every 2^max(i - ceil(layers/2), 0) points (c_i a power of two below
+    Ng, or Ng times one: the Ng x Ng panel grid).  Returns the skeleton mask."""
+    c1 = np.floor((-cB[0] + (colrad - h / 2) + X[:, 0]) / h + 0.5).astype(np.int64)
+    c2 = np.floor((-cB[1] + (rowrad - h / 2) + X[:, 1]) / h + 0.5).astype(np.int64)
+    max1, max2 = int(c1.max()), int(c2.max())
+    dmax = max(max1, max2)
+    depth = math.ceil(math.log2(dmax)) + 1
+    B = (c1 < layers) | (max1 - c1 < layers) | (c2 < layers) | (max2 - c2 < layers)
+    freq = math.ceil(layers / 2)
+    lNg = math.ceil(math.log2(Ng))
+    for i in range(2, depth + 1):
+        if 2 ** (i - 1) < Ng:
+            ci, mi = 2 ** (i - 1), Ng
+        else:
+            ci = Ng * 2 ** (i - 1 - lNg)
+            mi = 2 * ci
+        e = 2 ** max(i - freq, 0)
+        w = ((c1 == ci) | (c1 == max1 - ci)) & (((c2 % mi) % e == 0) | (c2 == max2 - ci))
+        w |= ((c2 == ci) | (c2 == max2 - ci)) & (((c1 % mi) % e == 0) | (c1 == max1 - ci))
+        B |= w
+    return B
+
+
+def whitney_skeleton(X_src, cB, lev, colrad, rowrad, prm: HSS2DParams):
+    """LOCAL_Preset_Skeleton_Info 'wdec' (:668-701): the Whitney decomposition's points,
+    ordered as the 'bdry' rule orders its sets.  Returns (J, k)."""
+    keep = whitney_mask(X_src, cB, colrad, rowrad, prm.layers, prm.h, prm.Ng)
+    if lev % 2 == 0:
+        nrm, tan, th0 = 0, 1, math.pi / 2
+    else:
+        nrm, tan, th0 = 1, 0, 0.0
+    idx = np.arange(X_src.shape[0])
     I_rs = idx[~keep]
     I_rs = I_rs[orient_residual(X_src[~keep], nrm, tan)]
     I_sk = idx[keep]
@@ -577,7 +622,10 @@ def interpolation_dense(prm: HSS2DParams, Xp, X_sk, X_rs):
         z = np.zeros((k, X_rs.shape[0]))
         return z, z
     kp = prm.kp
-    ls = idecomp.lstsq_qr if kp.flag != SL_H_2D else lstsq_tikhonov
+    # the damped least squares for the complex kernel and for the sampled / Whitney skeletons,
+    # whose proxy systems are numerically rank deficient; the boundary-layer rule keeps the
+    # plain Householder solve
+    ls = lstsq_tikhonov if (kp.flag == SL_H_2D or prm.skel_rule != "bdry") else idecomp.lstsq_qr
     K11 = kernel_eval(Xp, X_sk, kp)
     K21 = kernel_eval(Xp, X_rs, kp)
     Tu = ls(K11, K21)
