@@ -190,3 +190,21 @@ def test_helmholtz_id_skeleton_rule(gpu):
     y = G2.HSS2D_apply_nsym(t, None, x)
     assert _rel(y, O2.apply_nsym(ot, blk, x)) <= 1e-13
     assert _rel(G2.HSS2D_applyinv_nsym(t, None, y), O2.applyinv_nsym(ot, inv, y)) <= 1e-10
+
+
+def test_helmholtz_refinement_and_bicgstab(gpu):
+    """The other solvers on a complex tree: iterative refinement (complex vectors through the
+    real embedding, hss2d_solve) and BiCGSTAB (real inner products of the embedded system)
+    reach their tolerances, and agree with GMRES."""
+    from hssc_directsolver_gb300 import hss2d as G2
+    gp, op = _params(4)
+    t = G2.HSS2D_invert_nsym(G2.HSS2D_build_tree_nsym(gp))
+    r = np.random.default_rng(11)
+    f = r.standard_normal((op.N, 2)) + 1j * r.standard_normal((op.N, 2))
+    x1, rr1, it1 = G2.HSS2D_solve(t, f, 1e-10, 4)
+    assert rr1 <= 1e-10
+    x2, rr2, _ = G2.HSS2D_bicgstab(t, f, tol=1e-10, maxit=50, PRECOND=t)
+    assert rr2 <= 1e-10
+    x3, rr3, _ = G2.HSS2D_gmres(t, f, tol=1e-11, PRECOND=t)
+    assert rr3 <= 1e-11
+    assert _rel(x1, x3) <= 1e-9 and _rel(x2, x3) <= 1e-9
