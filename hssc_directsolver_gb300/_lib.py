@@ -40,6 +40,7 @@ HSS_SKEL_ID = 2
 HSS_SKEL_WDEC = 3
 HSS_PROXY_BDRY = 0
 HSS_PROXY_RAND = 1
+HSS_PROXY_WDEC = 2
 HSS_PREC_FP64 = 0
 HSS_PREC_MIXED = 1
 HSS_PREC_DFLOAT = 2

@@ -9,10 +9,12 @@
 //   proxies            HSS2D/build_box_proxy.m:52-88 via LOCAL_Build_Proxy :945-949
 //   proxy layers       :360-368
 //   'rand' proxies     LOCAL_Build_Proxy :883-905, LOCAL_random_sampler :964-1001
+//   'wdec' proxies     :877-881, Common/Whitney_decomposition_1Dcurve.m
 //   ID skeletons       :399-412, LOCAL_Non_Preset_Skeleton_Info :614-657 (kh > 0)
 #include "hss2d_tree.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <numeric>
 #include <random>
@@ -247,8 +249,8 @@ static void whitney_skeleton(const std::vector<double>& X, const std::vector<int
   std::vector<long long> c1(n), c2(n);
   long long max1 = 0, max2 = 0;
   for (int i = 0; i < n; ++i) {
-    c1[i] = (long long)std::floor((-cx + (colrad - h / 2) + X[2 * (size_t)I_src[i]]) / h + 0.5);
-    c2[i] = (long long)std::floor((-cy + (rowrad - h / 2) + X[2 * (size_t)I_src[i] + 1]) / h + 0.5);
+    c1[i] = (long long)std::round((-cx + (colrad - h / 2) + X[2 * (size_t)I_src[i]]) / h);
+    c2[i] = (long long)std::round((-cy + (rowrad - h / 2) + X[2 * (size_t)I_src[i] + 1]) / h);
     max1 = std::max(max1, c1[i]);
     max2 = std::max(max2, c2[i]);
   }
@@ -308,6 +310,82 @@ static void random_proxy(std::vector<double>& px, std::vector<double>& py, int n
   }
 }
 
+// Common/Whitney_decomposition_1Dcurve.m with C = (0, 0), R = (1, 1) (its only call, the
+// 'wdec' proxy rule of LOCAL_Build_Proxy :877-881): a quadtree over [-1, 1]^2 refines every
+// box that holds more than one point and lies within freq 1.5 rad of the box boundary
+// (freq = min(ceil(layers / 2), 2)), marking the points of least and largest integer
+// coordinate in each direction (first on ties) of every box it splits; the points within
+// layers h of the box boundary are added.  Keeps the marked points of (px, py).
+static void whitney_curve(std::vector<double>& px, std::vector<double>& py, double cx, double cy, double colrad,
+                          double rowrad, int layers, double h) {
+  const int N = (int)px.size();
+  if (N == 0) return;
+  std::vector<long long> c1(N), c2(N);
+  long long mn1 = LLONG_MAX, mx1 = LLONG_MIN, mn2 = LLONG_MAX, mx2 = LLONG_MIN;
+  for (int i = 0; i < N; ++i) {
+    c1[i] = (long long)std::round((0.0 + (1.0 - h / 2) + px[i]) / h);
+    c2[i] = (long long)std::round((0.0 + (1.0 - h / 2) + py[i]) / h);
+    mn1 = std::min(mn1, c1[i]); mx1 = std::max(mx1, c1[i]);
+    mn2 = std::min(mn2, c2[i]); mx2 = std::max(mx2, c2[i]);
+  }
+  const long long dmax = std::max(mx1 - mn1, mx2 - mn2);
+  const int depth = dmax > 0 ? (int)std::ceil(std::log2((double)dmax)) : 0;
+  const int freq = std::min((layers + 1) / 2, 2);
+  const double rB[2] = {colrad, rowrad}, cB[2] = {cx, cy};
+  std::vector<char> keep(N, 0);
+  struct Box { double c0, c1; std::vector<int> J; };
+  std::vector<Box> level(1);
+  level[0].c0 = 0.0;
+  level[0].c1 = 0.0;
+  level[0].J.resize(N);
+  std::iota(level[0].J.begin(), level[0].J.end(), 0);
+  const double cta[4][2] = {{-0.5, -0.5}, {-0.5, 0.5}, {0.5, -0.5}, {0.5, 0.5}};
+  for (int lev = 0; lev < depth; ++lev) {
+    std::vector<Box> nxt;
+    for (const Box& bx : level) {
+      const int n = (int)bx.J.size();
+      if (n == 0) continue;
+      int imn[2] = {0, 0}, imx[2] = {0, 0};
+      for (int q = 1; q < n; ++q) {
+        if (c1[bx.J[q]] < c1[bx.J[imn[0]]]) imn[0] = q;
+        if (c2[bx.J[q]] < c2[bx.J[imn[1]]]) imn[1] = q;
+        if (c1[bx.J[q]] > c1[bx.J[imx[0]]]) imx[0] = q;
+        if (c2[bx.J[q]] > c2[bx.J[imx[1]]]) imx[1] = q;
+      }
+      const double d0 = std::fabs(bx.c0 - cB[0]), d1 = std::fabs(bx.c1 - cB[1]);
+      const int i = (d1 > d0) ? 1 : 0;
+      const double dist = std::fabs(rB[i] - (i ? d1 : d0));
+      const double rad = std::ldexp(1.0, -lev);
+      if (n > 1 && dist < freq * 1.5 * rad) {
+        const long long rowmid = (long long)std::round((0.0 + (1.0 - h / 2) + bx.c0) / h);
+        const long long colmid = (long long)std::round((0.0 + (1.0 - h / 2) + bx.c1) / h);
+        for (int j = 0; j < 4; ++j) {
+          Box ch;
+          ch.c0 = bx.c0 + rad * cta[j][0];
+          ch.c1 = bx.c1 + rad * cta[j][1];
+          for (int q : bx.J) {
+            const bool lo1 = c1[q] < rowmid, lo2 = c2[q] < colmid;
+            const bool in = (j == 0) ? (lo1 && lo2) : (j == 1) ? (lo1 && !lo2) : (j == 2) ? (!lo1 && lo2) : (!lo1 && !lo2);
+            if (in) ch.J.push_back(q);
+          }
+          nxt.push_back(std::move(ch));
+        }
+        keep[bx.J[imn[0]]] = keep[bx.J[imn[1]]] = keep[bx.J[imx[0]]] = keep[bx.J[imx[1]]] = 1;
+      }
+    }
+    level.swap(nxt);
+  }
+  size_t o = 0;
+  for (int q = 0; q < N; ++q) {
+    const double a0 = std::fabs(px[q] - cx), a1 = std::fabs(py[q] - cy);
+    const double dist = std::min(std::fabs(colrad - a0), std::fabs(rowrad - a1));
+    const bool bdry = dist < layers * h && a0 < colrad + layers * h && a1 < rowrad + layers * h;
+    if (keep[q] || bdry) { px[o] = px[q]; py[o] = py[q]; ++o; }
+  }
+  px.resize(o);
+  py.resize(o);
+}
+
 // proxy layers of a level (:360-368): layers + 1 for the Laplace kernel, 2 round(min radius / h)
 // for kh > 0; the root keeps params.layers
 static int proxy_layers(const hss2d_params& prm, int lev, double colrad, double rowrad, double h) {
@@ -324,6 +402,8 @@ void level_proxy(const hss2d_params& prm, int lev, double cx, double cy, int n_s
   box_proxy(cx, cy, colrad, rowrad, proxy_layers(prm, lev, colrad, rowrad, h), h, px, py);
   if (prm.proxy_rule == HSS_PROXY_RAND)
     random_proxy(px, py, n_src, cx, cy, colrad, rowrad, lev, prm.layers, h, prm.lambda > 0 ? prm.lambda : 2.0);
+  else if (prm.proxy_rule == HSS_PROXY_WDEC)
+    whitney_curve(px, py, cx, cy, colrad, rowrad, 2 * prm.layers, h);
 }
 
 void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id_level) {
@@ -332,7 +412,8 @@ void build_tree_geometry(const hss2d_params& prm, Tree2D& T, const IdLevelFn& id
   HSS_REQUIRE(prm.layers >= 1, HSS_ERR_ARG, "layers must be >= 1");
   HSS_REQUIRE(prm.kp.flag == HSS_SL_L_2D || prm.kp.flag == HSS_SL_H_2D, HSS_ERR_ARG,
               "HSS2D takes the SL_L_2D and SL_H_2D kernels");
-  HSS_REQUIRE(prm.proxy_rule == HSS_PROXY_BDRY || prm.proxy_rule == HSS_PROXY_RAND, HSS_ERR_ARG, "unknown proxy rule");
+  HSS_REQUIRE(prm.proxy_rule == HSS_PROXY_BDRY || prm.proxy_rule == HSS_PROXY_RAND || prm.proxy_rule == HSS_PROXY_WDEC,
+              HSS_ERR_ARG, "unknown proxy rule");
   HSS_REQUIRE(prm.skel_rule == HSS_SKEL_BDRY || prm.skel_rule == HSS_SKEL_RAND || prm.skel_rule == HSS_SKEL_ID ||
                   prm.skel_rule == HSS_SKEL_WDEC,
               HSS_ERR_ARG, "unknown skeleton rule");

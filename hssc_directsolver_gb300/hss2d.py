@@ -44,7 +44,7 @@ class HSS2DParams:
     Fopts: str = "dense"
     k_cut: int = 2500         # low-rank T only where k < k_cut
     seed: int = 0             # key of the randomized ID's Gaussian samples
-    proxy_rule: str = "bdry"  # params.proxy_rule: "bdry" or "rand" (sampled proxy layers)
+    proxy_rule: str = "bdry"  # params.proxy_rule: "bdry", "rand" (sampled layers) or "wdec" (Whitney-thinned)
     skel_rule: str = "bdry"   # params.skel_rule: "bdry", "rand" (sampled box points), "wdec" (Whitney) or "ID" (kh > 0)
     lambda_: float = 2.0      # params.lambda of the "rand" rule
 
@@ -70,9 +70,9 @@ class HSS2DParams:
                 "dfloat_inv": L.HSS_PREC_DFLOAT_INV, "tc": L.HSS_PREC_TC}[self.precision]
         k = self.kernel
         k.h = self.h
-        rules = {"bdry": L.HSS_PROXY_BDRY, "rand": L.HSS_PROXY_RAND}
+        rules = {"bdry": L.HSS_PROXY_BDRY, "rand": L.HSS_PROXY_RAND, "wdec": L.HSS_PROXY_WDEC}
         if self.proxy_rule not in rules:
-            raise ValueError("proxy_rule must be 'bdry' or 'rand'")
+            raise ValueError("proxy_rule must be 'bdry', 'rand' or 'wdec'")
         skels = {"bdry": L.HSS_SKEL_BDRY, "rand": L.HSS_SKEL_RAND, "ID": L.HSS_SKEL_ID, "wdec": L.HSS_SKEL_WDEC}
         if self.skel_rule not in skels:
             raise ValueError("skel_rule must be 'bdry', 'rand', 'wdec' or 'ID'")

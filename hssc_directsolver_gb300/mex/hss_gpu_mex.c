@@ -175,7 +175,10 @@ static void hss2d_params_of(const mxArray* params, hss2d_params* p) {
     else if (!strcmp(buf, "tc")) p->precision = HSS_PREC_TC;
   }
   p->proxy_rule = HSS_PROXY_BDRY;
-  if (field_str(params, "proxy_rule", buf, sizeof buf) && !strcmp(buf, "rand")) p->proxy_rule = HSS_PROXY_RAND;
+  if (field_str(params, "proxy_rule", buf, sizeof buf)) {
+    if (!strcmp(buf, "rand")) p->proxy_rule = HSS_PROXY_RAND;
+    else if (!strcmp(buf, "wdec")) p->proxy_rule = HSS_PROXY_WDEC;
+  }
   p->skel_rule = HSS_SKEL_BDRY;
   if (field_str(params, "skel_rule", buf, sizeof buf)) {
     if (!strcmp(buf, "rand")) p->skel_rule = HSS_SKEL_RAND;

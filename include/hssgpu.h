@@ -66,6 +66,9 @@ extern "C" {
 #define HSS_PROXY_RAND 1 /* the layers sampled with probability 2^(-lambda l) by dyadic distance
                             band l until ceil(2/3 n) (even levels) or ceil(3/4 n) points remain
                             (LOCAL_Build_Proxy :883-905, LOCAL_random_sampler :964-1001) */
+#define HSS_PROXY_WDEC 2 /* the points of twice the proxy layers kept by a Whitney decomposition
+                            of the box boundary (LOCAL_Build_Proxy :877-881 over
+                            Common/Whitney_decomposition_1Dcurve.m) */
 
 /* precision modes */
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
@@ -311,7 +314,7 @@ typedef struct hss2d_params {
   int32_t k_cut;     /* low-rank T only where k < k_cut (0: 2500) */
   int32_t pad2_;
   uint64_t seed;     /* key of the randomized ID's Gaussian samples */
-  int32_t proxy_rule; /* HSS_PROXY_BDRY or HSS_PROXY_RAND (params.proxy_rule) */
+  int32_t proxy_rule; /* HSS_PROXY_BDRY, HSS_PROXY_RAND or HSS_PROXY_WDEC (params.proxy_rule) */
   int32_t pad3_;
   double lambda;      /* params.lambda of the 'rand' rules (0: 2) */
   int32_t skel_rule;  /* HSS_SKEL_BDRY, HSS_SKEL_RAND, HSS_SKEL_ID or HSS_SKEL_WDEC (params.skel_rule) */

@@ -264,6 +264,8 @@ def build_tree_nsym(prm: HSS2DParams, with_T: bool = True) -> HSS2DTree:
             Xp = build_box_proxy(cent[b], colrad, rowrad, lp, h)
             if prm.proxy_rule == "rand":
                 Xp = random_proxy(Xp, len(I_src[b]), cent[b], colrad, rowrad, lev, prm)
+            elif prm.proxy_rule == "wdec":
+                Xp = Xp[whitney_curve_mask(Xp, cent[b], np.array([colrad, rowrad]), 2 * prm.layers, h)]
             proxy[b] = Xp
             if prm.transinv and b != first:
                 followers.append(b)
@@ -383,6 +385,56 @@ def random_sampler(X, cB, colrad, rowrad, lam, lay, h):
     return X[sampler_mask(X, cB, colrad, rowrad, lam, lay, h)]
 
 
+def mround(x):
+    """MATLAB's round: half away from zero, exact (x - trunc(x) has no rounding error).
+    Returns int64."""
+    x = np.asarray(x, dtype=np.float64)
+    t = np.trunc(x)
+    return (t + np.sign(x) * (np.abs(x - t) >= 0.5)).astype(np.int64)
+
+
+def whitney_curve_mask(G, cB, rB, layers, h):
+    """Common/Whitney_decomposition_1Dcurve.m with C = (0, 0), R = (1, 1) (its only call,
+    LOCAL_Build_Proxy 'wdec', HSS2D_build_tree_nsym.m:877-881): a quadtree over [-1, 1]^2
+    refines every box that holds more than one point and lies within freq 1.5 rad of the
+    box boundary (freq = min(ceil(layers / 2), 2)), marking the points of least and largest
+    integer coordinate in each direction (first on ties) of every box it splits; the points
+    within layers h of the box boundary are added.  Returns the mask."""
+    N = G.shape[0]
+    coord = mround((0.0 + (1.0 - h / 2) + G) / h)
+    dmax = max(int(coord[:, 0].max() - coord[:, 0].min()), int(coord[:, 1].max() - coord[:, 1].min()))
+    depth = math.ceil(math.log2(dmax))
+    freq = min(math.ceil(layers / 2), 2)
+    B = np.zeros(N, dtype=bool)
+    level = [(np.zeros(2), np.arange(N))]   # (centre, point indices) of the level's boxes
+    cta = np.array([[-0.5, -0.5], [-0.5, 0.5], [0.5, -0.5], [0.5, 0.5]])
+    for lev in range(depth):
+        nxt = []
+        for cent, J in level:
+            if len(J) == 0:
+                continue
+            bc = coord[J]
+            id_mn = np.argmin(bc, axis=0)
+            id_mx = np.argmax(bc, axis=0)
+            d = np.abs(cent - cB)
+            i = int(np.argmax(d))
+            dist = abs(rB[i] - d[i])
+            rad = 2.0 ** (-lev)
+            if len(J) > 1 and dist < freq * 1.5 * rad:
+                cbc = mround((0.0 + (1.0 - h / 2) + cent) / h)
+                rowmid, colmid = int(cbc[0]), int(cbc[1])
+                masks = [(bc[:, 0] < rowmid) & (bc[:, 1] < colmid), (bc[:, 0] < rowmid) & (bc[:, 1] >= colmid),
+                         (bc[:, 0] >= rowmid) & (bc[:, 1] < colmid), (bc[:, 0] >= rowmid) & (bc[:, 1] >= colmid)]
+                for j in range(4):
+                    nxt.append((cent + 2.0 ** (-lev) * cta[j], J[masks[j]]))
+                B[J[[id_mn[0], id_mn[1], id_mx[0], id_mx[1]]]] = True
+        level = nxt
+    inf_nrm = np.abs(G - cB[None, :])
+    dist = np.min(np.abs(rB[None, :] - inf_nrm), axis=1)
+    bdry = (dist < layers * h) & (inf_nrm[:, 0] < rB[0] + layers * h) & (inf_nrm[:, 1] < rB[1] + layers * h)
+    return B | bdry
+
+
 def random_skeleton(X_src, cB, lev, colrad, rowrad, prm: HSS2DParams):
     """LOCAL_Preset_Skeleton_Info 'rand' (:703-730): the box's own points sampled by
     LOCAL_random_sampler (each retry on the full set with 0.9 lambda) until the sample
@@ -414,8 +466,8 @@ def whitney_mask(X, cB, colrad, rowrad, layers, h, Ng):
     boundary layers, then for each finer dyadic scale i the lines at distance c_i from the
     box edges sampled every 2^max(i - ceil(layers/2), 0) points (c_i a power of two below
     Ng, or Ng times one: the Ng x Ng panel grid).  Returns the skeleton mask."""
-    c1 = np.floor((-cB[0] + (colrad - h / 2) + X[:, 0]) / h + 0.5).astype(np.int64)
-    c2 = np.floor((-cB[1] + (rowrad - h / 2) + X[:, 1]) / h + 0.5).astype(np.int64)
+    c1 = mround((-cB[0] + (colrad - h / 2) + X[:, 0]) / h)
+    c2 = mround((-cB[1] + (rowrad - h / 2) + X[:, 1]) / h)
     max1, max2 = int(c1.max()), int(c2.max())
     dmax = max(max1, max2)
     depth = math.ceil(math.log2(dmax)) + 1

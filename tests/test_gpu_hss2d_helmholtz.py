@@ -49,7 +49,7 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-CASES = [(4, "bdry"), (8, "rand")]
+CASES = [(4, "bdry"), (8, "rand"), (8, "wdec")]
 
 
 @pytest.mark.parametrize("npan,rule", CASES)

@@ -1,8 +1,9 @@
 """LOCAL_Build_Proxy on the host (no GPU): the library's proxy points of a box equal the
 oracle's, point for point, for the 'bdry' rule (build_box_proxy.m:52-88 with the layer count
-of HSS2D_build_tree_nsym.m:360-368, Laplace and kh > 0) and the 'rand' rule (LOCAL_Build_Proxy
+of HSS2D_build_tree_nsym.m:360-368, Laplace and kh > 0), the 'rand' rule (LOCAL_Build_Proxy
 :883-905 over LOCAL_random_sampler :964-1001: the Mersenne Twister reset to seed 5489 on every
-call, its 53-bit uniforms)."""
+call, its 53-bit uniforms) and the 'wdec' rule (:877-881 over
+Common/Whitney_decomposition_1Dcurve.m)."""
 import numpy as np
 import pytest
 
@@ -26,11 +27,14 @@ def _oracle_proxy(op, box, n_src):
     Xp = O2.build_box_proxy(cent[box], colrad, rowrad, O2.lay_prox(op, lev), op.h)
     if op.proxy_rule == "rand":
         Xp = O2.random_proxy(Xp, n_src, cent[box], colrad, rowrad, lev, op)
+    elif op.proxy_rule == "wdec":
+        Xp = Xp[O2.whitney_curve_mask(Xp, cent[box], np.array([colrad, rowrad]), 2 * op.layers, op.h)]
     return Xp
 
 
 @pytest.mark.parametrize("npan,kh,rule", [(4, 0.0, "bdry"), (8, 0.0, "bdry"), (8, 20.0, "bdry"),
-                                          (4, 0.0, "rand"), (8, 20.0, "rand"), (16, 20.0, "rand")])
+                                          (4, 0.0, "rand"), (8, 20.0, "rand"), (16, 20.0, "rand"),
+                                          (4, 0.0, "wdec"), (8, 0.0, "wdec"), (8, 20.0, "wdec")])
 def test_proxy_points_equal_oracle(npan, kh, rule):
     from hssc_directsolver_gb300 import hss2d as G2
     gp, op = _both(npan, kh, rule)
