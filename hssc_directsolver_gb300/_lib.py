@@ -103,6 +103,7 @@ SIGNATURES = {
     "hss1d_compress_lr": (C.c_int, [C.POINTER(_P), _P, _P, C.c_int64, C.c_int32, C.c_int64, C.c_int64, C.c_int32,
                                     C.c_double, C.c_uint64]),
     "hss1d_forest_info": (C.c_int, [_P, _I32P, _I64P, _I32P, _I64P]),
+    "hss1d_is_complex": (C.c_int, [_P, _I32P]),
     "hss1d_info": (C.c_int, [_P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P]),
     "hss1d_export_box": (C.c_int, [_P, C.c_int32, _I32P, _I32P, _I32P, _I32P, _DP, _DP]),
     "hss1d_invert": (C.c_int, [_P]),

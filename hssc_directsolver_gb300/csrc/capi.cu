@@ -438,16 +438,26 @@ int hss_mlp_destroy(hss_mlp* M) {
   HSS_CATCH
 }
 
+// a complex handle counts unknowns internally (two per point); the interface counts points
+static long long pts1(const HSS1D* h, long long v) { return h->cplx ? v / 2 : v; }
+
 int hss1d_forest_info(const hss1d_matrix* H, int32_t* nprob, int64_t* Ntot, int32_t* root, int64_t* pbase) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
   const HSS1D* h = H->impl;
   if (nprob) *nprob = h->nprob;
-  if (Ntot) *Ntot = h->Ntot;
+  if (Ntot) *Ntot = pts1(h, h->Ntot);
   for (int p = 0; p < h->nprob; ++p) {
     if (root) root[p] = h->proot[p];
-    if (pbase) pbase[p] = h->pbase[p];
+    if (pbase) pbase[p] = pts1(h, h->pbase[p]);
   }
+  HSS_CATCH
+}
+
+int hss1d_is_complex(const hss1d_matrix* H, int32_t* is_complex) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && is_complex, HSS_ERR_ARG, "NULL argument");
+  *is_complex = H->impl->cplx ? 1 : 0;
   HSS_CATCH
 }
 
@@ -462,10 +472,10 @@ int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* 
     if (parent) parent[b] = h->parent[b];
     if (c1) c1[b] = h->c1[b];
     if (c2) c2[b] = h->c2[b];
-    if (off) off[b] = h->off[b];
-    if (cnt) cnt[b] = h->cnt[b];
-    if (nskel) nskel[b] = h->nskel[b];
-    if (kskel) kskel[b] = h->kskel[b];
+    if (off) off[b] = (int32_t)pts1(h, h->off[b]);
+    if (cnt) cnt[b] = (int32_t)pts1(h, h->cnt[b]);
+    if (nskel) nskel[b] = (int32_t)pts1(h, h->nskel[b]);
+    if (kskel) kskel[b] = (int32_t)pts1(h, h->kskel[b]);
   }
   HSS_CATCH
 }
@@ -477,6 +487,34 @@ int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_
   const HSS1D* h = H->impl;
   HSS_REQUIRE(box >= 0 && box < h->nboxes && h->parent[box] >= 0, HSS_ERR_ARG,
               "box out of range (a root has no skeleton)");
+  if (h->cplx) {
+    // points and complex T (interleaved), de-embedded: T = E(0::2, 0::2) + i E(1::2, 0::2);
+    // T_DN is kept conjugated
+    const int n = h->nskel[box] / 2, k = h->kskel[box] / 2, k2 = 2 * k;
+    for (int t = 0; t < k; ++t) {
+      if (I_skup) I_skup[t] = h->I_SKUP[box][2 * t] / 2;
+      if (I_skdn) I_skdn[t] = h->I_SKDN[box][2 * t] / 2;
+    }
+    for (int t = 0; t < n; ++t) {
+      if (J_up) J_up[t] = h->J_UP[box][2 * t] / 2;
+      if (J_dn) J_dn[t] = h->J_DN[box][2 * t] / 2;
+    }
+    const size_t tc = (size_t)k2 * (2 * (n - k));
+    std::vector<double> E(tc);
+    for (int side = 0; side < 2; ++side) {
+      double* dst = side ? T_dn : T_up;
+      if (!dst || tc == 0) continue;
+      const double* src = side ? h->T_DN.p + h->oT[box] : h->T_UP.p + h->oT[box];
+      HSS_CUDA(cudaMemcpy(E.data(), src, tc * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int c = 0; c < n - k; ++c)
+        for (int r = 0; r < k; ++r) {
+          const size_t e = 2 * r + (size_t)(2 * c) * k2;
+          dst[2 * (r + (size_t)c * k)] = E[e];
+          dst[2 * (r + (size_t)c * k) + 1] = side ? -E[e + 1] : E[e + 1];
+        }
+    }
+    return HSS_OK;
+  }
   const int n = h->nskel[box], k = h->kskel[box];
   const int nd = h->rn()[box], kd = h->rk()[box];
   if (I_skup) std::memcpy(I_skup, h->I_SKUP[box].data(), k * sizeof(int32_t));
@@ -517,12 +555,12 @@ int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t*
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");
   const HSS1D* h = H->impl;
-  if (M) *M = h->rows();
+  if (M) *M = pts1(h, h->rows());
   for (int b = 0; b < h->nboxes; ++b) {
-    if (off_in) off_in[b] = h->roff()[b];
-    if (cnt_in) cnt_in[b] = h->rcnt()[b];
-    if (nskel_in) nskel_in[b] = h->rn()[b];
-    if (kskel_in) kskel_in[b] = h->rk()[b];
+    if (off_in) off_in[b] = (int32_t)pts1(h, h->roff()[b]);
+    if (cnt_in) cnt_in[b] = (int32_t)pts1(h, h->rcnt()[b]);
+    if (nskel_in) nskel_in[b] = (int32_t)pts1(h, h->rn()[b]);
+    if (kskel_in) kskel_in[b] = (int32_t)pts1(h, h->rk()[b]);
   }
   HSS_CATCH
 }
@@ -703,6 +741,7 @@ int hss1d_apply_submatrix(hss1d_matrix* H, const uint8_t* I_dn, const uint8_t* I
   HSS_REQUIRE(H && H->impl && I_dn && I_up && qq && uu && nrhs >= 1, HSS_ERR_ARG, "bad arguments");
   HSS1D* h = H->impl;
   HSS_REQUIRE(!h->rect, HSS_ERR_ARG, "apply_submatrix is defined for square handles only");
+  HSS_REQUIRE(!h->cplx, HSS_ERR_ARG, "apply_submatrix of a complex handle is not built (real handles only)");
   const size_t N = (size_t)h->Ntot;
   // K(I_dn, I_up) qq(I_up) = rows I_dn of K (qq with the columns outside I_up zeroed)
   std::vector<double> q(N * nrhs), y(N * nrhs);
@@ -723,6 +762,7 @@ int hss1d_apply_submatrix_boxes(const hss1d_matrix* H, const uint8_t* I_dn, cons
                                 uint8_t* Box_up) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl && !H->impl->rect, HSS_ERR_ARG, "square handle required");
+  HSS_REQUIRE(!H->impl->cplx, HSS_ERR_ARG, "point masks of a complex handle are not built (real handles only)");
   HSS_REQUIRE(H && H->impl && I_dn && I_up && Box_dn && Box_up, HSS_ERR_ARG, "NULL argument");
   const HSS1D* h = H->impl;
   // children have larger ids than their parents: one pass from the leaves up
@@ -1267,7 +1307,7 @@ int hss1d_kernel_residual(hss1d_matrix* H, const double* f, const double* x, int
   HSS_REQUIRE(H && H->impl && f && x && relres && nrhs >= 1, HSS_ERR_ARG, "kernel residual: bad arguments");
   auto* h = H->impl;
   HSS_REQUIRE(!h->rect, HSS_ERR_ARG, "kernel residual: square handles only");
-  HSS_REQUIRE(h->kernel_op && (h->kdev.flag == HSS_SL_L_2D || h->kdev.flag == HSS_DL_L_2D), HSS_ERR_ARG,
+  HSS_REQUIRE(h->kernel_op, HSS_ERR_ARG,
               "kernel residual: the handle holds no kernel matrix of its points (a low-rank or algebra result)");
   std::vector<KmvP> P;
   for (size_t p = 0; p < h->pN.size(); ++p)

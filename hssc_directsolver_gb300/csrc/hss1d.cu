@@ -216,7 +216,15 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
                      bool sym_) {
   kernel_op = true;
   HSS_REQUIRE(np_ >= 1 && Np && Xp && ldx && leaf_ >= 1 && acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad compress args");
-  HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D, HSS_ERR_ARG, "unknown kernel");
+  HSS_REQUIRE(kp_.flag == HSS_SL_L_2D || kp_.flag == HSS_DL_L_2D || kp_.flag == HSS_SL_H_2D, HSS_ERR_ARG,
+              "unknown kernel");
+  // complex (Helmholtz) kernel: the blocks are generated and skeletonized in the real 2 x 2
+  // embedding (pair-pivoted ID); the finished handle is the real 2N x 2N embedded matrix
+  const bool cx = (kp_.flag == HSS_SL_H_2D);
+  HSS_REQUIRE(!cx || (!sym_ && !mlp && !id_df), HSS_ERR_ARG,
+              "complex compression: the nsym form with the plain FP64 ID and no rank predictor");
+  cplx = cx;
+  const int rep = cx ? 2 : 1;
   using clk = std::chrono::steady_clock;
   std::fill(phase_s, phase_s + NPHASE, 0.0);
   auto tick = clk::now();
@@ -288,23 +296,47 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       std::sort(l.begin(), l.end());
     }
   }, 1);
-  // ---- point table: Ntot points + NPROXY proxies per non-root box; a box's proxy slot
-  // follows the order levels are compressed in, so each level uploads one contiguous range
-  std::vector<int> pslot(nboxes, -1);
-  int nslot = 0;
+  // ---- point table: the Ntot points, then one proxy slot per non-root box in the order the
+  // levels are compressed in, so each level uploads one contiguous range.  A slot holds
+  // NPROXY points; with the Helmholtz kernel the ring's size grows with the circle
+  // (proxy_count), and the slot holds the count for the diagonal of the box's bounding box,
+  // which bounds the radius of any circle centred inside it.  A complex handle keeps every
+  // entry twice (table entries 2v and 2v + 1 are logical point v: the two real unknowns of
+  // a point read the same point).
+  std::vector<long long> poff(nboxes, -1);
+  std::vector<int> pcap(nboxes, 0);
+  long long nprx = 0;
   for (int L = maxlev; L >= 1; --L)
     for (int b = 0; b < nboxes; ++b)
-      if (level[b] == L) pslot[b] = nslot++;
-  const size_t npts = (size_t)Ntot + (size_t)NPROXY * nslot;
+      if (level[b] == L) {
+        int cap = NPROXY;
+        if (cx) {
+          double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+          for (int i = off[b]; i < off[b] + cnt[b]; ++i) {
+            x0 = std::min(x0, X[6 * (size_t)i]); x1 = std::max(x1, X[6 * (size_t)i]);
+            y0 = std::min(y0, X[6 * (size_t)i + 1]); y1 = std::max(y1, X[6 * (size_t)i + 1]);
+          }
+          cap = proxy_count(kp, std::hypot(x1 - x0, y1 - y0) * (1.0 + 1e-12), pN[prob[b]]);
+        }
+        poff[b] = nprx;
+        pcap[b] = cap;
+        nprx += cap;
+      }
+  const size_t npts = (size_t)rep * ((size_t)Ntot + (size_t)nprx);
   HSS_REQUIRE(npts < (1ULL << 31), HSS_ERR_ARG, "point table exceeds 2^31 entries");
   std::vector<double> hx(npts, 0.0), hy(npts, 0.0), hnx(npts, 0.0), hny(npts, 0.0), hw(npts, 0.0),
       hk(npts, 0.0);
-  for (long long i = 0; i < Ntot; ++i) {
-    hx[i] = X[6 * i]; hy[i] = X[6 * i + 1]; hnx[i] = X[6 * i + 2]; hny[i] = X[6 * i + 3];
-    hw[i] = X[6 * i + 4]; hk[i] = X[6 * i + 5];
-  }
+  auto put = [&](size_t v, double x, double y, double nx, double ny, double w, double kap) {
+    for (int r = 0; r < rep; ++r) {
+      const size_t e = (size_t)rep * v + r;
+      hx[e] = x; hy[e] = y; hnx[e] = nx; hny[e] = ny; hw[e] = w; hk[e] = kap;
+    }
+  };
+  for (long long i = 0; i < Ntot; ++i)
+    put((size_t)i, X[6 * i], X[6 * i + 1], X[6 * i + 2], X[6 * i + 3], X[6 * i + 4], X[6 * i + 5]);
   pts.reserve(npts);
-  pts.upload_range(0, (size_t)Ntot, hx.data(), hy.data(), hnx.data(), hny.data(), hw.data(), hk.data(), kp, stream);
+  pts.upload_range(0, (size_t)rep * Ntot, hx.data(), hy.data(), hnx.data(), hny.data(), hw.data(), hk.data(), kp,
+                   stream);
   nskel.assign(nboxes, 0);
   kskel.assign(nboxes, 0);
   I_SKUP.assign(nboxes, {});
@@ -350,19 +382,16 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       double xc, yc, R;
       circum_circle(X, both, xc, yc, R);
       const double Rp = RADIUS_REL * R;
+      const int npx = proxy_count(kp, R, pN[prob[b]]);
+      HSS_REQUIRE(npx <= pcap[b], HSS_ERR_ARG, "proxy ring larger than its slot");
       // LOCAL_construct_circle: tt = linspace(0, 2 pi (1 - 1/n), n)
-      const double stop = 2.0 * M_PI * (1.0 - 1.0 / NPROXY);
-      const double step = stop / (double)(NPROXY - 1);
-      const size_t pb = (size_t)Ntot + (size_t)NPROXY * pslot[b];
-      for (int t = 0; t < NPROXY; ++t) {
-        const double tt = (t == NPROXY - 1) ? stop : (double)t * step;
+      const double stop = 2.0 * M_PI * (1.0 - 1.0 / npx);
+      const double step = (npx > 1) ? stop / (double)(npx - 1) : 0.0;
+      const size_t pb = (size_t)Ntot + (size_t)poff[b];
+      for (int t = 0; t < npx; ++t) {
+        const double tt = (t == npx - 1) ? stop : (double)t * step;
         const double c = std::cos(tt), s = std::sin(tt);
-        hx[pb + t] = xc + Rp * c;
-        hy[pb + t] = yc + Rp * s;
-        hnx[pb + t] = c;
-        hny[pb + t] = s;
-        hw[pb + t] = 2.0 * M_PI * Rp / NPROXY;
-        hk[pb + t] = 1.0 / Rp;
+        put(pb + t, xc + Rp * c, yc + Rp * s, c, s, 2.0 * M_PI * Rp / npx, 1.0 / Rp);
       }
     std::vector<int> out_maybe, in_maybe;
       for (int j : nei[b]) {
@@ -409,26 +438,32 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
         f[6] = (float)L / 16.f;
         f[7] = (float)kp.flag;
       }
-      for (int t = 0; t < NPROXY; ++t) {
+      for (int t = 0; t < npx; ++t) {
         rows_out[q].push_back((int)(pb + t));
         rows_in[q].push_back((int)(pb + t));
       }
-      HSS_REQUIRE(out.size() <= 4096, HSS_ERR_RANK, "skeleton set exceeds 4096 points");
+      HSS_REQUIRE(out.size() <= (size_t)(4096 / rep), HSS_ERR_RANK, "skeleton set exceeds the ID's 4096 columns");
     }, 16);
     lap(1);
     {
-      const size_t p0 = (size_t)Ntot + (size_t)NPROXY * pslot[boxes[0]];
-      pts.upload_range(p0, (size_t)NPROXY * nbL, hx.data() + p0, hy.data() + p0, hnx.data() + p0, hny.data() + p0,
+      const size_t p0 = (size_t)rep * ((size_t)Ntot + (size_t)poff[boxes[0]]);
+      const size_t p1 = (size_t)rep * ((size_t)Ntot + (size_t)poff[boxes.back()] + (size_t)pcap[boxes.back()]);
+      pts.upload_range(p0, p1 - p0, hx.data() + p0, hy.data() + p0, hnx.data() + p0, hny.data() + p0,
                        hw.data() + p0, hk.data() + p0, kp, stream);
     }
-    // index arrays and block storage
+    // index arrays (table entries: logical point v is entry v, or entries 2v, 2v + 1 of a
+    // complex handle) and block storage
     std::vector<int> idx;
     std::vector<long long> o_ro(nbL), o_ri(nbL), o_out(nbL), o_in(nbL);
+    auto push_ids = [&](const std::vector<int>& v) {
+      for (int a : v)
+        for (int r = 0; r < rep; ++r) idx.push_back(rep * a + r);
+    };
     for (int q = 0; q < nbL; ++q) {
-      o_ro[q] = idx.size(); idx.insert(idx.end(), rows_out[q].begin(), rows_out[q].end());
-      o_ri[q] = idx.size(); idx.insert(idx.end(), rows_in[q].begin(), rows_in[q].end());
-      o_out[q] = idx.size(); idx.insert(idx.end(), outs[q].begin(), outs[q].end());
-      o_in[q] = idx.size(); idx.insert(idx.end(), inns[q].begin(), inns[q].end());
+      o_ro[q] = idx.size(); push_ids(rows_out[q]);
+      o_ri[q] = idx.size(); push_ids(rows_in[q]);
+      o_out[q] = idx.size(); push_ids(outs[q]);
+      o_in[q] = idx.size(); push_ids(inns[q]);
     }
     DevBuf<int> didx;
     upload_vec(didx, idx, stream);
@@ -439,8 +474,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     for (int q = 0; q < nbL; ++q) {
       for (int s = 0; s < ps; ++s) {
         const int pr = ps * q + s;
-        const int m = (int)(s == 0 ? rows_out[q].size() : rows_in[q].size());
-        const int n = (int)outs[q].size();
+        const int m = rep * (int)(s == 0 ? rows_out[q].size() : rows_in[q].size());
+        const int n = rep * (int)outs[q].size();
         pm[pr] = m; pn[pr] = n;
         oA[pr] = tA; tA += (long long)m * n;
         oT2[pr] = tT; tT += (long long)n * n;
@@ -456,7 +491,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     std::vector<KgenP<double>> kg(nprob2);
     std::vector<IdP> ip(nprob2);
     for (int q = 0; q < nbL; ++q) {
-      const int n = (int)outs[q].size(), po = ps * q;
+      const int n = rep * (int)outs[q].size(), po = ps * q;
       kg[po] = KgenP<double>{didx.p + o_ro[q], didx.p + o_out[q], pm[po], n, A.p + oA[po], pm[po], 0};
       if (!sym)
         kg[po + 1] = KgenP<double>{didx.p + o_in[q], didx.p + o_ri[q], n, pm[po + 1], A.p + oA[po + 1], pm[po + 1], 1};
@@ -498,9 +533,16 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     } else if (id_step_test) {
       for (auto& q : ip) q.steps_hint = ID_EVERY_STEP;
     }
+    // complex blocks: the pair-pivoted ID of the embedding (the complex ID of Common/ID.m:40-65)
+    int maxn = 0;
+    for (int v : pn) maxn = std::max(maxn, v);
+    auto run_id = [&](const IdP* d, int cnt) {
+      if (cx) id_pairs_batched(d, cnt, maxn, acc, stream);
+      else id_adaptive_batched(d, cnt, acc, stream, id_df);
+    };
     DevBuf<IdP> dip;
     upload_vec(dip, ip, stream);
-    id_adaptive_batched(dip.p, nprob2, acc, stream, id_df);
+    run_id(dip.p, nprob2);
     std::vector<int> hr, hs;
     download(hr, rank.p, nprob2, stream);
     download(hs, stat.p, (size_t)2 * nprob2, stream);
@@ -514,7 +556,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       if (!redo.empty()) {
         DevBuf<IdP> dr;
         upload_vec(dr, redo, stream);
-        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream, id_df);
+        run_id(dr.p, (int)redo.size());
         download(hr, rank.p, nprob2, stream);
         download(hs, stat.p, (size_t)2 * nprob2, stream);
         HSS_CUDA(cudaStreamSynchronize(stream));
@@ -529,12 +571,12 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     bool any = false;
     std::vector<int> kbox(nbL);
     for (int q = 0; q < nbL; ++q) {
-      const int ko = hr[ps * q], ki = hr[ps * q + ps - 1];
+      const int ko = hr[ps * q] / rep, ki = hr[ps * q + ps - 1] / rep;  // ranks in points
       const int k = std::max(ko, ki);
       kbox[q] = k;
-      const int po = ps * q, pi = ps * q + ps - 1;
-      if (k != ko) { ip[po].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[po], pn[po]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
-      else if (k != ki) { ip[pi].force_k = k; any = true; HSS_REQUIRE(k <= std::min(pm[pi], pn[pi]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+      const int po = ps * q, pi = ps * q + ps - 1, kr = rep * k;
+      if (k != ko) { ip[po].force_k = kr; any = true; HSS_REQUIRE(kr <= std::min(pm[po], pn[po]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
+      else if (k != ki) { ip[pi].force_k = kr; any = true; HSS_REQUIRE(kr <= std::min(pm[pi], pn[pi]), HSS_ERR_RANK, "fixed rank exceeds block size"); }
     }
     if (any) {
       // a fixed-rank re-ID needs R(0:k, :) of the full factorization up to k
@@ -549,7 +591,7 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       if (!redo.empty()) {
         DevBuf<IdP> dr;
         upload_vec(dr, redo, stream);
-        id_adaptive_batched(dr.p, (int)redo.size(), acc, stream, id_df);
+        run_id(dr.p, (int)redo.size());
         HSS_CUDA(cudaStreamSynchronize(stream));
         reruns += (int)redo.size();
       }
@@ -565,8 +607,12 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       const int n = (int)outs[q].size(), k = kbox[q], po = ps * q, pi = ps * q + ps - 1;
       nskel[b] = n;
       kskel[b] = k;
-      J_UP[b].assign(hp.begin() + oP[po], hp.begin() + oP[po] + n);
-      J_DN[b].assign(hp.begin() + oP[pi], hp.begin() + oP[pi] + n);
+      J_UP[b].resize(n);
+      J_DN[b].resize(n);
+      for (int t = 0; t < n; ++t) {  // a pair-pivoted ID moves the two columns of a point together
+        J_UP[b][t] = hp[oP[po] + rep * t] / rep;
+        J_DN[b][t] = hp[oP[pi] + rep * t] / rep;
+      }
       I_SKUP[b].resize(k);
       I_SKDN[b].resize(k);
       for (int t = 0; t < k; ++t) {
@@ -575,9 +621,24 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
       }
       Toff[b] = {oT2[po], oT2[pi]};
       Tlev[b] = (int)Tkeep.size() - 1;
-      census[4 * b] = pm[po]; census[4 * b + 1] = pm[pi]; census[4 * b + 2] = n; census[4 * b + 3] = k;
+      census[4 * b] = pm[po] / rep; census[4 * b + 1] = pm[pi] / rep; census[4 * b + 2] = n; census[4 * b + 3] = k;
     }
     lap(4);
+  }
+  if (cx) {
+    // from here on the handle is the real 2N x 2N embedding: point i is unknowns 2i, 2i + 1
+    // (interleaved real and imaginary parts), and every size and index set counts unknowns
+    auto twice = [](std::vector<int>& v) {
+      std::vector<int> w(2 * v.size());
+      for (size_t i = 0; i < v.size(); ++i) { w[2 * i] = 2 * v[i]; w[2 * i + 1] = 2 * v[i] + 1; }
+      v.swap(w);
+    };
+    for (int b = 0; b < nboxes; ++b) {
+      off[b] *= 2; cnt[b] *= 2; nskel[b] *= 2; kskel[b] *= 2;
+      twice(I_SKUP[b]); twice(I_SKDN[b]); twice(J_UP[b]); twice(J_DN[b]);
+    }
+    for (int p = 0; p < nprob; ++p) { pN[p] *= 2; pbase[p] *= 2; }
+    Ntot *= 2;
   }
   // ---- compact T_UP / T_DN / T_DN^T and J arenas
   oT.assign(nboxes, 0);
@@ -696,6 +757,7 @@ void HSS1D::transforminv(HSS1D& K) {
   K.J_DN = J_UP;
   K.X = X; K.kp = kp; K.kdev = kdev; K.census = census;
   K.oT = oT; K.oSelf = oSelf; K.oSib = oSib; K.oJ = oJ;
+  K.cplx = cplx;
   K.inverted = false;
   const cudaStream_t st = stream;
   auto d2d = [&](DevBuf<double>& dst, const DevBuf<double>& src) {

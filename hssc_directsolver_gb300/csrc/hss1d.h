@@ -72,6 +72,11 @@ struct HSS1D {
   bool id_df = false;  // the IDs' pivoted QR in double-float arithmetic (k_id_adaptive_df)
   bool id_step_test = false;  // every ID's pivoted QR tests the truncation rule at every step
   bool kernel_op = false;  // the handle compresses the kernel matrix of its point table (compress)
+  // complex (HSS_SL_H_2D) matrix held as its real 2 x 2 embedding: point i is unknowns 2i, 2i + 1
+  // (re, im), and Ntot, off, cnt, nskel, kskel, the skeleton sets and J count unknowns; T_DN
+  // holds the embedding of conj(T_DN), so that the real L = [I; T_DN^T] is the embedding of
+  // the complex L = [I; T_DN.'] (HSS1D_invert_nsym.m:70-72)
+  bool cplx = false;
   std::vector<long long> pN, pbase;   // points per problem, first global point
   std::vector<int> proot;              // root box of each problem
   std::vector<unsigned long long> pseed;

@@ -28,6 +28,7 @@ __global__ void k_add_into(long long n, const double* __restrict__ d, double* __
 // places, every leaf's M_SELF is transposed, and each sibling pair's M_SIB blocks are
 // swapped and transposed (HSS1D_transpose.m:24-50).
 void HSS1D::transpose(HSS1D& K) const {
+  HSS_REQUIRE(!cplx, HSS_ERR_ARG, "the transpose of a complex handle is not built (real handles only)");
   HSS_REQUIRE(!rect, HSS_ERR_ARG, "transpose is defined for square handles only");
   K.Ntot = Ntot; K.nprob = nprob; K.nboxes = nboxes; K.leaf = leaf; K.maxlev = maxlev; K.acc = acc; K.sym = sym;
   K.pN = pN; K.pbase = pbase; K.proot = proot; K.pseed = pseed;
@@ -102,6 +103,7 @@ void HSS1D::scalarmult(double c) {
 // forward apply of identity columns, the rows of problem p kept.  (The reference builds
 // it from the telescoping factors, HSS1D_dense_matrix.m:17-92; both are the same matrix.)
 void HSS1D::dense_matrix(int p, double* Kd) {
+  HSS_REQUIRE(!cplx, HSS_ERR_ARG, "the dense export of a complex handle is not built (real handles only)");
   HSS_REQUIRE(!rect, HSS_ERR_ARG, "dense_matrix is defined for square handles only");
   HSS_REQUIRE(p >= 0 && p < nprob, HSS_ERR_ARG, "dense_matrix: problem index out of range");
   HSS_REQUIRE(Kd != nullptr, HSS_ERR_ARG, "dense_matrix: NULL output");
@@ -505,6 +507,7 @@ __global__ void __launch_bounds__(256) k_rform(const RformP* __restrict__ P) {
 }
 
 void HSS1D::sum(const HSS1D& A, const HSS1D& B, double acc_) {
+  HSS_REQUIRE(!A.cplx && !B.cplx, HSS_ERR_ARG, "the sum of complex handles is not built (real handles only)");
   HSS_REQUIRE(!A.rect && !B.rect, HSS_ERR_ARG, "sum is defined for square handles only");
   HSS_REQUIRE(A.nboxes == B.nboxes && A.level == B.level && A.parent == B.parent && A.c1 == B.c1 && A.c2 == B.c2 &&
                   A.off == B.off && A.cnt == B.cnt && A.M_SELF.n == B.M_SELF.n,

@@ -12,6 +12,15 @@ namespace hss {
 constexpr double RADIUS_REL = 1.75;  // HSS1D_compress_nsym.m:51
 constexpr int NPROXY = 50;           // HSS1D_compress_nsym.m:52
 
+// Proxy points of a box whose circumscribing circle has radius R, HSS1D_compress_nsym.m:111-114:
+// 50, or for the Helmholtz kernel min(max(50, round(4 kh 1.75 R + 30)), ntot) (four points per
+// wavelength on the ring); ntot = the problem's points.
+inline int proxy_count(const hss_kernel_params& kp, double R, long long ntot) {
+  if (kp.flag != HSS_SL_H_2D) return NPROXY;
+  const long long r = std::lround(4.0 * kp.kh * RADIUS_REL * R + 30.0);
+  return (int)std::min<long long>(std::max<long long>(NPROXY, r), ntot);
+}
+
 template <typename T>
 inline T* upload_vec(DevBuf<T>& buf, const std::vector<T>& h, cudaStream_t s) {
   buf.alloc(std::max<size_t>(h.size(), 1));

@@ -28,6 +28,10 @@ class HSS1DMatrix:
         self._h = handle
         self.N = N
         self.inverted = False
+        flag = C.c_int32(0)
+        L.check(L.lib().hss1d_is_complex(handle, C.byref(flag)))
+        # a complex (SL_H_2D) matrix takes and returns complex128 vectors
+        self.complex = bool(flag.value)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -70,9 +74,10 @@ class HSS1DMatrix:
         rinf = self.rect_info()
         n, k = int(inf["nskel"][box]), int(inf["kskel"][box])
         nd, kd = int(rinf["nskel_in"][box]), int(rinf["kskel_in"][box])
+        dt = np.complex128 if self.complex else np.float64
         out = dict(I_SKUP=np.zeros(k, np.int32), I_SKDN=np.zeros(kd, np.int32),
                    J_UP=np.zeros(n, np.int32), J_DN=np.zeros(nd, np.int32),
-                   T_UP=np.zeros((k, n - k), order="F"), T_DN=np.zeros((kd, nd - kd), order="F"))
+                   T_UP=np.zeros((k, n - k), dt, order="F"), T_DN=np.zeros((kd, nd - kd), dt, order="F"))
         ip = lambda a: a.ctypes.data_as(L._I32P)
         dp = lambda a: a.ctypes.data_as(L._DP)
         L.check(L.lib().hss1d_export_box(self._h, box, ip(out["I_SKUP"]), ip(out["I_SKDN"]), ip(out["J_UP"]),
@@ -111,6 +116,14 @@ class HSS1DMatrix:
 def _as_f64(a):
     a = np.asarray(a, dtype=np.float64)
     return np.asfortranarray(a)
+
+
+def _vec(K_HSS: HSS1DMatrix, a, rows=None):
+    """Column-major rows x r vectors in the matrix's arithmetic (complex128 for a complex
+    matrix, passed to the library as interleaved (re, im) doubles) and whether a was 1-D."""
+    dt = np.complex128 if K_HSS.complex else np.float64
+    a = np.asfortranarray(np.asarray(a, dtype=dt))
+    return a.reshape(K_HSS.N if rows is None else rows, -1, order="F"), a.ndim == 1
 
 
 def HSS1D_compress_nsym(type_: str, X, TREE: int, acc: float, knl_params: Kernel, seed: int = 0) -> HSS1DMatrix:
@@ -374,18 +387,14 @@ BHSS1D_apply_fsym = BHSS1D_apply_nsym
 
 
 def HSS1D_apply_nsym(K_HSS: HSS1DMatrix, qq) -> np.ndarray:
-    q = _as_f64(qq)
-    vec = q.ndim == 1
-    q2 = q.reshape(K_HSS.N, -1, order="F")
-    out = np.zeros((getattr(K_HSS, "M", K_HSS.N), q2.shape[1]), order="F")
+    q2, vec = _vec(K_HSS, qq)
+    out = np.zeros((getattr(K_HSS, "M", K_HSS.N), q2.shape[1]), q2.dtype, order="F")
     L.check(L.lib().hss1d_apply(K_HSS._h, L.ptr(q2), L.ptr(out), q2.shape[1]))
     return out[:, 0] if vec else out
 
 
 def HSS1D_applyinv_nsym(K_HSS: HSS1DMatrix, HSSinv, FTinv, ff) -> np.ndarray:
-    f = _as_f64(ff)
-    vec = f.ndim == 1
-    f2 = f.reshape(K_HSS.N, -1, order="F")
+    f2, vec = _vec(K_HSS, ff)
     out = np.zeros_like(f2, order="F")
     L.check(L.lib().hss1d_applyinv(K_HSS._h, L.ptr(f2), L.ptr(out), f2.shape[1]))
     return out[:, 0] if vec else out
@@ -394,9 +403,7 @@ def HSS1D_applyinv_nsym(K_HSS: HSS1DMatrix, HSSinv, FTinv, ff) -> np.ndarray:
 def HSS1D_solve(K_HSS: HSS1DMatrix, ff, tol: float = 1e-10, maxit: int = 5):
     """x = A^-1 f refined against the FP64 HSS1D forward operator
     (Common/Iterative_Refinement.m:20-35).  Returns (x, relres, inverse applies used)."""
-    f = _as_f64(ff)
-    vec = f.ndim == 1
-    f2 = f.reshape(K_HSS.N, -1, order="F")
+    f2, vec = _vec(K_HSS, ff)
     out = np.zeros_like(f2, order="F")
     rr = C.c_double()
     it = C.c_int32()
@@ -409,8 +416,8 @@ def HSS1D_kernel_residual(K_HSS: HSS1DMatrix, ff, xx) -> float:
     """max over columns of ||f - K x|| / ||f|| with K the kernel matrix of each curve itself
     (generated in FP64 on the GPU and applied on the fly, never formed): the dense-matrix
     residual the reference's tests print (Common/Iterative_Refinement.m:20-35)."""
-    f2 = _as_f64(ff).reshape(K_HSS.N, -1, order="F")
-    x2 = _as_f64(xx).reshape(K_HSS.N, -1, order="F")
+    f2, _ = _vec(K_HSS, ff)
+    x2, _ = _vec(K_HSS, xx)
     assert f2.shape == x2.shape
     rr = C.c_double()
     L.check(L.lib().hss1d_kernel_residual(K_HSS._h, L.ptr(f2), L.ptr(x2), f2.shape[1], C.byref(rr)))

@@ -138,7 +138,13 @@ typedef struct hss1d_matrix hss1d_matrix;
  *   HSS1D/HSS1D_compress_nsym.m:1 (tree :277-334, skeletons :84-216,
  *   self/sibling blocks :220-271).
  * X: N x 6 column-major [x y nx ny w kappa] (ldx >= N); leaf = nbox_max.
- * seed: key of the counter RNG drawing the rank-check vectors (ID.m:68-86). */
+ * seed: key of the counter RNG drawing the rank-check vectors (ID.m:68-86).
+ * HSS_SL_H_2D (also in hss1d_compress_batch): the complex Helmholtz matrix, with the proxy
+ *   ring of min(max(50, round(4 kh 1.75 R + 30)), N) points (:111-114) and complex IDs; its
+ *   vectors are N x nrhs complex, interleaved (re, im) doubles (2 N doubles per column), and
+ *   hss1d_info / hss1d_export_box report points and complex T (hss1d_is_complex).  Not with
+ *   hss1d_compress_fsym, the rank predictor or the double-float ID; hss1d_transpose, hss1d_sum,
+ *   hss1d_dense_matrix and the submatrix applies reject complex handles. */
 int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
                    double acc, const hss_kernel_params* kp, uint64_t seed);
 /* K_HSS = HSS1D_compress_fsym('green', X, TREE, acc, knl_params), HSS1D/HSS1D_compress_fsym.m:98-248:
@@ -157,13 +163,16 @@ int hss1d_compress_batch(hss1d_matrix** out, int32_t nprob, const int64_t* N, co
                          const uint64_t* seeds);
 /* problems of a forest: count, total points, root box and first stacked row of each (NULL ok) */
 int hss1d_forest_info(const hss1d_matrix* H, int32_t* nprob, int64_t* Ntot, int32_t* root, int64_t* pbase);
+/* 1 when the handle holds a complex (HSS_SL_H_2D) matrix, else 0 */
+int hss1d_is_complex(const hss1d_matrix* H, int32_t* is_complex);
 /* tree and skeleton sizes over the forest's global box ids: arrays of nboxes entries (NULL ok);
  * off is the global (stacked) first point of a box */
 int hss1d_info(const hss1d_matrix* H, int32_t* nboxes, int32_t* level, int32_t* parent,
                int32_t* c1, int32_t* c2, int32_t* off, int32_t* cnt, int32_t* nskel,
                int32_t* kskel);
 /* K_HSS{I_SKUP,I_SKDN,J_UP,J_DN,T_UP,T_DN} of one box (box_constants.m:33-52);
- * T_* are k x (n-k) column-major; any pointer may be NULL. */
+ * T_* are k x (n-k) column-major (complex handles: interleaved (re, im), 2 k (n-k) doubles);
+ * any pointer may be NULL. */
 int hss1d_export_box(const hss1d_matrix* H, int32_t box, int32_t* I_skup, int32_t* I_skdn,
                      int32_t* J_up, int32_t* J_dn, double* T_up, double* T_dn);
 /* K_HSS = HSS1D_compress_rectangular_nsym('green', Xin, Xout, TREE, acc, params)

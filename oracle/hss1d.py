@@ -23,11 +23,38 @@ import math
 
 import numpy as np
 
-from .kernels import KernelParams, kernel_eval, DL_L_2D, SL_L_2D
-from . import idecomp
+from .kernels import KernelParams, kernel_eval, DL_L_2D, SL_L_2D, SL_H_2D
+from . import cid, idecomp
 
 RADIUS_REL = 1.75   # HSS1D_compress_nsym.m:51
 NPROXY = 50         # HSS1D_compress_nsym.m:52
+
+
+def _mround(x: float) -> int:
+    """MATLAB's round (half away from zero), exact for x >= 0."""
+    t = math.floor(x)
+    return int(t) + (1 if x - t >= 0.5 else 0)
+
+
+def proxy_count(kp: KernelParams, R: float, ntot: int) -> int:
+    """Proxy points of a box, HSS1D_compress_nsym.m:111-114: 50, or for the Helmholtz
+    kernel min(max(50, round(4 kh 1.75 R + 30)), ntot) (four points per wavelength)."""
+    if kp.flag == SL_H_2D:
+        return min(max(NPROXY, _mround(4.0 * kp.kh * RADIUS_REL * R + 30.0)), ntot)
+    return NPROXY
+
+
+def _id_out(A, acc, seed, problem):
+    """ID(A, acc) of Common/ID.m:40-65, complex through oracle.cid for complex blocks."""
+    if np.iscomplexobj(A):
+        return cid.id_adaptive_complex(A, acc, seed, problem)
+    return idecomp.id_adaptive(A, acc, seed, problem)
+
+
+def _id_fixed(R, J, k):
+    if np.iscomplexobj(R):
+        return cid.id_fixed_complex(R, J, k)
+    return idecomp.id_fixed_from_qr(R, J, k)
 
 
 @dataclass
@@ -190,7 +217,7 @@ def compress_green_blocks(H, X, ibox, nei, kp: KernelParams, ntot):
     out, inn = _box_skel_sets(H, ibox)
     both = np.sort(np.concatenate([out, inn]), kind="stable")
     xxc, R = circum_circle(X[both])
-    nproxy = NPROXY
+    nproxy = proxy_count(kp, R, ntot)
     Cp = proxy_circle(xxc, RADIUS_REL * R, nproxy)
     out_maybe, in_maybe = [], []
     for j in nei[ibox]:
@@ -223,7 +250,9 @@ def compress_nsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: 
     """K_HSS = HSS1D_compress_nsym('green', X, TREE, acc, knl_params).
 
     ID problem numbering for the shared RNG: box b's outgoing ID is problem
-    2*b, its incoming ID 2*b+1.
+    2*b, its incoming ID 2*b+1.  With the Helmholtz kernel (SL_H_2D) every block is
+    complex: the proxy ring holds proxy_count points and the IDs are complex
+    (oracle.cid); T_DN is the ID's T of A_in.' (plain transpose), as in the reference.
     """
     X = np.asarray(X, dtype=np.float64)
     ntot = X.shape[0]
@@ -236,13 +265,13 @@ def compress_nsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: 
     nei = neighbor_list(X, t)
     for ibox in range(nb - 1, 0, -1):
         out, inn, A_out, A_in = compress_green_blocks(H, X, ibox, nei, kp, ntot)
-        Tout, Jout, kout, Rout = idecomp.id_adaptive(A_out, acc, seed, 2 * ibox)
-        Tin, Jin, kin, Rin = idecomp.id_adaptive(A_in.T, acc, seed, 2 * ibox + 1)
+        Tout, Jout, kout, Rout = _id_out(A_out, acc, seed, 2 * ibox)
+        Tin, Jin, kin, Rin = _id_out(A_in.T, acc, seed, 2 * ibox + 1)
         k = max(kout, kin)
         if k != kout:
-            Tout = idecomp.id_fixed_from_qr(Rout, Jout, k)
+            Tout = _id_fixed(Rout, Jout, k)
         elif k != kin:
-            Tin = idecomp.id_fixed_from_qr(Rin, Jin, k)
+            Tin = _id_fixed(Rin, Jin, k)
         H.I_SKUP[ibox] = out[Jout[:k]]
         H.T_UP[ibox] = Tout
         H.J_UP[ibox] = Jout
@@ -302,10 +331,11 @@ def compress_fsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: 
 def _RL(H, b):
     """R (k x n) and L (n x k) of HSS1D_invert_nsym.m:63-72."""
     n, k = H.nskel[b], H.kskel[b]
-    R = np.zeros((k, n))
+    dt = np.result_type(H.T_UP[b], H.T_DN[b], np.float64)
+    R = np.zeros((k, n), dtype=dt)
     R[:, H.J_UP[b][:k]] = np.eye(k)
     R[:, H.J_UP[b][k:]] = H.T_UP[b]
-    L = np.zeros((n, k))
+    L = np.zeros((n, k), dtype=dt)
     L[H.J_DN[b][:k], :] = np.eye(k)
     L[H.J_DN[b][k:], :] = H.T_DN[b].T
     return R, L
@@ -355,7 +385,7 @@ def _skel_proj(T, J, q):
 
 def _skel_eval(T, J, u):
     """LOCAL_skel_eval, HSS1D_apply_nsym.m:121-130."""
-    out = np.zeros((len(J), u.shape[1]))
+    out = np.zeros((len(J), u.shape[1]), dtype=np.result_type(T, u))
     if T.shape[1] == 0:
         out[J] = u
     else:
@@ -365,11 +395,17 @@ def _skel_eval(T, J, u):
     return out
 
 
+def _dtype(H: HSS1DMatrix, v):
+    """complex128 when the compressed matrix or the vector is complex, else float64."""
+    cplx = np.iscomplexobj(v) or any(m is not None and np.iscomplexobj(m) for m in H.M_SELF)
+    return np.complex128 if cplx else np.float64
+
+
 def apply_nsym(H: HSS1DMatrix, qq: np.ndarray) -> np.ndarray:
     """uu = HSS1D_apply_nsym(K_HSS, qq), HSS1D_apply_nsym.m:38-100."""
     t = H.tree
     nb = t.nboxes
-    qq = np.asarray(qq, dtype=np.float64)
+    qq = np.asarray(qq, dtype=_dtype(H, qq))
     vec = qq.ndim == 1
     if vec:
         qq = qq[:, None]
@@ -406,7 +442,7 @@ def applyinv_nsym(H: HSS1DMatrix, inv: dict, ff: np.ndarray) -> np.ndarray:
     """xx = HSS1D_applyinv_nsym(K_HSS, HSSinv, FTinv, ff), HSS1D_applyinv_nsym.m:43-86."""
     t = H.tree
     nb = t.nboxes
-    ff = np.asarray(ff, dtype=np.float64)
+    ff = np.asarray(ff, dtype=_dtype(H, ff))
     vec = ff.ndim == 1
     if vec:
         ff = ff[:, None]
