@@ -197,7 +197,8 @@ inline void run_graph(GraphCache& gc, int key, cudaStream_t s, bool enabled, F&&
     }
     HSS_CUDA(cudaStreamEndCapture(s, &graph));
     cudaGraphExec_t ex = nullptr;
-    cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+    // per-node priorities: kernels captured from a high-priority stream keep their priority
+    cudaError_t e = cudaGraphInstantiateWithFlags(&ex, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     HSS_REQUIRE(e == cudaSuccess, HSS_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
     it = gc.g.emplace(key, ex).first;

@@ -333,9 +333,48 @@ void SolvePlan<R>::run_step(const Step& st, cudaStream_t s) const {
   gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
 }
 
+PlanStreams::PlanStreams(size_t nsteps) {
+  int least = 0, greatest = 0;
+  HSS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  HSS_CUDA(cudaStreamCreateWithPriority(&crit, cudaStreamNonBlocking, greatest));
+  HSS_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, least));
+  for (cudaEvent_t* e : {&fork, &jc, &js}) HSS_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  ev.assign(nsteps, nullptr);
+  for (auto& e : ev) HSS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
+PlanStreams::~PlanStreams() {
+  for (auto e : ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : {fork, jc, js})
+    if (e) cudaEventDestroy(e);
+  if (crit) cudaStreamDestroy(crit);
+  if (side) cudaStreamDestroy(side);
+}
+
 template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
-  for (auto& st : steps) run_step(st, s);
+  if (!streams) {
+    for (auto& st : steps) run_step(st, s);
+  } else {
+    // fork both streams from s, issue every step after the steps it depends on, join
+    // both back into s (under graph capture the events become graph edges)
+    PlanStreams& S = *streams;
+    HSS_CUDA(cudaEventRecord(S.fork, s));
+    HSS_CUDA(cudaStreamWaitEvent(S.crit, S.fork, 0));
+    HSS_CUDA(cudaStreamWaitEvent(S.side, S.fork, 0));
+    for (size_t i = 0; i < steps.size(); ++i) {
+      const Step& st = steps[i];
+      cudaStream_t q = st.side ? S.side : S.crit;
+      for (int d : st.deps) HSS_CUDA(cudaStreamWaitEvent(q, S.ev[d], 0));
+      run_step(st, q);
+      if (st.rec) HSS_CUDA(cudaEventRecord(S.ev[i], q));
+    }
+    HSS_CUDA(cudaEventRecord(S.jc, S.crit));
+    HSS_CUDA(cudaEventRecord(S.js, S.side));
+    HSS_CUDA(cudaStreamWaitEvent(s, S.jc, 0));
+    HSS_CUDA(cudaStreamWaitEvent(s, S.js, 0));
+  }
   for (auto& st : tc_steps) st.run(s);
 }
 
@@ -1256,8 +1295,26 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       return pl;
     }
   }
-  // upward pass
-  for (int lev = depth; lev >= 1; --lev) {
+  // HSS2D_applyinv_nsym.m:74-243: the upward pass phi_up = U q (q: the right-hand sides
+  // at the leaves, the children's phi_up above), then per level out = FI q - G phi_up +
+  // GE phi_dn (phi_dn: the parent's output).  FI q needs only the level's input and
+  // - G phi_up only the level's own phi_up, so both leave the critical path: they run on a
+  // low-priority side stream as soon as the upward pass has produced their operands, while
+  // the high-priority stream runs the upward pass, the root and the + GE phi_dn
+  // accumulations.  The three parts are added in FP64 storage (beta = 1).
+  auto out_of = [&](int lev, int i, R*& out, int& ldo) {
+    if (lev == depth) {
+      const int b = (1 << lev) - 1 + i;
+      out = vout.p + (size_t)NG * geo.leaf_panel[b];
+      ldo = (int)N;
+    } else {
+      const auto& gc = geo.levels[lev + 1];
+      out = L[lev + 1].vec<R>(1).p + (size_t)(2 * i) * gc.k;
+      ldo = gc.nb * gc.k;
+    }
+  };
+  // part 0: U q (upward); 1: FI q; 2: G phi_up; 3: GE phi_dn
+  auto prods = [&](int lev, int part) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
     std::vector<GemmP<R>> P;
@@ -1265,35 +1322,50 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
       const R* q;
       int ldq;
       qptr(lev, i, q, ldq);
-      P.push_back(GemmP<R>{F(d, 2) + fo(i) * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n,
-                           g.k, ldq, g.nb * g.k});
-    }
-    pl.add(P, R(1), R(0), stream);
-  }
-  // downward pass
-  for (int lev = 0; lev <= depth; ++lev) {
-    const auto& g = geo.levels[lev];
-    auto& d = L[lev];
-    std::vector<GemmP<R>> P1, P2, P3;
-    std::vector<SegGemmP> PS;
-    for (int i = 0; i < g.nb; ++i) {
       R* out;
       int ldo;
-      if (lev == depth) {
-        const int b = (1 << lev) - 1 + i;
-        out = vout.p + (size_t)NG * geo.leaf_panel[b];
-        ldo = (int)N;
-      } else {
-        const auto& gc = geo.levels[lev + 1];
-        out = L[lev + 1].vec<R>(1).p + (size_t)(2 * i) * gc.k;
-        ldo = gc.nb * gc.k;
-      }
-      const R* q;
-      int ldq;
-      qptr(lev, i, q, ldq);
-      if constexpr (std::is_same<R, double>::value) {
-        if (use_df && lev > 0) {
-          // FI q - G phi_up + GE phi_dn as one double-float sum
+      out_of(lev, i, out, ldo);
+      if (part == 0)
+        P.push_back(GemmP<R>{F(d, 2) + fo(i) * g.k * g.n, q, d.vec<R>(0).p + (size_t)i * g.k, g.k, r, g.n, g.k,
+                             ldq, g.nb * g.k});
+      else if (part == 1)
+        P.push_back(GemmP<R>{F(d, 0) + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
+      else
+        P.push_back(GemmP<R>{F(d, part == 2 ? 3 : 4) + fo(i) * g.n * g.k,
+                             d.vec<R>(part == 2 ? 0 : 1).p + (size_t)i * g.k, out, g.n, r, g.k, g.n, g.nb * g.k,
+                             ldo});
+    }
+    return P;
+  };
+  auto mark = [&](int side, int dep) {
+    auto& st = pl.steps.back();
+    st.side = side;
+    if (dep >= 0) {
+      st.deps.push_back(dep);
+      pl.steps[dep].rec = true;
+    }
+    return (int)pl.steps.size() - 1;
+  };
+  auto push = [&](int lev, int part, R alpha, R beta, int side, int dep) {
+    auto P = prods(lev, part);
+    pl.add(P, alpha, beta, stream);
+    return mark(side, dep);
+  };
+  // the side stream's product of a level: FI q - G phi_up (one double-float sum with
+  // double-float operands), after the level's upward product
+  auto push_side = [&](int lev, int dep) {
+    if constexpr (std::is_same<R, double>::value) {
+      if (use_df) {
+        const auto& g = geo.levels[lev];
+        auto& d = L[lev];
+        std::vector<SegGemmP> PS;
+        for (int i = 0; i < g.nb; ++i) {
+          const R* q;
+          int ldq;
+          qptr(lev, i, q, ldq);
+          R* out;
+          int ldo;
+          out_of(lev, i, out, ldo);
           SegGemmP sp{};
           sp.A[0] = F(d, 0) + fo(i) * g.n * g.n;
           sp.B[0] = q;
@@ -1307,38 +1379,35 @@ SolvePlan<R>& HSS2D::inv_plan(int r) {
           sp.lda[1] = g.n;
           sp.ldb[1] = g.nb * g.k;
           sp.sign[1] = -1.0;
-          sp.A[2] = F(d, 4) + fo(i) * g.n * g.k;
-          sp.B[2] = d.vec<R>(1).p + (size_t)i * g.k;
-          sp.K[2] = g.k;
-          sp.lda[2] = g.n;
-          sp.ldb[2] = g.nb * g.k;
-          sp.sign[2] = 1.0;
           sp.C = out;
           sp.M = g.n;
           sp.N = r;
           sp.ldc = ldo;
           PS.push_back(sp);
-          continue;
         }
-      }
-      P1.push_back(GemmP<R>{F(d, 0) + fo(i) * g.n * g.n, q, out, g.n, r, g.n, g.n, ldq, ldo});
-      if (lev > 0) {
-        P2.push_back(GemmP<R>{F(d, 3) + fo(i) * g.n * g.k, d.vec<R>(0).p + (size_t)i * g.k, out, g.n, r,
-                              g.k, g.n, g.nb * g.k, ldo});
-        P3.push_back(GemmP<R>{F(d, 4) + fo(i) * g.n * g.k, d.vec<R>(1).p + (size_t)i * g.k, out, g.n, r,
-                              g.k, g.n, g.nb * g.k, ldo});
+        pl.add_seg(PS, R(1), R(0), stream);
+        return mark(1, dep);
       }
     }
-    if (!PS.empty()) {
-      pl.add_seg(PS, R(1), R(0), stream);
-      continue;
-    }
-    pl.add(P1, R(1), R(0), stream);
-    if (lev > 0) {
-      pl.add(P2, R(-1), R(1), stream);
-      pl.add(P3, R(1), R(1), stream);
-    }
+    push(lev, 1, R(1), R(0), 1, dep);
+    return push(lev, 2, R(-1), R(1), 1, -1);
+  };
+  // Issue order.  The side stream takes the lower half of the levels in the order the
+  // upward pass completes them (bottom up, overlapping the upward pass), then the upper
+  // half top down, which is the order the downward accumulations need them: the side
+  // product of level l + 1 overlaps the accumulation of level l.
+  const int mid = depth / 2;
+  std::vector<int> up(depth + 1, -1), side(depth + 1, -1);
+  for (int lev = depth; lev >= 1; --lev) {
+    up[lev] = push(lev, 0, R(1), R(0), 0, -1);
+    if (lev > mid) side[lev] = push_side(lev, up[lev]);
   }
+  push(0, 1, R(1), R(0), 0, -1);  // the root: FI q, after the whole upward pass
+  for (int lev = 1; lev <= depth; ++lev) {
+    if (lev <= mid) side[lev] = push_side(lev, up[lev]);
+    push(lev, 3, R(1), R(1), 0, side[lev]);
+  }
+  if (depth >= 1) pl.streams = std::make_shared<PlanStreams>(pl.steps.size());
   HSS_CUDA(cudaStreamSynchronize(stream));
   if (autotune) pl.tune(stream);
   return pl;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <map>
+#include <memory>
 #include <type_traits>
 #include <vector>
 
@@ -11,6 +12,18 @@
 #include "skinny_tc.cuh"
 
 namespace hss {
+
+// The two streams of a plan whose steps run concurrently: the critical chain on a
+// high-priority stream, the steps off it on a low-priority one; one event per step.
+struct PlanStreams {
+  cudaStream_t crit = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, jc = nullptr, js = nullptr;
+  std::vector<cudaEvent_t> ev;
+  explicit PlanStreams(size_t nsteps);
+  ~PlanStreams();
+  PlanStreams(const PlanStreams&) = delete;
+  PlanStreams& operator=(const PlanStreams&) = delete;
+};
 
 // A fixed sequence of batched skinny products (one inverse or forward apply
 // pass for a given number of right-hand sides); descriptors stay on the device.
@@ -22,8 +35,13 @@ struct SolvePlan {
     DevBuf<R> part;  // split-K partial sums
     int batch = 0, maxM = 0, maxN = 0, maxK = 0, ksplit = 1;
     R alpha = R(1), beta = R(0);
+    int side = 0;          // with streams: 0 the critical stream, 1 the side stream
+    std::vector<int> deps; // earlier steps (indices) this one waits for
+    bool rec = false;      // a later step waits for this one
   };
   std::vector<Step> steps;
+  // set: the steps are issued on two streams (fork from and join back to run()'s stream)
+  std::shared_ptr<PlanStreams> streams;
   std::vector<TcStep> tc_steps;  // tensor-core products (HSS_PREC_TC inverse applies)
   bool df = false;  // FP64 operands stored as float pairs, products on the FP32 pipes
   void run_step(const Step& st, cudaStream_t s) const;
