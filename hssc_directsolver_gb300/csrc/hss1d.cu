@@ -44,8 +44,14 @@ __global__ void __launch_bounds__(256) k_move(const MoveP* __restrict__ P) {
       double* d = p.dst + di + (size_t)c * p.ldd;
       const double v = p.src[i + (size_t)c * p.lds];
       *d = p.accumulate ? *d + v : v;
-    } else {  // 3: transpose copy dst(c, i) = src(i, c)
+    } else if (p.mode == 3) {  // transpose copy dst(c, i) = src(i, c)
       p.dst[c + (size_t)i * p.ldd] = p.src[i + (size_t)c * p.lds];
+    } else {
+      // real 2 x 2 embeddings (even offsets): 4 conjugate, E(conj X) = S E(X) S; 5 plain
+      // transpose, E(X.') = S E(X)^T S; S = diag(1, -1, 1, -1, ...)
+      const double v = ((i + c) & 1) ? -p.src[i + (size_t)c * p.lds] : p.src[i + (size_t)c * p.lds];
+      if (p.mode == 4) p.dst[i + (size_t)c * p.ldd] = v;
+      else p.dst[c + (size_t)i * p.ldd] = v;
     }
   }
 }
@@ -221,8 +227,8 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
   // complex (Helmholtz) kernel: the blocks are generated and skeletonized in the real 2 x 2
   // embedding (pair-pivoted ID); the finished handle is the real 2N x 2N embedded matrix
   const bool cx = (kp_.flag == HSS_SL_H_2D);
-  HSS_REQUIRE(!cx || (!sym_ && !mlp && !id_df), HSS_ERR_ARG,
-              "complex compression: the nsym form with the plain FP64 ID and no rank predictor");
+  HSS_REQUIRE(!cx || (!mlp && !id_df), HSS_ERR_ARG,
+              "complex compression: the plain FP64 ID and no rank predictor");
   cplx = cx;
   const int rep = cx ? 2 : 1;
   using clk = std::chrono::steady_clock;
@@ -660,8 +666,10 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     if (n - k <= 0 || k == 0) continue;
     const double* Tl = Tkeep[Tlev[b]].p;
     mv.push_back(MoveP{Tl + Toff[b][0], T_UP.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
-    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, 0, 0});
-    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, 3, 0});
+    // complex fsym: T_DN = T_UP is kept as conj(T_UP) (the handle's T_DN convention)
+    const bool cj = cplx && sym;
+    mv.push_back(MoveP{Tl + Toff[b][1], T_DN.p + oT[b], nullptr, k, n - k, n, k, cj ? 4 : 0, 0});
+    mv.push_back(MoveP{Tl + Toff[b][1], TDNT.p + oT[b], nullptr, k, n - k, n, n - k, cj ? 5 : 3, 0});
   }
   run_moves(mv, stream);
   upload_vec(JUPd, hJU, stream);
@@ -724,12 +732,12 @@ void HSS1D::compress(int np_, const long long* Np, const double* const* Xp, cons
     const int c = (int)std::min<size_t>(65535, kg.size() - o);
     kgen_batched<double>(dkg.p + o, c, maxe, view(pts), kdev, stream);
   }
-  if (sym) {  // M_SIB{c2} = M_SIB{c1}.' (HSS1D_compress_fsym.m:245)
+  if (sym) {  // M_SIB{c2} = M_SIB{c1}.' (HSS1D_compress_fsym.m:245; plain transpose when complex)
     std::vector<MoveP> mv;
     for (int b = 0; b < nboxes; ++b)
       if (!is_leaf(b) && kskel[c1[b]] > 0 && kskel[c2[b]] > 0)
         mv.push_back(MoveP{M_SIB.p + oSib[c1[b]], M_SIB.p + oSib[c2[b]], nullptr, kskel[c1[b]], kskel[c2[b]],
-                           kskel[c1[b]], kskel[c2[b]], 3, 0});
+                           kskel[c1[b]], kskel[c2[b]], cplx ? 5 : 3, 0});
     run_moves(mv, stream);
   }
   HSS_CUDA(cudaStreamSynchronize(stream));

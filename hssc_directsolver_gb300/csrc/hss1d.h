@@ -17,7 +17,9 @@ namespace hss {
 
 // Generic small block move: mode 0 row gather dst(i,c) = src(idx[i], c);
 // mode 1 column gather dst(i,c) = src(i, idx[c]); mode 2 row scatter
-// dst(idx[i], c) (+)= src(i, c); mode 3 transpose dst(c,i) = src(i,c).
+// dst(idx[i], c) (+)= src(i, c); mode 3 transpose dst(c,i) = src(i,c); on real 2 x 2
+// embeddings of complex blocks, mode 4 the conjugate and mode 5 the plain transpose
+// (dst(c,i) = (-1)^(i+c) src(i,c)).
 // idx == nullptr means identity.
 struct MoveP {
   const double* src;

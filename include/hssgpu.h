@@ -142,8 +142,9 @@ typedef struct hss1d_matrix hss1d_matrix;
  * HSS_SL_H_2D (also in hss1d_compress_batch): the complex Helmholtz matrix, with the proxy
  *   ring of min(max(50, round(4 kh 1.75 R + 30)), N) points (:111-114) and complex IDs; its
  *   vectors are N x nrhs complex, interleaved (re, im) doubles (2 N doubles per column), and
- *   hss1d_info / hss1d_export_box report points and complex T (hss1d_is_complex).  Not with
- *   hss1d_compress_fsym, the rank predictor or the double-float ID; hss1d_transpose, hss1d_sum,
+ *   hss1d_info / hss1d_export_box report points and complex T (hss1d_is_complex); with
+ *   hss1d_compress_fsym the matrix is taken as complex symmetric (K.' = K, plain transposes).
+ *   Not with the rank predictor or the double-float ID; hss1d_transpose, hss1d_sum,
  *   hss1d_dense_matrix and the submatrix applies reject complex handles. */
 int hss1d_compress(hss1d_matrix** out, const double* X, int64_t N, int64_t ldx, int32_t leaf,
                    double acc, const hss_kernel_params* kp, uint64_t seed);

@@ -310,7 +310,7 @@ def compress_fsym(X: np.ndarray, leaf: int, acc: float, kp: KernelParams, seed: 
     nei = neighbor_list(X, t)
     for ibox in range(nb - 1, 0, -1):
         out, _, A_out, _ = compress_green_blocks(H, X, ibox, nei, kp, ntot)
-        T, J, k, _ = idecomp.id_adaptive(A_out, acc, seed, 2 * ibox)
+        T, J, k, _ = _id_out(A_out, acc, seed, 2 * ibox)
         H.I_SKUP[ibox] = H.I_SKDN[ibox] = out[J[:k]]
         H.T_UP[ibox] = H.T_DN[ibox] = T
         H.J_UP[ibox] = H.J_DN[ibox] = J

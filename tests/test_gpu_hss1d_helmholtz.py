@@ -129,5 +129,32 @@ def test_complex_forest_matches_single_curves(gpu):
         assert np.array_equal(kF[roots[p] + 1:roots[p] + nb], np.array(Ho.kskel[1:]))
         s = slice(int(base[p]), int(base[p]) + X.shape[0])
         assert _rel(u[s], O1.apply_nsym(Ho, q[s])) <= 1e-12
-    with pytest.raises(Exception):
-        G1.HSS1D_compress_fsym("green", Xs[0], LEAF, ACC, gk)   # the fsym form is real only
+
+
+def test_complex_symmetric_fsym(gpu):
+    """HSS1D_compress_fsym on a complex symmetric matrix (b = c, so K.' = K): one complex ID
+    per box, T_DN = T_UP and M_SIB{c2} = M_SIB{c1}.' (plain transposes,
+    HSS1D_compress_fsym.m:186-198, :245).  Ranks and skeletons equal the oracle's; the applies
+    match it and the dense matrix."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    gb, ob = GK.Modulation(0.5, 0.3, 0.0, 2.0), OK.Modulation(0.5, 0.3, 0.0, 2.0)
+    gk = GK.Kernel("SL_H_2D", H, gb, gb, KH, DR)
+    ok = OK.KernelParams(flag=OK.SL_H_2D, h=H, b=ob, c=ob, kh=KH, dr=DR)
+    X = geometry.star_curve(768)
+    K = OK.kernel_eval(X, X, ok)
+    assert np.abs(K - K.T).max() <= 1e-15 * np.abs(K).max()
+    Hg = G1.HSS1D_compress_fsym("green", X, LEAF, ACC, gk)
+    Ho = O1.compress_fsym(X, LEAF, ACC, ok)
+    assert Hg.complex
+    assert np.array_equal(Hg.info()["kskel"][1:], np.array(Ho.kskel[1:]))
+    for b in range(1, len(Ho.kskel)):
+        e = Hg.export_box(b)
+        assert np.array_equal(e["I_SKUP"], Ho.I_SKUP[b]) and np.array_equal(e["I_SKDN"], Ho.I_SKUP[b]), b
+        assert np.array_equal(e["T_UP"], e["T_DN"]), b
+    r = np.random.default_rng(10)
+    q = r.standard_normal((768, 2)) + 1j * r.standard_normal((768, 2))
+    u = G1.HSS1D_apply_nsym(Hg, q)
+    assert _rel(u, O1.apply_nsym(Ho, q)) <= 1e-12 and _rel(u, K @ q) <= 1e-9
+    G1.HSS1D_invert_nsym(Hg)
+    x = G1.HSS1D_applyinv_nsym(Hg, None, None, u)
+    assert _rel(x, O1.applyinv_nsym(Ho, O1.invert_nsym(Ho), u)) <= 1e-11 and _rel(x, q) <= 1e-11
