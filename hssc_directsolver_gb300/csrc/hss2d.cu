@@ -1494,13 +1494,14 @@ void HSS2D::fwd_prepare(int r) {
       fp.up[lev].add(P, 1.0, 1.0, stream);
     }
   }
-  // every level's sibling and leaf products (lam) read only the finished upward pass and the
-  // input: one step holds them all (fp.lam[0]); the downward pass then runs eta and the
-  // scatters, which add onto what lam wrote
-  std::vector<GemmP<double>> P;
+  // the sibling products of level lev (the leaves' self products at lev = depth) read the
+  // upward pass of level lev + 1 (the input at the leaves): fp.lam[lev] runs on a side
+  // stream once that level is done; the downward pass then runs eta and the scatters,
+  // which add onto what lam wrote
   for (int lev = 0; lev <= depth; ++lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
+    std::vector<GemmP<double>> P;
     for (int i = 0; i < g.nb; ++i) {
       double* out;
       int ldo;
@@ -1530,8 +1531,9 @@ void HSS2D::fwd_prepare(int r) {
                                   d.tmF.p + (size_t)i * nr, nr, r, g.k, nr, g.nb * g.k, g.nb * nr});
       fp.eta[lev].add(Q, 1.0, 0.0, stream);
     }
+    fp.lam[lev].add(P, 1.0, 0.0, stream);
   }
-  fp.lam[0].add(P, 1.0, 0.0, stream);
+  fp.streams = std::make_shared<PlanStreams>(2 * (size_t)(depth + 1));
   HSS_CUDA(cudaStreamSynchronize(stream));
   if (autotune)
     for (int lev = 0; lev <= depth; ++lev) {
@@ -1551,6 +1553,19 @@ void HSS2D::apply_stage_body(int r) {
   FwdPlan& fp = fwd_plans[r];
   const int depth = geo.depth;
   const long long N = geo.N;
+  // HSS2D_apply_nsym.m:74-218 on two streams: the upward pass, then per level the
+  // downward evaluation and scatter on a high-priority stream; each level's sibling
+  // products (the leaves' self products) on a low-priority stream as soon as the upward
+  // pass has produced their operands
+  PlanStreams& S = *fp.streams;
+  cudaStream_t cs = S.crit, ss = S.side;
+  auto ev_up = [&](int lev) { return S.ev[lev]; };
+  auto ev_lam = [&](int lev) { return S.ev[depth + 1 + lev]; };
+  HSS_CUDA(cudaEventRecord(S.fork, stream));
+  HSS_CUDA(cudaStreamWaitEvent(cs, S.fork, 0));
+  HSS_CUDA(cudaStreamWaitEvent(ss, S.fork, 0));
+  fp.lam[depth].run(ss);  // the leaves' self products: the input only
+  HSS_CUDA(cudaEventRecord(ev_lam(depth), ss));
   for (int lev = depth; lev >= 1; --lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
@@ -1559,12 +1574,15 @@ void HSS2D::apply_stage_body(int r) {
     const double* src = leaf ? Xd.p : L[lev + 1].upF.p;
     const long long lds = leaf ? N : (long long)geo.levels[lev + 1].nb * kc;
     const int nr = g.n - g.k;
-    k_fwd_gather<<<grid_for((long long)g.nb * g.n * r), 256, 0, stream>>>(
+    k_fwd_gather<<<grid_for((long long)g.nb * g.n * r), 256, 0, cs>>>(
         g.nb, g.n, g.k, kc, leaf ? 1 : 0, r, d.J.p, d.IsrcJ.p, src, lds, d.upF.p, (long long)g.nb * g.k, d.rsF.p,
         (long long)g.nb * std::max(nr, 1));
-    fp.up[lev].run(stream);
+    fp.up[lev].run(cs);
+    HSS_CUDA(cudaEventRecord(ev_up(lev), cs));
+    HSS_CUDA(cudaStreamWaitEvent(ss, ev_up(lev), 0));
+    fp.lam[lev - 1].run(ss);  // the siblings of level lev - 1: this level's upward values
+    HSS_CUDA(cudaEventRecord(ev_lam(lev - 1), ss));
   }
-  fp.lam[0].run(stream);  // every level's lam products
   for (int lev = 1; lev <= depth; ++lev) {
     const auto& g = geo.levels[lev];
     auto& d = L[lev];
@@ -1573,11 +1591,17 @@ void HSS2D::apply_stage_body(int r) {
     double* dst = leaf ? Yd.p : L[lev + 1].dnF.p;
     const long long ldd = leaf ? N : (long long)geo.levels[lev + 1].nb * kc;
     const int nr = g.n - g.k;
-    fp.eta[lev].run(stream);
-    k_fwd_scatter<<<grid_for((long long)g.nb * g.n * r), 256, 0, stream>>>(
+    HSS_CUDA(cudaStreamWaitEvent(cs, ev_lam(lev - 1), 0));  // this level's downward input
+    fp.eta[lev].run(cs);
+    HSS_CUDA(cudaStreamWaitEvent(cs, ev_lam(lev), 0));  // the scatter adds onto lam's output
+    k_fwd_scatter<<<grid_for((long long)g.nb * g.n * r), 256, 0, cs>>>(
         g.nb, g.n, g.k, kc, leaf ? 1 : 0, r, d.J.p, d.IsrcJ.p, dst, ldd, d.dnF.p, (long long)g.nb * g.k, d.tmF.p,
         (long long)g.nb * std::max(nr, 1));
   }
+  HSS_CUDA(cudaEventRecord(S.jc, cs));
+  HSS_CUDA(cudaEventRecord(S.js, ss));
+  HSS_CUDA(cudaStreamWaitEvent(stream, S.jc, 0));
+  HSS_CUDA(cudaStreamWaitEvent(stream, S.js, 0));
   check_launch("apply");
 }
 

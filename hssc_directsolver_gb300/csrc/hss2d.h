@@ -98,6 +98,9 @@ struct Level2Dev {
 
 struct FwdPlan {
   std::vector<SolvePlan<double>> up, lam, eta;
+  // two streams: events 0..depth after each level's upward product, depth+1.. after each
+  // level's sibling (leaf: self) products
+  std::shared_ptr<PlanStreams> streams;
 };
 
 struct HSS2D {
