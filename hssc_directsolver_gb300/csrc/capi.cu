@@ -583,6 +583,24 @@ int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_ma
   HSS_CATCH
 }
 
+int hss1d_recompress(const hss1d_matrix* A, double acc, hss1d_matrix** out) {
+  HSS_TRY
+  HSS_REQUIRE(A && A->impl && out, HSS_ERR_ARG, "NULL argument");
+  require_device();
+  *out = nullptr;
+  auto* h = new hss1d_matrix{nullptr};
+  try {
+    h->impl = new HSS1D();
+    h->impl->recompress(*A->impl, acc);
+  } catch (...) {
+    delete h->impl;
+    delete h;
+    throw;
+  }
+  *out = h;
+  HSS_CATCH
+}
+
 int hss1d_compress_lr(hss1d_matrix** out, const double* U, const double* V, int64_t N, int32_t r, int64_t ldu,
                       int64_t ldv, int32_t leaf, double acc, uint64_t seed) {
   HSS_TRY

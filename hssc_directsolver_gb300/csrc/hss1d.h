@@ -157,6 +157,8 @@ struct HSS1D {
               const std::vector<int>& Tlev);
   // *this = A + B for two square handles on one forest (HSS1D_sum_nsym)
   void sum(const HSS1D& A, const HSS1D& B, double acc);
+  // *this = A with its ranks reduced to acc (HSS1D_recompress_nsym)
+  void recompress(const HSS1D& A, double acc);
   // K = the inverse in compressed format (HSS1D_transforminv_nsym)
   void transforminv(HSS1D& K);
   // K = the transpose in compressed format (HSS1D_transpose)

@@ -977,3 +977,618 @@ void HSS1D::compress_lr(long long N, int r, const double* U, long long ldu, cons
 }
 
 }  // namespace hss
+
+namespace hss {
+
+// ---------------------------------------------------------------------------
+// A_NEW = HSS1D_recompress_nsym(A, acc), HSS1D/HSS1D_recompress_nsym.m:26-247: the ranks of
+// a compressed matrix reduced to what acc needs (after sums and low-rank updates).
+//  (I) top down (:30-146), level by level over every parent: the root's sibling blocks are
+//      truncated by their SVDs (singular values above the absolute acc); every other parent
+//      stacks its sons' sibling blocks with its far-field factors, Sson = [B, L0 S0] and
+//      Tson = [B; T0 R0], and truncates their SVDs, which gives each son a reduced row basis
+//      Q^H R and column basis L P, and the parent's reduced sibling blocks;
+//  (II) bottom up (:148-246): each box IDs its reduced bases at full rank (pivoted QR of
+//      RNEW and LNEW^T, k = min(size)), keeps RHO / LAMBDA, and the sibling blocks become
+//      LAMBDA_s1 sib RHO_s2.
+// The SVDs are one-sided Jacobi on the GPU (Hestenes; the basis of a cluster of equal
+// singular values is the method's own, but every quantity the result keeps is invariant
+// under that choice: the skeleton pivots depend on the column norms of projections, T on
+// the row space, the sibling blocks on the operator).
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct SvdP {
+  double* X;  // m x n, ld m: overwritten by X V = U S (orthogonal columns)
+  double* V;  // n x n, ld n: the accumulated rotations
+  double* s;  // n: the column norms of X V (the singular values, unsorted)
+  int m, n;
+};
+
+__global__ void __launch_bounds__(256) k_jacobi_svd(const SvdP* __restrict__ P) {
+  const SvdP p = P[blockIdx.x];
+  const int m = p.m, n = p.n, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  __shared__ int s_rot;
+  for (int e = tid; e < n * n; e += 256) p.V[e] = ((e % n) == (e / n)) ? 1.0 : 0.0;
+  __syncthreads();
+  const int K2 = (n % 2 == 0) ? n : n + 1;
+  for (int sweep = 0; sweep < 60 && n > 1; ++sweep) {
+    if (tid == 0) s_rot = 0;
+    __syncthreads();
+    for (int rnd = 0; rnd < K2 - 1; ++rnd) {
+      for (int pi = w; pi < K2 / 2; pi += 8) {
+        int a, b;
+        if (pi == 0) { a = K2 - 1; b = rnd; }
+        else { a = (rnd + pi) % (K2 - 1); b = (rnd - pi + K2 - 1) % (K2 - 1); }
+        if (a >= n || b >= n) continue;
+        if (a > b) { const int t = a; a = b; b = t; }
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int i = lane; i < m; i += 32) {
+          const double u = p.X[i + (size_t)a * m], v = p.X[i + (size_t)b * m];
+          al += u * u; be += v * v; ga += u * v;
+        }
+        al = warp_sum_d(al); be = warp_sum_d(be); ga = warp_sum_d(ga);
+        double c = 1.0, s = 0.0;
+        int rot = 0;
+        if (lane == 0 && ga != 0.0 && fabs(ga) > 1e-15 * sqrt(al * be)) {
+          const double zeta = (be - al) / (2.0 * ga);
+          const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = c * t;
+          rot = 1;
+        }
+        rot = __shfl_sync(0xffffffffu, rot, 0);
+        if (rot) {
+          c = __shfl_sync(0xffffffffu, c, 0);
+          s = __shfl_sync(0xffffffffu, s, 0);
+          for (int i = lane; i < m; i += 32) {
+            const double u = p.X[i + (size_t)a * m], v = p.X[i + (size_t)b * m];
+            p.X[i + (size_t)a * m] = c * u - s * v;
+            p.X[i + (size_t)b * m] = s * u + c * v;
+          }
+          for (int i = lane; i < n; i += 32) {
+            const double u = p.V[i + (size_t)a * n], v = p.V[i + (size_t)b * n];
+            p.V[i + (size_t)a * n] = c * u - s * v;
+            p.V[i + (size_t)b * n] = s * u + c * v;
+          }
+          if (lane == 0) s_rot = 1;
+        }
+      }
+      __syncthreads();
+    }
+    const int any = s_rot;
+    __syncthreads();
+    if (!any) break;
+  }
+  for (int j = w; j < n; j += 8) {
+    double d = 0.0;
+    for (int i = lane; i < m; i += 32) { const double v = p.X[i + (size_t)j * m]; d += v * v; }
+    d = warp_sum_d(d);
+    if (lane == 0) p.s[j] = sqrt(d);
+  }
+}
+
+// dst (rows x cols, ld ldd) = src columns idx[j] (ld lds), each scaled by scale[j] (or 1)
+struct GatherP {
+  const double* src;
+  double* dst;
+  const int* idx;
+  const double* scale;
+  int rows, cols, lds, ldd;
+};
+
+__global__ void __launch_bounds__(256) k_gather_cols(const GatherP* __restrict__ P) {
+  const GatherP p = P[blockIdx.x];
+  const long long tot = (long long)p.rows * p.cols;
+  for (long long e = threadIdx.x; e < tot; e += 256) {
+    const int i = (int)(e % p.rows), j = (int)(e / p.rows);
+    const double f = p.scale ? p.scale[j] : 1.0;
+    p.dst[i + (size_t)j * p.ldd] = f * p.src[i + (size_t)p.idx[j] * p.lds];
+  }
+}
+
+static void run_gathers(const std::vector<GatherP>& G, cudaStream_t s) {
+  if (G.empty()) return;
+  DevBuf<GatherP> d;
+  upload_vec(d, G, s);
+  for (size_t o = 0; o < G.size(); o += 65535) {
+    const int c = (int)std::min<size_t>(65535, G.size() - o);
+    k_gather_cols<<<c, 256, 0, s>>>(d.p + o);
+    check_launch("k_gather_cols");
+  }
+  HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+// a rectangular diagonal matrix (rows x cols, the diagonal d of min(rows, cols) entries)
+struct RDiag {
+  int rows = 0, cols = 0;
+  std::vector<double> d;
+};
+
+void HSS1D::recompress(const HSS1D& A, double acc_) {
+  HSS_REQUIRE(!A.cplx && !A.rect, HSS_ERR_ARG, "recompress is defined for real square handles");
+  HSS_REQUIRE(acc_ > 0 && acc_ < 1, HSS_ERR_ARG, "bad recompress tolerance");
+  const cudaStream_t st = stream;
+  std::fill(phase_s, phase_s + NPHASE, 0.0);
+  Ntot = A.Ntot; nprob = A.nprob; nboxes = A.nboxes; leaf = A.leaf; maxlev = A.maxlev; acc = acc_;
+  sym = false; rect = false; id_df = false; cplx = false; kernel_op = false;
+  pN = A.pN; pbase = A.pbase; proot = A.proot; pseed = A.pseed;
+  prob = A.prob; level = A.level; parent = A.parent; c1 = A.c1; c2 = A.c2; off = A.off; cnt = A.cnt;
+  X = A.X; kp = A.kp; kdev = A.kdev;
+  precision = HSS_PREC_FP64;
+  inverted = false;
+  clear_plans();
+  for (int b = 0; b < nboxes; ++b)
+    HSS_REQUIRE(is_leaf(b) || (c1[b] >= 0 && c2[b] >= 0), HSS_ERR_ARG, "recompress: one-child boxes");
+  const int nb = nboxes;
+  // the operand's R = [I T_UP](:, J_UP) (k x n) and L^T = [I T_DN](:, J_DN) of every box
+  std::vector<DevBuf<double>> Rf(nb), Lt(nb);
+  {
+    std::vector<RformP> rf;
+    for (int b = 0; b < nb; ++b) {
+      if (parent[b] < 0) continue;
+      const int k = A.kskel[b], n = A.nskel[b];
+      Rf[b].alloc(std::max((size_t)k * n, (size_t)1));
+      Lt[b].alloc(std::max((size_t)k * n, (size_t)1));
+      Rf[b].zero(st);
+      Lt[b].zero(st);
+      if (k == 0) continue;
+      rf.push_back(RformP{A.T_UP.p + A.oT[b], A.JUPd.p + A.oJ[b], Rf[b].p, k, n, k});
+      rf.push_back(RformP{A.T_DN.p + A.oT[b], A.JDNd.p + A.oJ[b], Lt[b].p, k, n, k});
+    }
+    if (!rf.empty()) {
+      DevBuf<RformP> drf;
+      upload_vec(drf, rf, st);
+      for (size_t o = 0; o < rf.size(); o += 65535) {
+        const int c = (int)std::min<size_t>(65535, rf.size() - o);
+        k_rform<<<c, 256, 0, st>>>(drf.p + o);
+        check_launch("k_rform");
+      }
+    }
+  }
+  // (I) top down.  Per box: Rp (kn x n_b: rows of the reduced outgoing basis), Lp (n_b x kn),
+  // the diagonal factors Tp / Sp, and the reduced sibling block sib (kn_s1 x kn_s2).
+  std::vector<DevBuf<double>> Rp(nb), Lp(nb), sib(nb);
+  std::vector<int> kn(nb, 0);
+  std::vector<RDiag> Tp(nb), Sp(nb);
+  const double* Asib = A.M_SIB.p;
+  auto gemm = [](std::vector<GemmP<double>>& v, const double* a, int lda, const double* b, int ldb, double* c, int ldc,
+                 int M, int N, int K) {
+    if (M > 0 && N > 0 && K > 0) v.push_back(GemmP<double>{a, b, c, M, N, K, lda, ldb, ldc});
+  };
+  for (int L = 0; L < maxlev; ++L) {
+    std::vector<int> par;
+    for (int b = 0; b < nb; ++b)
+      if (level[b] == L && !is_leaf(b)) par.push_back(b);
+    if (par.empty()) continue;
+    const int np = (int)par.size();
+    // the SVD inputs: root [B1 | B2]; other parents T1 = [B2; T0 R0(:, :k1)], T2 = [B1; T0
+    // R0(:, k1:)], S1^T = [B1 | L0(:k1, :) S0]^T, S2^T
+    struct Job { int m, n; };
+    std::vector<std::array<Job, 4>> jobs(np);
+    std::vector<std::array<long long, 4>> oX(np), oV(np), oS(np);
+    long long tXs = 0, tVs = 0, tSs = 0;
+    for (int q = 0; q < np; ++q) {
+      const int b = par[q], s1 = c1[b], s2 = c2[b], k1 = A.kskel[s1], k2 = A.kskel[s2];
+      if (parent[b] < 0) {
+        jobs[q] = {Job{k1, k2}, Job{k2, k1}, Job{0, 0}, Job{0, 0}};
+      } else {
+        const int rT = Tp[b].rows, cS = Sp[b].cols;
+        jobs[q] = {Job{k2 + rT, k1}, Job{k1 + rT, k2}, Job{k2 + cS, k1}, Job{k1 + cS, k2}};
+      }
+      for (int j = 0; j < 4; ++j) {
+        oX[q][j] = tXs; tXs += (long long)jobs[q][j].m * jobs[q][j].n;
+        oV[q][j] = tVs; tVs += (long long)jobs[q][j].n * jobs[q][j].n;
+        oS[q][j] = tSs; tSs += jobs[q][j].n;
+      }
+    }
+    DevBuf<double> Xs(std::max(tXs, 1LL)), Vs(std::max(tVs, 1LL)), Ss(std::max(tSs, 1LL)), tmp;
+    Xs.zero(st);
+    std::vector<MoveP> mv;
+    std::vector<GemmP<double>> gNN, gTN;  // plain products; A transposed
+    // far-field parts of the stacks: T0 R0(:, cols) and L0(rows, :) S0 through diagonal factors
+    // (host-built dense diagonal matrices, small)
+    std::vector<DevBuf<double>> Dm(2 * np);
+    for (int q = 0; q < np; ++q) {
+      const int b = par[q], s1 = c1[b], s2 = c2[b], k1 = A.kskel[s1], k2 = A.kskel[s2];
+      const double* B1 = Asib + A.oSib[s1];
+      const double* B2 = Asib + A.oSib[s2];
+      if (parent[b] < 0) {
+        mv.push_back(MoveP{B1, Xs.p + oX[q][0], nullptr, k1, k2, k1, k1, 0, 0});
+        mv.push_back(MoveP{B2, Xs.p + oX[q][1], nullptr, k2, k1, k2, k2, 0, 0});
+        continue;
+      }
+      const RDiag &T0 = Tp[b], &S0 = Sp[b];
+      std::vector<double> hT((size_t)T0.rows * T0.cols, 0.0), hS((size_t)S0.rows * S0.cols, 0.0);
+      for (size_t i = 0; i < T0.d.size(); ++i) hT[i + i * T0.rows] = T0.d[i];
+      for (size_t i = 0; i < S0.d.size(); ++i) hS[i + i * S0.rows] = S0.d[i];
+      upload_vec(Dm[2 * q], hT, st);
+      upload_vec(Dm[2 * q + 1], hS, st);
+      const int kb = kn[b];  // = T0.cols = S0.rows = rows of R0 = cols of L0
+      const double* R0 = Rp[b].p;  // kb x (k1 + k2)
+      const double* L0 = Lp[b].p;  // (k1 + k2) x kb
+      const int rT = T0.rows, cS = S0.cols;
+      // job 0: T1 = [B2; T0 R0(:, :k1)]  ((k2 + rT) x k1)
+      mv.push_back(MoveP{B2, Xs.p + oX[q][0], nullptr, k2, k1, k2, k2 + rT, 0, 0});
+      gemm(gNN, Dm[2 * q].p, rT, R0, kb, Xs.p + oX[q][0] + k2, k2 + rT, rT, k1, kb);
+      // job 1: T2 = [B1; T0 R0(:, k1:)]  ((k1 + rT) x k2)
+      mv.push_back(MoveP{B1, Xs.p + oX[q][1], nullptr, k1, k2, k1, k1 + rT, 0, 0});
+      gemm(gNN, Dm[2 * q].p, rT, R0 + (size_t)k1 * kb, kb, Xs.p + oX[q][1] + k1, k1 + rT, rT, k2, kb);
+      // job 2: S1^T = [B1 | L0(:k1, :) S0]^T = [B1^T; S0^T L0(:k1, :)^T]  ((k2 + cS) x k1)
+      mv.push_back(MoveP{B1, Xs.p + oX[q][2], nullptr, k1, k2, k1, k2 + cS, 3, 0});
+      // (S0^T L0(:k1,:)^T) = (L0(:k1,:) S0)^T: C (cS x k1) = S0^T (cS x kb) * L0(:k1,:)^T
+      gemm(gTN, Dm[2 * q + 1].p, kb, L0, k1 + k2, Xs.p + oX[q][2] + k2, k2 + cS, cS, k1, kb);
+      // job 3: S2^T = [B2^T; S0^T L0(k1:, :)^T]  ((k1 + cS) x k2)
+      mv.push_back(MoveP{B2, Xs.p + oX[q][3], nullptr, k2, k1, k2, k1 + cS, 3, 0});
+      gemm(gTN, Dm[2 * q + 1].p, kb, L0 + k1, k1 + k2, Xs.p + oX[q][3] + k1, k1 + cS, cS, k2, kb);
+    }
+    run_moves(mv, st);
+    // the L0 rows are read transposed: C = S0^T * L0(rows, :)^T needs B transposed too
+    if (!gNN.empty()) run_gemms(gNN, false, false, 1.0, 0.0, st);
+    if (!gTN.empty()) run_gemms(gTN, true, true, 1.0, 0.0, st);
+    std::vector<SvdP> sp;
+    for (int q = 0; q < np; ++q)
+      for (int j = 0; j < 4; ++j)
+        if (jobs[q][j].m > 0 && jobs[q][j].n > 0)
+          sp.push_back(SvdP{Xs.p + oX[q][j], Vs.p + oV[q][j], Ss.p + oS[q][j], jobs[q][j].m, jobs[q][j].n});
+    {
+      DevBuf<SvdP> dsp;
+      upload_vec(dsp, sp, st);
+      for (size_t o = 0; o < sp.size(); o += 65535) {
+        const int c = (int)std::min<size_t>(65535, sp.size() - o);
+        k_jacobi_svd<<<c, 256, 0, st>>>(dsp.p + o);
+        check_launch("k_jacobi_svd");
+      }
+    }
+    std::vector<double> hs;
+    download(hs, Ss.p, std::max(tSs, 1LL), st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    // sorted singular values per job, the truncation ranks, and the gathered factors
+    std::vector<std::array<std::vector<int>, 4>> ord(np);
+    std::vector<std::array<std::vector<double>, 4>> sv(np);
+    std::vector<int> hidx;
+    std::vector<double> hscale;
+    std::vector<std::array<long long, 4>> oI(np);
+    for (int q = 0; q < np; ++q)
+      for (int j = 0; j < 4; ++j) {
+        const int n = jobs[q][j].n;
+        std::vector<int> o(n);
+        std::iota(o.begin(), o.end(), 0);
+        const double* s = hs.data() + oS[q][j];
+        std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return s[a] > s[b]; });
+        // a thin SVD keeps min(m, n) values
+        const int r = std::min(jobs[q][j].m, n);
+        ord[q][j] = o;
+        sv[q][j].resize(r);
+        for (int t = 0; t < r; ++t) sv[q][j][t] = s[o[t]];
+        oI[q][j] = (long long)hidx.size();
+        for (int t = 0; t < n; ++t) {
+          hidx.push_back(o[t]);
+          hscale.push_back((t < r && s[o[t]] > 0.0) ? 1.0 / s[o[t]] : 0.0);
+        }
+      }
+    DevBuf<int> didx;
+    DevBuf<double> dscale;
+    upload_vec(didx, hidx, st);
+    upload_vec(dscale, hscale, st);
+    auto count = [&](const std::vector<double>& v) {
+      int c = 0;
+      for (double x : v) c += (x > acc) ? 1 : 0;
+      return c;
+    };
+    // per parent: P1 (k1 x k1n), P2, Q1 (k1 x k1n), Q2 (k2 x k2n), Y1 (rows of T1 x k1n), Y2
+    std::vector<std::array<DevBuf<double>, 6>> F(np);
+    std::vector<GatherP> gat;
+    for (int q = 0; q < np; ++q) {
+      const int b = par[q], s1 = c1[b], s2 = c2[b], k1 = A.kskel[s1], k2 = A.kskel[s2];
+      int k1n, k2n;
+      if (parent[b] < 0) {
+        k1n = count(sv[q][0]);  // B1 = P1 D1 Q2^H
+        k2n = count(sv[q][1]);  // B2 = P2 D2 Q1^H
+        // P1: the normalised columns of X1 V; Q2: V of job 0; P2, Q1 from job 1
+        F[q][0].alloc(std::max(1, k1 * k1n));  // P1
+        F[q][1].alloc(std::max(1, k2 * k2n));  // P2
+        F[q][2].alloc(std::max(1, k1 * k1n));  // Q1
+        F[q][3].alloc(std::max(1, k2 * k2n));  // Q2
+        gat.push_back(GatherP{Xs.p + oX[q][0], F[q][0].p, didx.p + oI[q][0], dscale.p + oI[q][0], k1, k1n, k1, k1});
+        gat.push_back(GatherP{Xs.p + oX[q][1], F[q][1].p, didx.p + oI[q][1], dscale.p + oI[q][1], k2, k2n, k2, k2});
+        gat.push_back(GatherP{Vs.p + oV[q][1], F[q][2].p, didx.p + oI[q][1], nullptr, k1, k1n, k1, k1});
+        gat.push_back(GatherP{Vs.p + oV[q][0], F[q][3].p, didx.p + oI[q][0], nullptr, k2, k2n, k2, k2});
+        // sib{s1} = D1m (k1n x k2n), sib{s2} = D2m; Tp{s1} = D2m, Tp{s2} = D1m; Sp{s1} = D1m,
+        // Sp{s2} = D2m (:52-60)
+        RDiag D1m, D2m;
+        D1m.rows = k1n; D1m.cols = k2n;
+        D2m.rows = k2n; D2m.cols = k1n;
+        for (int t = 0; t < std::min(k1n, k2n); ++t) { D1m.d.push_back(sv[q][0][t]); D2m.d.push_back(sv[q][1][t]); }
+        Tp[s1] = D2m; Tp[s2] = D1m; Sp[s1] = D1m; Sp[s2] = D2m;
+        for (int s : {s1, s2}) {
+          const RDiag& D = (s == s1) ? D1m : D2m;
+          std::vector<double> h((size_t)D.rows * D.cols, 0.0);
+          for (size_t i = 0; i < D.d.size(); ++i) h[i + i * D.rows] = D.d[i];
+          upload_vec(sib[s], h, st);
+          if (h.empty()) sib[s].alloc(1);
+        }
+      } else {
+        const int rT = Tp[b].rows;
+        const int kt1 = count(sv[q][0]), kt2 = count(sv[q][1]), ks1 = count(sv[q][2]), ks2 = count(sv[q][3]);
+        k1n = std::max(kt1, ks1);
+        k2n = std::max(kt2, ks2);
+        HSS_REQUIRE(k1n <= (int)sv[q][0].size() && k1n <= (int)sv[q][2].size() && k2n <= (int)sv[q][1].size() &&
+                        k2n <= (int)sv[q][3].size(),
+                    HSS_ERR_RANK, "recompress: truncation rank above the block size");
+        F[q][0].alloc(std::max(1, k1 * k1n));          // P1: V of job 2
+        F[q][1].alloc(std::max(1, k2 * k2n));          // P2: V of job 3
+        F[q][2].alloc(std::max(1, k1 * k1n));          // Q1: V of job 0
+        F[q][3].alloc(std::max(1, k2 * k2n));          // Q2: V of job 1
+        F[q][4].alloc(std::max(1, (k2 + rT) * k1n));   // Y1 (normalised)
+        F[q][5].alloc(std::max(1, (k1 + rT) * k2n));   // Y2
+        gat.push_back(GatherP{Vs.p + oV[q][2], F[q][0].p, didx.p + oI[q][2], nullptr, k1, k1n, k1, k1});
+        gat.push_back(GatherP{Vs.p + oV[q][3], F[q][1].p, didx.p + oI[q][3], nullptr, k2, k2n, k2, k2});
+        gat.push_back(GatherP{Vs.p + oV[q][0], F[q][2].p, didx.p + oI[q][0], nullptr, k1, k1n, k1, k1});
+        gat.push_back(GatherP{Vs.p + oV[q][1], F[q][3].p, didx.p + oI[q][1], nullptr, k2, k2n, k2, k2});
+        gat.push_back(GatherP{Xs.p + oX[q][0], F[q][4].p, didx.p + oI[q][0], dscale.p + oI[q][0], k2 + rT, k1n, k2 + rT,
+                              k2 + rT});
+        gat.push_back(GatherP{Xs.p + oX[q][1], F[q][5].p, didx.p + oI[q][1], dscale.p + oI[q][1], k1 + rT, k2n, k1 + rT,
+                              k1 + rT});
+        RDiag DT1, DT2, DS1, DS2;
+        DT1.rows = DT1.cols = k1n; DS1.rows = DS1.cols = k1n;
+        DT2.rows = DT2.cols = k2n; DS2.rows = DS2.cols = k2n;
+        DT1.d.assign(sv[q][0].begin(), sv[q][0].begin() + k1n);
+        DT2.d.assign(sv[q][1].begin(), sv[q][1].begin() + k2n);
+        DS1.d.assign(sv[q][2].begin(), sv[q][2].begin() + k1n);
+        DS2.d.assign(sv[q][3].begin(), sv[q][3].begin() + k2n);
+        Tp[s1] = DT1; Tp[s2] = DT2; Sp[s1] = DS1; Sp[s2] = DS2;
+      }
+      kn[s1] = k1n;
+      kn[s2] = k2n;
+    }
+    run_gathers(gat, st);
+    // sib, Rp / Lp of the parent (non-root) and of the sons
+    std::vector<GemmP<double>> g1, g2, g3, g4;  // NN, TN (A^T B), NT (A B^T), TT
+    std::vector<DevBuf<double>> W(np);
+    for (int q = 0; q < np; ++q) {
+      const int b = par[q], s1 = c1[b], s2 = c2[b], k1 = A.kskel[s1], k2 = A.kskel[s2];
+      const int k1n = kn[s1], k2n = kn[s2];
+      const double *P1 = F[q][0].p, *P2 = F[q][1].p, *Q1 = F[q][2].p, *Q2 = F[q][3].p;
+      if (parent[b] >= 0) {
+        const int rT = Tp[b].rows, kb = kn[b];
+        // sib{s1} = P1^H Y2(:k1, :) DT2 ; sib{s2} = P2^H Y1(:k2, :) DT1 (Y already divided by
+        // the singular values, so Y DT = the unnormalised columns of T V)
+        sib[s1].alloc(std::max(1, k1n * k2n));
+        sib[s2].alloc(std::max(1, k2n * k1n));
+        W[q].alloc(std::max<size_t>(1, (size_t)(k1 + rT) * k2n + (size_t)(k2 + rT) * k1n));
+        double* U2 = W[q].p;                              // (k1 + rT) x k2n: T2 V(:, ord)
+        double* U1 = W[q].p + (size_t)(k1 + rT) * k2n;    // (k2 + rT) x k1n
+        // Y DT: gather the unscaled columns
+        std::vector<GatherP> gg;
+        gg.push_back(GatherP{Xs.p + oX[q][1], U2, didx.p + oI[q][1], nullptr, k1 + rT, k2n, k1 + rT, k1 + rT});
+        gg.push_back(GatherP{Xs.p + oX[q][0], U1, didx.p + oI[q][0], nullptr, k2 + rT, k1n, k2 + rT, k2 + rT});
+        run_gathers(gg, st);
+        gemm(g2, P1, k1, U2, k1 + rT, sib[s1].p, std::max(k1n, 1), k1n, k2n, k1);
+        gemm(g2, P2, k2, U1, k2 + rT, sib[s2].p, std::max(k2n, 1), k2n, k1n, k2);
+        // Rp{b} = [R0(:, :k1) Q1, R0(:, k1:) Q2]  (kb x (k1n + k2n)); Lp{b} = [P1^H L0(:k1, :);
+        // P2^H L0(k1:, :)]  ((k1n + k2n) x kb)
+        DevBuf<double> Rn(std::max(1, kb * (k1n + k2n))), Ln(std::max(1, (k1n + k2n) * kb));
+        gemm(g1, Rp[b].p, kb, Q1, k1, Rn.p, kb, kb, k1n, k1);
+        gemm(g1, Rp[b].p + (size_t)k1 * kb, kb, Q2, k2, Rn.p + (size_t)k1n * kb, kb, kb, k2n, k2);
+        gemm(g2, P1, k1, Lp[b].p, k1 + k2, Ln.p, k1n + k2n, k1n, kb, k1);
+        gemm(g2, P2, k2, Lp[b].p + k1, k1 + k2, Ln.p + k1n, k1n + k2n, k2n, kb, k2);
+        // run now: Rp{b} / Lp{b} are replaced below
+        run_gemms(g1, false, false, 1.0, 0.0, st);
+        run_gemms(g2, true, false, 1.0, 0.0, st);
+        g1.clear();
+        g2.clear();
+        Rp[b] = std::move(Rn);
+        Lp[b] = std::move(Ln);
+      }
+      // sons: Rp{s} = Q^H R_s (kn_s x n_s), Lp{s} = L_s P (n_s x kn_s) = (L_s^T)^T P
+      for (int side = 0; side < 2; ++side) {
+        const int s = side ? s2 : s1, ks = A.kskel[s], ns = A.nskel[s], kns = kn[s];
+        const double* Q = side ? Q2 : Q1;
+        const double* Pm = side ? P2 : P1;
+        Rp[s].alloc(std::max(1, kns * ns));
+        Lp[s].alloc(std::max(1, ns * kns));
+        gemm(g2, Q, ks, Rf[s].p, ks, Rp[s].p, std::max(kns, 1), kns, ns, ks);
+        gemm(g2, Lt[s].p, ks, Pm, ks, Lp[s].p, ns, ns, kns, ks);
+      }
+    }
+    run_gemms(g2, true, false, 1.0, 0.0, st);
+  }
+  // (II) bottom up
+  nskel.assign(nb, 0); kskel.assign(nb, 0);
+  I_SKUP.assign(nb, {}); I_SKDN.assign(nb, {});
+  J_UP.assign(nb, {}); J_DN.assign(nb, {});
+  census.assign(4 * (size_t)nb, 0);
+  feat.assign((size_t)NFEAT * nb, 0.f);
+  qr_steps = qr_steps_full = 0;
+  reruns = 0;
+  std::vector<DevBuf<double>> rho(nb), lam(nb);  // rho: kn x k, lam: k x kn
+  std::vector<DevBuf<double>> Tkeep;
+  std::vector<std::array<long long, 2>> Toff(nb);
+  std::vector<int> Tlev(nb, -1);
+  // new sibling blocks: offsets over the final ranks, filled level by level
+  std::vector<DevBuf<double>> msib(nb);
+  for (int L = maxlev; L >= 0; --L) {
+    std::vector<int> boxes;
+    for (int b = 0; b < nb; ++b)
+      if (level[b] == L) boxes.push_back(b);
+    if (boxes.empty()) continue;
+    // sibling blocks of this level's parents (their sons are final) and RNEW / LNEW^T
+    std::vector<GemmP<double>> g1, g2;
+    std::vector<DevBuf<double>> tmp(2 * boxes.size());
+    for (size_t q = 0; q < boxes.size(); ++q) {
+      const int b = boxes[q];
+      if (is_leaf(b)) continue;
+      const int s1 = c1[b], s2 = c2[b];
+      for (int side = 0; side < 2; ++side) {
+        const int sa = side ? s2 : s1, sb = side ? s1 : s2;
+        const int ka = kskel[sa], kb2 = kskel[sb], kna = kn[sa], knb = kn[sb];
+        tmp[2 * q + side].alloc(std::max(1, ka * knb));
+        msib[sa].alloc(std::max(1, ka * kb2));
+        // lam{sa} sib{sa} (ka x knb), then times rho{sb} (knb x kb2)
+        gemm(g1, lam[sa].p, std::max(ka, 1), sib[sa].p, std::max(kna, 1), tmp[2 * q + side].p, std::max(ka, 1), ka,
+             knb, kna);
+      }
+    }
+    run_gemms(g1, false, false, 1.0, 0.0, st);
+    g1.clear();
+    for (size_t q = 0; q < boxes.size(); ++q) {
+      const int b = boxes[q];
+      if (is_leaf(b)) continue;
+      const int s1 = c1[b], s2 = c2[b];
+      for (int side = 0; side < 2; ++side) {
+        const int sa = side ? s2 : s1, sb = side ? s1 : s2;
+        const int ka = kskel[sa], kb2 = kskel[sb], knb = kn[sb];
+        gemm(g1, tmp[2 * q + side].p, std::max(ka, 1), rho[sb].p, std::max(knb, 1), msib[sa].p, std::max(ka, 1), ka,
+             kb2, knb);
+      }
+    }
+    run_gemms(g1, false, false, 1.0, 0.0, st);
+    g1.clear();
+    if (L == 0) break;
+    // RNEW (kn x n) and LNEW^T (kn x n) of every box of the level
+    const int nbL = (int)boxes.size();
+    std::vector<int> m(nbL), n(nbL);
+    std::vector<long long> oZ(2 * nbL);
+    long long tZ = 0;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q];
+      m[q] = kn[b];
+      n[q] = is_leaf(b) ? cnt[b] : kskel[c1[b]] + kskel[c2[b]];
+      HSS_REQUIRE(m[q] >= 1 && n[q] >= 1 && n[q] <= 4096, HSS_ERR_RANK, "recompress: empty or oversized basis");
+      oZ[2 * q] = tZ; tZ += (long long)m[q] * n[q];
+      oZ[2 * q + 1] = tZ; tZ += (long long)m[q] * n[q];
+    }
+    DevBuf<double> Z(std::max(tZ, 1LL));
+    Z.zero(st);
+    std::vector<MoveP> mv;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], kb = m[q];
+      double* RN = Z.p + oZ[2 * q];
+      double* LNt = Z.p + oZ[2 * q + 1];
+      if (is_leaf(b)) {
+        mv.push_back(MoveP{Rp[b].p, RN, nullptr, kb, n[q], kb, kb, 0, 0});
+        mv.push_back(MoveP{Lp[b].p, LNt, nullptr, n[q], kb, n[q], kb, 3, 0});  // (n x kb)^T
+        continue;
+      }
+      const int s1 = c1[b], s2 = c2[b], ka1 = kn[s1], ka2 = kn[s2];
+      // RNEW = [RA(:, :ka1) rho{s1}, RA(:, ka1:) rho{s2}]
+      gemm(g1, Rp[b].p, kb, rho[s1].p, std::max(ka1, 1), RN, kb, kb, kskel[s1], ka1);
+      gemm(g1, Rp[b].p + (size_t)ka1 * kb, kb, rho[s2].p, std::max(ka2, 1), RN + (size_t)kskel[s1] * kb, kb, kb,
+           kskel[s2], ka2);
+      // LNEW^T = [LA(:ka1, :)^T lam{s1}^T, LA(ka1:, :)^T lam{s2}^T]: C = A^T B^T
+      gemm(g2, Lp[b].p, ka1 + ka2, lam[s1].p, std::max(kskel[s1], 1), LNt, kb, kb, kskel[s1], ka1);
+      gemm(g2, Lp[b].p + ka1, ka1 + ka2, lam[s2].p, std::max(kskel[s2], 1), LNt + (size_t)kskel[s1] * kb, kb, kb,
+           kskel[s2], ka2);
+    }
+    run_moves(mv, st);
+    run_gemms(g1, false, false, 1.0, 0.0, st);
+    run_gemms(g2, true, true, 1.0, 0.0, st);
+    // full pivoted QR of both, fixed-rank ID at k = min(kn, n)
+    const int nprob2 = 2 * nbL;
+    std::vector<long long> oT2(nprob2), oXw(nprob2), oYw(nprob2), oP(nprob2);
+    long long tT = 0, tX = 0, tYw = 0, tP = 0;
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int q = pr / 2;
+      oT2[pr] = tT; tT += (long long)n[q] * n[q];
+      oXw[pr] = tX; tX += 2LL * n[q];
+      oYw[pr] = tYw; tYw += (long long)m[q] + n[q];
+      oP[pr] = tP; tP += n[q];
+    }
+    DevBuf<double> Wq(std::max(tZ, 1LL)), SW(tT), SV(tT), xw(tX), yw(tYw);
+    Tkeep.emplace_back(tT);
+    DevBuf<double>& Tb = Tkeep.back();
+    DevBuf<int> perm(tP), rank(nprob2);
+    std::vector<IdP> ip(nprob2);
+    for (int pr = 0; pr < nprob2; ++pr) {
+      const int q = pr / 2, b = boxes[q];
+      ip[pr] = IdP{Z.p + oZ[pr], Wq.p + oZ[pr], m[q], n[q], perm.p + oP[pr], rank.p + pr, Tb.p + oT2[pr], -1,
+                   SW.p + oT2[pr], SV.p + oT2[pr], xw.p + oXw[pr], yw.p + oYw[pr], 2 * (b - proot[prob[b]]) + pr % 2,
+                   ID_QR_ONLY, pseed[prob[b]], nullptr};
+    }
+    DevBuf<IdP> dip;
+    upload_vec(dip, ip, st);
+    id_adaptive_batched(dip.p, nprob2, acc, st, false);
+    for (int pr = 0; pr < nprob2; ++pr) ip[pr].force_k = std::min(m[pr / 2], n[pr / 2]);
+    HSS_CUDA(cudaMemcpyAsync(dip.p, ip.data(), nprob2 * sizeof(IdP), cudaMemcpyHostToDevice, st));
+    id_fixed_batched(dip.p, nprob2, st);
+    std::vector<int> hp;
+    download(hp, perm.p, tP, st);
+    HSS_CUDA(cudaStreamSynchronize(st));
+    std::vector<MoveP> mk;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], k = std::min(m[q], n[q]), nn = n[q];
+      rho[b].alloc(std::max(1, m[q] * k));
+      lam[b].alloc(std::max(1, k * m[q]));
+      // rho = RNEW(:, Jout(1:k)) (kn x k); lam = LNEW(Jin(1:k), :) = (LNEW^T(:, Jin(1:k)))^T
+      mk.push_back(MoveP{Z.p + oZ[2 * q], rho[b].p, perm.p + oP[2 * q], m[q], k, m[q], m[q], 1, 0});
+      std::vector<int> outs, inns;
+      if (is_leaf(b)) {
+        outs.resize(cnt[b]);
+        std::iota(outs.begin(), outs.end(), off[b]);
+        inns = outs;
+      } else {
+        outs = I_SKUP[c1[b]];
+        outs.insert(outs.end(), I_SKUP[c2[b]].begin(), I_SKUP[c2[b]].end());
+        inns = I_SKDN[c1[b]];
+        inns.insert(inns.end(), I_SKDN[c2[b]].begin(), I_SKDN[c2[b]].end());
+      }
+      nskel[b] = nn;
+      kskel[b] = k;
+      J_UP[b].assign(hp.begin() + oP[2 * q], hp.begin() + oP[2 * q] + nn);
+      J_DN[b].assign(hp.begin() + oP[2 * q + 1], hp.begin() + oP[2 * q + 1] + nn);
+      I_SKUP[b].resize(k);
+      I_SKDN[b].resize(k);
+      for (int t = 0; t < k; ++t) {
+        I_SKUP[b][t] = outs[J_UP[b][t]];
+        I_SKDN[b][t] = inns[J_DN[b][t]];
+      }
+      Toff[b] = {oT2[2 * q], oT2[2 * q + 1]};
+      Tlev[b] = (int)Tkeep.size() - 1;
+      census[4 * b] = m[q]; census[4 * b + 1] = m[q]; census[4 * b + 2] = nn; census[4 * b + 3] = k;
+    }
+    run_moves(mk, st);
+    // lam (k x kn) = transpose of the gathered columns of LNEW^T
+    std::vector<DevBuf<double>> lt(nbL);
+    std::vector<MoveP> mg, mt;
+    for (int q = 0; q < nbL; ++q) {
+      const int b = boxes[q], k = kskel[b];
+      lt[q].alloc(std::max(1, m[q] * k));
+      mg.push_back(MoveP{Z.p + oZ[2 * q + 1], lt[q].p, perm.p + oP[2 * q + 1], m[q], k, m[q], m[q], 1, 0});
+      mt.push_back(MoveP{lt[q].p, lam[b].p, nullptr, m[q], k, m[q], std::max(k, 1), 3, 0});
+    }
+    run_moves(mg, st);
+    run_moves(mt, st);
+  }
+  pack_T(Tkeep, Toff, Tlev);
+  // M_SELF (the operand's) and the new sibling blocks
+  oSelf = A.oSelf;
+  M_SELF.alloc(std::max<size_t>(A.M_SELF.n, 1));
+  if (A.M_SELF.n) HSS_CUDA(cudaMemcpyAsync(M_SELF.p, A.M_SELF.p, A.M_SELF.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  oSib.assign(nb, -1);
+  long long tb = 0;
+  for (int b = 0; b < nb; ++b)
+    if (!is_leaf(b)) {
+      oSib[c1[b]] = tb; tb += (long long)kskel[c1[b]] * kskel[c2[b]];
+      oSib[c2[b]] = tb; tb += (long long)kskel[c2[b]] * kskel[c1[b]];
+    }
+  M_SIB.alloc(std::max(tb, 1LL));
+  std::vector<MoveP> mv;
+  for (int b = 0; b < nb; ++b)
+    if (!is_leaf(b))
+      for (int s : {c1[b], c2[b]}) {
+        const int o = (s == c1[b]) ? c2[b] : c1[b];
+        if (kskel[s] > 0 && kskel[o] > 0)
+          mv.push_back(MoveP{msib[s].p, M_SIB.p + oSib[s], nullptr, kskel[s], kskel[o], kskel[s], kskel[s], 0, 0});
+      }
+  run_moves(mv, st);
+  HSS_CUDA(cudaStreamSynchronize(st));
+  inverted = false;
+  clear_plans();
+}
+
+}  // namespace hss

@@ -298,6 +298,17 @@ def HSS1D_sum_nsym(A_HSS: HSS1DMatrix, B_HSS: HSS1DMatrix, acc: float) -> HSS1DM
     return K
 
 
+def HSS1D_recompress_nsym(A_HSS: HSS1DMatrix, acc: float) -> HSS1DMatrix:
+    """A_NEW = HSS1D_recompress_nsym(A, acc) (HSS1D/HSS1D_recompress_nsym.m:1): A with its
+    ranks reduced to what acc needs, as a new (not inverted) compressed matrix."""
+    h = C.c_void_p()
+    L.check(L.lib().hss1d_recompress(A_HSS._h, float(acc), C.byref(h)))
+    K = HSS1DMatrix(h, A_HSS.N)
+    if hasattr(A_HSS, "sizes"):
+        K.sizes = A_HSS.sizes
+    return K
+
+
 def HSS1D_compressLR_nsym(U, V, TREE: int, acc: float, seed: int = 0) -> HSS1DMatrix:
     """K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc) (HSS1D/HSS1D_compressLR_nsym.m:1): the
     N x N matrix U V^T in compressed form on the halving tree of leaf size TREE."""

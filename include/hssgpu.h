@@ -201,6 +201,12 @@ int hss1d_rect_info(const hss1d_matrix* H, int64_t* M, int32_t* off_in, int32_t*
  * The result is an ordinary handle (invert, apply, solve ...); fsym operands are accepted
  * and give an nsym result. */
 int hss1d_sum(const hss1d_matrix* A, const hss1d_matrix* B, double acc, hss1d_matrix** C);
+/* A_NEW = HSS1D_recompress_nsym(A, acc) (HSS1D/HSS1D_recompress_nsym.m:1): a new handle
+ *   holding A with its ranks reduced to what acc needs (after sums and low-rank updates):
+ *   top down, SVD truncation (absolute acc) of the sons' sibling blocks stacked with their
+ *   parent's far-field factors (:30-146, one-sided Jacobi SVDs on the GPU); bottom up, the
+ *   full-rank ID of each box's reduced bases (:148-246).  Real square handles; not inverted. */
+int hss1d_recompress(const hss1d_matrix* A, double acc, hss1d_matrix** out);
 /* K_HSS = HSS1D_compressLR_nsym(U, V, TREE, acc), HSS1D/HSS1D_compressLR_nsym.m:1: the N x N
  * matrix U V^T (U, V: N x r column-major, ld ldu / ldv) on the halving tree with leaf size
  * `leaf`; every box IDs V(out,:).' and U(in,:).' at tolerance acc (seed keys the rank check).

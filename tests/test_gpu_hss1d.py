@@ -600,3 +600,39 @@ def test_fsym_sum_and_low_rank_forms(gpu):
     assert rr < 1e-10
     xd = np.linalg.solve(Sd, f)
     assert np.linalg.norm(x - xd) <= 1e-7 * np.linalg.norm(xd)
+
+
+@pytest.mark.parametrize("acc", [1e-6, 1e-9])
+def test_recompress_matches_oracle(gpu, acc):
+    """HSS1D_recompress_nsym (HSS1D/HSS1D_recompress_nsym.m:26-247) on the GPU: a star-curve
+    compression at 1e-12 recompressed at acc.  The SVD truncation ranks, the full-rank IDs'
+    skeletons and the operator equal the oracle's restatement on the same (exported-equal)
+    operand; the ranks drop and the operator stays within ~acc of the original."""
+    from hssc_directsolver_gb300 import hss1d as G1, kernels as GK
+    X = geometry.star_curve(1024)
+    kp = OK.KernelParams(flag=OK.DL_L_2D)
+    A = G1.HSS1D_compress_nsym("green", X, 64, 1e-12, GK.Kernel("DL_L_2D"))
+    Ao = O1.compress_nsym(X, 64, 1e-12, kp)
+    inf = A.info()
+    assert np.array_equal(inf["kskel"][1:], np.array(Ao.kskel[1:]))
+    R = G1.HSS1D_recompress_nsym(A, acc)
+    Ro = O1.recompress_nsym(Ao, acc)
+    ri = R.info()
+    print(f"recompress {acc:g}: ranks {list(inf['kskel'][1:5])} -> {list(ri['kskel'][1:5])} "
+          f"(oracle {Ro.kskel[1:5]})")
+    assert np.array_equal(ri["kskel"][1:], np.array(Ro.kskel[1:]))
+    assert max(ri["kskel"][1:]) < max(inf["kskel"][1:])
+    nb = ri["nboxes"]
+    same = 0
+    for b in range(1, nb):
+        e = R.export_box(b)
+        same += int(np.array_equal(e["I_SKUP"], Ro.I_SKUP[b]) and np.array_equal(e["I_SKDN"], Ro.I_SKDN[b]))
+    q = np.random.default_rng(11).standard_normal((1024, 3))
+    u, uo, ua = G1.HSS1D_apply_nsym(R, q), O1.apply_nsym(Ro, q), G1.HSS1D_apply_nsym(A, q)
+    d_or, d_a = np.linalg.norm(u - uo) / np.linalg.norm(uo), np.linalg.norm(u - ua) / np.linalg.norm(ua)
+    print(f"  skeletons equal in {same}/{nb - 1} boxes; apply vs oracle {d_or:.2e}, vs the operand {d_a:.2e}")
+    assert same >= nb - 1 - 2
+    assert d_or <= 1e-8 and d_a <= 50 * acc
+    G1.HSS1D_invert_nsym(R)
+    x = G1.HSS1D_applyinv_nsym(R, None, None, u)
+    assert np.linalg.norm(x - q) <= 1e-8 * np.linalg.norm(q)
