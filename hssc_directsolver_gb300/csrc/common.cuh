@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <map>
+#include <memory>
 #include <atomic>
 #include <mutex>
 #include <exception>
@@ -165,6 +166,45 @@ inline void download(std::vector<T>& h, const T* d, size_t cnt, cudaStream_t s) 
 
 // Instantiated CUDA graphs of fixed launch sequences, keyed by the number of
 // right-hand sides.
+// The two streams of a plan whose steps run concurrently: the critical chain on a
+// high-priority stream, the steps off it on a low-priority one; one event per step.
+struct PlanStreams {
+  cudaStream_t crit = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, jc = nullptr, js = nullptr;
+  std::vector<cudaEvent_t> ev;
+  explicit PlanStreams(size_t nsteps) {
+    int least = 0, greatest = 0;
+    HSS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    HSS_CUDA(cudaStreamCreateWithPriority(&crit, cudaStreamNonBlocking, greatest));
+    HSS_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, least));
+    for (cudaEvent_t* e : {&fork, &jc, &js}) HSS_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    ev.assign(nsteps, nullptr);
+    for (auto& e : ev) HSS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  ~PlanStreams() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {fork, jc, js})
+      if (e) cudaEventDestroy(e);
+    if (crit) cudaStreamDestroy(crit);
+    if (side) cudaStreamDestroy(side);
+  }
+  PlanStreams(const PlanStreams&) = delete;
+  PlanStreams& operator=(const PlanStreams&) = delete;
+  // fork both streams from s / join both back into s
+  void fork_from(cudaStream_t s) {
+    HSS_CUDA(cudaEventRecord(fork, s));
+    HSS_CUDA(cudaStreamWaitEvent(crit, fork, 0));
+    HSS_CUDA(cudaStreamWaitEvent(side, fork, 0));
+  }
+  void join_into(cudaStream_t s) {
+    HSS_CUDA(cudaEventRecord(jc, crit));
+    HSS_CUDA(cudaEventRecord(js, side));
+    HSS_CUDA(cudaStreamWaitEvent(s, jc, 0));
+    HSS_CUDA(cudaStreamWaitEvent(s, js, 0));
+  }
+};
+
 struct GraphCache {
   std::map<int, cudaGraphExec_t> g;
   GraphCache() = default;

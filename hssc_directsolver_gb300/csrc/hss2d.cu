@@ -333,25 +333,6 @@ void SolvePlan<R>::run_step(const Step& st, cudaStream_t s) const {
   gemm_skinny_split<R>(st.d.p, st.batch, st.maxM, st.maxN, st.alpha, st.beta, st.ksplit, st.part.p, s);
 }
 
-PlanStreams::PlanStreams(size_t nsteps) {
-  int least = 0, greatest = 0;
-  HSS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-  HSS_CUDA(cudaStreamCreateWithPriority(&crit, cudaStreamNonBlocking, greatest));
-  HSS_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, least));
-  for (cudaEvent_t* e : {&fork, &jc, &js}) HSS_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-  ev.assign(nsteps, nullptr);
-  for (auto& e : ev) HSS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-}
-
-PlanStreams::~PlanStreams() {
-  for (auto e : ev)
-    if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e : {fork, jc, js})
-    if (e) cudaEventDestroy(e);
-  if (crit) cudaStreamDestroy(crit);
-  if (side) cudaStreamDestroy(side);
-}
-
 template <typename R>
 void SolvePlan<R>::run(cudaStream_t s) const {
   if (!streams) {

@@ -13,18 +13,6 @@
 
 namespace hss {
 
-// The two streams of a plan whose steps run concurrently: the critical chain on a
-// high-priority stream, the steps off it on a low-priority one; one event per step.
-struct PlanStreams {
-  cudaStream_t crit = nullptr, side = nullptr;
-  cudaEvent_t fork = nullptr, jc = nullptr, js = nullptr;
-  std::vector<cudaEvent_t> ev;
-  explicit PlanStreams(size_t nsteps);
-  ~PlanStreams();
-  PlanStreams(const PlanStreams&) = delete;
-  PlanStreams& operator=(const PlanStreams&) = delete;
-};
-
 // A fixed sequence of batched skinny products (one inverse or forward apply
 // pass for a given number of right-hand sides); descriptors stay on the device.
 template <typename R>
