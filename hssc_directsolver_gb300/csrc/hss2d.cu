@@ -341,9 +341,7 @@ void SolvePlan<R>::run(cudaStream_t s) const {
     // fork both streams from s, issue every step after the steps it depends on, join
     // both back into s (under graph capture the events become graph edges)
     PlanStreams& S = *streams;
-    HSS_CUDA(cudaEventRecord(S.fork, s));
-    HSS_CUDA(cudaStreamWaitEvent(S.crit, S.fork, 0));
-    HSS_CUDA(cudaStreamWaitEvent(S.side, S.fork, 0));
+    S.fork_from(s);
     for (size_t i = 0; i < steps.size(); ++i) {
       const Step& st = steps[i];
       cudaStream_t q = st.side ? S.side : S.crit;
@@ -351,10 +349,7 @@ void SolvePlan<R>::run(cudaStream_t s) const {
       run_step(st, q);
       if (st.rec) HSS_CUDA(cudaEventRecord(S.ev[i], q));
     }
-    HSS_CUDA(cudaEventRecord(S.jc, S.crit));
-    HSS_CUDA(cudaEventRecord(S.js, S.side));
-    HSS_CUDA(cudaStreamWaitEvent(s, S.jc, 0));
-    HSS_CUDA(cudaStreamWaitEvent(s, S.js, 0));
+    S.join_into(s);
   }
   for (auto& st : tc_steps) st.run(s);
 }
@@ -1542,9 +1537,7 @@ void HSS2D::apply_stage_body(int r) {
   cudaStream_t cs = S.crit, ss = S.side;
   auto ev_up = [&](int lev) { return S.ev[lev]; };
   auto ev_lam = [&](int lev) { return S.ev[depth + 1 + lev]; };
-  HSS_CUDA(cudaEventRecord(S.fork, stream));
-  HSS_CUDA(cudaStreamWaitEvent(cs, S.fork, 0));
-  HSS_CUDA(cudaStreamWaitEvent(ss, S.fork, 0));
+  S.fork_from(stream);
   fp.lam[depth].run(ss);  // the leaves' self products: the input only
   HSS_CUDA(cudaEventRecord(ev_lam(depth), ss));
   for (int lev = depth; lev >= 1; --lev) {
@@ -1579,10 +1572,7 @@ void HSS2D::apply_stage_body(int r) {
         g.nb, g.n, g.k, kc, leaf ? 1 : 0, r, d.J.p, d.IsrcJ.p, dst, ldd, d.dnF.p, (long long)g.nb * g.k, d.tmF.p,
         (long long)g.nb * std::max(nr, 1));
   }
-  HSS_CUDA(cudaEventRecord(S.jc, cs));
-  HSS_CUDA(cudaEventRecord(S.js, ss));
-  HSS_CUDA(cudaStreamWaitEvent(stream, S.jc, 0));
-  HSS_CUDA(cudaStreamWaitEvent(stream, S.js, 0));
+  S.join_into(stream);
   check_launch("apply");
 }
 
