@@ -104,6 +104,7 @@ SIGNATURES = {
                                     C.c_double, C.c_uint64]),
     "hss1d_forest_info": (C.c_int, [_P, _I32P, _I64P, _I32P, _I64P]),
     "hss1d_is_complex": (C.c_int, [_P, _I32P]),
+    "hss2d_is_complex": (C.c_int, [_P, _I32P]),
     "hss1d_recompress": (C.c_int, [_P, C.c_double, C.POINTER(_P)]),
     "hss1d_info": (C.c_int, [_P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P]),
     "hss1d_export_box": (C.c_int, [_P, C.c_int32, _I32P, _I32P, _I32P, _I32P, _DP, _DP]),

@@ -928,6 +928,13 @@ int hss2d_set_autotune(hss2d_matrix* H, int32_t on) {
   HSS_CATCH
 }
 
+int hss2d_is_complex(const hss2d_matrix* H, int32_t* is_complex) {
+  HSS_TRY
+  HSS_REQUIRE(H && H->impl && is_complex, HSS_ERR_ARG, "NULL argument");
+  *is_complex = H->impl->cplx ? 1 : 0;
+  HSS_CATCH
+}
+
 int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N) {
   HSS_TRY
   HSS_REQUIRE(H && H->impl, HSS_ERR_ARG, "NULL handle");

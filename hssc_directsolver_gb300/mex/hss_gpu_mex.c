@@ -118,10 +118,13 @@ static int flag_of(const mxArray* params) {
   return -1;
 }
 
-/* b(x), c(y): explicit fields, else the Laplace choice of LOCAL_get_bc (Kernel_Eval.m:141-159) */
+/* b(x), c(y): explicit fields (b_kind / c_kind: HSS_MOD_*), else the choice of LOCAL_get_bc
+ * (Kernel_Eval.m:111-159) from params.sym, .transinv, .proxy (default 0) and .kh */
 static void modulations(const mxArray* params, hss_kernel_params* kp) {
   const int sym = (int)field_or(params, "sym", 0), ti = (int)field_or(params, "transinv", 0);
-  if (mxGetField(params, 0, "b_alpha") || mxGetField(params, 0, "c_alpha")) {
+  const int proxy = (int)field_or(params, "proxy", 0);
+  if (mxGetField(params, 0, "b_alpha") || mxGetField(params, 0, "c_alpha") || mxGetField(params, 0, "b_kind") ||
+      mxGetField(params, 0, "c_kind")) {
     kp->b_alpha = field_or(params, "b_alpha", 0.0);
     kp->b_x0 = field_or(params, "b_x0", 0.0);
     kp->b_y0 = field_or(params, "b_y0", 0.0);
@@ -130,16 +133,31 @@ static void modulations(const mxArray* params, hss_kernel_params* kp) {
     kp->c_x0 = field_or(params, "c_x0", 0.0);
     kp->c_y0 = field_or(params, "c_y0", 0.0);
     kp->c_isig = field_or(params, "c_isig", 1.0);
+    kp->b_kind = (int32_t)field_or(params, "b_kind", HSS_MOD_GAUSS);
+    kp->c_kind = (int32_t)field_or(params, "c_kind", HSS_MOD_GAUSS);
     return;
   }
   kp->b_isig = kp->c_isig = 1.0;
+  if (sym == 0 && kp->kh > 0) {  /* nonsymmetric Lippmann-Schwinger (:113-125) */
+    if (proxy <= 0) kp->b_kind = HSS_MOD_BUMP;
+    return;
+  }
   if (ti) return;
-  kp->b_alpha = 0.25;
-  kp->b_x0 = 0.3;
-  kp->b_y0 = 0.6;
-  kp->c_alpha = 0.25;
-  kp->c_x0 = sym ? 0.3 : 0.2;
-  kp->c_y0 = sym ? 0.6 : -0.6;
+  if (kp->kh > 0) {  /* symmetric Lippmann-Schwinger (:129-140) */
+    if (proxy <= 0) kp->b_kind = HSS_MOD_SQRT_BUMP;
+    if (proxy >= 0) kp->c_kind = HSS_MOD_SQRT_BUMP;
+    return;
+  }
+  if (proxy <= 0) {
+    kp->b_alpha = 0.25;
+    kp->b_x0 = 0.3;
+    kp->b_y0 = 0.6;
+  }
+  if (proxy >= 0) {
+    kp->c_alpha = 0.25;
+    kp->c_x0 = sym ? 0.3 : 0.2;
+    kp->c_y0 = sym ? 0.6 : -0.6;
+  }
 }
 
 static void kernel_params(const mxArray* params, hss_kernel_params* kp) {
@@ -147,7 +165,51 @@ static void kernel_params(const mxArray* params, hss_kernel_params* kp) {
   kp->flag = flag_of(params);
   kp->h = field_or(params, "h", 1.0);
   kp->kh = field_or(params, "kh", 0.0);
-  if (kp->flag == HSS_SL_L_2D) modulations(params, kp);
+  if (kp->flag != HSS_DL_L_2D) modulations(params, kp);
+  if (kp->flag == HSS_SL_H_2D) {  /* params.dr_weights: the complex diagonal weight */
+    const mxArray* dr = mxGetField(params, 0, "dr_weights");
+    if (dr && mxIsComplex(dr)) {
+      kp->dr_re = mxGetComplexDoubles(dr)[0].real;
+      kp->dr_im = mxGetComplexDoubles(dr)[0].imag;
+    } else if (dr) {
+      kp->dr_re = mxGetScalar(dr);
+    }
+  }
+}
+
+/* A double matrix's data in the library's layout: interleaved (re, im) pairs for a complex
+ * handle (a real X is widened into *tmp), plain doubles otherwise */
+static const double* vec_in(const mxArray* X, int cplx, mxArray** tmp) {
+  if (!mxIsDouble(X)) mexErrMsgIdAndTxt("hss:gpu", "vectors must be double");
+  if (!cplx) {
+    if (mxIsComplex(X)) mexErrMsgIdAndTxt("hss:gpu", "a complex vector for a real matrix");
+    return mxGetDoubles(X);
+  }
+  if (mxIsComplex(X)) return (const double*)mxGetComplexDoubles(X);
+  const size_t n = mxGetNumberOfElements(X);
+  *tmp = mxCreateDoubleMatrix(mxGetM(X), mxGetN(X), mxCOMPLEX);
+  mxComplexDouble* d = mxGetComplexDoubles(*tmp);
+  const double* s = mxGetDoubles(X);
+  for (size_t i = 0; i < n; ++i) { d[i].real = s[i]; d[i].imag = 0.0; }
+  return (const double*)d;
+}
+
+static mxArray* vec_out(mwSize m, mwSize n, int cplx, double** data) {
+  mxArray* a = mxCreateDoubleMatrix(m, n, cplx ? mxCOMPLEX : mxREAL);
+  *data = cplx ? (double*)mxGetComplexDoubles(a) : mxGetDoubles(a);
+  return a;
+}
+
+static int tree_complex(hss2d_matrix* H) {
+  int32_t c = 0;
+  check(hss2d_is_complex(H, &c));
+  return c;
+}
+
+static int khss_complex(hss1d_matrix* H) {
+  int32_t c = 0;
+  check(hss1d_is_complex(H, &c));
+  return c;
 }
 
 static void hss2d_params_of(const mxArray* params, hss2d_params* p) {
@@ -220,14 +282,15 @@ static mxArray* info_tree(hss2d_matrix* H) {
   check(hss2d_box_sizes(H, n, k, px));
   const char* bf[] = {"levbox", "parent", "child", "n_skel", "k", "I_src", "J", "T_up", "T_dn"};
   mxArray* box = mxCreateStructMatrix((mwSize)nb, 1, 9, bf);
+  const int cx = tree_complex(H), w = cx ? 2 : 1;  /* complex trees export complex T */
   int32_t* isrc = (int32_t*)xmalloc(sizeof(int32_t) * (size_t)N);
   int32_t* J = (int32_t*)xmalloc(sizeof(int32_t) * (size_t)N);
   for (int b = 0; b < nb; ++b) {
     int lev = 0;
     while ((2 << lev) - 1 <= b) ++lev;  /* BFS numbering: level l holds boxes 2^l - 1 .. 2^(l+1) - 2 */
     const int nr = n[b] - k[b];
-    double* Tu = (double*)xmalloc(sizeof(double) * (size_t)k[b] * (nr > 0 ? nr : 1));
-    double* Td = (double*)xmalloc(sizeof(double) * (size_t)k[b] * (nr > 0 ? nr : 1));
+    double* Tu = (double*)xmalloc(sizeof(double) * w * (size_t)k[b] * (nr > 0 ? nr : 1));
+    double* Td = (double*)xmalloc(sizeof(double) * w * (size_t)k[b] * (nr > 0 ? nr : 1));
     check(hss2d_export_box(H, b, isrc, J, b > 0 ? Tu : NULL, b > 0 ? Td : NULL));
     mxSetField(box, b, "levbox", scalar(lev));
     mxSetField(box, b, "parent", scalar(b > 0 ? (b - 1) / 2 + 1 : 0));
@@ -242,11 +305,12 @@ static mxArray* info_tree(hss2d_matrix* H) {
     mxSetField(box, b, "I_src", index_row(isrc, n[b]));
     mxSetField(box, b, "J", index_row(J, n[b]));
     if (b > 0 && nr > 0) {
-      mxArray* U = mxCreateDoubleMatrix((mwSize)k[b], (mwSize)nr, mxREAL);
-      memcpy(mxGetDoubles(U), Tu, sizeof(double) * (size_t)k[b] * nr);
+      double* d = NULL;
+      mxArray* U = vec_out((mwSize)k[b], (mwSize)nr, cx, &d);
+      memcpy(d, Tu, sizeof(double) * w * (size_t)k[b] * nr);
       mxSetField(box, b, "T_up", tstruct(U, nr));
-      U = mxCreateDoubleMatrix((mwSize)k[b], (mwSize)nr, mxREAL);
-      memcpy(mxGetDoubles(U), Td, sizeof(double) * (size_t)k[b] * nr);
+      U = vec_out((mwSize)k[b], (mwSize)nr, cx, &d);
+      memcpy(d, Td, sizeof(double) * w * (size_t)k[b] * nr);
       mxSetField(box, b, "T_dn", tstruct(U, nr));
     }
     free(Tu);
@@ -284,10 +348,12 @@ static mxArray* a_hss(hss2d_matrix* H, int inverted) {
   int32_t* n = (int32_t*)xmalloc(sizeof(int32_t) * nb);
   int32_t* k = (int32_t*)xmalloc(sizeof(int32_t) * nb);
   check(hss2d_box_sizes(H, n, k, NULL));
+  const int cx = tree_complex(H);
   for (int b = 0; b < nb; ++b) {
-    mxArray* FI = mxCreateDoubleMatrix((mwSize)n[b], (mwSize)n[b], mxREAL);
-    mxArray* E = (b > 0) ? mxCreateDoubleMatrix((mwSize)k[b], (mwSize)k[b], mxREAL) : NULL;
-    check(hss2d_export_inverse(H, b, mxGetDoubles(FI), E ? mxGetDoubles(E) : NULL));
+    double *fi = NULL, *e = NULL;
+    mxArray* FI = vec_out((mwSize)n[b], (mwSize)n[b], cx, &fi);
+    mxArray* E = (b > 0) ? vec_out((mwSize)k[b], (mwSize)k[b], cx, &e) : NULL;
+    check(hss2d_export_inverse(H, b, fi, e));
     mxSetField(a, b, "FI", FI);
     if (E) mxSetField(a, b, "E", E);
   }
@@ -315,6 +381,7 @@ static mxArray* k_hss(hss1d_matrix* H) {
           *ns = lv + 6 * nb, *ks = lv + 7 * nb;
   check(hss1d_info(H, &nb, lv, par, c1, c2, off, cnt, ns, ks));
   mxArray* K = mxCreateCellMatrix(BOX_ROWS, (mwSize)nb);
+  const int cx = khss_complex(H);
   for (int b = 0; b < nb; ++b) {
     set_row(K, BOX_LEVEL, b, scalar(lv[b]));
     set_row(K, BOX_PARENT, b, scalar(par[b] >= 0 ? par[b] + 1 : 0));
@@ -328,9 +395,10 @@ static mxArray* k_hss(hss1d_matrix* H) {
     const int n = ns[b], k = ks[b], nr = n - k;
     int32_t* iu = (int32_t*)xmalloc(sizeof(int32_t) * (size_t)(2 * k + 2 * n));
     int32_t *id = iu + k, *ju = iu + 2 * k, *jd = ju + n;
-    mxArray* Tu = mxCreateDoubleMatrix((mwSize)k, (mwSize)(nr > 0 ? nr : 0), mxREAL);
-    mxArray* Td = mxCreateDoubleMatrix((mwSize)k, (mwSize)(nr > 0 ? nr : 0), mxREAL);
-    check(hss1d_export_box(H, b, iu, id, ju, jd, mxGetDoubles(Tu), mxGetDoubles(Td)));
+    double *tu = NULL, *td = NULL;
+    mxArray* Tu = vec_out((mwSize)k, (mwSize)(nr > 0 ? nr : 0), cx, &tu);  /* complex for a complex handle */
+    mxArray* Td = vec_out((mwSize)k, (mwSize)(nr > 0 ? nr : 0), cx, &td);
+    check(hss1d_export_box(H, b, iu, id, ju, jd, tu, td));
     set_row(K, BOX_I_SKUP, b, index_row(iu, k));
     set_row(K, BOX_I_SKDN, b, index_row(id, k));
     set_row(K, BOX_J_UP, b, index_row(ju, n));
@@ -378,20 +446,26 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     NEED(4);
     hss2d_matrix* H = tree_handle(prhs[1]);
     const mxArray* X = prhs[3];
-    if (!mxIsDouble(X)) mexErrMsgIdAndTxt("hss:gpu", "X must be double");
+    const int cx = tree_complex(H);
+    mxArray* tmp = NULL;
+    const double* x = vec_in(X, cx, &tmp);
     const mwSize N = mxGetM(X), r = mxGetN(X);
-    plhs[0] = mxCreateDoubleMatrix(N, r, mxREAL);
-    if (!strcmp(op, "HSS2D_applyinv_nsym")) check(hss2d_applyinv(H, mxGetDoubles(X), mxGetDoubles(plhs[0]), (int32_t)r));
-    else check(hss2d_apply(H, mxGetDoubles(X), mxGetDoubles(plhs[0]), (int32_t)r));
+    double* y = NULL;
+    plhs[0] = vec_out(N, r, cx, &y);
+    if (!strcmp(op, "HSS2D_applyinv_nsym")) check(hss2d_applyinv(H, x, y, (int32_t)r));
+    else check(hss2d_apply(H, x, y, (int32_t)r));
   } else if (!strcmp(op, "Iterative_Refinement")) {
     NEED(5);
     hss2d_matrix* H = tree_handle(prhs[1]);
     const mwSize N = mxGetM(prhs[2]), r = mxGetN(prhs[2]);
     double relres = 0.0;
     int32_t iters = 0;
-    plhs[0] = mxCreateDoubleMatrix(N, r, mxREAL);
-    check(hss2d_solve(H, mxGetDoubles(prhs[2]), mxGetDoubles(plhs[0]), (int32_t)r, mxGetScalar(prhs[3]),
-                      (int32_t)mxGetScalar(prhs[4]), &relres, &iters));
+    const int cx = tree_complex(H);
+    mxArray* tmp = NULL;
+    const double* f = vec_in(prhs[2], cx, &tmp);
+    double* x = NULL;
+    plhs[0] = vec_out(N, r, cx, &x);
+    check(hss2d_solve(H, f, x, (int32_t)r, mxGetScalar(prhs[3]), (int32_t)mxGetScalar(prhs[4]), &relres, &iters));
     if (nlhs > 1) plhs[1] = scalar(relres);
     if (nlhs > 2) plhs[2] = scalar(iters);
   } else if (!strcmp(op, "HSS2D_destroy")) {
@@ -420,14 +494,22 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   } else if (!strcmp(op, "HSS1D_apply_nsym")) {
     NEED(3);
     hss1d_matrix* K = khss_handle(prhs[1]);
-    plhs[0] = mxCreateDoubleMatrix((mwSize)hss1d_rows(K), mxGetN(prhs[2]), mxREAL);
-    check(hss1d_apply(K, mxGetDoubles(prhs[2]), mxGetDoubles(plhs[0]), (int32_t)mxGetN(prhs[2])));
+    const int cx = khss_complex(K);
+    mxArray* tmp = NULL;
+    const double* q = vec_in(prhs[2], cx, &tmp);
+    double* u = NULL;
+    plhs[0] = vec_out((mwSize)hss1d_rows(K), mxGetN(prhs[2]), cx, &u);
+    check(hss1d_apply(K, q, u, (int32_t)mxGetN(prhs[2])));
   } else if (!strcmp(op, "HSS1D_applyinv_nsym")) {
     NEED(5);
     hss1d_matrix* K = khss_handle(prhs[1]);
     const mwSize N = mxGetM(prhs[4]), r = mxGetN(prhs[4]);
-    plhs[0] = mxCreateDoubleMatrix(N, r, mxREAL);
-    check(hss1d_applyinv(K, mxGetDoubles(prhs[4]), mxGetDoubles(plhs[0]), (int32_t)r));
+    const int cx = khss_complex(K);
+    mxArray* tmp = NULL;
+    const double* f = vec_in(prhs[4], cx, &tmp);
+    double* x = NULL;
+    plhs[0] = vec_out(N, r, cx, &x);
+    check(hss1d_applyinv(K, f, x, (int32_t)r));
   } else if (!strcmp(op, "HSS1D_destroy")) {
     NEED(2);
     check(hss1d_destroy(khss_handle(prhs[1])));
@@ -436,9 +518,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     hss_kernel_params kp;
     kernel_params(prhs[3], &kp);
     const mwSize m = mxGetM(prhs[1]), n = mxGetM(prhs[2]);
-    plhs[0] = mxCreateDoubleMatrix(m, n, mxREAL);
-    check(hss_kernel_eval(&kp, mxGetDoubles(prhs[1]), (int64_t)m, mxGetDoubles(prhs[2]), (int64_t)n,
-                          mxGetDoubles(plhs[0])));
+    double* A = NULL;
+    plhs[0] = vec_out(m, n, kp.flag == HSS_SL_H_2D, &A);  /* complex for the Helmholtz kernel */
+    check(hss_kernel_eval(&kp, mxGetDoubles(prhs[1]), (int64_t)m, mxGetDoubles(prhs[2]), (int64_t)n, A));
   } else {
     mexErrMsgIdAndTxt("hss:gpu", "unknown operation %s", op);
   }

@@ -412,6 +412,8 @@ int hss2d_kernel_residual_rows(hss2d_matrix* H, int64_t row0, int64_t nrows, con
 int hss2d_proxy_points(const hss2d_params* p, int32_t box, int32_t n_src, double* xy, int32_t cap,
                        int32_t* count);
 int hss2d_info(const hss2d_matrix* H, int32_t* depth, int32_t* nboxes, int64_t* N);
+/* 1 when the tree holds a complex (HSS_SL_H_2D) matrix, else 0 */
+int hss2d_is_complex(const hss2d_matrix* H, int32_t* is_complex);
 /* per-box sizes: n (|I_src|), k (|I_sk|), proxy count; arrays of nboxes (NULL ok) */
 int hss2d_box_sizes(const hss2d_matrix* H, int32_t* n, int32_t* k, int32_t* nproxy);
 /* INFO_TREE.BOX(b).{I_src, J, T_up, T_dn} (T_* k x (n-k) column-major); NULL ok */

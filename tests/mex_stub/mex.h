@@ -25,6 +25,7 @@ typedef enum {
   mxINT32_CLASS, mxUINT32_CLASS, mxINT64_CLASS, mxUINT64_CLASS
 } mxClassID;
 typedef double mxDouble;
+typedef struct { double real, imag; } mxComplexDouble;
 
 mxArray* mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c);
 mxArray* mxCreateDoubleScalar(double v);
@@ -37,6 +38,8 @@ mxArray* mxGetCell(const mxArray* cell, mwIndex i);
 void mxSetField(mxArray* s, mwIndex i, const char* name, mxArray* v);
 mxArray* mxGetField(const mxArray* s, mwIndex i, const char* name);
 mxDouble* mxGetDoubles(const mxArray* a);
+mxComplexDouble* mxGetComplexDoubles(const mxArray* a);
+int mxIsComplex(const mxArray* a);
 void* mxGetData(const mxArray* a);
 double mxGetScalar(const mxArray* a);
 int mxGetString(const mxArray* a, char* buf, mwSize len);

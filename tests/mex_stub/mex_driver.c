@@ -2,9 +2,12 @@
  * Runs the MEX shim (hssc_directsolver_gb300/mex/hss_gpu_mex.c) through the host-side
  * stand-ins of mex_stub.c, as the reference's scripts would call it from MATLAB:
  *   params -> HSS2D_build_tree_nsym -> HSS2D_compress_nsym -> HSS2D_invert_nsym ->
- *   HSS2D_applyinv_nsym, then HSS1D_compress_nsym -> HSS1D_invert_nsym -> HSS1D_applyinv_nsym.
+ *   HSS2D_applyinv_nsym, then HSS1D_compress_nsym -> HSS1D_invert_nsym -> HSS1D_applyinv_nsym,
+ *   then the same HSS1D sequence with the complex Helmholtz kernel (SL_H_2D, complex
+ *   right-hand side) and Kernel_Eval of it.
  * usage: mex_driver DIR   (DIR holds sizes.txt "N npan M", x_source.bin (N x 2), rhs.bin
- * (N x 2), curve.bin (M x 6), column-major doubles).  Writes y2d.bin, y1d.bin, info.txt.
+ * (N x 2), curve.bin (M x 6), column-major doubles).  Writes y2d.bin, y1d.bin, y1c.bin,
+ * ke.bin, info.txt.
  * Exit 0 on success, 3 when the shim raised a MATLAB error (printed as "MEXERR: ...").
  */
 #include <setjmp.h>
@@ -141,6 +144,59 @@ int main(int argc, char** argv) {
   for (size_t i = 0; i < mxGetNumberOfElements(isk); ++i) fprintf(fo, "%g ", mxGetDoubles(isk)[i]);
   fprintf(fo, "\n");
   fclose(fo);
+  /* the complex Helmholtz curve: SL_H_2D, kh = 20, h = 0.05, dr_weights 0.3 + 0.1i, explicit
+   * Gaussian b and c; the right-hand side rhs(:, 1) + i rhs(:, 2) */
+  const char* hn[] = {"flag_pot", "kh", "h", "dr_weights", "b_alpha", "b_x0", "b_y0", "b_isig",
+                      "c_alpha", "c_x0", "c_y0", "c_isig"};
+  mxArray* hk = mxCreateStructMatrix(1, 1, 12, hn);
+  mxSetField(hk, 0, "flag_pot", mxCreateString("SL_H_2D"));
+  mxSetField(hk, 0, "kh", mxCreateDoubleScalar(20));
+  mxSetField(hk, 0, "h", mxCreateDoubleScalar(0.05));
+  mxArray* dr = mxCreateDoubleMatrix(1, 1, mxCOMPLEX);
+  mxGetComplexDoubles(dr)[0].real = 0.3;
+  mxGetComplexDoubles(dr)[0].imag = 0.1;
+  mxSetField(hk, 0, "dr_weights", dr);
+  mxSetField(hk, 0, "b_alpha", mxCreateDoubleScalar(0.5));
+  mxSetField(hk, 0, "b_x0", mxCreateDoubleScalar(0.3));
+  mxSetField(hk, 0, "b_y0", mxCreateDoubleScalar(0));
+  mxSetField(hk, 0, "b_isig", mxCreateDoubleScalar(2));
+  mxSetField(hk, 0, "c_alpha", mxCreateDoubleScalar(-0.3));
+  mxSetField(hk, 0, "c_x0", mxCreateDoubleScalar(0));
+  mxSetField(hk, 0, "c_y0", mxCreateDoubleScalar(-0.2));
+  mxSetField(hk, 0, "c_isig", mxCreateDoubleScalar(3));
+  in[0] = mxCreateString("green");
+  in[1] = matrix(curve, (size_t)M, 6);
+  in[2] = mxCreateDoubleScalar(64);
+  in[3] = mxCreateDoubleScalar(1e-10);
+  in[4] = hk;
+  mxArray* Kc = call("HSS1D_compress_nsym", 1, NULL, 5, in);
+  in[0] = Kc;
+  in[1] = mxCreateDoubleScalar(1e-10);
+  call("HSS1D_invert_nsym", 2, inv, 2, in);
+  mxArray* fc = mxCreateDoubleMatrix((size_t)M, 1, mxCOMPLEX);
+  for (long i = 0; i < M; ++i) {
+    mxGetComplexDoubles(fc)[i].real = rhs[i];
+    mxGetComplexDoubles(fc)[i].imag = rhs[N + i];
+  }
+  in[0] = Kc;
+  in[1] = inv[0];
+  in[2] = inv[1];
+  in[3] = fc;
+  mxArray* xc = call("HSS1D_applyinv_nsym", 1, NULL, 4, in);
+  if (!mxIsComplex(xc)) { printf("MEXERR: complex handle returned a real vector\n"); return 3; }
+  write_doubles("y1c.bin", (const double*)mxGetComplexDoubles(xc), (size_t)M * 2);
+  in[0] = matrix(curve, 8, 2);  /* Kernel_Eval(X(1:8, 1:2), X(1:8, 1:2), params): rows 1..8 */
+  {
+    double* q = mxGetDoubles(in[0]);
+    for (int i = 0; i < 8; ++i) { q[i] = curve[i]; q[8 + i] = curve[M + i]; }
+  }
+  in[1] = in[0];
+  in[2] = hk;
+  mxArray* ke = call("Kernel_Eval", 1, NULL, 3, in);
+  if (!mxIsComplex(ke)) { printf("MEXERR: Kernel_Eval of SL_H_2D is not complex\n"); return 3; }
+  write_doubles("ke.bin", (const double*)mxGetComplexDoubles(ke), 64 * 2);
+  in[0] = Kc;
+  call("HSS1D_destroy", 0, NULL, 1, in);
   in[0] = info;
   call("HSS2D_destroy", 0, NULL, 1, in);
   in[0] = K;

@@ -16,6 +16,7 @@
 struct mxArray_tag {
   mxClassID cls;
   mwSize m, n;
+  int cplx;             /* complex double: (re, im) pairs in data (the interleaved API) */
   void* data;           /* numeric / char payload */
   int nfields;
   char** names;         /* struct field names */
@@ -34,9 +35,9 @@ static mxArray* alloc_array(mxClassID cls, mwSize m, mwSize n) {
 }
 
 mxArray* mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c) {
-  (void)c;
   mxArray* a = alloc_array(mxDOUBLE_CLASS, m, n);
-  a->data = calloc((m * n) > 0 ? m * n : 1, sizeof(double));
+  a->cplx = (c == mxCOMPLEX);
+  a->data = calloc((m * n) > 0 ? m * n * (a->cplx ? 2 : 1) : 1, sizeof(double));
   return a;
 }
 mxArray* mxCreateDoubleScalar(double v) {
@@ -94,7 +95,11 @@ mxArray* mxGetField(const mxArray* s, mwIndex i, const char* name) {
   const int f = field_index(s, name);
   return f < 0 ? NULL : s->items[i * s->nfields + f];
 }
-mxDouble* mxGetDoubles(const mxArray* a) { return a->cls == mxDOUBLE_CLASS ? (double*)a->data : NULL; }
+mxDouble* mxGetDoubles(const mxArray* a) { return (a->cls == mxDOUBLE_CLASS && !a->cplx) ? (double*)a->data : NULL; }
+mxComplexDouble* mxGetComplexDoubles(const mxArray* a) {
+  return (a->cls == mxDOUBLE_CLASS && a->cplx) ? (mxComplexDouble*)a->data : NULL;
+}
+int mxIsComplex(const mxArray* a) { return a && a->cplx; }
 void* mxGetData(const mxArray* a) { return a->data; }
 double mxGetScalar(const mxArray* a) {
   if (a->cls == mxDOUBLE_CLASS) return *(double*)a->data;

@@ -89,3 +89,15 @@ def test_mex_shim_matches_python_binding(gpu, tmp_path):
     assert int(lines[4]) == len(inf["kskel"])
     assert [int(float(v)) for v in lines[5].split()] == list(inf["kskel"])
     assert [int(float(v)) for v in lines[6].split()] == list(H.export_box(1)["I_SKUP"] + 1)
+    # the complex Helmholtz curve through the shim: complex right-hand side in, complex out
+    gb, gc = GK.Modulation(0.5, 0.3, 0.0, 2.0), GK.Modulation(-0.3, 0.0, -0.2, 3.0)
+    hk = GK.Kernel("SL_H_2D", 0.05, gb, gc, 20.0, 0.3 + 0.1j)
+    Hc = G1.HSS1D_compress_nsym("green", C, 64, 1e-10, hk)
+    G1.HSS1D_invert_nsym(Hc)
+    xc = G1.HSS1D_applyinv_nsym(Hc, None, None, F[:M, 0] + 1j * F[:M, 1])
+    yc = np.fromfile(os.path.join(tmp_path, "y1c.bin")).view(np.complex128)
+    assert np.linalg.norm(yc - xc) <= 1e-13 * np.linalg.norm(xc)
+    ke = np.fromfile(os.path.join(tmp_path, "ke.bin")).view(np.complex128).reshape(8, 8, order="F")
+    P = np.asfortranarray(C[:8, :2])
+    ref_ke = GK.Kernel_Eval(P, P, hk)
+    assert np.abs(ke - ref_ke).max() <= 1e-15 * np.abs(ref_ke).max()
