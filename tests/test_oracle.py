@@ -379,6 +379,31 @@ def test_hss2d_helmholtz_oracle():
     assert np.linalg.norm(hss2d.apply_nsym(tree, hss2d.compress_nsym(tree, prm), x) - f) <= 1e-9 * np.linalg.norm(f)
 
 
+def test_hss1d_complex_helmholtz_oracle():
+    """HSS1D_compress_nsym / _fsym restated for the complex Helmholtz kernel: the proxy ring of
+    min(max(50, round(4 kh 1.75 R + 30)), N) points (HSS1D_compress_nsym.m:111-114), complex
+    IDs of A_out and A_in.' (plain transpose); the compressed operator matches the dense
+    matrix and the inverse apply inverts it.  fsym on a complex symmetric matrix (b = c)."""
+    from oracle import hss1d as O
+    X = geometry.star_curve(512)
+    ob, oc = kernels.Modulation(0.5, 0.3, 0.0, 2.0), kernels.Modulation(-0.3, 0.0, -0.2, 3.0)
+    r = np.random.default_rng(4)
+    q = r.standard_normal((512, 2)) + 1j * r.standard_normal((512, 2))
+    for b, c, fs in ((ob, oc, False), (ob, ob, True)):
+        kp = kernels.KernelParams(flag=kernels.SL_H_2D, h=0.05, b=b, c=c, kh=10.0, dr=0.3 + 0.1j)
+        H = (O.compress_fsym if fs else O.compress_nsym)(X, 64, 1e-10, kp)
+        assert np.iscomplexobj(H.T_UP[1]) and np.iscomplexobj(H.M_SELF[-1])
+        assert max(c_[0] for c_ in H.census[1:3]) > 50      # the Helmholtz ring is larger
+        K = kernels.kernel_eval(X, X, kp)
+        u = O.apply_nsym(H, q)
+        assert np.linalg.norm(u - K @ q) <= 1e-9 * np.linalg.norm(K @ q)
+        x = O.applyinv_nsym(H, O.invert_nsym(H), u)
+        assert np.linalg.norm(x - q) <= 1e-12 * np.linalg.norm(q)
+    assert O.proxy_count(kp, 0.5, 512) == max(50, round(4 * 10.0 * 1.75 * 0.5 + 30))
+    assert O.proxy_count(kernels.KernelParams(flag=kernels.DL_L_2D), 0.5, 512) == 50
+    assert O.proxy_count(kp, 100.0, 512) == 512                  # capped at the curve's N
+
+
 def test_hss1d_recompress():
     """HSS1D_recompress_nsym restated: a compression at 1e-14 recompressed at acc keeps the
     operator to ~acc with much smaller ranks (SVD truncation of the far-field blocks)."""
