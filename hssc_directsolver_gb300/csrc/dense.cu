@@ -1553,6 +1553,39 @@ __global__ void __launch_bounds__(256) k_qr_update(const QrP<R>* __restrict__ P,
   }
 }
 
+// Shared-memory operands of the double-float trailing update, stored in the form the
+// f32x2 products take them, so the inner loops issue one 64-bit load per operand and no
+// register moves.  A 32-row chunk of V is kept as the broadcast pairs (vh, vh),
+// (-vh, -vh), (-vl, -vl); the odd row stride (33 pairs) keeps both the row-wise and the
+// column-wise reads free of bank conflicts.  A 32 x 32 tile X of A (or of W2) is kept as
+// 16 column pairs per row: pair p = c + 8 u (c < 8, u < 2) holds columns (c + 16 u,
+// c + 16 u + 8), the two columns one thread owns together.
+struct DfVChunk {
+  f32x2 b[32][33], bn[32][33], bl[32][33];
+};
+struct DfXTile {
+  f32x2 h[32][17], l[32][17];
+};
+// float slot of column cc within a row of a DfXTile
+__device__ __forceinline__ int dfx_slot(int cc) { return 2 * ((cc & 7) + 8 * (cc >> 4)) + ((cc >> 3) & 1); }
+__device__ __forceinline__ void dfx_put(DfXTile& X, int i, int cc, float h, float l) {
+  reinterpret_cast<float*>(X.h[i])[dfx_slot(cc)] = h;
+  reinterpret_cast<float*>(X.l[i])[dfx_slot(cc)] = l;
+}
+// rows r0 .. r0+31 of V (rows past re and columns past nbk read as zero)
+__device__ __forceinline__ void dfv_stage(DfVChunk& S, const double* __restrict__ V, int m, int j0, int r0, int re,
+                                          int nbk, int tid) {
+  for (int e = tid; e < 32 * 32; e += 256) {
+    const int i = e & 31, jj = e >> 5;
+    const int gi = r0 + i;
+    float h, l;
+    split_d2f((gi < re && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
+    S.b[i][jj] = x2_pack(h, h);
+    S.bn[i][jj] = x2_pack(-h, -h);
+    S.bl[i][jj] = x2_pack(-l, -l);
+  }
+}
+
 // k_qr_update in double-float arithmetic for FP64 problems: W = V^T A,
 // W2 = Tf^T W and A -= V W2 for one 32-column tile, with every product on the
 // FP32 pipes (rows of V are the broadcast operand, column pairs of A / W2 the
@@ -1568,43 +1601,28 @@ __global__ void __launch_bounds__(256) k_qr_update_df(const QrP<double>* __restr
   double* A = p.A;
   const size_t lda = p.lda;
   const double* V = p.V;
-  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
-  __shared__ float Xh[32][33], Xl[32][33];  // A chunk in phase 1, W2 in phase 3
+  __shared__ DfVChunk Vc;
+  __shared__ DfXTile X;  // A chunk in phase 1, W2 in phase 3
   __shared__ float Wh[32][33], Wl[32][33];
   const int lo5 = tid & 31, hi3 = tid >> 5;
-  auto stage_v = [&](int r0) {
-    for (int e = tid; e < 32 * 32; e += 256) {
-      const int i = e & 31, jj = e >> 5;
-      const int gi = r0 + i;
-      float h, l;
-      split_d2f((gi < m && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
-      Vh[i][jj] = h;
-      Vhn[i][jj] = -h;
-      Vln[i][jj] = -l;
-    }
-  };
   // phase 1: thread owns W[jj = lo5][cc in {hi3, hi3+8} and {hi3+16, hi3+24}]
   f32x2 sh[2] = {0ULL, 0ULL}, sl[2] = {0ULL, 0ULL};
   for (int r0 = j0; r0 < m; r0 += 32) {
-    stage_v(r0);
+    dfv_stage(Vc, V, m, j0, r0, m, nbk, tid);
     for (int e = tid; e < 32 * 32; e += 256) {
       const int i = e & 31, cc = e >> 5;
       const int gi = r0 + i;
       float h, l;
       split_d2f((gi < m && cc < nc) ? A[gi + (size_t)(c0 + cc) * lda] : 0.0, h, l);
-      Xh[i][cc] = h;
-      Xl[i][cc] = l;
+      dfx_put(X, i, cc, h, l);
     }
     __syncthreads();
 #pragma unroll 4
     for (int i = 0; i < 32; ++i) {
-      const float vh = Vh[i][lo5], vhn = Vhn[i][lo5], vln = Vln[i][lo5];
-      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+      const f32x2 b2 = Vc.b[i][lo5], bn2 = Vc.bn[i][lo5], bl2 = Vc.bl[i][lo5];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int ca = hi3 + 16 * u, cb = ca + 8;
-        df_madd_x2(sh[u], sl[u], x2_pack(Xh[i][ca], Xh[i][cb]), x2_pack(Xl[i][ca], Xl[i][cb]), b2, bn2, bl2);
-      }
+      for (int u = 0; u < 2; ++u)
+        df_madd_x2(sh[u], sl[u], X.h[i][hi3 + 8 * u], X.l[i][hi3 + 8 * u], b2, bn2, bl2);
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {  // renormalise once per chunk
@@ -1635,23 +1653,19 @@ __global__ void __launch_bounds__(256) k_qr_update_df(const QrP<double>* __restr
         split_d2f(p.Tf[a + lo5 * QR_NB], fh, fl);
         df_madd(th, tl, Wh[a][cc], Wl[a][cc], fh, fl);
       }
-    Xh[lo5][cc] = th;  // W2 (the A chunk is no longer needed)
-    Xl[lo5][cc] = tl;
+    dfx_put(X, lo5, cc, th, tl);  // W2 (the A chunk is no longer needed)
   }
   __syncthreads();
   // phase 3: A -= V W2; thread owns rows i = lo5 of the chunk, columns as in phase 1
   for (int r0 = j0; r0 < m; r0 += 32) {
-    stage_v(r0);
+    dfv_stage(Vc, V, m, j0, r0, m, nbk, tid);
     __syncthreads();
     f32x2 ah[2] = {0ULL, 0ULL}, al[2] = {0ULL, 0ULL};
     for (int jj = 0; jj < nbk; ++jj) {
-      const float vh = Vh[lo5][jj], vhn = Vhn[lo5][jj], vln = Vln[lo5][jj];
-      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+      const f32x2 b2 = Vc.b[lo5][jj], bn2 = Vc.bn[lo5][jj], bl2 = Vc.bl[lo5][jj];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int ca = hi3 + 16 * u, cb = ca + 8;
-        df_madd_x2(ah[u], al[u], x2_pack(Xh[jj][ca], Xh[jj][cb]), x2_pack(Xl[jj][ca], Xl[jj][cb]), b2, bn2, bl2);
-      }
+      for (int u = 0; u < 2; ++u)
+        df_madd_x2(ah[u], al[u], X.h[jj][hi3 + 8 * u], X.l[jj][hi3 + 8 * u], b2, bn2, bl2);
     }
     const int gi = r0 + lo5;
 #pragma unroll
@@ -1701,33 +1715,26 @@ __global__ void __launch_bounds__(256) k_qr_wpart_df(const QrP<double>* __restri
   const double* A = p.A;
   const size_t lda = p.lda;
   const double* V = p.V;
-  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
-  __shared__ float Xh[32][33], Xl[32][33];
+  __shared__ DfVChunk Vc;
+  __shared__ DfXTile X;
   const int lo5 = tid & 31, hi3 = tid >> 5;
   f32x2 sh[2] = {0ULL, 0ULL}, sl[2] = {0ULL, 0ULL};
   for (int r0 = rb; r0 < re; r0 += 32) {
+    dfv_stage(Vc, V, m, j0, r0, re, nbk, tid);
     for (int e = tid; e < 32 * 32; e += 256) {
-      const int i = e & 31, jj = e >> 5;
+      const int i = e & 31, cc = e >> 5;
       const int gi = r0 + i;
       float h, l;
-      split_d2f((gi < re && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
-      Vh[i][jj] = h;
-      Vhn[i][jj] = -h;
-      Vln[i][jj] = -l;
-      split_d2f((gi < re && jj < nc) ? A[gi + (size_t)(c0 + jj) * lda] : 0.0, h, l);
-      Xh[i][jj] = h;
-      Xl[i][jj] = l;
+      split_d2f((gi < re && cc < nc) ? A[gi + (size_t)(c0 + cc) * lda] : 0.0, h, l);
+      dfx_put(X, i, cc, h, l);
     }
     __syncthreads();
 #pragma unroll 4
     for (int i = 0; i < 32; ++i) {
-      const float vh = Vh[i][lo5], vhn = Vhn[i][lo5], vln = Vln[i][lo5];
-      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+      const f32x2 b2 = Vc.b[i][lo5], bn2 = Vc.bn[i][lo5], bl2 = Vc.bl[i][lo5];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int ca = hi3 + 16 * u, cb = ca + 8;
-        df_madd_x2(sh[u], sl[u], x2_pack(Xh[i][ca], Xh[i][cb]), x2_pack(Xl[i][ca], Xl[i][cb]), b2, bn2, bl2);
-      }
+      for (int u = 0; u < 2; ++u)
+        df_madd_x2(sh[u], sl[u], X.h[i][hi3 + 8 * u], X.l[i][hi3 + 8 * u], b2, bn2, bl2);
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -1763,8 +1770,8 @@ __global__ void __launch_bounds__(256) k_qr_apply_df(const QrP<double>* __restri
   double* A = p.A;
   const size_t lda = p.lda;
   const double* V = p.V;
-  __shared__ float Vh[32][33], Vhn[32][33], Vln[32][33];
-  __shared__ float Xh[32][33], Xl[32][33];
+  __shared__ DfVChunk Vc;
+  __shared__ DfXTile X;  // W2
   __shared__ float Wh[32][33], Wl[32][33];
   const int lo5 = tid & 31, hi3 = tid >> 5;
   // W = the slices' partials, added in slice order
@@ -1790,30 +1797,18 @@ __global__ void __launch_bounds__(256) k_qr_apply_df(const QrP<double>* __restri
         split_d2f(p.Tf[a + lo5 * QR_NB], fh, fl);
         df_madd(th, tl, Wh[a][cc], Wl[a][cc], fh, fl);
       }
-    Xh[lo5][cc] = th;
-    Xl[lo5][cc] = tl;
+    dfx_put(X, lo5, cc, th, tl);
   }
   __syncthreads();
   for (int r0 = rb; r0 < re; r0 += 32) {
-    for (int e = tid; e < 32 * 32; e += 256) {
-      const int i = e & 31, jj = e >> 5;
-      const int gi = r0 + i;
-      float h, l;
-      split_d2f((gi < re && jj < nbk) ? V[(gi - j0) + (size_t)jj * m] : 0.0, h, l);
-      Vh[i][jj] = h;
-      Vhn[i][jj] = -h;
-      Vln[i][jj] = -l;
-    }
+    dfv_stage(Vc, V, m, j0, r0, re, nbk, tid);
     __syncthreads();
     f32x2 ah[2] = {0ULL, 0ULL}, al[2] = {0ULL, 0ULL};
     for (int jj = 0; jj < nbk; ++jj) {
-      const float vh = Vh[lo5][jj], vhn = Vhn[lo5][jj], vln = Vln[lo5][jj];
-      const f32x2 b2 = x2_pack(vh, vh), bn2 = x2_pack(vhn, vhn), bl2 = x2_pack(vln, vln);
+      const f32x2 b2 = Vc.b[lo5][jj], bn2 = Vc.bn[lo5][jj], bl2 = Vc.bl[lo5][jj];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int ca = hi3 + 16 * u, cb = ca + 8;
-        df_madd_x2(ah[u], al[u], x2_pack(Xh[jj][ca], Xh[jj][cb]), x2_pack(Xl[jj][ca], Xl[jj][cb]), b2, bn2, bl2);
-      }
+      for (int u = 0; u < 2; ++u)
+        df_madd_x2(ah[u], al[u], X.h[jj][hi3 + 8 * u], X.l[jj][hi3 + 8 * u], b2, bn2, bl2);
     }
     const int gi = r0 + lo5;
 #pragma unroll
