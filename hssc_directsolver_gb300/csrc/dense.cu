@@ -356,6 +356,15 @@ __device__ __forceinline__ double df_epilogue(float th, float tl, float ah, floa
   return df_to_double(th, tl);
 }
 
+// Sum of a double-float value over a warp (xor butterfly); every lane gets the same (h, l).
+__device__ __forceinline__ void warp_sum_df(float& h, float& l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    df_add(h, l, oh, ol);
+  }
+}
+
 // Paired-FP32 SIMD (sm_100+ f32x2): two lanes of FP32 per instruction, used for
 // the two rows a thread owns.  Values are 64-bit registers {row0, row1}.
 typedef unsigned long long f32x2;
@@ -1480,6 +1489,201 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl(const QrP<R>* __rest
   cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
+// k_qr_panel_cl in double-float arithmetic, for the FP64 problems of the double-float
+// modes: the panel is held as float pairs in the cluster's shared memory (the same 8 bytes
+// per entry), and the column norms, reflector dot products, rank-1 panel updates and the
+// Gram matrix run on the FP32 pipes (~2^-48 relative).  The Householder scalars, the
+// cluster totals of the squared norms, the Gram totals and the compact-WY factor stay in
+// FP64.  Same cluster layout, barriers, fixed summation order and outputs (R in A, V, Tf,
+// diag) as k_qr_panel_cl.
+__global__ void __launch_bounds__(QR_THREADS) k_qr_panel_cl_df(const QrP<double>* __restrict__ P, int j0) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int crank = (int)cl.block_rank();
+  const QrP<double> p = P[blockIdx.x / C];
+  if (j0 >= p.kf) return;  // same for the whole cluster
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  float2* pan = reinterpret_cast<float2*>(s_raw);  // rows_per x QR_NB, ld rows_per
+  __shared__ float2 slot1[2];      // partial squared norm; alpha (owner of row j)
+  __shared__ float2 slot2[QR_NB];  // partial reflector dot products
+  __shared__ float2 s_dot[QR_NB];  // tau (v . a_c), cluster totals
+  __shared__ float s_hf[4];        // scal and tau as float pairs
+  __shared__ double s_tau[QR_NB], s_beta[QR_NB];
+  __shared__ float shh[QR_THREADS / 32], shl[QR_THREADS / 32];
+  __shared__ double s_gram[QR_NB][QR_NB + 1];
+  __shared__ double s_tf[QR_NB][QR_NB + 1];
+  const int m = p.m, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  const int jend = min(j0 + QR_NB, p.kf), nbk = jend - j0;
+  const int mm = m - j0;
+  const int rows_per = (mm + C - 1) / C;
+  const int r0 = j0 + crank * rows_per, r1 = min(m, r0 + rows_per);
+  double* A = p.A;
+  const size_t lda = p.lda;
+  for (int e = tid; e < rows_per * QR_NB; e += nt) {
+    const int i = e % rows_per, c = e / rows_per;
+    float h = 0.f, l = 0.f;
+    if (c < nbk && r0 + i < r1) split_d2f(A[(r0 + i) + (size_t)(j0 + c) * lda], h, l);
+    pan[i + c * rows_per] = make_float2(h, l);
+  }
+  __syncthreads();
+  for (int j = j0; j < jend; ++j) {
+    const int jj = j - j0;
+    // squared norm of the column below the diagonal: CTA total in double-float
+    float nh = 0.f, nl = 0.f;
+    for (int i = max(j + 1, r0) + tid; i < r1; i += nt) {
+      const float2 v = pan[(i - r0) + jj * rows_per];
+      df_madd(nh, nl, v.x, v.y, v.x, v.y);
+    }
+    warp_sum_df(nh, nl);
+    __syncthreads();
+    if (lane == 0) { shh[w] = nh; shl[w] = nl; }
+    __syncthreads();
+    if (tid == 0) {
+      float th = shh[0], tl = shl[0];
+      for (int q = 1; q < nw; ++q) df_add(th, tl, shh[q], shl[q]);
+      slot1[0] = make_float2(th, tl);
+      // the owner of row j publishes alpha before anyone may rewrite it
+      if (j >= r0 && j < r1) slot1[1] = pan[(j - r0) + jj * rows_per];
+    }
+    cl.sync();
+    // the column's Householder scalars in FP64, by thread 0 of every CTA
+    const int oj = (j - j0) / rows_per;
+    if (tid == 0) {
+      double xn2 = 0.0;
+      for (int q = 0; q < C; ++q) {
+        const float2 t = *cl.map_shared_rank(&slot1[0], q);
+        xn2 += (double)t.x + (double)t.y;
+      }
+      const float2 a = *cl.map_shared_rank(&slot1[1], oj);
+      const double alpha = (double)a.x + (double)a.y;
+      double tau = 0.0, beta = alpha, scal = 0.0;
+      if (xn2 != 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      s_tau[jj] = tau;
+      s_beta[jj] = beta;
+      split_d2f(scal, s_hf[0], s_hf[1]);
+      split_d2f(tau, s_hf[2], s_hf[3]);
+    }
+    __syncthreads();
+    // reflector into the panel column (v_j = 1 on the diagonal row)
+    const float sch = s_hf[0], scl = s_hf[1];
+    for (int i = r0 + tid; i < r1; i += nt) {
+      float2* x = pan + (i - r0) + jj * rows_per;
+      if (i > j) {
+        float2 v = *x;
+        df_mul(v.x, v.y, sch, scl);
+        *x = v;
+      } else if (i == j) {
+        *x = make_float2(1.f, 0.f);
+      }
+    }
+    __syncthreads();
+    // partial dot products v . a_c for the remaining panel columns
+    for (int c = jj + 1 + w; c < nbk; c += nw) {
+      float dh = 0.f, dl = 0.f;
+      for (int i = max(j, r0) + lane; i < r1; i += 32) {
+        const float2 v = pan[(i - r0) + jj * rows_per], a = pan[(i - r0) + c * rows_per];
+        df_madd(dh, dl, v.x, v.y, a.x, a.y);
+      }
+      warp_sum_df(dh, dl);
+      if (lane == 0) slot2[c] = make_float2(dh, dl);
+    }
+    cl.sync();
+    if (tid < nbk && tid > jj) {
+      float th = 0.f, tl = 0.f;
+      for (int q = 0; q < C; ++q) {
+        const float2 t = *cl.map_shared_rank(&slot2[tid], q);
+        df_add(th, tl, t.x, t.y);
+      }
+      df_mul(th, tl, s_hf[2], s_hf[3]);
+      s_dot[tid] = make_float2(th, tl);
+    }
+    __syncthreads();
+    for (int e = tid; e < rows_per * nbk; e += nt) {
+      const int i = e % rows_per, c = e / rows_per;
+      const int gi = r0 + i;
+      if (c <= jj || gi >= r1 || gi < j) continue;
+      const float2 v = pan[i + jj * rows_per], d = s_dot[c];
+      float2 a = pan[i + c * rows_per];
+      df_madd(a.x, a.y, -d.x, -d.y, v.x, v.y);
+      pan[i + c * rows_per] = a;
+    }
+    if (crank == oj && tid == 0) p.diag[j] = fabs(s_beta[jj]);
+    __syncthreads();
+  }
+  // partial Gram matrix V^T V of the own rows (v_b is zero above row j0 + b)
+  for (int e = tid; e < nbk * nbk; e += nt) {
+    const int a = e % nbk, b = e / nbk;
+    float dh = 0.f, dl = 0.f;
+    if (a < b)
+      for (int i = max(r0, j0 + b); i < r1; ++i) {
+        const float2 va = pan[(i - r0) + a * rows_per], vb = pan[(i - r0) + b * rows_per];
+        df_madd(dh, dl, va.x, va.y, vb.x, vb.y);
+      }
+    s_gram[a][b] = (double)dh + (double)dl;
+  }
+  // V (explicit, zero above the diagonal) back to FP64
+  for (int e = tid; e < rows_per * QR_NB; e += nt) {
+    const int i = e % rows_per, c = e / rows_per;
+    const int gi = r0 + i;
+    if (gi >= r1) continue;
+    double v = 0.0;
+    if (c < nbk) {
+      const int gj = j0 + c;
+      if (gi > gj) {
+        const float2 t = pan[i + c * rows_per];
+        v = df_to_double(t.x, t.y);
+      } else if (gi == gj) {
+        v = 1.0;
+      }
+    }
+    p.V[(gi - j0) + (size_t)c * m] = v;
+  }
+  cl.sync();
+  if (crank == 0) {
+    // R's upper triangle (rows j0..jend-1 live in the first CTAs; beta on the diagonal)
+    for (int e = tid; e < nbk * nbk; e += nt) {
+      const int a = e % nbk, b = e / nbk;  // row j0+a, column j0+b
+      if (a > b) continue;
+      const int gi = j0 + a;
+      const int o = (gi - j0) / rows_per;
+      double v;
+      if (a == b) v = s_beta[b];
+      else {
+        const float2 t = *cl.map_shared_rank(&pan[(gi - j0 - o * rows_per) + b * rows_per], o);
+        v = df_to_double(t.x, t.y);
+      }
+      A[gi + (size_t)(j0 + b) * lda] = v;
+    }
+    // cluster totals of the Gram entries in FP64, stored in place (each entry read by
+    // every rank's sum, then overwritten by the one thread that owns it)
+    for (int e = tid; e < nbk * nbk; e += nt) {
+      const int a = e % nbk, b = e / nbk;
+      if (a >= b) continue;
+      double t = 0.0;
+      for (int q = 0; q < C; ++q) t += cl.map_shared_rank(&s_gram[0][0], q)[a * (QR_NB + 1) + b];
+      s_gram[a][b] = t;
+    }
+    for (int e = tid; e < QR_NB * QR_NB; e += nt) s_tf[e % QR_NB][e / QR_NB] = 0.0;
+    __syncthreads();
+    for (int b = 0; b < nbk; ++b) {
+      if (tid == 0) s_tf[b][b] = s_tau[b];
+      if (tid < b) {
+        const int a = tid;
+        double t = 0.0;
+        for (int c = a; c < b; ++c) t += s_tf[a][c] * s_gram[c][b];
+        s_tf[a][b] = -s_tau[b] * t;
+      }
+      __syncthreads();
+    }
+    for (int e = tid; e < QR_NB * QR_NB; e += nt) p.Tf[e] = s_tf[e % QR_NB][e / QR_NB];
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
 // Apply (I - V Tf V^T)^T = I - V Tf^T V^T to A[j0:m, jend:n] in 32-column tiles.
 template <typename R>
 __global__ void __launch_bounds__(256) k_qr_update(const QrP<R>* __restrict__ P, int j0) {
@@ -1989,9 +2193,26 @@ void lstsq_batched(const QrP<R>* dP, int batch, int maxm, int maxn, int maxkf, c
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   require_cluster_fits(k_qr_panel_cl<R>, cfg, C);
+  if constexpr (std::is_same<R, double>::value) {
+    if (df) {
+      static PerDeviceOnce attr_once_df;
+      attr_once_df.run([] {
+        HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl_df, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        HSS_CUDA(cudaFuncSetAttribute(k_qr_panel_cl_df, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      });
+      require_cluster_fits(k_qr_panel_cl_df, cfg, C);
+    }
+  }
   DevBuf<double> wpart;  // row-split partial W of the double-float update (float pairs)
   for (int j0 = 0; j0 < maxkf; j0 += QR_NB) {
-    HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl<R>, dP, j0, cap));
+    bool panel_done = false;
+    if constexpr (std::is_same<R, double>::value) {
+      if (df) {
+        HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl_df, dP, j0));
+        panel_done = true;
+      }
+    }
+    if (!panel_done) HSS_CUDA(cudaLaunchKernelEx(&cfg, k_qr_panel_cl<R>, dP, j0, cap));
     const int jend = std::min(j0 + QR_NB, maxkf);
     const int ncols = maxn - jend;
     if (ncols > 0) {
@@ -2549,14 +2770,6 @@ __device__ __forceinline__ void block_sum256_df(float& h, float& l, float* shh, 
 #pragma unroll
   for (int i = 1; i < 8; ++i) df_add(h, l, shh[i], shl[i]);
   __syncthreads();
-}
-
-__device__ __forceinline__ void warp_sum_df(float& h, float& l) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
-    df_add(h, l, oh, ol);
-  }
 }
 
 __device__ __forceinline__ double df_val(float2 v) { return (double)v.x + (double)v.y; }
