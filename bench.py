@@ -541,15 +541,22 @@ def main():
     paths = [p for p in args.paths.split(",") if p]
     for prec in paths:
         prm = workload_params(prec, args.npan)
-        barrier()
-        t0 = time.perf_counter()
-        tree = G2.HSS2D_build_tree_nsym(prm)
-        t1 = time.perf_counter()
-        G2.HSS2D_compress_nsym(tree)
-        t2 = time.perf_counter()
-        G2.HSS2D_invert_nsym(tree)
-        torch.cuda.synchronize()
-        t3 = time.perf_counter()
+        # built twice: the first build of a process also pays the first use of each kernel
+        # (module loading, one-time attributes); the second, warm build is the one reported
+        first_ci = None
+        for rep in range(2):
+            tree = None
+            barrier()
+            t0 = time.perf_counter()
+            tree = G2.HSS2D_build_tree_nsym(prm)
+            t1 = time.perf_counter()
+            G2.HSS2D_compress_nsym(tree)
+            t2 = time.perf_counter()
+            G2.HSS2D_invert_nsym(tree)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            if rep == 0:
+                first_ci = max_over_ranks(t3 - t0)
         ci = max_over_ranks(t3 - t0)
         # the solve plans tune their K splits when first built (in the warm-up solves)
         tree.set_autotune(True)
@@ -635,7 +642,7 @@ def main():
                 _, grr, gits = G2.HSS2D_gmres(tree, Fg, tol=1e-10, restart=20, maxit=40, PRECOND=tree)
             gm = {"ms_host_buffers": (time.perf_counter() - tg0) / max(1, args.steps // 4) * 1e3, "steps": gits,
                   "relres": grr}
-        results[prec] = dict(kernel_relres=kres, compress_invert_s=ci, tree_s=t1 - t0, compress_s=t2 - t1, invert_s=t3 - t2, gmres=gm,
+        results[prec] = dict(kernel_relres=kres, compress_invert_s=ci, first_compress_invert_s=first_ci, tree_s=t1 - t0, compress_s=t2 - t1, invert_s=t3 - t2, gmres=gm,
                              solve_ms=ms, relres=rr.value, solves_used=it.value, applyinv_ms=inv_ms,
                              apply_ms=fwd_ms,
                              solve_bytes=tree.solve_bytes(), launches=tree.solve_launches(dF.shape[0]),
@@ -682,6 +689,7 @@ def main():
         "config": {"workload": WORKLOAD, "nrhs": nrhs, "path": best, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (factors %.2f GB per solve)" % (r["solve_bytes"] / 1e9)},
         "compress_invert_s": {p: results[p]["compress_invert_s"] for p in results},
+        "compress_invert_first_build_s": {p: results[p]["first_compress_invert_s"] for p in results},
         "stages_s": {p: {k: results[p][k] for k in ("tree_s", "compress_s", "invert_s")} for p in results},
         "solves_per_s": {p: 1e3 / results[p]["solve_ms"] for p in results},
         "mixed_gmres": results.get("mixed", {}).get("gmres"),

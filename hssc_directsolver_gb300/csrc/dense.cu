@@ -998,40 +998,73 @@ __global__ void __launch_bounds__(256) k_gj_gather(const InvP<R>* __restrict__ P
   if (*p.info != 0) return;
   const int jend = min(j0 + GJ_NB, n), nbk = jend - j0;
   __shared__ int pos[2 * GJ_NB], src[2 * GJ_NB];
-  __shared__ int s_cnt, s_np;
-  __shared__ int rsrc[GJ_NB], prow[GJ_NB], psrc[GJ_NB];
-  if (threadIdx.x == 0) {
+  __shared__ int s_np;
+  __shared__ int rsrc[GJ_NB], psrc[GJ_NB];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (w == 0) {
+    // warp 0 composes the block's interchanges: pos lists the rows touched (first-touch
+    // order, at most 2 GJ_NB), src[q] the row whose content ends up in row pos[q]; a
+    // lookup is one ballot over the list
     int cnt = 0;
     auto find = [&](int r) {
-      for (int q = 0; q < cnt; ++q)
-        if (pos[q] == r) return q;
-      pos[cnt] = r;
-      src[cnt] = r;
+      const unsigned m0 = __ballot_sync(0xffffffffu, lane < cnt && pos[lane] == r);
+      const unsigned m1 = __ballot_sync(0xffffffffu, lane + 32 < cnt && pos[lane + 32] == r);
+      if (m0) return __ffs(m0) - 1;
+      if (m1) return 31 + __ffs(m1);
+      if (lane == 0) {
+        pos[cnt] = r;
+        src[cnt] = r;
+      }
+      __syncwarp();
       return cnt++;
     };
     for (int j = j0; j < jend; ++j) {
       const int a = find(j), b = find(p.ipiv[j]);
-      const int t = src[a]; src[a] = src[b]; src[b] = t;
+      if (lane == 0) {
+        const int t = src[a];
+        src[a] = src[b];
+        src[b] = t;
+      }
+      __syncwarp();
     }
+    for (int r = 0; r < nbk; ++r) {
+      const int q = find(j0 + r);  // every row of the block was touched above
+      if (lane == 0) rsrc[r] = src[q];
+    }
+    // the displaced rows outside the block, in list order
     int np = 0;
-    for (int r = 0; r < nbk; ++r) rsrc[r] = src[find(j0 + r)];
-    for (int q = 0; q < cnt; ++q)
-      if ((pos[q] < j0 || pos[q] >= jend) && src[q] != pos[q]) { prow[np] = pos[q]; psrc[np] = src[q]; ++np; }
-    s_cnt = cnt;
-    s_np = np;
-    if (blockIdx.x == 0) {
-      p.aux[0] = np;
-      for (int q = 0; q < np; ++q) p.aux[1 + q] = prow[q];
+    for (int base = 0; base < cnt; base += 32) {
+      const int q = base + lane;
+      const bool take = q < cnt && (pos[q] < j0 || pos[q] >= jend) && src[q] != pos[q];
+      const unsigned mk = __ballot_sync(0xffffffffu, take);
+      if (take) {
+        const int slot = np + __popc(mk & ((1u << lane) - 1u));
+        psrc[slot] = src[q];
+        if (blockIdx.x == 0) p.aux[1 + slot] = pos[q];
+      }
+      np += __popc(mk);
+    }
+    if (lane == 0) {
+      s_np = np;
+      if (blockIdx.x == 0) p.aux[0] = np;
     }
   }
   __syncthreads();
+  // one warp per non-panel column: lane r copies the block's row r (and displaced row r)
   const int np = s_np;
-  const R* A = p.A;
+  const R* __restrict__ A = p.A;
+  R* __restrict__ W = p.W;
   const size_t lda = p.lda;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+  const int ra = (lane < nbk) ? rsrc[lane] : 0, rb = (lane < np) ? psrc[lane] : 0;
+  const int nwarp = gridDim.x * (blockDim.x >> 5);
+  for (int c = blockIdx.x * (blockDim.x >> 5) + w; c < n; c += nwarp) {
     if (c >= j0 && c < jend) continue;
-    for (int r = 0; r < nbk; ++r) p.W[r + (size_t)c * 2 * GJ_NB] = A[rsrc[r] + c * lda];
-    for (int q = 0; q < np; ++q) p.W[GJ_NB + q + (size_t)c * 2 * GJ_NB] = A[psrc[q] + c * lda];
+    const R* col = A + (size_t)c * lda;
+    const R v0 = (lane < nbk) ? col[ra] : R(0);
+    const R v1 = (lane < np) ? col[rb] : R(0);
+    R* wc = W + (size_t)c * 2 * GJ_NB;
+    if (lane < nbk) wc[lane] = v0;
+    if (lane < np) wc[GJ_NB + lane] = v1;
   }
 }
 
@@ -1284,7 +1317,7 @@ void invert_batched(const InvP<R>* dP, int batch, int maxn, cudaStream_t s, bool
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   require_cluster_fits(k_gj_panel_cl<R>, cfg, C);
-  const int gcols = std::max(1, std::min(ceil_div(maxn, 256), 64));
+  const int gcols = std::max(1, std::min(ceil_div(maxn, 64), 128));  // <= 8 columns per warp up to n = 8192
   for (int j0 = 0; j0 < maxn; j0 += GJ_NB) {
     HSS_CUDA(cudaLaunchKernelEx(&cfg, k_gj_panel_cl<R>, dP, j0, rows_per));
     k_gj_gather<R><<<dim3(gcols, batch), 256, 0, s>>>(dP, j0);
@@ -2098,12 +2131,15 @@ __global__ void __launch_bounds__(256) k_trsm_step(const QrP<R>* __restrict__ P,
   }
 }
 
-// k_trsm_step with the update of the rows above in double-float arithmetic (the 32 x 32
-// block solve stays FP64): R(i, b0:b1) and X as float pairs, each product exact by FMA, the
-// 32-term sum in a (hi, lo) accumulator, subtracted from C in FP64.
+// k_trsm_step in double-float arithmetic, for the FP64 problems of the double-float modes.
+// The 32 x 32 block solve runs on float pairs: the diagonal's reciprocals are formed once in
+// FP64 (32 lanes, one division each) and split, and every warp carries its four columns
+// through the 32 back-substitution steps together.  The update of the rows above,
+// C(rows, cols) -= R(rows, b0:b1) X, uses the tiling of the least-squares trailing update
+// (R's rows as broadcast pairs, X as column pairs, paired-FP32 products) and adds the result
+// into C in double-float.  ~2^-48 relative, every sum in a fixed order.
 __global__ void __launch_bounds__(256) k_trsm_step_df(const QrP<double>* __restrict__ P, int blk) {
-  using R = double;
-  const QrP<R> p = P[blockIdx.z];
+  const QrP<double> p = P[blockIdx.z];
   const int kf = p.kf, ncol = p.n - p.kf;
   const int b0 = blk * 32;
   if (b0 >= kf) return;
@@ -2113,54 +2149,91 @@ __global__ void __launch_bounds__(256) k_trsm_step_df(const QrP<double>* __restr
   const int rc0 = blockIdx.y * 256;
   if (blockIdx.y > 0 && rc0 >= b0) return;
   const int nc = min(32, ncol - c0);
-  R* A = p.A;
+  double* A = p.A;
   const size_t lda = p.lda;
-  R* C = A + (size_t)kf * lda;
-  __shared__ R Rs[32][33];
-  __shared__ R Xs[32][33];
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  double* C = A + (size_t)kf * lda;
+  __shared__ float Rh[32][33], Rl[32][33];  // the diagonal block
+  __shared__ float Dh[32], Dl[32];          // 1 / R(r, r)
+  __shared__ DfXTile X;                      // the block's solution, 32 rows x 32 columns
+  __shared__ DfVChunk Vc;                    // 32 rows of R(rows above, b0:b1)
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, lo5 = lane, hi3 = w;
   for (int e = tid; e < 32 * 32; e += 256) {
     const int i = e & 31, j = e >> 5;
-    Rs[i][j] = (i < nb && j < nb) ? A[(b0 + i) + (size_t)(b0 + j) * lda] : R(0);
-    Xs[i][j] = (i < nb && j < nc) ? C[(b0 + i) + (size_t)(c0 + j) * lda] : R(0);
+    float h = 0.f, l = 0.f;
+    if (i < nb && j < nb) split_d2f(A[(b0 + i) + (size_t)(b0 + j) * lda], h, l);
+    Rh[i][j] = h;
+    Rl[i][j] = l;
   }
-  __syncthreads();
+  if (tid < 32) {
+    const double d = (tid < nb) ? A[(b0 + tid) + (size_t)(b0 + tid) * lda] : 1.0;
+    split_d2f(1.0 / d, Dh[tid], Dl[tid]);
+  }
+  // each warp's four columns cc = w + 8 q, row `lane` in registers
+  float xh[4], xl[4];
+#pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int cc = w + 8 * q;
-    R x = Xs[lane][cc];
-    for (int r = nb - 1; r >= 0; --r) {
-      R xr = __shfl_sync(0xffffffffu, x, r);
-      xr = xr / Rs[r][r];
-      if (lane == r) x = xr;
-      if (lane < r) x -= Rs[lane][r] * xr;
-    }
-    Xs[lane][cc] = x;
+    xh[q] = 0.f;
+    xl[q] = 0.f;
+    if (lane < nb && cc < nc) split_d2f(C[(b0 + lane) + (size_t)(c0 + cc) * lda], xh[q], xl[q]);
   }
   __syncthreads();
-  if (blockIdx.y == 0) {
-    for (int e = tid; e < 32 * 32; e += 256) {
-      const int i = e & 31, j = e >> 5;
-      if (i < nb && j < nc) p.X[(b0 + i) + (size_t)(c0 + j) * p.ldx] = Xs[i][j];
+  for (int r = nb - 1; r >= 0; --r) {
+    const float dh = Dh[r], dl = Dl[r];
+    const float nrh = -Rh[lane][r], nrl = -Rl[lane][r];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float yh = __shfl_sync(0xffffffffu, xh[q], r), yl = __shfl_sync(0xffffffffu, xl[q], r);
+      df_mul(yh, yl, dh, dl);
+      if (lane == r) {
+        xh[q] = yh;
+        xl[q] = yl;
+      } else if (lane < r) {
+        df_madd(xh[q], xl[q], nrh, nrl, yh, yl);  // x(lane) -= R(lane, r) x(r)
+      }
     }
   }
-  __shared__ float Xh[32][33], Xl[32][33];
-  for (int e = tid; e < 32 * 32; e += 256) {
-    const int t = e & 31, j = e >> 5;
-    split_d2f(Xs[t][j], Xh[t][j], Xl[t][j]);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int cc = w + 8 * q;
+    dfx_put(X, lane, cc, xh[q], xl[q]);
+    if (blockIdx.y == 0 && lane < nb && cc < nc)
+      p.X[(b0 + lane) + (size_t)(c0 + cc) * p.ldx] = df_to_double(xh[q], xl[q]);
   }
   __syncthreads();
+  // rows above the block: thread owns row lo5 of each 32-row chunk and the columns
+  // {hi3, hi3 + 8} and {hi3 + 16, hi3 + 24} of the tile
   const int rend = min(b0, rc0 + 256);
-  for (int i = rc0 + tid; i < rend; i += 256) {
-    float rh[32], rl[32];
+  for (int r0 = rc0; r0 < rend; r0 += 32) {
+    dfv_stage(Vc, A + (size_t)b0 * lda, (int)lda, 0, r0, rend, nb, tid);
+    __syncthreads();
+    f32x2 ah[2] = {0ULL, 0ULL}, al[2] = {0ULL, 0ULL};
+    for (int jj = 0; jj < nb; ++jj) {
+      const f32x2 b2 = Vc.b[lo5][jj], bn2 = Vc.bn[lo5][jj], bl2 = Vc.bl[lo5][jj];
 #pragma unroll
-    for (int t = 0; t < 32; ++t) split_d2f((t < nb) ? A[i + (size_t)(b0 + t) * lda] : 0.0, rh[t], rl[t]);
-    for (int j = 0; j < nc; ++j) {
-      float sh = 0.f, sl = 0.f;
-#pragma unroll
-      for (int t = 0; t < 32; ++t) df_madd(sh, sl, rh[t], rl[t], Xh[t][j], Xl[t][j]);
-      double* c = C + i + (size_t)(c0 + j) * lda;
-      *c = (*c - (double)sh) - (double)sl;
+      for (int u = 0; u < 2; ++u)
+        df_madd_x2(ah[u], al[u], X.h[jj][hi3 + 8 * u], X.l[jj][hi3 + 8 * u], b2, bn2, bl2);
     }
+    const int gi = r0 + lo5;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const f32x2 h = x2_add(ah[u], al[u]);
+      const f32x2 l = x2_sub(al[u], x2_sub(h, ah[u]));
+      float h2[2], l2[2];
+      x2_unpack(h, h2[0], h2[1]);
+      x2_unpack(l, l2[0], l2[1]);
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int cc = hi3 + 16 * u + 8 * v;
+        if (gi >= rend || cc >= nc) continue;
+        double* c = C + gi + (size_t)(c0 + cc) * lda;
+        float ch, cl;
+        split_d2f(*c, ch, cl);
+        df_add(ch, cl, -h2[v], -l2[v]);
+        *c = df_to_double(ch, cl);
+      }
+    }
+    __syncthreads();
   }
 }
 
