@@ -162,6 +162,7 @@ SIGNATURES = {
     "hss_batched_inverse_device_f32": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P]),
     "hss_batched_inverse_noalloc_device": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P]),
     "hss_batched_lstsq_device": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "hss_batched_lstsq_device_ex": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
     "hss_batched_id_device": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
                                         C.c_int32, _P, _P, _P, _P]),
     "hss_batched_gemm_device": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),

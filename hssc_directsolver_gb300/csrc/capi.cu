@@ -1202,8 +1202,7 @@ int hss_batched_inverse_device_f32(float* d_A, int32_t n, int32_t batch, int32_t
   HSS_CATCH
 }
 
-int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch, void* stream) {
-  HSS_TRY
+static void batched_lstsq(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch, bool df, void* stream) {
   HSS_REQUIRE(d_A && m > 0 && n > kf && kf > 0 && kf <= m && batch > 0, HSS_ERR_ARG, "bad arguments");
   cudaStream_t s = as_stream(stream);
   const int nr = n - kf;
@@ -1215,13 +1214,27 @@ int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int3
                        Tf.p + (size_t)b * QR_NB * QR_NB, diag.p + (size_t)b * kf, X.p + (size_t)b * kf * nr, kf};
   DevBuf<QrP<double>> dP(batch);
   HSS_CUDA(cudaMemcpyAsync(dP.p, P.data(), batch * sizeof(QrP<double>), cudaMemcpyHostToDevice, s));
-  lstsq_batched<double>(dP.p, batch, m, n, kf, s);
+  lstsq_batched<double>(dP.p, batch, m, n, kf, s, df);
   // the solution goes to A(0:kf, kf:n) (leading dimension m)
   for (int b = 0; b < batch; ++b)
     HSS_CUDA(cudaMemcpy2DAsync(d_A + (size_t)b * m * n + (size_t)kf * m, (size_t)m * sizeof(double),
                                X.p + (size_t)b * kf * nr, (size_t)kf * sizeof(double), (size_t)kf * sizeof(double),
                                nr, cudaMemcpyDeviceToDevice, s));
   HSS_CUDA(cudaStreamSynchronize(s));
+}
+
+int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch, void* stream) {
+  HSS_TRY
+  batched_lstsq(d_A, m, n, kf, batch, false, stream);
+  HSS_CATCH
+}
+
+int hss_batched_lstsq_device_ex(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch, int32_t precision,
+                                void* stream) {
+  HSS_TRY
+  HSS_REQUIRE(precision == HSS_PREC_FP64 || precision == HSS_PREC_DFLOAT, HSS_ERR_ARG,
+              "least-squares precision must be HSS_PREC_FP64 or HSS_PREC_DFLOAT");
+  batched_lstsq(d_A, m, n, kf, batch, precision == HSS_PREC_DFLOAT, stream);
   HSS_CATCH
 }
 

@@ -72,11 +72,12 @@ extern "C" {
 
 /* precision modes */
 #define HSS_PREC_FP64 0  /* plain FP64 everywhere */
-#define HSS_PREC_MIXED 1 /* FP32 inverse factors; least-squares updates and the refinement's
-                            forward products in double-float; FP64 refinement residual */
-#define HSS_PREC_DFLOAT 2 /* FP64 inversion; the interpolation least squares' trailing updates and
-                             the solve products in paired FP32 arithmetic (~2^-48); FP64
-                             refinement against the forward operator */
+#define HSS_PREC_MIXED 1 /* FP32 inverse factors; the least squares (panels, updates, back
+                            substitution) and the refinement's forward products in double-float;
+                            FP64 refinement residual */
+#define HSS_PREC_DFLOAT 2 /* FP64 inversion; the interpolation least squares (panels, trailing
+                             updates, back substitution) and the solve products in paired FP32
+                             arithmetic (~2^-48); FP64 refinement against the forward operator */
 #define HSS_PREC_DFLOAT_INV 3 /* HSS_PREC_DFLOAT plus the inversion's and the least squares'
                                  trailing updates and products in paired FP32 (factors ~5 bits
                                  short of FP64; refinement restores the residual) */
@@ -458,6 +459,13 @@ int hss_batched_inverse_noalloc_device(double* d_A, int32_t n, int32_t batch, in
  * back (device); X overwrites A_b(0:kf, kf:n). */
 int hss_batched_lstsq_device(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch,
                              void* stream);
+/* hss_batched_lstsq_device with the arithmetic chosen: HSS_PREC_FP64 (as
+ * hss_batched_lstsq_device) or HSS_PREC_DFLOAT (the Householder panels, the compact-WY
+ * trailing updates and the back substitution in paired FP32, ~2^-48 relative; the least
+ * squares of the interpolation operators, T = K(Xp,X_sk) \ K(Xp,X_rs), in the tree's
+ * double-float and mixed modes).  Any other precision: HSS_ERR_ARG. */
+int hss_batched_lstsq_device_ex(double* d_A, int32_t m, int32_t n, int32_t kf, int32_t batch,
+                                int32_t precision, void* stream);
 /* Interpolative decomposition of `batch` m x n blocks (device, back to back):
  * rank[b], perm[b*n..], T[b*n*n..] (k x (n-k), ld n).  force_k < 0: adaptive
  * (ID.m:40-65), else fixed rank (ID.m:106-113). */

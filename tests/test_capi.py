@@ -55,6 +55,10 @@ def test_status_paths_without_gpu(lib):
     assert lib.hss1d_sum(None, None, 1e-10, None) == _lib.HSS_ERR_ARG
     assert lib.hss1d_compress_rect(None, None, 0, 0, None, 0, 0, 64, 1e-10, None, 0) == _lib.HSS_ERR_ARG
     assert lib.hss1d_rect_info(None, None, None, None, None, None) == _lib.HSS_ERR_ARG
+    # the least squares' precision is checked first: only FP64 and DFLOAT are accepted
+    assert lib.hss_batched_lstsq_device_ex(None, 8, 4, 2, 1, _lib.HSS_PREC_MIXED, None) == _lib.HSS_ERR_ARG
+    assert b"HSS_PREC_DFLOAT" in lib.hss_last_error()
+    assert lib.hss_batched_lstsq_device_ex(None, 8, 4, 2, 1, _lib.HSS_PREC_DFLOAT, None) == _lib.HSS_ERR_ARG
     if n.value == 0:
         h = C.c_void_p()
         p = _lib.hss2d_params(8, 4, 2, 0, 0, 0, 0, 0, 1e-10, _lib.hss_kernel_params())

@@ -98,6 +98,45 @@ def test_lstsq(env, m, n, kf):
         assert np.abs(X - out[b].T[:kf, kf:]).max() <= 1e-11 * np.abs(X).max()
 
 
+@pytest.mark.parametrize("m,n,kf", [(40, 30, 20), (132, 64, 48), (300, 200, 150), (700, 240, 200),
+                                    (2340, 2016, 1520)])
+def test_lstsq_dfloat(env, m, n, kf):
+    """The double-float least squares (hss_batched_lstsq_device_ex, HSS_PREC_DFLOAT): panels,
+    trailing updates and back substitution in paired FP32.  Shapes cover one CTA per
+    problem, the cluster panel (m > 256 with few problems), the row-split update (tall
+    problems) and a last panel narrower than 32 columns.  The solution matches NumPy's to
+    the double-float precision times the system's condition and the FP64 path's closely."""
+    torch, L, lib = env
+    r = np.random.default_rng(m + 1)
+    A = r.standard_normal((3, n, m))
+    A[2, :kf] *= np.logspace(0, -6, kf)[:, None]      # a graded (cond ~1e6) system
+    out = {}
+    for prec in (L.HSS_PREC_FP64, L.HSS_PREC_DFLOAT):
+        dA = _dev(torch, A)
+        L.check(lib.hss_batched_lstsq_device_ex(L.ptr(dA), m, n, kf, 3, prec, None))
+        torch.cuda.synchronize()
+        out[prec] = dA.cpu().numpy()
+    worst = []
+    for b in range(3):
+        Am = A[b].T
+        X = np.linalg.lstsq(Am[:, :kf], Am[:, kf:], rcond=None)[0]
+        cond = np.linalg.cond(Am[:, :kf])
+        X64 = out[L.HSS_PREC_FP64][b].T[:kf, kf:]
+        Xdf = out[L.HSS_PREC_DFLOAT][b].T[:kf, kf:]
+        e_np = np.abs(Xdf - X).max() / np.abs(X).max()
+        e_64 = np.abs(Xdf - X64).max() / np.abs(X64).max()
+        worst.append((e_np, e_64, cond))
+        # ~2^-48 per operation, amplified by the condition of the skeleton columns
+        assert e_np <= 2e-13 * max(1.0, cond) and e_64 <= 2e-13 * max(1.0, cond), (b, e_np, e_64, cond)
+        # what the solution does: the residual of the normal equations is as small as FP64's
+        res_df = np.linalg.norm(Am[:, :kf].T @ (Am[:, :kf] @ Xdf - Am[:, kf:]))
+        res_64 = np.linalg.norm(Am[:, :kf].T @ (Am[:, :kf] @ X64 - Am[:, kf:]))
+        scale = np.linalg.norm(Am[:, :kf]) ** 2 * np.linalg.norm(X) + 1e-300
+        assert res_df / scale <= 1e-12 and res_64 / scale <= 1e-13
+    print(f"double-float least squares {m}x{n} (kf={kf}): vs NumPy / FP64 path " +
+          ", ".join(f"{a:.1e}/{b_:.1e} (cond {c:.0e})" for a, b_, c in worst))
+
+
 def _id_gpu(env, A, acc, force=-1):
     torch, L, lib = env
     m, n = A.shape
