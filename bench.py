@@ -704,8 +704,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_PER_APPLYINV.get(best),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the inverse apply's "
-                                       "kernels at this workload (profiles/skinny_hss2d_n65536.md), "
-                                       "not measured in this run",
+                                       "kernels, summed over one capture of this workload's solve; not measured "
+                                       "in this run",
                      "kernel": {"dfloat": "k_skinny_df", "dfloat_inv": "k_skinny_df", "tc": "k_skinny_tc",
                                 "mixed": "k_skinny<float>"}.get(best, "k_skinny<double>")
                                + " chain of one inverse apply",
